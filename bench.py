@@ -1,0 +1,402 @@
+"""Benchmark of the GB300 stencil library: T_eff of the 3-D diffusion step (ParallelStencil's
+README metric, A_eff = (2*D_u + D_k) bytes per step / time per step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (headline): the 3-D diffusion step in flux form with a spatially varying conductivity
+array (T, T2, Ci, lam; FP64; 512^3), memopt z-sweep kernel -- D_u = T, D_k = {lam, Ci}, so
+A_eff = 4 words/cell = 4.295 GB per step. Inputs: T ~ U(0,1) (seed 2), lam = 1 + 0.5 U(0,1)
+(seed 3), Ci = 1, dt = min(dx,dy,dz)^2 / max(lam) / 8.1. All arrays (4.3 GB) are far larger
+than L2 (129 MB), so no L2 flush is needed between steps. Also reported: memcopy3D, the README
+(T, T2, Ci) form, plain vs memopt, FP32, and 256^3.
+
+Rank 0 prints ONE JSON line. `--impl reference` times the CPU oracle (a C/OpenMP restatement
+of the reference's Threads-backend kernel) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "parallelstencil.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORDS_FLUX_LAM = 4  # T read, T2 write, lam read, Ci read
+WORDS_README = 3  # T read, T2 write, Ci read
+WORDS_MEMCOPY = 3
+NT_JOB = 50  # time steps of one diffusion job (the e2e unit)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(name):
+    """dram bytes per launch recorded in profiles/<name>.md ('traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while the timed work runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [r for r in rows if r[2] > 300.0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in load for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "samples_under_load": len(load),
+                "power_w_max": max(r[2] for r in rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def time_steps(torch, step_fn, steps, warmup, barrier, stream):
+    for i in range(warmup):
+        step_fn(i)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        step_fn(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3  # seconds for `steps` steps
+
+
+def run_ours(a, world, rank, local):
+    import torch
+
+    import ps_gb300 as ps
+    from ps_gb300 import _lib
+    from ps_gb300.core import descriptor, stream_handle
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ps.init_parallel_stencil(ps.GB300, "Float64", 3, device=local)
+    stream = torch.cuda.current_stream()
+    n = a.n
+    lx = 10.0
+    dx = lx / (n - 1)
+    _dx = 1.0 / dx
+    dt = dx * dx / 1.5 / 8.1
+
+    def fields(dtype, nn):
+        g = torch.Generator(device="cuda")
+        tdt = torch.float64 if dtype == np.float64 else torch.float32
+        T = ps.empty(nn, nn, nn, dtype=dtype)
+        g.manual_seed(2)
+        T.copy_(torch.rand((nn, nn, nn), generator=g, device="cuda", dtype=torch.float64).to(tdt))
+        T2 = ps.empty(nn, nn, nn, dtype=dtype)
+        T2.copy_(T)
+        lam = ps.empty(nn, nn, nn, dtype=dtype)
+        g.manual_seed(3)
+        lam.copy_((1 + 0.5 * torch.rand((nn, nn, nn), generator=g, device="cuda", dtype=torch.float64)).to(tdt))
+        Ci = ps.ones(nn, nn, nn, dtype=dtype)
+        torch.cuda.synchronize()
+        return T, T2, lam, Ci
+
+    results = {}
+    launches = 0
+
+    def bench_kernel(label, kernel, arrs, scalars, memopt, words, nn, dtype, nsteps):
+        nonlocal launches
+        T, T2, lam, Ci = arrs
+        bufs = [T, T2]
+
+        def step(i):
+            src, dst = bufs[i % 2], bufs[(i + 1) % 2]
+            if kernel is ps.kernels.copy3D:
+                ps.parallel(kernel, dst, src, Ci, memopt=memopt, sync=False)
+            elif kernel is ps.kernels.diffusion3D_step_flux_lam:
+                ps.parallel(kernel, dst, src, Ci, lam, *scalars, memopt=memopt, sync=False)
+            else:
+                ps.parallel(kernel, dst, src, Ci, 1.0, *scalars, memopt=memopt, sync=False)
+
+        secs = time_steps(torch, step, nsteps, a.warmup, barrier, stream)
+        secs = max_over_ranks(secs)
+        launches += nsteps
+        bytes_step = words * nn ** 3 * np.dtype(dtype).itemsize
+        t_step = secs / nsteps
+        results[label] = {"t_step_ms": t_step * 1e3, "T_eff_GBs": bytes_step / t_step / 1e9,
+                          "A_eff_GB": bytes_step / 1e9}
+        return t_step, bytes_step
+
+    peak, peak_kind = measured_peaks()
+    with ClockSampler(local) as clk:
+        arrs64 = fields(np.float64, n)
+        t_head, b_head = bench_kernel("diffusion3d_flux_lam_f64_memopt", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                                      (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float64, a.steps)
+        if not a.quick:
+            bench_kernel("diffusion3d_flux_lam_f64_plain", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                         (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, a.steps)
+            bench_kernel("diffusion3d_readme_f64_memopt", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx), True,
+                         WORDS_README, n, np.float64, a.steps)
+            bench_kernel("diffusion3d_readme_f64_plain", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx), False,
+                         WORDS_README, n, np.float64, a.steps)
+            bench_kernel("memcopy3d_f64", ps.kernels.copy3D, arrs64, (), False, WORDS_MEMCOPY, n, np.float64, a.steps)
+        # e2e: one diffusion job (NT_JOB steps) through the C ABI from pinned host buffers:
+        # H2D of T, Ci, lam; NT_JOB steps; D2H of T -- all inside the timed region.
+        lib = _lib.load()
+        T, T2, lam, Ci = arrs64
+        hostbufs = [torch.empty((n, n, n), dtype=torch.float64, pin_memory=True) for _ in range(4)]
+        hT, hCi, hlam, hout = hostbufs
+        hT.copy_(T.cpu().permute(2, 1, 0))  # column-major device layout == C order of (nz, ny, nx)
+        hCi.fill_(1.0)
+        hlam.copy_(lam.cpu().permute(2, 1, 0))
+        s = stream_handle(stream)
+        dT, dT2, dCi, dlam = descriptor(T), descriptor(T2), descriptor(Ci), descriptor(lam)
+        cfg = _lib.PSLaunch()
+        cfg.memopt = 1
+
+        def e2e_job():
+            _lib.check(lib.ps_copy_h2d(dT, ctypes.c_void_p(hT.data_ptr()), s))
+            _lib.check(lib.ps_copy_h2d(dT2, ctypes.c_void_p(hT.data_ptr()), s))
+            _lib.check(lib.ps_copy_h2d(dCi, ctypes.c_void_p(hCi.data_ptr()), s))
+            _lib.check(lib.ps_copy_h2d(dlam, ctypes.c_void_p(hlam.data_ptr()), s))
+            a_, b_ = dT, dT2
+            for _ in range(NT_JOB):
+                _lib.check(lib.ps_diffusion3d_step(3, b_, a_, dCi, dlam, 0.0, dt, _dx, _dx, _dx, ctypes.byref(cfg), s,
+                                                   0))
+                a_, b_ = b_, a_
+            _lib.check(lib.ps_copy_d2h(ctypes.c_void_p(hout.data_ptr()), a_, s))
+
+        e2e_job()
+        barrier()
+        torch.cuda.synchronize()
+        jobs = max(1, a.e2e_jobs)
+        t0 = time.perf_counter()
+        for _ in range(jobs):
+            e2e_job()
+        torch.cuda.synchronize()
+        t_e2e = max_over_ranks((time.perf_counter() - t0) / jobs)
+        launches += jobs * NT_JOB
+        del hostbufs, hT, hCi, hlam, hout
+        if not a.quick:
+            del arrs64, T, T2, lam, Ci
+            torch.cuda.empty_cache()
+            arrs32 = fields(np.float32, n)
+            bench_kernel("diffusion3d_flux_lam_f32_memopt", ps.kernels.diffusion3D_step_flux_lam, arrs32,
+                         (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float32, a.steps)
+            bench_kernel("diffusion3d_flux_lam_f32_plain", ps.kernels.diffusion3D_step_flux_lam, arrs32,
+                         (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float32, a.steps)
+            bench_kernel("memcopy3d_f32", ps.kernels.copy3D, arrs32, (), False, WORDS_MEMCOPY, n, np.float32, a.steps)
+            del arrs32
+            torch.cuda.empty_cache()
+            n2 = 256
+            arrs256 = fields(np.float64, n2)
+            bench_kernel("diffusion3d_flux_lam_f64_memopt_256", ps.kernels.diffusion3D_step_flux_lam, arrs256,
+                         (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n2, np.float64, a.steps)
+            bench_kernel("memcopy3d_f64_256", ps.kernels.copy3D, arrs256, (), False, WORDS_MEMCOPY, n2, np.float64,
+                         a.steps)
+            del arrs256
+    clocks = clk.summary()
+
+    value = world * b_head / t_head / 1e9
+    e2e_bytes = NT_JOB * b_head
+    out = {
+        "metric": "T_eff", "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(t_head * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U(0,1) T, 1+0.5U(0,1) lam, Ci=1)",
+        "config": {"workload": f"diffusion3D flux form with lam array, memopt z-sweep, {n}^3 FP64",
+                   "global_batch": world * n ** 3, "cells_per_gpu": n ** 3, "parallelism": f"replicas{world}",
+                   "l2": "inputs 4.3 GB >> 129 MB L2 (no flush needed)"},
+        "pct_of_hbm_peak": round(100 * (value / world) / peak, 2),
+        "roofline": {"bound": "hbm", "achieved": round(b_head / t_head / 1e9, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round((b_head / t_head / 1e9) / peak, 4), "peak_kind": f"{peak_kind} hbm_gbs (burst)",
+                     "traffic": ncu_traffic("diffusion3d_flux_lam_f64_512"),
+                     "kernel": "diff3d_zsweep_tma<double,FLUX_LAM>", "algorithmic_bytes_per_launch": b_head},
+        "e2e": {"value": round(world * e2e_bytes / t_e2e / 1e9, 2), "unit": "GB/s",
+                "h2d_bytes_per_step": 4 * n ** 3 * 8, "d2h_bytes_per_step": n ** 3 * 8,
+                "step": f"one {NT_JOB}-step diffusion job from pinned host buffers through the C ABI",
+                "seconds_per_job": round(t_e2e, 5)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "variants": results,
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(a, n)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _oracle_slab_steps(n, slab, steps, warmup):
+    """Time the oracle's flux-lam diffusion step over a z-slab of an n^3 FP64 job."""
+    import oracle
+
+    oracle.build()
+    rng2, rng3 = np.random.default_rng(2), np.random.default_rng(3)
+    nz = slab + 2
+    shape = (n, n, nz)
+    T = np.asfortranarray(rng2.random(shape))
+    lam = np.asfortranarray(1 + 0.5 * rng3.random(shape))
+    Ci = np.asfortranarray(np.ones(shape))
+    T2 = T.copy(order="F")
+    dx = 10.0 / (n - 1)
+    _dx = 1 / dx
+    dt = dx * dx / 1.5 / 8.1
+    for _ in range(warmup):
+        oracle.diffusion3d_step(3, T2, T, Ci, lam, 0.0, dt, _dx, _dx, _dx)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.diffusion3d_step(3, T2, T, Ci, lam, 0.0, dt, _dx, _dx, _dx)
+        T, T2 = T2, T
+    secs = (time.perf_counter() - t0) / steps
+    cells = n * n * slab  # updated planes (the slab's interior in z)
+    return WORDS_FLUX_LAM * cells * 8 / secs / 1e9, secs
+
+
+def cpu_baseline(a, n):
+    import oracle
+
+    oracle.build()
+    slab = 128
+    teff, secs = _oracle_slab_steps(n, slab, a.cpu_steps, 1)
+    return {"value": round(teff, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{a.cpu_steps} steps of the oracle (C/OpenMP, -O3) over a {n}x{n}x{slab} z-slab of the "
+                      f"{n}^3 FP64 flux-lam job ({secs * 1e3:.1f} ms/step)"}
+
+
+def run_reference(a, world, rank):
+    """CPU oracle of the reference's Threads-backend kernel, timed on the host cores."""
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    slab = a.ref_slab
+    teff, secs = _oracle_slab_steps(a.n, slab, a.steps, a.warmup)
+    out = {
+        "metric": "T_eff", "value": round(teff, 3), "unit": "GB/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(secs * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U(0,1) T, 1+0.5U(0,1) lam, Ci=1)",
+        "impl": "reference",
+        "config": {"workload": f"diffusion3D flux form with lam array, {a.n}^3 FP64 (CPU, z-slab sample)",
+                   "global_batch": a.n ** 3, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(teff, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"each step: one diffusion step over a {a.n}x{a.n}x{slab} z-slab of the "
+                                   f"{a.n}^3 job (C/OpenMP restatement of the reference kernel)"},
+        "e2e": {"value": round(teff, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--quick", action="store_true", help="headline + e2e only")
+    ap.add_argument("--e2e-jobs", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--ref-slab", type=int, default=32)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    if a.warmup < 3:
+        a.warmup = 3
+    world, rank, local = dist_setup()
+    if a.impl == "reference":
+        run_reference(a, world, rank)
+        return
+    run_ours(a, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,202 @@
+/*
+ * ps_gb300.h -- C ABI of libps_b200.so, the GB300 (sm_103a) stencil library.
+ *
+ * The library replaces the kernel-launch layer that ParallelStencil.jl uses for its
+ * `@parallel` / `@parallel_indices` finite-difference kernels on CUDA:
+ *   - `@parallel k!(args...)` lowers to `CUDA.@cuda blocks threads stream k!(args..., ranges,
+ *     rlx, rly, rlz)` followed by `CUDA.synchronize(stream)`
+ *     (src/ParallelKernel/parallel.jl:303-334, 883-918, 375);
+ *   - `@parallel_async` omits the synchronisation (src/ParallelKernel/parallel.jl:884).
+ * Every entry point below takes the same arrays and scalars as the reference kernel it
+ * replaces, plus a stream and a `sync` flag (1 = `@parallel`, 0 = `@parallel_async`).
+ *
+ * Conventions
+ *   - Arrays are dense, column-major (x fastest), caller-owned device memory: element
+ *     (ix,iy,iz) (0-based) lives at ptr[ix + n[0]*(iy + n[1]*iz)]. 2-D arrays use n[2] = 1,
+ *     1-D arrays n[1] = n[2] = 1. This is `Data.Array` of the reference
+ *     (src/ParallelKernel/Data.jl:271) with `padding=false`.
+ *   - Every call returns a ps_status; nothing aborts, traps or throws across the ABI.
+ *     ps_last_error() gives a thread-local message for the last failing call.
+ *   - FP arithmetic is IEEE without FMA contraction, in the operation order of the
+ *     reference's macros, so FP64 results are bit-identical to the reference's CPU path.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).
+ */
+#ifndef PS_GB300_H
+#define PS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PS_ABI_VERSION 1
+
+/* Status codes. The reference raises typed Julia exceptions for the same conditions
+ * (src/ParallelKernel/Exceptions.jl:5-15); here they are return codes. */
+typedef enum {
+    PS_OK                = 0,
+    PS_ERR_ARG           = -1,  /* invalid scalar argument / enum value          (ArgumentError) */
+    PS_ERR_NULL          = -2,  /* NULL pointer where an array is required                        */
+    PS_ERR_SHAPE         = -3,  /* incoherent array sizes                     (IncoherentArgumentError) */
+    PS_ERR_DTYPE         = -4,  /* unsupported or mixed element types                              */
+    PS_ERR_ALIGN         = -5,  /* misaligned device pointer                                       */
+    PS_ERR_CUDA          = -6,  /* a CUDA runtime call failed (message in ps_last_error)           */
+    PS_ERR_NOT_CONVERGED = -7,  /* iteration cap reached before the tolerance                      */
+    PS_ERR_TIMEOUT       = -8,  /* a bounded device-side wait gave up                              */
+    PS_ERR_NOT_INIT      = -9,  /* ps_init not called                        (NotInitializedError) */
+    PS_ERR_NOMEM         = -10, /* device allocation failed                                        */
+    PS_ERR_NONFINITE     = -11, /* NaN/Inf detected in a residual                                  */
+    PS_ERR_UNSUPPORTED   = -12  /* valid request that this build does not implement               */
+} ps_status;
+
+/* Element types (the reference's `numbertype`, src/ParallelKernel/shared.jl:59). */
+typedef enum { PS_F64 = 0, PS_F32 = 1, PS_BF16 = 2 } ps_dtype;
+
+/* Array descriptor: a device pointer plus its extents (`size(A)`) and element type. */
+typedef struct ps_array {
+    void*   ptr;
+    int64_t n[3];
+    int32_t dtype;
+    int32_t reserved;
+} ps_array;
+
+/* Launch configuration of one kernel call (the `@parallel` keyword arguments). */
+typedef struct ps_launch {
+    int32_t memopt;       /* 0: one thread per cell (`memopt=false`);
+                             1: z-sweep with TMA-staged planes (`memopt=true`, loopdim z) */
+    int32_t loopsize;     /* z-planes swept by one CTA (`loopsize`); 0 = library default   */
+    int64_t range_lo[3];  /* `ranges` of the call as 0-based half-open thread-index boxes  */
+    int64_t range_hi[3];  /* (hi <= lo in every dimension, or a NULL ps_launch = full grid) */
+} ps_launch;
+
+/* ------------------------------------------------------------------------------------ */
+/* Core: device, memory, streams.                                                        */
+/* ------------------------------------------------------------------------------------ */
+
+/* Select and initialise a device (the `@init_parallel_stencil(GB300, ...)` hook,
+ * src/init_parallel_stencil.jl:36-51). Idempotent per device. */
+int ps_init(int device);
+/* Release library-owned resources (streams, scratch, cached descriptors). */
+int ps_finalize(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* ps_last_error(void);
+int ps_abi_version(void);
+/* Number of CUDA devices visible (0 without a driver). Needs no ps_init. */
+int ps_device_count(int* count);
+
+/* `@zeros(nx,ny,nz)` allocation (src/ParallelKernel/allocators.jl:279-293,
+ * CUDAExt/allocators.jl:3): zero-filled device array owned by the caller. */
+int ps_alloc(ps_array* a, int32_t dtype, int64_t nx, int64_t ny, int64_t nz);
+int ps_free(ps_array* a);
+/* `@fill!(A, v)` / `A .= v` on the device (src/ParallelKernel/allocators.jl:327-375). */
+int ps_fill(ps_array a, double value, void* stream);
+/* Host <-> device copies of a whole array (`Data.Array(host)` / `Array(A)`). */
+int ps_copy_h2d(ps_array dst, const void* host_src, void* stream);
+int ps_copy_d2h(void* host_dst, ps_array src, void* stream);
+
+/* Streams of the `@hide_communication` split (CUDAExt/shared.jl:17-31): priority 1 =
+ * high-priority non-blocking stream (boundary slabs), 0 = normal non-blocking stream. */
+int ps_stream_create(int priority, void** stream);
+int ps_stream_destroy(void* stream);
+/* `@synchronize(stream)` (src/ParallelKernel/parallel.jl:175-184). */
+int ps_synchronize(void* stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Finite-difference operators (src/FiniteDifferences.jl).                               */
+/* ------------------------------------------------------------------------------------ */
+
+/* Operator kinds of the FiniteDifferences{1,2,3}D macros. */
+typedef enum {
+    PS_FD_SEL    = 0, /* @all, @inn, @inn_x ... @inn_yz                                  */
+    PS_FD_DIFF   = 1, /* @d_xa/@d_ya/@d_za, @d_xi/@d_yi/@d_zi (1-D: @d)                  */
+    PS_FD_DIFF2  = 2, /* @d2_xa/@d2_ya (2-D), @d2_xi/@d2_yi/@d2_zi (1-D: @d2)            */
+    PS_FD_AV     = 3, /* @av, @av_xa ... @av_yzi                                         */
+    PS_FD_HARM   = 4, /* @harm, @harm_xa ... @harm_yzi                                   */
+    PS_FD_MAXLOC = 5, /* @maxloc                                                         */
+    PS_FD_MINLOC = 6  /* @minloc                                                         */
+} ps_fd_kind;
+
+/* One FD macro as a descriptor. Bit d of a mask refers to dimension d (x=1, y=2, z=4).
+ *   opdims: dimensions the operator differences / averages over
+ *   inn:    dimensions whose base index is the inner index (ixi = ix+1)
+ * Examples (3-D): @d_xi = {DIFF, x, y|z}; @d2_yi = {DIFF2, y, x|y|z}; @av_xyi = {AV, x|y, z};
+ * @inn_xz = {SEL, 0, x|z}; @maxloc = {MAXLOC, x|y|z, x|y|z}. */
+typedef struct ps_fd_op {
+    int32_t kind;
+    int32_t opdims;
+    int32_t inn;
+    int32_t ndims;   /* 1, 2 or 3: the FiniteDifferences module the macro comes from */
+} ps_fd_op;
+
+/* `@<lhs>(R) = @<op>(A)` as a one-statement `@parallel` kernel: thread grid = max extents of
+ * R and A (src/ParallelKernel/parallel.jl:795-798), statement masked by `@within` of the
+ * left-hand selection (src/FiniteDifferences.jl:397-408; src/parallel.jl:654-680).
+ * lhs_inn is the inn-mask of the left-hand macro (@all = 0, @inn = all dims, @inn_x = x ...).
+ * Returns PS_ERR_SHAPE if a thread passing the mask would read outside A. */
+int ps_fd_apply(ps_fd_op op, int32_t lhs_inn, ps_array R, ps_array A, void* stream, int sync);
+
+/* ------------------------------------------------------------------------------------ */
+/* 3-D kernels of the examples (examples/memcopy3D.jl, examples/diffusion3D_*.jl).       */
+/* ------------------------------------------------------------------------------------ */
+
+/* `@all(T2) = @all(T) + @all(Ci)` (examples/memcopy3D.jl:10-13;
+ * `@parallel_indices` form examples/memcopy3D_parindices.jl:9-12). */
+int ps_memcopy3d(ps_array T2, ps_array T, ps_array Ci, const ps_launch* cfg, void* stream, int sync);
+
+/* Statement forms of the 3-D diffusion step. */
+typedef enum {
+    /* @inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)/dx^2 + @d2_yi(T)/dy^2 + @d2_zi(T)/dz^2))
+     * examples/diffusion3D_novis_noperf.jl:10-13; h = (dx, dy, dz) */
+    PS_DIFF_DIV      = 0,
+    /* @inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)*_dx^2 + @d2_yi(T)*_dy^2 + @d2_zi(T)*_dz^2))
+     * examples/diffusion3D_multigpucpu_hidecomm_novis.jl:12-15; h = (_dx, _dy, _dz) */
+    PS_DIFF_MUL      = 1,
+    /* on-the-fly flux form with scalar lam (test/test_parallel.jl:420-426):
+     *   @all(qx) = -lam*@d_xi(T)*_dx ... ;
+     *   @all(dTdt) = @inn(Ci)*(-@d_xa(qx)*_dx - @d_ya(qy)*_dy - @d_za(qz)*_dz);
+     *   @inn(T2) = @inn(T) + dt*@all(dTdt)                        h = (_dx, _dy, _dz) */
+    PS_DIFF_FLUX     = 2,
+    /* the same flux form with a conductivity array and face values @av_xi(lam) etc.:
+     *   @all(qx) = -@av_xi(lam)*@d_xi(T)*_dx ...                  h = (_dx, _dy, _dz) */
+    PS_DIFF_FLUX_LAM = 3
+} ps_diffusion_form;
+
+/* One diffusion step `@parallel diffusion3D_step!(T2, T, Ci, lam, dt, h...)`. All arrays
+ * n^3 of one dtype; lam_arr is used (and must be non-NULL) only for PS_DIFF_FLUX_LAM.
+ * Scalars are cast to the array dtype first, as the reference's literal typing does
+ * (src/ParallelKernel/parallel.jl:400-418). Boundary cells of T2 are not written. */
+int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr,
+                        double lam, double dt, double hx, double hy, double hz,
+                        const ps_launch* cfg, void* stream, int sync);
+
+/* Host callback run by the split launcher once the boundary slabs are complete: the
+ * communication / boundary-condition slot of `@hide_communication`. */
+typedef int (*ps_comm_fn)(void* ctx);
+
+/* `@hide_communication bw begin @parallel diffusion3D_step!(...); comm(ctx) end`
+ * (src/ParallelKernel/hide_communication.jl:177-258, ranges :350-394): the six boundary
+ * slabs of width bw run on s_boundary, the inner box on s_inner; comm (may be NULL) runs
+ * after the boundary slabs finish and before the inner box is waited for. On return both
+ * streams are synchronised. Result identical to ps_diffusion3d_step. */
+int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr,
+                              double lam, double dt, double hx, double hy, double hz,
+                              int32_t memopt, const int64_t bw[3], void* s_boundary, void* s_inner,
+                              ps_comm_fn comm, void* comm_ctx);
+
+/* ------------------------------------------------------------------------------------ */
+/* acoustic3D (miniapps/acoustic3D.jl:11-21).                                            */
+/* ------------------------------------------------------------------------------------ */
+
+/* `@inn(Vx) = @inn(Vx) - dt/ρ*@d_xi(P)/dx` etc. Vx (n+1,n,n), Vy (n,n+1,n), Vz (n,n,n+1). */
+int ps_acoustic3d_v(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
+                    double dt, double rho, double dx, double dy, double dz, void* stream, int sync);
+/* `@all(P) = @all(P) - dt*k*(@d_xa(Vx)/dx + @d_ya(Vy)/dy + @d_za(Vz)/dz)`. */
+int ps_acoustic3d_p(ps_array P, ps_array Vx, ps_array Vy, ps_array Vz,
+                    double dt, double k, double dx, double dy, double dz, void* stream, int sync);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PS_GB300_H */

@@ -1,0 +1,123 @@
+"""CPU oracle of the GB300 stencil library -- TEST INFRASTRUCTURE ONLY.
+
+A ctypes wrapper around ``oracle/ps_oracle.c`` (a plain-C + OpenMP restatement of
+ParallelStencil.jl's FiniteDifferences macros and the example / miniapp kernels built
+from them). Only the tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+leg use it, and only as the checker / the timed CPU reference; the product path
+(``ps_gb300``) never imports it.
+
+Arrays are numpy arrays in Julia layout: shape ``(nx, ny, nz)`` (or ``(nx, ny)``,
+``(nx,)``), Fortran order, so ``A[ix, iy, iz]`` (0-based) is the reference's
+``A[ix+1, iy+1, iz+1]``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "libps_oracle.so")
+_SOURCES = [os.path.join(_HERE, "ps_oracle.c"), os.path.join(_HERE, "ps_oracle_body.h")]
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (-O3 -fopenmp -ffp-contract=off) into oracle/_build."""
+    os.makedirs(_BUILD, exist_ok=True)
+    newest_src = max(os.path.getmtime(s) for s in _SOURCES)
+    if not force and os.path.exists(_LIB_PATH) and os.path.getmtime(_LIB_PATH) >= newest_src:
+        return _LIB_PATH
+    tmp = _LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-o", tmp, os.path.join(_HERE, "ps_oracle.c"), "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+    return _lib
+
+
+_SUFFIX = {np.dtype(np.float64): "_f64", np.dtype(np.float32): "_f32"}
+
+
+def _real(dtype):
+    return ctypes.c_double if np.dtype(dtype) == np.float64 else ctypes.c_float
+
+
+def _n3(a: np.ndarray):
+    s = list(a.shape) + [1] * (3 - a.ndim)
+    return (ctypes.c_int64 * 3)(*s)
+
+
+def _ptr(a: np.ndarray):
+    if not a.flags.f_contiguous:
+        raise ValueError("oracle arrays must be Fortran-contiguous (Julia layout)")
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _fn(name: str, dtype):
+    return getattr(lib(), name + _SUFFIX[np.dtype(dtype)])
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise ValueError(f"oracle {what} failed with status {rc}")
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+def set_num_threads(n: int) -> None:
+    lib().orc_set_num_threads(int(n))
+
+
+def fd_apply(kind: int, opdims: int, inn: int, ndims: int, lhs_inn: int, R: np.ndarray, A: np.ndarray) -> None:
+    """``@<lhs>(R) = @<op>(A)`` in place on R."""
+    f = _fn("orc_fd_apply", R.dtype)
+    _check(f(kind, opdims, inn, ndims, lhs_inn, _ptr(R), _n3(R), _ptr(A), _n3(A)), "fd_apply")
+
+
+def _box(n, lo, hi):
+    lo = [0, 0, 0] if lo is None else list(lo)
+    hi = list(n) if hi is None else list(hi)
+    return (ctypes.c_int64 * 3)(*lo), (ctypes.c_int64 * 3)(*hi)
+
+
+def memcopy3d(T2, T, Ci, lo=None, hi=None) -> None:
+    n = _n3(T)
+    l, h = _box(list(n), lo, hi)
+    _check(_fn("orc_memcopy3d", T.dtype)(_ptr(T2), _ptr(T), _ptr(Ci), n, l, h), "memcopy3d")
+
+
+def diffusion3d_step(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, lo=None, hi=None) -> None:
+    """One diffusion step; (lo, hi) is the `@parallel` thread box (default: full grid)."""
+    R = _real(T.dtype)
+    n = _n3(T)
+    l, h = _box(list(n), lo, hi)
+    lam_p = _ptr(lam_arr) if lam_arr is not None else None
+    _check(_fn("orc_diffusion3d_step", T.dtype)(int(form), _ptr(T2), _ptr(T), _ptr(Ci), lam_p, R(lam), R(dt),
+                                                R(hx), R(hy), R(hz), n, l, h), "diffusion3d_step")
+
+
+def acoustic3d_v(Vx, Vy, Vz, P, dt, rho, dx, dy, dz) -> None:
+    R = _real(P.dtype)
+    _check(_fn("orc_acoustic3d_v", P.dtype)(_ptr(Vx), _ptr(Vy), _ptr(Vz), _ptr(P), _n3(P), R(dt), R(rho), R(dx),
+                                            R(dy), R(dz)), "acoustic3d_v")
+
+
+def acoustic3d_p(P, Vx, Vy, Vz, dt, k, dx, dy, dz) -> None:
+    R = _real(P.dtype)
+    _check(_fn("orc_acoustic3d_p", P.dtype)(_ptr(P), _ptr(Vx), _ptr(Vy), _ptr(Vz), _n3(P), R(dt), R(k), R(dx),
+                                            R(dy), R(dz)), "acoustic3d_p")

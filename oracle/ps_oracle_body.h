@@ -1,0 +1,228 @@
+/*
+ * ps_oracle_body.h -- type-generic body of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+ * Included twice by ps_oracle.c with REAL = double / float and SFX(name) = name_f64 / name_f32.
+ */
+
+#define OIDX(a, b, c, n) ((int64_t)(a) + (n)[0] * ((int64_t)(b) + (n)[1] * (int64_t)(c)))
+
+/* Julia's Base.max / Base.min for IEEE floats (NaN-propagating, -0.0 < 0.0). */
+static inline REAL SFX(jl_max)(REAL x, REAL y) {
+    REAL diff = x - y;
+    REAL r = signbit(diff) ? y : x;
+    return (isnan(x) || isnan(y)) ? diff : r;
+}
+static inline REAL SFX(jl_min)(REAL x, REAL y) {
+    REAL diff = x - y;
+    REAL r = signbit(diff) ? x : y;
+    return (isnan(x) || isnan(y)) ? diff : r;
+}
+
+/* Value of the FD macro {kind, opdims, inn} of A at thread index t
+ * (src/FiniteDifferences.jl:54-61, 160-185, 328-394). */
+static REAL SFX(fd_eval)(int kind, int opdims, int inn, int ndims, const REAL* A, const int64_t* nA,
+                         const int64_t* t) {
+    int64_t b[3];
+    for (int d = 0; d < 3; d++) b[d] = t[d] + ((inn >> d) & 1);
+    switch (kind) {
+    case 0: /* selection */
+        return A[OIDX(b[0], b[1], b[2], nA)];
+    case 1: { /* A[i+1] - A[i] */
+        int d = (opdims & 1) ? 0 : (opdims & 2) ? 1 : 2;
+        int64_t p[3] = {b[0], b[1], b[2]};
+        p[d] += 1;
+        return A[OIDX(p[0], p[1], p[2], nA)] - A[OIDX(b[0], b[1], b[2], nA)];
+    }
+    case 2: { /* (A[i+1] - A[i]) - (A[i] - A[i-1]) */
+        int d = (opdims & 1) ? 0 : (opdims & 2) ? 1 : 2;
+        int64_t p[3] = {b[0], b[1], b[2]}, m[3] = {b[0], b[1], b[2]};
+        p[d] += 1;
+        m[d] -= 1;
+        REAL c = A[OIDX(b[0], b[1], b[2], nA)];
+        return (A[OIDX(p[0], p[1], p[2], nA)] - c) - (c - A[OIDX(m[0], m[1], m[2], nA)]);
+    }
+    case 3:   /* average: corners in x-fastest order, left-fold sum, times 0.5 / 0.25 / 0.125 */
+    case 4: { /* harmonic: 1.0/(1.0/a + 1.0/b + ...)*k */
+        int dims[3], k = 0;
+        for (int d = 0; d < 3; d++)
+            if ((opdims >> d) & 1) dims[k++] = d;
+        int ncorner = 1 << k;
+        REAL s = (REAL)0;
+        for (int c = 0; c < ncorner; c++) {
+            int64_t p[3] = {b[0], b[1], b[2]};
+            for (int j = 0; j < k; j++) p[dims[j]] += (c >> j) & 1;
+            REAL v = A[OIDX(p[0], p[1], p[2], nA)];
+            if (kind == 4) v = (REAL)1.0 / v;
+            s = (c == 0) ? v : s + v;
+        }
+        if (kind == 3) return s * ((REAL)1.0 / (REAL)ncorner);
+        return ((REAL)1.0 / s) * (REAL)ncorner;
+    }
+    case 5:
+    case 6: { /* maxloc / minloc: op(op(op(x-, x+), c), op(y-, y+)), ... */
+        REAL m = 0;
+        for (int d = 0; d < ndims; d++) {
+            int64_t p[3] = {b[0], b[1], b[2]}, q[3] = {b[0], b[1], b[2]};
+            p[d] -= 1;
+            q[d] += 1;
+            REAL lo = A[OIDX(p[0], p[1], p[2], nA)], hi = A[OIDX(q[0], q[1], q[2], nA)];
+            REAL pair = (kind == 5) ? SFX(jl_max)(lo, hi) : SFX(jl_min)(lo, hi);
+            if (d == 0) {
+                REAL c = A[OIDX(b[0], b[1], b[2], nA)];
+                m = (kind == 5) ? SFX(jl_max)(pair, c) : SFX(jl_min)(pair, c);
+            } else {
+                m = (kind == 5) ? SFX(jl_max)(m, pair) : SFX(jl_min)(m, pair);
+            }
+        }
+        return m;
+    }
+    }
+    return (REAL)0;
+}
+
+/* `@<lhs>(R) = @<op>(A)`: grid = max(size(R), size(A)); statement masked by `@within`
+ * of the left-hand selection (lhs_inn), src/parallel.jl:654-680. */
+int SFX(orc_fd_apply)(int kind, int opdims, int inn, int ndims, int lhs_inn, REAL* R, const int64_t* nR,
+                      const REAL* A, const int64_t* nA) {
+    int64_t lo[3], hi[3], tmax[3];
+    for (int d = 0; d < 3; d++) {
+        int li = (lhs_inn >> d) & 1;
+        tmax[d] = nR[d] - 2 * li; /* threads passing the mask: 0 <= t < tmax */
+        int rlo = 0, rhi = 0;
+        if (kind == 1 || kind == 3 || kind == 4) rhi = (opdims >> d) & 1;
+        if (kind == 2 || kind == 5 || kind == 6) rlo = rhi = (opdims >> d) & 1;
+        lo[d] = ((inn >> d) & 1) - rlo;
+        hi[d] = ((inn >> d) & 1) + rhi;
+    }
+    if (tmax[0] <= 0 || tmax[1] <= 0 || tmax[2] <= 0) return ORC_OK;
+    for (int d = 0; d < 3; d++)
+        if (lo[d] < 0 || tmax[d] - 1 + hi[d] > nA[d] - 1) return ORC_ERR_SHAPE;
+    int lx = lhs_inn & 1, ly = (lhs_inn >> 1) & 1, lz = (lhs_inn >> 2) & 1;
+#pragma omp parallel for schedule(static)
+    for (int64_t tz = 0; tz < tmax[2]; tz++)
+        for (int64_t ty = 0; ty < tmax[1]; ty++)
+            for (int64_t tx = 0; tx < tmax[0]; tx++) {
+                int64_t t[3] = {tx, ty, tz};
+                R[OIDX(tx + lx, ty + ly, tz + lz, nR)] = SFX(fd_eval)(kind, opdims, inn, ndims, A, nA, t);
+            }
+    return ORC_OK;
+}
+
+/* `@all(T2) = @all(T) + @all(Ci)` over thread box [lo, hi) (examples/memcopy3D.jl:10-13). */
+int SFX(orc_memcopy3d)(REAL* T2, const REAL* T, const REAL* Ci, const int64_t* n, const int64_t* lo,
+                       const int64_t* hi) {
+#pragma omp parallel for schedule(static)
+    for (int64_t iz = lo[2]; iz < hi[2]; iz++)
+        for (int64_t iy = lo[1]; iy < hi[1]; iy++)
+            for (int64_t ix = lo[0]; ix < hi[0]; ix++) {
+                int64_t i = OIDX(ix, iy, iz, n);
+                T2[i] = T[i] + Ci[i];
+            }
+    return ORC_OK;
+}
+
+/* One step of the 3-D diffusion kernel in one of the four statement forms
+ * (form 0: examples/diffusion3D_novis_noperf.jl:10-13; 1: examples/
+ * diffusion3D_multigpucpu_hidecomm_novis.jl:12-15; 2: test/test_parallel.jl:420-426;
+ * 3: the flux form with face conductivities @av_xi(lam) etc.). Thread box [lo, hi) of
+ * the `@parallel` grid; the `@inn(T2)` mask gives cell c = t + 1 for t < n - 2. */
+int SFX(orc_diffusion3d_step)(int form, REAL* T2, const REAL* T, const REAL* Ci, const REAL* lam_arr, REAL lam,
+                              REAL dt, REAL hx, REAL hy, REAL hz, const int64_t* n, const int64_t* lo,
+                              const int64_t* hi) {
+    if (form < 0 || form > 3) return ORC_ERR_ARG;
+    int64_t a[3], e[3];
+    for (int d = 0; d < 3; d++) {
+        a[d] = lo[d] < 0 ? 0 : lo[d];
+        e[d] = hi[d] > n[d] - 2 ? n[d] - 2 : hi[d];
+    }
+    const int64_t sx = 1, sy = n[0], sz = n[0] * n[1];
+#pragma omp parallel for schedule(static)
+    for (int64_t tz = a[2]; tz < e[2]; tz++)
+        for (int64_t ty = a[1]; ty < e[1]; ty++)
+            for (int64_t tx = a[0]; tx < e[0]; tx++) {
+                int64_t c = OIDX(tx + 1, ty + 1, tz + 1, n);
+                REAL Tc = T[c];
+                REAL out;
+                if (form == 0 || form == 1) {
+                    REAL d2x = (T[c + sx] - Tc) - (Tc - T[c - sx]);
+                    REAL d2y = (T[c + sy] - Tc) - (Tc - T[c - sy]);
+                    REAL d2z = (T[c + sz] - Tc) - (Tc - T[c - sz]);
+                    REAL s;
+                    if (form == 0)
+                        s = (d2x / (hx * hx) + d2y / (hy * hy)) + d2z / (hz * hz);
+                    else
+                        s = (d2x * (hx * hx) + d2y * (hy * hy)) + d2z * (hz * hz);
+                    out = Tc + dt * ((lam * Ci[c]) * s);
+                } else {
+                    REAL kxp, kxm, kyp, kym, kzp, kzm;
+                    if (form == 2) {
+                        kxp = kxm = kyp = kym = kzp = kzm = lam;
+                    } else {
+                        REAL lc = lam_arr[c];
+                        kxp = (lc + lam_arr[c + sx]) * (REAL)0.5;
+                        kxm = (lam_arr[c - sx] + lc) * (REAL)0.5;
+                        kyp = (lc + lam_arr[c + sy]) * (REAL)0.5;
+                        kym = (lam_arr[c - sy] + lc) * (REAL)0.5;
+                        kzp = (lc + lam_arr[c + sz]) * (REAL)0.5;
+                        kzm = (lam_arr[c - sz] + lc) * (REAL)0.5;
+                    }
+                    REAL qxp = ((-kxp) * (T[c + sx] - Tc)) * hx, qxm = ((-kxm) * (Tc - T[c - sx])) * hx;
+                    REAL qyp = ((-kyp) * (T[c + sy] - Tc)) * hy, qym = ((-kym) * (Tc - T[c - sy])) * hy;
+                    REAL qzp = ((-kzp) * (T[c + sz] - Tc)) * hz, qzm = ((-kzm) * (Tc - T[c - sz])) * hz;
+                    REAL dTdt = Ci[c] * (((-(qxp - qxm)) * hx - (qyp - qym) * hy) - (qzp - qzm) * hz);
+                    out = Tc + dt * dTdt;
+                }
+                T2[c] = out;
+            }
+    return ORC_OK;
+}
+
+/* acoustic3D compute_V! (miniapps/acoustic3D.jl:11-16): grid (nx+1, ny+1, nz+1);
+ * P is (nx, ny, nz), Vx (nx+1, ny, nz), Vy (nx, ny+1, nz), Vz (nx, ny, nz+1). */
+int SFX(orc_acoustic3d_v)(REAL* Vx, REAL* Vy, REAL* Vz, const REAL* P, const int64_t* n, REAL dt, REAL rho,
+                          REAL dx, REAL dy, REAL dz) {
+    int64_t nx = n[0], ny = n[1], nz = n[2];
+    int64_t nVx[3] = {nx + 1, ny, nz}, nVy[3] = {nx, ny + 1, nz}, nVz[3] = {nx, ny, nz + 1};
+    REAL dtr = dt / rho;
+#pragma omp parallel for schedule(static)
+    for (int64_t tz = 0; tz < nz + 1; tz++)
+        for (int64_t ty = 0; ty < ny + 1; ty++)
+            for (int64_t tx = 0; tx < nx + 1; tx++) {
+                if (tx < nVx[0] - 2 && ty < nVx[1] - 2 && tz < nVx[2] - 2) {
+                    int64_t v = OIDX(tx + 1, ty + 1, tz + 1, nVx);
+                    REAL d = P[OIDX(tx + 1, ty + 1, tz + 1, n)] - P[OIDX(tx, ty + 1, tz + 1, n)];
+                    Vx[v] = Vx[v] - (dtr * d) / dx;
+                }
+                if (tx < nVy[0] - 2 && ty < nVy[1] - 2 && tz < nVy[2] - 2) {
+                    int64_t v = OIDX(tx + 1, ty + 1, tz + 1, nVy);
+                    REAL d = P[OIDX(tx + 1, ty + 1, tz + 1, n)] - P[OIDX(tx + 1, ty, tz + 1, n)];
+                    Vy[v] = Vy[v] - (dtr * d) / dy;
+                }
+                if (tx < nVz[0] - 2 && ty < nVz[1] - 2 && tz < nVz[2] - 2) {
+                    int64_t v = OIDX(tx + 1, ty + 1, tz + 1, nVz);
+                    REAL d = P[OIDX(tx + 1, ty + 1, tz + 1, n)] - P[OIDX(tx + 1, ty + 1, tz, n)];
+                    Vz[v] = Vz[v] - (dtr * d) / dz;
+                }
+            }
+    return ORC_OK;
+}
+
+/* acoustic3D compute_P! (miniapps/acoustic3D.jl:18-21). */
+int SFX(orc_acoustic3d_p)(REAL* P, const REAL* Vx, const REAL* Vy, const REAL* Vz, const int64_t* n, REAL dt,
+                          REAL k, REAL dx, REAL dy, REAL dz) {
+    int64_t nx = n[0], ny = n[1], nz = n[2];
+    int64_t nVx[3] = {nx + 1, ny, nz}, nVy[3] = {nx, ny + 1, nz}, nVz[3] = {nx, ny, nz + 1};
+    REAL dtk = dt * k;
+#pragma omp parallel for schedule(static)
+    for (int64_t iz = 0; iz < nz; iz++)
+        for (int64_t iy = 0; iy < ny; iy++)
+            for (int64_t ix = 0; ix < nx; ix++) {
+                REAL ax = Vx[OIDX(ix + 1, iy, iz, nVx)] - Vx[OIDX(ix, iy, iz, nVx)];
+                REAL ay = Vy[OIDX(ix, iy + 1, iz, nVy)] - Vy[OIDX(ix, iy, iz, nVy)];
+                REAL az = Vz[OIDX(ix, iy, iz + 1, nVz)] - Vz[OIDX(ix, iy, iz, nVz)];
+                int64_t p = OIDX(ix, iy, iz, n);
+                P[p] = P[p] - dtk * ((ax / dx + ay / dy) + az / dz);
+            }
+    return ORC_OK;
+}
+
+#undef OIDX

@@ -1,0 +1,287 @@
+// ps_core.cu -- device state, errors, memory, streams and TMA descriptors of libps_b200.so.
+//
+// Replaces the CUDA-extension plumbing of ParallelStencil.jl: device selection at
+// `@init_parallel_stencil` (src/init_parallel_stencil.jl:36-51), `@zeros`/`@fill!`
+// allocation (src/ParallelKernel/CUDAExt/allocators.jl:3-8), and the priority / normal
+// stream pools of `@hide_communication` (src/ParallelKernel/CUDAExt/shared.jl:17-31).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "ps_common.cuh"
+
+namespace ps {
+
+static thread_local char g_errmsg[512] = "";
+static constexpr int kMaxDevices = 64;
+static DeviceState g_dev[kMaxDevices];
+static std::mutex g_mutex;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn g_encode = nullptr;
+
+int fail(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_errmsg, sizeof(g_errmsg), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(PS_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+void clear_error() { g_errmsg[0] = '\0'; }
+
+int current_state(DeviceState** st) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices || !g_dev[dev].ready)
+        return fail(PS_ERR_NOT_INIT, "ps_init has not been called for the current device");
+    *st = &g_dev[dev];
+    return PS_OK;
+}
+
+int check_device_error(DeviceState* st, cudaStream_t s) {
+    int h = 0;
+    PS_CUDA_TRY(cudaMemcpyAsync(&h, st->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h != DEV_ERR_NONE) {
+        int zero = 0;
+        PS_CUDA_TRY(cudaMemcpyAsync(st->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+        PS_CUDA_TRY(cudaStreamSynchronize(s));
+        return fail(PS_ERR_TIMEOUT, "a bounded device-side wait gave up (device error code %d)", h);
+    }
+    return PS_OK;
+}
+
+int finish_launch(cudaStream_t s, int sync, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (sync) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(e, what);
+        DeviceState* st = nullptr;
+        PS_TRY(current_state(&st));
+        PS_TRY(check_device_error(st, s));
+    }
+    return PS_OK;
+}
+
+int check_array(const ps_array& a, const char* name) {
+    if (a.ptr == nullptr) return fail(PS_ERR_NULL, "array %s: NULL device pointer", name);
+    if (a.dtype != PS_F64 && a.dtype != PS_F32) return fail(PS_ERR_DTYPE, "array %s: unsupported dtype %d", name, a.dtype);
+    for (int d = 0; d < 3; d++)
+        if (a.n[d] < 1) return fail(PS_ERR_SHAPE, "array %s: extent n[%d] = %lld < 1", name, d, (long long)a.n[d]);
+    if ((reinterpret_cast<uintptr_t>(a.ptr) % elsize(a.dtype)) != 0)
+        return fail(PS_ERR_ALIGN, "array %s: pointer not aligned to its element size", name);
+    return PS_OK;
+}
+
+int check_same_dtype(const ps_array& a, const ps_array& b, const char* na, const char* nb) {
+    if (a.dtype != b.dtype) return fail(PS_ERR_DTYPE, "arrays %s and %s have different dtypes", na, nb);
+    return PS_OK;
+}
+
+int check_shape(const ps_array& a, int64_t nx, int64_t ny, int64_t nz, const char* name) {
+    if (a.n[0] != nx || a.n[1] != ny || a.n[2] != nz)
+        return fail(PS_ERR_SHAPE, "array %s: size (%lld,%lld,%lld), expected (%lld,%lld,%lld)", name,
+                    (long long)a.n[0], (long long)a.n[1], (long long)a.n[2], (long long)nx, (long long)ny,
+                    (long long)nz);
+    return PS_OK;
+}
+
+Box launch_box(const ps_launch* cfg, const int64_t grid[3]) {
+    Box b;
+    bool use = cfg != nullptr;
+    if (use) {
+        bool any = false;
+        for (int d = 0; d < 3; d++) any |= cfg->range_hi[d] > cfg->range_lo[d];
+        use = any;
+    }
+    for (int d = 0; d < 3; d++) {
+        b.lo[d] = use ? cfg->range_lo[d] : 0;
+        b.hi[d] = use ? cfg->range_hi[d] : grid[d];
+        if (b.lo[d] < 0) b.lo[d] = 0;
+        if (b.hi[d] > grid[d]) b.hi[d] = grid[d];
+    }
+    return b;
+}
+
+bool tma_eligible(const ps_array& a) {
+    size_t es = elsize(a.dtype);
+    if (reinterpret_cast<uintptr_t>(a.ptr) % 16 != 0) return false;
+    if ((a.n[0] * es) % 16 != 0) return false;
+    if ((a.n[0] * a.n[1] * es) % 16 != 0) return false;
+    if (a.n[0] >= (1ll << 32) || a.n[1] >= (1ll << 32) || a.n[2] >= (1ll << 32)) return false;
+    return g_encode != nullptr;
+}
+
+int encode_plane_map(CUtensorMap* map, const ps_array& a, uint32_t bx, uint32_t by) {
+    if (!tma_eligible(a)) return fail(PS_ERR_ALIGN, "array not eligible for TMA (16-byte base/stride rule)");
+    size_t es = elsize(a.dtype);
+    if ((bx * es) % 16 != 0 || bx > 256 || by > 256) return fail(PS_ERR_ARG, "invalid TMA box (%u, %u)", bx, by);
+    cuuint64_t dims[3] = {(cuuint64_t)a.n[0], (cuuint64_t)a.n[1], (cuuint64_t)a.n[2]};
+    cuuint64_t strides[2] = {(cuuint64_t)(a.n[0] * es), (cuuint64_t)(a.n[0] * a.n[1] * es)};
+    cuuint32_t box[3] = {bx, by, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUtensorMapDataType dt = a.dtype == PS_F64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    CUresult r = g_encode(map, dt, 3, a.ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+    return PS_OK;
+}
+
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" {
+
+int ps_abi_version(void) { return PS_ABI_VERSION; }
+
+const char* ps_last_error(void) { return g_errmsg; }
+
+int ps_device_count(int* count) {
+    if (!count) return fail(PS_ERR_NULL, "ps_device_count: NULL output");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return PS_OK;
+}
+
+int ps_init(int device) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(PS_ERR_CUDA, "ps_init: no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n || device >= kMaxDevices)
+        return fail(PS_ERR_ARG, "ps_init: device %d out of range (0..%d)", device, n - 1);
+    PS_CUDA_TRY(cudaSetDevice(device));
+    DeviceState& st = g_dev[device];
+    if (st.ready) return PS_OK;
+    cudaDeviceProp prop;
+    PS_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    if (prop.major < 10) return fail(PS_ERR_UNSUPPORTED, "ps_init: device %d is sm_%d%d; this build targets sm_103a", device, prop.major, prop.minor);
+    st.num_sms = prop.multiProcessorCount;
+    PS_CUDA_TRY(cudaMalloc(&st.d_err, sizeof(int)));
+    PS_CUDA_TRY(cudaMemset(st.d_err, 0, sizeof(int)));
+    st.scratch_bytes = 64 * 1024;
+    PS_CUDA_TRY(cudaMalloc(&st.d_scratch, st.scratch_bytes));
+    if (g_encode == nullptr) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<EncodeTiledFn>(fn);
+        cudaGetLastError();
+    }
+    PS_CUDA_TRY(cudaDeviceSynchronize());
+    st.ready = true;
+    clear_error();
+    return PS_OK;
+}
+
+int ps_finalize(void) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (int d = 0; d < kMaxDevices; d++) {
+        DeviceState& st = g_dev[d];
+        if (!st.ready) continue;
+        cudaSetDevice(d);
+        cudaDeviceSynchronize();
+        cudaFree(st.d_err);
+        cudaFree(st.d_scratch);
+        st = DeviceState();
+    }
+    cudaSetDevice(cur);
+    cudaGetLastError();
+    return PS_OK;
+}
+
+int ps_alloc(ps_array* a, int32_t dtype, int64_t nx, int64_t ny, int64_t nz) {
+    if (!a) return fail(PS_ERR_NULL, "ps_alloc: NULL descriptor");
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    if (dtype != PS_F64 && dtype != PS_F32 && dtype != PS_BF16) return fail(PS_ERR_DTYPE, "ps_alloc: dtype %d", dtype);
+    if (nx < 1 || ny < 1 || nz < 1) return fail(PS_ERR_SHAPE, "ps_alloc: extents must be >= 1");
+    size_t bytes = (size_t)nx * (size_t)ny * (size_t)nz * elsize(dtype);
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PS_ERR_NOMEM, "ps_alloc: cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    PS_CUDA_TRY(cudaMemset(p, 0, bytes));
+    a->ptr = p;
+    a->n[0] = nx;
+    a->n[1] = ny;
+    a->n[2] = nz;
+    a->dtype = dtype;
+    a->reserved = 0;
+    return PS_OK;
+}
+
+int ps_free(ps_array* a) {
+    if (!a) return fail(PS_ERR_NULL, "ps_free: NULL descriptor");
+    if (a->ptr) PS_CUDA_TRY(cudaFree(a->ptr));
+    a->ptr = nullptr;
+    return PS_OK;
+}
+
+int ps_copy_h2d(ps_array dst, const void* host_src, void* stream) {
+    PS_TRY(check_array(dst, "dst"));
+    if (!host_src) return fail(PS_ERR_NULL, "ps_copy_h2d: NULL host pointer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PS_CUDA_TRY(cudaMemcpyAsync(dst.ptr, host_src, numel(dst) * elsize(dst.dtype), cudaMemcpyHostToDevice, s));
+    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    return PS_OK;
+}
+
+int ps_copy_d2h(void* host_dst, ps_array src, void* stream) {
+    PS_TRY(check_array(src, "src"));
+    if (!host_dst) return fail(PS_ERR_NULL, "ps_copy_d2h: NULL host pointer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PS_CUDA_TRY(cudaMemcpyAsync(host_dst, src.ptr, numel(src) * elsize(src.dtype), cudaMemcpyDeviceToHost, s));
+    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    return PS_OK;
+}
+
+int ps_stream_create(int priority, void** stream) {
+    if (!stream) return fail(PS_ERR_NULL, "ps_stream_create: NULL output");
+    int lo = 0, hi = 0;
+    PS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    cudaStream_t s;
+    PS_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, priority > 0 ? hi : lo));
+    *stream = s;
+    return PS_OK;
+}
+
+int ps_stream_destroy(void* stream) {
+    if (stream) PS_CUDA_TRY(cudaStreamDestroy(static_cast<cudaStream_t>(stream)));
+    return PS_OK;
+}
+
+int ps_synchronize(void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    return check_device_error(st, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,882 @@
+// ps_stencil3d.cu -- FD operators, memcopy3D and diffusion3D kernels of libps_b200.so.
+//
+// Kernels:
+//   fd_apply_kernel      one-statement `@parallel` kernels of every FiniteDifferences macro
+//                        (src/FiniteDifferences.jl:54-61, 160-185, 328-394)
+//   memcopy_flat/_box    `@all(T2) = @all(T) + @all(Ci)` (examples/memcopy3D.jl:10-13)
+//   diff3d_plain         diffusion step, one thread per cell (`memopt=false`)
+//   diff3d_zsweep_tma    diffusion step, z-sweep with TMA-staged x-y planes in a shared-memory
+//                        ring and register-rotated z neighbours (`memopt=true`; the reference's
+//                        memopt codegen is src/memopt.jl:190-573)
+//   diff3d_zsweep_smem   the same sweep with thread-loaded planes, for arrays whose extents break
+//                        TMA's 16-byte stride rule (odd nx, e.g. the reference's 31/33/127 sizes)
+// All arithmetic is compiled without FMA contraction (--fmad=false) in the macros' operation
+// order, so FP64 results are bit-identical to the reference's CPU path.
+#include <algorithm>
+
+#include "ps_common.cuh"
+
+namespace ps {
+
+// =======================================================================================
+// Fill
+// =======================================================================================
+template <typename T>
+__global__ void fill_kernel(T* __restrict__ a, int64_t n, T v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
+// =======================================================================================
+// Generic FD operator kernel
+// =======================================================================================
+struct FdDesc {
+    int kind, opdims, inn, ndims, lhs_inn;
+    int64_t nR[3], nA[3], tmax[3];
+};
+
+template <typename T>
+__device__ __forceinline__ T fd_load(const T* A, const int64_t* nA, int64_t x, int64_t y, int64_t z) {
+    return A[x + nA[0] * (y + nA[1] * z)];
+}
+
+template <typename T>
+__device__ T fd_eval(const FdDesc& d, const T* __restrict__ A, const int64_t t[3]) {
+    int64_t b[3];
+    for (int k = 0; k < 3; k++) b[k] = t[k] + ((d.inn >> k) & 1);
+    switch (d.kind) {
+    case PS_FD_SEL:
+        return fd_load(A, d.nA, b[0], b[1], b[2]);
+    case PS_FD_DIFF: {
+        int k = (d.opdims & 1) ? 0 : (d.opdims & 2) ? 1 : 2;
+        int64_t p[3] = {b[0], b[1], b[2]};
+        p[k] += 1;
+        return fd_load(A, d.nA, p[0], p[1], p[2]) - fd_load(A, d.nA, b[0], b[1], b[2]);
+    }
+    case PS_FD_DIFF2: {
+        int k = (d.opdims & 1) ? 0 : (d.opdims & 2) ? 1 : 2;
+        int64_t p[3] = {b[0], b[1], b[2]}, m[3] = {b[0], b[1], b[2]};
+        p[k] += 1;
+        m[k] -= 1;
+        T c = fd_load(A, d.nA, b[0], b[1], b[2]);
+        return (fd_load(A, d.nA, p[0], p[1], p[2]) - c) - (c - fd_load(A, d.nA, m[0], m[1], m[2]));
+    }
+    case PS_FD_AV:
+    case PS_FD_HARM: {
+        int dims[3], nd = 0;
+        for (int k = 0; k < 3; k++)
+            if ((d.opdims >> k) & 1) dims[nd++] = k;
+        int nc = 1 << nd;
+        T s = T(0);
+        for (int c = 0; c < nc; c++) {
+            int64_t p[3] = {b[0], b[1], b[2]};
+            for (int j = 0; j < nd; j++) p[dims[j]] += (c >> j) & 1;
+            T v = fd_load(A, d.nA, p[0], p[1], p[2]);
+            if (d.kind == PS_FD_HARM) v = T(1) / v;
+            s = (c == 0) ? v : s + v;
+        }
+        if (d.kind == PS_FD_AV) return s * (T(1) / T(nc));
+        return (T(1) / s) * T(nc);
+    }
+    default: {  // maxloc / minloc
+        bool mx = d.kind == PS_FD_MAXLOC;
+        T m = T(0);
+        for (int k = 0; k < d.ndims; k++) {
+            int64_t p[3] = {b[0], b[1], b[2]}, q[3] = {b[0], b[1], b[2]};
+            p[k] -= 1;
+            q[k] += 1;
+            T lo = fd_load(A, d.nA, p[0], p[1], p[2]), hi = fd_load(A, d.nA, q[0], q[1], q[2]);
+            T pair = mx ? jl_max(lo, hi) : jl_min(lo, hi);
+            if (k == 0) {
+                T c = fd_load(A, d.nA, b[0], b[1], b[2]);
+                m = mx ? jl_max(pair, c) : jl_min(pair, c);
+            } else {
+                m = mx ? jl_max(m, pair) : jl_min(m, pair);
+            }
+        }
+        return m;
+    }
+    }
+}
+
+template <typename T>
+__global__ void fd_apply_kernel(T* __restrict__ R, const T* __restrict__ A, FdDesc d) {
+    int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (tx >= d.tmax[0] || ty >= d.tmax[1]) return;
+    for (int64_t tz = blockIdx.z; tz < d.tmax[2]; tz += gridDim.z) {
+        int64_t t[3] = {tx, ty, tz};
+        int64_t rx = tx + (d.lhs_inn & 1), ry = ty + ((d.lhs_inn >> 1) & 1), rz = tz + ((d.lhs_inn >> 2) & 1);
+        R[rx + d.nR[0] * (ry + d.nR[1] * rz)] = fd_eval(d, A, t);
+    }
+}
+
+// =======================================================================================
+// memcopy3D
+// =======================================================================================
+template <typename T>
+struct Vec;
+template <>
+struct Vec<double> {
+    static constexpr int N = 2;
+    using type = double2;
+};
+template <>
+struct Vec<float> {
+    static constexpr int N = 4;
+    using type = float4;
+};
+
+template <typename T>
+__device__ __forceinline__ typename Vec<T>::type vadd(typename Vec<T>::type a, typename Vec<T>::type b);
+template <>
+__device__ __forceinline__ double2 vadd<double>(double2 a, double2 b) {
+    return make_double2(a.x + b.x, a.y + b.y);
+}
+template <>
+__device__ __forceinline__ float4 vadd<float>(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// Flat streaming form over whole arrays (the full `@parallel` grid): 128-bit loads and
+// stores, 4 independent vectors in flight per thread per iteration.
+template <typename T>
+__global__ void __launch_bounds__(256) memcopy_flat(T* __restrict__ T2, const T* __restrict__ Tin,
+                                                    const T* __restrict__ Ci, int64_t n) {
+    using V = typename Vec<T>::type;
+    constexpr int VN = Vec<T>::N;
+    constexpr int U = 4;
+    const int64_t nv = n / VN;
+    const V* a = reinterpret_cast<const V*>(Tin);
+    const V* b = reinterpret_cast<const V*>(Ci);
+    V* o = reinterpret_cast<V*>(T2);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < nv; i += U * stride) {
+        V x[U], y[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            x[u] = __ldcs(a + i + u * stride);
+            y[u] = __ldcs(b + i + u * stride);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) __stcs(o + i + u * stride, vadd<T>(x[u], y[u]));
+    }
+    for (; i < nv; i += stride) __stcs(o + i, vadd<T>(__ldcs(a + i), __ldcs(b + i)));
+    // scalar tail
+    int64_t t = nv * VN + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) T2[t] = Tin[t] + Ci[t];
+}
+
+template <typename T>
+__global__ void memcopy_box(T* __restrict__ T2, const T* __restrict__ Tin, const T* __restrict__ Ci, int64_t nx,
+                            int64_t ny, Box b) {
+    int64_t x = b.lo[0] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t y = b.lo[1] + blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (x >= b.hi[0] || y >= b.hi[1]) return;
+    for (int64_t z = b.lo[2] + blockIdx.z; z < b.hi[2]; z += gridDim.z) {
+        int64_t i = x + nx * (y + ny * z);
+        T2[i] = Tin[i] + Ci[i];
+    }
+}
+
+// =======================================================================================
+// diffusion3D
+// =======================================================================================
+template <typename T>
+struct DiffParams {
+    T lam, dt, hx, hy, hz;
+};
+
+// One cell of the diffusion statement in form FORM (see ps_diffusion_form). Operation order
+// follows the Julia expression exactly; negation is exact so (-a)*b == -(a*b).
+template <typename T, int FORM>
+__device__ __forceinline__ T diff_cell(const DiffParams<T>& p, T Tc, T Txm, T Txp, T Tym, T Typ, T Tzm, T Tzp, T ci,
+                                       T lc, T lxm, T lxp, T lym, T lyp, T lzm, T lzp) {
+    if constexpr (FORM == PS_DIFF_DIV || FORM == PS_DIFF_MUL) {
+        T d2x = (Txp - Tc) - (Tc - Txm);
+        T d2y = (Typ - Tc) - (Tc - Tym);
+        T d2z = (Tzp - Tc) - (Tc - Tzm);
+        T s;
+        if constexpr (FORM == PS_DIFF_DIV)
+            s = (d2x / (p.hx * p.hx) + d2y / (p.hy * p.hy)) + d2z / (p.hz * p.hz);
+        else
+            s = (d2x * (p.hx * p.hx) + d2y * (p.hy * p.hy)) + d2z * (p.hz * p.hz);
+        return Tc + p.dt * ((p.lam * ci) * s);
+    } else {
+        T kxp, kxm, kyp, kym, kzp, kzm;
+        if constexpr (FORM == PS_DIFF_FLUX) {
+            kxp = kxm = kyp = kym = kzp = kzm = p.lam;
+        } else {
+            kxp = (lc + lxp) * T(0.5);
+            kxm = (lxm + lc) * T(0.5);
+            kyp = (lc + lyp) * T(0.5);
+            kym = (lym + lc) * T(0.5);
+            kzp = (lc + lzp) * T(0.5);
+            kzm = (lzm + lc) * T(0.5);
+        }
+        T qxp = ((-kxp) * (Txp - Tc)) * p.hx, qxm = ((-kxm) * (Tc - Txm)) * p.hx;
+        T qyp = ((-kyp) * (Typ - Tc)) * p.hy, qym = ((-kym) * (Tc - Tym)) * p.hy;
+        T qzp = ((-kzp) * (Tzp - Tc)) * p.hz, qzm = ((-kzm) * (Tc - Tzm)) * p.hz;
+        T dTdt = ci * (((-(qxp - qxm)) * p.hx - (qyp - qym) * p.hy) - (qzp - qzm) * p.hz);
+        return Tc + p.dt * dTdt;
+    }
+}
+
+// --- plain: one thread per cell, (32, 8, 1) threads like the reference's default --------
+template <typename T, int FORM>
+__global__ void __launch_bounds__(256) diff3d_plain(T* __restrict__ T2, const T* __restrict__ Tin,
+                                                    const T* __restrict__ Ci, const T* __restrict__ lam,
+                                                    DiffParams<T> p, int64_t nx, int64_t ny, Box cb) {
+    int64_t cx = cb.lo[0] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t cy = cb.lo[1] + blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (cx >= cb.hi[0] || cy >= cb.hi[1]) return;
+    const int64_t sy = nx, sz = nx * ny;
+    constexpr bool L = FORM == PS_DIFF_FLUX_LAM;
+    for (int64_t cz = cb.lo[2] + blockIdx.z; cz < cb.hi[2]; cz += gridDim.z) {
+        int64_t c = cx + sy * cy + sz * cz;
+        T Tc = __ldg(Tin + c);
+        T lc = L ? __ldg(lam + c) : T(0);
+        T r = diff_cell<T, FORM>(p, Tc, __ldg(Tin + c - 1), __ldg(Tin + c + 1), __ldg(Tin + c - sy), __ldg(Tin + c + sy),
+                                 __ldg(Tin + c - sz), __ldg(Tin + c + sz), __ldg(Ci + c), lc,
+                                 L ? __ldg(lam + c - 1) : T(0), L ? __ldg(lam + c + 1) : T(0),
+                                 L ? __ldg(lam + c - sy) : T(0), L ? __ldg(lam + c + sy) : T(0),
+                                 L ? __ldg(lam + c - sz) : T(0), L ? __ldg(lam + c + sz) : T(0));
+        T2[c] = r;
+    }
+}
+
+// --- z-sweep with TMA-staged planes -----------------------------------------------------
+// A CTA owns a TX x TY column of cells and sweeps `L` planes in z. Plane z of T (and lam)
+// is staged with its x-y halo by one TMA copy into slot (z mod S) of a shared-memory ring;
+// an mbarrier per slot signals completion. Each thread keeps the z-1 / z / z+1 values of
+// its VEC cells in registers (rotated every step) and reads x-y neighbours from the staged
+// plane. Ci is staged without halo in the same slot. T2 is written with 128-bit stores.
+template <typename T, int FORM, int TY, int S>
+struct ZSweep {
+    static constexpr int VEC = 16 / (int)sizeof(T);
+    static constexpr int TX = 32 * VEC;
+    static constexpr int H = VEC;  // x halo: keeps every TMA x coordinate 16-byte aligned
+    static constexpr int PW = TX + 2 * H;
+    static constexpr int PH = TY + 2;
+    static constexpr bool HAS_LAM = FORM == PS_DIFF_FLUX_LAM;
+    static constexpr int PLANE_BYTES = ((PW * PH * (int)sizeof(T) + 127) / 128) * 128;
+    static constexpr int CI_BYTES = ((TX * TY * (int)sizeof(T) + 127) / 128) * 128;
+    static constexpr int STAGE_BYTES = PLANE_BYTES * (HAS_LAM ? 2 : 1) + CI_BYTES;
+    static constexpr uint32_t TX_BYTES =
+        (uint32_t)(PW * PH * sizeof(T) * (HAS_LAM ? 2 : 1) + TX * TY * sizeof(T));
+    static constexpr int SMEM = S * STAGE_BYTES + 8 * S;
+};
+
+template <typename T, int FORM, int TY, int S>
+__global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_constant__ CUtensorMap mT,
+                                                             const __grid_constant__ CUtensorMap mL,
+                                                             const __grid_constant__ CUtensorMap mC,
+                                                             T* __restrict__ T2, DiffParams<T> p, int64_t nx,
+                                                             int64_t ny, Box cb, int L, int* __restrict__ err) {
+    using Z = ZSweep<T, FORM, TY, S>;
+    constexpr int VEC = Z::VEC;
+    using V = typename Vec<T>::type;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * Z::STAGE_BYTES);
+
+    const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
+    const int X0 = (int)(cb.lo[0] & ~(int64_t)(VEC - 1)) + blockIdx.x * Z::TX;
+    const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
+    const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
+    const int nk = min(L, (int)cb.hi[2] - Z0);
+    const int nq = nk + 2;  // planes Z0-1 .. Z0+nk
+
+    auto tplane = [&](int q) { return reinterpret_cast<T*>(smem + (q % S) * Z::STAGE_BYTES); };
+    auto lplane = [&](int q) { return reinterpret_cast<T*>(smem + (q % S) * Z::STAGE_BYTES + Z::PLANE_BYTES); };
+    auto cplane = [&](int q) {
+        return reinterpret_cast<T*>(smem + (q % S) * Z::STAGE_BYTES + Z::PLANE_BYTES * (Z::HAS_LAM ? 2 : 1));
+    };
+
+    if (tid == 0) {
+        prefetch_tensormap(&mT);
+        if constexpr (Z::HAS_LAM) prefetch_tensormap(&mL);
+        prefetch_tensormap(&mC);
+        for (int s = 0; s < S; s++) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    int next_q = 0;
+    auto issue = [&](int q) {
+        int s = q % S, z = Z0 - 1 + q;
+        mbar_arrive_expect_tx(&bar[s], Z::TX_BYTES);
+        tma_load_3d(tplane(q), &mT, &bar[s], X0 - Z::H, Y0 - 1, z);
+        if constexpr (Z::HAS_LAM) tma_load_3d(lplane(q), &mL, &bar[s], X0 - Z::H, Y0 - 1, z);
+        tma_load_3d(cplane(q), &mC, &bar[s], X0, Y0, z);
+    };
+    if (tid == 0)
+        for (; next_q < min(S, nq); ++next_q) issue(next_q);
+
+    const int px = Z::H + lx * VEC;  // staged-plane column of this thread's first cell
+    const int py = 1 + ly;
+    const int64_t gx = X0 + lx * VEC, gy = Y0 + ly;
+    const bool row_in = gy >= cb.lo[1] && gy < cb.hi[1];
+    bool full_vec = row_in && gx >= cb.lo[0] && gx + VEC <= cb.hi[0];
+
+    T Tzm[VEC], Tc[VEC], Tzp[VEC], lzm[VEC], lc[VEC], lzp[VEC];
+    bool timed_out = false;
+    timed_out |= !mbar_wait_bounded(&bar[0], 0);
+    timed_out |= !mbar_wait_bounded(&bar[1 % S], (1 / S) & 1);
+    if (!timed_out) {
+        const V a = *reinterpret_cast<const V*>(tplane(0) + py * Z::PW + px);
+        const V b = *reinterpret_cast<const V*>(tplane(1) + py * Z::PW + px);
+        const T* av = reinterpret_cast<const T*>(&a);
+        const T* bv = reinterpret_cast<const T*>(&b);
+#pragma unroll
+        for (int j = 0; j < VEC; j++) {
+            Tzm[j] = av[j];
+            Tc[j] = bv[j];
+        }
+        if constexpr (Z::HAS_LAM) {
+            const V la = *reinterpret_cast<const V*>(lplane(0) + py * Z::PW + px);
+            const V lb = *reinterpret_cast<const V*>(lplane(1) + py * Z::PW + px);
+            const T* lav = reinterpret_cast<const T*>(&la);
+            const T* lbv = reinterpret_cast<const T*>(&lb);
+#pragma unroll
+            for (int j = 0; j < VEC; j++) {
+                lzm[j] = lav[j];
+                lc[j] = lbv[j];
+            }
+        }
+    }
+
+    for (int k = 0; k < nk; ++k) {
+        const int q = k + 2;
+        timed_out |= !mbar_wait_bounded(&bar[q % S], (q / S) & 1);
+        if (!timed_out) {
+            const T* tp = tplane(k + 1);
+            {
+                const V zp = *reinterpret_cast<const V*>(tplane(q) + py * Z::PW + px);
+                const T* zv = reinterpret_cast<const T*>(&zp);
+#pragma unroll
+                for (int j = 0; j < VEC; j++) Tzp[j] = zv[j];
+            }
+            const V ym = *reinterpret_cast<const V*>(tp + (py - 1) * Z::PW + px);
+            const V yp = *reinterpret_cast<const V*>(tp + (py + 1) * Z::PW + px);
+            const T xm = tp[py * Z::PW + px - 1];
+            const T xp = tp[py * Z::PW + px + VEC];
+            const V cv = *reinterpret_cast<const V*>(cplane(k + 1) + ly * Z::TX + lx * VEC);
+            const T* ymv = reinterpret_cast<const T*>(&ym);
+            const T* ypv = reinterpret_cast<const T*>(&yp);
+            const T* civ = reinterpret_cast<const T*>(&cv);
+            T lym_[VEC], lyp_[VEC], lxm = T(0), lxp = T(0);
+            if constexpr (Z::HAS_LAM) {
+                const T* lp = lplane(k + 1);
+                const V zp = *reinterpret_cast<const V*>(lplane(q) + py * Z::PW + px);
+                const T* zv = reinterpret_cast<const T*>(&zp);
+                const V a = *reinterpret_cast<const V*>(lp + (py - 1) * Z::PW + px);
+                const V b = *reinterpret_cast<const V*>(lp + (py + 1) * Z::PW + px);
+                const T* av = reinterpret_cast<const T*>(&a);
+                const T* bv = reinterpret_cast<const T*>(&b);
+#pragma unroll
+                for (int j = 0; j < VEC; j++) {
+                    lzp[j] = zv[j];
+                    lym_[j] = av[j];
+                    lyp_[j] = bv[j];
+                }
+                lxm = lp[py * Z::PW + px - 1];
+                lxp = lp[py * Z::PW + px + VEC];
+            } else {
+#pragma unroll
+                for (int j = 0; j < VEC; j++) lym_[j] = lyp_[j] = lzp[j] = lc[j] = lzm[j] = T(0);
+            }
+            T out[VEC];
+#pragma unroll
+            for (int j = 0; j < VEC; j++) {
+                T txm = j == 0 ? xm : Tc[j - 1];
+                T txp = j == VEC - 1 ? xp : Tc[j + 1];
+                T lxm_j = j == 0 ? lxm : lc[j - 1];
+                T lxp_j = j == VEC - 1 ? lxp : lc[j + 1];
+                out[j] = diff_cell<T, FORM>(p, Tc[j], txm, txp, ymv[j], ypv[j], Tzm[j], Tzp[j], civ[j], lc[j], lxm_j,
+                                            lxp_j, lym_[j], lyp_[j], lzm[j], lzp[j]);
+            }
+            const int64_t gz = Z0 + k;
+            T* dst = T2 + gx + nx * (gy + ny * gz);
+            if (full_vec) {
+                V o;
+                T* ov = reinterpret_cast<T*>(&o);
+#pragma unroll
+                for (int j = 0; j < VEC; j++) ov[j] = out[j];
+                *reinterpret_cast<V*>(dst) = o;
+            } else if (row_in) {
+#pragma unroll
+                for (int j = 0; j < VEC; j++)
+                    if (gx + j >= cb.lo[0] && gx + j < cb.hi[0]) dst[j] = out[j];
+            }
+#pragma unroll
+            for (int j = 0; j < VEC; j++) {
+                Tzm[j] = Tc[j];
+                Tc[j] = Tzp[j];
+                if constexpr (Z::HAS_LAM) {
+                    lzm[j] = lc[j];
+                    lc[j] = lzp[j];
+                }
+            }
+        }
+        // Every thread is done with plane k+1: its slot may be refilled.
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0) {
+                atomicExch(err, DEV_ERR_TMA_TIMEOUT);
+                for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % S], (r / S) & 1);
+            }
+            return;
+        }
+        if (tid == 0)
+            for (; next_q < min(nq, k + 2 + S); ++next_q) issue(next_q);
+    }
+}
+
+// --- z-sweep with thread-loaded planes (fallback for non-TMA-eligible arrays) ----------
+// The reference's memopt structure: per z step, the x-y halo plane of T (and lam) is loaded
+// into shared memory between two barriers; z neighbours rotate through registers.
+template <typename T, int FORM, int TY>
+__global__ void __launch_bounds__(32 * TY) diff3d_zsweep_smem(T* __restrict__ T2, const T* __restrict__ Tin,
+                                                              const T* __restrict__ Ci, const T* __restrict__ lam,
+                                                              DiffParams<T> p, int64_t nx, int64_t ny, int64_t nz,
+                                                              Box cb, int L) {
+    constexpr bool HAS_LAM = FORM == PS_DIFF_FLUX_LAM;
+    constexpr int PW = 32 + 2, PH = TY + 2;
+    __shared__ T sT[PH][PW];
+    __shared__ T sL[HAS_LAM ? PH : 1][HAS_LAM ? PW : 1];
+    const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
+    const int64_t X0 = cb.lo[0] + blockIdx.x * 32, Y0 = cb.lo[1] + blockIdx.y * TY;
+    const int64_t Z0 = cb.lo[2] + blockIdx.z * (int64_t)L;
+    const int64_t Z1 = min(Z0 + L, cb.hi[2]);
+    const int64_t gx = X0 + lx, gy = Y0 + ly;
+    const bool active = gx < cb.hi[0] && gy < cb.hi[1];
+    const int64_t sy = nx, sz = nx * ny;
+    auto ld = [&](const T* A, int64_t x, int64_t y, int64_t z) -> T {
+        return (x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz) ? __ldg(A + x + sy * y + sz * z) : T(0);
+    };
+    T Tzm = active ? ld(Tin, gx, gy, Z0 - 1) : T(0), Tc = active ? ld(Tin, gx, gy, Z0) : T(0), Tzp;
+    T lzm = (HAS_LAM && active) ? ld(lam, gx, gy, Z0 - 1) : T(0), lc = (HAS_LAM && active) ? ld(lam, gx, gy, Z0) : T(0),
+      lzp = T(0);
+    for (int64_t z = Z0; z < Z1; ++z) {
+        __syncthreads();
+        for (int i = tid; i < PW * PH; i += 32 * TY) {
+            int hx = i % PW, hy = i / PW;
+            sT[hy][hx] = ld(Tin, X0 - 1 + hx, Y0 - 1 + hy, z);
+            if constexpr (HAS_LAM) sL[hy][hx] = ld(lam, X0 - 1 + hx, Y0 - 1 + hy, z);
+        }
+        __syncthreads();
+        Tzp = active ? ld(Tin, gx, gy, z + 1) : T(0);
+        if constexpr (HAS_LAM) lzp = active ? ld(lam, gx, gy, z + 1) : T(0);
+        if (active) {
+            const int sx = lx + 1, sy_ = ly + 1;
+            T r = diff_cell<T, FORM>(p, Tc, sT[sy_][sx - 1], sT[sy_][sx + 1], sT[sy_ - 1][sx], sT[sy_ + 1][sx], Tzm, Tzp,
+                                     __ldg(Ci + gx + sy * gy + sz * z), lc, HAS_LAM ? sL[sy_][sx - 1] : T(0),
+                                     HAS_LAM ? sL[sy_][sx + 1] : T(0), HAS_LAM ? sL[sy_ - 1][sx] : T(0),
+                                     HAS_LAM ? sL[sy_ + 1][sx] : T(0), lzm, lzp);
+            T2[gx + sy * gy + sz * z] = r;
+        }
+        Tzm = Tc;
+        Tc = Tzp;
+        lzm = lc;
+        lc = lzp;
+    }
+}
+
+// =======================================================================================
+// acoustic3D (miniapps/acoustic3D.jl:11-21)
+// =======================================================================================
+template <typename T>
+__global__ void acoustic_v_kernel(T* __restrict__ Vx, T* __restrict__ Vy, T* __restrict__ Vz, const T* __restrict__ P,
+                                  int64_t nx, int64_t ny, int64_t nz, T dtr, T dx, T dy, T dz) {
+    // grid = (nx+1, ny+1, nz+1); each statement masked by @inn of its left-hand array.
+    int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (tx > nx || ty > ny) return;
+    const int64_t sy = nx, sz = nx * ny;
+    for (int64_t tz = blockIdx.z; tz <= nz; tz += gridDim.z) {
+        if (tx < nx - 1 && ty < ny - 2 && tz < nz - 2) {  // @inn(Vx): Vx is (nx+1, ny, nz)
+            int64_t v = (tx + 1) + (nx + 1) * ((ty + 1) + ny * (tz + 1));
+            int64_t pc = (tx + 1) + sy * (ty + 1) + sz * (tz + 1);
+            Vx[v] = Vx[v] - (dtr * (P[pc] - P[pc - 1])) / dx;
+        }
+        if (tx < nx - 2 && ty < ny - 1 && tz < nz - 2) {  // @inn(Vy): Vy is (nx, ny+1, nz)
+            int64_t v = (tx + 1) + nx * ((ty + 1) + (ny + 1) * (tz + 1));
+            int64_t pc = (tx + 1) + sy * (ty + 1) + sz * (tz + 1);
+            Vy[v] = Vy[v] - (dtr * (P[pc] - P[pc - sy])) / dy;
+        }
+        if (tx < nx - 2 && ty < ny - 2 && tz < nz - 1) {  // @inn(Vz): Vz is (nx, ny, nz+1)
+            int64_t v = (tx + 1) + nx * ((ty + 1) + ny * (tz + 1));
+            int64_t pc = (tx + 1) + sy * (ty + 1) + sz * (tz + 1);
+            Vz[v] = Vz[v] - (dtr * (P[pc] - P[pc - sz])) / dz;
+        }
+    }
+}
+
+template <typename T>
+__global__ void acoustic_p_kernel(T* __restrict__ P, const T* __restrict__ Vx, const T* __restrict__ Vy,
+                                  const T* __restrict__ Vz, int64_t nx, int64_t ny, int64_t nz, T dtk, T dx, T dy,
+                                  T dz) {
+    int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (ix >= nx || iy >= ny) return;
+    for (int64_t iz = blockIdx.z; iz < nz; iz += gridDim.z) {
+        T ax = Vx[(ix + 1) + (nx + 1) * (iy + ny * iz)] - Vx[ix + (nx + 1) * (iy + ny * iz)];
+        T ay = Vy[ix + nx * ((iy + 1) + (ny + 1) * iz)] - Vy[ix + nx * (iy + (ny + 1) * iz)];
+        T az = Vz[ix + nx * (iy + ny * (iz + 1))] - Vz[ix + nx * (iy + ny * iz)];
+        int64_t pc = ix + nx * (iy + ny * iz);
+        P[pc] = P[pc] - dtk * ((ax / dx + ay / dy) + az / dz);
+    }
+}
+
+// =======================================================================================
+// Host launchers
+// =======================================================================================
+static dim3 grid3(int64_t wx, int64_t wy, int64_t wz, dim3 blk) {
+    return dim3((unsigned)((wx + blk.x - 1) / blk.x), (unsigned)((wy + blk.y - 1) / blk.y),
+                (unsigned)std::min<int64_t>(std::max<int64_t>(wz, 1), 65535));
+}
+
+template <typename T>
+static DiffParams<T> diff_params(double lam, double dt, double hx, double hy, double hz) {
+    return DiffParams<T>{(T)lam, (T)dt, (T)hx, (T)hy, (T)hz};
+}
+
+// Default z-sweep length (`loopsize`): the reference uses 64 on compute capability >= 9
+// (src/parallel.jl:532-543); the same default is kept.
+static constexpr int kDefaultLoopsize = 64;
+
+template <typename T, int FORM, int TY, int S>
+static int launch_zsweep_tma(const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                             const DiffParams<T>& p, const Box& cb, int L, cudaStream_t s, int* d_err) {
+    using Z = ZSweep<T, FORM, TY, S>;
+    CUtensorMap mT, mL, mC;
+    PS_TRY(encode_plane_map(&mT, Tin, Z::PW, Z::PH));
+    if (Z::HAS_LAM)
+        PS_TRY(encode_plane_map(&mL, *lam, Z::PW, Z::PH));
+    else
+        mL = mT;
+    PS_TRY(encode_plane_map(&mC, Ci, Z::TX, TY));
+    static bool attr_set = false;
+    if (!attr_set) {
+        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_zsweep_tma<T, FORM, TY, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Z::SMEM));
+        attr_set = true;
+    }
+    int64_t x0 = cb.lo[0] & ~(int64_t)(Z::VEC - 1);
+    dim3 blk(32, TY, 1);
+    dim3 grd((unsigned)((cb.hi[0] - x0 + Z::TX - 1) / Z::TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
+             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    diff3d_zsweep_tma<T, FORM, TY, S><<<grd, blk, Z::SMEM, s>>>(mT, mL, mC, static_cast<T*>(T2.ptr), p, T2.n[0],
+                                                                T2.n[1], cb, L, d_err);
+    return PS_OK;
+}
+
+template <typename T, int FORM>
+static int launch_diffusion(const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                            const DiffParams<T>& p, const Box& cb, int memopt, int loopsize, cudaStream_t s,
+                            int* d_err) {
+    const int64_t wx = cb.hi[0] - cb.lo[0], wy = cb.hi[1] - cb.lo[1], wz = cb.hi[2] - cb.lo[2];
+    if (wx <= 0 || wy <= 0 || wz <= 0) return PS_OK;
+    const T* lp = lam ? static_cast<const T*>(lam->ptr) : nullptr;
+    int L = loopsize > 0 ? loopsize : kDefaultLoopsize;
+    if (memopt) {
+        bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
+        if (tma) return launch_zsweep_tma<T, FORM, 8, 4>(T2, Tin, Ci, lam, p, cb, L, s, d_err);
+        dim3 blk(32, 4, 1);
+        dim3 grd((unsigned)((wx + 31) / 32), (unsigned)((wy + 3) / 4), (unsigned)((wz + L - 1) / L));
+        diff3d_zsweep_smem<T, FORM, 4><<<grd, blk, 0, s>>>(static_cast<T*>(T2.ptr), static_cast<const T*>(Tin.ptr),
+                                                            static_cast<const T*>(Ci.ptr), lp, p, T2.n[0], T2.n[1],
+                                                            T2.n[2], cb, L);
+        return PS_OK;
+    }
+    dim3 blk(32, 8, 1);
+    diff3d_plain<T, FORM><<<grid3(wx, wy, wz, blk), blk, 0, s>>>(static_cast<T*>(T2.ptr),
+                                                                 static_cast<const T*>(Tin.ptr),
+                                                                 static_cast<const T*>(Ci.ptr), lp, p, T2.n[0],
+                                                                 T2.n[1], cb);
+    return PS_OK;
+}
+
+template <typename T>
+static int dispatch_diffusion(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci,
+                              const ps_array* lam, double lam_s, double dt, double hx, double hy, double hz,
+                              const Box& cb, int memopt, int loopsize, cudaStream_t s, int* d_err) {
+    DiffParams<T> p = diff_params<T>(lam_s, dt, hx, hy, hz);
+    switch (form) {
+    case PS_DIFF_DIV: return launch_diffusion<T, PS_DIFF_DIV>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err);
+    case PS_DIFF_MUL: return launch_diffusion<T, PS_DIFF_MUL>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err);
+    case PS_DIFF_FLUX: return launch_diffusion<T, PS_DIFF_FLUX>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err);
+    case PS_DIFF_FLUX_LAM: return launch_diffusion<T, PS_DIFF_FLUX_LAM>(T2, Tin, Ci, lam, p, cb, memopt, loopsize, s, d_err);
+    }
+    return fail(PS_ERR_ARG, "ps_diffusion3d_step: unknown form %d", form);
+}
+
+// Validates the diffusion arguments and converts the thread box into the box of written
+// cells (`@inn(T2)` mask: c = t + 1 for 0 <= t < n - 2).
+static int diffusion_args(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci,
+                          const ps_array& lam) {
+    PS_TRY(check_array(T2, "T2"));
+    PS_TRY(check_array(Tin, "T"));
+    PS_TRY(check_array(Ci, "Ci"));
+    PS_TRY(check_same_dtype(T2, Tin, "T2", "T"));
+    PS_TRY(check_same_dtype(T2, Ci, "T2", "Ci"));
+    PS_TRY(check_shape(Tin, T2.n[0], T2.n[1], T2.n[2], "T"));
+    PS_TRY(check_shape(Ci, T2.n[0], T2.n[1], T2.n[2], "Ci"));
+    if (form < 0 || form > 3) return fail(PS_ERR_ARG, "diffusion: unknown form %d", form);
+    if (form == PS_DIFF_FLUX_LAM) {
+        PS_TRY(check_array(lam, "lam"));
+        PS_TRY(check_same_dtype(T2, lam, "T2", "lam"));
+        PS_TRY(check_shape(lam, T2.n[0], T2.n[1], T2.n[2], "lam"));
+    }
+    if (T2.ptr == Tin.ptr) return fail(PS_ERR_ARG, "diffusion: T2 and T must be distinct arrays");
+    return PS_OK;
+}
+
+static Box inner_cells(const Box& tb, const int64_t n[3]) {
+    Box cb;
+    for (int d = 0; d < 3; d++) {
+        int64_t lo = std::max<int64_t>(tb.lo[d], 0), hi = std::min<int64_t>(tb.hi[d], n[d] - 2);
+        cb.lo[d] = lo + 1;
+        cb.hi[d] = std::max(hi, lo) + 1;
+    }
+    return cb;
+}
+
+int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam,
+                  double lam_s, double dt, double hx, double hy, double hz, const Box& thread_box, int memopt,
+                  int loopsize, cudaStream_t s, int* d_err) {
+    Box cb = inner_cells(thread_box, T2.n);
+    const ps_array* lp = form == PS_DIFF_FLUX_LAM ? &lam : nullptr;
+    if (T2.dtype == PS_F64)
+        return dispatch_diffusion<double>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err);
+    return dispatch_diffusion<float>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err);
+}
+
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" {
+
+int ps_fill(ps_array a, double value, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_array(a, "A"));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int64_t n = numel(a);
+    unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)st->num_sms * 32);
+    if (a.dtype == PS_F64)
+        fill_kernel<double><<<g, 256, 0, s>>>(static_cast<double*>(a.ptr), n, value);
+    else
+        fill_kernel<float><<<g, 256, 0, s>>>(static_cast<float*>(a.ptr), n, (float)value);
+    return finish_launch(s, 1, "ps_fill");
+}
+
+int ps_fd_apply(ps_fd_op op, int32_t lhs_inn, ps_array R, ps_array A, void* stream, int sync) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_array(R, "R"));
+    PS_TRY(check_array(A, "A"));
+    PS_TRY(check_same_dtype(R, A, "R", "A"));
+    if (op.kind < PS_FD_SEL || op.kind > PS_FD_MINLOC) return fail(PS_ERR_ARG, "ps_fd_apply: unknown kind %d", op.kind);
+    if (op.ndims < 1 || op.ndims > 3) return fail(PS_ERR_ARG, "ps_fd_apply: ndims %d", op.ndims);
+    int dmask = (1 << op.ndims) - 1;
+    if ((op.opdims & ~dmask) || (op.inn & ~dmask) || (lhs_inn & ~dmask))
+        return fail(PS_ERR_ARG, "ps_fd_apply: dimension masks exceed ndims");
+    if ((op.kind == PS_FD_DIFF || op.kind == PS_FD_DIFF2) && __builtin_popcount(op.opdims) != 1)
+        return fail(PS_ERR_ARG, "ps_fd_apply: a difference acts along exactly one dimension");
+    if ((op.kind == PS_FD_AV || op.kind == PS_FD_HARM) && op.opdims == 0)
+        return fail(PS_ERR_ARG, "ps_fd_apply: an average needs at least one dimension");
+    for (int d = op.ndims; d < 3; d++)
+        if (R.n[d] != 1 || A.n[d] != 1) return fail(PS_ERR_SHAPE, "ps_fd_apply: array has more dimensions than ndims");
+    FdDesc d;
+    d.kind = op.kind;
+    d.opdims = op.opdims;
+    d.inn = op.inn;
+    d.ndims = op.ndims;
+    d.lhs_inn = lhs_inn;
+    for (int k = 0; k < 3; k++) {
+        d.nR[k] = R.n[k];
+        d.nA[k] = A.n[k];
+        d.tmax[k] = R.n[k] - 2 * ((lhs_inn >> k) & 1);
+        int rlo = 0, rhi = 0;
+        if (op.kind == PS_FD_DIFF || op.kind == PS_FD_AV || op.kind == PS_FD_HARM) rhi = (op.opdims >> k) & 1;
+        if (op.kind == PS_FD_DIFF2 || op.kind == PS_FD_MAXLOC || op.kind == PS_FD_MINLOC)
+            rlo = rhi = (op.opdims >> k) & 1;
+        int64_t lo = ((op.inn >> k) & 1) - rlo, hi = ((op.inn >> k) & 1) + rhi;
+        if (d.tmax[k] > 0 && (lo < 0 || d.tmax[k] - 1 + hi > A.n[k] - 1))
+            return fail(PS_ERR_SHAPE, "ps_fd_apply: the operator reads outside A along dimension %d", k);
+    }
+    if (d.tmax[0] <= 0 || d.tmax[1] <= 0 || d.tmax[2] <= 0) return PS_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dim3 blk(32, 8, 1);
+    dim3 grd = grid3(d.tmax[0], d.tmax[1], d.tmax[2], blk);
+    if (R.dtype == PS_F64)
+        fd_apply_kernel<double><<<grd, blk, 0, s>>>(static_cast<double*>(R.ptr), static_cast<const double*>(A.ptr), d);
+    else
+        fd_apply_kernel<float><<<grd, blk, 0, s>>>(static_cast<float*>(R.ptr), static_cast<const float*>(A.ptr), d);
+    return finish_launch(s, sync, "ps_fd_apply");
+}
+
+int ps_memcopy3d(ps_array T2, ps_array T, ps_array Ci, const ps_launch* cfg, void* stream, int sync) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_array(T2, "T2"));
+    PS_TRY(check_array(T, "T"));
+    PS_TRY(check_array(Ci, "Ci"));
+    PS_TRY(check_same_dtype(T2, T, "T2", "T"));
+    PS_TRY(check_same_dtype(T2, Ci, "T2", "Ci"));
+    PS_TRY(check_shape(T, T2.n[0], T2.n[1], T2.n[2], "T"));
+    PS_TRY(check_shape(Ci, T2.n[0], T2.n[1], T2.n[2], "Ci"));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Box b = launch_box(cfg, T2.n);
+    bool full = b.lo[0] == 0 && b.lo[1] == 0 && b.lo[2] == 0 && b.hi[0] == T2.n[0] && b.hi[1] == T2.n[1] &&
+                b.hi[2] == T2.n[2];
+    bool aligned = (reinterpret_cast<uintptr_t>(T2.ptr) | reinterpret_cast<uintptr_t>(T.ptr) |
+                    reinterpret_cast<uintptr_t>(Ci.ptr)) % 16 == 0;
+    int64_t n = numel(T2);
+    if (full && aligned) {
+        int64_t vn = n / (T2.dtype == PS_F64 ? 2 : 4);
+        unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((vn + 1023) / 1024, (int64_t)st->num_sms * 16));
+        if (T2.dtype == PS_F64)
+            memcopy_flat<double><<<g, 256, 0, s>>>(static_cast<double*>(T2.ptr), static_cast<const double*>(T.ptr),
+                                                   static_cast<const double*>(Ci.ptr), n);
+        else
+            memcopy_flat<float><<<g, 256, 0, s>>>(static_cast<float*>(T2.ptr), static_cast<const float*>(T.ptr),
+                                                  static_cast<const float*>(Ci.ptr), n);
+    } else {
+        int64_t wx = b.hi[0] - b.lo[0], wy = b.hi[1] - b.lo[1], wz = b.hi[2] - b.lo[2];
+        if (wx > 0 && wy > 0 && wz > 0) {
+            dim3 blk(32, 8, 1);
+            if (T2.dtype == PS_F64)
+                memcopy_box<double><<<grid3(wx, wy, wz, blk), blk, 0, s>>>(
+                    static_cast<double*>(T2.ptr), static_cast<const double*>(T.ptr),
+                    static_cast<const double*>(Ci.ptr), T2.n[0], T2.n[1], b);
+            else
+                memcopy_box<float><<<grid3(wx, wy, wz, blk), blk, 0, s>>>(
+                    static_cast<float*>(T2.ptr), static_cast<const float*>(T.ptr), static_cast<const float*>(Ci.ptr),
+                    T2.n[0], T2.n[1], b);
+        }
+    }
+    return finish_launch(s, sync, "ps_memcopy3d");
+}
+
+int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr, double lam, double dt,
+                        double hx, double hy, double hz, const ps_launch* cfg, void* stream, int sync) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(diffusion_args(form, T2, T, Ci, lam_arr));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Box tb = launch_box(cfg, T2.n);
+    int memopt = cfg ? cfg->memopt : 0;
+    int loopsize = cfg ? cfg->loopsize : 0;
+    if (loopsize < 0) return fail(PS_ERR_ARG, "ps_diffusion3d_step: loopsize must be >= 0");
+    PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, tb, memopt, loopsize, s, st->d_err));
+    return finish_launch(s, sync, "ps_diffusion3d_step");
+}
+
+int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr, double lam,
+                              double dt, double hx, double hy, double hz, int32_t memopt, const int64_t bw[3],
+                              void* s_boundary, void* s_inner, ps_comm_fn comm, void* comm_ctx) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(diffusion_args(form, T2, T, Ci, lam_arr));
+    if (!bw) return fail(PS_ERR_NULL, "ps_diffusion3d_step_split: NULL boundary width");
+    const int64_t* ms = T2.n;  // the kernel's `@parallel` grid: all arguments are n^3
+    // validate_ranges_args (src/ParallelKernel/hide_communication.jl:396-403)
+    bool any_gt1 = false;
+    for (int d = 0; d < 3; d++) {
+        if (bw[d] < 0) return fail(PS_ERR_ARG, "boundary width must be >= 0");
+        if (!(ms[d] > 2 * bw[d])) return fail(PS_ERR_SHAPE, "@hide_communication: length(ranges) > 2*boundary_width violated");
+        if (ms[d] > 1 && bw[d] == 0) return fail(PS_ERR_SHAPE, "@hide_communication: boundary_width 0 in a dimension of length > 1");
+        any_gt1 |= ms[d] > 1;
+    }
+    if (!any_gt1) return fail(PS_ERR_SHAPE, "@hide_communication: all ranges have length 1");
+    cudaStream_t sb = static_cast<cudaStream_t>(s_boundary), si = static_cast<cudaStream_t>(s_inner);
+    // get_ranges_outer / get_ranges_inner (src/ParallelKernel/hide_communication.jl:350-394), 3-D case,
+    // converted to 0-based half-open boxes.
+    Box outer[6] = {
+        {{0, bw[1], bw[2]}, {bw[0], ms[1] - bw[1], ms[2] - bw[2]}},
+        {{0, 0, 0}, {ms[0], ms[1], bw[2]}},
+        {{0, 0, ms[2] - bw[2]}, {ms[0], ms[1], ms[2]}},
+        {{ms[0] - bw[0], bw[1], bw[2]}, {ms[0], ms[1] - bw[1], ms[2] - bw[2]}},
+        {{0, 0, bw[2]}, {ms[0], bw[1], ms[2] - bw[2]}},
+        {{0, ms[1] - bw[1], bw[2]}, {ms[0], ms[1], ms[2] - bw[2]}},
+    };
+    Box inner = {{bw[0], bw[1], bw[2]}, {ms[0] - bw[0], ms[1] - bw[1], ms[2] - bw[2]}};
+    for (int i = 0; i < 6; i++) {
+        bool empty = false;
+        for (int d = 0; d < 3; d++) empty |= outer[i].hi[d] <= outer[i].lo[d];
+        if (empty) continue;
+        PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, outer[i], memopt, 0, sb, st->d_err));
+    }
+    PS_TRY(finish_launch(sb, 0, "ps_diffusion3d_step_split(boundary)"));
+    PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, inner, memopt, 0, si, st->d_err));
+    PS_TRY(finish_launch(si, 0, "ps_diffusion3d_step_split(inner)"));
+    PS_TRY(finish_launch(sb, 1, "ps_diffusion3d_step_split(boundary sync)"));
+    int crc = PS_OK;
+    if (comm) crc = comm(comm_ctx);
+    PS_TRY(finish_launch(si, 1, "ps_diffusion3d_step_split(inner sync)"));
+    if (crc != PS_OK) return fail(crc, "ps_diffusion3d_step_split: communication callback returned %d", crc);
+    return PS_OK;
+}
+
+int ps_acoustic3d_v(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P, double dt, double rho, double dx, double dy,
+                    double dz, void* stream, int sync) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_array(P, "P"));
+    PS_TRY(check_array(Vx, "Vx"));
+    PS_TRY(check_array(Vy, "Vy"));
+    PS_TRY(check_array(Vz, "Vz"));
+    PS_TRY(check_same_dtype(P, Vx, "P", "Vx"));
+    PS_TRY(check_same_dtype(P, Vy, "P", "Vy"));
+    PS_TRY(check_same_dtype(P, Vz, "P", "Vz"));
+    int64_t nx = P.n[0], ny = P.n[1], nz = P.n[2];
+    PS_TRY(check_shape(Vx, nx + 1, ny, nz, "Vx"));
+    PS_TRY(check_shape(Vy, nx, ny + 1, nz, "Vy"));
+    PS_TRY(check_shape(Vz, nx, ny, nz + 1, "Vz"));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dim3 blk(32, 8, 1);
+    dim3 grd = grid3(nx + 1, ny + 1, nz + 1, blk);
+    if (P.dtype == PS_F64)
+        acoustic_v_kernel<double><<<grd, blk, 0, s>>>(static_cast<double*>(Vx.ptr), static_cast<double*>(Vy.ptr),
+                                                      static_cast<double*>(Vz.ptr), static_cast<const double*>(P.ptr),
+                                                      nx, ny, nz, dt / rho, dx, dy, dz);
+    else
+        acoustic_v_kernel<float><<<grd, blk, 0, s>>>(static_cast<float*>(Vx.ptr), static_cast<float*>(Vy.ptr),
+                                                     static_cast<float*>(Vz.ptr), static_cast<const float*>(P.ptr), nx,
+                                                     ny, nz, (float)dt / (float)rho, (float)dx, (float)dy, (float)dz);
+    return finish_launch(s, sync, "ps_acoustic3d_v");
+}
+
+int ps_acoustic3d_p(ps_array P, ps_array Vx, ps_array Vy, ps_array Vz, double dt, double k, double dx, double dy,
+                    double dz, void* stream, int sync) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_array(P, "P"));
+    PS_TRY(check_array(Vx, "Vx"));
+    PS_TRY(check_array(Vy, "Vy"));
+    PS_TRY(check_array(Vz, "Vz"));
+    PS_TRY(check_same_dtype(P, Vx, "P", "Vx"));
+    PS_TRY(check_same_dtype(P, Vy, "P", "Vy"));
+    PS_TRY(check_same_dtype(P, Vz, "P", "Vz"));
+    int64_t nx = P.n[0], ny = P.n[1], nz = P.n[2];
+    PS_TRY(check_shape(Vx, nx + 1, ny, nz, "Vx"));
+    PS_TRY(check_shape(Vy, nx, ny + 1, nz, "Vy"));
+    PS_TRY(check_shape(Vz, nx, ny, nz + 1, "Vz"));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dim3 blk(32, 8, 1);
+    dim3 grd = grid3(nx, ny, nz, blk);
+    if (P.dtype == PS_F64)
+        acoustic_p_kernel<double><<<grd, blk, 0, s>>>(static_cast<double*>(P.ptr), static_cast<const double*>(Vx.ptr),
+                                                      static_cast<const double*>(Vy.ptr),
+                                                      static_cast<const double*>(Vz.ptr), nx, ny, nz, dt * k, dx, dy, dz);
+    else
+        acoustic_p_kernel<float><<<grd, blk, 0, s>>>(static_cast<float*>(P.ptr), static_cast<const float*>(Vx.ptr),
+                                                     static_cast<const float*>(Vy.ptr), static_cast<const float*>(Vz.ptr),
+                                                     nx, ny, nz, (float)dt * (float)k, (float)dx, (float)dy, (float)dz);
+    return finish_launch(s, sync, "ps_acoustic3d_p");
+}
+
+}  // extern "C"

@@ -1,0 +1,253 @@
+"""The recognised `@parallel` kernels and the `parallel` / `hide_communication` launchers.
+
+``parallel(kernel, *args, memopt=..., ranges=..., stream=..., sync=True)`` mirrors
+``@parallel [ranges] [memopt=...] [stream=...] kernel!(args...)``
+(src/parallel.jl:216-276 -> src/ParallelKernel/parallel.jl:303-334): it launches the
+libps_b200.so kernel for `kernel` on the device arrays in `args` and, unless ``sync=False``
+(``@parallel_async``), synchronises the stream.
+
+Recognised kernels (each is one statement body of the reference, matched by ``from_source``):
+  copy3D                   examples/memcopy3D.jl:10-13
+  diffusion3D_step         examples/diffusion3D_novis_noperf.jl:10-13           (…/dx^2 form)
+  diffusion3D_step_inv     examples/diffusion3D_multigpucpu_hidecomm_novis.jl:12-15 (…*_dx^2)
+  diffusion3D_step_flux    test/test_parallel.jl:420-426 (on-the-fly flux form, scalar lam)
+  diffusion3D_step_flux_lam  the flux form with a conductivity array (@av_xi(lam) faces)
+  acoustic3D_compute_V / _P  miniapps/acoustic3D.jl:11-21
+  fd_kernel("@<sel>(R) = @<macro>(A)")  every FiniteDifferences macro (ps_fd_apply)
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+from dataclasses import dataclass
+
+from . import _lib
+from ._lib import PSLaunch
+from .core import ArgumentError, default_memopt, descriptor, require_initialized, stream_handle
+from .fd import FdKernel, fd_kernel
+
+PS_DIFF_DIV, PS_DIFF_MUL, PS_DIFF_FLUX, PS_DIFF_FLUX_LAM = 0, 1, 2, 3
+
+
+def _launch_cfg(memopt: bool, loopsize: int, ranges):
+    cfg = PSLaunch()
+    cfg.memopt = int(bool(memopt))
+    cfg.loopsize = int(loopsize or 0)
+    if ranges is not None:
+        lo, hi = ranges_to_box(ranges)
+        for d in range(3):
+            cfg.range_lo[d], cfg.range_hi[d] = lo[d], hi[d]
+    return cfg
+
+
+def ranges_to_box(ranges):
+    """Julia `ranges` (1-based inclusive UnitRanges as (start, stop) pairs, or python ranges
+    over 0-based indices) -> 0-based half-open (lo, hi) boxes."""
+    lo, hi = [0, 0, 0], [1, 1, 1]
+    if len(ranges) > 3:
+        raise ArgumentError("ranges must have at most 3 dimensions")
+    for d, r in enumerate(ranges):
+        if isinstance(r, range):
+            if r.step != 1:
+                raise ArgumentError("ranges must have step 1")
+            lo[d], hi[d] = r.start, r.stop
+        else:
+            start, stop = r
+            lo[d], hi[d] = int(start) - 1, int(stop)
+    return lo, hi
+
+
+@dataclass(frozen=True)
+class Kernel:
+    name: str
+    nargs: int
+
+    def launch(self, args, memopt, loopsize, ranges, stream, sync):  # pragma: no cover - abstract
+        raise NotImplementedError
+
+
+@dataclass(frozen=True)
+class Copy3D(Kernel):
+    def launch(self, args, memopt, loopsize, ranges, stream, sync):
+        T2, T, Ci = args
+        cfg = _launch_cfg(memopt, loopsize, ranges)
+        _lib.call("ps_memcopy3d", descriptor(T2), descriptor(T), descriptor(Ci), ctypes.byref(cfg),
+                  stream_handle(stream), int(bool(sync)))
+
+
+@dataclass(frozen=True)
+class Diffusion3D(Kernel):
+    form: int
+
+    def split_args(self, args):
+        T2, T, Ci, lam, dt, hx, hy, hz = args
+        if self.form == PS_DIFF_FLUX_LAM:
+            return T2, T, Ci, lam, 0.0, dt, hx, hy, hz
+        return T2, T, Ci, None, lam, dt, hx, hy, hz
+
+    def launch(self, args, memopt, loopsize, ranges, stream, sync):
+        T2, T, Ci, lam_arr, lam, dt, hx, hy, hz = self.split_args(args)
+        cfg = _launch_cfg(memopt, loopsize, ranges)
+        _lib.call("ps_diffusion3d_step", self.form, descriptor(T2), descriptor(T), descriptor(Ci),
+                  descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), ctypes.byref(cfg),
+                  stream_handle(stream), int(bool(sync)))
+
+
+@dataclass(frozen=True)
+class Acoustic3D(Kernel):
+    which: str
+
+    def launch(self, args, memopt, loopsize, ranges, stream, sync):
+        if ranges is not None:
+            raise ArgumentError(f"{self.name}: explicit ranges are not supported")
+        if self.which == "V":
+            Vx, Vy, Vz, P, dt, rho, dx, dy, dz = args
+            _lib.call("ps_acoustic3d_v", descriptor(Vx), descriptor(Vy), descriptor(Vz), descriptor(P), float(dt),
+                      float(rho), float(dx), float(dy), float(dz), stream_handle(stream), int(bool(sync)))
+        else:
+            P, Vx, Vy, Vz, dt, k, dx, dy, dz = args
+            _lib.call("ps_acoustic3d_p", descriptor(P), descriptor(Vx), descriptor(Vy), descriptor(Vz), float(dt),
+                      float(k), float(dx), float(dy), float(dz), stream_handle(stream), int(bool(sync)))
+
+
+copy3D = Copy3D("copy3D!", 3)
+diffusion3D_step = Diffusion3D("diffusion3D_step!", 8, PS_DIFF_DIV)
+diffusion3D_step_inv = Diffusion3D("diffusion3D_step!", 8, PS_DIFF_MUL)
+diffusion3D_step_flux = Diffusion3D("diffusion3D_step!", 8, PS_DIFF_FLUX)
+diffusion3D_step_flux_lam = Diffusion3D("diffusion3D_step!", 8, PS_DIFF_FLUX_LAM)
+acoustic3D_compute_V = Acoustic3D("compute_V!", 9, "V")
+acoustic3D_compute_P = Acoustic3D("compute_P!", 9, "P")
+
+# Kernel bodies as written in the reference (whitespace-insensitive) -> kernel.
+_SOURCES = {
+    "@all(T2) = @all(T) + @all(Ci)": copy3D,
+    "@inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)/dx^2 + @d2_yi(T)/dy^2 + @d2_zi(T)/dz^2))": diffusion3D_step,
+    "@inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)*_dx^2 + @d2_yi(T)*_dy^2 + @d2_zi(T)*_dz^2))":
+        diffusion3D_step_inv,
+    ("@all(qx) = -lam*@d_xi(T)*_dx; @all(qy) = -lam*@d_yi(T)*_dy; @all(qz) = -lam*@d_zi(T)*_dz; "
+     "@all(dTdt) = @inn(Ci)*(-@d_xa(qx)*_dx - @d_ya(qy)*_dy - @d_za(qz)*_dz); "
+     "@inn(T2) = @inn(T) + dt*@all(dTdt)"): diffusion3D_step_flux,
+    ("@all(qx) = -@av_xi(lam)*@d_xi(T)*_dx; @all(qy) = -@av_yi(lam)*@d_yi(T)*_dy; "
+     "@all(qz) = -@av_zi(lam)*@d_zi(T)*_dz; "
+     "@all(dTdt) = @inn(Ci)*(-@d_xa(qx)*_dx - @d_ya(qy)*_dy - @d_za(qz)*_dz); "
+     "@inn(T2) = @inn(T) + dt*@all(dTdt)"): diffusion3D_step_flux_lam,
+    ("@inn(Vx) = @inn(Vx) - dt/ρ*@d_xi(P)/dx; @inn(Vy) = @inn(Vy) - dt/ρ*@d_yi(P)/dy; "
+     "@inn(Vz) = @inn(Vz) - dt/ρ*@d_zi(P)/dz"): acoustic3D_compute_V,
+    "@all(P) = @all(P) - dt*k*(@d_xa(Vx)/dx + @d_ya(Vy)/dy + @d_za(Vz)/dz)": acoustic3D_compute_P,
+}
+
+
+def _normalise(src: str) -> str:
+    src = re.sub(r"#[^\n]*", "", src)
+    parts = [re.sub(r"\s+", "", p) for p in re.split(r"[;\n]", src)]
+    return ";".join(p for p in parts if p and p != "return")
+
+
+_NORMALISED = {_normalise(k): v for k, v in _SOURCES.items()}
+
+
+def from_source(body: str, ndims: int = 3):
+    """Recognise a `@parallel` kernel body (statements separated by ';' or newlines).
+
+    This is the pattern matching the `:GB300` package performs on kernel ASTs: known
+    bodies map to their libps_b200.so kernel; one-statement FD bodies map to ps_fd_apply.
+    Anything else raises ArgumentError (there is no generic code generator and no fallback).
+    """
+    key = _normalise(body)
+    if key in _NORMALISED:
+        return _NORMALISED[key]
+    if ";" not in key:
+        return fd_kernel(body.strip().rstrip(";"), ndims)
+    raise ArgumentError("unsupported @parallel kernel body for the GB300 package")
+
+
+def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True):
+    """`@parallel [ranges] [memopt=...] kernel!(args...)`."""
+    require_initialized()
+    if isinstance(kernel, FdKernel):
+        if ranges is not None or memopt:
+            raise ArgumentError("FD operator kernels take no ranges/memopt")
+        R, A = args
+        kernel.launch(R, A, stream=stream, sync=sync)
+        return
+    if not isinstance(kernel, Kernel):
+        raise ArgumentError(f"not a GB300 kernel: {kernel!r}")
+    if len(args) != kernel.nargs:
+        raise ArgumentError(f"{kernel.name} takes {kernel.nargs} arguments (obtained {len(args)})")
+    if memopt is None:
+        memopt = default_memopt()
+    kernel.launch(args, memopt, loopsize, ranges, stream, sync)
+
+
+def parallel_async(kernel, *args, **kw):
+    """`@parallel_async kernel!(args...)`: no synchronisation."""
+    kw["sync"] = False
+    parallel(kernel, *args, **kw)
+
+
+def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, s_boundary=None, s_inner=None):
+    """`@hide_communication boundary_width begin @parallel kernel!(args...); comm() end`.
+
+    The six boundary slabs run on a high-priority stream and the inner box on a normal
+    stream (src/ParallelKernel/hide_communication.jl:177-258); `comm` runs on the host once
+    the boundary slabs are done. Only the diffusion kernels are split.
+    """
+    require_initialized()
+    if not isinstance(kernel, Diffusion3D):
+        raise ArgumentError("@hide_communication is implemented for the diffusion3D kernels")
+    bw = boundary_width if isinstance(boundary_width, (tuple, list)) else (boundary_width,) * 3
+    if len(bw) != 3:
+        raise ArgumentError("boundary_width must be an integer or a 3-tuple")
+    T2, T, Ci, lam_arr, lam, dt, hx, hy, hz = kernel.split_args(args)
+    memopt = default_memopt() if memopt is None else memopt
+    own = []
+    if s_boundary is None:
+        s_boundary = ctypes.c_void_p()
+        _lib.call("ps_stream_create", 1, ctypes.byref(s_boundary))
+        own.append(s_boundary)
+    if s_inner is None:
+        s_inner = ctypes.c_void_p()
+        _lib.call("ps_stream_create", 0, ctypes.byref(s_inner))
+        own.append(s_inner)
+    errors = []
+
+    def _cb(_ctx):
+        try:
+            if comm is not None:
+                comm()
+            return 0
+        except Exception as e:  # noqa: BLE001 - reported after the call
+            errors.append(e)
+            return -1
+
+    cb = _lib.COMM_FN(_cb)
+    bw_arr = (ctypes.c_int64 * 3)(*[int(b) for b in bw])
+    try:
+        _lib.call("ps_diffusion3d_step_split", kernel.form, descriptor(T2), descriptor(T), descriptor(Ci),
+                  descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), int(bool(memopt)),
+                  bw_arr, s_boundary, s_inner, cb, None)
+    finally:
+        for s in own:
+            _lib.call("ps_stream_destroy", s)
+    if errors:
+        raise errors[0]
+
+
+def get_ranges_outer(boundary_width, maxsize):
+    """The six boundary boxes of `@hide_communication` (3-D), 0-based half-open
+    (src/ParallelKernel/hide_communication.jl:350-381)."""
+    bw, ms = boundary_width, maxsize
+    boxes = [
+        ((0, bw[1], bw[2]), (bw[0], ms[1] - bw[1], ms[2] - bw[2])),
+        ((0, 0, 0), (ms[0], ms[1], bw[2])),
+        ((0, 0, ms[2] - bw[2]), (ms[0], ms[1], ms[2])),
+        ((ms[0] - bw[0], bw[1], bw[2]), (ms[0], ms[1] - bw[1], ms[2] - bw[2])),
+        ((0, 0, bw[2]), (ms[0], bw[1], ms[2] - bw[2])),
+        ((0, ms[1] - bw[1], bw[2]), (ms[0], ms[1], ms[2] - bw[2])),
+    ]
+    return [b for b in boxes if all(h > l for l, h in zip(*b))]
+
+
+def get_ranges_inner(boundary_width, maxsize):
+    bw, ms = boundary_width, maxsize
+    return [((bw[0], bw[1], bw[2]), (ms[0] - bw[0], ms[1] - bw[1], ms[2] - bw[2]))]
