@@ -195,6 +195,64 @@ int ps_acoustic3d_v(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
 int ps_acoustic3d_p(ps_array P, ps_array Vx, ps_array Vy, ps_array Vz,
                     double dt, double k, double dx, double dy, double dz, void* stream, int sync);
 
+/* ------------------------------------------------------------------------------------ */
+/* Stokes2D pseudo-transient solver (miniapps/Stokes2D.jl).                              */
+/* ------------------------------------------------------------------------------------ */
+
+/* The arrays of the miniapp (Stokes2D.jl:79-101), nx = size(Pt,1), ny = size(Pt,2):
+ * Pt, dtauPt, divV (∇V), txx, tyy, Mus, Rog: (nx, ny); Vx: (nx+1, ny); Vy: (nx, ny+1);
+ * txy: (nx-1, ny-1); Rx, dVxdtau, dtauVx: (nx-1, ny-2); Ry, dVydtau, dtauVy: (nx-2, ny-1).
+ * All 2-D (n[2] = 1), one dtype. */
+typedef struct ps_stokes2d_fields {
+    ps_array Pt, dtauPt, divV, Vx, Vy, txx, tyy, txy, Rx, Ry, dVxdtau, dVydtau, dtauVx, dtauVy, Mus, Rog;
+} ps_stokes2d_fields;
+
+/* Scalars of the kernels (Stokes2D.jl:73-77): dx, dy, dampX = 1-Vdmp/nx, dampY = 1-Vdmp/ny,
+ * Vsc, Ptsc, min_dxy2 = min(dx,dy)^2, max_nxy = max(nx,ny). */
+typedef struct ps_stokes2d_params {
+    double dx, dy, dampX, dampY, Vsc, Ptsc, min_dxy2;
+    int64_t max_nxy;
+} ps_stokes2d_params;
+
+typedef struct ps_solve_stats {
+    int64_t iters;     /* pseudo-transient iterations executed (all precisions)          */
+    int64_t outer;     /* defect-correction outer iterations (1 for the plain FP64 solve) */
+    double err;        /* final max(mean|Rx|, mean|Ry|, mean|∇V|), evaluated in FP64      */
+    double seconds;    /* wall time of the solve                                          */
+    int32_t converged; /* err < tol                                                       */
+    int32_t reserved;
+} ps_solve_stats;
+
+/* The six `@parallel` calls of the PT loop, one-to-one (Stokes2D.jl:11-55). */
+int ps_stokes2d_timesteps(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, void* stream, int sync);
+int ps_stokes2d_compute_P(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, void* stream, int sync);
+int ps_stokes2d_compute_tau(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, void* stream, int sync);
+int ps_stokes2d_compute_dV(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, void* stream, int sync);
+int ps_stokes2d_compute_V(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, void* stream, int sync);
+/* `bc_x!(A)`: A[1,:] = A[2,:], A[end,:] = A[end-1,:]; `bc_y!(A)` the same along y (2-D). */
+int ps_bc_x2d(ps_array A, void* stream, int sync);
+int ps_bc_y2d(ps_array A, void* stream, int sync);
+
+/* n_iter iterations of the PT loop body (compute_P!, compute_τ!, compute_dV!, compute_V!,
+ * bc_y!(Vx), bc_x!(Vy); Stokes2D.jl:111-116) with one fused kernel per iteration. Every array,
+ * temporaries included, ends bit-identical to the six-call sequence. Synchronises. */
+int ps_stokes2d_iterate(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int64_t n_iter, void* stream);
+
+/* mean(abs.(Rx)), mean(abs.(Ry)), mean(abs.(∇V)) of the stored arrays (Stokes2D.jl:119). */
+int ps_stokes2d_err(const ps_stokes2d_fields* f, double out_mean_abs[3], void* stream);
+
+/* PT solve from the current state until err = max(mean|Rx|, mean|Ry|, mean|∇V|) < tol
+ * (the miniapp's `while err > ε` loop, checked every `nout` iterations; nout even).
+ *   mode 0: FP64 PT iterations.
+ *   mode 1: FP32 PT iterations on the correction (δP, δV) driven by the FP64 residual of the
+ *           state (defect correction); the residual, the state update and the convergence check
+ *           are FP64.
+ * The state arrays must be FP64. dtau arrays are recomputed from Mus with the compute_timesteps!
+ * formulas. Returns PS_ERR_NOT_CONVERGED at max_iter, PS_ERR_TIMEOUT after max_seconds (> 0),
+ * PS_ERR_NONFINITE on NaN/Inf residuals. Only Pt, Vx, Vy, dVxdtau, dVydtau are updated. */
+int ps_stokes2d_solve(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int32_t mode, double tol,
+                      int64_t max_iter, int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,6 +117,60 @@ def acoustic3d_v(Vx, Vy, Vz, P, dt, rho, dx, dy, dz) -> None:
                                             R(dy), R(dz)), "acoustic3d_v")
 
 
+class Stokes2D:
+    """The Stokes2D miniapp's arrays on the host and its kernels (miniapps/Stokes2D.jl:11-55)
+    run by the oracle; same field names as ps_gb300.stokes.Stokes2D."""
+
+    def __init__(self, nx, ny, dx, dy, Mus, Rog, Vdmp=4.0, Vsc=1.0, Ptsc=0.25, dtype=np.float64):
+        z = lambda *s: np.asfortranarray(np.zeros(s, dtype=dtype))  # noqa: E731
+        self.nx, self.ny, self.dtype = nx, ny, np.dtype(dtype)
+        self.a = {"Pt": z(nx, ny), "dtauPt": z(nx, ny), "divV": z(nx, ny), "Vx": z(nx + 1, ny), "Vy": z(nx, ny + 1),
+                  "txx": z(nx, ny), "tyy": z(nx, ny), "txy": z(nx - 1, ny - 1), "Rx": z(nx - 1, ny - 2),
+                  "Ry": z(nx - 2, ny - 1), "dVxdtau": z(nx - 1, ny - 2), "dVydtau": z(nx - 2, ny - 1),
+                  "dtauVx": z(nx - 1, ny - 2), "dtauVy": z(nx - 2, ny - 1),
+                  "Mus": np.asfortranarray(Mus.astype(dtype)), "Rog": np.asfortranarray(Rog.astype(dtype))}
+        self.dx, self.dy = dx, dy
+        self.dampX, self.dampY = 1.0 - Vdmp / nx, 1.0 - Vdmp / ny
+        self.Vsc, self.Ptsc = Vsc, Ptsc
+        self.min_dxy2, self.max_nxy = min(dx, dy) ** 2, max(nx, ny)
+
+    def _f(self, name):
+        return _fn(name, self.dtype)
+
+    def __getitem__(self, k):
+        return self.a[k]
+
+    def compute_timesteps(self):
+        R, a = _real(self.dtype), self.a
+        _check(self._f("orc_stokes2d_timesteps")(_ptr(a["dtauVx"]), _ptr(a["dtauVy"]), _ptr(a["dtauPt"]),
+                                                 _ptr(a["Mus"]), ctypes.c_int64(self.nx), ctypes.c_int64(self.ny),
+                                                 R(self.Vsc), R(self.Ptsc), R(self.min_dxy2),
+                                                 ctypes.c_int64(self.max_nxy)), "stokes2d_timesteps")
+
+    def step(self):
+        """compute_P!, compute_τ!, compute_dV!, compute_V!, bc_y!(Vx), bc_x!(Vy) (Stokes2D.jl:111-116)."""
+        R, a, i64 = _real(self.dtype), self.a, ctypes.c_int64
+        nx, ny = i64(self.nx), i64(self.ny)
+        _check(self._f("orc_stokes2d_P")(_ptr(a["divV"]), _ptr(a["Pt"]), _ptr(a["Vx"]), _ptr(a["Vy"]),
+                                         _ptr(a["dtauPt"]), nx, ny, R(self.dx), R(self.dy)), "P")
+        _check(self._f("orc_stokes2d_tau")(_ptr(a["divV"]), _ptr(a["txx"]), _ptr(a["tyy"]), _ptr(a["txy"]),
+                                           _ptr(a["Vx"]), _ptr(a["Vy"]), _ptr(a["Mus"]), nx, ny, R(self.dx),
+                                           R(self.dy)), "tau")
+        _check(self._f("orc_stokes2d_dV")(_ptr(a["Rx"]), _ptr(a["Ry"]), _ptr(a["dVxdtau"]), _ptr(a["dVydtau"]),
+                                          _ptr(a["Pt"]), _ptr(a["Rog"]), _ptr(a["txx"]), _ptr(a["tyy"]),
+                                          _ptr(a["txy"]), nx, ny, R(self.dampX), R(self.dampY), R(self.dx),
+                                          R(self.dy)), "dV")
+        _check(self._f("orc_stokes2d_V")(_ptr(a["Vx"]), _ptr(a["Vy"]), _ptr(a["dVxdtau"]), _ptr(a["dVydtau"]),
+                                         _ptr(a["dtauVx"]), _ptr(a["dtauVy"]), nx, ny), "V")
+        _check(self._f("orc_bc_y2d")(_ptr(a["Vx"]), i64(self.nx + 1), ny), "bc_y")
+        _check(self._f("orc_bc_x2d")(_ptr(a["Vy"]), nx, i64(self.ny + 1)), "bc_x")
+
+    def err(self):
+        """max(mean|Rx|, mean|Ry|, mean|∇V|) (Stokes2D.jl:119-120)."""
+        m = [float(np.mean(np.abs(self.a[k]))) for k in ("Rx", "Ry", "divV")]
+        return max(m), tuple(m)
+
+
 def acoustic3d_p(P, Vx, Vy, Vz, dt, k, dx, dy, dz) -> None:
     R = _real(P.dtype)
     _check(_fn("orc_acoustic3d_p", P.dtype)(_ptr(P), _ptr(Vx), _ptr(Vy), _ptr(Vz), _n3(P), R(dt), R(k), R(dx),

@@ -225,4 +225,131 @@ int SFX(orc_acoustic3d_p)(REAL* P, const REAL* Vx, const REAL* Vy, const REAL* V
     return ORC_OK;
 }
 
+/* ------------------------------------------------------------------------------------- */
+/* Stokes2D miniapp kernels (miniapps/Stokes2D.jl:11-55). nx, ny: cell counts. Arrays:    */
+/* Pt, dtPt, divV, txx, tyy, Mus, Rog (nx,ny); Vx (nx+1,ny); Vy (nx,ny+1); txy (nx-1,ny-1);*/
+/* Rx, dVxdt, dtVx (nx-1,ny-2); Ry, dVydt, dtVy (nx-2,ny-1). A[ix + n0*iy].               */
+/* ------------------------------------------------------------------------------------- */
+#define I2(a, b, n0) ((int64_t)(a) + (int64_t)(n0) * (int64_t)(b))
+
+/* compute_timesteps! (Stokes2D.jl:11-16): grid (nx, ny). */
+int SFX(orc_stokes2d_timesteps)(REAL* dtVx, REAL* dtVy, REAL* dtPt, const REAL* Mus, int64_t nx, int64_t ny, REAL Vsc,
+                                REAL Ptsc, REAL min_dxy2, int64_t max_nxy) {
+    const REAL c41 = (REAL)4.1, h = (REAL)0.5, mn = (REAL)max_nxy;
+#pragma omp parallel for schedule(static)
+    for (int64_t ty = 0; ty < ny; ty++)
+        for (int64_t tx = 0; tx < nx; tx++) {
+            if (tx < nx - 1 && ty < ny - 2) {
+                REAL av = (Mus[I2(tx, ty + 1, nx)] + Mus[I2(tx + 1, ty + 1, nx)]) * h;
+                dtVx[I2(tx, ty, nx - 1)] = ((Vsc * min_dxy2) / av) / c41;
+            }
+            if (tx < nx - 2 && ty < ny - 1) {
+                REAL av = (Mus[I2(tx + 1, ty, nx)] + Mus[I2(tx + 1, ty + 1, nx)]) * h;
+                dtVy[I2(tx, ty, nx - 2)] = ((Vsc * min_dxy2) / av) / c41;
+            }
+            dtPt[I2(tx, ty, nx)] = ((Ptsc * c41) * Mus[I2(tx, ty, nx)]) / mn;
+        }
+    return ORC_OK;
+}
+
+/* compute_P! (Stokes2D.jl:18-22): grid (nx+1, ny+1); statements masked by @all(divV), @all(Pt). */
+int SFX(orc_stokes2d_P)(REAL* divV, REAL* Pt, const REAL* Vx, const REAL* Vy, const REAL* dtPt, int64_t nx, int64_t ny,
+                        REAL dx, REAL dy) {
+#pragma omp parallel for schedule(static)
+    for (int64_t ty = 0; ty < ny; ty++)
+        for (int64_t tx = 0; tx < nx; tx++) {
+            int64_t c = I2(tx, ty, nx);
+            divV[c] = (Vx[I2(tx + 1, ty, nx + 1)] - Vx[I2(tx, ty, nx + 1)]) / dx +
+                      (Vy[I2(tx, ty + 1, nx)] - Vy[I2(tx, ty, nx)]) / dy;
+            Pt[c] = Pt[c] - dtPt[c] * divV[c];
+        }
+    return ORC_OK;
+}
+
+/* compute_τ! (Stokes2D.jl:24-29): grid (nx+1, ny+1). */
+int SFX(orc_stokes2d_tau)(const REAL* divV, REAL* txx, REAL* tyy, REAL* txy, const REAL* Vx, const REAL* Vy,
+                          const REAL* Mus, int64_t nx, int64_t ny, REAL dx, REAL dy) {
+    const REAL two = (REAL)2.0, third = (REAL)1.0 / (REAL)3.0, h = (REAL)0.5, q = (REAL)0.25;
+#pragma omp parallel for schedule(static)
+    for (int64_t ty = 0; ty < ny; ty++)
+        for (int64_t tx = 0; tx < nx; tx++) {
+            int64_t c = I2(tx, ty, nx);
+            REAL m2 = two * Mus[c];
+            txx[c] = m2 * ((Vx[I2(tx + 1, ty, nx + 1)] - Vx[I2(tx, ty, nx + 1)]) / dx - third * divV[c]);
+            tyy[c] = m2 * ((Vy[I2(tx, ty + 1, nx)] - Vy[I2(tx, ty, nx)]) / dy - third * divV[c]);
+            if (tx < nx - 1 && ty < ny - 1) {
+                REAL av = (((Mus[I2(tx, ty, nx)] + Mus[I2(tx + 1, ty, nx)]) + Mus[I2(tx, ty + 1, nx)]) +
+                           Mus[I2(tx + 1, ty + 1, nx)]) * q;
+                REAL dyVx = Vx[I2(tx + 1, ty + 1, nx + 1)] - Vx[I2(tx + 1, ty, nx + 1)];
+                REAL dxVy = Vy[I2(tx + 1, ty + 1, nx)] - Vy[I2(tx, ty + 1, nx)];
+                txy[I2(tx, ty, nx - 1)] = (two * av) * (h * (dyVx / dy + dxVy / dx));
+            }
+        }
+    return ORC_OK;
+}
+
+/* compute_dV! (Stokes2D.jl:31-37): grid (nx, ny). */
+int SFX(orc_stokes2d_dV)(REAL* Rx, REAL* Ry, REAL* dVxdt, REAL* dVydt, const REAL* Pt, const REAL* Rog, const REAL* txx,
+                         const REAL* tyy, const REAL* txy, int64_t nx, int64_t ny, REAL dampX, REAL dampY, REAL dx,
+                         REAL dy) {
+    const REAL h = (REAL)0.5;
+#pragma omp parallel for schedule(static)
+    for (int64_t ty = 0; ty < ny; ty++)
+        for (int64_t tx = 0; tx < nx; tx++) {
+            if (tx < nx - 1 && ty < ny - 2) {
+                int64_t r = I2(tx, ty, nx - 1);
+                REAL a = txx[I2(tx + 1, ty + 1, nx)] - txx[I2(tx, ty + 1, nx)];
+                REAL b = txy[I2(tx, ty + 1, nx - 1)] - txy[I2(tx, ty, nx - 1)];
+                REAL c = Pt[I2(tx + 1, ty + 1, nx)] - Pt[I2(tx, ty + 1, nx)];
+                Rx[r] = (a / dx + b / dy) - c / dx;
+                dVxdt[r] = dampX * dVxdt[r] + Rx[r];
+            }
+            if (tx < nx - 2 && ty < ny - 1) {
+                int64_t r = I2(tx, ty, nx - 2);
+                REAL a = tyy[I2(tx + 1, ty + 1, nx)] - tyy[I2(tx + 1, ty, nx)];
+                REAL b = txy[I2(tx + 1, ty, nx - 1)] - txy[I2(tx, ty, nx - 1)];
+                REAL c = Pt[I2(tx + 1, ty + 1, nx)] - Pt[I2(tx + 1, ty, nx)];
+                REAL g = (Rog[I2(tx + 1, ty, nx)] + Rog[I2(tx + 1, ty + 1, nx)]) * h;
+                Ry[r] = ((a / dy + b / dx) - c / dy) + g;
+                dVydt[r] = dampY * dVydt[r] + Ry[r];
+            }
+        }
+    return ORC_OK;
+}
+
+/* compute_V! (Stokes2D.jl:39-43): grid (nx+1, ny+1); @inn(Vx), @inn(Vy). */
+int SFX(orc_stokes2d_V)(REAL* Vx, REAL* Vy, const REAL* dVxdt, const REAL* dVydt, const REAL* dtVx, const REAL* dtVy,
+                        int64_t nx, int64_t ny) {
+#pragma omp parallel for schedule(static)
+    for (int64_t ty = 0; ty < ny; ty++)
+        for (int64_t tx = 0; tx < nx; tx++) {
+            if (tx < nx - 1 && ty < ny - 2) {
+                int64_t v = I2(tx + 1, ty + 1, nx + 1), r = I2(tx, ty, nx - 1);
+                Vx[v] = Vx[v] + dtVx[r] * dVxdt[r];
+            }
+            if (tx < nx - 2 && ty < ny - 1) {
+                int64_t v = I2(tx + 1, ty + 1, nx), r = I2(tx, ty, nx - 2);
+                Vy[v] = Vy[v] + dtVy[r] * dVydt[r];
+            }
+        }
+    return ORC_OK;
+}
+
+/* bc_x! / bc_y! (Stokes2D.jl:45-55): copy the first inner line onto the boundary line. */
+int SFX(orc_bc_x2d)(REAL* A, int64_t n0, int64_t n1) {
+    for (int64_t iy = 0; iy < n1; iy++) {
+        A[I2(0, iy, n0)] = A[I2(1, iy, n0)];
+        A[I2(n0 - 1, iy, n0)] = A[I2(n0 - 2, iy, n0)];
+    }
+    return ORC_OK;
+}
+int SFX(orc_bc_y2d)(REAL* A, int64_t n0, int64_t n1) {
+    for (int64_t ix = 0; ix < n0; ix++) {
+        A[I2(ix, 0, n0)] = A[I2(ix, 1, n0)];
+        A[I2(ix, n1 - 1, n0)] = A[I2(ix, n1 - 2, n0)];
+    }
+    return ORC_OK;
+}
+#undef I2
+
 #undef OIDX

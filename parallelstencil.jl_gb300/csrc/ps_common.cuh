@@ -42,6 +42,9 @@ struct DeviceState {
 
 // Returns PS_ERR_NOT_INIT unless ps_init succeeded for the current device.
 int current_state(DeviceState** st);
+// Frees library-owned solver scratch (ps_finalize).
+void stokes2d_free_scratch();
+
 // Reads (and clears) the device error word after a synchronisation.
 int check_device_error(DeviceState* st, cudaStream_t s);
 

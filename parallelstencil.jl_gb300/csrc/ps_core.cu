@@ -199,6 +199,7 @@ int ps_finalize(void) {
     std::lock_guard<std::mutex> lock(g_mutex);
     int cur = 0;
     cudaGetDevice(&cur);
+    stokes2d_free_scratch();
     for (int d = 0; d < kMaxDevices; d++) {
         DeviceState& st = g_dev[d];
         if (!st.ready) continue;

@@ -244,8 +244,56 @@ def diffusion_project(dt):
     return dict(T0=T0, Ci=Ci0, T=T, scalars=np.array([lam, dt_, dxs, dys, dzs], dtype=dt))
 
 
+def stokes2d_numpy(nx, ny, iters, dt):
+    """miniapps/Stokes2D.jl:11-55, 93-116 restated with numpy broadcasting (lx = ly = 10,
+    μs0 = 1, μsi = 0.1, ρgi = 1, Vdmp = 4, Vsc = 1, Ptsc = 1/4)."""
+    lx = ly = 10.0
+    dx, dy = lx / (nx - 1), ly / (ny - 1)
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    radc = (ix * dx - 0.5 * lx) ** 2 + (iy * dy - 0.5 * ly) ** 2
+    Mus = np.ones((nx, ny))
+    Rog = np.zeros((nx, ny))
+    Mus[radc < 1.0] = 0.1
+    Rog[radc < 1.0] = 1.0
+    Mus, Rog = Mus.astype(dt), Rog.astype(dt)
+    c = lambda v: dt(v)  # noqa: E731 - literal typing
+    dxs, dys = c(dx), c(dy)
+    dampX, dampY = c(1.0 - 4.0 / nx), c(1.0 - 4.0 / ny)
+    Vsc, Ptsc, min_dxy2, max_nxy = c(1.0), c(0.25), c(min(dx, dy) ** 2), c(max(nx, ny))
+    d_xa = lambda A: A[1:, :] - A[:-1, :]  # noqa: E731
+    d_ya = lambda A: A[:, 1:] - A[:, :-1]  # noqa: E731
+    d_xi = lambda A: A[1:, 1:-1] - A[:-1, 1:-1]  # noqa: E731
+    d_yi = lambda A: A[1:-1, 1:] - A[1:-1, :-1]  # noqa: E731
+    av = lambda A: (((A[:-1, :-1] + A[1:, :-1]) + A[:-1, 1:]) + A[1:, 1:]) * c(0.25)  # noqa: E731
+    av_xi = lambda A: (A[:-1, 1:-1] + A[1:, 1:-1]) * c(0.5)  # noqa: E731
+    av_yi = lambda A: (A[1:-1, :-1] + A[1:-1, 1:]) * c(0.5)  # noqa: E731
+    dtauVx = ((Vsc * min_dxy2) / av_xi(Mus)) / c(4.1)
+    dtauVy = ((Vsc * min_dxy2) / av_yi(Mus)) / c(4.1)
+    dtauPt = ((Ptsc * c(4.1)) * Mus) / max_nxy
+    Pt = np.zeros((nx, ny), dt)
+    Vx, Vy = np.zeros((nx + 1, ny), dt), np.zeros((nx, ny + 1), dt)
+    dVxdtau, dVydtau = np.zeros((nx - 1, ny - 2), dt), np.zeros((nx - 2, ny - 1), dt)
+    for _ in range(iters):
+        divV = d_xa(Vx) / dxs + d_ya(Vy) / dys
+        Pt = Pt - dtauPt * divV
+        txx = (c(2.0) * Mus) * (d_xa(Vx) / dxs - (c(1.0) / c(3.0)) * divV)
+        tyy = (c(2.0) * Mus) * (d_ya(Vy) / dys - (c(1.0) / c(3.0)) * divV)
+        txy = (c(2.0) * av(Mus)) * (c(0.5) * (d_yi(Vx) / dys + d_xi(Vy) / dxs))
+        Rx = (d_xi(txx) / dxs + d_ya(txy) / dys) - d_xi(Pt) / dxs
+        Ry = ((d_yi(tyy) / dys + d_xa(txy) / dxs) - d_yi(Pt) / dys) + av_yi(Rog)
+        dVxdtau = dampX * dVxdtau + Rx
+        dVydtau = dampY * dVydtau + Ry
+        Vx[1:-1, 1:-1] = Vx[1:-1, 1:-1] + dtauVx * dVxdtau
+        Vy[1:-1, 1:-1] = Vy[1:-1, 1:-1] + dtauVy * dVydtau
+        Vx[:, 0], Vx[:, -1] = Vx[:, 1], Vx[:, -2]
+        Vy[0, :], Vy[-1, :] = Vy[1, :], Vy[-2, :]
+    out = dict(Mus=Mus, Rog=Rog, Pt=Pt, Vx=Vx, Vy=Vy, divV=divV, txx=txx, tyy=tyy, txy=txy, Rx=Rx, Ry=Ry,
+               dVxdtau=dVxdtau, dVydtau=dVydtau, dtauVx=dtauVx, dtauVy=dtauVy, dtauPt=dtauPt)
+    return {k: np.asfortranarray(v) for k, v in out.items()}
+
+
 def main():
-    arrays, meta = {}, {"fd": [], "diffusion": []}
+    arrays, meta = {}, {"fd": [], "diffusion": [], "stokes2d": []}
     for dtn, dt in (("f64", np.float64), ("f32", np.float32)):
         for nd, (templates, grid, gen) in {3: (FIELD3, (9, 7, 8), None), 2: (FIELD2, (9, 7), None),
                                             1: (FIELD1, (9,), None)}.items():
@@ -270,6 +318,10 @@ def main():
         p = diffusion_project(dt)
         for k, v in p.items():
             arrays[f"project8_{dtn}_{k}"] = v
+        nx, ny, iters = 31, 17, 40
+        for k, v in stokes2d_numpy(nx, ny, iters, dt).items():
+            arrays[f"stokes2d_{dtn}_{k}"] = v
+        meta["stokes2d"].append({"prefix": f"stokes2d_{dtn}_", "nx": nx, "ny": ny, "iters": iters, "dtype": dtn})
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as fh:
         json.dump(meta, fh, indent=1)

@@ -94,3 +94,21 @@ def test_oracle_ranges_compose(oracle):
     for lo, hi in get_ranges_outer(bw, n) + get_ranges_inner(bw, n):
         oracle.diffusion3d_step(1, split, T, Ci, None, 1.0, 1e-3, 2.0, 2.0, 2.0, lo=lo, hi=hi)
     assert np.array_equal(full, split)
+
+
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_oracle_stokes2d_vs_broadcasting(oracle, golden, dtn):
+    """miniapps/Stokes2D.jl kernels: the oracle's loops equal the broadcasting restatement."""
+    meta, arr = golden
+    case = [c for c in meta["stokes2d"] if c["dtype"] == dtn][0]
+    g = {k[len(case["prefix"]):]: v for k, v in arr.items() if k.startswith(case["prefix"])}
+    nx, ny = case["nx"], case["ny"]
+    s = oracle.Stokes2D(nx, ny, 10.0 / (nx - 1), 10.0 / (ny - 1), g["Mus"], g["Rog"], dtype=DT[dtn])
+    s.compute_timesteps()
+    for k in ("dtauVx", "dtauVy", "dtauPt"):
+        assert np.array_equal(s[k], g[k]), k
+    for _ in range(case["iters"]):
+        s.step()
+    for k in ("Pt", "Vx", "Vy", "divV", "txx", "tyy", "txy", "Rx", "Ry", "dVxdtau", "dVydtau"):
+        assert np.array_equal(s[k], g[k]), k
+    assert s.err()[0] > 0
