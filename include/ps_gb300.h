@@ -68,7 +68,14 @@ typedef struct ps_launch {
     int32_t loopsize;     /* z-planes swept by one CTA (`loopsize`); 0 = library default   */
     int64_t range_lo[3];  /* `ranges` of the call as 0-based half-open thread-index boxes  */
     int64_t range_hi[3];  /* (hi <= lo in every dimension, or a NULL ps_launch = full grid) */
+    int32_t fp64_mode;    /* FP64 arrays only. PS_FP64_IEEE: IEEE double arithmetic on the FP64
+                             pipe, bit-identical to the reference. PS_FP64_SPLIT: arithmetic on
+                             pairs of FP32 numbers (47-bit significand) on the FP32/integer pipes,
+                             <= 1e-12 relative max-norm from the reference (see ps_diffusion3d_step) */
+    int32_t reserved;
 } ps_launch;
+
+enum { PS_FP64_IEEE = 0, PS_FP64_SPLIT = 1 };
 
 /* ------------------------------------------------------------------------------------ */
 /* Core: device, memory, streams.                                                        */
@@ -178,10 +185,11 @@ typedef int (*ps_comm_fn)(void* ctx);
  * (src/ParallelKernel/hide_communication.jl:177-258, ranges :350-394): the six boundary
  * slabs of width bw run on s_boundary, the inner box on s_inner; comm (may be NULL) runs
  * after the boundary slabs finish and before the inner box is waited for. On return both
- * streams are synchronised. Result identical to ps_diffusion3d_step. */
+ * streams are synchronised. cfg supplies memopt and fp64_mode (its ranges are ignored).
+ * Result identical to ps_diffusion3d_step. */
 int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr,
                               double lam, double dt, double hx, double hy, double hz,
-                              int32_t memopt, const int64_t bw[3], void* s_boundary, void* s_inner,
+                              const ps_launch* cfg, const int64_t bw[3], void* s_boundary, void* s_inner,
                               ps_comm_fn comm, void* comm_ctx);
 
 /* ------------------------------------------------------------------------------------ */

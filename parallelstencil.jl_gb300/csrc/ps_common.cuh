@@ -28,8 +28,8 @@ void clear_error();
         if (_ps_rc != PS_OK) return _ps_rc; \
     } while (0)
 
-// Device-side error word codes (written by kernels whose bounded waits gave up).
-enum : int { DEV_ERR_NONE = 0, DEV_ERR_TMA_TIMEOUT = 1, DEV_ERR_GRID_TIMEOUT = 2 };
+// Device-side error word bits (kernels OR them in; the host reads and clears the word).
+enum : int { DEV_ERR_NONE = 0, DEV_ERR_TMA_TIMEOUT = 1, DEV_ERR_GRID_TIMEOUT = 2, DEV_ERR_RANGE = 4 };
 
 // Per-device library state.
 struct DeviceState {

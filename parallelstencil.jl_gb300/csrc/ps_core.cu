@@ -54,7 +54,10 @@ int check_device_error(DeviceState* st, cudaStream_t s) {
         int zero = 0;
         PS_CUDA_TRY(cudaMemcpyAsync(st->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
         PS_CUDA_TRY(cudaStreamSynchronize(s));
-        return fail(PS_ERR_TIMEOUT, "a bounded device-side wait gave up (device error code %d)", h);
+        if (h & (DEV_ERR_TMA_TIMEOUT | DEV_ERR_GRID_TIMEOUT))
+            return fail(PS_ERR_TIMEOUT, "a bounded device-side wait gave up (device error bits %d)", h);
+        return fail(PS_ERR_UNSUPPORTED, "an FP64 value outside the split-arithmetic range (|x| >= 2^128 or "
+                    "non-finite) was seen; rerun with fp64_mode = PS_FP64_IEEE (device error bits %d)", h);
     }
     return PS_OK;
 }

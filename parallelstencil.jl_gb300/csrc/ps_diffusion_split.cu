@@ -1,0 +1,356 @@
+// ps_diffusion_split.cu -- FP64 diffusion step with split-FP32 arithmetic (fp64_mode = PS_FP64_SPLIT).
+//
+// GB300 executes FP64 arithmetic, and f64<->f32 conversions, at 2 instructions / clk / SM, but
+// FP32 and integer instructions at 128 / clk / SM. An IEEE-FP64 z-sweep of the diffusion step
+// therefore runs at ~6 % of HBM bandwidth. This kernel keeps the arrays in FP64 but evaluates the
+// stencil on pairs of FP32 numbers (h + l, a 47-bit significand):
+//   - doubles are split into (h, l) with integer bit operations, never with conversions;
+//   - sums use the exact two-sum of the high parts plus an FP32 sum of the low parts;
+//   - products use FMA to recover the rounding error of h*h;
+//   - the update is applied in FP64 as T2 = (T + δh) + δl (two FP64 additions per cell), so T
+//     itself is never truncated.
+// The result differs from the IEEE evaluation of the reference's statements by <= ~1e-14 of
+// max|T| per step (the fixed tolerance is 1e-12 relative max-norm). Magnitudes >= 2^128 raise a
+// device flag (PS_ERR_UNSUPPORTED at the next synchronisation); magnitudes < 2^-80 keep 24 bits
+// (absolute error < 2^-104), so the bound holds for fields with max|T| >= 2^-60.
+//
+// Staging is the same TMA z-sweep as diff3d_zsweep_tma: planes of T (and lam) with an x-y halo
+// and of Ci land in a shared-memory ring; each plane is converted in place once (every value is
+// split exactly once per step), face fluxes are shared between the two cells of a face (x faces
+// inside a thread, y faces through shared memory, z faces through registers).
+#include <algorithm>
+
+#include "ps_common.cuh"
+
+namespace ps {
+
+struct dd {
+    float h, l;
+};
+
+// Split a double into two floats with integer operations only (see file comment).
+__device__ __forceinline__ dd dd_split(double x, bool& big) {
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned t = hw & 0x7FFFFFFFu;
+    const unsigned sgn = hw & 0x80000000u;
+    // high part: sign | (e - 896) << 23 | top 23 mantissa bits (truncated), for e in [897, 1150]
+    const unsigned fb = __funnelshift_l(lw, hw, 3) ^ 0x40000000u;
+    float h = __uint_as_float((fb & 0x7FFFFFFFu) | sgn);
+    // low part: the next 23 mantissa bits m, as m * 2^(e - 1069), for e >= 943
+    const float m = __uint_as_float(((lw >> 6) & 0x7FFFFFu) | 0x4B000000u) - 8388608.0f;
+    const unsigned sb = (((hw << 3) & 0xFF800000u) - 0xD7000000u) | sgn;
+    float l = m * __uint_as_float(sb);
+    h = t < 0x38100000u ? 0.0f : h;  // e < 897: below FP32's normal range
+    l = t < 0x3AF00000u ? 0.0f : l;  // e < 943: keep the 24-bit high part only
+    big |= t >= 0x47F00000u;         // e >= 1151: outside FP32's range (or inf / nan)
+    return {h, l};
+}
+
+// Exact conversion of a float to double with integer operations (zero and denormals -> ±0 / tiny).
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned b = __float_as_uint(f);
+    unsigned hi = (((b >> 3) & 0x0FFFFFFFu) + 0x38000000u) | (b & 0x80000000u);
+    hi = (b & 0x7F800000u) ? hi : (b & 0x80000000u);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+__device__ __forceinline__ dd dd_add(dd a, dd b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb);
+    return {s, e + (a.l + b.l)};
+}
+__device__ __forceinline__ dd dd_sub(dd a, dd b) { return dd_add(a, dd{-b.h, -b.l}); }
+__device__ __forceinline__ dd dd_mul(dd a, dd b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return {p, e};
+}
+
+struct SplitParams {
+    dd c[3];    // per-dimension coefficients (unused when ISO)
+    dd g;       // δ = (Ci * g) * Σ_d c_d (F_d+ - F_d-)
+};
+
+constexpr int SP_TY = 8;   // rows (warps) per CTA
+constexpr int SP_TX = 64;  // cells per row (32 lanes x 2)
+constexpr int SP_S = 4;    // TMA ring stages
+
+template <bool LAM>
+struct SplitCfg {
+    static constexpr int PW = SP_TX + 4;  // staged plane: x in [X0-2, X0+66) keeps TMA x 16-byte aligned
+    static constexpr int PH = SP_TY + 2;
+    static constexpr int PLANE = ((PW * PH * 8 + 127) / 128) * 128;
+    static constexpr int CIB = SP_TX * SP_TY * 8;
+    static constexpr int STAGE = PLANE * (LAM ? 2 : 1) + CIB;
+    static constexpr uint32_t TX_BYTES = (uint32_t)(PW * PH * 8 * (LAM ? 2 : 1) + SP_TX * SP_TY * 8);
+    static constexpr int FACE = (SP_TY + 1) * SP_TX * 8;  // y-face fluxes, one float2 per cell
+    static constexpr int HALO = 2 * PH + 2 * SP_TX;       // converted halo values per array
+    static constexpr int SMEM = SP_S * STAGE + FACE + 8 * SP_S;
+};
+
+// Face flux between cells a (lower) and b (upper): K*D (LAM) or D, D = T_b - T_a, K = l_a + l_b.
+template <bool LAM>
+__device__ __forceinline__ dd face(dd Ta, dd Tb, dd la, dd lb) {
+    dd D = dd_sub(Tb, Ta);
+    if constexpr (LAM) return dd_mul(dd_add(la, lb), D);
+    return D;
+}
+
+template <bool LAM, bool ISO>
+__global__ void __launch_bounds__(32 * SP_TY, 3) diff3d_split_tma(const __grid_constant__ CUtensorMap mT,
+                                                               const __grid_constant__ CUtensorMap mL,
+                                                               const __grid_constant__ CUtensorMap mC,
+                                                               double* __restrict__ T2, SplitParams p, int64_t nx,
+                                                               int64_t ny, Box cb, int L, int* __restrict__ err) {
+    using C = SplitCfg<LAM>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2* faceY = reinterpret_cast<float2*>(smem + SP_S * C::STAGE);  // [SP_TY+1][SP_TX]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SP_S * C::STAGE + C::FACE);
+
+    const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
+    const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
+    const int Y0 = (int)cb.lo[1] + blockIdx.y * SP_TY;
+    const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
+    const int nk = min(L, (int)cb.hi[2] - Z0);
+    const int nq = nk + 2;
+
+    auto tslot = [&](int q) { return reinterpret_cast<double*>(smem + (q % SP_S) * C::STAGE); };
+    auto lslot = [&](int q) { return reinterpret_cast<double*>(smem + (q % SP_S) * C::STAGE + C::PLANE); };
+    auto cslot = [&](int q) {
+        return reinterpret_cast<double*>(smem + (q % SP_S) * C::STAGE + C::PLANE * (LAM ? 2 : 1));
+    };
+
+    if (tid == 0) {
+        prefetch_tensormap(&mT);
+        if constexpr (LAM) prefetch_tensormap(&mL);
+        prefetch_tensormap(&mC);
+        for (int s = 0; s < SP_S; s++) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int next_q = 0;
+    auto issue = [&](int q) {
+        int s = q % SP_S, z = Z0 - 1 + q;
+        mbar_arrive_expect_tx(&bar[s], C::TX_BYTES);
+        tma_load_3d(tslot(q), &mT, &bar[s], X0 - 2, Y0 - 1, z);
+        if constexpr (LAM) tma_load_3d(lslot(q), &mL, &bar[s], X0 - 2, Y0 - 1, z);
+        tma_load_3d(cslot(q), &mC, &bar[s], X0, Y0, z);
+    };
+    if (tid == 0)
+        for (; next_q < min(SP_S, nq); ++next_q) issue(next_q);
+
+    const int col = 2 + 2 * lx;  // staged-plane column of this thread's first cell
+    const int py = 1 + ly;
+    const int own = py * C::PW + col;
+    const int64_t gx = X0 + 2 * lx, gy = Y0 + ly;
+    const bool row_in = gy >= cb.lo[1] && gy < cb.hi[1];
+    const bool in0 = row_in && gx >= cb.lo[0] && gx < cb.hi[0];
+    const bool in1 = row_in && gx + 1 >= cb.lo[0] && gx + 1 < cb.hi[0];
+
+    bool big = false, timed_out = false;
+    // Converts plane q in place: own cells (returned, raw T kept) and this thread's halo share.
+    auto convert = [&](int q, dd* Tn, dd* ln, double2& rawT) {
+        double* tp = tslot(q);
+        rawT = *reinterpret_cast<const double2*>(tp + own);
+        Tn[0] = dd_split(rawT.x, big);
+        Tn[1] = dd_split(rawT.y, big);
+        *reinterpret_cast<float4*>(tp + own) = make_float4(Tn[0].h, Tn[0].l, Tn[1].h, Tn[1].l);
+        if constexpr (LAM) {
+            double* lp = lslot(q);
+            double2 r = *reinterpret_cast<const double2*>(lp + own);
+            ln[0] = dd_split(r.x, big);
+            ln[1] = dd_split(r.y, big);
+            *reinterpret_cast<float4*>(lp + own) = make_float4(ln[0].h, ln[0].l, ln[1].h, ln[1].l);
+        }
+        // halo: columns 1 and PW-2 of every row, rows 0 and PH-1 of the interior columns
+        for (int h = tid; h < C::HALO * (LAM ? 2 : 1); h += 32 * SP_TY) {
+            int a = h % C::HALO;
+            double* base = (h < C::HALO) ? tp : lslot(q);
+            int idx = a < 2 * C::PH ? (a % C::PH) * C::PW + (a < C::PH ? 1 : C::PW - 2)
+                                    : ((a - 2 * C::PH) < SP_TX ? 0 : (C::PH - 1)) * C::PW + 2 +
+                                          ((a - 2 * C::PH) % SP_TX);
+            dd v = dd_split(base[idx], big);
+            *reinterpret_cast<float2*>(base + idx) = make_float2(v.h, v.l);
+        }
+    };
+    auto ld2 = [&](const double* plane, int off) {
+        float2 v = *reinterpret_cast<const float2*>(plane + off);
+        return dd{v.x, v.y};
+    };
+
+    dd Tc[2], lc[2], Tz[2], lz[2], Fzm[2];
+    double2 rawTc, rawTz;
+    timed_out |= !mbar_wait_bounded(&bar[0], 0);
+    timed_out |= !mbar_wait_bounded(&bar[1], 0);
+    {
+        dd T0[2], l0[2];
+        double2 r0;
+        convert(0, T0, l0, r0);
+        convert(1, Tc, lc, rawTc);
+#pragma unroll
+        for (int j = 0; j < 2; j++) Fzm[j] = face<LAM>(T0[j], Tc[j], l0[j], lc[j]);
+    }
+
+    for (int k = 0; k < nk; ++k) {
+        const int q = k + 2;
+        timed_out |= !mbar_wait_bounded(&bar[q % SP_S], (q / SP_S) & 1);
+        if (!timed_out) convert(q, Tz, lz, rawTz);
+        __syncthreads();  // A: plane q converted
+        const double* tp = tslot(k + 1);
+        const double* lp = LAM ? lslot(k + 1) : nullptr;
+        dd Fx[3], Fym[2], Fzp[2], ci[2];
+        if (!timed_out) {
+            double2 rc = *reinterpret_cast<const double2*>(cslot(k + 1) + ly * SP_TX + 2 * lx);
+            ci[0] = dd_split(rc.x, big);
+            ci[1] = dd_split(rc.y, big);
+            // x faces: left of cell 0, between the cells, right of cell 1
+            dd Txm = ld2(tp, own - 1), Txp = ld2(tp, own + 2);
+            dd lxm{0.f, 0.f}, lxp{0.f, 0.f};
+            if constexpr (LAM) {
+                lxm = ld2(lp, own - 1);
+                lxp = ld2(lp, own + 2);
+            }
+            Fx[0] = face<LAM>(Txm, Tc[0], lxm, lc[0]);
+            Fx[1] = face<LAM>(Tc[0], Tc[1], lc[0], lc[1]);
+            Fx[2] = face<LAM>(Tc[1], Txp, lc[1], lxp);
+            // y faces below this row (and above, for the top row) go through shared memory
+            {
+                float4 tb = *reinterpret_cast<const float4*>(tp + own - C::PW);
+                float4 lb = LAM ? *reinterpret_cast<const float4*>(lp + own - C::PW) : make_float4(0, 0, 0, 0);
+                Fym[0] = face<LAM>(dd{tb.x, tb.y}, Tc[0], dd{lb.x, lb.y}, lc[0]);
+                Fym[1] = face<LAM>(dd{tb.z, tb.w}, Tc[1], dd{lb.z, lb.w}, lc[1]);
+                *reinterpret_cast<float4*>(faceY + ly * SP_TX + 2 * lx) =
+                    make_float4(Fym[0].h, Fym[0].l, Fym[1].h, Fym[1].l);
+            }
+            if (ly == SP_TY - 1) {
+                float4 ta = *reinterpret_cast<const float4*>(tp + own + C::PW);
+                float4 la = LAM ? *reinterpret_cast<const float4*>(lp + own + C::PW) : make_float4(0, 0, 0, 0);
+                dd f0 = face<LAM>(Tc[0], dd{ta.x, ta.y}, lc[0], dd{la.x, la.y});
+                dd f1 = face<LAM>(Tc[1], dd{ta.z, ta.w}, lc[1], dd{la.z, la.w});
+                *reinterpret_cast<float4*>(faceY + SP_TY * SP_TX + 2 * lx) = make_float4(f0.h, f0.l, f1.h, f1.l);
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++) Fzp[j] = face<LAM>(Tc[j], Tz[j], lc[j], lz[j]);
+        }
+        // B: y faces published; planes <= k+1 are no longer read
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0) {
+                atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+                for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % SP_S], (r / SP_S) & 1);
+            }
+            return;
+        }
+        if (tid == 0)
+            for (; next_q < min(nq, k + 2 + SP_S); ++next_q) issue(next_q);
+        float4 fa = *reinterpret_cast<const float4*>(faceY + (ly + 1) * SP_TX + 2 * lx);
+        dd Fyp[2] = {dd{fa.x, fa.y}, dd{fa.z, fa.w}};
+        double out[2];
+        const double rawc[2] = {rawTc.x, rawTc.y};
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            dd S;
+            if constexpr (ISO) {
+                S = dd_sub(Fx[j + 1], Fx[j]);
+                S = dd_add(S, Fyp[j]);
+                S = dd_sub(S, Fym[j]);
+                S = dd_add(S, Fzp[j]);
+                S = dd_sub(S, Fzm[j]);
+            } else {
+                S = dd_mul(p.c[0], dd_sub(Fx[j + 1], Fx[j]));
+                S = dd_add(S, dd_mul(p.c[1], dd_sub(Fyp[j], Fym[j])));
+                S = dd_add(S, dd_mul(p.c[2], dd_sub(Fzp[j], Fzm[j])));
+            }
+            dd delta = dd_mul(dd_mul(ci[j], p.g), S);
+            out[j] = (rawc[j] + f32_to_f64(delta.h)) + f32_to_f64(delta.l);
+        }
+        const int64_t gz = Z0 + k;
+        double* dst = T2 + gx + nx * (gy + ny * gz);
+        if (in0 && in1)
+            *reinterpret_cast<double2*>(dst) = make_double2(out[0], out[1]);
+        else {
+            if (in0) dst[0] = out[0];
+            if (in1) dst[1] = out[1];
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            Tc[j] = Tz[j];
+            lc[j] = lz[j];
+            Fzm[j] = Fzp[j];
+        }
+        rawTc = rawTz;
+    }
+    if (__syncthreads_or(big) && tid == 0) atomicOr(err, DEV_ERR_RANGE);
+}
+
+static void split_const(dd& d, double v) {
+    float h = (float)v;
+    d.h = h;
+    d.l = (float)(v - (double)h);
+}
+
+// Launches the split-arithmetic z-sweep; returns PS_ERR_UNSUPPORTED when the arrays are not
+// TMA-eligible (the caller then uses the IEEE kernels).
+int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                           double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
+                           cudaStream_t s, int* d_err) {
+    bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
+    if (!tma || T2.dtype != PS_F64) return PS_ERR_UNSUPPORTED;
+    SplitParams p{};
+    double c[3], g;
+    const double h[3] = {hx, hy, hz};
+    for (int d = 0; d < 3; d++) {
+        switch (form) {
+        case PS_DIFF_DIV: c[d] = 1.0 / (h[d] * h[d]); break;
+        case PS_DIFF_FLUX_LAM: c[d] = 0.5 * (h[d] * h[d]); break;
+        default: c[d] = h[d] * h[d]; break;
+        }
+    }
+    g = form == PS_DIFF_FLUX_LAM ? dt : dt * lam_s;
+    const bool iso = c[0] == c[1] && c[1] == c[2];
+    if (iso) g *= c[0];
+    for (int d = 0; d < 3; d++) split_const(p.c[d], c[d]);
+    split_const(p.g, g);
+    const bool has_lam = form == PS_DIFF_FLUX_LAM;
+    CUtensorMap mT, mL, mC;
+    const int PW = SP_TX + 4, PH = SP_TY + 2;
+    PS_TRY(encode_plane_map(&mT, Tin, PW, PH));
+    if (has_lam)
+        PS_TRY(encode_plane_map(&mL, *lam, PW, PH));
+    else
+        mL = mT;
+    PS_TRY(encode_plane_map(&mC, Ci, SP_TX, SP_TY));
+    int64_t x0 = cb.lo[0] & ~(int64_t)1;
+    dim3 blk(32, SP_TY, 1);
+    dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + SP_TY - 1) / SP_TY),
+             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    double* out = static_cast<double*>(T2.ptr);
+#define PS_SPLIT_LAUNCH(LAMV, ISOV)                                                                              \
+    do {                                                                                                         \
+        static bool attr = false;                                                                                \
+        if (!attr) {                                                                                             \
+            PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_split_tma<LAMV, ISOV>,                                       \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, SplitCfg<LAMV>::SMEM)); \
+            attr = true;                                                                                         \
+        }                                                                                                        \
+        diff3d_split_tma<LAMV, ISOV><<<grd, blk, SplitCfg<LAMV>::SMEM, s>>>(mT, mL, mC, out, p, T2.n[0], T2.n[1], \
+                                                                            cb, L, d_err);                       \
+    } while (0)
+    if (has_lam) {
+        if (iso)
+            PS_SPLIT_LAUNCH(true, true);
+        else
+            PS_SPLIT_LAUNCH(true, false);
+    } else {
+        if (iso)
+            PS_SPLIT_LAUNCH(false, true);
+        else
+            PS_SPLIT_LAUNCH(false, false);
+    }
+#undef PS_SPLIT_LAUNCH
+    return PS_OK;
+}
+
+}  // namespace ps

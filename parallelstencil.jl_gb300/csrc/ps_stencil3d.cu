@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
         // Every thread is done with plane k+1: its slot may be refilled.
         if (__syncthreads_or(timed_out)) {
             if (tid == 0) {
-                atomicExch(err, DEV_ERR_TMA_TIMEOUT);
+                atomicOr(err, DEV_ERR_TMA_TIMEOUT);
                 for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % S], (r / S) & 1);
             }
             return;
@@ -541,6 +541,10 @@ static DiffParams<T> diff_params(double lam, double dt, double hx, double hy, do
     return DiffParams<T>{(T)lam, (T)dt, (T)hx, (T)hy, (T)hz};
 }
 
+int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                           double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
+                           cudaStream_t s, int* d_err);
+
 // Default z-sweep length (`loopsize`): the reference uses 64 on compute capability >= 9
 // (src/parallel.jl:532-543); the same default is kept.
 static constexpr int kDefaultLoopsize = 64;
@@ -644,9 +648,15 @@ static Box inner_cells(const Box& tb, const int64_t n[3]) {
 
 int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam,
                   double lam_s, double dt, double hx, double hy, double hz, const Box& thread_box, int memopt,
-                  int loopsize, cudaStream_t s, int* d_err) {
+                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err) {
     Box cb = inner_cells(thread_box, T2.n);
     const ps_array* lp = form == PS_DIFF_FLUX_LAM ? &lam : nullptr;
+    if (cb.hi[0] <= cb.lo[0] || cb.hi[1] <= cb.lo[1] || cb.hi[2] <= cb.lo[2]) return PS_OK;
+    if (T2.dtype == PS_F64 && fp64_mode == PS_FP64_SPLIT) {
+        int L = loopsize > 0 ? loopsize : kDefaultLoopsize;
+        int rc = launch_diffusion_split(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, L, s, d_err);
+        if (rc != PS_ERR_UNSUPPORTED) return rc;  // not TMA-eligible: IEEE kernels below
+    }
     if (T2.dtype == PS_F64)
         return dispatch_diffusion<double>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err);
     return dispatch_diffusion<float>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err);
@@ -770,15 +780,18 @@ int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_a
     Box tb = launch_box(cfg, T2.n);
     int memopt = cfg ? cfg->memopt : 0;
     int loopsize = cfg ? cfg->loopsize : 0;
+    int fp64_mode = cfg ? cfg->fp64_mode : PS_FP64_IEEE;
     if (loopsize < 0) return fail(PS_ERR_ARG, "ps_diffusion3d_step: loopsize must be >= 0");
-    PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, tb, memopt, loopsize, s, st->d_err));
+    if (fp64_mode != PS_FP64_IEEE && fp64_mode != PS_FP64_SPLIT) return fail(PS_ERR_ARG, "unknown fp64_mode %d", fp64_mode);
+    PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, tb, memopt, loopsize, fp64_mode, s, st->d_err));
     return finish_launch(s, sync, "ps_diffusion3d_step");
 }
 
 int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr, double lam,
-                              double dt, double hx, double hy, double hz, int32_t memopt, const int64_t bw[3],
+                              double dt, double hx, double hy, double hz, const ps_launch* cfg, const int64_t bw[3],
                               void* s_boundary, void* s_inner, ps_comm_fn comm, void* comm_ctx) {
     DeviceState* st = nullptr;
+    const int memopt = cfg ? cfg->memopt : 0, fp64_mode = cfg ? cfg->fp64_mode : PS_FP64_IEEE;
     PS_TRY(current_state(&st));
     PS_TRY(diffusion_args(form, T2, T, Ci, lam_arr));
     if (!bw) return fail(PS_ERR_NULL, "ps_diffusion3d_step_split: NULL boundary width");
@@ -808,10 +821,10 @@ int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci
         bool empty = false;
         for (int d = 0; d < 3; d++) empty |= outer[i].hi[d] <= outer[i].lo[d];
         if (empty) continue;
-        PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, outer[i], memopt, 0, sb, st->d_err));
+        PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, outer[i], memopt, 0, fp64_mode, sb, st->d_err));
     }
     PS_TRY(finish_launch(sb, 0, "ps_diffusion3d_step_split(boundary)"));
-    PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, inner, memopt, 0, si, st->d_err));
+    PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, inner, memopt, 0, fp64_mode, si, st->d_err));
     PS_TRY(finish_launch(si, 0, "ps_diffusion3d_step_split(inner)"));
     PS_TRY(finish_launch(sb, 1, "ps_diffusion3d_step_split(boundary sync)"));
     int crc = PS_OK;

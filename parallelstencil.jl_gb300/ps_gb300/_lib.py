@@ -35,7 +35,7 @@ class PSArray(ctypes.Structure):
 
 class PSLaunch(ctypes.Structure):
     _fields_ = [("memopt", ctypes.c_int32), ("loopsize", ctypes.c_int32), ("range_lo", ctypes.c_int64 * 3),
-                ("range_hi", ctypes.c_int64 * 3)]
+                ("range_hi", ctypes.c_int64 * 3), ("fp64_mode", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class PSFdOp(ctypes.Structure):
@@ -70,7 +70,8 @@ SIGNATURES = {
     "ps_fd_apply": [PSFdOp, _I32, _A, _A, _P, _I],
     "ps_memcopy3d": [_A, _A, _A, ctypes.POINTER(PSLaunch), _P, _I],
     "ps_diffusion3d_step": [_I32, _A, _A, _A, _A, _D, _D, _D, _D, _D, ctypes.POINTER(PSLaunch), _P, _I],
-    "ps_diffusion3d_step_split": [_I32, _A, _A, _A, _A, _D, _D, _D, _D, _D, _I32, ctypes.POINTER(_I64), _P, _P,
+    "ps_diffusion3d_step_split": [_I32, _A, _A, _A, _A, _D, _D, _D, _D, _D, ctypes.POINTER(PSLaunch),
+                                  ctypes.POINTER(_I64), _P, _P,
                                   COMM_FN, _P],
     "ps_acoustic3d_v": [_A, _A, _A, _A, _D, _D, _D, _D, _D, _P, _I],
     "ps_acoustic3d_p": [_A, _A, _A, _A, _D, _D, _D, _D, _D, _P, _I],

@@ -27,12 +27,16 @@ from .core import ArgumentError, default_memopt, descriptor, require_initialized
 from .fd import FdKernel, fd_kernel
 
 PS_DIFF_DIV, PS_DIFF_MUL, PS_DIFF_FLUX, PS_DIFF_FLUX_LAM = 0, 1, 2, 3
+FP64_MODES = {"ieee": 0, "split": 1}
 
 
-def _launch_cfg(memopt: bool, loopsize: int, ranges):
+def _launch_cfg(memopt: bool, loopsize: int, ranges, fp64: str = "ieee"):
     cfg = PSLaunch()
     cfg.memopt = int(bool(memopt))
     cfg.loopsize = int(loopsize or 0)
+    if fp64 not in FP64_MODES:
+        raise ArgumentError(f"fp64 must be one of {tuple(FP64_MODES)} (obtained {fp64!r})")
+    cfg.fp64_mode = FP64_MODES[fp64]
     if ranges is not None:
         lo, hi = ranges_to_box(ranges)
         for d in range(3):
@@ -62,15 +66,15 @@ class Kernel:
     name: str
     nargs: int
 
-    def launch(self, args, memopt, loopsize, ranges, stream, sync):  # pragma: no cover - abstract
+    def launch(self, args, memopt, loopsize, ranges, stream, sync, fp64="ieee"):  # pragma: no cover - abstract
         raise NotImplementedError
 
 
 @dataclass(frozen=True)
 class Copy3D(Kernel):
-    def launch(self, args, memopt, loopsize, ranges, stream, sync):
+    def launch(self, args, memopt, loopsize, ranges, stream, sync, fp64="ieee"):
         T2, T, Ci = args
-        cfg = _launch_cfg(memopt, loopsize, ranges)
+        cfg = _launch_cfg(memopt, loopsize, ranges, fp64)
         _lib.call("ps_memcopy3d", descriptor(T2), descriptor(T), descriptor(Ci), ctypes.byref(cfg),
                   stream_handle(stream), int(bool(sync)))
 
@@ -85,9 +89,9 @@ class Diffusion3D(Kernel):
             return T2, T, Ci, lam, 0.0, dt, hx, hy, hz
         return T2, T, Ci, None, lam, dt, hx, hy, hz
 
-    def launch(self, args, memopt, loopsize, ranges, stream, sync):
+    def launch(self, args, memopt, loopsize, ranges, stream, sync, fp64="ieee"):
         T2, T, Ci, lam_arr, lam, dt, hx, hy, hz = self.split_args(args)
-        cfg = _launch_cfg(memopt, loopsize, ranges)
+        cfg = _launch_cfg(memopt, loopsize, ranges, fp64)
         _lib.call("ps_diffusion3d_step", self.form, descriptor(T2), descriptor(T), descriptor(Ci),
                   descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), ctypes.byref(cfg),
                   stream_handle(stream), int(bool(sync)))
@@ -97,7 +101,7 @@ class Diffusion3D(Kernel):
 class Acoustic3D(Kernel):
     which: str
 
-    def launch(self, args, memopt, loopsize, ranges, stream, sync):
+    def launch(self, args, memopt, loopsize, ranges, stream, sync, fp64="ieee"):
         if ranges is not None:
             raise ArgumentError(f"{self.name}: explicit ranges are not supported")
         if self.which == "V":
@@ -161,7 +165,7 @@ def from_source(body: str, ndims: int = 3):
     raise ArgumentError("unsupported @parallel kernel body for the GB300 package")
 
 
-def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True):
+def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True, fp64="ieee"):
     """`@parallel [ranges] [memopt=...] kernel!(args...)`."""
     require_initialized()
     if isinstance(kernel, FdKernel):
@@ -176,7 +180,7 @@ def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, s
         raise ArgumentError(f"{kernel.name} takes {kernel.nargs} arguments (obtained {len(args)})")
     if memopt is None:
         memopt = default_memopt()
-    kernel.launch(args, memopt, loopsize, ranges, stream, sync)
+    kernel.launch(args, memopt, loopsize, ranges, stream, sync, fp64)
 
 
 def parallel_async(kernel, *args, **kw):
@@ -185,7 +189,8 @@ def parallel_async(kernel, *args, **kw):
     parallel(kernel, *args, **kw)
 
 
-def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, s_boundary=None, s_inner=None):
+def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, s_boundary=None, s_inner=None,
+                       fp64="ieee"):
     """`@hide_communication boundary_width begin @parallel kernel!(args...); comm() end`.
 
     The six boundary slabs run on a high-priority stream and the inner box on a normal
@@ -222,9 +227,10 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
 
     cb = _lib.COMM_FN(_cb)
     bw_arr = (ctypes.c_int64 * 3)(*[int(b) for b in bw])
+    cfg = _launch_cfg(memopt, 0, None, fp64)
     try:
         _lib.call("ps_diffusion3d_step_split", kernel.form, descriptor(T2), descriptor(T), descriptor(Ci),
-                  descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), int(bool(memopt)),
+                  descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), ctypes.byref(cfg),
                   bw_arr, s_boundary, s_inner, cb, None)
     finally:
         for s in own:

@@ -77,8 +77,8 @@ def test_stokes2d_fp64_solver_iterates_match_oracle(ps, oracle):
 def test_stokes2d_mixed_solver_matches_fp64(ps, oracle, n):
     """FP32 PT sweeps + FP64 defect correction reach the FP64 tolerance and the FP64 solution."""
     nx, ny = n
-    a, _ = _pair(ps, oracle, nx, ny, "f64", lx=1.0, musi=1e-3)
-    b, _ = _pair(ps, oracle, nx, ny, "f64", lx=1.0, musi=1e-3)
+    a, _ = _pair(ps, oracle, nx, ny, "f64", lx=1.0, musi=0.1)
+    b, _ = _pair(ps, oracle, nx, ny, "f64", lx=1.0, musi=0.1)
     tol = 1e-8
     sa = a.solve(tol=tol, mode=0, max_iter=2_000_000)
     sb = b.solve(tol=tol, mode=1, max_iter=2_000_000)
