@@ -193,6 +193,32 @@ int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci
                               ps_comm_fn comm, void* comm_ctx);
 
 /* ------------------------------------------------------------------------------------ */
+/* Adjoint of the diffusion step (replaces `@parallel ∇=(T->T̄, lam->lam̄) step!(...)`,     */
+/* src/ParallelKernel/parallel.jl:265-301, for PS_DIFF_FLUX_LAM).                         */
+/* ------------------------------------------------------------------------------------ */
+
+/* One reverse step of T2 = step(T, lam) (PS_DIFF_FLUX_LAM with h = (_dx, _dy, _dz)):
+ * lamT = (∂T2/∂T)^T lamT2 on inner cells (0 on boundary cells, whose values are constants) and
+ * glam += (∂T2/∂lam)^T lamT2. T is the step's input state. All arrays n^3, one dtype. */
+int ps_diffusion3d_adjoint_step(ps_array lamT, ps_array lamT2, ps_array T, ps_array Ci, ps_array lam, ps_array glam,
+                                double dt, double hx, double hy, double hz, void* stream, int sync);
+
+typedef struct ps_adjoint_stats {
+    double loss;               /* 0.5 * ||T_nt - T_obs||^2                  */
+    int64_t checkpoints;       /* forward states kept (one every ce steps)  */
+    int64_t recomputed_steps;  /* forward steps recomputed in the reverse sweep */
+    double seconds;
+} ps_adjoint_stats;
+
+/* Gradient of L(lam) = 0.5 ||T_nt - T_obs||^2, T_nt = nt diffusion steps (PS_DIFF_FLUX_LAM) from
+ * T0, by the adjoint with a checkpoint every `checkpoint_every` steps and recomputation of each
+ * segment. cfg selects memopt / fp64_mode of the forward steps (NULL: memopt, IEEE). FP64 arrays.
+ * dL_dlam is overwritten; T_final (ptr may be NULL) receives T_nt. Synchronises. */
+int ps_diffusion3d_misfit_gradient(ps_array T0, ps_array T_obs, ps_array Ci, ps_array lam, double dt, double hx,
+                                   double hy, double hz, int64_t nt, int64_t checkpoint_every, const ps_launch* cfg,
+                                   ps_array dL_dlam, ps_array T_final, ps_adjoint_stats* stats, void* stream);
+
+/* ------------------------------------------------------------------------------------ */
 /* acoustic3D (miniapps/acoustic3D.jl:11-21).                                            */
 /* ------------------------------------------------------------------------------------ */
 

@@ -117,6 +117,39 @@ def acoustic3d_v(Vx, Vy, Vz, P, dt, rho, dx, dy, dz) -> None:
                                             R(dy), R(dz)), "acoustic3d_v")
 
 
+def diffusion3d_adjoint_step(lamT, lamT2, T, Ci, lam, glam, dt, hx, hy, hz) -> None:
+    """One reverse step of the flux-form diffusion step (lamT overwritten, glam accumulated)."""
+    R = _real(T.dtype)
+    _check(_fn("orc_diffusion3d_adjoint_step", T.dtype)(_ptr(lamT), _ptr(lamT2), _ptr(T), _ptr(Ci), _ptr(lam),
+                                                        _ptr(glam), R(dt), R(hx), R(hy), R(hz), _n3(T)),
+           "diffusion3d_adjoint_step")
+
+
+def misfit_forward(T0, Ci, lam, dt, h, nt):
+    """nt flux-form diffusion steps from T0 (the oracle's forward; returns all states)."""
+    states = [np.asfortranarray(T0.copy())]
+    for _ in range(nt):
+        T2 = np.asfortranarray(states[-1].copy())
+        diffusion3d_step(3, T2, states[-1], Ci, lam, 0.0, dt, *h)
+        states.append(T2)
+    return states
+
+
+def misfit_gradient(T0, T_obs, Ci, lam, dt, h, nt):
+    """(loss, dL/dlam) of L = 0.5 ||T_nt - T_obs||^2 by the oracle's forward and reverse sweeps."""
+    states = misfit_forward(T0, Ci, lam, dt, h, nt)
+    r = states[-1] - T_obs
+    loss = 0.5 * float(np.sum(r * r))
+    lamT = np.asfortranarray(np.zeros_like(T0))
+    lamT[1:-1, 1:-1, 1:-1] = r[1:-1, 1:-1, 1:-1]
+    glam = np.asfortranarray(np.zeros_like(T0))
+    buf = np.asfortranarray(np.zeros_like(T0))
+    for n in range(nt - 1, -1, -1):
+        diffusion3d_adjoint_step(buf, lamT, states[n], Ci, lam, glam, dt, *h)
+        lamT, buf = buf, lamT
+    return loss, glam
+
+
 class Stokes2D:
     """The Stokes2D miniapp's arrays on the host and its kernels (miniapps/Stokes2D.jl:11-55)
     run by the oracle; same field names as ps_gb300.stokes.Stokes2D."""

@@ -176,6 +176,54 @@ int SFX(orc_diffusion3d_step)(int form, REAL* T2, const REAL* T, const REAL* Ci,
     return ORC_OK;
 }
 
+/* Adjoint of one flux-form diffusion step with a conductivity array (form 3 above).
+ * Forward: T2[c] = T[c] + dt*Ci[c]*Σ_d h_d*(-(q_d+ - q_d-)), q_d± the face fluxes with face
+ * conductivity (lam_a + lam_b)*0.5, for inner cells c; boundary cells are fixed values.
+ * Given lamT2 = ∂L/∂T2 (ignored on boundary cells), with μ = dt*Ci*lamT2 on inner cells and 0
+ * elsewhere:
+ *   lamT[c]  = lamT2[c] + Σ_d h_d² (k_d+(μ[c+e] - μ[c]) - k_d-(μ[c] - μ[c-e]))   (inner c; 0 else)
+ *   glam[c] += 0.5 Σ_{faces (a, b=a+e) of c} (μ[a] - μ[b]) h_d² (T[b] - T[a])   (all cells)
+ * This is the transpose of the forward step's Jacobian (the operator is symmetric in T). */
+int SFX(orc_diffusion3d_adjoint_step)(REAL* lamT, const REAL* lamT2, const REAL* T, const REAL* Ci, const REAL* lam,
+                                      REAL* glam, REAL dt, REAL hx, REAL hy, REAL hz, const int64_t* n) {
+    const int64_t nx = n[0], ny = n[1], nz = n[2], sy = nx, sz = nx * ny;
+    const REAL hh[3] = {hx * hx, hy * hy, hz * hz};
+    const int64_t st[3] = {1, sy, sz};
+#define INNER(i, j, k) ((i) >= 1 && (i) <= nx - 2 && (j) >= 1 && (j) <= ny - 2 && (k) >= 1 && (k) <= nz - 2)
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nz; k++)
+        for (int64_t j = 0; j < ny; j++)
+            for (int64_t i = 0; i < nx; i++) {
+                const int64_t c = OIDX(i, j, k, n);
+                const int64_t idx[3] = {i, j, k}, ext[3] = {nx, ny, nz};
+                const int inner_c = INNER(i, j, k);
+                const REAL mu_c = inner_c ? dt * Ci[c] * lamT2[c] : (REAL)0;
+                REAL acc = (REAL)0, g = (REAL)0;
+                for (int d = 0; d < 3; d++) {
+                    for (int sgn = -1; sgn <= 1; sgn += 2) {
+                        const int64_t q = idx[d] + sgn;
+                        if (q < 0 || q >= ext[d]) continue;
+                        int64_t ii = i, jj = j, kk = k;
+                        if (d == 0) ii = q;
+                        if (d == 1) jj = q;
+                        if (d == 2) kk = q;
+                        const int64_t nb = c + sgn * st[d];
+                        const REAL mu_n = INNER(ii, jj, kk) ? dt * Ci[nb] * lamT2[nb] : (REAL)0;
+                        const REAL kf = (lam[c] + lam[nb]) * (REAL)0.5;
+                        /* face (a, b) with a the lower cell */
+                        const REAL mua = sgn > 0 ? mu_c : mu_n, mub = sgn > 0 ? mu_n : mu_c;
+                        const REAL Ta = sgn > 0 ? T[c] : T[nb], Tb = sgn > 0 ? T[nb] : T[c];
+                        acc += hh[d] * kf * (mu_n - mu_c);
+                        g += (REAL)0.5 * (mua - mub) * hh[d] * (Tb - Ta);
+                    }
+                }
+                lamT[c] = inner_c ? lamT2[c] + acc : (REAL)0;
+                glam[c] += g;
+            }
+#undef INNER
+    return ORC_OK;
+}
+
 /* acoustic3D compute_V! (miniapps/acoustic3D.jl:11-16): grid (nx+1, ny+1, nz+1);
  * P is (nx, ny, nz), Vx (nx+1, ny, nz), Vy (nx, ny+1, nz), Vz (nx, ny, nz+1). */
 int SFX(orc_acoustic3d_v)(REAL* Vx, REAL* Vy, REAL* Vz, const REAL* P, const int64_t* n, REAL dt, REAL rho,

@@ -143,6 +143,18 @@ def empty(*size, dtype=None):
     return torch.empty_strided(size, tuple(strides), dtype=dt, device=f"cuda:{_state.device}")
 
 
+def empty_like(A):
+    """Uninitialised device array with the size, layout and element type of A."""
+    torch = _torch()
+    return torch.empty_strided(tuple(A.shape), tuple(A.stride()), dtype=A.dtype, device=A.device)
+
+
+def zeros_like(A):
+    Z = empty_like(A)
+    fill_(Z, 0.0)
+    return Z
+
+
 def zeros(*size, dtype=None):
     """`@zeros(size...)`."""
     A = empty(*size, dtype=dtype)

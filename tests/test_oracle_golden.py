@@ -112,3 +112,26 @@ def test_oracle_stokes2d_vs_broadcasting(oracle, golden, dtn):
     for k in ("Pt", "Vx", "Vy", "divV", "txx", "tyy", "txy", "Rx", "Ry", "dVxdtau", "dVydtau"):
         assert np.array_equal(s[k], g[k]), k
     assert s.err()[0] > 0
+
+
+def test_oracle_adjoint_matches_finite_differences(oracle):
+    """The oracle's reverse sweep (the restatement the GPU adjoint is checked against) agrees
+    with central finite differences of its own forward solver on random directions."""
+    rng = np.random.default_rng(4)
+    n = (10, 9, 8)
+    T0 = np.asfortranarray(rng.random(n))
+    Ci = np.asfortranarray(0.5 + rng.random(n))
+    lam = np.asfortranarray(np.exp(0.3 * rng.standard_normal(n)))
+    T_obs = np.asfortranarray(T0 + 0.1 * rng.standard_normal(n))
+    h = (9.0, 8.0, 7.0)
+    dt = (1 / 9.0) ** 2 / lam.max() / 8.1
+    nt = 6
+    _, g = oracle.misfit_gradient(T0, T_obs, Ci, lam, dt, h, nt)
+    for _ in range(4):
+        v = np.asfortranarray(rng.standard_normal(n))
+        eps = 1e-6
+        lp, _ = oracle.misfit_gradient(T0, T_obs, Ci, np.asfortranarray(lam + eps * v), dt, h, nt)
+        lm, _ = oracle.misfit_gradient(T0, T_obs, Ci, np.asfortranarray(lam - eps * v), dt, h, nt)
+        fd = (lp - lm) / (2 * eps)
+        ad = float(np.sum(g * v))
+        assert abs(fd - ad) <= 1e-6 * max(1.0, abs(ad)), (fd, ad)
