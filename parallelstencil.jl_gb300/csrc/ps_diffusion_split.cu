@@ -18,6 +18,8 @@
 // and of Ci land in a shared-memory ring; each plane is converted in place once (every value is
 // split exactly once per step), face fluxes are shared between the two cells of a face (x faces
 // inside a thread, y faces through shared memory, z faces through registers).
+#include <stdlib.h>
+
 #include <algorithm>
 
 #include "ps_common.cuh"
@@ -70,25 +72,25 @@ __device__ __forceinline__ dd dd_mul(dd a, dd b) {
 }
 
 struct SplitParams {
-    dd c[3];    // per-dimension coefficients (unused when ISO)
-    dd g;       // δ = (Ci * g) * Σ_d c_d (F_d+ - F_d-)
+    dd c[3];  // per-dimension coefficients (unused when ISO)
+    dd g;     // δ = (Ci * g) * Σ_d c_d (F_d+ - F_d-)
 };
 
-constexpr int SP_TY = 8;   // rows (warps) per CTA
 constexpr int SP_TX = 64;  // cells per row (32 lanes x 2)
-constexpr int SP_S = 4;    // TMA ring stages
 
-template <bool LAM>
+template <bool LAM, int TY, int S>
 struct SplitCfg {
     static constexpr int PW = SP_TX + 4;  // staged plane: x in [X0-2, X0+66) keeps TMA x 16-byte aligned
-    static constexpr int PH = SP_TY + 2;
+    static constexpr int PH = TY + 2;
     static constexpr int PLANE = ((PW * PH * 8 + 127) / 128) * 128;
-    static constexpr int CIB = SP_TX * SP_TY * 8;
+    static constexpr int CIB = SP_TX * TY * 8;
     static constexpr int STAGE = PLANE * (LAM ? 2 : 1) + CIB;
-    static constexpr uint32_t TX_BYTES = (uint32_t)(PW * PH * 8 * (LAM ? 2 : 1) + SP_TX * SP_TY * 8);
-    static constexpr int FACE = (SP_TY + 1) * SP_TX * 8;  // y-face fluxes, one float2 per cell
-    static constexpr int HALO = 2 * PH + 2 * SP_TX;       // converted halo values per array
-    static constexpr int SMEM = SP_S * STAGE + FACE + 8 * SP_S;
+    static constexpr uint32_t TX_BYTES = (uint32_t)(PW * PH * 8 * (LAM ? 2 : 1) + SP_TX * TY * 8);
+    static constexpr int FACE = (TY + 1) * SP_TX * 8;  // y-face fluxes, one float2 per cell
+    static constexpr int HALO = 2 * PH + 2 * SP_TX;    // converted halo values per array
+    static constexpr int NHALO = HALO * (LAM ? 2 : 1);
+    static constexpr int HPT = (NHALO + 32 * TY - 1) / (32 * TY);  // halo values per thread
+    static constexpr int SMEM = S * STAGE + FACE + 8 * S;
 };
 
 // Face flux between cells a (lower) and b (upper): K*D (LAM) or D, D = T_b - T_a, K = l_a + l_b.
@@ -99,81 +101,85 @@ __device__ __forceinline__ dd face(dd Ta, dd Tb, dd la, dd lb) {
     return D;
 }
 
-template <bool LAM, bool ISO>
-__global__ void __launch_bounds__(32 * SP_TY, 3) diff3d_split_tma(const __grid_constant__ CUtensorMap mT,
-                                                               const __grid_constant__ CUtensorMap mL,
-                                                               const __grid_constant__ CUtensorMap mC,
-                                                               double* __restrict__ T2, SplitParams p, int64_t nx,
-                                                               int64_t ny, Box cb, int L, int* __restrict__ err) {
-    using C = SplitCfg<LAM>;
+template <bool LAM, bool ISO, int TY, int S, int MINB>
+__global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_constant__ CUtensorMap mT,
+                                                                  const __grid_constant__ CUtensorMap mL,
+                                                                  const __grid_constant__ CUtensorMap mC,
+                                                                  double* __restrict__ T2, SplitParams p, int64_t nx,
+                                                                  int64_t ny, Box cb, int L, int* __restrict__ err) {
+    using C = SplitCfg<LAM, TY, S>;
     extern __shared__ __align__(128) unsigned char smem[];
-    float2* faceY = reinterpret_cast<float2*>(smem + SP_S * C::STAGE);  // [SP_TY+1][SP_TX]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SP_S * C::STAGE + C::FACE);
+    float2* faceY = reinterpret_cast<float2*>(smem + S * C::STAGE);  // [TY+1][SP_TX]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + C::FACE);
 
     const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
     const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
-    const int Y0 = (int)cb.lo[1] + blockIdx.y * SP_TY;
+    const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
     const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
     const int nk = min(L, (int)cb.hi[2] - Z0);
     const int nq = nk + 2;
 
-    auto tslot = [&](int q) { return reinterpret_cast<double*>(smem + (q % SP_S) * C::STAGE); };
-    auto lslot = [&](int q) { return reinterpret_cast<double*>(smem + (q % SP_S) * C::STAGE + C::PLANE); };
-    auto cslot = [&](int q) {
-        return reinterpret_cast<double*>(smem + (q % SP_S) * C::STAGE + C::PLANE * (LAM ? 2 : 1));
-    };
-
+    auto slot = [&](int q) { return smem + (q % S) * C::STAGE; };
     if (tid == 0) {
         prefetch_tensormap(&mT);
         if constexpr (LAM) prefetch_tensormap(&mL);
         prefetch_tensormap(&mC);
-        for (int s = 0; s < SP_S; s++) mbar_init(&bar[s], 1);
+        for (int s = 0; s < S; s++) mbar_init(&bar[s], 1);
         fence_mbar_init();
     }
     __syncthreads();
     int next_q = 0;
     auto issue = [&](int q) {
-        int s = q % SP_S, z = Z0 - 1 + q;
+        unsigned char* b = slot(q);
+        int s = q % S, z = Z0 - 1 + q;
         mbar_arrive_expect_tx(&bar[s], C::TX_BYTES);
-        tma_load_3d(tslot(q), &mT, &bar[s], X0 - 2, Y0 - 1, z);
-        if constexpr (LAM) tma_load_3d(lslot(q), &mL, &bar[s], X0 - 2, Y0 - 1, z);
-        tma_load_3d(cslot(q), &mC, &bar[s], X0, Y0, z);
+        tma_load_3d(b, &mT, &bar[s], X0 - 2, Y0 - 1, z);
+        if constexpr (LAM) tma_load_3d(b + C::PLANE, &mL, &bar[s], X0 - 2, Y0 - 1, z);
+        tma_load_3d(b + C::PLANE * (LAM ? 2 : 1), &mC, &bar[s], X0, Y0, z);
     };
     if (tid == 0)
-        for (; next_q < min(SP_S, nq); ++next_q) issue(next_q);
+        for (; next_q < min(S, nq); ++next_q) issue(next_q);
 
-    const int col = 2 + 2 * lx;  // staged-plane column of this thread's first cell
-    const int py = 1 + ly;
-    const int own = py * C::PW + col;
+    const int own = (1 + ly) * C::PW + 2 + 2 * lx;  // staged-plane index of this thread's first cell
     const int64_t gx = X0 + 2 * lx, gy = Y0 + ly;
     const bool row_in = gy >= cb.lo[1] && gy < cb.hi[1];
     const bool in0 = row_in && gx >= cb.lo[0] && gx < cb.hi[0];
     const bool in1 = row_in && gx + 1 >= cb.lo[0] && gx + 1 < cb.hi[0];
+    // this thread's halo values (byte offsets inside a stage; -1 = none): columns 1 and PW-2 of
+    // every row, then rows 0 and PH-1 of the interior columns; T first, then lam
+    int hoff[C::HPT];
+#pragma unroll
+    for (int r = 0; r < C::HPT; r++) {
+        const int h = tid + r * 32 * TY;
+        const int a = h % C::HALO;
+        const int idx = a < 2 * C::PH ? (a % C::PH) * C::PW + (a < C::PH ? 1 : C::PW - 2)
+                                      : ((a - 2 * C::PH) < SP_TX ? 0 : (C::PH - 1)) * C::PW + 2 + ((a - 2 * C::PH) % SP_TX);
+        hoff[r] = h < C::NHALO ? (h < C::HALO ? 0 : C::PLANE) + idx * 8 : -1;
+    }
 
     bool big = false, timed_out = false;
-    // Converts plane q in place: own cells (returned, raw T kept) and this thread's halo share.
+    // Converts plane q in place: own cells (returned, raw T kept) and this thread's halo values.
     auto convert = [&](int q, dd* Tn, dd* ln, double2& rawT) {
-        double* tp = tslot(q);
+        unsigned char* b = slot(q);
+        double* tp = reinterpret_cast<double*>(b);
         rawT = *reinterpret_cast<const double2*>(tp + own);
         Tn[0] = dd_split(rawT.x, big);
         Tn[1] = dd_split(rawT.y, big);
         *reinterpret_cast<float4*>(tp + own) = make_float4(Tn[0].h, Tn[0].l, Tn[1].h, Tn[1].l);
         if constexpr (LAM) {
-            double* lp = lslot(q);
+            double* lp = reinterpret_cast<double*>(b + C::PLANE);
             double2 r = *reinterpret_cast<const double2*>(lp + own);
             ln[0] = dd_split(r.x, big);
             ln[1] = dd_split(r.y, big);
             *reinterpret_cast<float4*>(lp + own) = make_float4(ln[0].h, ln[0].l, ln[1].h, ln[1].l);
         }
-        // halo: columns 1 and PW-2 of every row, rows 0 and PH-1 of the interior columns
-        for (int h = tid; h < C::HALO * (LAM ? 2 : 1); h += 32 * SP_TY) {
-            int a = h % C::HALO;
-            double* base = (h < C::HALO) ? tp : lslot(q);
-            int idx = a < 2 * C::PH ? (a % C::PH) * C::PW + (a < C::PH ? 1 : C::PW - 2)
-                                    : ((a - 2 * C::PH) < SP_TX ? 0 : (C::PH - 1)) * C::PW + 2 +
-                                          ((a - 2 * C::PH) % SP_TX);
-            dd v = dd_split(base[idx], big);
-            *reinterpret_cast<float2*>(base + idx) = make_float2(v.h, v.l);
+#pragma unroll
+        for (int r = 0; r < C::HPT; r++) {
+            if (hoff[r] >= 0) {
+                double* v = reinterpret_cast<double*>(b + hoff[r]);
+                dd d = dd_split(*v, big);
+                *reinterpret_cast<float2*>(v) = make_float2(d.h, d.l);
+            }
         }
     };
     auto ld2 = [&](const double* plane, int off) {
@@ -196,14 +202,16 @@ __global__ void __launch_bounds__(32 * SP_TY, 3) diff3d_split_tma(const __grid_c
 
     for (int k = 0; k < nk; ++k) {
         const int q = k + 2;
-        timed_out |= !mbar_wait_bounded(&bar[q % SP_S], (q / SP_S) & 1);
+        timed_out |= !mbar_wait_bounded(&bar[q % S], (q / S) & 1);
         if (!timed_out) convert(q, Tz, lz, rawTz);
         __syncthreads();  // A: plane q converted
-        const double* tp = tslot(k + 1);
-        const double* lp = LAM ? lslot(k + 1) : nullptr;
+        const unsigned char* b1 = slot(k + 1);
+        const double* tp = reinterpret_cast<const double*>(b1);
+        const double* lp = reinterpret_cast<const double*>(b1 + C::PLANE);
         dd Fx[3], Fym[2], Fzp[2], ci[2];
         if (!timed_out) {
-            double2 rc = *reinterpret_cast<const double2*>(cslot(k + 1) + ly * SP_TX + 2 * lx);
+            double2 rc = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(b1 + C::PLANE * (LAM ? 2 : 1)) +
+                                                           ly * SP_TX + 2 * lx);
             ci[0] = dd_split(rc.x, big);
             ci[1] = dd_split(rc.y, big);
             // x faces: left of cell 0, between the cells, right of cell 1
@@ -225,12 +233,12 @@ __global__ void __launch_bounds__(32 * SP_TY, 3) diff3d_split_tma(const __grid_c
                 *reinterpret_cast<float4*>(faceY + ly * SP_TX + 2 * lx) =
                     make_float4(Fym[0].h, Fym[0].l, Fym[1].h, Fym[1].l);
             }
-            if (ly == SP_TY - 1) {
+            if (ly == TY - 1) {
                 float4 ta = *reinterpret_cast<const float4*>(tp + own + C::PW);
                 float4 la = LAM ? *reinterpret_cast<const float4*>(lp + own + C::PW) : make_float4(0, 0, 0, 0);
                 dd f0 = face<LAM>(Tc[0], dd{ta.x, ta.y}, lc[0], dd{la.x, la.y});
                 dd f1 = face<LAM>(Tc[1], dd{ta.z, ta.w}, lc[1], dd{la.z, la.w});
-                *reinterpret_cast<float4*>(faceY + SP_TY * SP_TX + 2 * lx) = make_float4(f0.h, f0.l, f1.h, f1.l);
+                *reinterpret_cast<float4*>(faceY + TY * SP_TX + 2 * lx) = make_float4(f0.h, f0.l, f1.h, f1.l);
             }
 #pragma unroll
             for (int j = 0; j < 2; j++) Fzp[j] = face<LAM>(Tc[j], Tz[j], lc[j], lz[j]);
@@ -239,31 +247,31 @@ __global__ void __launch_bounds__(32 * SP_TY, 3) diff3d_split_tma(const __grid_c
         if (__syncthreads_or(timed_out)) {
             if (tid == 0) {
                 atomicOr(err, DEV_ERR_TMA_TIMEOUT);
-                for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % SP_S], (r / SP_S) & 1);
+                for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % S], (r / S) & 1);
             }
             return;
         }
         if (tid == 0)
-            for (; next_q < min(nq, k + 2 + SP_S); ++next_q) issue(next_q);
+            for (; next_q < min(nq, k + 2 + S); ++next_q) issue(next_q);
         float4 fa = *reinterpret_cast<const float4*>(faceY + (ly + 1) * SP_TX + 2 * lx);
         dd Fyp[2] = {dd{fa.x, fa.y}, dd{fa.z, fa.w}};
         double out[2];
         const double rawc[2] = {rawTc.x, rawTc.y};
 #pragma unroll
         for (int j = 0; j < 2; j++) {
-            dd S;
+            dd Sm;
             if constexpr (ISO) {
-                S = dd_sub(Fx[j + 1], Fx[j]);
-                S = dd_add(S, Fyp[j]);
-                S = dd_sub(S, Fym[j]);
-                S = dd_add(S, Fzp[j]);
-                S = dd_sub(S, Fzm[j]);
+                Sm = dd_sub(Fx[j + 1], Fx[j]);
+                Sm = dd_add(Sm, Fyp[j]);
+                Sm = dd_sub(Sm, Fym[j]);
+                Sm = dd_add(Sm, Fzp[j]);
+                Sm = dd_sub(Sm, Fzm[j]);
             } else {
-                S = dd_mul(p.c[0], dd_sub(Fx[j + 1], Fx[j]));
-                S = dd_add(S, dd_mul(p.c[1], dd_sub(Fyp[j], Fym[j])));
-                S = dd_add(S, dd_mul(p.c[2], dd_sub(Fzp[j], Fzm[j])));
+                Sm = dd_mul(p.c[0], dd_sub(Fx[j + 1], Fx[j]));
+                Sm = dd_add(Sm, dd_mul(p.c[1], dd_sub(Fyp[j], Fym[j])));
+                Sm = dd_add(Sm, dd_mul(p.c[2], dd_sub(Fzp[j], Fzm[j])));
             }
-            dd delta = dd_mul(dd_mul(ci[j], p.g), S);
+            dd delta = dd_mul(dd_mul(ci[j], p.g), Sm);
             out[j] = (rawc[j] + f32_to_f64(delta.h)) + f32_to_f64(delta.l);
         }
         const int64_t gz = Z0 + k;
@@ -291,6 +299,53 @@ static void split_const(dd& d, double v) {
     d.l = (float)(v - (double)h);
 }
 
+template <bool LAM, bool ISO, int TY, int S, int MINB>
+static int launch_split_variant(const CUtensorMap& mT, const CUtensorMap& mL, const CUtensorMap& mC, double* out,
+                                const SplitParams& p, const ps_array& T2, const Box& cb, int L, cudaStream_t s,
+                                int* d_err) {
+    using C = SplitCfg<LAM, TY, S>;
+    static bool attr = false;
+    if (!attr) {
+        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_split_tma<LAM, ISO, TY, S, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+        attr = true;
+    }
+    int64_t x0 = cb.lo[0] & ~(int64_t)1;
+    dim3 blk(32, TY, 1);
+    dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
+             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    diff3d_split_tma<LAM, ISO, TY, S, MINB><<<grd, blk, C::SMEM, s>>>(mT, mL, mC, out, p, T2.n[0], T2.n[1], cb, L,
+                                                                      d_err);
+    return PS_OK;
+}
+
+// Tile height of the split kernel: PS_SPLIT_TY (8 or 16) overrides the default (tuning knob).
+static int split_ty() {
+    static int ty = [] {
+        const char* e = getenv("PS_SPLIT_TY");
+        int v = e ? atoi(e) : 8;
+        return (v == 16) ? 16 : 8;
+    }();
+    return ty;
+}
+
+template <bool LAM, bool ISO>
+static int launch_split_tiled(const ps_array& Tin, const ps_array& Ci, const ps_array* lam, double* out,
+                              const SplitParams& p, const ps_array& T2, const Box& cb, int L, cudaStream_t s,
+                              int* d_err) {
+    const int TY = split_ty();
+    const int PW = SP_TX + 4, PH = TY + 2;
+    CUtensorMap mT, mL, mC;
+    PS_TRY(encode_plane_map(&mT, Tin, PW, PH));
+    if (LAM)
+        PS_TRY(encode_plane_map(&mL, *lam, PW, PH));
+    else
+        mL = mT;
+    PS_TRY(encode_plane_map(&mC, Ci, SP_TX, TY));
+    if (TY == 16) return launch_split_variant<LAM, ISO, 16, 3, 2>(mT, mL, mC, out, p, T2, cb, L, s, d_err);
+    return launch_split_variant<LAM, ISO, 8, 4, 3>(mT, mL, mC, out, p, T2, cb, L, s, d_err);
+}
+
 // Launches the split-arithmetic z-sweep; returns PS_ERR_UNSUPPORTED when the arrays are not
 // TMA-eligible (the caller then uses the IEEE kernels).
 int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
@@ -313,44 +368,12 @@ int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, co
     if (iso) g *= c[0];
     for (int d = 0; d < 3; d++) split_const(p.c[d], c[d]);
     split_const(p.g, g);
-    const bool has_lam = form == PS_DIFF_FLUX_LAM;
-    CUtensorMap mT, mL, mC;
-    const int PW = SP_TX + 4, PH = SP_TY + 2;
-    PS_TRY(encode_plane_map(&mT, Tin, PW, PH));
-    if (has_lam)
-        PS_TRY(encode_plane_map(&mL, *lam, PW, PH));
-    else
-        mL = mT;
-    PS_TRY(encode_plane_map(&mC, Ci, SP_TX, SP_TY));
-    int64_t x0 = cb.lo[0] & ~(int64_t)1;
-    dim3 blk(32, SP_TY, 1);
-    dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + SP_TY - 1) / SP_TY),
-             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
     double* out = static_cast<double*>(T2.ptr);
-#define PS_SPLIT_LAUNCH(LAMV, ISOV)                                                                              \
-    do {                                                                                                         \
-        static bool attr = false;                                                                                \
-        if (!attr) {                                                                                             \
-            PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_split_tma<LAMV, ISOV>,                                       \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, SplitCfg<LAMV>::SMEM)); \
-            attr = true;                                                                                         \
-        }                                                                                                        \
-        diff3d_split_tma<LAMV, ISOV><<<grd, blk, SplitCfg<LAMV>::SMEM, s>>>(mT, mL, mC, out, p, T2.n[0], T2.n[1], \
-                                                                            cb, L, d_err);                       \
-    } while (0)
-    if (has_lam) {
-        if (iso)
-            PS_SPLIT_LAUNCH(true, true);
-        else
-            PS_SPLIT_LAUNCH(true, false);
-    } else {
-        if (iso)
-            PS_SPLIT_LAUNCH(false, true);
-        else
-            PS_SPLIT_LAUNCH(false, false);
-    }
-#undef PS_SPLIT_LAUNCH
-    return PS_OK;
+    if (form == PS_DIFF_FLUX_LAM)
+        return iso ? launch_split_tiled<true, true>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err)
+                   : launch_split_tiled<true, false>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err);
+    return iso ? launch_split_tiled<false, true>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err)
+               : launch_split_tiled<false, false>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err);
 }
 
 }  // namespace ps
