@@ -215,12 +215,37 @@ def run_ours(a, world, rank, local):
                           "A_eff_GB": bytes_step / 1e9}
         return t_step, bytes_step
 
+    def bench_run(label, kernel, arrs, scalars, words, nn, dtype, nsteps, fp64):
+        """K steps of the time loop through one ps_diffusion3d_run call (T, T2 swapped inside)."""
+        nonlocal launches
+        T, T2, lam, Ci = arrs
+        arg = lam if kernel is ps.kernels.diffusion3D_step_flux_lam else 1.0
+        ps.kernels.run(kernel, T, T2, Ci, arg, *scalars, a.warmup, fp64=fp64, sync=False)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ps.kernels.run(kernel, T, T2, Ci, arg, *scalars, nsteps, fp64=fp64, sync=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        secs = max_over_ranks(e0.elapsed_time(e1) / 1e3)
+        launches += nsteps + (3 if fp64 != "ieee" else 0)
+        bytes_step = words * nn ** 3 * np.dtype(dtype).itemsize
+        t_step = secs / nsteps
+        results[label] = {"t_step_ms": t_step * 1e3, "T_eff_GBs": bytes_step / t_step / 1e9,
+                          "A_eff_GB": bytes_step / 1e9}
+        return t_step, bytes_step
+
     peak, peak_kind = measured_peaks()
     with ClockSampler(local) as clk:
         arrs64 = fields(np.float64, n)
-        t_head, b_head = bench_kernel("diffusion3d_flux_lam_f64_split_memopt", ps.kernels.diffusion3D_step_flux_lam,
-                                      arrs64, (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float64, a.steps,
-                                      fp64="split")
+        t_head, b_head = bench_run("diffusion3d_flux_lam_f64_split_run", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                                   (dt, _dx, _dx, _dx), WORDS_FLUX_LAM, n, np.float64, a.steps, "split")
+        bench_run("diffusion3d_flux_lam_f64_split_state_run", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                  (dt, _dx, _dx, _dx), WORDS_FLUX_LAM, n, np.float64, a.steps, "split_state")
+        bench_kernel("diffusion3d_flux_lam_f64_split_memopt_step", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                     (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float64, a.steps, fp64="split")
         # accuracy of the split-FP32 arithmetic: one step against the bit-exact IEEE kernel
         T, T2, lam, Ci = arrs64
         ref = torch.empty_like(T2)
@@ -263,12 +288,9 @@ def run_ours(a, world, rank, local):
             _lib.check(lib.ps_copy_h2d(dT2, ctypes.c_void_p(hT.data_ptr()), s))
             _lib.check(lib.ps_copy_h2d(dCi, ctypes.c_void_p(hCi.data_ptr()), s))
             _lib.check(lib.ps_copy_h2d(dlam, ctypes.c_void_p(hlam.data_ptr()), s))
-            a_, b_ = dT, dT2
-            for _ in range(NT_JOB):
-                _lib.check(lib.ps_diffusion3d_step(3, b_, a_, dCi, dlam, 0.0, dt, _dx, _dx, _dx, ctypes.byref(cfg), s,
-                                                   0))
-                a_, b_ = b_, a_
-            _lib.check(lib.ps_copy_d2h(ctypes.c_void_p(hout.data_ptr()), a_, s))
+            _lib.check(lib.ps_diffusion3d_run(3, dT, dT2, dCi, dlam, 0.0, dt, _dx, _dx, _dx, NT_JOB, ctypes.byref(cfg),
+                                              s))
+            _lib.check(lib.ps_copy_d2h(ctypes.c_void_p(hout.data_ptr()), dT, s))
 
         e2e_job()
         barrier()
@@ -316,7 +338,7 @@ def run_ours(a, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": round(b_head / t_head / 1e9, 2), "peak": peak, "unit": "GB/s",
                      "frac": round((b_head / t_head / 1e9) / peak, 4), "peak_kind": f"{peak_kind} hbm_gbs (burst)",
                      "traffic": ncu_traffic("diffusion3d_split_flux_lam_f64_512"),
-                     "kernel": "diff3d_split_tma<LAM=true,ISO=true>", "algorithmic_bytes_per_launch": b_head},
+                     "kernel": "diff3d_split_tma<LAM,ISO,PRE>", "algorithmic_bytes_per_launch": b_head},
         "e2e": {"value": round(world * e2e_bytes / t_e2e / 1e9, 2), "unit": "GB/s",
                 "h2d_bytes_per_step": 4 * n ** 3 * 8, "d2h_bytes_per_step": n ** 3 * 8,
                 "step": f"one {NT_JOB}-step diffusion job from pinned host buffers through the C ABI",

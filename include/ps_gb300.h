@@ -75,7 +75,10 @@ typedef struct ps_launch {
     int32_t reserved;
 } ps_launch;
 
-enum { PS_FP64_IEEE = 0, PS_FP64_SPLIT = 1 };
+/* PS_FP64_SPLIT_STATE (multi-step runs only, see ps_diffusion3d_run): as PS_FP64_SPLIT, but the
+ * state between steps is kept as split pairs (8 bytes per value, as FP64) in library scratch and
+ * converted from / to IEEE doubles at the start / end of the run. */
+enum { PS_FP64_IEEE = 0, PS_FP64_SPLIT = 1, PS_FP64_SPLIT_STATE = 2 };
 
 /* ------------------------------------------------------------------------------------ */
 /* Core: device, memory, streams.                                                        */
@@ -176,6 +179,16 @@ typedef enum {
 int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr,
                         double lam, double dt, double hx, double hy, double hz,
                         const ps_launch* cfg, void* stream, int sync);
+
+/* The time loop of the examples, `for it = 1:nt; @parallel diffusion3D_step!(T2, T, ...);
+ * T, T2 = T2, T; end` (examples/diffusion3D_novis_noperf.jl:43-46), as one call. On return T
+ * holds the state after nt steps (the boundary values of T and T2 must agree, as in the
+ * examples' `T2 .= T`); T2's interior is workspace. cfg->memopt and cfg->fp64_mode apply; with
+ * PS_FP64_SPLIT / PS_FP64_SPLIT_STATE the static arrays lam and Ci are split once per call into
+ * library scratch (grow-only, freed by ps_finalize), so each step converts only T (SPLIT) or
+ * nothing (SPLIT_STATE). Asynchronous on `stream`. */
+int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_array Ci, ps_array lam_arr, double lam, double dt,
+                       double hx, double hy, double hz, int64_t nt, const ps_launch* cfg, void* stream);
 
 /* Host callback run by the split launcher once the boundary slabs are complete: the
  * communication / boundary-condition slot of `@hide_communication`. */

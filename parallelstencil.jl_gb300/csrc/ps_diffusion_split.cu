@@ -86,12 +86,16 @@ struct SplitCfg {
     static constexpr int CIB = SP_TX * TY * 8;
     static constexpr int STAGE = PLANE * (LAM ? 2 : 1) + CIB;
     static constexpr uint32_t TX_BYTES = (uint32_t)(PW * PH * 8 * (LAM ? 2 : 1) + SP_TX * TY * 8);
-    static constexpr int FACE = (TY + 1) * SP_TX * 8;  // y-face fluxes, one float2 per cell
-    static constexpr int HALO = 2 * PH + 2 * SP_TX;    // converted halo values per array
-    static constexpr int NHALO = HALO * (LAM ? 2 : 1);
-    static constexpr int HPT = (NHALO + 32 * TY - 1) / (32 * TY);  // halo values per thread
-    static constexpr int SMEM = S * STAGE + FACE + 8 * S;
+    static constexpr int FACE = (TY + 1) * SP_TX * 8;  // y-face fluxes, one float2 per cell (x2 buffers)
+    static constexpr int HALO = 2 * PH + 2 * SP_TX;    // halo values per staged array
+    static constexpr int SMEM = S * STAGE + 2 * FACE + 8 * S;
 };
+
+// dd normalisation (fast two-sum; |a.l| is small against |a.h|)
+__device__ __forceinline__ dd dd_norm(dd a) {
+    const float s = a.h + a.l;
+    return {s, a.l - (s - a.h)};
+}
 
 // Face flux between cells a (lower) and b (upper): K*D (LAM) or D, D = T_b - T_a, K = l_a + l_b.
 template <bool LAM>
@@ -101,16 +105,22 @@ __device__ __forceinline__ dd face(dd Ta, dd Tb, dd la, dd lb) {
     return D;
 }
 
-template <bool LAM, bool ISO, int TY, int S, int MINB>
+// PRE:   lam and Ci arrays already hold split pairs (float2 per cell, 8 bytes like a double).
+// STATE: T and T2 hold split pairs too (the state of a multi-step run); otherwise IEEE doubles.
+template <bool LAM, bool ISO, int TY, int S, int MINB, bool PRE, bool STATE>
 __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_constant__ CUtensorMap mT,
                                                                   const __grid_constant__ CUtensorMap mL,
                                                                   const __grid_constant__ CUtensorMap mC,
                                                                   double* __restrict__ T2, SplitParams p, int64_t nx,
                                                                   int64_t ny, Box cb, int L, int* __restrict__ err) {
     using C = SplitCfg<LAM, TY, S>;
+    // staged arrays converted in place each step: T (unless STATE) and lam (unless PRE)
+    constexpr int NCONV = (STATE ? 0 : 1) + ((LAM && !PRE) ? 1 : 0);
+    constexpr int NHALO = C::HALO * NCONV;
+    constexpr int HPT = NHALO > 0 ? (NHALO + 32 * TY - 1) / (32 * TY) : 1;
     extern __shared__ __align__(128) unsigned char smem[];
-    float2* faceY = reinterpret_cast<float2*>(smem + S * C::STAGE);  // [TY+1][SP_TX]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + C::FACE);
+    float2* faceY0 = reinterpret_cast<float2*>(smem + S * C::STAGE);  // 2 x [TY+1][SP_TX]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + 2 * C::FACE);
 
     const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
     const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
@@ -147,38 +157,53 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
     const bool in1 = row_in && gx + 1 >= cb.lo[0] && gx + 1 < cb.hi[0];
     // this thread's halo values (byte offsets inside a stage; -1 = none): columns 1 and PW-2 of
     // every row, then rows 0 and PH-1 of the interior columns; T first, then lam
-    int hoff[C::HPT];
+    int hoff[HPT];
 #pragma unroll
-    for (int r = 0; r < C::HPT; r++) {
+    for (int r = 0; r < HPT; r++) {
         const int h = tid + r * 32 * TY;
         const int a = h % C::HALO;
         const int idx = a < 2 * C::PH ? (a % C::PH) * C::PW + (a < C::PH ? 1 : C::PW - 2)
                                       : ((a - 2 * C::PH) < SP_TX ? 0 : (C::PH - 1)) * C::PW + 2 + ((a - 2 * C::PH) % SP_TX);
-        hoff[r] = h < C::NHALO ? (h < C::HALO ? 0 : C::PLANE) + idx * 8 : -1;
+        const int base = (h < C::HALO && !STATE) ? 0 : C::PLANE;  // T plane first unless T is already split
+        hoff[r] = h < NHALO ? base + idx * 8 : -1;
     }
 
     bool big = false, timed_out = false;
-    // Converts plane q in place: own cells (returned, raw T kept) and this thread's halo values.
+    // Converts plane q in place (own cells, returned; raw T kept) and this thread's halo values.
     auto convert = [&](int q, dd* Tn, dd* ln, double2& rawT) {
         unsigned char* b = slot(q);
         double* tp = reinterpret_cast<double*>(b);
-        rawT = *reinterpret_cast<const double2*>(tp + own);
-        Tn[0] = dd_split(rawT.x, big);
-        Tn[1] = dd_split(rawT.y, big);
-        *reinterpret_cast<float4*>(tp + own) = make_float4(Tn[0].h, Tn[0].l, Tn[1].h, Tn[1].l);
+        if constexpr (STATE) {
+            float4 v = *reinterpret_cast<const float4*>(tp + own);
+            Tn[0] = dd{v.x, v.y};
+            Tn[1] = dd{v.z, v.w};
+        } else {
+            rawT = *reinterpret_cast<const double2*>(tp + own);
+            Tn[0] = dd_split(rawT.x, big);
+            Tn[1] = dd_split(rawT.y, big);
+            *reinterpret_cast<float4*>(tp + own) = make_float4(Tn[0].h, Tn[0].l, Tn[1].h, Tn[1].l);
+        }
         if constexpr (LAM) {
             double* lp = reinterpret_cast<double*>(b + C::PLANE);
-            double2 r = *reinterpret_cast<const double2*>(lp + own);
-            ln[0] = dd_split(r.x, big);
-            ln[1] = dd_split(r.y, big);
-            *reinterpret_cast<float4*>(lp + own) = make_float4(ln[0].h, ln[0].l, ln[1].h, ln[1].l);
+            if constexpr (PRE) {
+                float4 v = *reinterpret_cast<const float4*>(lp + own);
+                ln[0] = dd{v.x, v.y};
+                ln[1] = dd{v.z, v.w};
+            } else {
+                double2 r = *reinterpret_cast<const double2*>(lp + own);
+                ln[0] = dd_split(r.x, big);
+                ln[1] = dd_split(r.y, big);
+                *reinterpret_cast<float4*>(lp + own) = make_float4(ln[0].h, ln[0].l, ln[1].h, ln[1].l);
+            }
         }
+        if constexpr (NHALO > 0) {
 #pragma unroll
-        for (int r = 0; r < C::HPT; r++) {
-            if (hoff[r] >= 0) {
-                double* v = reinterpret_cast<double*>(b + hoff[r]);
-                dd d = dd_split(*v, big);
-                *reinterpret_cast<float2*>(v) = make_float2(d.h, d.l);
+            for (int r = 0; r < HPT; r++) {
+                if (hoff[r] >= 0) {
+                    double* v = reinterpret_cast<double*>(b + hoff[r]);
+                    dd d = dd_split(*v, big);
+                    *reinterpret_cast<float2*>(v) = make_float2(d.h, d.l);
+                }
             }
         }
     };
@@ -204,16 +229,23 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
         const int q = k + 2;
         timed_out |= !mbar_wait_bounded(&bar[q % S], (q / S) & 1);
         if (!timed_out) convert(q, Tz, lz, rawTz);
-        __syncthreads();  // A: plane q converted
+        if constexpr (NCONV > 0) __syncthreads();  // A: plane q converted in place
+        float2* faceY = faceY0 + (k & 1) * (TY + 1) * SP_TX;
         const unsigned char* b1 = slot(k + 1);
         const double* tp = reinterpret_cast<const double*>(b1);
         const double* lp = reinterpret_cast<const double*>(b1 + C::PLANE);
         dd Fx[3], Fym[2], Fzp[2], ci[2];
         if (!timed_out) {
-            double2 rc = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(b1 + C::PLANE * (LAM ? 2 : 1)) +
-                                                           ly * SP_TX + 2 * lx);
-            ci[0] = dd_split(rc.x, big);
-            ci[1] = dd_split(rc.y, big);
+            const double* cp = reinterpret_cast<const double*>(b1 + C::PLANE * (LAM ? 2 : 1)) + ly * SP_TX + 2 * lx;
+            if constexpr (PRE) {
+                float4 v = *reinterpret_cast<const float4*>(cp);
+                ci[0] = dd{v.x, v.y};
+                ci[1] = dd{v.z, v.w};
+            } else {
+                double2 rc = *reinterpret_cast<const double2*>(cp);
+                ci[0] = dd_split(rc.x, big);
+                ci[1] = dd_split(rc.y, big);
+            }
             // x faces: left of cell 0, between the cells, right of cell 1
             dd Txm = ld2(tp, own - 1), Txp = ld2(tp, own + 2);
             dd lxm{0.f, 0.f}, lxp{0.f, 0.f};
@@ -272,7 +304,12 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
                 Sm = dd_add(Sm, dd_mul(p.c[2], dd_sub(Fzp[j], Fzm[j])));
             }
             dd delta = dd_mul(dd_mul(ci[j], p.g), Sm);
-            out[j] = (rawc[j] + f32_to_f64(delta.h)) + f32_to_f64(delta.l);
+            if constexpr (STATE) {
+                dd r = dd_norm(dd_add(Tc[j], delta));
+                out[j] = __hiloint2double(__float_as_int(r.l), __float_as_int(r.h));  // (h, l) bit pair
+            } else {
+                out[j] = (rawc[j] + f32_to_f64(delta.h)) + f32_to_f64(delta.l);
+            }
         }
         const int64_t gz = Z0 + k;
         double* dst = T2 + gx + nx * (gy + ny * gz);
@@ -299,14 +336,21 @@ static void split_const(dd& d, double v) {
     d.l = (float)(v - (double)h);
 }
 
-template <bool LAM, bool ISO, int TY, int S, int MINB>
-static int launch_split_variant(const CUtensorMap& mT, const CUtensorMap& mL, const CUtensorMap& mC, double* out,
-                                const SplitParams& p, const ps_array& T2, const Box& cb, int L, cudaStream_t s,
-                                int* d_err) {
+template <bool LAM, bool ISO, bool PRE, bool STATE>
+static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const ps_array* lam, const ps_array& T2,
+                                const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err) {
+    constexpr int TY = 8, S = 4, MINB = 3;
     using C = SplitCfg<LAM, TY, S>;
+    CUtensorMap mT, mL, mC;
+    PS_TRY(encode_plane_map(&mT, Tin, C::PW, C::PH));
+    if (LAM)
+        PS_TRY(encode_plane_map(&mL, *lam, C::PW, C::PH));
+    else
+        mL = mT;
+    PS_TRY(encode_plane_map(&mC, Ci, SP_TX, TY));
     static bool attr = false;
     if (!attr) {
-        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_split_tma<LAM, ISO, TY, S, MINB>,
+        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
         attr = true;
     }
@@ -314,43 +358,28 @@ static int launch_split_variant(const CUtensorMap& mT, const CUtensorMap& mL, co
     dim3 blk(32, TY, 1);
     dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
              (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
-    diff3d_split_tma<LAM, ISO, TY, S, MINB><<<grd, blk, C::SMEM, s>>>(mT, mL, mC, out, p, T2.n[0], T2.n[1], cb, L,
-                                                                      d_err);
+    diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE><<<grd, blk, C::SMEM, s>>>(
+        mT, mL, mC, static_cast<double*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err);
     return PS_OK;
 }
 
-// Tile height of the split kernel: PS_SPLIT_TY (8 or 16) overrides the default (tuning knob).
-static int split_ty() {
-    static int ty = [] {
-        const char* e = getenv("PS_SPLIT_TY");
-        int v = e ? atoi(e) : 8;
-        return (v == 16) ? 16 : 8;
-    }();
-    return ty;
-}
-
 template <bool LAM, bool ISO>
-static int launch_split_tiled(const ps_array& Tin, const ps_array& Ci, const ps_array* lam, double* out,
-                              const SplitParams& p, const ps_array& T2, const Box& cb, int L, cudaStream_t s,
+static int launch_split_flags(bool pre, bool state, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                              const ps_array& T2, const SplitParams& p, const Box& cb, int L, cudaStream_t s,
                               int* d_err) {
-    const int TY = split_ty();
-    const int PW = SP_TX + 4, PH = TY + 2;
-    CUtensorMap mT, mL, mC;
-    PS_TRY(encode_plane_map(&mT, Tin, PW, PH));
-    if (LAM)
-        PS_TRY(encode_plane_map(&mL, *lam, PW, PH));
-    else
-        mL = mT;
-    PS_TRY(encode_plane_map(&mC, Ci, SP_TX, TY));
-    if (TY == 16) return launch_split_variant<LAM, ISO, 16, 3, 2>(mT, mL, mC, out, p, T2, cb, L, s, d_err);
-    return launch_split_variant<LAM, ISO, 8, 4, 3>(mT, mL, mC, out, p, T2, cb, L, s, d_err);
+    if (pre)
+        return state ? launch_split_variant<LAM, ISO, true, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err)
+                     : launch_split_variant<LAM, ISO, true, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err);
+    return state ? launch_split_variant<LAM, ISO, false, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err)
+                 : launch_split_variant<LAM, ISO, false, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err);
 }
 
-// Launches the split-arithmetic z-sweep; returns PS_ERR_UNSUPPORTED when the arrays are not
-// TMA-eligible (the caller then uses the IEEE kernels).
-int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
-                           double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
-                           cudaStream_t s, int* d_err) {
+// Split-arithmetic z-sweep over the cell box cb. pre: lam / Ci hold split pairs; state: T / T2
+// hold split pairs. Returns PS_ERR_UNSUPPORTED when the arrays are not TMA-eligible (the caller
+// then uses the IEEE kernels).
+static int launch_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                        double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L, bool pre,
+                        bool state, cudaStream_t s, int* d_err) {
     bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
     if (!tma || T2.dtype != PS_F64) return PS_ERR_UNSUPPORTED;
     SplitParams p{};
@@ -368,12 +397,132 @@ int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, co
     if (iso) g *= c[0];
     for (int d = 0; d < 3; d++) split_const(p.c[d], c[d]);
     split_const(p.g, g);
-    double* out = static_cast<double*>(T2.ptr);
     if (form == PS_DIFF_FLUX_LAM)
-        return iso ? launch_split_tiled<true, true>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err)
-                   : launch_split_tiled<true, false>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err);
-    return iso ? launch_split_tiled<false, true>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err)
-               : launch_split_tiled<false, false>(Tin, Ci, lam, out, p, T2, cb, L, s, d_err);
+        return iso ? launch_split_flags<true, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err)
+                   : launch_split_flags<true, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err);
+    return iso ? launch_split_flags<false, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err)
+               : launch_split_flags<false, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err);
+}
+
+int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
+                           double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
+                           cudaStream_t s, int* d_err) {
+    return launch_split(form, T2, Tin, Ci, lam, lam_s, dt, hx, hy, hz, cb, L, false, false, s, d_err);
+}
+
+// ---- multi-step runs -------------------------------------------------------------------
+__global__ void split_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n, int* err) {
+    bool big = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd d = dd_split(in[i], big);
+        out[i] = __hiloint2double(__float_as_int(d.l), __float_as_int(d.h));
+    }
+    if (big) atomicOr(err, DEV_ERR_RANGE);
+}
+
+__global__ void join_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = in[i];
+        out[i] = f32_to_f64(__int_as_float(__double2loint(v))) + f32_to_f64(__int_as_float(__double2hiint(v)));
+    }
+}
+
+// Grow-only scratch for the split pairs of lam, Ci and the run state (freed by ps_finalize).
+static void* g_run_scratch = nullptr;
+static size_t g_run_bytes = 0;
+
+void diffusion_free_scratch() {
+    if (g_run_scratch) cudaFree(g_run_scratch);
+    g_run_scratch = nullptr;
+    g_run_bytes = 0;
+}
+
+static int run_scratch(size_t bytes, char** p) {
+    if (bytes > g_run_bytes) {
+        diffusion_free_scratch();
+        if (cudaMalloc(&g_run_scratch, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            g_run_scratch = nullptr;
+            return fail(PS_ERR_NOMEM, "ps_diffusion3d_run: scratch allocation of %zu bytes failed", bytes);
+        }
+        g_run_bytes = bytes;
+    }
+    *p = static_cast<char*>(g_run_scratch);
+    return PS_OK;
 }
 
 }  // namespace ps
+
+using namespace ps;
+
+namespace ps {
+int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam,
+                  double lam_s, double dt, double hx, double hy, double hz, const Box& thread_box, int memopt,
+                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err);
+int diffusion_args(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam);
+}
+
+extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_array Ci, ps_array lam_arr, double lam,
+                                  double dt, double hx, double hy, double hz, int64_t nt, const ps_launch* cfg,
+                                  void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(diffusion_args(form, T2, T, Ci, lam_arr));
+    if (nt < 0) return fail(PS_ERR_ARG, "ps_diffusion3d_run: nt must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int memopt = cfg ? cfg->memopt : 1, loopsize = cfg ? cfg->loopsize : 0;
+    int mode = cfg ? cfg->fp64_mode : PS_FP64_IEEE;
+    if (mode < PS_FP64_IEEE || mode > PS_FP64_SPLIT_STATE) return fail(PS_ERR_ARG, "unknown fp64_mode %d", mode);
+    const int64_t n = numel(T);
+    const size_t bytes = (size_t)n * 8;
+    const bool has_lam = form == PS_DIFF_FLUX_LAM;
+    const Box full = {{0, 0, 0}, {T.n[0], T.n[1], T.n[2]}};
+    const Box cells = {{1, 1, 1}, {T.n[0] - 1, T.n[1] - 1, T.n[2] - 1}};
+    const int L = loopsize > 0 ? loopsize : 64;
+    bool split = T.dtype == PS_F64 && mode != PS_FP64_IEEE && tma_eligible(T) && tma_eligible(T2) &&
+                 tma_eligible(Ci) && (!has_lam || tma_eligible(lam_arr)) && cells.hi[0] > cells.lo[0] &&
+                 cells.hi[1] > cells.lo[1] && cells.hi[2] > cells.lo[2];
+    ps_array A = T, B = T2;
+    if (!split) {
+        for (int64_t it = 0; it < nt; ++it) {
+            PS_TRY(diffusion_box(form, B, A, Ci, lam_arr, lam, dt, hx, hy, hz, full, memopt, loopsize, PS_FP64_IEEE, s,
+                                 st->d_err));
+            std::swap(A, B);
+        }
+    } else {
+        const bool state = mode == PS_FP64_SPLIT_STATE;
+        char* scr = nullptr;
+        const size_t need = bytes * ((has_lam ? 2 : 1) + (state ? 2 : 0));
+        PS_TRY(run_scratch(need, &scr));
+        ps_array Cs = Ci, Ls = lam_arr, Sa = T, Sb = T;
+        Cs.ptr = scr;
+        if (has_lam) Ls.ptr = scr + bytes;
+        const int g = st->num_sms * 8;
+        split_pairs_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(Ci.ptr), static_cast<double*>(Cs.ptr), n,
+                                             st->d_err);
+        if (has_lam)
+            split_pairs_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(lam_arr.ptr),
+                                                 static_cast<double*>(Ls.ptr), n, st->d_err);
+        if (state) {
+            Sa.ptr = scr + bytes * (has_lam ? 2 : 1);
+            Sb.ptr = static_cast<char*>(Sa.ptr) + bytes;
+            split_pairs_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(T.ptr), static_cast<double*>(Sa.ptr), n,
+                                                 st->d_err);
+            PS_CUDA_TRY(cudaMemcpyAsync(Sb.ptr, Sa.ptr, bytes, cudaMemcpyDeviceToDevice, s));
+            A = Sa;
+            B = Sb;
+        }
+        for (int64_t it = 0; it < nt; ++it) {
+            PS_TRY(launch_split(form, B, A, Cs, has_lam ? &Ls : nullptr, lam, dt, hx, hy, hz, cells, L, true, state, s,
+                                st->d_err));
+            std::swap(A, B);
+        }
+        if (state) {
+            join_pairs_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(A.ptr), static_cast<double*>(T.ptr), n);
+            A = T;
+        }
+    }
+    if (A.ptr != T.ptr)  // odd nt: the last state is in T2
+        PS_CUDA_TRY(cudaMemcpyAsync(T.ptr, A.ptr, (size_t)n * elsize(T.dtype), cudaMemcpyDeviceToDevice, s));
+    return finish_launch(s, 0, "ps_diffusion3d_run");
+}

@@ -617,7 +617,7 @@ static int dispatch_diffusion(int form, const ps_array& T2, const ps_array& Tin,
 
 // Validates the diffusion arguments and converts the thread box into the box of written
 // cells (`@inn(T2)` mask: c = t + 1 for 0 <= t < n - 2).
-static int diffusion_args(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci,
+int diffusion_args(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci,
                           const ps_array& lam) {
     PS_TRY(check_array(T2, "T2"));
     PS_TRY(check_array(Tin, "T"));
@@ -782,7 +782,9 @@ int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_a
     int loopsize = cfg ? cfg->loopsize : 0;
     int fp64_mode = cfg ? cfg->fp64_mode : PS_FP64_IEEE;
     if (loopsize < 0) return fail(PS_ERR_ARG, "ps_diffusion3d_step: loopsize must be >= 0");
-    if (fp64_mode != PS_FP64_IEEE && fp64_mode != PS_FP64_SPLIT) return fail(PS_ERR_ARG, "unknown fp64_mode %d", fp64_mode);
+    if (fp64_mode < PS_FP64_IEEE || fp64_mode > PS_FP64_SPLIT_STATE)
+        return fail(PS_ERR_ARG, "unknown fp64_mode %d", fp64_mode);
+    if (fp64_mode == PS_FP64_SPLIT_STATE) fp64_mode = PS_FP64_SPLIT;  // one step: the state stays IEEE
     PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, tb, memopt, loopsize, fp64_mode, s, st->d_err));
     return finish_launch(s, sync, "ps_diffusion3d_step");
 }

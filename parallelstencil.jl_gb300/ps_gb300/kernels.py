@@ -27,7 +27,10 @@ from .core import ArgumentError, default_memopt, descriptor, require_initialized
 from .fd import FdKernel, fd_kernel
 
 PS_DIFF_DIV, PS_DIFF_MUL, PS_DIFF_FLUX, PS_DIFF_FLUX_LAM = 0, 1, 2, 3
-FP64_MODES = {"ieee": 0, "split": 1}
+FP64_MODES = {"ieee": 0, "split": 1, "split_state": 2}
+
+_lib.register("ps_diffusion3d_run", [ctypes.c_int32] + [_lib.PSArray] * 4 + [ctypes.c_double] * 5 +
+              [ctypes.c_int64, ctypes.POINTER(PSLaunch), ctypes.c_void_p])
 
 
 def _launch_cfg(memopt: bool, loopsize: int, ranges, fp64: str = "ieee"):
@@ -181,6 +184,24 @@ def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, s
     if memopt is None:
         memopt = default_memopt()
     kernel.launch(args, memopt, loopsize, ranges, stream, sync, fp64)
+
+
+def run(kernel, T, T2, Ci, lam, dt, hx, hy, hz, nt, *, memopt=True, loopsize=0, fp64="ieee", stream=None,
+        sync=True):
+    """`for it = 1:nt; @parallel kernel!(T2, T, Ci, lam, dt, h...); T, T2 = T2, T; end` as one call
+    (ps_diffusion3d_run); on return T holds the state after nt steps."""
+    require_initialized()
+    if not isinstance(kernel, Diffusion3D):
+        raise ArgumentError("run() is implemented for the diffusion3D kernels")
+    _, _, _, lam_arr, lam_s, _, _, _, _ = kernel.split_args((T2, T, Ci, lam, dt, hx, hy, hz))
+    cfg = _launch_cfg(memopt, loopsize, None, fp64)
+    _lib.call("ps_diffusion3d_run", kernel.form, descriptor(T), descriptor(T2), descriptor(Ci), descriptor(lam_arr),
+              float(lam_s), float(dt), float(hx), float(hy), float(hz), int(nt), ctypes.byref(cfg),
+              stream_handle(stream))
+    if sync:
+        from .core import synchronize
+
+        synchronize(stream)
 
 
 def parallel_async(kernel, *args, **kw):

@@ -115,3 +115,37 @@ def test_split_odd_extent_uses_ieee_path(ps, oracle):
     ps.parallel(ps.kernels.diffusion3D_step_inv, T2, ps.from_host(T), ps.from_host(Ci), 1.0, dt, *hs, memopt=True,
                 fp64="split")
     assert np.array_equal(ps.to_host(T2), ref)
+
+
+@pytest.mark.parametrize("nt", [7, 8])
+@pytest.mark.parametrize("fp64", ["ieee", "split", "split_state"])
+@pytest.mark.parametrize("form", [0, 3])
+def test_run_driver_vs_oracle_loop(ps, oracle, nt, fp64, form):
+    """ps_diffusion3d_run == the examples' time loop (T, T2 swapped each step)."""
+    n = (64, 34, 30)
+    T, Ci, lam, hs, dt = _setup(n, form, seed=11)
+    a, b = T.copy(order="F"), T.copy(order="F")
+    for _ in range(nt):
+        oracle.diffusion3d_step(form, b, a, Ci, lam if form == 3 else None, 1.3, dt, *hs)
+        a, b = b, a
+    k = getattr(ps.kernels, KERNELS[form])
+    dT, dT2 = ps.from_host(T), ps.from_host(T)
+    ps.kernels.run(k, dT, dT2, ps.from_host(Ci), ps.from_host(lam) if form == 3 else 1.3, dt, *hs, nt, fp64=fp64)
+    got = ps.to_host(dT)
+    if fp64 == "ieee":
+        assert np.array_equal(got, a)
+    else:
+        assert relerr(got, a) <= 1e-12
+
+
+def test_run_driver_odd_size_falls_back(ps, oracle):
+    n = (33, 20, 18)
+    T, Ci, lam, hs, dt = _setup(n, 3, seed=12)
+    a, b = T.copy(order="F"), T.copy(order="F")
+    for _ in range(5):
+        oracle.diffusion3d_step(3, b, a, Ci, lam, 0.0, dt, *hs)
+        a, b = b, a
+    dT, dT2 = ps.from_host(T), ps.from_host(T)
+    ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, dT, dT2, ps.from_host(Ci), ps.from_host(lam), dt, *hs, 5,
+                   fp64="split_state")
+    assert np.array_equal(ps.to_host(dT), a)
