@@ -108,7 +108,7 @@ __device__ __forceinline__ dd face(dd Ta, dd Tb, dd la, dd lb) {
 // PRE:   lam and Ci arrays already hold split pairs (float2 per cell, 8 bytes like a double).
 // STATE: T and T2 hold split pairs too (the state of a multi-step run); otherwise IEEE doubles.
 template <bool LAM, bool ISO, int TY, int S, int MINB, bool PRE, bool STATE>
-__global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __grid_constant__ CUtensorMap mT,
+__global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_constant__ CUtensorMap mT,
                                                                   const __grid_constant__ CUtensorMap mL,
                                                                   const __grid_constant__ CUtensorMap mC,
                                                                   double* __restrict__ T2, SplitParams p, int64_t nx,
@@ -117,15 +117,12 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
     // staged arrays converted in place each step: T (unless STATE) and lam (unless PRE)
     constexpr int NCONV = (STATE ? 0 : 1) + ((LAM && !PRE) ? 1 : 0);
     constexpr int NHALO = C::HALO * NCONV;
-    constexpr int NT = 32 * (TY + 1);  // TY cell warps + one face warp (the tile's top y faces, TMA issue)
-    constexpr int HPT = NHALO > 0 ? (NHALO + NT - 1) / NT : 1;
+    constexpr int HPT = NHALO > 0 ? (NHALO + 32 * TY - 1) / (32 * TY) : 1;
     extern __shared__ __align__(128) unsigned char smem[];
     float2* faceY0 = reinterpret_cast<float2*>(smem + S * C::STAGE);  // 2 x [TY+1][SP_TX]
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + 2 * C::FACE);
 
     const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
-    const bool fw = ly == TY;              // the face warp
-    const bool issuer = tid == 32 * TY;   // its first lane issues the TMA copies
     const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
     const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
     const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
@@ -133,7 +130,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
     const int nq = nk + 2;
 
     auto slot = [&](int q) { return smem + (q % S) * C::STAGE; };
-    if (issuer) {
+    if (tid == 0) {
         prefetch_tensormap(&mT);
         if constexpr (LAM) prefetch_tensormap(&mL);
         prefetch_tensormap(&mC);
@@ -150,7 +147,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
         if constexpr (LAM) tma_load_3d(b + C::PLANE, &mL, &bar[s], X0 - 2, Y0 - 1, z);
         tma_load_3d(b + C::PLANE * (LAM ? 2 : 1), &mC, &bar[s], X0, Y0, z);
     };
-    if (issuer)
+    if (tid == 0)
         for (; next_q < min(S, nq); ++next_q) issue(next_q);
 
     const int own = (1 + ly) * C::PW + 2 + 2 * lx;  // staged-plane index of this thread's first cell
@@ -163,7 +160,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
     int hoff[HPT];
 #pragma unroll
     for (int r = 0; r < HPT; r++) {
-        const int h = tid + r * NT;
+        const int h = tid + r * 32 * TY;
         const int a = h % C::HALO;
         const int idx = a < 2 * C::PH ? (a % C::PH) * C::PW + (a < C::PH ? 1 : C::PW - 2)
                                       : ((a - 2 * C::PH) < SP_TX ? 0 : (C::PH - 1)) * C::PW + 2 + ((a - 2 * C::PH) % SP_TX);
@@ -176,7 +173,6 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
     auto convert = [&](int q, dd* Tn, dd* ln, double2& rawT) {
         unsigned char* b = slot(q);
         double* tp = reinterpret_cast<double*>(b);
-        if (!fw) {
         if constexpr (STATE) {
             float4 v = *reinterpret_cast<const float4*>(tp + own);
             Tn[0] = dd{v.x, v.y};
@@ -200,7 +196,6 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
                 *reinterpret_cast<float4*>(lp + own) = make_float4(ln[0].h, ln[0].l, ln[1].h, ln[1].l);
             }
         }
-        }  // !fw
         if constexpr (NHALO > 0) {
 #pragma unroll
             for (int r = 0; r < HPT; r++) {
@@ -240,17 +235,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
         const double* tp = reinterpret_cast<const double*>(b1);
         const double* lp = reinterpret_cast<const double*>(b1 + C::PLANE);
         dd Fx[3], Fym[2], Fzp[2], ci[2];
-        if (!timed_out && fw) {
-            // faces between the tile's top row and the halo row above it
-            const int top = TY * C::PW + 2 + 2 * lx;
-            float4 tr = *reinterpret_cast<const float4*>(tp + top), ta = *reinterpret_cast<const float4*>(tp + top + C::PW);
-            float4 lr = LAM ? *reinterpret_cast<const float4*>(lp + top) : make_float4(0, 0, 0, 0);
-            float4 la = LAM ? *reinterpret_cast<const float4*>(lp + top + C::PW) : make_float4(0, 0, 0, 0);
-            dd f0 = face<LAM>(dd{tr.x, tr.y}, dd{ta.x, ta.y}, dd{lr.x, lr.y}, dd{la.x, la.y});
-            dd f1 = face<LAM>(dd{tr.z, tr.w}, dd{ta.z, ta.w}, dd{lr.z, lr.w}, dd{la.z, la.w});
-            *reinterpret_cast<float4*>(faceY + TY * SP_TX + 2 * lx) = make_float4(f0.h, f0.l, f1.h, f1.l);
-        }
-        if (!timed_out && !fw) {
+        if (!timed_out) {
             const double* cp = reinterpret_cast<const double*>(b1 + C::PLANE * (LAM ? 2 : 1)) + ly * SP_TX + 2 * lx;
             if constexpr (PRE) {
                 float4 v = *reinterpret_cast<const float4*>(cp);
@@ -280,20 +265,26 @@ __global__ void __launch_bounds__(32 * (TY + 1), MINB) diff3d_split_tma(const __
                 *reinterpret_cast<float4*>(faceY + ly * SP_TX + 2 * lx) =
                     make_float4(Fym[0].h, Fym[0].l, Fym[1].h, Fym[1].l);
             }
+            if (ly == TY - 1) {
+                float4 ta = *reinterpret_cast<const float4*>(tp + own + C::PW);
+                float4 la = LAM ? *reinterpret_cast<const float4*>(lp + own + C::PW) : make_float4(0, 0, 0, 0);
+                dd f0 = face<LAM>(Tc[0], dd{ta.x, ta.y}, lc[0], dd{la.x, la.y});
+                dd f1 = face<LAM>(Tc[1], dd{ta.z, ta.w}, lc[1], dd{la.z, la.w});
+                *reinterpret_cast<float4*>(faceY + TY * SP_TX + 2 * lx) = make_float4(f0.h, f0.l, f1.h, f1.l);
+            }
 #pragma unroll
             for (int j = 0; j < 2; j++) Fzp[j] = face<LAM>(Tc[j], Tz[j], lc[j], lz[j]);
         }
         // B: y faces published; planes <= k+1 are no longer read
         if (__syncthreads_or(timed_out)) {
-            if (issuer) {
+            if (tid == 0) {
                 atomicOr(err, DEV_ERR_TMA_TIMEOUT);
                 for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % S], (r / S) & 1);
             }
             return;
         }
-        if (issuer)
+        if (tid == 0)
             for (; next_q < min(nq, k + 2 + S); ++next_q) issue(next_q);
-        if (fw) continue;
         float4 fa = *reinterpret_cast<const float4*>(faceY + (ly + 1) * SP_TX + 2 * lx);
         dd Fyp[2] = {dd{fa.x, fa.y}, dd{fa.z, fa.w}};
         double out[2];
@@ -364,7 +355,7 @@ static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const p
         attr = true;
     }
     int64_t x0 = cb.lo[0] & ~(int64_t)1;
-    dim3 blk(32, TY + 1, 1);
+    dim3 blk(32, TY, 1);
     dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
              (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
     diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE><<<grd, blk, C::SMEM, s>>>(
