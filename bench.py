@@ -416,6 +416,31 @@ def run_reference(a, world, rank):
     print(json.dumps(out), flush=True)
 
 
+def only_run(a):
+    """A short run of the headline workload (for ncu captures of one kernel)."""
+    import torch
+
+    import ps_gb300 as ps
+
+    ps.init_parallel_stencil(ps.GB300, "Float64", 3)
+    n = a.n
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2)
+    T = ps.empty(n, n, n)
+    T.copy_(torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64))
+    T2 = ps.empty(n, n, n)
+    T2.copy_(T)
+    g.manual_seed(3)
+    lam = ps.empty(n, n, n)
+    lam.copy_(1 + 0.5 * torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64))
+    Ci = ps.ones(n, n, n)
+    dx = 10.0 / (n - 1)
+    ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, T, T2, Ci, lam, dx * dx / 1.5 / 8.1, 1 / dx, 1 / dx, 1 / dx,
+                   a.steps, fp64=a.only_run)
+    torch.cuda.synchronize()
+    print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -428,7 +453,12 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-run", choices=["ieee", "split", "split_state"], default=None,
+                    help="profiling aid: run --steps steps of the headline workload in this fp64 mode and exit")
     a = ap.parse_args()
+    if a.only_run:
+        only_run(a)
+        return
     if a.warmup < 3:
         a.warmup = 3
     world, rank, local = dist_setup()
