@@ -285,6 +285,21 @@ int ps_bc_y2d(ps_array A, void* stream, int sync);
  * temporaries included, ends bit-identical to the six-call sequence. Synchronises. */
 int ps_stokes2d_iterate(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int64_t n_iter, void* stream);
 
+/* ps_stokes2d_iterate without any device allocation. This entry point has no counterpart in the
+ * reference: it exists for callers that cannot let a library allocate device memory, e.g. a host
+ * whose device memory is owned by its own pool allocator (a cudaMalloc behind the pool's back can
+ * fail or fragment it) or a code path that must not call cudaFree (it synchronises the device).
+ * The three ping-pong buffers of the fused iteration come from a file-scope device array of
+ * 16 MiB compiled into the library (present on every device that loads it, until exit), so
+ * ((nx+1)*ny + nx*(ny+1) + nx*ny) * sizeof(T), each term rounded up to 256 bytes, must not exceed
+ * 16 MiB (about 830 x 830 cells in FP64); larger grids return PS_ERR_SHAPE. The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress, with that device current),
+ * so make that first call before any stream capture. All calls share the one array and it keeps
+ * the last call's contents (every element a call reads is written by that call first): calls that
+ * overlap on the GPU (concurrent streams, several host threads) race. Allocates nothing; results
+ * are bit-identical to ps_stokes2d_iterate. Synchronises. */
+int ps_stokes2d_iterate_static(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int64_t n_iter, void* stream);
+
 /* mean(abs.(Rx)), mean(abs.(Ry)), mean(abs.(∇V)) of the stored arrays (Stokes2D.jl:119). */
 int ps_stokes2d_err(const ps_stokes2d_fields* f, double out_mean_abs[3], void* stream);
 

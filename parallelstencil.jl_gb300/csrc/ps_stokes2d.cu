@@ -972,3 +972,116 @@ int ps_stokes2d_solve(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, 
 
 }  // extern "C"
 
+
+// =======================================================================================
+// ps_stokes2d_iterate_static: the fused PT iteration without any device allocation.
+//
+// ps_stokes2d_iterate needs three ping-pong buffers (the old/new Vx, Vy, Pt) and allocates them
+// per call. Some hosts cannot let a library allocate device memory: an application whose device
+// memory is fully owned by its own pool allocator (CUDA.jl's memory pool, a framework caching
+// allocator), where a cudaMalloc behind its back fails or fragments the pool, and code that must
+// not call cudaFree, which synchronises the whole device. This variant takes its ping-pong buffers
+// from a fixed device array compiled into the library instead.
+//
+// The array is file-scope, kStaticScratchBytes (16 MiB) on every device that loads the library,
+// held until process exit. Host code must not pass the array's name to a kernel (on the host it
+// is only a stand-in symbol): its device address is looked up once per device with
+// cudaGetSymbolAddress, on the first call on that device, with that device current.
+// =======================================================================================
+namespace ps {
+
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+static constexpr int kStaticMaxDevices = 64;
+static void* g_static_scratch_addr[kStaticMaxDevices] = {};
+static std::mutex g_static_mutex;
+
+// Device address of g_static_scratch on the current device (looked up once per device).
+static int static_scratch(void** out) {
+    int dev = -1;
+    PS_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kStaticMaxDevices) return fail(PS_ERR_ARG, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_scratch_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+        g_static_scratch_addr[dev] = p;
+    }
+    *out = g_static_scratch_addr[dev];
+    return PS_OK;
+}
+
+static size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+template <typename T>
+static int iterate_static(const ps_stokes2d_fields* f, const ps_stokes2d_params* pp, int64_t n_iter, cudaStream_t s) {
+    const int64_t nx = f->Pt.n[0], ny = f->Pt.n[1];
+    const size_t bx = (nx + 1) * ny * sizeof(T), by = nx * (ny + 1) * sizeof(T), bp = nx * ny * sizeof(T);
+    const size_t need = round256(bx) + round256(by) + round256(bp);
+    if (need > kStaticScratchBytes)
+        return fail(PS_ERR_SHAPE,
+                    "ps_stokes2d_iterate_static: a %lld x %lld grid needs %zu bytes of scratch; the static buffer "
+                    "holds %zu bytes (use ps_stokes2d_iterate)",
+                    (long long)nx, (long long)ny, need, kStaticScratchBytes);
+    void* base = nullptr;
+    PS_TRY(static_scratch(&base));
+    char* c = static_cast<char*>(base);
+    T* B[3] = {reinterpret_cast<T*>(c), reinterpret_cast<T*>(c + round256(bx)),
+               reinterpret_cast<T*>(c + round256(bx) + round256(by))};
+    T* A[3] = {P_<T>(f->Vx), P_<T>(f->Vy), P_<T>(f->Pt)};
+    S2P<T> p = s2p<T>(*pp);
+    S2Fused<T> a{};
+    a.Mus = P_<T>(f->Mus);
+    a.Rog = P_<T>(f->Rog);
+    a.dtVx = P_<T>(f->dtauVx);
+    a.dtVy = P_<T>(f->dtauVy);
+    a.dtPt = P_<T>(f->dtauPt);
+    a.dVxdt = P_<T>(f->dVxdtau);
+    a.dVydt = P_<T>(f->dVydtau);
+    a.divV = P_<T>(f->divV);
+    a.txx = P_<T>(f->txx);
+    a.tyy = P_<T>(f->tyy);
+    a.txy = P_<T>(f->txy);
+    a.Rx = P_<T>(f->Rx);
+    a.Ry = P_<T>(f->Ry);
+    a.red = nullptr;
+    a.nx = nx;
+    a.ny = ny;
+    // every element of the buffers in use is written before it is read within a call, so the
+    // contents left by the previous call never matter
+    for (int64_t it = 0; it < n_iter; ++it) {
+        T** in = (it % 2 == 0) ? A : B;
+        T** out = (it % 2 == 0) ? B : A;
+        a.Vx_in = in[0];
+        a.Vy_in = in[1];
+        a.P_in = in[2];
+        a.Vx_out = out[0];
+        a.Vy_out = out[1];
+        a.P_out = out[2];
+        launch_fused<T, false, true, true>(a, p, s);
+    }
+    if (n_iter % 2 == 1) {
+        PS_CUDA_TRY(cudaMemcpyAsync(A[0], B[0], bx, cudaMemcpyDeviceToDevice, s));
+        PS_CUDA_TRY(cudaMemcpyAsync(A[1], B[1], by, cudaMemcpyDeviceToDevice, s));
+        PS_CUDA_TRY(cudaMemcpyAsync(A[2], B[2], bp, cudaMemcpyDeviceToDevice, s));
+    }
+    return PS_OK;
+}
+
+}  // namespace ps
+
+extern "C" int ps_stokes2d_iterate_static(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int64_t n_iter,
+                                          void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    int64_t nx, ny;
+    PS_TRY(check_fields(f, &nx, &ny, true));
+    if (!p) return fail(PS_ERR_NULL, "NULL params");
+    if (n_iter < 0) return fail(PS_ERR_ARG, "n_iter must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc = f->Pt.dtype == PS_F64 ? iterate_static<double>(f, p, n_iter, s) : iterate_static<float>(f, p, n_iter, s);
+    PS_TRY(rc);
+    return finish_launch(s, 1, "ps_stokes2d_iterate_static");
+}

@@ -47,6 +47,7 @@ for _name in ("ps_stokes2d_timesteps", "ps_stokes2d_compute_P", "ps_stokes2d_com
 _lib.register("ps_bc_x2d", [PSArray, ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_bc_y2d", [PSArray, ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_stokes2d_iterate", [_F, _PP, ctypes.c_int64, ctypes.c_void_p])
+_lib.register("ps_stokes2d_iterate_static", [_F, _PP, ctypes.c_int64, ctypes.c_void_p])
 _lib.register("ps_stokes2d_err", [_F, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p])
 _lib.register("ps_stokes2d_solve", [_F, _PP, ctypes.c_int32, ctypes.c_double, ctypes.c_int64, ctypes.c_int64,
                                     ctypes.c_double, ctypes.POINTER(PSSolveStats), ctypes.c_void_p])
