@@ -36,6 +36,7 @@ WORDS_FLUX_LAM = 4  # T read, T2 write, lam read, Ci read
 WORDS_README = 3  # T read, T2 write, Ci read
 WORDS_MEMCOPY = 3
 NT_JOB = 50  # time steps of one diffusion job (the e2e unit)
+NT_ERR = 20  # time steps of the accuracy check of the multi-step modes against the IEEE run
 
 
 def measured_peaks():
@@ -237,6 +238,25 @@ def run_ours(a, world, rank, local):
                           "A_eff_GB": bytes_step / 1e9}
         return t_step, bytes_step
 
+    def run_errors(arrs, scalars, nt):
+        """Relative max-norm error of each multi-step FP64 mode after nt steps against the IEEE run
+        (bit-identical to the reference's statements) from the same initial state."""
+        T, T2, lam, Ci = arrs
+        T0 = T.clone()
+        ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, T, T2, Ci, lam, *scalars, nt, fp64="ieee")
+        ref = T.clone()
+        errs = {}
+        for mode in ("split", "split_state", "split_grid"):
+            T.copy_(T0)
+            T2.copy_(T0)
+            ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, T, T2, Ci, lam, *scalars, nt, fp64=mode)
+            errs[mode] = float((T - ref).abs().max() / ref.abs().max())
+        T.copy_(T0)
+        T2.copy_(T0)
+        del T0, ref
+        torch.cuda.synchronize()
+        return errs
+
     peak, peak_kind = measured_peaks()
     with ClockSampler(local) as clk:
         arrs64 = fields(np.float64, n)
@@ -244,6 +264,10 @@ def run_ours(a, world, rank, local):
                                    (dt, _dx, _dx, _dx), WORDS_FLUX_LAM, n, np.float64, a.steps, "split")
         bench_run("diffusion3d_flux_lam_f64_split_state_run", ps.kernels.diffusion3D_step_flux_lam, arrs64,
                   (dt, _dx, _dx, _dx), WORDS_FLUX_LAM, n, np.float64, a.steps, "split_state")
+        bench_run("diffusion3d_flux_lam_f64_split_grid_run", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                  (dt, _dx, _dx, _dx), WORDS_FLUX_LAM, n, np.float64, a.steps, "split_grid")
+        run_err = run_errors(arrs64, (dt, _dx, _dx, _dx), NT_ERR)
+        launches += (len(run_err) + 1) * NT_ERR
         bench_kernel("diffusion3d_flux_lam_f64_split_memopt_step", ps.kernels.diffusion3D_step_flux_lam, arrs64,
                      (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float64, a.steps, fp64="split")
         # accuracy of the split-FP32 arithmetic: one step against the bit-exact IEEE kernel
@@ -335,6 +359,7 @@ def run_ours(a, world, rank, local):
                    "l2": "inputs 4.3 GB >> 129 MB L2 (no flush needed)"},
         "pct_of_hbm_peak": round(100 * (value / world) / peak, 2),
         "err_vs_ieee_fp64_one_step": split_err,
+        "err_vs_ieee_fp64_run": {"steps": NT_ERR, **run_err},
         "roofline": {"bound": "hbm", "achieved": round(b_head / t_head / 1e9, 2), "peak": peak, "unit": "GB/s",
                      "frac": round((b_head / t_head / 1e9) / peak, 4), "peak_kind": f"{peak_kind} hbm_gbs (burst)",
                      "traffic": ncu_traffic("diffusion3d_split_flux_lam_f64_512"),
@@ -453,7 +478,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only-run", choices=["ieee", "split", "split_state"], default=None,
+    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode and exit")
     a = ap.parse_args()
     if a.only_run:

@@ -77,8 +77,15 @@ typedef struct ps_launch {
 
 /* PS_FP64_SPLIT_STATE (multi-step runs only, see ps_diffusion3d_run): as PS_FP64_SPLIT, but the
  * state between steps is kept as split pairs (8 bytes per value, as FP64) in library scratch and
- * converted from / to IEEE doubles at the start / end of the run. */
-enum { PS_FP64_IEEE = 0, PS_FP64_SPLIT = 1, PS_FP64_SPLIT_STATE = 2 };
+ * converted from / to IEEE doubles at the start / end of the run.
+ * PS_FP64_SPLIT_GRID (multi-step runs only): the state and lam are kept as pairs of floats on a
+ * power-of-two grid fixed for the run from max|T| and max|lam| (an integer-valued high part of at
+ * most 2^23 grid units plus a low part), which makes differences and conductivity sums exact in
+ * one FP32 operation. Rounding <= 1.5 * 2^-47 of max|T| per step. If a value leaves the grid's
+ * range (max|T| growing past its initial power of two), the run is redone in
+ * PS_FP64_SPLIT_STATE; this mode therefore synchronises the stream before returning.
+ * Single steps (ps_diffusion3d_step) treat both multi-step modes as PS_FP64_SPLIT. */
+enum { PS_FP64_IEEE = 0, PS_FP64_SPLIT = 1, PS_FP64_SPLIT_STATE = 2, PS_FP64_SPLIT_GRID = 3 };
 
 /* ------------------------------------------------------------------------------------ */
 /* Core: device, memory, streams.                                                        */

@@ -374,6 +374,26 @@ static int launch_split_flags(bool pre, bool state, const ps_array& Tin, const p
                  : launch_split_variant<LAM, ISO, false, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err);
 }
 
+// Per-dimension coefficients of the forms (split into p->c) and the common factor g: the
+// increment is g * Ci * sum_d c_d (F_d+ - F_d-); isotropic c is folded into g (returns true).
+static bool split_coeffs(int form, double lam_s, double dt, double hx, double hy, double hz, SplitParams* p,
+                         double* g) {
+    double c[3];
+    const double h[3] = {hx, hy, hz};
+    for (int d = 0; d < 3; d++) {
+        switch (form) {
+        case PS_DIFF_DIV: c[d] = 1.0 / (h[d] * h[d]); break;
+        case PS_DIFF_FLUX_LAM: c[d] = 0.5 * (h[d] * h[d]); break;
+        default: c[d] = h[d] * h[d]; break;
+        }
+    }
+    *g = form == PS_DIFF_FLUX_LAM ? dt : dt * lam_s;
+    const bool iso = c[0] == c[1] && c[1] == c[2];
+    if (iso) *g *= c[0];
+    for (int d = 0; d < 3; d++) split_const(p->c[d], c[d]);
+    return iso;
+}
+
 // Split-arithmetic z-sweep over the cell box cb. pre: lam / Ci hold split pairs; state: T / T2
 // hold split pairs. Returns PS_ERR_UNSUPPORTED when the arrays are not TMA-eligible (the caller
 // then uses the IEEE kernels).
@@ -383,19 +403,8 @@ static int launch_split(int form, const ps_array& T2, const ps_array& Tin, const
     bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
     if (!tma || T2.dtype != PS_F64) return PS_ERR_UNSUPPORTED;
     SplitParams p{};
-    double c[3], g;
-    const double h[3] = {hx, hy, hz};
-    for (int d = 0; d < 3; d++) {
-        switch (form) {
-        case PS_DIFF_DIV: c[d] = 1.0 / (h[d] * h[d]); break;
-        case PS_DIFF_FLUX_LAM: c[d] = 0.5 * (h[d] * h[d]); break;
-        default: c[d] = h[d] * h[d]; break;
-        }
-    }
-    g = form == PS_DIFF_FLUX_LAM ? dt : dt * lam_s;
-    const bool iso = c[0] == c[1] && c[1] == c[2];
-    if (iso) g *= c[0];
-    for (int d = 0; d < 3; d++) split_const(p.c[d], c[d]);
+    double g;
+    const bool iso = split_coeffs(form, lam_s, dt, hx, hy, hz, &p, &g);
     split_const(p.g, g);
     if (form == PS_DIFF_FLUX_LAM)
         return iso ? launch_split_flags<true, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err)
@@ -408,6 +417,338 @@ int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, co
                            double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
                            cudaStream_t s, int* d_err) {
     return launch_split(form, T2, Tin, Ci, lam, lam_s, dt, hx, hy, hz, cb, L, false, false, s, d_err);
+}
+
+// =======================================================================================
+// Fixed-grid split state (PS_FP64_SPLIT_GRID, multi-step runs).
+//
+// T and lam are held as float pairs (h, l) on a power-of-two grid fixed for the whole run:
+// value = (h + l) * u, u = 2^-sh, where sh is chosen from max|T| (max|lam|) so that the largest
+// magnitude is below 2^23 grid units; h is an integer-valued float (|h| <= 2^23), |l| <= 1/2.
+// Differences of h parts (|.| <= 2^24) and sums of lam h parts are exact in one FP32 addition,
+// where value-relative pairs need a two-sum; the face flux K*D keeps the exact FMA remainder of
+// the high product, so a face costs 8 FP32 operations instead of 20. Rounding per value and step:
+// <= 1.5 * 2^-25 grid units, i.e. <= 1.5 * 2^-47 of max|T|.
+// =======================================================================================
+
+// Run header in library scratch (written by the setup kernels on the device).
+struct GridRun {
+    unsigned long long maxT, maxL;  // bit patterns of max|T|, max|lam| (non-negative doubles order as integers)
+    int shT, shL;                   // grid units = value * 2^sh
+    int bad;                        // a value left the grid range: the run is redone with split pairs
+    int pad;
+    double g;                       // coefficient scale G * 2^-shL folded into the Ci pairs
+};
+
+template <bool LAM>
+__device__ __forceinline__ dd gface(dd Ta, dd Tb, dd la, dd lb) {
+    const float Dh = Tb.h - Ta.h, Dl = Tb.l - Ta.l;  // Dh exact (integers, |.| <= 2^24)
+    if constexpr (!LAM) {
+        return {Dh, Dl};
+    } else {
+        const float Kh = la.h + lb.h, Kl = la.l + lb.l;  // Kh exact
+        const float pr = Kh * Dh;
+        float e = fmaf(Kh, Dh, -pr);  // exact remainder of the high product
+        e = fmaf(Kh, Dl, e);
+        e = fmaf(Kl, Dh, e);
+        return {pr, e};
+    }
+}
+
+// One step on grid pairs: T, lam, T2 as (h, l) grid pairs, Ci as value pairs of Ci * G * u_lam.
+template <bool LAM, bool ISO, int TY, int S, int MINB>
+__global__ void __launch_bounds__(32 * TY, MINB)
+    diff3d_grid_tma(const __grid_constant__ CUtensorMap mT, const __grid_constant__ CUtensorMap mL,
+                    const __grid_constant__ CUtensorMap mC, float2* __restrict__ T2, SplitParams p, int64_t nx,
+                    int64_t ny, Box cb, int L, int* __restrict__ err, int* __restrict__ bad_flag) {
+    using C = SplitCfg<LAM, TY, S>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2* faceY0 = reinterpret_cast<float2*>(smem + S * C::STAGE);  // 2 x [TY+1][SP_TX]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + 2 * C::FACE);
+
+    const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
+    const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
+    const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
+    const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
+    const int nk = min(L, (int)cb.hi[2] - Z0);
+    const int nq = nk + 2;
+
+    auto slot = [&](int q) { return smem + (q % S) * C::STAGE; };
+    if (tid == 0) {
+        prefetch_tensormap(&mT);
+        if constexpr (LAM) prefetch_tensormap(&mL);
+        prefetch_tensormap(&mC);
+        for (int s = 0; s < S; s++) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int next_q = 0;
+    auto issue = [&](int q) {
+        unsigned char* b = slot(q);
+        int s = q % S, z = Z0 - 1 + q;
+        mbar_arrive_expect_tx(&bar[s], C::TX_BYTES);
+        tma_load_3d(b, &mT, &bar[s], X0 - 2, Y0 - 1, z);
+        if constexpr (LAM) tma_load_3d(b + C::PLANE, &mL, &bar[s], X0 - 2, Y0 - 1, z);
+        tma_load_3d(b + C::PLANE * (LAM ? 2 : 1), &mC, &bar[s], X0, Y0, z);
+    };
+    if (tid == 0)
+        for (; next_q < min(S, nq); ++next_q) issue(next_q);
+
+    const int own = (1 + ly) * C::PW + 2 + 2 * lx;  // staged-plane index of this thread's first cell
+    const int64_t gx = X0 + 2 * lx, gy = Y0 + ly;
+    const bool row_in = gy >= cb.lo[1] && gy < cb.hi[1];
+    const bool in0 = row_in && gx >= cb.lo[0] && gx < cb.hi[0];
+    const bool in1 = row_in && gx + 1 >= cb.lo[0] && gx + 1 < cb.hi[0];
+    auto ld1 = [](const unsigned char* b, int off) {
+        const float2 v = reinterpret_cast<const float2*>(b)[off];
+        return dd{v.x, v.y};
+    };
+    auto ld2 = [](const unsigned char* b, int off, dd* v) {  // off even: 16-byte aligned
+        const float4 t = *reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(b) + off);
+        v[0] = dd{t.x, t.y};
+        v[1] = dd{t.z, t.w};
+    };
+
+    bool bad = false, timed_out = false;
+    dd Tc[2], lc[2], Tz[2], lz[2], Fzm[2];
+    timed_out |= !mbar_wait_bounded(&bar[0], 0);
+    timed_out |= !mbar_wait_bounded(&bar[1], 0);
+    {
+        dd T0[2], l0[2];
+        ld2(slot(0), own, T0);
+        ld2(slot(1), own, Tc);
+        if constexpr (LAM) {
+            ld2(slot(0) + C::PLANE, own, l0);
+            ld2(slot(1) + C::PLANE, own, lc);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) Fzm[j] = gface<LAM>(T0[j], Tc[j], l0[j], lc[j]);
+    }
+
+    for (int k = 0; k < nk; ++k) {
+        const int q = k + 2;
+        timed_out |= !mbar_wait_bounded(&bar[q % S], (q / S) & 1);
+        const unsigned char* bz = slot(q);
+        ld2(bz, own, Tz);
+        if constexpr (LAM) ld2(bz + C::PLANE, own, lz);
+        float2* faceY = faceY0 + (k & 1) * (TY + 1) * SP_TX;
+        const unsigned char* tp = slot(k + 1);
+        const unsigned char* lp = tp + C::PLANE;
+        dd Fx[3], Fym[2], Fzp[2], ci[2];
+        ld2(tp + C::PLANE * (LAM ? 2 : 1), ly * SP_TX + 2 * lx, ci);
+        {
+            const dd Txm = ld1(tp, own - 1), Txp = ld1(tp, own + 2);
+            dd lxm{0.f, 0.f}, lxp{0.f, 0.f};
+            if constexpr (LAM) {
+                lxm = ld1(lp, own - 1);
+                lxp = ld1(lp, own + 2);
+            }
+            Fx[0] = gface<LAM>(Txm, Tc[0], lxm, lc[0]);
+            Fx[1] = gface<LAM>(Tc[0], Tc[1], lc[0], lc[1]);
+            Fx[2] = gface<LAM>(Tc[1], Txp, lc[1], lxp);
+        }
+        {
+            dd tb[2], lb[2] = {{0.f, 0.f}, {0.f, 0.f}};
+            ld2(tp, own - C::PW, tb);
+            if constexpr (LAM) ld2(lp, own - C::PW, lb);
+            Fym[0] = gface<LAM>(tb[0], Tc[0], lb[0], lc[0]);
+            Fym[1] = gface<LAM>(tb[1], Tc[1], lb[1], lc[1]);
+            *reinterpret_cast<float4*>(faceY + ly * SP_TX + 2 * lx) = make_float4(Fym[0].h, Fym[0].l, Fym[1].h, Fym[1].l);
+        }
+        if (ly == TY - 1) {
+            dd ta[2], la[2] = {{0.f, 0.f}, {0.f, 0.f}};
+            ld2(tp, own + C::PW, ta);
+            if constexpr (LAM) ld2(lp, own + C::PW, la);
+            const dd f0 = gface<LAM>(Tc[0], ta[0], lc[0], la[0]);
+            const dd f1 = gface<LAM>(Tc[1], ta[1], lc[1], la[1]);
+            *reinterpret_cast<float4*>(faceY + TY * SP_TX + 2 * lx) = make_float4(f0.h, f0.l, f1.h, f1.l);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) Fzp[j] = gface<LAM>(Tc[j], Tz[j], lc[j], lz[j]);
+        // y faces published; planes <= k+1 are no longer read
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0) {
+                atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+                for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % S], (r / S) & 1);
+            }
+            return;
+        }
+        if (tid == 0)
+            for (; next_q < min(nq, k + 2 + S); ++next_q) issue(next_q);
+        const float4 fa = *reinterpret_cast<const float4*>(faceY + (ly + 1) * SP_TX + 2 * lx);
+        const dd Fyp[2] = {dd{fa.x, fa.y}, dd{fa.z, fa.w}};
+        float2 out[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            dd Sm;
+            if constexpr (ISO) {
+                Sm = dd_sub(Fx[j + 1], Fx[j]);
+                Sm = dd_add(Sm, Fyp[j]);
+                Sm = dd_sub(Sm, Fym[j]);
+                Sm = dd_add(Sm, Fzp[j]);
+                Sm = dd_sub(Sm, Fzm[j]);
+            } else {
+                Sm = dd_mul(p.c[0], dd_sub(Fx[j + 1], Fx[j]));
+                Sm = dd_add(Sm, dd_mul(p.c[1], dd_sub(Fyp[j], Fym[j])));
+                Sm = dd_add(Sm, dd_mul(p.c[2], dd_sub(Fzp[j], Fzm[j])));
+            }
+            const dd d = dd_mul(ci[j], Sm);  // increment in grid units
+            // T2 = T + d on the grid: move the integer part of d into h, keep |l| <= 1/2
+            constexpr float M = 12582912.0f;       // 1.5 * 2^23: (x + M) - M is an integer near x
+            const float q0 = (d.h + M) - M;
+            float l2 = (d.h - q0) + d.l;           // d.h - q0 exact
+            l2 = l2 + Tc[j].l;
+            const float q1 = (l2 + M) - M;
+            const float h2 = (Tc[j].h + q0) + q1;  // integers: exact while in range
+            bad |= !(fabsf(h2) <= 8388608.0f);     // left the grid (or not finite)
+            out[j] = make_float2(h2, l2 - q1);
+        }
+        const int64_t gz = Z0 + k;
+        float2* dst = T2 + gx + nx * (gy + ny * gz);
+        if (in0 && in1)
+            *reinterpret_cast<float4*>(dst) = make_float4(out[0].x, out[0].y, out[1].x, out[1].y);
+        else {
+            if (in0) dst[0] = out[0];
+            if (in1) dst[1] = out[1];
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            Tc[j] = Tz[j];
+            lc[j] = lz[j];
+            Fzm[j] = Fzp[j];
+        }
+    }
+    if (__syncthreads_or(bad) && tid == 0) atomicOr(bad_flag, 1);
+}
+
+// max |a[i]| as a bit pattern (atomicMax over warps)
+__global__ void absmax_bits_kernel(const double* __restrict__ a, int64_t n, unsigned long long* out) {
+    unsigned long long m = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(__ldcs(a + i)) & 0x7FFFFFFFFFFFFFFFull;
+        m = b > m ? b : m;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// Grid exponent of a maximum: largest magnitude < 2^23 grid units. Maxima outside
+// [2^-823, 2^877) (and non-finite ones) are left to the split-pair path.
+__device__ bool grid_shift(unsigned long long m, int* sh) {
+    if (m == 0) {
+        *sh = 0;
+        return true;
+    }
+    const int e = (int)(m >> 52);  // max in [2^(e-1023), 2^(e-1022))
+    if (e < 200 || e > 1900) return false;
+    *sh = 1045 - e;
+    return true;
+}
+
+__global__ void grid_setup_kernel(GridRun* r, double G, int has_lam) {
+    bool ok = grid_shift(r->maxT, &r->shT);
+    if (has_lam)
+        ok = ok && grid_shift(r->maxL, &r->shL);
+    else
+        r->shL = 0;
+    const double g = ok ? ldexp(G, -r->shL) : 0.0;
+    const double ag = fabs(g);
+    if (!ok || (ag != 0.0 && (ag < 0x1p-100 || ag > 0x1p100))) r->bad = 1;
+    r->g = g;
+}
+
+__device__ __forceinline__ float2 to_grid(double v, int sh, bool& bad) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0x7FF) {
+        bad = true;
+        return make_float2(0.f, 0.f);
+    }
+    if (e == 0 || e + sh <= 0) return make_float2(0.f, 0.f);  // below 2^-1022 grid units
+    const double x = __longlong_as_double(b + ((long long)sh << 52));  // v * 2^sh, |x| < 2^23
+    bool big = false;
+    const dd d = dd_split(x, big);
+    const float h = rintf(d.h);
+    return make_float2(h, (d.h - h) + d.l);
+}
+
+// T -> grid pairs (into a and, when b is non-NULL, b); lam -> grid pairs (lam_grid = 1)
+__global__ void to_grid_kernel(const double* __restrict__ in, float2* __restrict__ a, float2* __restrict__ b,
+                               int64_t n, GridRun* r, int lam_grid) {
+    if (r->bad) return;
+    const int sh = lam_grid ? r->shL : r->shT;
+    bool bad = false;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float2 v = to_grid(__ldcs(in + i), sh, bad);
+        a[i] = v;
+        if (b) b[i] = v;
+    }
+    if (bad) atomicOr(&r->bad, 1);
+}
+
+// Ci -> value pairs of Ci * g
+__global__ void ci_grid_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n, GridRun* r) {
+    if (r->bad) return;
+    const double g = r->g;
+    dd gd;
+    gd.h = (float)g;
+    gd.l = (float)(g - (double)gd.h);
+    bool big = false;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const dd c = dd_norm(dd_mul(dd_split(__ldcs(in + i), big), gd));
+        big |= !(fabsf(c.h) < 0x1p127f);
+        out[i] = make_float2(c.h, c.l);
+    }
+    if (big) atomicOr(&r->bad, 1);
+}
+
+// grid pairs -> T (skipped when the run left the grid range: T keeps its input)
+__global__ void from_grid_kernel(const float2* __restrict__ in, double* __restrict__ out, int64_t n,
+                                 const GridRun* r) {
+    if (r->bad) return;
+    const int sh = r->shT;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float2 v = in[i];
+        const double y = f32_to_f64(v.x) + f32_to_f64(v.y);
+        const long long b = __double_as_longlong(y);
+        const int e = (int)((b >> 52) & 0x7FF);
+        out[i] = (e == 0 || e - sh <= 0) ? 0.0 : __longlong_as_double(b - ((long long)sh << 52));
+    }
+}
+
+template <bool LAM, bool ISO>
+static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps_array* Ls, const ps_array& T2,
+                               const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, int* bad) {
+    constexpr int TY = 8, S = 4, MINB = 3;
+    using C = SplitCfg<LAM, TY, S>;
+    CUtensorMap mT, mL, mC;
+    PS_TRY(encode_plane_map(&mT, Tin, C::PW, C::PH));
+    if (LAM)
+        PS_TRY(encode_plane_map(&mL, *Ls, C::PW, C::PH));
+    else
+        mL = mT;
+    PS_TRY(encode_plane_map(&mC, Cs, SP_TX, TY));
+    static bool attr = false;
+    if (!attr) {
+        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_grid_tma<LAM, ISO, TY, S, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+        attr = true;
+    }
+    const int64_t x0 = cb.lo[0] & ~(int64_t)1;
+    dim3 blk(32, TY, 1);
+    dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
+             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    diff3d_grid_tma<LAM, ISO, TY, S, MINB><<<grd, blk, C::SMEM, s>>>(
+        mT, mL, mC, static_cast<float2*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err, bad);
+    return PS_OK;
 }
 
 // ---- multi-step runs -------------------------------------------------------------------
@@ -472,7 +813,7 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int memopt = cfg ? cfg->memopt : 1, loopsize = cfg ? cfg->loopsize : 0;
     int mode = cfg ? cfg->fp64_mode : PS_FP64_IEEE;
-    if (mode < PS_FP64_IEEE || mode > PS_FP64_SPLIT_STATE) return fail(PS_ERR_ARG, "unknown fp64_mode %d", mode);
+    if (mode < PS_FP64_IEEE || mode > PS_FP64_SPLIT_GRID) return fail(PS_ERR_ARG, "unknown fp64_mode %d", mode);
     const int64_t n = numel(T);
     const size_t bytes = (size_t)n * 8;
     const bool has_lam = form == PS_DIFF_FLUX_LAM;
@@ -483,6 +824,59 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
                  tma_eligible(Ci) && (!has_lam || tma_eligible(lam_arr)) && cells.hi[0] > cells.lo[0] &&
                  cells.hi[1] > cells.lo[1] && cells.hi[2] > cells.lo[2];
     ps_array A = T, B = T2;
+    if (split && mode == PS_FP64_SPLIT_GRID) {
+        // state, lam and Ci as grid / value pairs in scratch; T is written only by the final
+        // conversion, which the device skips when a value left the grid range
+        char* scr = nullptr;
+        const size_t head = 256;
+        PS_TRY(run_scratch(head + bytes * ((has_lam ? 1 : 0) + 3), &scr));
+        GridRun* r = reinterpret_cast<GridRun*>(scr);
+        ps_array Cs = Ci, Ls = lam_arr, Sa = T, Sb = T;
+        Cs.ptr = scr + head;
+        Sa.ptr = scr + head + bytes;
+        Sb.ptr = scr + head + 2 * bytes;
+        if (has_lam) Ls.ptr = scr + head + 3 * bytes;
+        SplitParams p{};
+        double G;
+        const bool iso = split_coeffs(form, lam, dt, hx, hy, hz, &p, &G);
+        const int g = st->num_sms * 8;
+        PS_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(GridRun), s));
+        absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(T.ptr), n, &r->maxT);
+        if (has_lam) absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(lam_arr.ptr), n, &r->maxL);
+        grid_setup_kernel<<<1, 1, 0, s>>>(r, G, has_lam ? 1 : 0);
+        // T2's boundary values are T's (the documented precondition), so one pass fills both states
+        to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(T.ptr), static_cast<float2*>(Sa.ptr),
+                                         static_cast<float2*>(Sb.ptr), n, r, 0);
+        if (has_lam)
+            to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(lam_arr.ptr), static_cast<float2*>(Ls.ptr),
+                                             nullptr, n, r, 1);
+        ci_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(Ci.ptr), static_cast<float2*>(Cs.ptr), n, r);
+        A = Sa;
+        B = Sb;
+        for (int64_t it = 0; it < nt; ++it) {
+            int rc;
+            if (form == PS_DIFF_FLUX_LAM)
+                rc = iso ? launch_grid_variant<true, true>(A, Cs, &Ls, B, p, cells, L, s, st->d_err, &r->bad)
+                         : launch_grid_variant<true, false>(A, Cs, &Ls, B, p, cells, L, s, st->d_err, &r->bad);
+            else
+                rc = iso ? launch_grid_variant<false, true>(A, Cs, nullptr, B, p, cells, L, s, st->d_err, &r->bad)
+                         : launch_grid_variant<false, false>(A, Cs, nullptr, B, p, cells, L, s, st->d_err, &r->bad);
+            PS_TRY(rc);
+            std::swap(A, B);
+        }
+        from_grid_kernel<<<g, 256, 0, s>>>(static_cast<const float2*>(A.ptr), static_cast<double*>(T.ptr), n, r);
+        PS_CUDA_TRY(cudaGetLastError());
+        int bad = 0;
+        PS_CUDA_TRY(cudaMemcpyAsync(&bad, &r->bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PS_CUDA_TRY(cudaStreamSynchronize(s));
+        if (bad) {  // a value outside the grid's range: redo the run with value-relative split pairs
+            ps_launch c2 = cfg ? *cfg : ps_launch{};
+            c2.memopt = memopt;
+            c2.fp64_mode = PS_FP64_SPLIT_STATE;
+            return ps_diffusion3d_run(form, T, T2, Ci, lam_arr, lam, dt, hx, hy, hz, nt, &c2, stream);
+        }
+        return finish_launch(s, 0, "ps_diffusion3d_run");
+    }
     if (!split) {
         for (int64_t it = 0; it < nt; ++it) {
             PS_TRY(diffusion_box(form, B, A, Ci, lam_arr, lam, dt, hx, hy, hz, full, memopt, loopsize, PS_FP64_IEEE, s,

@@ -782,9 +782,9 @@ int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_a
     int loopsize = cfg ? cfg->loopsize : 0;
     int fp64_mode = cfg ? cfg->fp64_mode : PS_FP64_IEEE;
     if (loopsize < 0) return fail(PS_ERR_ARG, "ps_diffusion3d_step: loopsize must be >= 0");
-    if (fp64_mode < PS_FP64_IEEE || fp64_mode > PS_FP64_SPLIT_STATE)
+    if (fp64_mode < PS_FP64_IEEE || fp64_mode > PS_FP64_SPLIT_GRID)
         return fail(PS_ERR_ARG, "unknown fp64_mode %d", fp64_mode);
-    if (fp64_mode == PS_FP64_SPLIT_STATE) fp64_mode = PS_FP64_SPLIT;  // one step: the state stays IEEE
+    if (fp64_mode != PS_FP64_IEEE) fp64_mode = PS_FP64_SPLIT;  // one step: the state stays IEEE
     PS_TRY(diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, tb, memopt, loopsize, fp64_mode, s, st->d_err));
     return finish_launch(s, sync, "ps_diffusion3d_step");
 }

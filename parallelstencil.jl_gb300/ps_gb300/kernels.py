@@ -27,7 +27,7 @@ from .core import ArgumentError, default_memopt, descriptor, require_initialized
 from .fd import FdKernel, fd_kernel
 
 PS_DIFF_DIV, PS_DIFF_MUL, PS_DIFF_FLUX, PS_DIFF_FLUX_LAM = 0, 1, 2, 3
-FP64_MODES = {"ieee": 0, "split": 1, "split_state": 2}
+FP64_MODES = {"ieee": 0, "split": 1, "split_state": 2, "split_grid": 3}
 
 _lib.register("ps_diffusion3d_run", [ctypes.c_int32] + [_lib.PSArray] * 4 + [ctypes.c_double] * 5 +
               [ctypes.c_int64, ctypes.POINTER(PSLaunch), ctypes.c_void_p])

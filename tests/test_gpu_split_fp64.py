@@ -149,3 +149,66 @@ def test_run_driver_odd_size_falls_back(ps, oracle):
     ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, dT, dT2, ps.from_host(Ci), ps.from_host(lam), dt, *hs, 5,
                    fp64="split_state")
     assert np.array_equal(ps.to_host(dT), a)
+
+
+@pytest.mark.parametrize("n", [(64, 64, 64), (64, 34, 30)])
+@pytest.mark.parametrize("form", [0, 1, 2, 3])
+@pytest.mark.parametrize("nt", [1, 20])
+def test_grid_run_vs_oracle_loop(ps, oracle, n, form, nt):
+    """fp64 = split_grid (state on a fixed power-of-two grid): isotropic (cubic) and anisotropic spacing."""
+    T, Ci, lam, hs, dt = _setup(n, form, seed=20 + form)
+    a, b = T.copy(order="F"), T.copy(order="F")
+    for _ in range(nt):
+        oracle.diffusion3d_step(form, b, a, Ci, lam if form == 3 else None, 1.3, dt, *hs)
+        a, b = b, a
+    k = getattr(ps.kernels, KERNELS[form])
+    dT, dT2 = ps.from_host(T), ps.from_host(T)
+    ps.kernels.run(k, dT, dT2, ps.from_host(Ci), ps.from_host(lam) if form == 3 else 1.3, dt, *hs, nt,
+                   fp64="split_grid")
+    e = relerr(ps.to_host(dT), a)
+    assert e <= 1e-12, e
+
+
+@pytest.mark.parametrize("shift,scale,lscale", [(-0.5, 1e-30, 1e5), (3.0, 7.0e20, 1e-7), (0.0, 1.0, 1.0)])
+def test_grid_run_value_ranges(ps, oracle, shift, scale, lscale):
+    """Negative values, magnitudes far outside FP32's range relative to 1, scaled conductivities."""
+    n = (64, 40, 36)
+    T, Ci, lam, hs, dt = _setup(n, 3, seed=31)
+    T = np.asfortranarray((T + shift) * scale)
+    lam = np.asfortranarray(lam * lscale)
+    dt = dt / lscale
+    a, b = T.copy(order="F"), T.copy(order="F")
+    for _ in range(10):
+        oracle.diffusion3d_step(3, b, a, Ci, lam, 0.0, dt, *hs)
+        a, b = b, a
+    dT, dT2 = ps.from_host(T), ps.from_host(T)
+    ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, dT, dT2, ps.from_host(Ci), ps.from_host(lam), dt, *hs, 10,
+                   fp64="split_grid")
+    e = relerr(ps.to_host(dT), a)
+    assert e <= 1e-12, e
+
+
+def test_grid_run_zero_field(ps):
+    n = (64, 40, 36)
+    _, Ci, lam, hs, dt = _setup(n, 3, seed=32)
+    Z = np.zeros(n, order="F")
+    dT, dT2 = ps.from_host(Z), ps.from_host(Z)
+    ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, dT, dT2, ps.from_host(Ci), ps.from_host(lam), dt, *hs, 4,
+                   fp64="split_grid")
+    assert not np.any(ps.to_host(dT))
+
+
+def test_grid_run_growth_falls_back_to_split_state(ps):
+    """An unstable dt makes max|T| grow past its initial power of two: the grid run is redone with
+    value-relative split pairs, so its result is bit-identical to a split_state run."""
+    n = (64, 40, 36)
+    T, Ci, lam, hs, dt = _setup(n, 3, seed=33)
+    dt = dt * 12.0
+    out = {}
+    for mode in ("split_grid", "split_state"):
+        dT, dT2 = ps.from_host(T), ps.from_host(T)
+        ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, dT, dT2, ps.from_host(Ci), ps.from_host(lam), dt, *hs,
+                       6, fp64=mode)
+        out[mode] = ps.to_host(dT)
+    assert np.abs(out["split_state"]).max() > 1.0  # left the grid of max|T0| < 1
+    assert np.array_equal(out["split_grid"], out["split_state"])
