@@ -455,13 +455,24 @@ __device__ __forceinline__ dd gface(dd Ta, dd Tb, dd la, dd lb) {
     }
 }
 
-// One step on grid pairs: T, lam, T2 as (h, l) grid pairs, Ci as value pairs of Ci * G * u_lam.
-template <bool LAM, bool ISO, int TY, int S, int MINB>
+// Exact double of the grid value (h + l) * 2^-sh (h, l floats; values below 2^-1022 -> 0).
+__device__ __forceinline__ double grid_to_f64(double y, int sh) {
+    const long long b = __double_as_longlong(y);
+    const int e = (int)((b >> 52) & 0x7FF);
+    return (e == 0 || e - sh <= 0) ? 0.0 : __longlong_as_double(b - ((long long)sh << 52));
+}
+
+// One step on grid pairs: T, lam as (h, l) grid pairs, Ci as value pairs of Ci * G * u_lam; T2 as
+// grid pairs, or (OUT64, the last step of a run) as IEEE doubles. Every launch returns at once when
+// an earlier kernel of the run flagged a value outside the grid (the run is then redone).
+template <bool LAM, bool ISO, int TY, int S, int MINB, bool OUT64>
 __global__ void __launch_bounds__(32 * TY, MINB)
     diff3d_grid_tma(const __grid_constant__ CUtensorMap mT, const __grid_constant__ CUtensorMap mL,
-                    const __grid_constant__ CUtensorMap mC, float2* __restrict__ T2, SplitParams p, int64_t nx,
-                    int64_t ny, Box cb, int L, int* __restrict__ err, int* __restrict__ bad_flag) {
+                    const __grid_constant__ CUtensorMap mC, void* __restrict__ T2v, SplitParams p, int64_t nx,
+                    int64_t ny, Box cb, int L, int* __restrict__ err, GridRun* __restrict__ run) {
     using C = SplitCfg<LAM, TY, S>;
+    if (*reinterpret_cast<volatile int*>(&run->bad)) return;
+    const int sh = run->shT;
     extern __shared__ __align__(128) unsigned char smem[];
     float2* faceY0 = reinterpret_cast<float2*>(smem + S * C::STAGE);  // 2 x [TY+1][SP_TX]
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + 2 * C::FACE);
@@ -578,6 +589,7 @@ __global__ void __launch_bounds__(32 * TY, MINB)
         const float4 fa = *reinterpret_cast<const float4*>(faceY + (ly + 1) * SP_TX + 2 * lx);
         const dd Fyp[2] = {dd{fa.x, fa.y}, dd{fa.z, fa.w}};
         float2 out[2];
+        double out64[2];
 #pragma unroll
         for (int j = 0; j < 2; j++) {
             dd Sm;
@@ -600,16 +612,36 @@ __global__ void __launch_bounds__(32 * TY, MINB)
             l2 = l2 + Tc[j].l;
             const float q1 = (l2 + M) - M;
             const float h2 = (Tc[j].h + q0) + q1;  // integers: exact while in range
-            bad |= !(fabsf(h2) <= 8388608.0f);     // left the grid (or not finite)
-            out[j] = make_float2(h2, l2 - q1);
+            const bool in_range = fabsf(h2) <= 8388608.0f;
+            if constexpr (OUT64) {
+                // the last step leaves the grid: a value that grew past it is summed in FP64 instead
+                const double y = in_range ? f32_to_f64(h2) + f32_to_f64(l2 - q1)
+                                          : ((f32_to_f64(Tc[j].h) + f32_to_f64(Tc[j].l)) + f32_to_f64(d.h)) +
+                                                f32_to_f64(d.l);
+                out64[j] = grid_to_f64(y, sh);
+            } else {
+                bad |= !in_range;  // left the grid (or not finite)
+                out[j] = make_float2(h2, l2 - q1);
+            }
         }
         const int64_t gz = Z0 + k;
-        float2* dst = T2 + gx + nx * (gy + ny * gz);
-        if (in0 && in1)
-            *reinterpret_cast<float4*>(dst) = make_float4(out[0].x, out[0].y, out[1].x, out[1].y);
-        else {
-            if (in0) dst[0] = out[0];
-            if (in1) dst[1] = out[1];
+        const int64_t o = gx + nx * (gy + ny * gz);
+        if constexpr (OUT64) {
+            double* dst = static_cast<double*>(T2v) + o;
+            if (in0 && in1)
+                *reinterpret_cast<double2*>(dst) = make_double2(out64[0], out64[1]);
+            else {
+                if (in0) dst[0] = out64[0];
+                if (in1) dst[1] = out64[1];
+            }
+        } else {
+            float2* dst = static_cast<float2*>(T2v) + o;
+            if (in0 && in1)
+                *reinterpret_cast<float4*>(dst) = make_float4(out[0].x, out[0].y, out[1].x, out[1].y);
+            else {
+                if (in0) dst[0] = out[0];
+                if (in1) dst[1] = out[1];
+            }
         }
 #pragma unroll
         for (int j = 0; j < 2; j++) {
@@ -618,16 +650,38 @@ __global__ void __launch_bounds__(32 * TY, MINB)
             Fzm[j] = Fzp[j];
         }
     }
-    if (__syncthreads_or(bad) && tid == 0) atomicOr(bad_flag, 1);
+    if (__syncthreads_or(bad) && tid == 0) atomicOr(&run->bad, 1);
 }
 
+// Boundary cells (the six faces) of a grid state copied from a to b: b's interior is written by
+// the first step, its boundary is read from the second step on.
+__global__ void grid_faces_kernel(const float2* __restrict__ a, float2* __restrict__ b, int64_t nx, int64_t ny,
+                                  int64_t nz, const GridRun* r) {
+    if (r->bad) return;
+    const int f = blockIdx.y;  // 0,1: z faces; 2,3: y faces; 4,5: x faces
+    const int64_t n0 = f < 4 ? nx : ny, n1 = f < 2 ? ny : nz;
+    const int64_t fixed = (f & 1) ? (f < 2 ? nz : f < 4 ? ny : nx) - 1 : 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n0 * n1; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i % n0, v = i / n0;
+        const int64_t ix = f < 4 ? u : fixed, iy = f < 2 ? v : f < 4 ? fixed : u, iz = f < 2 ? fixed : v;
+        const int64_t o = ix + nx * (iy + ny * iz);
+        b[o] = a[o];
+    }
+}
+
+// The setup kernels below run on TMA-eligible arrays (nx even), so they work on pairs of values
+// (16-byte accesses); n2 = numel / 2.
+
 // max |a[i]| as a bit pattern (atomicMax over warps)
-__global__ void absmax_bits_kernel(const double* __restrict__ a, int64_t n, unsigned long long* out) {
+__global__ void absmax_bits_kernel(const double2* __restrict__ a, int64_t n2, unsigned long long* out) {
     unsigned long long m = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const unsigned long long b = (unsigned long long)__double_as_longlong(__ldcs(a + i)) & 0x7FFFFFFFFFFFFFFFull;
-        m = b > m ? b : m;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += stride) {
+        const double2 v = __ldcs(a + i);
+        const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+        const unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+        m = b0 > m ? b0 : m;
+        m = b1 > m ? b1 : m;
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
@@ -677,23 +731,23 @@ __device__ __forceinline__ float2 to_grid(double v, int sh, bool& bad) {
     return make_float2(h, (d.h - h) + d.l);
 }
 
-// T -> grid pairs (into a and, when b is non-NULL, b); lam -> grid pairs (lam_grid = 1)
-__global__ void to_grid_kernel(const double* __restrict__ in, float2* __restrict__ a, float2* __restrict__ b,
-                               int64_t n, GridRun* r, int lam_grid) {
+// T -> grid pairs (lam_grid = 0) or lam -> grid pairs (lam_grid = 1)
+__global__ void to_grid_kernel(const double2* __restrict__ in, float4* __restrict__ a, int64_t n2, GridRun* r,
+                               int lam_grid) {
     if (r->bad) return;
     const int sh = lam_grid ? r->shL : r->shT;
     bool bad = false;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float2 v = to_grid(__ldcs(in + i), sh, bad);
-        a[i] = v;
-        if (b) b[i] = v;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += stride) {
+        const double2 v = __ldcs(in + i);
+        const float2 g0 = to_grid(v.x, sh, bad), g1 = to_grid(v.y, sh, bad);
+        a[i] = make_float4(g0.x, g0.y, g1.x, g1.y);
     }
     if (bad) atomicOr(&r->bad, 1);
 }
 
 // Ci -> value pairs of Ci * g
-__global__ void ci_grid_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n, GridRun* r) {
+__global__ void ci_grid_kernel(const double2* __restrict__ in, float4* __restrict__ out, int64_t n2, GridRun* r) {
     if (r->bad) return;
     const double g = r->g;
     dd gd;
@@ -701,32 +755,18 @@ __global__ void ci_grid_kernel(const double* __restrict__ in, float2* __restrict
     gd.l = (float)(g - (double)gd.h);
     bool big = false;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const dd c = dd_norm(dd_mul(dd_split(__ldcs(in + i), big), gd));
-        big |= !(fabsf(c.h) < 0x1p127f);
-        out[i] = make_float2(c.h, c.l);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += stride) {
+        const double2 v = __ldcs(in + i);
+        const dd c0 = dd_norm(dd_mul(dd_split(v.x, big), gd)), c1 = dd_norm(dd_mul(dd_split(v.y, big), gd));
+        big |= !(fabsf(c0.h) < 0x1p127f) || !(fabsf(c1.h) < 0x1p127f);
+        out[i] = make_float4(c0.h, c0.l, c1.h, c1.l);
     }
     if (big) atomicOr(&r->bad, 1);
 }
 
-// grid pairs -> T (skipped when the run left the grid range: T keeps its input)
-__global__ void from_grid_kernel(const float2* __restrict__ in, double* __restrict__ out, int64_t n,
-                                 const GridRun* r) {
-    if (r->bad) return;
-    const int sh = r->shT;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float2 v = in[i];
-        const double y = f32_to_f64(v.x) + f32_to_f64(v.y);
-        const long long b = __double_as_longlong(y);
-        const int e = (int)((b >> 52) & 0x7FF);
-        out[i] = (e == 0 || e - sh <= 0) ? 0.0 : __longlong_as_double(b - ((long long)sh << 52));
-    }
-}
-
-template <bool LAM, bool ISO>
+template <bool LAM, bool ISO, bool OUT64>
 static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps_array* Ls, const ps_array& T2,
-                               const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, int* bad) {
+                               const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, GridRun* run) {
     constexpr int TY = 8, S = 4, MINB = 3;
     using C = SplitCfg<LAM, TY, S>;
     CUtensorMap mT, mL, mC;
@@ -738,7 +778,7 @@ static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps
     PS_TRY(encode_plane_map(&mC, Cs, SP_TX, TY));
     static bool attr = false;
     if (!attr) {
-        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_grid_tma<LAM, ISO, TY, S, MINB>,
+        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
         attr = true;
     }
@@ -746,9 +786,16 @@ static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps
     dim3 blk(32, TY, 1);
     dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
              (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
-    diff3d_grid_tma<LAM, ISO, TY, S, MINB><<<grd, blk, C::SMEM, s>>>(
-        mT, mL, mC, static_cast<float2*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err, bad);
+    diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64><<<grd, blk, C::SMEM, s>>>(mT, mL, mC, T2.ptr, p, T2.n[0], T2.n[1],
+                                                                           cb, L, d_err, run);
     return PS_OK;
+}
+
+template <bool LAM, bool ISO>
+static int launch_grid_step(bool last, const ps_array& Tin, const ps_array& Cs, const ps_array* Ls, const ps_array& T2,
+                            const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, GridRun* run) {
+    return last ? launch_grid_variant<LAM, ISO, true>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run)
+                : launch_grid_variant<LAM, ISO, false>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run);
 }
 
 // ---- multi-step runs -------------------------------------------------------------------
@@ -824,7 +871,7 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
                  tma_eligible(Ci) && (!has_lam || tma_eligible(lam_arr)) && cells.hi[0] > cells.lo[0] &&
                  cells.hi[1] > cells.lo[1] && cells.hi[2] > cells.lo[2];
     ps_array A = T, B = T2;
-    if (split && mode == PS_FP64_SPLIT_GRID) {
+    if (split && mode == PS_FP64_SPLIT_GRID && nt > 0) {
         // state, lam and Ci as grid / value pairs in scratch; T is written only by the final
         // conversion, which the device skips when a value left the grid range
         char* scr = nullptr;
@@ -841,30 +888,33 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
         const bool iso = split_coeffs(form, lam, dt, hx, hy, hz, &p, &G);
         const int g = st->num_sms * 8;
         PS_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(GridRun), s));
-        absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(T.ptr), n, &r->maxT);
-        if (has_lam) absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(lam_arr.ptr), n, &r->maxL);
+        const int64_t n2 = n / 2;  // nx is even (TMA eligibility)
+        absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(T.ptr), n2, &r->maxT);
+        if (has_lam) absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(lam_arr.ptr), n2, &r->maxL);
         grid_setup_kernel<<<1, 1, 0, s>>>(r, G, has_lam ? 1 : 0);
-        // T2's boundary values are T's (the documented precondition), so one pass fills both states
-        to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(T.ptr), static_cast<float2*>(Sa.ptr),
-                                         static_cast<float2*>(Sb.ptr), n, r, 0);
+        // T2's boundary values are T's (the documented precondition): Sb gets Sa's faces
+        to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(T.ptr), static_cast<float4*>(Sa.ptr), n2, r, 0);
+        grid_faces_kernel<<<dim3(st->num_sms, 6), 256, 0, s>>>(static_cast<const float2*>(Sa.ptr),
+                                                               static_cast<float2*>(Sb.ptr), T.n[0], T.n[1], T.n[2], r);
         if (has_lam)
-            to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(lam_arr.ptr), static_cast<float2*>(Ls.ptr),
-                                             nullptr, n, r, 1);
-        ci_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(Ci.ptr), static_cast<float2*>(Cs.ptr), n, r);
+            to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(lam_arr.ptr), static_cast<float4*>(Ls.ptr), n2,
+                                             r, 1);
+        ci_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(Ci.ptr), static_cast<float4*>(Cs.ptr), n2, r);
         A = Sa;
         B = Sb;
         for (int64_t it = 0; it < nt; ++it) {
+            const bool last = it == nt - 1;  // the last step writes T as IEEE doubles
+            const ps_array& out = last ? T : B;
             int rc;
             if (form == PS_DIFF_FLUX_LAM)
-                rc = iso ? launch_grid_variant<true, true>(A, Cs, &Ls, B, p, cells, L, s, st->d_err, &r->bad)
-                         : launch_grid_variant<true, false>(A, Cs, &Ls, B, p, cells, L, s, st->d_err, &r->bad);
+                rc = iso ? launch_grid_step<true, true>(last, A, Cs, &Ls, out, p, cells, L, s, st->d_err, r)
+                         : launch_grid_step<true, false>(last, A, Cs, &Ls, out, p, cells, L, s, st->d_err, r);
             else
-                rc = iso ? launch_grid_variant<false, true>(A, Cs, nullptr, B, p, cells, L, s, st->d_err, &r->bad)
-                         : launch_grid_variant<false, false>(A, Cs, nullptr, B, p, cells, L, s, st->d_err, &r->bad);
+                rc = iso ? launch_grid_step<false, true>(last, A, Cs, nullptr, out, p, cells, L, s, st->d_err, r)
+                         : launch_grid_step<false, false>(last, A, Cs, nullptr, out, p, cells, L, s, st->d_err, r);
             PS_TRY(rc);
             std::swap(A, B);
         }
-        from_grid_kernel<<<g, 256, 0, s>>>(static_cast<const float2*>(A.ptr), static_cast<double*>(T.ptr), n, r);
         PS_CUDA_TRY(cudaGetLastError());
         int bad = 0;
         PS_CUDA_TRY(cudaMemcpyAsync(&bad, &r->bad, sizeof(int), cudaMemcpyDeviceToHost, s));

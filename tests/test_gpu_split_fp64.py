@@ -212,3 +212,19 @@ def test_grid_run_growth_falls_back_to_split_state(ps):
         out[mode] = ps.to_host(dT)
     assert np.abs(out["split_state"]).max() > 1.0  # left the grid of max|T0| < 1
     assert np.array_equal(out["split_grid"], out["split_state"])
+
+
+def test_grid_run_growth_in_last_step(ps, oracle):
+    """Growth past the grid in the last step only: that step writes IEEE doubles directly (summed in
+    FP64 where a value left the grid), so no rerun is needed and the result stays within tolerance."""
+    n = (64, 40, 36)
+    T, Ci, lam, hs, dt = _setup(n, 3, seed=34)
+    dt = dt * 12.0
+    ref = T.copy(order="F")
+    oracle.diffusion3d_step(3, ref, T, Ci, lam, 0.0, dt, *hs)
+    assert np.abs(ref).max() > 1.0
+    dT, dT2 = ps.from_host(T), ps.from_host(T)
+    ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, dT, dT2, ps.from_host(Ci), ps.from_host(lam), dt, *hs, 1,
+                   fp64="split_grid")
+    e = relerr(ps.to_host(dT), ref)
+    assert e <= 1e-12, e
