@@ -65,7 +65,9 @@ typedef struct ps_array {
 typedef struct ps_launch {
     int32_t memopt;       /* 0: one thread per cell (`memopt=false`);
                              1: z-sweep with TMA-staged planes (`memopt=true`, loopdim z) */
-    int32_t loopsize;     /* z-planes swept by one CTA (`loopsize`); 0 = library default   */
+    int32_t loopsize;     /* z-planes swept by one CTA (`loopsize`); 0 = library default:
+                             chosen per launch from the number of CTA waves (the results do
+                             not depend on it) */
     int64_t range_lo[3];  /* `ranges` of the call as 0-based half-open thread-index boxes  */
     int64_t range_hi[3];  /* (hi <= lo in every dimension, or a NULL ps_launch = full grid) */
     int32_t fp64_mode;    /* FP64 arrays only. PS_FP64_IEEE: IEEE double arithmetic on the FP64

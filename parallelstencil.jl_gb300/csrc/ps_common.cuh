@@ -76,6 +76,37 @@ Box launch_box(const ps_launch* cfg, const int64_t grid[3]);
 int encode_plane_map(CUtensorMap* map, const ps_array& a, uint32_t bx, uint32_t by);
 bool tma_eligible(const ps_array& a);
 
+// z-sweep length for loopsize = 0: a launch of cta_xy CTAs per z-block over wz planes with
+// `slots` CTAs resident at once (occupancy x SMs) loses the idle part of its last wave and
+// re-reads two halo planes per z-block; the candidate with the best product wins (ties: longer).
+// Results do not depend on the choice (every cell is computed the same way).
+inline int auto_loopsize(int64_t cta_xy, int64_t wz, int64_t slots) {
+    static const int cand[] = {64, 56, 48, 40, 32, 28, 24, 20, 16};
+    int best = 64;
+    double best_score = -1.0;
+    for (int L : cand) {
+        const int64_t ctas = cta_xy * ((wz + L - 1) / L);
+        const int64_t waves = (ctas + slots - 1) / slots;
+        const double score = (double)ctas / (double)(waves * slots) * (double)L / (L + 2.0);
+        if (score > best_score + 1e-9) {
+            best_score = score;
+            best = L;
+        }
+    }
+    return best;
+}
+
+// CTAs of `kernel` resident per SM (queried once per kernel by the caller's static cache).
+template <typename K>
+inline int resident_ctas(K kernel, int threads, int smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n;
+}
+
 // ---------------------------------------------------------------------------------------
 // Device helpers.
 // ---------------------------------------------------------------------------------------

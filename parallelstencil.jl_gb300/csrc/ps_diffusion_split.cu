@@ -356,8 +356,14 @@ static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const p
     }
     int64_t x0 = cb.lo[0] & ~(int64_t)1;
     dim3 blk(32, TY, 1);
-    dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
-             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    const int64_t bx = (cb.hi[0] - x0 + SP_TX - 1) / SP_TX, by = (cb.hi[1] - cb.lo[1] + TY - 1) / TY;
+    if (L <= 0) {
+        static const int occ = resident_ctas(diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE>, 32 * TY, C::SMEM);
+        DeviceState* st = nullptr;
+        PS_TRY(current_state(&st));
+        L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
+    }
+    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
     diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE><<<grd, blk, C::SMEM, s>>>(
         mT, mL, mC, static_cast<double*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err);
     return PS_OK;
@@ -784,8 +790,14 @@ static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps
     }
     const int64_t x0 = cb.lo[0] & ~(int64_t)1;
     dim3 blk(32, TY, 1);
-    dim3 grd((unsigned)((cb.hi[0] - x0 + SP_TX - 1) / SP_TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
-             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    const int64_t bx = (cb.hi[0] - x0 + SP_TX - 1) / SP_TX, by = (cb.hi[1] - cb.lo[1] + TY - 1) / TY;
+    if (L <= 0) {
+        static const int occ = resident_ctas(diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64>, 32 * TY, C::SMEM);
+        DeviceState* st = nullptr;
+        PS_TRY(current_state(&st));
+        L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
+    }
+    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
     diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64><<<grd, blk, C::SMEM, s>>>(mT, mL, mC, T2.ptr, p, T2.n[0], T2.n[1],
                                                                            cb, L, d_err, run);
     return PS_OK;
@@ -866,7 +878,7 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
     const bool has_lam = form == PS_DIFF_FLUX_LAM;
     const Box full = {{0, 0, 0}, {T.n[0], T.n[1], T.n[2]}};
     const Box cells = {{1, 1, 1}, {T.n[0] - 1, T.n[1] - 1, T.n[2] - 1}};
-    const int L = loopsize > 0 ? loopsize : 64;
+    const int L = loopsize;  // 0: chosen per launch from the wave count
     bool split = T.dtype == PS_F64 && mode != PS_FP64_IEEE && tma_eligible(T) && tma_eligible(T2) &&
                  tma_eligible(Ci) && (!has_lam || tma_eligible(lam_arr)) && cells.hi[0] > cells.lo[0] &&
                  cells.hi[1] > cells.lo[1] && cells.hi[2] > cells.lo[2];

@@ -545,8 +545,9 @@ int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, co
                            double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
                            cudaStream_t s, int* d_err);
 
-// Default z-sweep length (`loopsize`): the reference uses 64 on compute capability >= 9
-// (src/parallel.jl:532-543); the same default is kept.
+// z-sweep length (`loopsize`) of the shared-memory fallback when none is given: the reference
+// uses 64 on compute capability >= 9 (src/parallel.jl:532-543). The TMA z-sweeps choose theirs
+// from the wave count (auto_loopsize).
 static constexpr int kDefaultLoopsize = 64;
 
 template <typename T, int FORM, int TY, int S>
@@ -568,8 +569,14 @@ static int launch_zsweep_tma(const ps_array& T2, const ps_array& Tin, const ps_a
     }
     int64_t x0 = cb.lo[0] & ~(int64_t)(Z::VEC - 1);
     dim3 blk(32, TY, 1);
-    dim3 grd((unsigned)((cb.hi[0] - x0 + Z::TX - 1) / Z::TX), (unsigned)((cb.hi[1] - cb.lo[1] + TY - 1) / TY),
-             (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    const int64_t bx = (cb.hi[0] - x0 + Z::TX - 1) / Z::TX, by = (cb.hi[1] - cb.lo[1] + TY - 1) / TY;
+    if (L <= 0) {
+        static const int occ = resident_ctas(diff3d_zsweep_tma<T, FORM, TY, S>, 32 * TY, Z::SMEM);
+        DeviceState* st = nullptr;
+        PS_TRY(current_state(&st));
+        L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
+    }
+    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
     diff3d_zsweep_tma<T, FORM, TY, S><<<grd, blk, Z::SMEM, s>>>(mT, mL, mC, static_cast<T*>(T2.ptr), p, T2.n[0],
                                                                 T2.n[1], cb, L, d_err);
     return PS_OK;
@@ -585,7 +592,7 @@ static int launch_diffusion(const ps_array& T2, const ps_array& Tin, const ps_ar
     int L = loopsize > 0 ? loopsize : kDefaultLoopsize;
     if (memopt) {
         bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
-        if (tma) return launch_zsweep_tma<T, FORM, 8, 4>(T2, Tin, Ci, lam, p, cb, L, s, d_err);
+        if (tma) return launch_zsweep_tma<T, FORM, 8, 4>(T2, Tin, Ci, lam, p, cb, loopsize, s, d_err);
         dim3 blk(32, 4, 1);
         dim3 grd((unsigned)((wx + 31) / 32), (unsigned)((wy + 3) / 4), (unsigned)((wz + L - 1) / L));
         diff3d_zsweep_smem<T, FORM, 4><<<grd, blk, 0, s>>>(static_cast<T*>(T2.ptr), static_cast<const T*>(Tin.ptr),
@@ -653,8 +660,7 @@ int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const p
     const ps_array* lp = form == PS_DIFF_FLUX_LAM ? &lam : nullptr;
     if (cb.hi[0] <= cb.lo[0] || cb.hi[1] <= cb.lo[1] || cb.hi[2] <= cb.lo[2]) return PS_OK;
     if (T2.dtype == PS_F64 && fp64_mode == PS_FP64_SPLIT) {
-        int L = loopsize > 0 ? loopsize : kDefaultLoopsize;
-        int rc = launch_diffusion_split(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, L, s, d_err);
+        int rc = launch_diffusion_split(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, loopsize, s, d_err);
         if (rc != PS_ERR_UNSUPPORTED) return rc;  // not TMA-eligible: IEEE kernels below
     }
     if (T2.dtype == PS_F64)
