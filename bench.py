@@ -345,6 +345,9 @@ def run_ours(a, world, rank, local):
             bench_kernel("memcopy3d_f64_256", ps.kernels.copy3D, arrs256, (), False, WORDS_MEMCOPY, n2, np.float64,
                          a.steps)
             del arrs256
+        stokes = None if a.quick else bench_stokes2d(ps, torch)
+        if stokes:
+            launches += stokes["fp64"]["iterations"] + stokes["mixed"]["iterations"]
     clocks = clk.summary()
 
     value = world * b_head / t_head / 1e9
@@ -371,6 +374,7 @@ def run_ours(a, world, rank, local):
                 "step": f"one {NT_JOB}-step diffusion job from pinned host buffers through the C ABI",
                 "seconds_per_job": round(t_e2e, 5)},
         "gpu_launches": launches,
+        "stokes2d_time_to_tol": stokes,
         "clocks": clocks,
         "variants": results,
     }
@@ -380,6 +384,30 @@ def run_ours(a, world, rank, local):
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def bench_stokes2d(ps, torch, n=1023, tol=1e-8):
+    """The Stokes2D PT workload: wall time to max residual < tol for the FP64 PT solver and the FP32
+    PT + FP64 defect-correction solver (1023^2, unit box, one inclusion r = 0.1, viscosity ratio
+    0.1, rho*g = 1 inside). Each solve is one ps_stokes2d_solve call (CUDA graphs of nout fused
+    iterations, FP64 residual check every nout)."""
+    from ps_gb300.stokes import Stokes2D, Stokes2DParams, inclusion_setup
+
+    Mus, Rog = inclusion_setup(n, n, 1.0, 1.0, musi=0.1)
+    out = {"config": f"{n}x{n} cells, unit box, inclusion r=0.1, viscosity ratio 0.1, rho*g=1 inside, "
+                     f"free slip, max(mean|Rx|, mean|Ry|, mean|divV|) < {tol}"}
+    for name, mode in (("fp64", 0), ("mixed", 1)):
+        g = Stokes2D(Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog)
+        g.compute_timesteps()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = g.solve(tol=tol, mode=mode, max_iter=5_000_000)
+        torch.cuda.synchronize()
+        out[name] = {"seconds": round(time.perf_counter() - t0, 4), "iterations": int(st.iters),
+                     "outer": int(st.outer), "err": float(st.err), "converged": bool(st.converged)}
+        del g
+    out["mixed_over_fp64"] = round(out["mixed"]["seconds"] / out["fp64"]["seconds"], 4)
+    return out
 
 
 def _oracle_slab_steps(n, slab, steps, warmup):

@@ -324,6 +324,55 @@ int ps_stokes2d_err(const ps_stokes2d_fields* f, double out_mean_abs[3], void* s
 int ps_stokes2d_solve(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int32_t mode, double tol,
                       int64_t max_iter, int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
 
+/* ------------------------------------------------------------------------------------ */
+/* Stokes3D miniapp (miniapps/Stokes3D.jl): the PT kernels of the 3-D analogue.          */
+/* ------------------------------------------------------------------------------------ */
+
+/* The miniapp's arrays (Stokes3D.jl:89-110), all of one dtype, (nx, ny, nz) = size(Pt):
+ * Pt, dtauPt, divV, Mus, Rog (nx,ny,nz); Vx (nx+1,ny,nz), Vy (nx,ny+1,nz), Vz (nx,ny,nz+1);
+ * txx (nx,ny-2,nz-2), tyy (nx-2,ny,nz-2), tzz (nx-2,ny-2,nz); txy (nx-1,ny-1,nz-2),
+ * txz (nx-1,ny-2,nz-1), tyz (nx-2,ny-1,nz-1); Rx, dVxdtau, dtauVx (nx-1,ny-2,nz-2);
+ * Ry, dVydtau, dtauVy (nx-2,ny-1,nz-2); Rz, dVzdtau, dtauVz (nx-2,ny-2,nz-1). */
+typedef struct ps_stokes3d_fields {
+    ps_array Pt, dtauPt, divV, Vx, Vy, Vz, txx, tyy, tzz, txy, txz, tyz, Rx, Ry, Rz, dVxdtau, dVydtau, dVzdtau,
+        dtauVx, dtauVy, dtauVz, Mus, Rog;
+} ps_stokes3d_fields;
+
+/* Scalars of Stokes3D.jl:72-88: dx, dy, dz, dampX = 1-Vdmp/nx, dampY, dampZ, Vsc, Ptsc,
+ * min_dxyz2 = min(dx,dy,dz)^2, max_nxyz = max(nx,ny,nz). */
+typedef struct ps_stokes3d_params {
+    double dx, dy, dz, dampX, dampY, dampZ, Vsc, Ptsc, min_dxyz2;
+    int64_t max_nxyz;
+} ps_stokes3d_params;
+
+/* The `@parallel` kernels one-to-one (Stokes3D.jl:11-50), bit-identical to the reference
+ * (FP64 and FP32 arrays). */
+int ps_stokes3d_timesteps(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync);
+int ps_stokes3d_compute_P(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync);
+int ps_stokes3d_compute_tau(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync);
+int ps_stokes3d_compute_dV(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync);
+int ps_stokes3d_compute_V(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync);
+/* `@parallel_indices` free-slip copies bc_x! / bc_y! / bc_z! (Stokes3D.jl:52-68) of a 3-D array. */
+int ps_bc_x3d(ps_array A, void* stream, int sync);
+int ps_bc_y3d(ps_array A, void* stream, int sync);
+int ps_bc_z3d(ps_array A, void* stream, int sync);
+
+/* n_iter iterations of the loop body (Stokes3D.jl:134-143: compute_P!, compute_τ!, compute_dV!,
+ * compute_V!, six bc calls) in three launches each, bit-identical to the reference's sequence.
+ * Synchronises. */
+int ps_stokes3d_iterate(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, int64_t n_iter, void* stream);
+
+/* mean(abs.(Rx)), mean(abs.(Ry)), mean(abs.(Rz)), mean(abs.(∇V)) of the stored arrays
+ * (Stokes3D.jl:145-146), accumulated in FP64. */
+int ps_stokes3d_err(const ps_stokes3d_fields* f, double out_mean_abs[4], void* stream);
+
+/* The `while err > ε && iter <= iterMax` loop (Stokes3D.jl:131-149) in FP64: CUDA graphs of nout
+ * iterations, the error checked after each. The dtau arrays must have been computed
+ * (ps_stokes3d_timesteps). Returns PS_ERR_NOT_CONVERGED at max_iter, PS_ERR_TIMEOUT after
+ * max_seconds (> 0), PS_ERR_NONFINITE on NaN/Inf residuals. */
+int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, double tol, int64_t max_iter,
+                      int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

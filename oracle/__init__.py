@@ -204,6 +204,87 @@ class Stokes2D:
         return max(m), tuple(m)
 
 
+STOKES3D_SHAPES = {  # extents relative to (nx, ny, nz) = size(Pt) (miniapps/Stokes3D.jl:89-110)
+    "Pt": (0, 0, 0), "dtauPt": (0, 0, 0), "divV": (0, 0, 0), "Vx": (1, 0, 0), "Vy": (0, 1, 0), "Vz": (0, 0, 1),
+    "txx": (0, -2, -2), "tyy": (-2, 0, -2), "tzz": (-2, -2, 0), "txy": (-1, -1, -2), "txz": (-1, -2, -1),
+    "tyz": (-2, -1, -1), "Rx": (-1, -2, -2), "Ry": (-2, -1, -2), "Rz": (-2, -2, -1), "dVxdtau": (-1, -2, -2),
+    "dVydtau": (-2, -1, -2), "dVzdtau": (-2, -2, -1), "dtauVx": (-1, -2, -2), "dtauVy": (-2, -1, -2),
+    "dtauVz": (-2, -2, -1), "Mus": (0, 0, 0), "Rog": (0, 0, 0)}
+
+
+class Stokes3D:
+    """The Stokes3D miniapp's arrays on the host and its kernels (miniapps/Stokes3D.jl:11-68) run by
+    the oracle; same field names as ps_gb300.stokes3d.Stokes3D."""
+
+    def __init__(self, nx, ny, nz, dx, dy, dz, Mus, Rog, Vdmp=4.0, Vsc=1.0, Ptsc=0.25, dtype=np.float64):
+        n = (nx, ny, nz)
+        self.n, self.dtype = n, np.dtype(dtype)
+        self.a = {k: np.asfortranarray(np.zeros(tuple(m + o for m, o in zip(n, off)), dtype=dtype))
+                  for k, off in STOKES3D_SHAPES.items() if k not in ("Mus", "Rog")}
+        self.a["Mus"] = np.asfortranarray(Mus.astype(dtype))
+        self.a["Rog"] = np.asfortranarray(Rog.astype(dtype))
+        self.dx, self.dy, self.dz = dx, dy, dz
+        self.damp = tuple(1.0 - Vdmp / m for m in n)
+        self.Vsc, self.Ptsc = Vsc, Ptsc
+        self.min_dxyz2, self.max_nxyz = min(dx, dy, dz) ** 2, max(n)
+
+    def _f(self, name):
+        return _fn(name, self.dtype)
+
+    def __getitem__(self, k):
+        return self.a[k]
+
+    def compute_timesteps(self):
+        R, a, i64 = _real(self.dtype), self.a, ctypes.c_int64
+        _check(self._f("orc_stokes3d_timesteps")(_ptr(a["dtauVx"]), _ptr(a["dtauVy"]), _ptr(a["dtauVz"]),
+                                                 _ptr(a["dtauPt"]), _ptr(a["Mus"]), *map(i64, self.n), R(self.Vsc),
+                                                 R(self.Ptsc), R(self.min_dxyz2), i64(self.max_nxyz)), "timesteps")
+
+    def compute_P(self):
+        R, a, i64 = _real(self.dtype), self.a, ctypes.c_int64
+        _check(self._f("orc_stokes3d_P")(_ptr(a["divV"]), _ptr(a["Pt"]), _ptr(a["Vx"]), _ptr(a["Vy"]), _ptr(a["Vz"]),
+                                         _ptr(a["dtauPt"]), *map(i64, self.n), R(self.dx), R(self.dy), R(self.dz)),
+               "P")
+
+    def compute_tau(self):
+        R, a, i64 = _real(self.dtype), self.a, ctypes.c_int64
+        _check(self._f("orc_stokes3d_tau")(*[_ptr(a[k]) for k in ("divV", "txx", "tyy", "tzz", "txy", "txz", "tyz",
+                                                                   "Vx", "Vy", "Vz", "Mus")],
+                                           *map(i64, self.n), R(self.dx), R(self.dy), R(self.dz)), "tau")
+
+    def compute_dV(self):
+        R, a, i64 = _real(self.dtype), self.a, ctypes.c_int64
+        _check(self._f("orc_stokes3d_dV")(*[_ptr(a[k]) for k in ("Rx", "Ry", "Rz", "dVxdtau", "dVydtau", "dVzdtau",
+                                                                  "Pt", "Rog", "txx", "tyy", "tzz", "txy", "txz",
+                                                                  "tyz")],
+                                          *map(i64, self.n), *map(R, self.damp), R(self.dx), R(self.dy), R(self.dz)),
+               "dV")
+
+    def compute_V(self):
+        a, i64 = self.a, ctypes.c_int64
+        _check(self._f("orc_stokes3d_V")(*[_ptr(a[k]) for k in ("Vx", "Vy", "Vz", "dVxdtau", "dVydtau", "dVzdtau",
+                                                                 "dtauVx", "dtauVy", "dtauVz")],
+                                         *map(i64, self.n)), "V")
+
+    def bc(self, which, name):
+        A = self.a[name]
+        _check(self._f("orc_bc_" + which + "3d")(_ptr(A), *map(ctypes.c_int64, A.shape)), "bc")
+
+    def step(self):
+        """One PT iteration as the miniapp's loop body (Stokes3D.jl:134-143)."""
+        self.compute_P()
+        self.compute_tau()
+        self.compute_dV()
+        self.compute_V()
+        for which, name in (("x", "Vy"), ("x", "Vz"), ("y", "Vx"), ("y", "Vz"), ("z", "Vx"), ("z", "Vy")):
+            self.bc(which, name)
+
+    def err(self):
+        """max(mean|Rx|, mean|Ry|, mean|Rz|, mean|∇V|) (Stokes3D.jl:145-146)."""
+        m = [float(np.mean(np.abs(self.a[k]))) for k in ("Rx", "Ry", "Rz", "divV")]
+        return max(m), tuple(m)
+
+
 def acoustic3d_p(P, Vx, Vy, Vz, dt, k, dx, dy, dz) -> None:
     R = _real(P.dtype)
     _check(_fn("orc_acoustic3d_p", P.dtype)(_ptr(P), _ptr(Vx), _ptr(Vy), _ptr(Vz), _n3(P), R(dt), R(k), R(dx),

@@ -401,3 +401,192 @@ int SFX(orc_bc_y2d)(REAL* A, int64_t n0, int64_t n1) {
 #undef I2
 
 #undef OIDX
+
+/* ------------------------------------------------------------------------------------- */
+/* Stokes3D miniapp kernels (miniapps/Stokes3D.jl:11-68). Arrays column-major; nx, ny, nz = */
+/* size(Pt). Grid = max extents of each kernel's array arguments; one mask per statement.   */
+/* ------------------------------------------------------------------------------------- */
+#define I3(a, b, c, n0, n1) ((int64_t)(a) + (int64_t)(n0) * ((int64_t)(b) + (int64_t)(n1) * (int64_t)(c)))
+
+/* compute_timesteps! (Stokes3D.jl:11-17): grid (nx, ny, nz). */
+int SFX(orc_stokes3d_timesteps)(REAL* dtVx, REAL* dtVy, REAL* dtVz, REAL* dtPt, const REAL* M, int64_t nx, int64_t ny,
+                                int64_t nz, REAL Vsc, REAL Ptsc, REAL min_dxyz2, int64_t max_nxyz) {
+    const REAL c61 = (REAL)6.1, h = (REAL)0.5, mn = (REAL)max_nxyz;
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < nz; z++)
+        for (int64_t y = 0; y < ny; y++)
+            for (int64_t x = 0; x < nx; x++) {
+                if (x < nx - 1 && y < ny - 2 && z < nz - 2) {
+                    REAL av = (M[I3(x, y + 1, z + 1, nx, ny)] + M[I3(x + 1, y + 1, z + 1, nx, ny)]) * h;
+                    dtVx[I3(x, y, z, nx - 1, ny - 2)] = ((Vsc * min_dxyz2) / av) / c61;
+                }
+                if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
+                    REAL av = (M[I3(x + 1, y, z + 1, nx, ny)] + M[I3(x + 1, y + 1, z + 1, nx, ny)]) * h;
+                    dtVy[I3(x, y, z, nx - 2, ny - 1)] = ((Vsc * min_dxyz2) / av) / c61;
+                }
+                if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
+                    REAL av = (M[I3(x + 1, y + 1, z, nx, ny)] + M[I3(x + 1, y + 1, z + 1, nx, ny)]) * h;
+                    dtVz[I3(x, y, z, nx - 2, ny - 2)] = ((Vsc * min_dxyz2) / av) / c61;
+                }
+                dtPt[I3(x, y, z, nx, ny)] = ((Ptsc * c61) * M[I3(x, y, z, nx, ny)]) / mn;
+            }
+    return ORC_OK;
+}
+
+/* compute_P! (Stokes3D.jl:19-23): grid (nx+1, ny+1, nz+1); statements masked by @all(∇V), @all(Pt). */
+int SFX(orc_stokes3d_P)(REAL* divV, REAL* Pt, const REAL* Vx, const REAL* Vy, const REAL* Vz, const REAL* dtPt,
+                        int64_t nx, int64_t ny, int64_t nz, REAL dx, REAL dy, REAL dz) {
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < nz; z++)
+        for (int64_t y = 0; y < ny; y++)
+            for (int64_t x = 0; x < nx; x++) {
+                int64_t c = I3(x, y, z, nx, ny);
+                divV[c] = ((Vx[I3(x + 1, y, z, nx + 1, ny)] - Vx[I3(x, y, z, nx + 1, ny)]) / dx +
+                           (Vy[I3(x, y + 1, z, nx, ny + 1)] - Vy[I3(x, y, z, nx, ny + 1)]) / dy) +
+                          (Vz[I3(x, y, z + 1, nx, ny)] - Vz[I3(x, y, z, nx, ny)]) / dz;
+                Pt[c] = Pt[c] - dtPt[c] * divV[c];
+            }
+    return ORC_OK;
+}
+
+/* compute_τ! (Stokes3D.jl:25-33): grid (nx+1, ny+1, nz+1). */
+int SFX(orc_stokes3d_tau)(const REAL* divV, REAL* txx, REAL* tyy, REAL* tzz, REAL* txy, REAL* txz, REAL* tyz,
+                          const REAL* Vx, const REAL* Vy, const REAL* Vz, const REAL* M, int64_t nx, int64_t ny,
+                          int64_t nz, REAL dx, REAL dy, REAL dz) {
+    const REAL two = (REAL)2.0, third = (REAL)1.0 / (REAL)3.0, h = (REAL)0.5, q = (REAL)0.25;
+    const int64_t X1 = nx + 1, Y1 = ny + 1;
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < nz; z++)
+        for (int64_t y = 0; y < ny; y++)
+            for (int64_t x = 0; x < nx; x++) {
+                if (y < ny - 2 && z < nz - 2) {
+                    int64_t c = I3(x, y + 1, z + 1, nx, ny);
+                    REAL d = (Vx[I3(x + 1, y + 1, z + 1, X1, ny)] - Vx[I3(x, y + 1, z + 1, X1, ny)]) / dx;
+                    txx[I3(x, y, z, nx, ny - 2)] = (two * M[c]) * (d - third * divV[c]);
+                }
+                if (x < nx - 2 && z < nz - 2) {
+                    int64_t c = I3(x + 1, y, z + 1, nx, ny);
+                    REAL d = (Vy[I3(x + 1, y + 1, z + 1, nx, Y1)] - Vy[I3(x + 1, y, z + 1, nx, Y1)]) / dy;
+                    tyy[I3(x, y, z, nx - 2, ny)] = (two * M[c]) * (d - third * divV[c]);
+                }
+                if (x < nx - 2 && y < ny - 2) {
+                    int64_t c = I3(x + 1, y + 1, z, nx, ny);
+                    REAL d = (Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - Vz[I3(x + 1, y + 1, z, nx, ny)]) / dz;
+                    tzz[I3(x, y, z, nx - 2, ny - 2)] = (two * M[c]) * (d - third * divV[c]);
+                }
+                if (x < nx - 1 && y < ny - 1 && z < nz - 2) {
+                    REAL av = (((M[I3(x, y, z + 1, nx, ny)] + M[I3(x + 1, y, z + 1, nx, ny)]) +
+                                M[I3(x, y + 1, z + 1, nx, ny)]) + M[I3(x + 1, y + 1, z + 1, nx, ny)]) * q;
+                    REAL a = Vx[I3(x + 1, y + 1, z + 1, X1, ny)] - Vx[I3(x + 1, y, z + 1, X1, ny)];
+                    REAL b = Vy[I3(x + 1, y + 1, z + 1, nx, Y1)] - Vy[I3(x, y + 1, z + 1, nx, Y1)];
+                    txy[I3(x, y, z, nx - 1, ny - 1)] = (two * av) * (h * (a / dy + b / dx));
+                }
+                if (x < nx - 1 && y < ny - 2 && z < nz - 1) {
+                    REAL av = (((M[I3(x, y + 1, z, nx, ny)] + M[I3(x + 1, y + 1, z, nx, ny)]) +
+                                M[I3(x, y + 1, z + 1, nx, ny)]) + M[I3(x + 1, y + 1, z + 1, nx, ny)]) * q;
+                    REAL a = Vx[I3(x + 1, y + 1, z + 1, X1, ny)] - Vx[I3(x + 1, y + 1, z, X1, ny)];
+                    REAL b = Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - Vz[I3(x, y + 1, z + 1, nx, ny)];
+                    txz[I3(x, y, z, nx - 1, ny - 2)] = (two * av) * (h * (a / dz + b / dx));
+                }
+                if (x < nx - 2 && y < ny - 1 && z < nz - 1) {
+                    REAL av = (((M[I3(x + 1, y, z, nx, ny)] + M[I3(x + 1, y + 1, z, nx, ny)]) +
+                                M[I3(x + 1, y, z + 1, nx, ny)]) + M[I3(x + 1, y + 1, z + 1, nx, ny)]) * q;
+                    REAL a = Vy[I3(x + 1, y + 1, z + 1, nx, Y1)] - Vy[I3(x + 1, y + 1, z, nx, Y1)];
+                    REAL b = Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - Vz[I3(x + 1, y, z + 1, nx, ny)];
+                    tyz[I3(x, y, z, nx - 2, ny - 1)] = (two * av) * (h * (a / dz + b / dy));
+                }
+            }
+    return ORC_OK;
+}
+
+/* compute_dV! (Stokes3D.jl:35-43): grid (nx, ny, nz). */
+int SFX(orc_stokes3d_dV)(REAL* Rx, REAL* Ry, REAL* Rz, REAL* dVxdt, REAL* dVydt, REAL* dVzdt, const REAL* Pt,
+                         const REAL* Rog, const REAL* txx, const REAL* tyy, const REAL* tzz, const REAL* txy,
+                         const REAL* txz, const REAL* tyz, int64_t nx, int64_t ny, int64_t nz, REAL dampX, REAL dampY,
+                         REAL dampZ, REAL dx, REAL dy, REAL dz) {
+    const REAL h = (REAL)0.5;
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < nz; z++)
+        for (int64_t y = 0; y < ny; y++)
+            for (int64_t x = 0; x < nx; x++) {
+                if (x < nx - 1 && y < ny - 2 && z < nz - 2) {
+                    int64_t r = I3(x, y, z, nx - 1, ny - 2);
+                    REAL a = txx[I3(x + 1, y, z, nx, ny - 2)] - txx[I3(x, y, z, nx, ny - 2)];
+                    REAL b = txy[I3(x, y + 1, z, nx - 1, ny - 1)] - txy[I3(x, y, z, nx - 1, ny - 1)];
+                    REAL c = txz[I3(x, y, z + 1, nx - 1, ny - 2)] - txz[I3(x, y, z, nx - 1, ny - 2)];
+                    REAL p = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x, y + 1, z + 1, nx, ny)];
+                    Rx[r] = ((a / dx + b / dy) + c / dz) - p / dx;
+                    dVxdt[r] = dampX * dVxdt[r] + Rx[r];
+                }
+                if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
+                    int64_t r = I3(x, y, z, nx - 2, ny - 1);
+                    REAL a = tyy[I3(x, y + 1, z, nx - 2, ny)] - tyy[I3(x, y, z, nx - 2, ny)];
+                    REAL b = txy[I3(x + 1, y, z, nx - 1, ny - 1)] - txy[I3(x, y, z, nx - 1, ny - 1)];
+                    REAL c = tyz[I3(x, y, z + 1, nx - 2, ny - 1)] - tyz[I3(x, y, z, nx - 2, ny - 1)];
+                    REAL p = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y, z + 1, nx, ny)];
+                    Ry[r] = ((a / dy + b / dx) + c / dz) - p / dy;
+                    dVydt[r] = dampY * dVydt[r] + Ry[r];
+                }
+                if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
+                    int64_t r = I3(x, y, z, nx - 2, ny - 2);
+                    REAL a = tzz[I3(x, y, z + 1, nx - 2, ny - 2)] - tzz[I3(x, y, z, nx - 2, ny - 2)];
+                    REAL b = txz[I3(x + 1, y, z, nx - 1, ny - 2)] - txz[I3(x, y, z, nx - 1, ny - 2)];
+                    REAL c = tyz[I3(x, y + 1, z, nx - 2, ny - 1)] - tyz[I3(x, y, z, nx - 2, ny - 1)];
+                    REAL p = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y + 1, z, nx, ny)];
+                    REAL g = (Rog[I3(x + 1, y + 1, z, nx, ny)] + Rog[I3(x + 1, y + 1, z + 1, nx, ny)]) * h;
+                    Rz[r] = (((a / dz + b / dx) + c / dy) - p / dz) + g;
+                    dVzdt[r] = dampZ * dVzdt[r] + Rz[r];
+                }
+            }
+    return ORC_OK;
+}
+
+/* compute_V! (Stokes3D.jl:45-50): grid (nx+1, ny+1, nz+1); @inn(Vx), @inn(Vy), @inn(Vz). */
+int SFX(orc_stokes3d_V)(REAL* Vx, REAL* Vy, REAL* Vz, const REAL* dVxdt, const REAL* dVydt, const REAL* dVzdt,
+                        const REAL* dtVx, const REAL* dtVy, const REAL* dtVz, int64_t nx, int64_t ny, int64_t nz) {
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < nz; z++)
+        for (int64_t y = 0; y < ny; y++)
+            for (int64_t x = 0; x < nx; x++) {
+                if (x < nx - 1 && y < ny - 2 && z < nz - 2) {
+                    int64_t v = I3(x + 1, y + 1, z + 1, nx + 1, ny), r = I3(x, y, z, nx - 1, ny - 2);
+                    Vx[v] = Vx[v] + dtVx[r] * dVxdt[r];
+                }
+                if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
+                    int64_t v = I3(x + 1, y + 1, z + 1, nx, ny + 1), r = I3(x, y, z, nx - 2, ny - 1);
+                    Vy[v] = Vy[v] + dtVy[r] * dVydt[r];
+                }
+                if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
+                    int64_t v = I3(x + 1, y + 1, z + 1, nx, ny), r = I3(x, y, z, nx - 2, ny - 2);
+                    Vz[v] = Vz[v] + dtVz[r] * dVzdt[r];
+                }
+            }
+    return ORC_OK;
+}
+
+/* bc_x! / bc_y! / bc_z! (Stokes3D.jl:52-68): copy the first inner plane onto the boundary plane. */
+int SFX(orc_bc_x3d)(REAL* A, int64_t n0, int64_t n1, int64_t n2) {
+    for (int64_t k = 0; k < n2; k++)
+        for (int64_t j = 0; j < n1; j++) {
+            A[I3(0, j, k, n0, n1)] = A[I3(1, j, k, n0, n1)];
+            A[I3(n0 - 1, j, k, n0, n1)] = A[I3(n0 - 2, j, k, n0, n1)];
+        }
+    return ORC_OK;
+}
+int SFX(orc_bc_y3d)(REAL* A, int64_t n0, int64_t n1, int64_t n2) {
+    for (int64_t k = 0; k < n2; k++)
+        for (int64_t i = 0; i < n0; i++) {
+            A[I3(i, 0, k, n0, n1)] = A[I3(i, 1, k, n0, n1)];
+            A[I3(i, n1 - 1, k, n0, n1)] = A[I3(i, n1 - 2, k, n0, n1)];
+        }
+    return ORC_OK;
+}
+int SFX(orc_bc_z3d)(REAL* A, int64_t n0, int64_t n1, int64_t n2) {
+    for (int64_t j = 0; j < n1; j++)
+        for (int64_t i = 0; i < n0; i++) {
+            A[I3(i, j, 0, n0, n1)] = A[I3(i, j, 1, n0, n1)];
+            A[I3(i, j, n2 - 1, n0, n1)] = A[I3(i, j, n2 - 2, n0, n1)];
+        }
+    return ORC_OK;
+}
+#undef I3

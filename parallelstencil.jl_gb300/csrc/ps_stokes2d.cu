@@ -621,7 +621,8 @@ static int solve_fp64(const ps_stokes2d_fields* f, const ps_stokes2d_params* pp,
         }
         it += nout;
         err = std::max(std::max(h[0] / nrx, h[1] / nry), h[2] / nd);
-        if (!std::isfinite(err)) {
+        if (!std::isfinite(h[0]) || !std::isfinite(h[1]) || !std::isfinite(h[2])) {  // std::max drops a NaN
+            err = NAN;
             rc = fail(PS_ERR_NONFINITE, "ps_stokes2d_solve: non-finite residual after %lld iterations", (long long)it);
             break;
         }
@@ -707,7 +708,8 @@ static int solve_mixed(const ps_stokes2d_fields* f, const ps_stokes2d_params* pp
             break;
         }
         err = std::max(std::max(h[0] / nrx, h[1] / nry), h[2] / nd);
-        if (!std::isfinite(err)) {
+        if (!std::isfinite(h[0]) || !std::isfinite(h[1]) || !std::isfinite(h[2])) {
+            err = NAN;
             rc = fail(PS_ERR_NONFINITE, "ps_stokes2d_solve: non-finite FP64 residual");
             break;
         }
@@ -732,7 +734,7 @@ static int solve_mixed(const ps_stokes2d_fields* f, const ps_stokes2d_params* pp
             it += nout;
             double prev = ierr;
             ierr = std::max(std::max(h[0] / nrx, h[1] / nry), h[2] / nd);
-            if (!std::isfinite(ierr)) {
+            if (!std::isfinite(h[0]) || !std::isfinite(h[1]) || !std::isfinite(h[2])) {
                 rc = fail(PS_ERR_NONFINITE, "ps_stokes2d_solve: non-finite FP32 residual");
                 break;
             }

@@ -1,0 +1,642 @@
+// ps_stokes3d.cu -- pseudo-transient (PT) viscous Stokes 3-D kernels and solver of libps_b200.so.
+//
+// Reference: miniapps/Stokes3D.jl:11-68 (kernels), :131-149 (PT loop and error check).
+//
+//   s3_* device functions   the arithmetic of each reference statement (operation order and
+//                           literals of the FD macros, src/FiniteDifferences.jl:328-388), shared
+//                           by every kernel below so all paths round identically
+//   one-to-one kernels      compute_timesteps!, compute_P!, compute_τ!, compute_dV!, compute_V!,
+//                           bc_x!, bc_y!, bc_z! -- drop-in replacements of the `@parallel` calls
+//   iteration kernels       one PT iteration in three launches:
+//                             s3_Ptau_k  ∇V, Pt and the six stresses of a cell; the normal
+//                                        stresses are indexed so that every thread uses the ∇V
+//                                        of its own cell (no re-read of ∇V from memory),
+//                             s3_dVV_k   residuals, pseudo-velocity and velocity updates,
+//                             s3_bc_k    the six free-slip copies of the loop body at once: the
+//                                        copies along different axes commute, so each boundary
+//                                        value is the composed copy of an interior value.
+//                           Results are bit-identical to the reference's ten-launch loop body.
+//   ps_stokes3d_solve       the `while err > ε` loop in FP64: CUDA graphs of `nout` iterations
+//                           followed by the FP64 residual norms, checked on the host.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+
+#include "ps_common.cuh"
+
+namespace ps {
+
+template <typename T>
+struct S3P {
+    T dx, dy, dz, dampX, dampY, dampZ, Vsc, Ptsc, min_dxyz2, max_nxyz;
+};
+
+template <typename T>
+static S3P<T> s3p(const ps_stokes3d_params& p) {
+    return S3P<T>{(T)p.dx,   (T)p.dy,  (T)p.dz,   (T)p.dampX,     (T)p.dampY,
+                  (T)p.dampZ, (T)p.Vsc, (T)p.Ptsc, (T)p.min_dxyz2, (T)p.max_nxyz};
+}
+
+// Device pointers of the miniapp's arrays (sizes relative to (nx, ny, nz) = size(Pt) as in
+// Stokes3D.jl:89-110).
+template <typename T>
+struct S3A {
+    T *Pt, *dtPt, *divV, *Vx, *Vy, *Vz, *txx, *tyy, *tzz, *txy, *txz, *tyz, *Rx, *Ry, *Rz, *dVx, *dVy, *dVz, *dtVx,
+        *dtVy, *dtVz;
+    const T *Mus, *Rog;
+    int64_t nx, ny, nz;
+};
+
+#define I3(a, b, c, n0, n1) ((int64_t)(a) + (int64_t)(n0) * ((int64_t)(b) + (int64_t)(n1) * (int64_t)(c)))
+
+// ---- statement arithmetic ------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T s3_dtV(T Vsc, T mdx2, T m0, T m1) {
+    const T av = (m0 + m1) * T(0.5);
+    return ((Vsc * mdx2) / av) / T(6.1);
+}
+template <typename T>
+__device__ __forceinline__ T s3_dtPt(T Ptsc, T m, T mn) {
+    return ((Ptsc * T(6.1)) * m) / mn;
+}
+// @d_xa(Vx)/dx + @d_ya(Vy)/dy + @d_za(Vz)/dz at cell (x, y, z)
+template <typename T>
+__device__ __forceinline__ T s3_divV(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
+    const int64_t nx = a.nx, ny = a.ny;
+    return ((a.Vx[I3(x + 1, y, z, nx + 1, ny)] - a.Vx[I3(x, y, z, nx + 1, ny)]) / p.dx +
+            (a.Vy[I3(x, y + 1, z, nx, ny + 1)] - a.Vy[I3(x, y, z, nx, ny + 1)]) / p.dy) +
+           (a.Vz[I3(x, y, z + 1, nx, ny)] - a.Vz[I3(x, y, z, nx, ny)]) / p.dz;
+}
+// 2.0*μ*(dV/h - 1.0/3.0*∇V)
+template <typename T>
+__device__ __forceinline__ T s3_tnn(T m, T v1, T v0, T h, T d) {
+    return (T(2.0) * m) * ((v1 - v0) / h - (T(1.0) / T(3.0)) * d);
+}
+// 2.0*@av_..i(μ)*(0.5*(a/ha + b/hb)), the four μ in the macro's order
+template <typename T>
+__device__ __forceinline__ T s3_tsh(T m0, T m1, T m2, T m3, T a, T ha, T b, T hb) {
+    const T av = (((m0 + m1) + m2) + m3) * T(0.25);
+    return (T(2.0) * av) * (T(0.5) * (a / ha + b / hb));
+}
+
+template <typename T>
+__device__ __forceinline__ void s3_txy(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
+    const int64_t nx = a.nx, ny = a.ny;
+    const T* M = a.Mus;
+    a.txy[I3(x, y, z, nx - 1, ny - 1)] =
+        s3_tsh(M[I3(x, y, z + 1, nx, ny)], M[I3(x + 1, y, z + 1, nx, ny)], M[I3(x, y + 1, z + 1, nx, ny)],
+               M[I3(x + 1, y + 1, z + 1, nx, ny)],
+               a.Vx[I3(x + 1, y + 1, z + 1, nx + 1, ny)] - a.Vx[I3(x + 1, y, z + 1, nx + 1, ny)], p.dy,
+               a.Vy[I3(x + 1, y + 1, z + 1, nx, ny + 1)] - a.Vy[I3(x, y + 1, z + 1, nx, ny + 1)], p.dx);
+}
+template <typename T>
+__device__ __forceinline__ void s3_txz(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
+    const int64_t nx = a.nx, ny = a.ny;
+    const T* M = a.Mus;
+    a.txz[I3(x, y, z, nx - 1, ny - 2)] =
+        s3_tsh(M[I3(x, y + 1, z, nx, ny)], M[I3(x + 1, y + 1, z, nx, ny)], M[I3(x, y + 1, z + 1, nx, ny)],
+               M[I3(x + 1, y + 1, z + 1, nx, ny)],
+               a.Vx[I3(x + 1, y + 1, z + 1, nx + 1, ny)] - a.Vx[I3(x + 1, y + 1, z, nx + 1, ny)], p.dz,
+               a.Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - a.Vz[I3(x, y + 1, z + 1, nx, ny)], p.dx);
+}
+template <typename T>
+__device__ __forceinline__ void s3_tyz(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
+    const int64_t nx = a.nx, ny = a.ny;
+    const T* M = a.Mus;
+    a.tyz[I3(x, y, z, nx - 2, ny - 1)] =
+        s3_tsh(M[I3(x + 1, y, z, nx, ny)], M[I3(x + 1, y + 1, z, nx, ny)], M[I3(x + 1, y, z + 1, nx, ny)],
+               M[I3(x + 1, y + 1, z + 1, nx, ny)],
+               a.Vy[I3(x + 1, y + 1, z + 1, nx, ny + 1)] - a.Vy[I3(x + 1, y + 1, z, nx, ny + 1)], p.dz,
+               a.Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - a.Vz[I3(x + 1, y, z + 1, nx, ny)], p.dy);
+}
+
+// compute_dV! statements at residual index (x, y, z) and, with update_V, compute_V! at the same
+// index (it reads only the pseudo-velocity just written)
+template <typename T>
+__device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z,
+                                      bool update_V) {
+    const int64_t nx = a.nx, ny = a.ny, nz = a.nz;
+    const T* Pt = a.Pt;
+    if (x < nx - 1 && y < ny - 2 && z < nz - 2) {
+        const int64_t r = I3(x, y, z, nx - 1, ny - 2);
+        const T A = a.txx[I3(x + 1, y, z, nx, ny - 2)] - a.txx[I3(x, y, z, nx, ny - 2)];
+        const T B = a.txy[I3(x, y + 1, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
+        const T C = a.txz[I3(x, y, z + 1, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
+        const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x, y + 1, z + 1, nx, ny)];
+        const T R = ((A / p.dx + B / p.dy) + C / p.dz) - P / p.dx;
+        a.Rx[r] = R;
+        const T dv = p.dampX * a.dVx[r] + R;
+        a.dVx[r] = dv;
+        if (update_V) {
+            const int64_t v = I3(x + 1, y + 1, z + 1, nx + 1, ny);
+            a.Vx[v] = a.Vx[v] + a.dtVx[r] * dv;
+        }
+    }
+    if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
+        const int64_t r = I3(x, y, z, nx - 2, ny - 1);
+        const T A = a.tyy[I3(x, y + 1, z, nx - 2, ny)] - a.tyy[I3(x, y, z, nx - 2, ny)];
+        const T B = a.txy[I3(x + 1, y, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
+        const T C = a.tyz[I3(x, y, z + 1, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
+        const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y, z + 1, nx, ny)];
+        const T R = ((A / p.dy + B / p.dx) + C / p.dz) - P / p.dy;
+        a.Ry[r] = R;
+        const T dv = p.dampY * a.dVy[r] + R;
+        a.dVy[r] = dv;
+        if (update_V) {
+            const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny + 1);
+            a.Vy[v] = a.Vy[v] + a.dtVy[r] * dv;
+        }
+    }
+    if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
+        const int64_t r = I3(x, y, z, nx - 2, ny - 2);
+        const T A = a.tzz[I3(x, y, z + 1, nx - 2, ny - 2)] - a.tzz[I3(x, y, z, nx - 2, ny - 2)];
+        const T B = a.txz[I3(x + 1, y, z, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
+        const T C = a.tyz[I3(x, y + 1, z, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
+        const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y + 1, z, nx, ny)];
+        const T G = (a.Rog[I3(x + 1, y + 1, z, nx, ny)] + a.Rog[I3(x + 1, y + 1, z + 1, nx, ny)]) * T(0.5);
+        const T R = (((A / p.dz + B / p.dx) + C / p.dy) - P / p.dz) + G;
+        a.Rz[r] = R;
+        const T dv = p.dampZ * a.dVz[r] + R;
+        a.dVz[r] = dv;
+        if (update_V) {
+            const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny);
+            a.Vz[v] = a.Vz[v] + a.dtVz[r] * dv;
+        }
+    }
+}
+
+#define S3_IDX                                                                               \
+    const int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                        \
+    const int64_t y = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;                        \
+    const int64_t z = blockIdx.z;                                                            \
+    const int64_t nx = a.nx, ny = a.ny, nz = a.nz;                                           \
+    if (x >= nx || y >= ny || z >= nz) return
+
+// ---- one-to-one kernels (grid: max extents of the kernel's array arguments) ---------------
+template <typename T>
+__global__ void s3_timesteps_k(S3A<T> a, S3P<T> p) {
+    S3_IDX;
+    const T* M = a.Mus;
+    if (x < nx - 1 && y < ny - 2 && z < nz - 2)
+        a.dtVx[I3(x, y, z, nx - 1, ny - 2)] =
+            s3_dtV(p.Vsc, p.min_dxyz2, M[I3(x, y + 1, z + 1, nx, ny)], M[I3(x + 1, y + 1, z + 1, nx, ny)]);
+    if (x < nx - 2 && y < ny - 1 && z < nz - 2)
+        a.dtVy[I3(x, y, z, nx - 2, ny - 1)] =
+            s3_dtV(p.Vsc, p.min_dxyz2, M[I3(x + 1, y, z + 1, nx, ny)], M[I3(x + 1, y + 1, z + 1, nx, ny)]);
+    if (x < nx - 2 && y < ny - 2 && z < nz - 1)
+        a.dtVz[I3(x, y, z, nx - 2, ny - 2)] =
+            s3_dtV(p.Vsc, p.min_dxyz2, M[I3(x + 1, y + 1, z, nx, ny)], M[I3(x + 1, y + 1, z + 1, nx, ny)]);
+    a.dtPt[I3(x, y, z, nx, ny)] = s3_dtPt(p.Ptsc, M[I3(x, y, z, nx, ny)], p.max_nxyz);
+}
+
+template <typename T>
+__global__ void s3_P_k(S3A<T> a, S3P<T> p) {
+    S3_IDX;
+    const int64_t c = I3(x, y, z, nx, ny);
+    const T d = s3_divV(a, p, x, y, z);
+    a.divV[c] = d;
+    a.Pt[c] = a.Pt[c] - a.dtPt[c] * d;
+}
+
+template <typename T>
+__global__ void s3_tau_k(S3A<T> a, S3P<T> p) {
+    S3_IDX;
+    const T* M = a.Mus;
+    if (y < ny - 2 && z < nz - 2) {
+        const int64_t c = I3(x, y + 1, z + 1, nx, ny);
+        a.txx[I3(x, y, z, nx, ny - 2)] = s3_tnn(M[c], a.Vx[I3(x + 1, y + 1, z + 1, nx + 1, ny)],
+                                                a.Vx[I3(x, y + 1, z + 1, nx + 1, ny)], p.dx, a.divV[c]);
+    }
+    if (x < nx - 2 && z < nz - 2) {
+        const int64_t c = I3(x + 1, y, z + 1, nx, ny);
+        a.tyy[I3(x, y, z, nx - 2, ny)] = s3_tnn(M[c], a.Vy[I3(x + 1, y + 1, z + 1, nx, ny + 1)],
+                                                a.Vy[I3(x + 1, y, z + 1, nx, ny + 1)], p.dy, a.divV[c]);
+    }
+    if (x < nx - 2 && y < ny - 2) {
+        const int64_t c = I3(x + 1, y + 1, z, nx, ny);
+        a.tzz[I3(x, y, z, nx - 2, ny - 2)] = s3_tnn(M[c], a.Vz[I3(x + 1, y + 1, z + 1, nx, ny)],
+                                                    a.Vz[I3(x + 1, y + 1, z, nx, ny)], p.dz, a.divV[c]);
+    }
+    if (x < nx - 1 && y < ny - 1 && z < nz - 2) s3_txy(a, p, x, y, z);
+    if (x < nx - 1 && y < ny - 2 && z < nz - 1) s3_txz(a, p, x, y, z);
+    if (x < nx - 2 && y < ny - 1 && z < nz - 1) s3_tyz(a, p, x, y, z);
+}
+
+template <typename T>
+__global__ void s3_dV_k(S3A<T> a, S3P<T> p) {
+    S3_IDX;
+    s3_dV(a, p, x, y, z, false);
+}
+
+template <typename T>
+__global__ void s3_V_k(S3A<T> a) {
+    S3_IDX;
+    if (x < nx - 1 && y < ny - 2 && z < nz - 2) {
+        const int64_t v = I3(x + 1, y + 1, z + 1, nx + 1, ny), r = I3(x, y, z, nx - 1, ny - 2);
+        a.Vx[v] = a.Vx[v] + a.dtVx[r] * a.dVx[r];
+    }
+    if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
+        const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny + 1), r = I3(x, y, z, nx - 2, ny - 1);
+        a.Vy[v] = a.Vy[v] + a.dtVy[r] * a.dVy[r];
+    }
+    if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
+        const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny), r = I3(x, y, z, nx - 2, ny - 2);
+        a.Vz[v] = a.Vz[v] + a.dtVz[r] * a.dVz[r];
+    }
+}
+
+// bc_x! / bc_y! / bc_z! (Stokes3D.jl:52-68): the boundary planes of axis `ax` copy the first
+// inner planes; threads run over the other two axes.
+template <typename T>
+__global__ void s3_bc_axis_k(T* A, int64_t n0, int64_t n1, int64_t n2, int ax) {
+    const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, v = blockIdx.y;
+    const int64_t n[3] = {n0, n1, n2};
+    const int o0 = ax == 0 ? 1 : 0, o1 = ax == 2 ? 1 : 2;  // the two other axes
+    if (u >= n[o0] || v >= n[o1]) return;
+    int64_t i[3];
+    i[o0] = u;
+    i[o1] = v;
+    i[ax] = 0;
+    const int64_t lo = I3(i[0], i[1], i[2], n0, n1);
+    i[ax] = 1;
+    const int64_t lo1 = I3(i[0], i[1], i[2], n0, n1);
+    i[ax] = n[ax] - 1;
+    const int64_t hi = I3(i[0], i[1], i[2], n0, n1);
+    i[ax] = n[ax] - 2;
+    const int64_t hi1 = I3(i[0], i[1], i[2], n0, n1);
+    A[lo] = A[lo1];
+    A[hi] = A[hi1];
+}
+
+// ---- iteration kernels ---------------------------------------------------------------------
+// compute_P! and compute_τ! of cell (x, y, z): τxx, τyy, τzz are written at the index whose ∇V
+// is this cell's, τxy, τxz, τyz at the cell's own index.
+template <typename T>
+__global__ void s3_Ptau_k(S3A<T> a, S3P<T> p) {
+    S3_IDX;
+    const int64_t c = I3(x, y, z, nx, ny);
+    const T d = s3_divV(a, p, x, y, z);
+    a.divV[c] = d;
+    a.Pt[c] = a.Pt[c] - a.dtPt[c] * d;
+    const T m = a.Mus[c];
+    const bool iy = y >= 1 && y <= ny - 2, iz = z >= 1 && z <= nz - 2, ix = x >= 1 && x <= nx - 2;
+    if (iy && iz)
+        a.txx[I3(x, y - 1, z - 1, nx, ny - 2)] =
+            s3_tnn(m, a.Vx[I3(x + 1, y, z, nx + 1, ny)], a.Vx[I3(x, y, z, nx + 1, ny)], p.dx, d);
+    if (ix && iz)
+        a.tyy[I3(x - 1, y, z - 1, nx - 2, ny)] =
+            s3_tnn(m, a.Vy[I3(x, y + 1, z, nx, ny + 1)], a.Vy[I3(x, y, z, nx, ny + 1)], p.dy, d);
+    if (ix && iy)
+        a.tzz[I3(x - 1, y - 1, z, nx - 2, ny - 2)] =
+            s3_tnn(m, a.Vz[I3(x, y, z + 1, nx, ny)], a.Vz[I3(x, y, z, nx, ny)], p.dz, d);
+    if (x < nx - 1 && y < ny - 1 && z < nz - 2) s3_txy(a, p, x, y, z);
+    if (x < nx - 1 && y < ny - 2 && z < nz - 1) s3_txz(a, p, x, y, z);
+    if (x < nx - 2 && y < ny - 1 && z < nz - 1) s3_tyz(a, p, x, y, z);
+}
+
+template <typename T>
+__global__ void s3_dVV_k(S3A<T> a, S3P<T> p) {
+    S3_IDX;
+    s3_dV(a, p, x, y, z, true);
+}
+
+// The loop body's six copies (bc_x!(Vy), bc_x!(Vz), bc_y!(Vx), bc_y!(Vz), bc_z!(Vx), bc_z!(Vy)):
+// velocity component c is copied along the two axes other than c. Job j = 4*c + face: faces 0/1
+// are the low/high planes of the first copied axis, 2/3 of the second. The value written at a
+// boundary cell is A[clamp(i)] with every copied axis clamped into [1, n-2]: that is what the
+// sequence of two copies leaves, in either order, and no source is itself written here.
+template <typename T>
+__global__ void s3_bc_k(S3A<T> a) {
+    const int job = blockIdx.y, c = job >> 2, face = job & 3;
+    T* A = c == 0 ? a.Vx : c == 1 ? a.Vy : a.Vz;
+    const int64_t n[3] = {a.nx + (c == 0), a.ny + (c == 1), a.nz + (c == 2)};
+    const int ax0 = c == 0 ? 1 : 0, ax1 = c == 2 ? 1 : 2;  // the copied axes
+    const int fa = face < 2 ? ax0 : ax1;                   // this face's axis
+    const int u0 = fa == 0 ? 1 : 0, u1 = fa == 2 ? 1 : 2;  // axes spanning the face
+    const int64_t cnt = n[u0] * n[u1];
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < cnt; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i[3];
+        i[u0] = t % n[u0];
+        i[u1] = t / n[u0];
+        i[fa] = (face & 1) ? n[fa] - 1 : 0;
+        int64_t s[3] = {i[0], i[1], i[2]};
+        s[ax0] = s[ax0] < 1 ? 1 : s[ax0] > n[ax0] - 2 ? n[ax0] - 2 : s[ax0];
+        s[ax1] = s[ax1] < 1 ? 1 : s[ax1] > n[ax1] - 2 ? n[ax1] - 2 : s[ax1];
+        A[I3(i[0], i[1], i[2], n[0], n[1])] = A[I3(s[0], s[1], s[2], n[0], n[1])];
+    }
+}
+
+__device__ __forceinline__ double s3_warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// sum |a| of four arrays into out[0..3] (job = blockIdx.y)
+template <typename T>
+__global__ void s3_sum_abs_k(const T* a0, int64_t n0, const T* a1, int64_t n1, const T* a2, int64_t n2, const T* a3,
+                             int64_t n3, double* out) {
+    const T* a = blockIdx.y == 0 ? a0 : blockIdx.y == 1 ? a1 : blockIdx.y == 2 ? a2 : a3;
+    const int64_t n = blockIdx.y == 0 ? n0 : blockIdx.y == 1 ? n1 : blockIdx.y == 2 ? n2 : n3;
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += fabs((double)a[i]);
+    s = s3_warp_sum(s);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out + blockIdx.y, s);
+}
+
+// ---- host side -----------------------------------------------------------------------------
+static int check3(const ps_array& a, int64_t n0, int64_t n1, int64_t n2, int32_t dt, const char* name) {
+    PS_TRY(check_array(a, name));
+    if (a.dtype != dt) return fail(PS_ERR_DTYPE, "Stokes3D: array %s has a different dtype", name);
+    return check_shape(a, n0, n1, n2, name);
+}
+
+static int check_fields3(const ps_stokes3d_fields* f, bool need_dt) {
+    if (!f) return fail(PS_ERR_NULL, "Stokes3D: NULL fields");
+    PS_TRY(check_array(f->Pt, "Pt"));
+    const int64_t X = f->Pt.n[0], Y = f->Pt.n[1], Z = f->Pt.n[2];
+    const int32_t dt = f->Pt.dtype;
+    if (X < 3 || Y < 3 || Z < 3) return fail(PS_ERR_SHAPE, "Stokes3D: Pt must have nx, ny, nz >= 3");
+    if (X > (int64_t)INT32_MAX || Y > 65535 * 8 || Z > 65535) return fail(PS_ERR_SHAPE, "Stokes3D: grid too large");
+    PS_TRY(check3(f->Vx, X + 1, Y, Z, dt, "Vx"));
+    PS_TRY(check3(f->Vy, X, Y + 1, Z, dt, "Vy"));
+    PS_TRY(check3(f->Vz, X, Y, Z + 1, dt, "Vz"));
+    PS_TRY(check3(f->divV, X, Y, Z, dt, "∇V"));
+    PS_TRY(check3(f->txx, X, Y - 2, Z - 2, dt, "τxx"));
+    PS_TRY(check3(f->tyy, X - 2, Y, Z - 2, dt, "τyy"));
+    PS_TRY(check3(f->tzz, X - 2, Y - 2, Z, dt, "τzz"));
+    PS_TRY(check3(f->txy, X - 1, Y - 1, Z - 2, dt, "τxy"));
+    PS_TRY(check3(f->txz, X - 1, Y - 2, Z - 1, dt, "τxz"));
+    PS_TRY(check3(f->tyz, X - 2, Y - 1, Z - 1, dt, "τyz"));
+    PS_TRY(check3(f->Rx, X - 1, Y - 2, Z - 2, dt, "Rx"));
+    PS_TRY(check3(f->Ry, X - 2, Y - 1, Z - 2, dt, "Ry"));
+    PS_TRY(check3(f->Rz, X - 2, Y - 2, Z - 1, dt, "Rz"));
+    PS_TRY(check3(f->dVxdtau, X - 1, Y - 2, Z - 2, dt, "dVxdτ"));
+    PS_TRY(check3(f->dVydtau, X - 2, Y - 1, Z - 2, dt, "dVydτ"));
+    PS_TRY(check3(f->dVzdtau, X - 2, Y - 2, Z - 1, dt, "dVzdτ"));
+    PS_TRY(check3(f->Mus, X, Y, Z, dt, "Mus"));
+    PS_TRY(check3(f->Rog, X, Y, Z, dt, "Rog"));
+    if (need_dt) {
+        PS_TRY(check3(f->dtauPt, X, Y, Z, dt, "dτPt"));
+        PS_TRY(check3(f->dtauVx, X - 1, Y - 2, Z - 2, dt, "dτVx"));
+        PS_TRY(check3(f->dtauVy, X - 2, Y - 1, Z - 2, dt, "dτVy"));
+        PS_TRY(check3(f->dtauVz, X - 2, Y - 2, Z - 1, dt, "dτVz"));
+    }
+    return PS_OK;
+}
+
+template <typename T>
+static S3A<T> s3a(const ps_stokes3d_fields* f) {
+    auto P = [](const ps_array& a) { return static_cast<T*>(a.ptr); };
+    S3A<T> a;
+    a.Pt = P(f->Pt);
+    a.dtPt = P(f->dtauPt);
+    a.divV = P(f->divV);
+    a.Vx = P(f->Vx);
+    a.Vy = P(f->Vy);
+    a.Vz = P(f->Vz);
+    a.txx = P(f->txx);
+    a.tyy = P(f->tyy);
+    a.tzz = P(f->tzz);
+    a.txy = P(f->txy);
+    a.txz = P(f->txz);
+    a.tyz = P(f->tyz);
+    a.Rx = P(f->Rx);
+    a.Ry = P(f->Ry);
+    a.Rz = P(f->Rz);
+    a.dVx = P(f->dVxdtau);
+    a.dVy = P(f->dVydtau);
+    a.dVz = P(f->dVzdtau);
+    a.dtVx = P(f->dtauVx);
+    a.dtVy = P(f->dtauVy);
+    a.dtVz = P(f->dtauVz);
+    a.Mus = P(f->Mus);
+    a.Rog = P(f->Rog);
+    a.nx = f->Pt.n[0];
+    a.ny = f->Pt.n[1];
+    a.nz = f->Pt.n[2];
+    return a;
+}
+
+// grid over (wx, wy, wz) with (32, 8, 1) blocks
+static dim3 g3(int64_t wx, int64_t wy, int64_t wz) {
+    return dim3((unsigned)((wx + 31) / 32), (unsigned)((wy + 7) / 8), (unsigned)wz);
+}
+
+enum S3Kernel { S3_TIMESTEPS, S3_P, S3_TAU, S3_DV, S3_V, S3_PTAU, S3_DVV, S3_BC };
+
+template <typename T>
+static void s3_launch(S3Kernel k, const S3A<T>& a, const S3P<T>& p, cudaStream_t s) {
+    const dim3 b(32, 8, 1);
+    // The reference's grid is the max extent of the array arguments ((nx+1, ny+1, nz+1) where a
+    // staggered velocity is one), but every statement's mask lies inside (nx, ny, nz): the
+    // threads beyond it do nothing, so all kernels run on the cell grid.
+    const dim3 gc = g3(a.nx, a.ny, a.nz);
+    switch (k) {
+    case S3_TIMESTEPS: s3_timesteps_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_P: s3_P_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_TAU: s3_tau_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_DV: s3_dV_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_V: s3_V_k<T><<<gc, b, 0, s>>>(a); break;
+    case S3_PTAU: s3_Ptau_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_DVV: s3_dVV_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_BC: {
+        const int64_t face = std::max(std::max((a.nx + 1) * (a.ny + 1), (a.nx + 1) * (a.nz + 1)), (a.ny + 1) * (a.nz + 1));
+        s3_bc_k<T><<<dim3((unsigned)std::min<int64_t>((face + 255) / 256, 1024), 12), 256, 0, s>>>(a);
+        break;
+    }
+    }
+}
+
+template <typename T>
+static void s3_iteration(const S3A<T>& a, const S3P<T>& p, cudaStream_t s) {
+    s3_launch(S3_PTAU, a, p, s);
+    s3_launch(S3_DVV, a, p, s);
+    s3_launch(S3_BC, a, p, s);
+}
+
+static int s3_entry(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, S3Kernel k, void* stream, int sync,
+                    const char* what) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_fields3(f, true));
+    if (!p) return fail(PS_ERR_NULL, "NULL params");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (f->Pt.dtype == PS_F64)
+        s3_launch<double>(k, s3a<double>(f), s3p<double>(*p), s);
+    else
+        s3_launch<float>(k, s3a<float>(f), s3p<float>(*p), s);
+    return finish_launch(s, sync, what);
+}
+
+static double now_s3() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" {
+
+int ps_stokes3d_timesteps(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync) {
+    return s3_entry(f, p, S3_TIMESTEPS, stream, sync, "ps_stokes3d_timesteps");
+}
+int ps_stokes3d_compute_P(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync) {
+    return s3_entry(f, p, S3_P, stream, sync, "ps_stokes3d_compute_P");
+}
+int ps_stokes3d_compute_tau(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync) {
+    return s3_entry(f, p, S3_TAU, stream, sync, "ps_stokes3d_compute_tau");
+}
+int ps_stokes3d_compute_dV(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync) {
+    return s3_entry(f, p, S3_DV, stream, sync, "ps_stokes3d_compute_dV");
+}
+int ps_stokes3d_compute_V(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, void* stream, int sync) {
+    return s3_entry(f, p, S3_V, stream, sync, "ps_stokes3d_compute_V");
+}
+
+static int bc3(ps_array A, void* stream, int sync, int ax, const char* what) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_array(A, "A"));
+    if (A.n[0] < 3 || A.n[1] < 3 || A.n[2] < 3) return fail(PS_ERR_SHAPE, "%s: A must be 3-D with extents >= 3", what);
+    const int o0 = ax == 0 ? 1 : 0, o1 = ax == 2 ? 1 : 2;
+    if (A.n[o1] > 65535) return fail(PS_ERR_SHAPE, "%s: extent too large", what);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dim3 g((unsigned)((A.n[o0] + 127) / 128), (unsigned)A.n[o1]);
+    if (A.dtype == PS_F64)
+        s3_bc_axis_k<double><<<g, 128, 0, s>>>(static_cast<double*>(A.ptr), A.n[0], A.n[1], A.n[2], ax);
+    else
+        s3_bc_axis_k<float><<<g, 128, 0, s>>>(static_cast<float*>(A.ptr), A.n[0], A.n[1], A.n[2], ax);
+    return finish_launch(s, sync, what);
+}
+
+int ps_bc_x3d(ps_array A, void* stream, int sync) { return bc3(A, stream, sync, 0, "ps_bc_x3d"); }
+int ps_bc_y3d(ps_array A, void* stream, int sync) { return bc3(A, stream, sync, 1, "ps_bc_y3d"); }
+int ps_bc_z3d(ps_array A, void* stream, int sync) { return bc3(A, stream, sync, 2, "ps_bc_z3d"); }
+
+int ps_stokes3d_iterate(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, int64_t n_iter, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_fields3(f, true));
+    if (!p) return fail(PS_ERR_NULL, "NULL params");
+    if (n_iter < 0) return fail(PS_ERR_ARG, "n_iter must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (int64_t it = 0; it < n_iter; ++it) {
+        if (f->Pt.dtype == PS_F64)
+            s3_iteration<double>(s3a<double>(f), s3p<double>(*p), s);
+        else
+            s3_iteration<float>(s3a<float>(f), s3p<float>(*p), s);
+    }
+    return finish_launch(s, 1, "ps_stokes3d_iterate");
+}
+
+int ps_stokes3d_err(const ps_stokes3d_fields* f, double out_mean_abs[4], void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_fields3(f, false));
+    if (!out_mean_abs) return fail(PS_ERR_NULL, "NULL output");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* red = st->d_scratch;
+    const int64_t n[4] = {numel(f->Rx), numel(f->Ry), numel(f->Rz), numel(f->divV)};
+    PS_CUDA_TRY(cudaMemsetAsync(red, 0, 4 * sizeof(double), s));
+    const dim3 g((unsigned)std::max<int64_t>(1, std::min<int64_t>((n[3] + 1023) / 1024, 1024)), 4);
+    if (f->Pt.dtype == PS_F64)
+        s3_sum_abs_k<double><<<g, 256, 0, s>>>(static_cast<const double*>(f->Rx.ptr), n[0],
+                                               static_cast<const double*>(f->Ry.ptr), n[1],
+                                               static_cast<const double*>(f->Rz.ptr), n[2],
+                                               static_cast<const double*>(f->divV.ptr), n[3], red);
+    else
+        s3_sum_abs_k<float><<<g, 256, 0, s>>>(static_cast<const float*>(f->Rx.ptr), n[0],
+                                              static_cast<const float*>(f->Ry.ptr), n[1],
+                                              static_cast<const float*>(f->Rz.ptr), n[2],
+                                              static_cast<const float*>(f->divV.ptr), n[3], red);
+    double h[4];
+    PS_CUDA_TRY(cudaMemcpyAsync(h, red, sizeof(h), cudaMemcpyDeviceToHost, s));
+    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int k = 0; k < 4; k++) out_mean_abs[k] = h[k] / (double)n[k];
+    return finish_launch(s, 0, "ps_stokes3d_err");
+}
+
+int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, double tol, int64_t max_iter,
+                      int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_fields3(f, true));
+    if (!p || !stats) return fail(PS_ERR_NULL, "NULL params / stats");
+    if (f->Pt.dtype != PS_F64) return fail(PS_ERR_DTYPE, "ps_stokes3d_solve: the arrays must be FP64");
+    if (nout < 1) return fail(PS_ERR_ARG, "nout must be >= 1");
+    if (!(tol > 0) || max_iter < 0) return fail(PS_ERR_ARG, "invalid tol / max_iter");
+    memset(stats, 0, sizeof(*stats));
+    // graphs are captured on a private stream ordered after `stream`
+    cudaStream_t user = static_cast<cudaStream_t>(stream), s;
+    PS_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaEvent_t ev;
+    PS_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, user);
+    cudaStreamWaitEvent(s, ev, 0);
+    const S3A<double> a = s3a<double>(f);
+    const S3P<double> pp = s3p<double>(*p);
+    double* red = st->d_scratch;
+    const int64_t n[4] = {numel(f->Rx), numel(f->Ry), numel(f->Rz), numel(f->divV)};
+    const dim3 gr((unsigned)std::max<int64_t>(1, std::min<int64_t>((n[3] + 1023) / 1024, 1024)), 4);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int64_t i = 0; i < nout; ++i) s3_iteration<double>(a, pp, s);
+        cudaMemsetAsync(red, 0, 4 * sizeof(double), s);
+        s3_sum_abs_k<double><<<gr, 256, 0, s>>>(a.Rx, n[0], a.Ry, n[1], a.Rz, n[2], a.divV, n[3], red);
+        e = cudaStreamEndCapture(s, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    int rc = e == cudaSuccess ? PS_OK : cuda_fail(e, "ps_stokes3d_solve: graph capture");
+    const double t0 = now_s3();
+    double err = INFINITY, h[4];
+    int64_t it = 0;
+    while (rc == PS_OK && it < max_iter) {
+        e = cudaGraphLaunch(exec, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, red, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "ps_stokes3d_solve");
+            break;
+        }
+        it += nout;
+        err = 0;
+        bool finite = true;
+        for (int k = 0; k < 4; k++) {
+            finite = finite && std::isfinite(h[k]);
+            err = std::max(err, h[k] / (double)n[k]);
+        }
+        if (!finite) {
+            err = NAN;
+            rc = fail(PS_ERR_NONFINITE, "ps_stokes3d_solve: non-finite residual after %lld iterations", (long long)it);
+            break;
+        }
+        if (err < tol) break;
+        if (max_seconds > 0 && now_s3() - t0 > max_seconds) {
+            rc = fail(PS_ERR_TIMEOUT, "ps_stokes3d_solve: wall-clock limit reached (err %.3e)", err);
+            break;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamSynchronize(s);
+    cudaEventDestroy(ev);
+    cudaStreamDestroy(s);
+    cudaGetLastError();
+    stats->iters = it;
+    stats->outer = 1;
+    stats->err = err;
+    stats->seconds = now_s3() - t0;
+    stats->converged = err < tol;
+    if (rc == PS_OK && !(err < tol))
+        rc = fail(PS_ERR_NOT_CONVERGED, "ps_stokes3d_solve: err %.3e after %lld iterations", err, (long long)it);
+    return rc;
+}
+
+}  // extern "C"

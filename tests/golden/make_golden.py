@@ -292,8 +292,79 @@ def stokes2d_numpy(nx, ny, iters, dt):
     return {k: np.asfortranarray(v) for k, v in out.items()}
 
 
+def stokes3d_numpy(nx, ny, nz, iters, dt):
+    """miniapps/Stokes3D.jl:11-68, 116-143 restated with numpy broadcasting (lx = ly = lz = 10,
+    μs0 = 1, μsi = 0.1, ρgi = 1, Vdmp = 4, Vsc = 1, Ptsc = 1/4, inclusion Radc <= 1)."""
+    lx = 10.0
+    dx, dy, dz = lx / (nx - 1), lx / (ny - 1), lx / (nz - 1)
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    radc = (ix * dx - 0.5 * lx) ** 2 + (iy * dy - 0.5 * lx) ** 2 + (iz * dz - 0.5 * lx) ** 2
+    Mus = np.ones((nx, ny, nz))
+    Rog = np.zeros((nx, ny, nz))
+    Mus[radc <= 1.0] = 0.1
+    Rog[radc <= 1.0] = 1.0
+    Mus, Rog = Mus.astype(dt), Rog.astype(dt)
+    c = lambda v: dt(v)  # noqa: E731 - literal typing
+    dxs, dys, dzs = c(dx), c(dy), c(dz)
+    dampX, dampY, dampZ = c(1.0 - 4.0 / nx), c(1.0 - 4.0 / ny), c(1.0 - 4.0 / nz)
+    Vsc, Ptsc, min_dxyz2, max_nxyz = c(1.0), c(0.25), c(min(dx, dy, dz) ** 2), c(max(nx, ny, nz))
+    d_xa = lambda A: A[1:, :, :] - A[:-1, :, :]  # noqa: E731
+    d_ya = lambda A: A[:, 1:, :] - A[:, :-1, :]  # noqa: E731
+    d_za = lambda A: A[:, :, 1:] - A[:, :, :-1]  # noqa: E731
+    d_xi = lambda A: A[1:, 1:-1, 1:-1] - A[:-1, 1:-1, 1:-1]  # noqa: E731
+    d_yi = lambda A: A[1:-1, 1:, 1:-1] - A[1:-1, :-1, 1:-1]  # noqa: E731
+    d_zi = lambda A: A[1:-1, 1:-1, 1:] - A[1:-1, 1:-1, :-1]  # noqa: E731
+    inn_yz = lambda A: A[:, 1:-1, 1:-1]  # noqa: E731
+    inn_xz = lambda A: A[1:-1, :, 1:-1]  # noqa: E731
+    inn_xy = lambda A: A[1:-1, 1:-1, :]  # noqa: E731
+    av_xi = lambda A: (A[:-1, 1:-1, 1:-1] + A[1:, 1:-1, 1:-1]) * c(0.5)  # noqa: E731
+    av_yi = lambda A: (A[1:-1, :-1, 1:-1] + A[1:-1, 1:, 1:-1]) * c(0.5)  # noqa: E731
+    av_zi = lambda A: (A[1:-1, 1:-1, :-1] + A[1:-1, 1:-1, 1:]) * c(0.5)  # noqa: E731
+    av_xyi = lambda A: (((A[:-1, :-1, 1:-1] + A[1:, :-1, 1:-1]) + A[:-1, 1:, 1:-1]) + A[1:, 1:, 1:-1]) * c(0.25)  # noqa: E731
+    av_xzi = lambda A: (((A[:-1, 1:-1, :-1] + A[1:, 1:-1, :-1]) + A[:-1, 1:-1, 1:]) + A[1:, 1:-1, 1:]) * c(0.25)  # noqa: E731
+    av_yzi = lambda A: (((A[1:-1, :-1, :-1] + A[1:-1, 1:, :-1]) + A[1:-1, :-1, 1:]) + A[1:-1, 1:, 1:]) * c(0.25)  # noqa: E731
+    third = c(1.0) / c(3.0)
+    dtauVx = ((Vsc * min_dxyz2) / av_xi(Mus)) / c(6.1)
+    dtauVy = ((Vsc * min_dxyz2) / av_yi(Mus)) / c(6.1)
+    dtauVz = ((Vsc * min_dxyz2) / av_zi(Mus)) / c(6.1)
+    dtauPt = ((Ptsc * c(6.1)) * Mus) / max_nxyz
+    Pt = np.zeros((nx, ny, nz), dt)
+    Vx, Vy, Vz = np.zeros((nx + 1, ny, nz), dt), np.zeros((nx, ny + 1, nz), dt), np.zeros((nx, ny, nz + 1), dt)
+    dVxdtau = np.zeros((nx - 1, ny - 2, nz - 2), dt)
+    dVydtau = np.zeros((nx - 2, ny - 1, nz - 2), dt)
+    dVzdtau = np.zeros((nx - 2, ny - 2, nz - 1), dt)
+    for _ in range(iters):
+        divV = (d_xa(Vx) / dxs + d_ya(Vy) / dys) + d_za(Vz) / dzs
+        Pt = Pt - dtauPt * divV
+        txx = (c(2.0) * inn_yz(Mus)) * (d_xi(Vx) / dxs - third * inn_yz(divV))
+        tyy = (c(2.0) * inn_xz(Mus)) * (d_yi(Vy) / dys - third * inn_xz(divV))
+        tzz = (c(2.0) * inn_xy(Mus)) * (d_zi(Vz) / dzs - third * inn_xy(divV))
+        txy = (c(2.0) * av_xyi(Mus)) * (c(0.5) * (d_yi(Vx) / dys + d_xi(Vy) / dxs))
+        txz = (c(2.0) * av_xzi(Mus)) * (c(0.5) * (d_zi(Vx) / dzs + d_xi(Vz) / dxs))
+        tyz = (c(2.0) * av_yzi(Mus)) * (c(0.5) * (d_zi(Vy) / dzs + d_yi(Vz) / dys))
+        Rx = ((d_xa(txx) / dxs + d_ya(txy) / dys) + d_za(txz) / dzs) - d_xi(Pt) / dxs
+        Ry = ((d_ya(tyy) / dys + d_xa(txy) / dxs) + d_za(tyz) / dzs) - d_yi(Pt) / dys
+        Rz = (((d_za(tzz) / dzs + d_xa(txz) / dxs) + d_ya(tyz) / dys) - d_zi(Pt) / dzs) + av_zi(Rog)
+        dVxdtau = dampX * dVxdtau + Rx
+        dVydtau = dampY * dVydtau + Ry
+        dVzdtau = dampZ * dVzdtau + Rz
+        Vx[1:-1, 1:-1, 1:-1] = Vx[1:-1, 1:-1, 1:-1] + dtauVx * dVxdtau
+        Vy[1:-1, 1:-1, 1:-1] = Vy[1:-1, 1:-1, 1:-1] + dtauVy * dVydtau
+        Vz[1:-1, 1:-1, 1:-1] = Vz[1:-1, 1:-1, 1:-1] + dtauVz * dVzdtau
+        Vy[0, :, :], Vy[-1, :, :] = Vy[1, :, :], Vy[-2, :, :]
+        Vz[0, :, :], Vz[-1, :, :] = Vz[1, :, :], Vz[-2, :, :]
+        Vx[:, 0, :], Vx[:, -1, :] = Vx[:, 1, :], Vx[:, -2, :]
+        Vz[:, 0, :], Vz[:, -1, :] = Vz[:, 1, :], Vz[:, -2, :]
+        Vx[:, :, 0], Vx[:, :, -1] = Vx[:, :, 1], Vx[:, :, -2]
+        Vy[:, :, 0], Vy[:, :, -1] = Vy[:, :, 1], Vy[:, :, -2]
+    out = dict(Mus=Mus, Rog=Rog, Pt=Pt, Vx=Vx, Vy=Vy, Vz=Vz, divV=divV, txx=txx, tyy=tyy, tzz=tzz, txy=txy,
+               txz=txz, tyz=tyz, Rx=Rx, Ry=Ry, Rz=Rz, dVxdtau=dVxdtau, dVydtau=dVydtau, dVzdtau=dVzdtau,
+               dtauVx=dtauVx, dtauVy=dtauVy, dtauVz=dtauVz, dtauPt=dtauPt)
+    return {k: np.asfortranarray(v) for k, v in out.items()}
+
+
 def main():
-    arrays, meta = {}, {"fd": [], "diffusion": [], "stokes2d": []}
+    arrays, meta = {}, {"fd": [], "diffusion": [], "stokes2d": [], "stokes3d": []}
     for dtn, dt in (("f64", np.float64), ("f32", np.float32)):
         for nd, (templates, grid, gen) in {3: (FIELD3, (9, 7, 8), None), 2: (FIELD2, (9, 7), None),
                                             1: (FIELD1, (9,), None)}.items():
@@ -322,6 +393,10 @@ def main():
         for k, v in stokes2d_numpy(nx, ny, iters, dt).items():
             arrays[f"stokes2d_{dtn}_{k}"] = v
         meta["stokes2d"].append({"prefix": f"stokes2d_{dtn}_", "nx": nx, "ny": ny, "iters": iters, "dtype": dtn})
+        n3, iters3 = (15, 13, 11), 30
+        for k, v in stokes3d_numpy(*n3, iters3, dt).items():
+            arrays[f"stokes3d_{dtn}_{k}"] = v
+        meta["stokes3d"].append({"prefix": f"stokes3d_{dtn}_", "n": list(n3), "iters": iters3, "dtype": dtn})
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as fh:
         json.dump(meta, fh, indent=1)

@@ -114,6 +114,26 @@ def test_oracle_stokes2d_vs_broadcasting(oracle, golden, dtn):
     assert s.err()[0] > 0
 
 
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_oracle_stokes3d_vs_broadcasting(oracle, golden, dtn):
+    """miniapps/Stokes3D.jl kernels: the oracle's loops equal the broadcasting restatement."""
+    meta, arr = golden
+    case = [c for c in meta["stokes3d"] if c["dtype"] == dtn][0]
+    g = {k[len(case["prefix"]):]: v for k, v in arr.items() if k.startswith(case["prefix"])}
+    nx, ny, nz = case["n"]
+    s = oracle.Stokes3D(nx, ny, nz, 10.0 / (nx - 1), 10.0 / (ny - 1), 10.0 / (nz - 1), g["Mus"], g["Rog"],
+                        dtype=DT[dtn])
+    s.compute_timesteps()
+    for k in ("dtauVx", "dtauVy", "dtauVz", "dtauPt"):
+        assert np.array_equal(s[k], g[k]), k
+    for _ in range(case["iters"]):
+        s.step()
+    for k in ("Pt", "Vx", "Vy", "Vz", "divV", "txx", "tyy", "tzz", "txy", "txz", "tyz", "Rx", "Ry", "Rz", "dVxdtau",
+              "dVydtau", "dVzdtau"):
+        assert np.array_equal(s[k], g[k]), k
+    assert s.err()[0] > 0
+
+
 def test_oracle_adjoint_matches_finite_differences(oracle):
     """The oracle's reverse sweep (the restatement the GPU adjoint is checked against) agrees
     with central finite differences of its own forward solver on random directions."""
