@@ -373,6 +373,21 @@ int ps_stokes3d_err(const ps_stokes3d_fields* f, double out_mean_abs[4], void* s
 int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, double tol, int64_t max_iter,
                       int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
 
+/* ------------------------------------------------------------------------------------ */
+/* Learned warm start (no counterpart in the reference): BF16 conv encoder-decoder on the */
+/* tcgen05 tensor cores, trained and run by the library's own kernels.                    */
+/* ------------------------------------------------------------------------------------ */
+
+enum { PS_NN_RELU = 1, PS_NN_OUT_BF16 = 2, PS_NN_ACCUMULATE = 4 };
+
+/* C[M][N] = A[M][K] * B[N][K]^T for row-major bf16 device matrices A, B (K % 8 == 0, 16-byte
+ * aligned), FP32 accumulation in tensor memory; then + bias[n] (bias may be NULL), ReLU
+ * (PS_NN_RELU), and C stored as bf16 (PS_NN_OUT_BF16), added into FP32 C with atomics
+ * (PS_NN_ACCUMULATE; required for split > 1, K split over `split` CTAs per tile), or stored as
+ * FP32. Synchronises. */
+int ps_nn_gemm_bf16(const void* A, const void* B, void* C, int64_t M, int64_t N, int64_t K, const float* bias,
+                    int32_t flags, int32_t split, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,6 +75,10 @@ Box launch_box(const ps_launch* cfg, const int64_t grid[3]);
 // fill. Returns PS_ERR_ALIGN if the array does not meet TMA's 16-byte rules.
 int encode_plane_map(CUtensorMap* map, const ps_array& a, uint32_t bx, uint32_t by);
 bool tma_eligible(const ps_array& a);
+// 2-D map of a row-major bf16 matrix [rows][cols] with 128-byte swizzle; box = box_rows x 64
+// columns (one 128-byte swizzle row). Reads past the matrix are zero-filled.
+int encode_bf16_rows_sw128(CUtensorMap* map, const void* ptr, uint64_t cols, uint64_t rows, uint32_t box_cols,
+                           uint32_t box_rows);
 
 // z-sweep length for loopsize = 0: a launch of cta_xy CTAs per z-block over wz planes with
 // `slots` CTAs resident at once (occupancy x SMs) loses the idle part of its last wave and

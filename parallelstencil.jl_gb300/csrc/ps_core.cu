@@ -140,6 +140,23 @@ int encode_plane_map(CUtensorMap* map, const ps_array& a, uint32_t bx, uint32_t 
     return PS_OK;
 }
 
+int encode_bf16_rows_sw128(CUtensorMap* map, const void* ptr, uint64_t cols, uint64_t rows, uint32_t box_cols,
+                           uint32_t box_rows) {
+    if (!g_encode) return fail(PS_ERR_NOT_INIT, "TMA encoder unavailable (ps_init not called)");
+    if ((reinterpret_cast<uintptr_t>(ptr) & 15) || (cols * 2) % 16 || cols == 0 || rows == 0)
+        return fail(PS_ERR_ALIGN, "bf16 matrix not TMA-eligible (16-byte base and row stride)");
+    if (box_cols * 2 != 128 || box_rows == 0 || box_rows > 256) return fail(PS_ERR_ARG, "invalid bf16 TMA box");
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(cols * 2)};
+    cuuint32_t box[2] = {box_cols, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled (bf16) failed (CUresult %d)", (int)r);
+    return PS_OK;
+}
+
 }  // namespace ps
 
 using namespace ps;

@@ -1,0 +1,242 @@
+// ps_nn_gemm.cu -- BF16 GEMM on the 5th-generation tensor cores (tcgen05) for the learned warm
+// start's convolutions: D[M][N] = A[M][K] * B[N][K]^T, A and B bf16 row-major (K contiguous), FP32
+// accumulation in tensor memory (TMEM).
+//
+// One CTA of 128 threads computes a 128 x 128 tile of D:
+//   - thread 0 streams 128 x 64 tiles of A and B into a 4-stage shared-memory ring with TMA
+//     (cp.async.bulk.tensor.2d, 128-byte swizzle, zero fill past the matrix edges, so M, N and K
+//     need no padding beyond K % 8 == 0) and issues tcgen05.mma (kind::f16, M = 128, N = 128,
+//     K = 16) on each stage; tcgen05.commit arrives on the stage's "empty" mbarrier when its MMAs
+//     have read it, and the stage is refilled;
+//   - all four warps then read the accumulator with tcgen05.ld (warp w owns TMEM lanes / tile
+//     rows 32w..32w+31) and apply the epilogue: + bias[n], ReLU, store as bf16 or FP32, or add
+//     into FP32 output with atomics (split-K over blockIdx.z).
+// Every mbarrier wait is bounded: on a timeout the kernel raises DEV_ERR_TMA_TIMEOUT, drains
+// the copies it issued, frees its TMEM columns and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "ps_common.cuh"
+#include "ps_nn.cuh"
+
+namespace ps {
+
+constexpr int G_BM = 128, G_BN = 128, G_BK = 64, G_S = 4;
+constexpr int G_ABYTES = G_BM * G_BK * 2;  // 16 KB
+constexpr int G_BBYTES = G_BN * G_BK * 2;  // 16 KB
+constexpr int G_STAGE = G_ABYTES + G_BBYTES;
+constexpr int G_SMEM = G_S * G_STAGE + 1024 + 128;  // ring (1024-aligned) + barriers and TMEM slot
+constexpr uint32_t G_TMEM_COLS = 128;              // FP32 accumulator: one column per n
+
+// tcgen05 instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// Shared-memory matrix descriptor of a K-major tile stored by TMA with 128-byte swizzle: rows of
+// 128 bytes, 8-row (1024-byte) swizzle atoms; start address in 16-byte units.
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void tc_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(128, 1)
+    nn_gemm_tc(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, int64_t K,
+               int kb_per_split, GemmEpilogue e, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + G_S * G_STAGE);
+    uint64_t* empty = full + G_S;
+    uint64_t* done = empty + G_S;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * G_BM, n0 = blockIdx.y * G_BN;
+    const int KB = (int)((K + G_BK - 1) / G_BK);
+    const int kb0 = blockIdx.z * kb_per_split;
+    const int nkb = min(KB, kb0 + kb_per_split) - kb0;
+
+    if (threadIdx.x == 0) {
+        prefetch_tensormap(&mA);
+        prefetch_tensormap(&mB);
+        for (int s = 0; s < G_S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tc_alloc(tmem_slot, G_TMEM_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 0) {
+        constexpr uint32_t idesc = umma_idesc_bf16(G_BM, G_BN);
+        int issued = 0, consumed = 0;
+        bool ok = true;
+        auto load = [&](int i) {
+            unsigned char* st = smem + (i % G_S) * G_STAGE;
+            mbar_arrive_expect_tx(&full[i % G_S], G_STAGE);
+            tma_load_2d(st, &mA, &full[i % G_S], (kb0 + i) * G_BK, m0);
+            tma_load_2d(st + G_ABYTES, &mB, &full[i % G_S], (kb0 + i) * G_BK, n0);
+            ++issued;
+        };
+        for (int i = 0; i < min(G_S, nkb); i++) load(i);
+        for (int i = 0; i < nkb; i++) {
+            const int s = i % G_S;
+            if (!mbar_wait_bounded(&full[s], (i / G_S) & 1)) {
+                ok = false;
+                break;
+            }
+            ++consumed;
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + s * G_STAGE);
+            const uint64_t da = umma_desc_sw128(sa), db = umma_desc_sw128(sa + G_ABYTES);
+#pragma unroll
+            for (int k = 0; k < G_BK / 16; k++)  // K = 16 per MMA: +32 bytes along the swizzled row
+                tc_mma(tmem, da + 2 * k, db + 2 * k, idesc, (i > 0 || k > 0) ? 1u : 0u);
+            tc_commit(&empty[s]);
+            // refill the stage the previous MMAs read, once they have finished with it
+            if (i >= 1 && i - 1 + G_S < nkb) {
+                if (!mbar_wait_bounded(&empty[(i - 1) % G_S], ((i - 1) / G_S) & 1)) {
+                    ok = false;
+                    break;
+                }
+                load(i - 1 + G_S);
+            }
+        }
+        tc_commit(done);  // arrives when every MMA issued above has completed
+        if (!ok) {
+            atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+            for (int j = consumed; j < issued; j++) mbar_wait_bounded(&full[j % G_S], (j / G_S) & 1);
+        }
+    }
+    __syncwarp();
+    const bool have = mbar_wait_bounded(done, 0);
+    tc_fence_after();
+    if (!have) {
+        if (threadIdx.x == 0) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+    } else if (nkb > 0) {
+        const int row = warp * 32 + lane;
+        const int64_t gm = (int64_t)m0 + row;
+        const bool row_ok = gm < e.M;
+        for (int c = 0; c < G_BN; c += 16) {
+            float v[16];
+            tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);  // whole warp, no divergence
+            if (!row_ok) continue;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int64_t gn = (int64_t)n0 + c + j;
+                if (gn >= e.N) break;
+                float x = v[j] * e.alpha;
+                if (e.bias) x += e.bias[gn];
+                if (e.relu) x = fmaxf(x, 0.0f);
+                const int64_t o = gm * e.ldc + gn;
+                if (e.out_bf16)
+                    e.outh[o] = __float2bfloat16_rn(x);
+                else if (e.atomic)
+                    atomicAdd(e.outf + o, x);
+                else
+                    e.outf[o] = x;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, G_TMEM_COLS);
+}
+
+int nn_gemm(const void* A, int64_t M, const void* B, int64_t N, int64_t K, const GemmEpilogue& e, int split,
+            cudaStream_t s, int* d_err) {
+    if (M <= 0 || N <= 0 || K <= 0) return PS_OK;
+    if (K % 8) return fail(PS_ERR_SHAPE, "nn_gemm: K = %lld must be a multiple of 8", (long long)K);
+    if (M > ((int64_t)65535 * 32768) || N > 65535LL * G_BN) return fail(PS_ERR_SHAPE, "nn_gemm: matrix too large");
+    CUtensorMap mA, mB;
+    PS_TRY(encode_bf16_rows_sw128(&mA, A, (uint64_t)K, (uint64_t)M, G_BK, G_BM));
+    PS_TRY(encode_bf16_rows_sw128(&mB, B, (uint64_t)K, (uint64_t)N, G_BK, G_BN));
+    static bool attr = false;
+    if (!attr) {
+        PS_CUDA_TRY(cudaFuncSetAttribute(nn_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM));
+        attr = true;
+    }
+    const int KB = (int)((K + G_BK - 1) / G_BK);
+    split = std::max(1, std::min(split, KB));
+    if (split > 1 && (!e.atomic || e.out_bf16 || e.bias || e.relu))
+        return fail(PS_ERR_ARG, "nn_gemm: split-K needs a plain FP32 atomic epilogue");
+    const int per = (KB + split - 1) / split;
+    const dim3 grid((unsigned)((M + G_BM - 1) / G_BM), (unsigned)((N + G_BN - 1) / G_BN), (unsigned)((KB + per - 1) / per));
+    nn_gemm_tc<<<grid, 128, G_SMEM, s>>>(mA, mB, K, per, e, d_err);
+    PS_CUDA_TRY(cudaGetLastError());
+    return PS_OK;
+}
+
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" int ps_nn_gemm_bf16(const void* A, const void* B, void* C, int64_t M, int64_t N, int64_t K,
+                               const float* bias, int32_t flags, int32_t split, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    if (!A || !B || !C) return fail(PS_ERR_NULL, "ps_nn_gemm_bf16: NULL matrix");
+    GemmEpilogue e{};
+    e.M = M;
+    e.N = N;
+    e.ldc = N;
+    e.alpha = 1.0f;
+    e.bias = bias;
+    e.relu = (flags & PS_NN_RELU) != 0;
+    e.out_bf16 = (flags & PS_NN_OUT_BF16) != 0;
+    e.atomic = (flags & PS_NN_ACCUMULATE) != 0;
+    e.outf = static_cast<float*>(C);
+    e.outh = static_cast<__nv_bfloat16*>(C);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PS_TRY(nn_gemm(A, M, B, N, K, e, split < 1 ? 1 : split, s, st->d_err));
+    return finish_launch(s, 1, "ps_nn_gemm_bf16");
+}
