@@ -388,6 +388,44 @@ enum { PS_NN_RELU = 1, PS_NN_OUT_BF16 = 2, PS_NN_ACCUMULATE = 4 };
 int ps_nn_gemm_bf16(const void* A, const void* B, void* C, int64_t M, int64_t N, int64_t K, const float* bias,
                     int32_t flags, int32_t split, void* stream);
 
+/* The warm-start network: a 4-level conv encoder-decoder (3x3 convs, ReLU, 2x2 average pooling,
+ * nearest x2 upsampling with skip concatenation; 32, 64, 128, 256 channels; 1x1 output conv),
+ * input [B][H][W][2] (log10 viscosity, rho*g; normalised with the net's scales), output
+ * [B][H][W][3] (P, Vx, Vy at cells, normalised). Activations and weights bf16, accumulation FP32;
+ * FP32 master weights with Adam. H, W multiples of 8; B <= max_batch. All pointers are device
+ * memory unless named host. Every call synchronises. */
+int ps_nn_create(int64_t H, int64_t W, int32_t max_batch, uint64_t seed, void** net);
+int ps_nn_destroy(void* net);
+int ps_nn_forward(void* net, const float* x, int32_t B, float* y, void* stream);
+/* Gradient of the last forward pass for output gradient dy [B][H][W][3], added to the
+ * parameters' gradients (ps_nn_zero_grad clears them). */
+int ps_nn_backward(void* net, const float* dy, void* stream);
+int ps_nn_zero_grad(void* net, void* stream);
+int ps_nn_adam_step(void* net, float lr, float beta1, float beta2, float eps, void* stream);
+/* forward + mean squared error against t [B][H][W][3] (per-pixel weights w [B][H][W] or NULL,
+ * loss = sum w (y - t)^2 / (3 B H W), written to host *loss) + backward + Adam (0.9, 0.999, 1e-8). */
+int ps_nn_train_step(void* net, const float* x, const float* t, const float* w, int32_t B, float lr, double* loss,
+                     void* stream);
+/* Output of layer 0..14 of the last forward pass, [B][h][w][cout] as host FP32 (hidden layers
+ * are stored as bf16; layer 14 is the network output). */
+int ps_nn_get_activation(void* net, int32_t layer, float* host);
+/* Parameters (host FP32), layer by layer: W [cout][ky][kx][cin] then b [cout]. */
+int ps_nn_param_count(void* net, int64_t* count);
+int ps_nn_get_params(void* net, float* host);
+int ps_nn_set_params(void* net, const float* host);
+int ps_nn_get_grads(void* net, float* host);
+/* scales: input offsets/scales (log10 mu: [0], [1]; rho*g: [2], [3]), output scales P, Vx, Vy
+ * ([4..6]); [7] unused. Stored with the weights. */
+int ps_nn_set_scales(void* net, const float scales[8]);
+int ps_nn_get_scales(void* net, float scales[8]);
+int ps_nn_save(void* net, const char* path);
+int ps_nn_load(void* net, const char* path);
+
+/* Warm start of the Stokes2D PT solve: the network's P, Vx, Vy for the viscosity and buoyancy
+ * of f, predicted on the network's nvalid x nvalid node grid (the fields resampled bilinearly
+ * onto it) and interpolated onto f's staggered arrays; dVxdtau, dVydtau zeroed. FP64 fields. */
+int ps_stokes2d_warm_start(void* net, const ps_stokes2d_fields* f, int32_t nvalid, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
