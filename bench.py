@@ -348,6 +348,10 @@ def run_ours(a, world, rank, local):
         stokes = None if a.quick else bench_stokes2d(ps, torch)
         if stokes:
             launches += stokes["fp64"]["iterations"] + stokes["mixed"]["iterations"]
+        warm = None if a.quick else bench_warm_start(a.warm_seeds)
+        if warm:
+            for r in (warm["fp64"], warm["mixed"]):
+                launches += int(r["seeds"] * (r["iters_zero_mean"] + r["iters_warm_mean"]))
     clocks = clk.summary()
 
     value = world * b_head / t_head / 1e9
@@ -375,6 +379,7 @@ def run_ours(a, world, rank, local):
                 "seconds_per_job": round(t_e2e, 5)},
         "gpu_launches": launches,
         "stokes2d_time_to_tol": stokes,
+        "warm_start_time_to_tol": warm,
         "clocks": clocks,
         "variants": results,
     }
@@ -407,6 +412,24 @@ def bench_stokes2d(ps, torch, n=1023, tol=1e-8):
                      "outer": int(st.outer), "err": float(st.err), "converged": bool(st.converged)}
         del g
     out["mixed_over_fp64"] = round(out["mixed"]["seconds"] / out["fp64"]["seconds"], 4)
+    return out
+
+
+def bench_warm_start(seeds, n=1023, tol=1e-8):
+    """The learned warm start on unseen random setups at 1023^2 (1-5 inclusions): wall time and PT
+    iterations to max residual < tol from the zero start and from the network's prediction
+    (inference + interpolation inside the warm time), for the FP64 and the mixed-precision solver."""
+    from ps_gb300 import warm_start as W
+
+    net = W.load_default()
+    out = {"config": f"{seeds} unseen setups at {n}^2, 1-5 inclusions r~U(0.05,0.2), viscosity 10^U(-0.5,0.5), "
+                     f"rho*g=+-1, tol {tol}; network trained at 255^2 on PT solutions generated by the library"}
+    for mode, name in ((0, "fp64"), (1, "mixed")):
+        r = W.evaluate(net, seeds, n=n, tol=tol, mode=mode)
+        r.pop("rows")
+        out[name] = r
+    out["mixed_warm_over_fp64_zero"] = round(out["mixed"]["seconds_warm"] / out["fp64"]["seconds_zero"], 4)
+    net.close()
     return out
 
 
@@ -508,6 +531,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode and exit")
     a = ap.parse_args()

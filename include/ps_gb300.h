@@ -423,7 +423,9 @@ int ps_nn_load(void* net, const char* path);
 
 /* Warm start of the Stokes2D PT solve: the network's P, Vx, Vy for the viscosity and buoyancy
  * of f, predicted on the network's nvalid x nvalid node grid (the fields resampled bilinearly
- * onto it) and interpolated onto f's staggered arrays; dVxdtau, dVydtau zeroed. FP64 fields. */
+ * onto it) and interpolated onto f's staggered arrays; the wall-normal faces (Vx at x walls, Vy
+ * at y walls), which the PT iteration keeps fixed, are set to 0, the free-slip copies bc_y!(Vx),
+ * bc_x!(Vy) are applied; dVxdtau, dVydtau zeroed. FP64 fields. */
 int ps_stokes2d_warm_start(void* net, const ps_stokes2d_fields* f, int32_t nvalid, void* stream);
 
 #ifdef __cplusplus

@@ -274,11 +274,14 @@ __global__ void nn_ws_output_k(const float* __restrict__ y, int NH, int NW, int 
         } else if (i < nP + nVx) {
             const int64_t j = i - nP;
             const int ix = (int)(j % (nx + 1)), iy = (int)(j / (nx + 1));  // face between nodes ix-1 and ix
-            Vx[j] = (double)(nn_bilinear(y, NW, nvalid, 3, 1, iy * ry, (ix - 0.5f) * rx) * sc[5]);
+            // the wall faces carry no normal flow and the PT iteration never updates them
+            Vx[j] = (ix == 0 || ix == nx) ? 0.0
+                                          : (double)(nn_bilinear(y, NW, nvalid, 3, 1, iy * ry, (ix - 0.5f) * rx) * sc[5]);
         } else {
             const int64_t j = i - nP - nVx;
             const int ix = (int)(j % nx), iy = (int)(j / nx);
-            Vy[j] = (double)(nn_bilinear(y, NW, nvalid, 3, 2, (iy - 0.5f) * ry, ix * rx) * sc[6]);
+            Vy[j] = (iy == 0 || iy == ny) ? 0.0
+                                          : (double)(nn_bilinear(y, NW, nvalid, 3, 2, (iy - 0.5f) * ry, ix * rx) * sc[6]);
         }
     }
 }
@@ -866,6 +869,9 @@ int ps_stokes2d_warm_start(void* net, const ps_stokes2d_fields* f, int32_t nvali
                                              static_cast<double*>(f->Vy.ptr));
     PS_CUDA_TRY(cudaMemsetAsync(f->dVxdtau.ptr, 0, (size_t)numel(f->dVxdtau) * 8, s));
     PS_CUDA_TRY(cudaMemsetAsync(f->dVydtau.ptr, 0, (size_t)numel(f->dVydtau) * 8, s));
+    // the loop body's free-slip copies, so the start state satisfies them like every PT iterate
+    PS_TRY(ps_bc_y2d(f->Vx, stream, 0));
+    PS_TRY(ps_bc_x2d(f->Vy, stream, 0));
     return finish_launch(s, 1, "ps_stokes2d_warm_start");
 }
 

@@ -670,6 +670,11 @@ static int solve_mixed(const ps_stokes2d_fields* f, const ps_stokes2d_params* pp
     if (e != cudaSuccess) rc = cuda_fail(e, "memset");
     const double* Mus = P_<double>(f->Mus);
     s2_to_f32<<<256, 256, 0, s>>>(F(11), Mus, nP);
+    // The corrections keep the free-slip copies (bc_y!(Vx), bc_x!(Vy)) of the state they are added
+    // to, so a start state that violates them (an externally supplied guess) would keep its
+    // violation: apply the copies once, as the first FP64 PT iteration would.
+    s2_bc_y_k<double><<<(unsigned)((nx + 1 + 255) / 256), 256, 0, s>>>(P_<double>(f->Vx), nx + 1, ny);
+    s2_bc_x_k<double><<<(unsigned)((ny + 1 + 255) / 256), 256, 0, s>>>(P_<double>(f->Vy), nx, ny + 1);
 
     PTRunner<float, true> r;
     r.p = s2p<float>(*pp);

@@ -1,0 +1,223 @@
+"""Learned warm start of the Stokes2D PT solver (no counterpart in the reference).
+
+Data: random unit-box setups with 1-5 circular inclusions (radius U(0.05, 0.2), viscosity
+10^U(-0.5, 0.5) against the background's 1, rho*g = +1 or -1 each), solved to max residual < tol by
+the library's own PT solver (``Stokes2D.solve``). The reference's PT scheme (Vdmp = 4, Vsc = 1,
+Ptsc = 1/4) diverges beyond viscosity contrasts of about 10 (measured at 255^2 with one inclusion:
+ratios 0.1 .. 10 converge, 0.03 and 30 give non-finite residuals); with several inclusions the
+contrast between two touching inclusions counts, hence the +-0.5 decades, which bound every
+contrast by 10. A setup whose solve still fails is redrawn (counted in the statistics).
+
+Network input: log10(Mus), Rog on the n x n node grid, padded by edge replication to the
+network's size; targets: P, and Vx, Vy averaged onto the nodes. Warm start at any resolution:
+the fields are resampled onto the network's grid, the prediction is interpolated back onto the
+staggered arrays (``ps_stokes2d_warm_start``), and the PT solve starts from it.
+
+Command line (runs on the GPU):
+    python -m ps_gb300.warm_start train --samples 2000 --epochs 20 --out weights.bin
+    python -m ps_gb300.warm_start eval --weights weights.bin --seeds 200 --n 1023
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib, nn
+from .core import init_parallel_stencil, is_initialized
+from .stokes import Stokes2D, Stokes2DParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_WEIGHTS = os.path.join(HERE, "data", "warm_start_unet32_255.bin")
+NET_N = 256   # network grid (nodes); the training grid's 255 nodes fill it but for one padded row / column
+TRAIN_N = 255
+
+
+def random_setup(n, rng, lx=1.0):
+    """Mus, Rog (Fortran (n, n) FP64) of one random setup on the n x n node grid of [0, lx]^2."""
+    dx = lx / (n - 1)
+    ix, iy = np.meshgrid(np.arange(n) * dx, np.arange(n) * dx, indexing="ij")
+    Mus = np.ones((n, n))
+    Rog = np.zeros((n, n))
+    for _ in range(int(rng.integers(1, 6))):
+        cx, cy = rng.uniform(0.15, 0.85, size=2) * lx
+        r = rng.uniform(0.05, 0.2) * lx
+        inside = (ix - cx) ** 2 + (iy - cy) ** 2 < r * r
+        Mus[inside] = 10.0 ** rng.uniform(-0.5, 0.5)
+        Rog[inside] = rng.choice([-1.0, 1.0])
+    return np.asfortranarray(Mus), np.asfortranarray(Rog)
+
+
+def solve_setup(Mus, Rog, tol=1e-8, mode=1, warm=None, nvalid=TRAIN_N, max_iter=2_000_000):
+    """PT solve of one setup; returns (Stokes2D, stats, seconds incl. the warm start's inference)."""
+    import torch
+
+    n = Mus.shape[0]
+    g = Stokes2D(Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog)
+    g.compute_timesteps()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if warm is not None:
+        nn.warm_start(warm, g, nvalid=nvalid)
+    st = g.solve(tol=tol, mode=mode, max_iter=max_iter)
+    torch.cuda.synchronize()
+    return g, st, time.perf_counter() - t0
+
+
+def _pad_nodes(a, N=NET_N):
+    """(n, n) node field (x, y) -> [N, N] (rows y, columns x), edge-replicated."""
+    t = np.asarray(a).T
+    return np.pad(t, ((0, N - t.shape[0]), (0, N - t.shape[1])), mode="edge")
+
+
+def sample_arrays(Mus, Rog, g):
+    """Network input [N, N, 2] and target [N, N, 3] (float32, unnormalised) of a solved setup."""
+    P, Vx, Vy = g.host("Pt"), g.host("Vx"), g.host("Vy")
+    x = np.stack([_pad_nodes(np.log10(Mus)), _pad_nodes(Rog)], axis=-1)
+    Vxn = 0.5 * (Vx[:-1, :] + Vx[1:, :])
+    Vyn = 0.5 * (Vy[:, :-1] + Vy[:, 1:])
+    t = np.stack([_pad_nodes(P), _pad_nodes(Vxn), _pad_nodes(Vyn)], axis=-1)
+    return x.astype(np.float32), t.astype(np.float32)
+
+
+def generate(samples, seed=1000, n=TRAIN_N, tol=1e-8, log=None):
+    """-> X [S, N, N, 2], T [S, N, N, 3] (host float32) and per-sample solve statistics."""
+    rng = np.random.default_rng(seed)
+    X = np.empty((samples, NET_N, NET_N, 2), np.float32)
+    T = np.empty((samples, NET_N, NET_N, 3), np.float32)
+    iters, failed = [], 0
+    t0 = time.perf_counter()
+    for i in range(samples):
+        while True:
+            Mus, Rog = random_setup(n, rng)
+            try:
+                g, st, _ = solve_setup(Mus, Rog, tol=tol, mode=1)
+                break
+            except _lib.PSError:
+                failed += 1
+                if failed > samples:
+                    raise
+        X[i], T[i] = sample_arrays(Mus, Rog, g)
+        iters.append(int(st.iters))
+        if log and (i + 1) % 200 == 0:
+            log(f"generated {i + 1}/{samples} ({time.perf_counter() - t0:.1f} s, {failed} redrawn)")
+    return X, T, iters
+
+
+def train(net, X, T, epochs=20, batch=8, lr=1e-3, lr_min=1e-5, seed=0, log=None):
+    """Adam on the weighted MSE of normalised targets (the padded row / column weighted 0)."""
+    import torch
+
+    S = X.shape[0]
+    sc = [0.0, 1.0, 0.0, 1.0] + [float(T[..., c].std()) + 1e-30 for c in range(3)] + [0.0]
+    net.scales = sc
+    Xd = torch.from_numpy(X).cuda()
+    Td = torch.from_numpy(T / np.array(sc[4:7], np.float32)).cuda()
+    w = torch.zeros(batch, NET_N, NET_N, device="cuda")
+    w[:, :TRAIN_N, :TRAIN_N] = 1.0
+    rng = np.random.default_rng(seed)
+    steps = epochs * (S // batch)
+    hist, k, t0 = [], 0, time.perf_counter()
+    for ep in range(epochs):
+        perm = rng.permutation(S)
+        tot = 0.0
+        for b in range(S // batch):
+            idx = torch.from_numpy(perm[b * batch:(b + 1) * batch]).cuda()
+            rate = lr_min + 0.5 * (lr - lr_min) * (1 + np.cos(np.pi * k / steps))
+            tot += net.train_step(Xd[idx], Td[idx], rate, w=w)
+            k += 1
+        hist.append(tot / (S // batch))
+        if log:
+            log(f"epoch {ep + 1}/{epochs}: loss {hist[-1]:.4e} ({time.perf_counter() - t0:.1f} s)")
+    return hist
+
+
+def evaluate(net, seeds, n=1023, tol=1e-8, mode=0, seed0=900_000, log=None):
+    """Zero start vs warm start on unseen setups: iterations and wall time to max residual < tol
+    (warm start time includes the network's inference and the interpolation)."""
+    rng = np.random.default_rng(seed0)
+    rows = []
+    failed = 0
+    while len(rows) < seeds:
+        Mus, Rog = random_setup(n, rng)
+        try:
+            _, s0, t0 = solve_setup(Mus, Rog, tol=tol, mode=mode)
+        except _lib.PSError:  # the zero-start PT itself fails on this setup: not a valid test case
+            failed += 1
+            continue
+        try:
+            _, s1, t1 = solve_setup(Mus, Rog, tol=tol, mode=mode, warm=net, nvalid=TRAIN_N)
+            rows.append({"iters_zero": int(s0.iters), "iters_warm": int(s1.iters), "s_zero": t0, "s_warm": t1})
+        except _lib.PSError as e:
+            rows.append({"iters_zero": int(s0.iters), "iters_warm": None, "s_zero": t0, "s_warm": None,
+                         "warm_failed": str(e)[:80]})
+        if log:
+            log(json.dumps(rows[-1]))
+    ok = [r for r in rows if r["iters_warm"] is not None]
+    if not ok:
+        return {"seeds": seeds, "n": n, "warm_failures": len(rows), "zero_start_failures": failed, "rows": rows}
+    rows_all, rows = rows, ok
+    iz = np.array([r["iters_zero"] for r in rows], float)
+    iw = np.array([r["iters_warm"] for r in rows], float)
+    tz = np.array([r["s_zero"] for r in rows])
+    tw = np.array([r["s_warm"] for r in rows])
+    return {"seeds": seeds, "n": n, "tol": tol, "solver": "fp64" if mode == 0 else "mixed",
+            "warm_failures": len(rows_all) - len(rows), "zero_start_failures": failed,
+            "iters_zero_mean": float(iz.mean()), "iters_warm_mean": float(iw.mean()),
+            "iters_ratio": float(iw.sum() / iz.sum()), "seconds_zero": float(tz.sum()),
+            "seconds_warm": float(tw.sum()), "time_ratio": float(tw.sum() / tz.sum()), "rows": rows_all}
+
+
+def load_default(max_batch=1):
+    net = nn.Net(NET_N, NET_N, max_batch=max_batch)
+    net.load(DEFAULT_WEIGHTS)
+    return net
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train")
+    t.add_argument("--samples", type=int, default=2000)
+    t.add_argument("--epochs", type=int, default=20)
+    t.add_argument("--batch", type=int, default=8)
+    t.add_argument("--lr", type=float, default=1e-3)
+    t.add_argument("--out", default=DEFAULT_WEIGHTS)
+    t.add_argument("--eval-seeds", type=int, default=4)
+    e = sub.add_parser("eval")
+    e.add_argument("--weights", default=DEFAULT_WEIGHTS)
+    e.add_argument("--seeds", type=int, default=200)
+    e.add_argument("--n", type=int, default=1023)
+    e.add_argument("--mode", type=int, default=0)
+    e.add_argument("--tol", type=float, default=1e-8)
+    a = ap.parse_args(argv)
+    if not is_initialized():
+        init_parallel_stencil("GB300", "Float64", 2)
+
+    def log(m):
+        print(m, flush=True)
+
+    if a.cmd == "train":
+        X, T, iters = generate(a.samples, log=log)
+        log(f"PT iterations per sample: mean {np.mean(iters):.0f}")
+        net = nn.Net(NET_N, NET_N, max_batch=a.batch)
+        hist = train(net, X, T, epochs=a.epochs, batch=a.batch, lr=a.lr, log=log)
+        os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+        net.save(a.out)
+        res = evaluate(net, a.eval_seeds, n=TRAIN_N, mode=1, log=log)
+        res.pop("rows")
+        log(json.dumps({"loss_first": hist[0], "loss_last": hist[-1], "eval_255": res}))
+    else:
+        net = load_default() if a.weights == DEFAULT_WEIGHTS else nn.Net(NET_N, NET_N, max_batch=1)
+        if a.weights != DEFAULT_WEIGHTS:
+            net.load(a.weights)
+        res = evaluate(net, a.seeds, n=a.n, tol=a.tol, mode=a.mode, log=log)
+        res.pop("rows")
+        log(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
