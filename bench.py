@@ -345,6 +345,10 @@ def run_ours(a, world, rank, local):
             bench_kernel("memcopy3d_f64_256", ps.kernels.copy3D, arrs256, (), False, WORDS_MEMCOPY, n2, np.float64,
                          a.steps)
             del arrs256
+        if not a.quick:
+            gemm = bench_gemm(torch)
+            results["nn_gemm_bf16_8192"] = gemm
+            launches += gemm["launches"]
         stokes = None if a.quick else bench_stokes2d(ps, torch)
         if stokes:
             launches += stokes["fp64"]["iterations"] + stokes["mixed"]["iterations"]
@@ -413,6 +417,38 @@ def bench_stokes2d(ps, torch, n=1023, tol=1e-8):
         del g
     out["mixed_over_fp64"] = round(out["mixed"]["seconds"] / out["fp64"]["seconds"], 4)
     return out
+
+
+def bench_gemm(torch, n=8192, reps=5):
+    """The warm start's tcgen05 BF16 GEMM (C = A B^T, FP32 accumulation) on an n^3 problem, against
+    the measured dense bf16 peak (burst): 2 n^3 flops per call, CUDA events around each call."""
+    from ps_gb300 import nn
+
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A = torch.randn(n, n, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(n, n, device="cuda", generator=g).to(torch.bfloat16)
+    C = torch.empty(n, n, device="cuda")
+    for _ in range(2):
+        nn.gemm_bf16(A, B, C)
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        nn.gemm_bf16(A, B, C)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = min(times)
+    tf = 2.0 * n ** 3 / t / 1e12
+    peak = None
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            peak = float(json.load(fh)["bf16_tflops"])
+    del A, B, C
+    torch.cuda.empty_cache()
+    return {"shape": f"{n}x{n}x{n}", "ms": round(t * 1e3, 4), "TFLOPs": round(tf, 1),
+            "frac_of_measured_bf16_peak": round(tf / peak, 4) if peak else None, "launches": reps + 2}
 
 
 def bench_warm_start(seeds, n=1023, tol=1e-8):
@@ -502,6 +538,18 @@ def only_run(a):
 
     ps.init_parallel_stencil(ps.GB300, "Float64", 3)
     n = a.n
+    if a.only_run == "gemm":  # the warm start's tcgen05 GEMM on an n^3 bf16 problem, --steps calls
+        from ps_gb300 import nn
+
+        g = torch.Generator(device="cuda").manual_seed(0)
+        A = torch.randn(n, n, device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn(n, n, device="cuda", generator=g).to(torch.bfloat16)
+        C = torch.empty(n, n, device="cuda")
+        for _ in range(a.steps):
+            nn.gemm_bf16(A, B, C)
+        torch.cuda.synchronize()
+        print(json.dumps({"only_run": "gemm", "n": n, "steps": a.steps}))
+        return
     g = torch.Generator(device="cuda")
     g.manual_seed(2)
     T = ps.empty(n, n, n)
@@ -532,8 +580,9 @@ def main():
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
-    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid"], default=None,
-                    help="profiling aid: run --steps steps of the headline workload in this fp64 mode and exit")
+    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm"], default=None,
+                    help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or --steps "
+                         "calls of the tcgen05 GEMM on an --n cubed bf16 problem) and exit")
     a = ap.parse_args()
     if a.only_run:
         only_run(a)

@@ -388,11 +388,11 @@ enum { PS_NN_RELU = 1, PS_NN_OUT_BF16 = 2, PS_NN_ACCUMULATE = 4 };
 int ps_nn_gemm_bf16(const void* A, const void* B, void* C, int64_t M, int64_t N, int64_t K, const float* bias,
                     int32_t flags, int32_t split, void* stream);
 
-/* The warm-start network: a 4-level conv encoder-decoder (3x3 convs, ReLU, 2x2 average pooling,
- * nearest x2 upsampling with skip concatenation; 32, 64, 128, 256 channels; 1x1 output conv),
+/* The warm-start network: a 4-level conv encoder-decoder (3x3 convs, ReLU, 4x4 average pooling,
+ * nearest x4 upsampling with skip concatenation; 32, 64, 128, 256 channels; 1x1 output conv),
  * input [B][H][W][2] (log10 viscosity, rho*g; normalised with the net's scales), output
  * [B][H][W][3] (P, Vx, Vy at cells, normalised). Activations and weights bf16, accumulation FP32;
- * FP32 master weights with Adam. H, W multiples of 8; B <= max_batch. All pointers are device
+ * FP32 master weights with Adam. H, W multiples of 64; B <= max_batch. All pointers are device
  * memory unless named host. Every call synchronises. */
 int ps_nn_create(int64_t H, int64_t W, int32_t max_batch, uint64_t seed, void** net);
 int ps_nn_destroy(void* net);

@@ -1,6 +1,6 @@
 """CPU reference of the warm-start network (TEST INFRASTRUCTURE ONLY).
 
-The same encoder-decoder as libps_b200.so's ps_nn_* entry points, in torch FP32 on the CPU, with
+The same encoder-decoder as libps_b200.so's ps_nn_* entry points (4x4 pooling, x4 upsampling), in torch FP32 on the CPU, with
 the GPU's bf16 roundings restated in the forward pass: the input, every weight and every hidden
 activation are rounded to bf16 (round to nearest even), accumulation is FP32. The roundings pass
 gradients straight through, so reference gradients are those of the FP32 computation on the
@@ -108,10 +108,10 @@ class Reference:
             return r(F.relu(z)) if i < 14 else z
 
         def pool(a):
-            return r(F.avg_pool2d(a, 2))
+            return r(F.avg_pool2d(a, 4))
 
         def upcat(low, skip):
-            return torch.cat([F.interpolate(low, scale_factor=2, mode="nearest"), skip], dim=1)
+            return torch.cat([F.interpolate(low, scale_factor=4, mode="nearest"), skip], dim=1)
 
         a1 = conv(1, conv(0, x))
         a3 = conv(3, conv(2, pool(a1)))

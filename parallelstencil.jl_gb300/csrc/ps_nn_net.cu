@@ -9,9 +9,11 @@
 //   dW  += dz^T * col    (GEMM over K = P, split-K with FP32 atomics; col built transposed)
 //   dcol = dz * W        (GEMM, B operand = W^T); dx = col2im(dcol) (gather, no atomics).
 // Network (base 32 channels, input 2: log10 viscosity and rho*g; output 3: P, Vx, Vy at cells):
-//   enc: [conv3 c->c, conv3 c->c] at 1, 1/2, 1/4, 1/8 resolution (c = 32, 64, 128, 256; 2x2 average
-//        pooling between levels); dec: nearest x2 upsampling, concatenation with the encoder output
-//        of that level, [conv3, conv3] (256+128 -> 128, 128+64 -> 64, 64+32 -> 32); 1x1 conv 32 -> 3.
+//   enc: [conv3 c->c, conv3 c->c] at 1, 1/4, 1/16, 1/64 resolution (c = 32, 64, 128, 256; 4x4 average
+//        pooling between levels, so that the coarsest level's 3x3 convolutions span the whole
+//        domain: 2-D Stokes flow is long-range); dec: nearest x4 upsampling, concatenation with the
+//        encoder output of that level, [conv3, conv3] (256+128 -> 128, 128+64 -> 64, 64+32 -> 32);
+//        1x1 conv 32 -> 3.
 // Optimiser: Adam on FP32 master weights, bf16 copies (and transposes) refreshed after each step.
 #include <cuda_bf16.h>
 #include <stdio.h>
@@ -33,22 +35,23 @@ typedef __nv_bfloat16 bf16;
 static inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::min<int64_t>((n + t - 1) / t, 1 << 20); }
 #define GSTRIDE(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
-// col[p][k] (or colT[k][p] when transposed) of a 3x3 "same" convolution over x [B][H][W][C]
+// col[p][k] of a 3x3 "same" convolution over x [B][H][W][C], or (ldp > 0) colT[k][p] with row stride
+// ldp >= P and zero columns P..ldp
 __global__ void nn_im2col3_k(const bf16* __restrict__ x, int64_t P, int H, int W, int C, int kpad, bf16* col,
-                             int transposed) {
-    const int64_t n = P * kpad;
+                             int64_t ldp) {
+    const int64_t n = (ldp > 0 ? ldp : P) * kpad;
     GSTRIDE(i, n) {
         int64_t p, k;
-        if (transposed) {
-            k = i / P;
-            p = i - k * P;
+        if (ldp > 0) {
+            k = i / ldp;
+            p = i - k * ldp;
         } else {
             p = i / kpad;
             k = i - p * kpad;
         }
         const int tap = (int)(k / C), c = (int)(k - (int64_t)tap * C);
         bf16 v = __float2bfloat16(0.0f);
-        if (tap < 9) {
+        if (tap < 9 && p < P) {
             const int64_t b = p / ((int64_t)H * W);
             const int rem = (int)(p - b * H * W), y = rem / W, xx = rem - y * W;
             const int sy = y + tap / 3 - 1, sx = xx + tap % 3 - 1;
@@ -100,8 +103,9 @@ __global__ void nn_relu_bwd_k(const float* __restrict__ dy, int ldy, const bf16*
     for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(gb + c, part[c]);
 }
 
-// out[c][r] = in[r][c] for a bf16 matrix [R][C] with row stride ld (tiles of 32 x 32)
-__global__ void nn_transpose_k(const bf16* __restrict__ in, int64_t R, int C, int ld, bf16* out) {
+// out[c][r] = in[r][c] for a bf16 matrix [R][C] with row stride ld; out rows have stride ldo >= R
+// with zero columns R..ldo (tiles of 32 x 32; the grid covers ldo)
+__global__ void nn_transpose_k(const bf16* __restrict__ in, int64_t R, int C, int ld, bf16* out, int64_t ldo) {
     __shared__ bf16 t[32][33];
     const int64_t r0 = blockIdx.x * 32LL;
     const int c0 = blockIdx.y * 32;
@@ -114,62 +118,69 @@ __global__ void nn_transpose_k(const bf16* __restrict__ in, int64_t R, int C, in
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         const int c = c0 + j;
         const int64_t r = r0 + threadIdx.x;
-        if (c < C && r < R) out[(int64_t)c * R + r] = t[threadIdx.x][j];
+        if (c < C && r < ldo) out[(int64_t)c * ldo + r] = t[threadIdx.x][j];
     }
 }
 
-// 2x2 average pooling of x [B][H][W][C] -> [B][H/2][W/2][C] (FP32 sum, bf16 result)
-__global__ void nn_pool2_k(const bf16* __restrict__ x, int64_t B, int H, int W, int C, bf16* y) {
-    const int h = H / 2, w = W / 2;
+// f x f average pooling of x [B][H][W][C] -> [B][H/f][W/f][C] (FP32 sum row by row, bf16 result)
+__global__ void nn_pool_k(const bf16* __restrict__ x, int64_t B, int H, int W, int C, int f, bf16* y) {
+    const int h = H / f, w = W / f;
     const int64_t n = B * h * w * C;
+    const float inv = 1.0f / (float)(f * f);
     GSTRIDE(i, n) {
         const int c = (int)(i % C);
         const int64_t q = i / C;
         const int xx = (int)(q % w), yy = (int)((q / w) % h);
         const int64_t b = q / ((int64_t)w * h);
-        const bf16* s = x + ((b * H + 2 * yy) * W + 2 * xx) * C + c;
-        const float v = (__bfloat162float(s[0]) + __bfloat162float(s[C])) +
-                        (__bfloat162float(s[(int64_t)W * C]) + __bfloat162float(s[(int64_t)W * C + C]));
-        y[i] = __float2bfloat16_rn(0.25f * v);
+        const bf16* s = x + ((b * H + (int64_t)f * yy) * W + (int64_t)f * xx) * C + c;
+        float v = 0.0f;
+        for (int r = 0; r < f; r++)
+            for (int k = 0; k < f; k++) v += __bfloat162float(s[((int64_t)r * W + k) * C]);
+        y[i] = __float2bfloat16_rn(v * inv);
     }
 }
-// dx [B][H][W][C] (+)= 0.25 * dy [B][H/2][W/2][C] broadcast
-__global__ void nn_pool2_bwd_k(const float* __restrict__ dy, int64_t B, int H, int W, int C, float* dx, int accumulate) {
-    const int h = H / 2, w = W / 2;
+// dx [B][H][W][C] (+)= dy [B][H/f][W/f][C] / f^2 broadcast
+__global__ void nn_pool_bwd_k(const float* __restrict__ dy, int64_t B, int H, int W, int C, int f, float* dx,
+                              int accumulate) {
+    const int h = H / f, w = W / f;
     const int64_t n = B * H * W * C;
+    const float inv = 1.0f / (float)(f * f);
     GSTRIDE(i, n) {
         const int c = (int)(i % C);
         const int64_t q = i / C;
         const int xx = (int)(q % W), yy = (int)((q / W) % H);
         const int64_t b = q / ((int64_t)W * H);
-        const float v = 0.25f * dy[((b * h + yy / 2) * w + xx / 2) * C + c];
+        const float v = inv * dy[((b * h + yy / f) * w + xx / f) * C + c];
         dx[i] = accumulate ? dx[i] + v : v;
     }
 }
-// y[b][Y][X][coff + c] = x[b][Y/2][X/2][c]   (x: [B][H/2][W/2][C], y row stride ldy)
-__global__ void nn_up2_k(const bf16* __restrict__ x, int64_t B, int H, int W, int C, bf16* y, int ldy, int coff) {
-    const int h = H / 2, w = W / 2;
+// y[b][Y][X][coff + c] = x[b][Y/f][X/f][c]   (x: [B][H/f][W/f][C], y row stride ldy)
+__global__ void nn_up_k(const bf16* __restrict__ x, int64_t B, int H, int W, int C, int f, bf16* y, int ldy, int coff) {
+    const int h = H / f, w = W / f;
     const int64_t n = B * H * W * C;
     GSTRIDE(i, n) {
         const int c = (int)(i % C);
         const int64_t q = i / C;
         const int xx = (int)(q % W), yy = (int)((q / W) % H);
         const int64_t b = q / ((int64_t)W * H);
-        y[q * ldy + coff + c] = x[((b * h + yy / 2) * w + xx / 2) * C + c];
+        y[q * ldy + coff + c] = x[((b * h + yy / f) * w + xx / f) * C + c];
     }
 }
-// dx[b][y][x][c] = sum over the 2x2 children of dk[.][coff + c] (dk row stride ldk)
-__global__ void nn_up2_bwd_k(const float* __restrict__ dk, int ldk, int coff, int64_t B, int H, int W, int C, float* dx) {
-    const int h = H / 2, w = W / 2;
+// dx[b][y][x][c] = sum over the f x f children of dk[.][coff + c] (dk row stride ldk)
+__global__ void nn_up_bwd_k(const float* __restrict__ dk, int ldk, int coff, int64_t B, int H, int W, int C, int f,
+                            float* dx) {
+    const int h = H / f, w = W / f;
     const int64_t n = B * h * w * C;
     GSTRIDE(i, n) {
         const int c = (int)(i % C);
         const int64_t q = i / C;
         const int xx = (int)(q % w), yy = (int)((q / w) % h);
         const int64_t b = q / ((int64_t)w * h);
-        const int64_t p00 = (b * H + 2 * yy) * W + 2 * xx;
-        dx[i] = (dk[p00 * ldk + coff + c] + dk[(p00 + 1) * ldk + coff + c]) +
-                (dk[(p00 + W) * ldk + coff + c] + dk[(p00 + W + 1) * ldk + coff + c]);
+        const int64_t p00 = (b * H + (int64_t)f * yy) * W + (int64_t)f * xx;
+        float v = 0.0f;
+        for (int r = 0; r < f; r++)
+            for (int k = 0; k < f; k++) v += dk[(p00 + (int64_t)r * W + k) * ldk + coff + c];
+        dx[i] = v;
     }
 }
 // dst[p][doff + c] = src[p][soff + c] (bf16 or FP32 copies of channel ranges)
@@ -225,11 +236,12 @@ __global__ void nn_wt_k(const float* __restrict__ src, int N, int K, bf16* dst, 
 }
 
 // Bilinear sample of channel ch of an NHWC FP32 field (row stride W pixels) at (fy, fx), clamped to
-// the ext x ext valid corner of the field.
-__device__ __forceinline__ float nn_bilinear(const float* f, int W, int ext, int C, int ch, float fy, float fx) {
-    fy = fminf(fmaxf(fy, 0.0f), (float)(ext - 1));
-    fx = fminf(fmaxf(fx, 0.0f), (float)(ext - 1));
-    const int y0 = min((int)fy, ext - 2), x0 = min((int)fx, ext - 2);
+// the exty x extx valid corner of the field.
+__device__ __forceinline__ float nn_bilinear(const float* f, int W, int exty, int extx, int C, int ch, float fy,
+                                             float fx) {
+    fy = fminf(fmaxf(fy, 0.0f), (float)(exty - 1));
+    fx = fminf(fmaxf(fx, 0.0f), (float)(extx - 1));
+    const int y0 = min((int)fy, exty - 2), x0 = min((int)fx, extx - 2);
     const int y1 = y0 + 1, x1 = x0 + 1;
     const float ty = fy - y0, tx = fx - x0;
     const float a = f[((int64_t)y0 * W + x0) * C + ch], b = f[((int64_t)y0 * W + x1) * C + ch];
@@ -261,8 +273,10 @@ __global__ void nn_ws_input_k(const double* __restrict__ Mus, const double* __re
         x[i * 2 + 1] = (rg - sc[2]) * sc[3];
     }
 }
-// Fine P (nx x ny), Vx ((nx+1) x ny), Vy (nx x (ny+1)) from the network output y [NH][NW][3]
-// (cell values of P, Vx, Vy on the nvalid x nvalid node grid), rescaled by sc[4..6].
+// Fine P (nx x ny), Vx ((nx+1) x ny), Vy (nx x (ny+1)) from the network output y [NH][NW][3], which
+// holds the staggered arrays of an nvalid x nvalid node grid (P at (row iy, col ix) for nodes,
+// Vx at (iy, face ix) with nvalid + 1 faces, Vy at (face iy, ix)), rescaled by sc[4..6]. Positions
+// map through physical coordinates: node i at i*h, face i at (i - 1/2)*h.
 __global__ void nn_ws_output_k(const float* __restrict__ y, int NH, int NW, int nvalid, int nx, int ny, const float* sc,
                                double* Pt, double* Vx, double* Vy) {
     const int64_t nP = (int64_t)nx * ny, nVx = (int64_t)(nx + 1) * ny, nVy = (int64_t)nx * (ny + 1);
@@ -270,18 +284,20 @@ __global__ void nn_ws_output_k(const float* __restrict__ y, int NH, int NW, int 
     GSTRIDE(i, nP + nVx + nVy) {
         if (i < nP) {
             const int ix = (int)(i % nx), iy = (int)(i / nx);
-            Pt[i] = (double)(nn_bilinear(y, NW, nvalid, 3, 0, iy * ry, ix * rx) * sc[4]);
+            Pt[i] = (double)(nn_bilinear(y, NW, nvalid, nvalid, 3, 0, iy * ry, ix * rx) * sc[4]);
         } else if (i < nP + nVx) {
             const int64_t j = i - nP;
             const int ix = (int)(j % (nx + 1)), iy = (int)(j / (nx + 1));  // face between nodes ix-1 and ix
             // the wall faces carry no normal flow and the PT iteration never updates them
-            Vx[j] = (ix == 0 || ix == nx) ? 0.0
-                                          : (double)(nn_bilinear(y, NW, nvalid, 3, 1, iy * ry, (ix - 0.5f) * rx) * sc[5]);
+            Vx[j] = (ix == 0 || ix == nx)
+                        ? 0.0
+                        : (double)(nn_bilinear(y, NW, nvalid, nvalid + 1, 3, 1, iy * ry, (ix - 0.5f) * rx + 0.5f) * sc[5]);
         } else {
             const int64_t j = i - nP - nVx;
             const int ix = (int)(j % nx), iy = (int)(j / nx);
-            Vy[j] = (iy == 0 || iy == ny) ? 0.0
-                                          : (double)(nn_bilinear(y, NW, nvalid, 3, 2, (iy - 0.5f) * ry, ix * rx) * sc[6]);
+            Vy[j] = (iy == 0 || iy == ny)
+                        ? 0.0
+                        : (double)(nn_bilinear(y, NW, nvalid + 1, nvalid, 3, 2, (iy - 0.5f) * ry + 0.5f, ix * rx) * sc[6]);
         }
     }
 }
@@ -300,6 +316,7 @@ struct Conv {
 
 struct NNet {
     int H = 0, W = 0, Bmax = 0, base = 32;
+    int pf = 4;  // pooling / upsampling factor between levels (levels at 1, 1/4, 1/16, 1/64)
     std::vector<Conv> conv;      // 15 layers, order below
     std::vector<void*> allocs;
     int64_t step = 0;
@@ -356,7 +373,17 @@ static void nn_layers(NNet* n) {
     }
 }
 
-static int64_t nn_level_P(const NNet* n, int B, int lev) { return (int64_t)B * (n->H >> lev) * (n->W >> lev); }
+static int nn_level_H(const NNet* n, int lev) {
+    int h = n->H;
+    for (int i = 0; i < lev; i++) h /= n->pf;
+    return h;
+}
+static int nn_level_W(const NNet* n, int lev) {
+    int w = n->W;
+    for (int i = 0; i < lev; i++) w /= n->pf;
+    return w;
+}
+static int64_t nn_level_P(const NNet* n, int B, int lev) { return (int64_t)B * nn_level_H(n, lev) * nn_level_W(n, lev); }
 
 static int nn_refresh_bf16(NNet* n, Conv& L, cudaStream_t s) {
     const int64_t nw = (int64_t)L.cout * L.kpad;
@@ -419,8 +446,9 @@ static int nn_create(NNet* n, int H, int W, int Bmax, uint64_t seed) {
     PS_TRY(nn_alloc_t(n, &n->gk0, P0 * 3 * c));
     int64_t colmax = 0, dzmax = 0;
     for (int i = 0; i < 15; i++) {
-        colmax = std::max(colmax, Pl[i] * n->conv[i].kpad);
-        dzmax = std::max(dzmax, Pl[i] * (int64_t)n->conv[i].ldt);
+        const int64_t Pk = (Pl[i] + 7) / 8 * 8;
+        colmax = std::max(colmax, Pk * n->conv[i].kpad);
+        dzmax = std::max(dzmax, Pk * (int64_t)n->conv[i].ldt);
     }
     PS_TRY(nn_alloc_t(n, &n->col, colmax));
     PS_TRY(nn_alloc_t(n, &n->colT, colmax));
@@ -462,17 +490,18 @@ static int nn_conv_fwd(NNet* n, Conv& L, const bf16* x, int B, int h, int w, voi
 static int nn_conv_bwd(NNet* n, Conv& L, const bf16* x, const bf16* yact, const float* dy, int ldy, int B, int h, int w,
                        float* dx, int accumulate, cudaStream_t s, int* err) {
     const int64_t P = (int64_t)B * h * w;
+    const int64_t Pk = (P + 7) / 8 * 8;  // pixel count padded for the weight-gradient GEMM's K (zeros)
     nn_relu_bwd_k<<<nblk(P * L.ldt), 256, 0, s>>>(dy, ldy, yact, P, L.cout, L.relu, n->dz, L.ldt, L.gb);
-    // dz^T [cout][P]
-    nn_transpose_k<<<dim3((unsigned)((P + 31) / 32), (unsigned)((L.cout + 31) / 32)), dim3(32, 8), 0, s>>>(
-        n->dz, P, L.cout, L.ldt, n->dzT);
+    // dz^T [cout][Pk]
+    nn_transpose_k<<<dim3((unsigned)((Pk + 31) / 32), (unsigned)((L.cout + 31) / 32)), dim3(32, 8), 0, s>>>(
+        n->dz, P, L.cout, L.ldt, n->dzT, Pk);
     const bf16* colT = nullptr;
     if (L.k == 3) {
-        nn_im2col3_k<<<nblk(P * L.kpad), 256, 0, s>>>(x, P, h, w, L.cin, (int)L.kpad, n->colT, 1);
+        nn_im2col3_k<<<nblk(Pk * L.kpad), 256, 0, s>>>(x, P, h, w, L.cin, (int)L.kpad, n->colT, Pk);
         colT = n->colT;
     } else {
-        nn_transpose_k<<<dim3((unsigned)((P + 31) / 32), (unsigned)((L.cin + 31) / 32)), dim3(32, 8), 0, s>>>(
-            x, P, L.cin, L.cin, n->colT);
+        nn_transpose_k<<<dim3((unsigned)((Pk + 31) / 32), (unsigned)((L.cin + 31) / 32)), dim3(32, 8), 0, s>>>(
+            x, P, L.cin, L.cin, n->colT, Pk);
         colT = n->colT;
     }
     GemmEpilogue gw{};
@@ -482,10 +511,10 @@ static int nn_conv_bwd(NNet* n, Conv& L, const bf16* x, const bf16* yact, const 
     gw.alpha = 1.0f;
     gw.atomic = 1;
     gw.outf = L.gW;
-    const int64_t kb = (P + 63) / 64;
+    const int64_t kb = (Pk + 63) / 64;
     const int64_t tiles = ((L.cout + 127) / 128) * ((L.kpad + 127) / 128);
     const int split = (int)std::max<int64_t>(1, std::min<int64_t>(kb, (2 * 152 + tiles - 1) / tiles));
-    PS_TRY(nn_gemm(n->dzT, L.cout, colT, L.kpad, P, gw, split, s, err));
+    PS_TRY(nn_gemm(n->dzT, L.cout, colT, L.kpad, Pk, gw, split, s, err));
     if (dx) {
         GemmEpilogue gd{};
         gd.M = P;
@@ -504,15 +533,18 @@ static int nn_conv_bwd(NNet* n, Conv& L, const bf16* x, const bf16* yact, const 
 }
 
 static int nn_forward(NNet* n, int B, cudaStream_t s, int* err) {
-    const int c = n->base, H = n->H, W = n->W;
+    const int c = n->base, f = n->pf;
     auto& L = n->conv;
-    auto cv = [&](int i, const bf16* x, int lev, void* y) { return nn_conv_fwd(n, L[i], x, B, H >> lev, W >> lev, y, s, err); };
+    auto cv = [&](int i, const bf16* x, int lev, void* y) {
+        return nn_conv_fwd(n, L[i], x, B, nn_level_H(n, lev), nn_level_W(n, lev), y, s, err);
+    };
     auto pool = [&](const bf16* x, int lev, int C, bf16* y) {
-        nn_pool2_k<<<nblk(nn_level_P(n, B, lev + 1) * C), 256, 0, s>>>(x, B, H >> lev, W >> lev, C, y);
+        nn_pool_k<<<nblk(nn_level_P(n, B, lev + 1) * C), 256, 0, s>>>(x, B, nn_level_H(n, lev), nn_level_W(n, lev), C,
+                                                                      f, y);
     };
     auto upcat = [&](const bf16* low, int Cl, const bf16* skip, int Cs, int lev, bf16* k) {
         const int64_t P = nn_level_P(n, B, lev);
-        nn_up2_k<<<nblk(P * Cl), 256, 0, s>>>(low, B, H >> lev, W >> lev, Cl, k, Cl + Cs, 0);
+        nn_up_k<<<nblk(P * Cl), 256, 0, s>>>(low, B, nn_level_H(n, lev), nn_level_W(n, lev), Cl, f, k, Cl + Cs, 0);
         nn_copy_ch_k<bf16><<<nblk(P * Cs), 256, 0, s>>>(skip, Cs, 0, P, Cs, k, Cl + Cs, Cl);
     };
     PS_TRY(cv(0, n->x0, 0, n->a[0]));
@@ -543,18 +575,20 @@ static int nn_forward(NNet* n, int B, cudaStream_t s, int* err) {
 
 // dy: FP32 [P0][3] gradient of the output; accumulates gW, gb of every layer
 static int nn_backward(NNet* n, const float* dy, cudaStream_t s, int* err) {
-    const int B = n->lastB, c = n->base, H = n->H, W = n->W;
+    const int B = n->lastB, c = n->base, f = n->pf;
     auto& L = n->conv;
     auto bw = [&](int i, const bf16* x, const bf16* yact, const float* g, int ldg, int lev, float* dx, int acc) {
-        return nn_conv_bwd(n, L[i], x, yact, g, ldg, B, H >> lev, W >> lev, dx, acc, s, err);
+        return nn_conv_bwd(n, L[i], x, yact, g, ldg, B, nn_level_H(n, lev), nn_level_W(n, lev), dx, acc, s, err);
     };
     auto catbwd = [&](const float* gk, int Cl, int Cs, int lev, float* glow, float* gskip) {
         const int64_t P = nn_level_P(n, B, lev), Pl = nn_level_P(n, B, lev + 1);
-        nn_up2_bwd_k<<<nblk(Pl * Cl), 256, 0, s>>>(gk, Cl + Cs, 0, B, H >> lev, W >> lev, Cl, glow);
+        nn_up_bwd_k<<<nblk(Pl * Cl), 256, 0, s>>>(gk, Cl + Cs, 0, B, nn_level_H(n, lev), nn_level_W(n, lev), Cl, f,
+                                                  glow);
         nn_copy_ch_k<float><<<nblk(P * Cs), 256, 0, s>>>(gk, Cl + Cs, Cl, P, Cs, gskip, Cs, 0);
     };
     auto poolbwd = [&](const float* gp, int lev, int C, float* gx) {
-        nn_pool2_bwd_k<<<nblk(nn_level_P(n, B, lev) * C), 256, 0, s>>>(gp, B, H >> lev, W >> lev, C, gx, 1);
+        nn_pool_bwd_k<<<nblk(nn_level_P(n, B, lev) * C), 256, 0, s>>>(gp, B, nn_level_H(n, lev), nn_level_W(n, lev), C,
+                                                                      f, gx, 1);
     };
     PS_TRY(bw(14, n->a[13], nullptr, dy, 3, 0, n->ga[13], 0));
     PS_TRY(bw(13, n->a[12], n->a[13], n->ga[13], c, 0, n->ga[12], 0));
@@ -653,8 +687,8 @@ int ps_nn_create(int64_t H, int64_t W, int32_t max_batch, uint64_t seed, void** 
     PS_TRY(current_state(&st));
     if (!net) return fail(PS_ERR_NULL, "ps_nn_create: NULL output");
     *net = nullptr;
-    if (H < 16 || W < 16 || H % 8 || W % 8 || H * W > (1 << 24))
-        return fail(PS_ERR_SHAPE, "ps_nn_create: H, W must be multiples of 8 in [16, 4096]");
+    if (H < 64 || W < 64 || H % 64 || W % 64 || H * W > (1 << 24))
+        return fail(PS_ERR_SHAPE, "ps_nn_create: H, W must be multiples of 64 in [64, 4096]");
     if (max_batch < 1 || (int64_t)max_batch * H * W > ((int64_t)1 << 26))
         return fail(PS_ERR_ARG, "ps_nn_create: max_batch * H * W must be in [1, 2^26]");
     NNet* n = new NNet();
@@ -856,7 +890,7 @@ int ps_stokes2d_warm_start(void* net, const ps_stokes2d_fields* f, int32_t nvali
         return fail(PS_ERR_DTYPE, "ps_stokes2d_warm_start: FP64 fields with nx, ny >= 3 required");
     if (f->Vx.n[0] != nx + 1 || f->Vy.n[1] != ny + 1 || f->Mus.n[0] != nx || f->Rog.n[1] != ny)
         return fail(PS_ERR_SHAPE, "ps_stokes2d_warm_start: incoherent field sizes");
-    if (nvalid < 2 || nvalid > n->H || nvalid > n->W) return fail(PS_ERR_ARG, "ps_stokes2d_warm_start: bad nvalid");
+    if (nvalid < 2 || nvalid >= n->H || nvalid >= n->W) return fail(PS_ERR_ARG, "ps_stokes2d_warm_start: bad nvalid");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int64_t P0 = (int64_t)n->H * n->W;
     nn_ws_input_k<<<nblk(P0), 256, 0, s>>>(static_cast<const double*>(f->Mus.ptr), static_cast<const double*>(f->Rog.ptr),

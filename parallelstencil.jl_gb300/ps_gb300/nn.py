@@ -130,7 +130,7 @@ class Net:
 
         lev = (0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0, 0)[layer]
         c = (32, 32, 64, 64, 128, 128, 256, 256, 128, 128, 64, 64, 32, 32, 3)[layer]
-        a = np.empty((B, self.H >> lev, self.W >> lev, c), dtype=np.float32)
+        a = np.empty((B, self.H // 4 ** lev, self.W // 4 ** lev, c), dtype=np.float32)
         _lib.call("ps_nn_get_activation", self._h, int(layer), a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
         return a
 

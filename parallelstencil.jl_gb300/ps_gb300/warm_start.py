@@ -9,12 +9,14 @@ contrast between two touching inclusions counts, hence the +-0.5 decades, which 
 contrast by 10. A setup whose solve still fails is redrawn (counted in the statistics).
 
 Network input: log10(Mus), Rog on the n x n node grid, padded by edge replication to the
-network's size; targets: P, and Vx, Vy averaged onto the nodes. Warm start at any resolution:
+network's size; targets: the staggered P (n x n), Vx (n+1 faces x n) and Vy (n x n+1 faces), which
+the network's (n+1) x (n+1) grid holds exactly (edge-replicated where an array is one short).
+Warm start at any resolution:
 the fields are resampled onto the network's grid, the prediction is interpolated back onto the
 staggered arrays (``ps_stokes2d_warm_start``), and the PT solve starts from it.
 
 Command line (runs on the GPU):
-    python -m ps_gb300.warm_start train --samples 2000 --epochs 20 --out weights.bin
+    python -m ps_gb300.warm_start train --samples 2000 --epochs 60 --lr 2e-3 --out weights.bin
     python -m ps_gb300.warm_start eval --weights weights.bin --seeds 200 --n 1023
 """
 from __future__ import annotations
@@ -77,9 +79,7 @@ def sample_arrays(Mus, Rog, g):
     """Network input [N, N, 2] and target [N, N, 3] (float32, unnormalised) of a solved setup."""
     P, Vx, Vy = g.host("Pt"), g.host("Vx"), g.host("Vy")
     x = np.stack([_pad_nodes(np.log10(Mus)), _pad_nodes(Rog)], axis=-1)
-    Vxn = 0.5 * (Vx[:-1, :] + Vx[1:, :])
-    Vyn = 0.5 * (Vy[:, :-1] + Vy[:, 1:])
-    t = np.stack([_pad_nodes(P), _pad_nodes(Vxn), _pad_nodes(Vyn)], axis=-1)
+    t = np.stack([_pad_nodes(P), _pad_nodes(Vx), _pad_nodes(Vy)], axis=-1)
     return x.astype(np.float32), t.astype(np.float32)
 
 
@@ -108,7 +108,7 @@ def generate(samples, seed=1000, n=TRAIN_N, tol=1e-8, log=None):
 
 
 def train(net, X, T, epochs=20, batch=8, lr=1e-3, lr_min=1e-5, seed=0, log=None):
-    """Adam on the weighted MSE of normalised targets (the padded row / column weighted 0)."""
+    """Adam on the MSE of normalised targets (cosine learning-rate decay, flip augmentation)."""
     import torch
 
     S = X.shape[0]
@@ -116,18 +116,48 @@ def train(net, X, T, epochs=20, batch=8, lr=1e-3, lr_min=1e-5, seed=0, log=None)
     net.scales = sc
     Xd = torch.from_numpy(X).cuda()
     Td = torch.from_numpy(T / np.array(sc[4:7], np.float32)).cuda()
-    w = torch.zeros(batch, NET_N, NET_N, device="cuda")
-    w[:, :TRAIN_N, :TRAIN_N] = 1.0
+    w = torch.ones(batch, NET_N, NET_N, device="cuda")
     rng = np.random.default_rng(seed)
     steps = epochs * (S // batch)
     hist, k, t0 = [], 0, time.perf_counter()
+    def mirror(a, dim, face_ch):
+        # mirror the node-aligned channels over nodes 0..n-1 (re-padding the last row / column) and
+        # the face-aligned channel face_ch over all n + 1 faces
+        out = a.clone()
+        node = [c for c in range(a.shape[-1]) if c != face_ch]
+        sl = [slice(None)] * 4
+        sl[dim] = slice(0, TRAIN_N)
+        src = a[..., node][tuple(sl)].flip(dim)
+        dst = [slice(None)] * 4
+        dst[dim] = slice(0, TRAIN_N)
+        tmp = out[..., node]
+        tmp[tuple(dst)] = src
+        pad = [slice(None)] * 4
+        pad[dim] = slice(TRAIN_N, TRAIN_N + 1)
+        last = [slice(None)] * 4
+        last[dim] = slice(TRAIN_N - 1, TRAIN_N)
+        tmp[tuple(pad)] = tmp[tuple(last)]
+        out[..., node] = tmp
+        if face_ch is not None:
+            out[..., face_ch] = a[..., face_ch].flip(dim)
+        return out
+
+    # symmetries of the problem used as augmentation: mirroring x negates Vx; mirroring y with
+    # rho*g negated (gravity acts along y) negates Vy
+    sx_t = torch.tensor([1.0, -1.0, 1.0], device="cuda")
+    sy_x, sy_t = torch.tensor([1.0, -1.0], device="cuda"), torch.tensor([1.0, 1.0, -1.0], device="cuda")
     for ep in range(epochs):
         perm = rng.permutation(S)
         tot = 0.0
         for b in range(S // batch):
             idx = torch.from_numpy(perm[b * batch:(b + 1) * batch]).cuda()
             rate = lr_min + 0.5 * (lr - lr_min) * (1 + np.cos(np.pi * k / steps))
-            tot += net.train_step(Xd[idx], Td[idx], rate, w=w)
+            xb, tb = Xd[idx], Td[idx]
+            if rng.random() < 0.5:  # x (dim 2): Vx (channel 1) lives on faces
+                xb, tb = mirror(xb, 2, None), mirror(tb, 2, 1) * sx_t
+            if rng.random() < 0.5:  # y (dim 1): Vy (channel 2) lives on faces
+                xb, tb = mirror(xb, 1, None) * sy_x, mirror(tb, 1, 2) * sy_t
+            tot += net.train_step(xb, tb, rate, w=w)
             k += 1
         hist.append(tot / (S // batch))
         if log:
@@ -182,7 +212,7 @@ def main(argv=None):
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train")
     t.add_argument("--samples", type=int, default=2000)
-    t.add_argument("--epochs", type=int, default=20)
+    t.add_argument("--epochs", type=int, default=60)
     t.add_argument("--batch", type=int, default=8)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--out", default=DEFAULT_WEIGHTS)

@@ -8,7 +8,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _setup(ps, H=32, W=32, B=2, seed=3):
+def _setup(ps, H=128, W=128, B=2, seed=3):
     import torch
 
     from ps_gb300 import nn
@@ -81,7 +81,8 @@ def test_network_gradients_per_layer(ps):
     assert max(max(e) for e in errs[False]) <= 0.15, errs[False]
     # backward accumulates until zero_grad
     net.backward(dy)
-    assert np.allclose(net.get_grads(), 2 * gg, rtol=1e-4, atol=1e-6)
+    # (split-K weight gradients add partial sums with FP32 atomics in any order: compare norm-wise)
+    assert _relerr(net.get_grads(), 2 * gg) <= 1e-5
 
 
 def test_train_step_loss_and_adam(ps):
