@@ -2,12 +2,14 @@
 // start's convolutions: D[M][N] = A[M][K] * B[N][K]^T, A and B bf16 row-major (K contiguous), FP32
 // accumulation in tensor memory (TMEM).
 //
-// One CTA of 128 threads computes a 128 x 128 tile of D:
-//   - thread 0 streams 128 x 64 tiles of A and B into a 4-stage shared-memory ring with TMA
-//     (cp.async.bulk.tensor.2d, 128-byte swizzle, zero fill past the matrix edges, so M, N and K
-//     need no padding beyond K % 8 == 0) and issues tcgen05.mma (kind::f16, M = 128, N = 128,
-//     K = 16) on each stage; tcgen05.commit arrives on the stage's "empty" mbarrier when its MMAs
-//     have read it, and the stage is refilled;
+// One CTA of 128 threads computes a 128 x BN tile of D (BN = 128, or 256 when N > 128):
+//   - warp 0 (one thread) streams 128 x 64 / BN x 64 tiles of A and B into a 6-stage (BN = 256: 4) ring with
+//     TMA (cp.async.bulk.tensor.2d, 128-byte swizzle, zero fill past the matrix edges, so M, N and
+//     K need no padding beyond K % 8 == 0), refilling a stage as soon as its "empty" mbarrier says
+//     the MMAs that read it are done;
+//   - warp 1 (one thread) waits for each stage's "full" mbarrier and issues tcgen05.mma
+//     (kind::f16, M = 128, N = BN, K = 16) on it; tcgen05.commit arrives on the stage's "empty"
+//     mbarrier when those MMAs have read it;
 //   - all four warps then read the accumulator with tcgen05.ld (warp w owns TMEM lanes / tile
 //     rows 32w..32w+31) and apply the epilogue: + bias[n], ReLU, store as bf16 or FP32, or add
 //     into FP32 output with atomics (split-K over blockIdx.z).
@@ -22,12 +24,18 @@
 
 namespace ps {
 
-constexpr int G_BM = 128, G_BN = 128, G_BK = 64, G_S = 4;
+constexpr int G_BM = 128, G_BK = 64;
 constexpr int G_ABYTES = G_BM * G_BK * 2;  // 16 KB
-constexpr int G_BBYTES = G_BN * G_BK * 2;  // 16 KB
-constexpr int G_STAGE = G_ABYTES + G_BBYTES;
-constexpr int G_SMEM = G_S * G_STAGE + 1024 + 128;  // ring (1024-aligned) + barriers and TMEM slot
-constexpr uint32_t G_TMEM_COLS = 128;              // FP32 accumulator: one column per n
+// Tile N = 128 (6-stage ring) or 256 (4 stages; an MMA then reads A once for twice the work, which
+// keeps the instruction off the shared-memory bandwidth limit a 128 x 128 x 16 MMA sits at).
+template <int BN>
+struct GCfg {
+    static constexpr int S = BN == 256 ? 4 : 6;
+    static constexpr int BBYTES = BN * G_BK * 2;
+    static constexpr int STAGE = G_ABYTES + BBYTES;
+    static constexpr int SMEM = S * STAGE + 1024 + 256;  // ring (1024-aligned) + barriers, TMEM slot, counters
+    static constexpr uint32_t TMEM = BN;                 // FP32 accumulator: one column per n
+};
 
 // tcgen05 instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
@@ -84,9 +92,12 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+template <int BN>
 __global__ void __launch_bounds__(128, 1)
     nn_gemm_tc(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, int64_t K,
                int kb_per_split, GemmEpilogue e, int* __restrict__ err) {
+    using C = GCfg<BN>;
+    constexpr int G_S = C::S, G_STAGE = C::STAGE;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -94,8 +105,9 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t* empty = full + G_S;
     uint64_t* done = empty + G_S;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    int* counts = reinterpret_cast<int*>(tmem_slot + 1);  // [0] copies issued, [1] stages consumed
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * G_BM, n0 = blockIdx.y * G_BN;
+    const int m0 = blockIdx.x * G_BM, n0 = blockIdx.y * BN;
     const int KB = (int)((K + G_BK - 1) / G_BK);
     const int kb0 = blockIdx.z * kb_per_split;
     const int nkb = min(KB, kb0 + kb_per_split) - kb0;
@@ -110,31 +122,31 @@ __global__ void __launch_bounds__(128, 1)
         mbar_init(done, 1);
         fence_mbar_init();
     }
-    if (warp == 0) tc_alloc(tmem_slot, G_TMEM_COLS);
+    if (warp == 0) tc_alloc(tmem_slot, C::TMEM);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (threadIdx.x == 0) {
-        constexpr uint32_t idesc = umma_idesc_bf16(G_BM, G_BN);
-        int issued = 0, consumed = 0;
-        bool ok = true;
-        auto load = [&](int i) {
-            unsigned char* st = smem + (i % G_S) * G_STAGE;
-            mbar_arrive_expect_tx(&full[i % G_S], G_STAGE);
-            tma_load_2d(st, &mA, &full[i % G_S], (kb0 + i) * G_BK, m0);
-            tma_load_2d(st + G_ABYTES, &mB, &full[i % G_S], (kb0 + i) * G_BK, n0);
-            ++issued;
-        };
-        for (int i = 0; i < min(G_S, nkb); i++) load(i);
-        for (int i = 0; i < nkb; i++) {
+    if (threadIdx.x == 0) {  // TMA producer
+        int i = 0;
+        for (; i < nkb; i++) {
             const int s = i % G_S;
-            if (!mbar_wait_bounded(&full[s], (i / G_S) & 1)) {
-                ok = false;
-                break;
-            }
-            ++consumed;
+            // stage s was last read by the MMAs of k-block i - G_S: its empty barrier's (i/G_S - 1)th phase
+            if (i >= G_S && !mbar_wait_bounded(&empty[s], ((i / G_S) - 1) & 1)) break;
+            unsigned char* st = smem + s * G_STAGE;
+            mbar_arrive_expect_tx(&full[s], G_STAGE);
+            tma_load_2d(st, &mA, &full[s], (kb0 + i) * G_BK, m0);
+            tma_load_2d(st + G_ABYTES, &mB, &full[s], (kb0 + i) * G_BK, n0);
+        }
+        counts[0] = i;
+        if (i < nkb) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+    } else if (threadIdx.x == 32) {  // MMA issuer
+        constexpr uint32_t idesc = umma_idesc_bf16(G_BM, BN);
+        int i = 0;
+        for (; i < nkb; i++) {
+            const int s = i % G_S;
+            if (!mbar_wait_bounded(&full[s], (i / G_S) & 1)) break;
             tc_fence_after();
             const uint32_t sa = smem_u32(smem + s * G_STAGE);
             const uint64_t da = umma_desc_sw128(sa), db = umma_desc_sw128(sa + G_ABYTES);
@@ -142,31 +154,22 @@ __global__ void __launch_bounds__(128, 1)
             for (int k = 0; k < G_BK / 16; k++)  // K = 16 per MMA: +32 bytes along the swizzled row
                 tc_mma(tmem, da + 2 * k, db + 2 * k, idesc, (i > 0 || k > 0) ? 1u : 0u);
             tc_commit(&empty[s]);
-            // refill the stage the previous MMAs read, once they have finished with it
-            if (i >= 1 && i - 1 + G_S < nkb) {
-                if (!mbar_wait_bounded(&empty[(i - 1) % G_S], ((i - 1) / G_S) & 1)) {
-                    ok = false;
-                    break;
-                }
-                load(i - 1 + G_S);
-            }
         }
+        counts[1] = i;
+        if (i < nkb) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
         tc_commit(done);  // arrives when every MMA issued above has completed
-        if (!ok) {
-            atomicOr(err, DEV_ERR_TMA_TIMEOUT);
-            for (int j = consumed; j < issued; j++) mbar_wait_bounded(&full[j % G_S], (j / G_S) & 1);
-        }
     }
     __syncwarp();
     const bool have = mbar_wait_bounded(done, 0);
     tc_fence_after();
+    __syncthreads();  // counts[] visible; every warp converged before the collective tcgen05.ld
     if (!have) {
         if (threadIdx.x == 0) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
     } else if (nkb > 0) {
         const int row = warp * 32 + lane;
         const int64_t gm = (int64_t)m0 + row;
         const bool row_ok = gm < e.M;
-        for (int c = 0; c < G_BN; c += 16) {
+        for (int c = 0; c < BN; c += 16) {
             float v[16];
             tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);  // whole warp, no divergence
             if (!row_ok) continue;
@@ -187,22 +190,24 @@ __global__ void __launch_bounds__(128, 1)
             }
         }
     }
+    if (threadIdx.x == 0 && counts[1] < counts[0])  // a wait gave up: drain the copies still in flight
+        for (int j = counts[1]; j < counts[0]; j++) mbar_wait_bounded(&full[j % G_S], (j / G_S) & 1);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc_dealloc(tmem, G_TMEM_COLS);
+    if (warp == 0) tc_dealloc(tmem, C::TMEM);
 }
 
-int nn_gemm(const void* A, int64_t M, const void* B, int64_t N, int64_t K, const GemmEpilogue& e, int split,
-            cudaStream_t s, int* d_err) {
-    if (M <= 0 || N <= 0 || K <= 0) return PS_OK;
-    if (K % 8) return fail(PS_ERR_SHAPE, "nn_gemm: K = %lld must be a multiple of 8", (long long)K);
-    if (M > ((int64_t)65535 * 32768) || N > 65535LL * G_BN) return fail(PS_ERR_SHAPE, "nn_gemm: matrix too large");
+template <int BN>
+static int nn_gemm_bn(const void* A, int64_t M, const void* B, int64_t N, int64_t K, const GemmEpilogue& e,
+                      int split, cudaStream_t s, int* d_err) {
+    using C = GCfg<BN>;
+    if (M > ((int64_t)65535 * 32768) || N > 65535LL * BN) return fail(PS_ERR_SHAPE, "nn_gemm: matrix too large");
     CUtensorMap mA, mB;
     PS_TRY(encode_bf16_rows_sw128(&mA, A, (uint64_t)K, (uint64_t)M, G_BK, G_BM));
-    PS_TRY(encode_bf16_rows_sw128(&mB, B, (uint64_t)K, (uint64_t)N, G_BK, G_BN));
+    PS_TRY(encode_bf16_rows_sw128(&mB, B, (uint64_t)K, (uint64_t)N, G_BK, BN));
     static bool attr = false;
     if (!attr) {
-        PS_CUDA_TRY(cudaFuncSetAttribute(nn_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM));
+        PS_CUDA_TRY(cudaFuncSetAttribute(nn_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
         attr = true;
     }
     const int KB = (int)((K + G_BK - 1) / G_BK);
@@ -210,10 +215,18 @@ int nn_gemm(const void* A, int64_t M, const void* B, int64_t N, int64_t K, const
     if (split > 1 && (!e.atomic || e.out_bf16 || e.bias || e.relu))
         return fail(PS_ERR_ARG, "nn_gemm: split-K needs a plain FP32 atomic epilogue");
     const int per = (KB + split - 1) / split;
-    const dim3 grid((unsigned)((M + G_BM - 1) / G_BM), (unsigned)((N + G_BN - 1) / G_BN), (unsigned)((KB + per - 1) / per));
-    nn_gemm_tc<<<grid, 128, G_SMEM, s>>>(mA, mB, K, per, e, d_err);
+    const dim3 grid((unsigned)((M + G_BM - 1) / G_BM), (unsigned)((N + BN - 1) / BN), (unsigned)((KB + per - 1) / per));
+    nn_gemm_tc<BN><<<grid, 128, C::SMEM, s>>>(mA, mB, K, per, e, d_err);
     PS_CUDA_TRY(cudaGetLastError());
     return PS_OK;
+}
+
+int nn_gemm(const void* A, int64_t M, const void* B, int64_t N, int64_t K, const GemmEpilogue& e, int split,
+            cudaStream_t s, int* d_err) {
+    if (M <= 0 || N <= 0 || K <= 0) return PS_OK;
+    if (K % 8) return fail(PS_ERR_SHAPE, "nn_gemm: K = %lld must be a multiple of 8", (long long)K);
+    return N > 128 ? nn_gemm_bn<256>(A, M, B, N, K, e, split, s, d_err)
+                   : nn_gemm_bn<128>(A, M, B, N, K, e, split, s, d_err);
 }
 
 }  // namespace ps
