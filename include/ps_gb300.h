@@ -374,6 +374,28 @@ int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, 
                       int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
 
 /* ------------------------------------------------------------------------------------ */
+/* Run-time compiled kernels: any `@parallel` body of FiniteDifferences macros, or a       */
+/* `@parallel_indices` body, beyond the fixed set above (src/parallel.jl:192-277 parses    */
+/* them; src/ParallelKernel/parallel.jl:303-315 launches them).                           */
+/* ------------------------------------------------------------------------------------ */
+
+/* Compile CUDA C `source` (as generated by ps_gb300/jit.py) with NVRTC for sm_103a, without FMA
+ * contraction, and load it on the current device. `entry` is the extern "C" kernel, which takes
+ * one argument block by value:
+ *   struct { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err; }
+ * (array pointers and extents, scalars, first thread index and thread counts per dimension, and
+ * the kernel's out-of-bounds flag, one device int owned by the handle).
+ * Compile errors return PS_ERR_ARG with the compiler log in ps_last_error(). */
+int ps_jit_compile(const char* source, const char* entry, void** kernel);
+/* Launch a compiled kernel over count[0] x count[1] x count[2] threads starting at thread index
+ * lo (0-based), blocks of 32 x 8 x 1, with the given arrays (one dtype) and scalars. With sync,
+ * a set out-of-bounds flag (from this or an earlier asynchronous launch of the same handle) is
+ * cleared and returned as PS_ERR_ARG, the counterpart of Julia's BoundsError. */
+int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                  const int64_t lo[3], const int64_t count[3], void* stream, int sync);
+int ps_jit_destroy(void* kernel);
+
+/* ------------------------------------------------------------------------------------ */
 /* Learned warm start (no counterpart in the reference): BF16 conv encoder-decoder on the */
 /* tcgen05 tensor cores, trained and run by the library's own kernels.                    */
 /* ------------------------------------------------------------------------------------ */

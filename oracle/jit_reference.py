@@ -1,0 +1,543 @@
+"""Test oracle for the run-time compiled kernels (test infrastructure; only the tests use it, as the
+checker): a CPU interpreter of `@parallel` / `@parallel_indices` kernel definitions.
+
+It is written independently of the product's translator (ps_gb300/jit.py): its own tokenizer and
+precedence parser for the Julia subset, FiniteDifferences macros decoded from their names, and a
+plain per-thread evaluation loop. It follows
+- src/FiniteDifferences.jl: index patterns and operation orders of the macros (left-to-right sums,
+  `*0.5` / `*0.25` / `*0.125` averages, `1.0/(sum of 1.0/A)*k` harmonic averages, nested
+  `max`/`min` for @maxloc/@minloc) and the `@within` masks of left-hand selections;
+- src/parallel.jl:789-859: a left-hand array that is not an argument is computed on the fly, its
+  expression evaluated at the index where it is read (only `@all` is allowed for it);
+- src/ParallelKernel/parallel.jl:584-598: literals take the kernel's number type;
+- Julia's arithmetic: `x^2` and `x^3` as products (Base.literal_pow), `Bool * x` as
+  `ifelse(b, x, copysign(0, x))`, NaN-propagating `max`/`min` with max(-0.0, 0.0) == 0.0, 1-based
+  indices with bounds checks (an index outside the array raises IndexError, Julia's BoundsError).
+
+Arithmetic is IEEE double through Python floats, or IEEE single through numpy.float32 scalars, one
+operation at a time with no contraction, so FP64/FP32 results of +, -, *, / and comparisons are the
+exact values a conforming machine produces. Math functions (exp, sqrt of a non-square, pow with a
+non-literal exponent) come from the host's libm and may differ from the device's in the last bits.
+
+Arrays are numpy arrays indexed A[ix-1, iy-1, iz-1] (x first, as Julia's column-major arrays).
+"""
+from __future__ import annotations
+
+import math
+import re
+
+import numpy as np
+
+__all__ = ["parse", "run", "OracleKernel"]
+
+# ---------------------------------------------------------------- tokens
+_TOKEN = re.compile(r"""
+    (?P<nl>\n) | (?P<ws>[ \t\r]+) | (?P<com>\#[^\n]*) |
+    (?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eE][+-]?\d+)?(?:f0)?) |
+    (?P<mac>@[A-Za-z_][A-Za-z0-9_]*) |
+    (?P<id>(?:[A-Za-z_]|[^\x00-\x7f])(?:[A-Za-z0-9_!]|[^\x00-\x7f])*) |
+    (?P<op>==|!=|<=|>=|&&|\|\||::|[-+*/^<>=!(),;\[\]?:.{}$])
+""", re.X)
+
+
+def _tokens(text):
+    text = text.replace("≤", "<=").replace("≥", ">=").replace("≠", "!=")
+    out, depth = [], 0
+    for m in _TOKEN.finditer(text):
+        kind, val = m.lastgroup, m.group()
+        if kind in ("ws", "com") or val == "$":
+            continue
+        if kind == "id" and val.endswith("!") and m.end() < len(text) and text[m.end()] == "=":
+            # `a!=b`: the identifier does not own the `!`
+            val = val[:-1]
+            out.append(("id", val))
+            out.append(("op", "!"))
+            continue
+        if kind == "op" and val in "([{":
+            depth += 1
+        elif kind == "op" and val in ")]}":
+            depth -= 1
+        if kind == "nl":
+            if depth > 0:
+                continue
+            if out and out[-1] == ("nl", "\n"):
+                continue
+        if kind == "op" and val == ";" and depth == 0:
+            kind, val = "nl", "\n"
+        out.append((kind, val))
+    out.append(("eof", ""))
+    return out
+
+
+class _P:
+    """Recursive-descent parser of statements and expressions (Julia precedence)."""
+
+    def __init__(self, toks):
+        self.t, self.i = toks, 0
+
+    def peek(self, k=0):
+        return self.t[self.i + k]
+
+    def next(self):
+        tok = self.t[self.i]
+        self.i += 1
+        return tok
+
+    def expect(self, val):
+        tok = self.next()
+        if tok[1] != val:
+            raise SyntaxError(f"expected {val!r}, got {tok[1]!r}")
+        return tok
+
+    def skip_nl(self):
+        while self.peek()[0] == "nl":
+            self.i += 1
+
+    # statements
+    def block(self, stops):
+        out = []
+        while True:
+            self.skip_nl()
+            tok = self.peek()
+            if tok[0] == "eof" or (tok[0] == "id" and tok[1] in stops):
+                return out
+            s = self.statement()
+            if s is not None:
+                out.append(s)
+
+    def statement(self):
+        tok = self.peek()
+        if tok == ("id", "return"):
+            self.next()
+            if self.peek()[0] not in ("nl", "eof") and self.peek()[1] != "end":
+                self.expr()
+            return None
+        if tok == ("id", "if"):
+            return self.if_stmt()
+        lhs = self.expr()
+        if self.peek()[1] != "=":
+            raise SyntaxError("kernel statements are assignments or if-blocks")
+        self.next()
+        self.skip_nl()
+        return ("assign", lhs, self.expr())
+
+    def if_stmt(self):
+        self.next()  # if / elseif
+        cond = self.expr()
+        body = self.block(("elseif", "else", "end"))
+        tok = self.next()
+        if tok[1] == "end":
+            return ("if", cond, body, [])
+        if tok[1] == "else":
+            other = self.block(("end",))
+            self.expect("end")
+            return ("if", cond, body, other)
+        self.i -= 1  # elseif: parse as a nested if owning the final `end`
+        return ("if", cond, body, [self.if_stmt()])
+
+    # expressions, lowest precedence first
+    def expr(self):
+        c = self.or_()
+        if self.peek()[1] == "?":
+            self.next()
+            a = self.expr()
+            self.expect(":")
+            return ("ifelse", c, a, self.expr())
+        return c
+
+    def or_(self):
+        a = self.and_()
+        while self.peek()[1] == "||":
+            self.next()
+            self.skip_nl()
+            a = ("or", a, self.and_())
+        return a
+
+    def and_(self):
+        a = self.cmp()
+        while self.peek()[1] == "&&":
+            self.next()
+            self.skip_nl()
+            a = ("and", a, self.cmp())
+        return a
+
+    def cmp(self):
+        first = self.arith()
+        ops, rest = [], []
+        while self.peek()[1] in ("<", "<=", ">", ">=", "==", "!="):
+            ops.append(self.next()[1])
+            self.skip_nl()
+            rest.append(self.arith())
+        return ("cmp", ops, [first] + rest) if ops else first
+
+    def arith(self):
+        a = self.term()
+        while self.peek()[1] in ("+", "-"):
+            op = self.next()[1]
+            self.skip_nl()
+            a = ("bin", op, a, self.term())
+        return a
+
+    def term(self):
+        a = self.unary()
+        while self.peek()[1] in ("*", "/"):
+            op = self.next()[1]
+            self.skip_nl()
+            a = ("bin", op, a, self.unary())
+        return a
+
+    def unary(self):
+        if self.peek()[1] in ("-", "+", "!"):
+            op = self.next()[1]
+            x = self.unary()
+            return ("not", x) if op == "!" else (("neg", x) if op == "-" else x)
+        return self.power()
+
+    def power(self):
+        base = self.postfix()
+        if self.peek()[1] == "^":
+            self.next()
+            return ("pow", base, self.unary())  # right-associative, binds tighter than unary minus on its left
+        return base
+
+    def postfix(self):
+        tok = self.next()
+        if tok[0] == "num":
+            v = tok[1]
+            if v.endswith("f0") or "." in v or "e" in v.lower():
+                return ("num", float(v.replace("f0", "")), True)
+            return ("num", int(v), False)
+        if tok[0] == "mac":
+            self.expect("(")
+            name = self.next()
+            if name[0] != "id":
+                raise SyntaxError("a macro takes an array name")
+            self.expect(")")
+            return ("macro", tok[1][1:], name[1])
+        if tok[1] == "(":
+            e = self.expr()
+            self.expect(")")
+            return e
+        if tok[0] == "id":
+            if self.peek()[1] == "(":
+                self.next()
+                args = []
+                while self.peek()[1] != ")":
+                    args.append(self.expr())
+                    if self.peek()[1] == ",":
+                        self.next()
+                self.expect(")")
+                return ("call", tok[1], args)
+            if self.peek()[1] == "[":
+                self.next()
+                idx = []
+                while self.peek()[1] != "]":
+                    idx.append(self.expr())
+                    if self.peek()[1] == ",":
+                        self.next()
+                self.expect("]")
+                return ("index", tok[1], idx)
+            if tok[1] in ("true", "false"):
+                return ("bool", tok[1] == "true")
+            return ("name", tok[1])
+        raise SyntaxError(f"unexpected token {tok[1]!r}")
+
+
+class OracleKernel:
+    def __init__(self, name, kind, indices, argnames, body, ndims_opt):
+        self.name, self.kind, self.indices = name, kind, indices
+        self.argnames, self.body, self.ndims_opt = argnames, body, ndims_opt
+
+
+def parse(src: str) -> OracleKernel:
+    """Read a `@parallel` / `@parallel_indices` function definition."""
+    m = re.search(r"@parallel(_indices)?\b(.*?)\bfunction\s+([^\s(]+)\s*\(", src, re.S)
+    if not m:
+        raise SyntaxError("not a kernel definition")
+    kind = "parallel_indices" if m.group(1) else "parallel"
+    head, indices = m.group(2).strip(), []
+    if kind == "parallel_indices":
+        mi = re.match(r"\(([^)]*)\)|(\S+)", head)
+        indices = [s.strip() for s in (mi.group(1) if mi.group(1) is not None else mi.group(2)).split(",") if s.strip()]
+        head = head[mi.end():]
+    opts = dict(o.split("=", 1) for o in head.split())
+    depth, j = 0, m.end() - 1
+    for j in range(m.end() - 1, len(src)):
+        depth += src[j] == "("
+        depth -= src[j] == ")"
+        if depth == 0:
+            break
+    argnames = [a.split("::")[0].strip() for a in src[m.end():j].split(",") if a.strip()]
+    rest = src[j + 1:].strip()
+    rest = re.sub(r"^where\s*(\{[^}]*\}|[^\n]*)", "", rest).strip()
+    assert rest.endswith("end")
+    p = _P(_tokens(rest[:-3]))
+    body = p.block(())
+    return OracleKernel(m.group(3), kind, indices, argnames, body, int(opts["ndims"]) if "ndims" in opts else None)
+
+
+# ---------------------------------------------------------------- FiniteDifferences macros by name
+_AX = "xyz"
+
+
+def _decode(name, nd):
+    """Macro name -> (kind, operated dims, dims selected inner). kind: sel | d | d2 | av | harm | maxloc | minloc."""
+    if name in ("maxloc", "minloc"):
+        return name, [], list(range(nd))
+    if name == "all":
+        return "sel", [], []
+    if name == "inn":
+        return "sel", [], list(range(nd))
+    if name.startswith("inn_"):
+        return "sel", [], [_AX.index(c) for c in name[4:]]
+    m = re.fullmatch(r"(d2|d|av|harm)(?:_([xyz]+)([ai]))?", name)
+    if not m:
+        raise KeyError(name)
+    kind, dims, mode = m.group(1), m.group(2), m.group(3)
+    if dims is None:  # 1-D @d/@d2 along x; @av/@harm (any nd) over all dimensions
+        ops = [0] if kind in ("d", "d2") else list(range(nd))
+        inner = []
+    else:
+        ops = [_AX.index(c) for c in dims]
+        inner = [d for d in range(nd) if d not in ops] if mode == "i" else []
+    if any(d >= nd for d in ops):
+        raise KeyError(name)
+    if kind in ("d", "d2") and len(ops) != 1:
+        raise KeyError(name)
+    return kind, ops, inner
+
+
+# ---------------------------------------------------------------- evaluation
+def _jl_max(x, y):
+    if x != x or y != y:
+        return x + y  # NaN
+    if x == y:
+        return y if math.copysign(1.0, float(x)) < 0 else x  # max(-0.0, 0.0) == 0.0
+    return x if x > y else y
+
+
+def _jl_min(x, y):
+    if x != x or y != y:
+        return x + y
+    if x == y:
+        return x if math.copysign(1.0, float(x)) < 0 else y
+    return x if x < y else y
+
+
+_FUN = {"exp": (math.exp, np.exp), "log": (math.log, np.log), "sqrt": (math.sqrt, np.sqrt),
+        "sin": (math.sin, np.sin), "cos": (math.cos, np.cos), "tan": (math.tan, np.tan),
+        "tanh": (math.tanh, np.tanh), "sinh": (math.sinh, np.sinh), "cosh": (math.cosh, np.cosh),
+        "atan": (math.atan, np.arctan), "asin": (math.asin, np.arcsin), "acos": (math.acos, np.arccos),
+        "log10": (math.log10, np.log10), "exp2": (lambda v: 2.0 ** v, np.exp2), "cbrt": (np.cbrt, np.cbrt)}
+
+
+class _Thread:
+    def __init__(self, k, arrays, scalars, temps, R, nd):
+        self.k, self.A, self.S, self.temps, self.R, self.nd = k, arrays, scalars, temps, R, nd
+
+    def real(self, v):
+        return self.R(v) if isinstance(v, (int, bool, float)) and not isinstance(v, self.R) else v
+
+    def load(self, name, idx, depth=0):
+        """Array `name` at 1-based index tuple idx."""
+        if name in self.temps:  # on-the-fly: its expression at this index
+            return self.ev(self.temps[name], tuple(idx) + (1,) * (3 - len(idx)), depth + 1)
+        a = self.A[name]
+        idx = list(idx) + [1] * (a.ndim - len(idx))
+        if len(idx) > a.ndim and any(i != 1 for i in idx[a.ndim:]):
+            raise IndexError(f"{name}{tuple(idx)}")
+        for d in range(a.ndim):
+            if not 1 <= idx[d] <= a.shape[d]:
+                raise IndexError(f"BoundsError: {name}{tuple(idx)} outside {a.shape}")
+        return a[tuple(i - 1 for i in idx[:a.ndim])]
+
+    def macro(self, mname, name, I, depth):
+        kind, ops, inner = _decode(mname, self.nd)
+        base = [I[d] + (1 if d in inner else 0) for d in range(self.nd)]
+
+        def at(shift):
+            return self.load(name, [base[d] + shift.get(d, 0) for d in range(self.nd)], depth)
+
+        if kind == "sel":
+            return at({})
+        if kind == "d":
+            return at({ops[0]: 1}) - at({})
+        if kind == "d2":
+            d = ops[0]
+            c = [I[e] + (1 if (e in inner or e == d) else 0) for e in range(self.nd)]
+            g = lambda s: self.load(name, [c[e] + (s if e == d else 0) for e in range(self.nd)], depth)  # noqa: E731
+            return (g(1) - g(0)) - (g(0) - g(-1))
+        if kind in ("av", "harm"):
+            terms = []
+            for corner in range(1 << len(ops)):  # first operated dimension varies fastest
+                v = at({d: (corner >> j) & 1 for j, d in enumerate(ops)})
+                terms.append(self.R(1.0) / v if kind == "harm" else v)
+            s = terms[0]
+            for t in terms[1:]:
+                s = s + t
+            w = self.R(float(1 << len(ops)))
+            return s * (self.R(1.0) / w) if kind == "av" else (self.R(1.0) / s) * w
+        if kind in ("maxloc", "minloc"):
+            f = _jl_max if kind == "maxloc" else _jl_min
+            m = f(f(at({0: -1}), at({0: 1})), at({}))
+            for d in range(1, self.nd):
+                m = f(m, f(at({d: -1}), at({d: 1})))
+            return m
+        raise KeyError(mname)
+
+    def ev(self, e, I, depth=0):
+        if depth > 64:
+            raise RecursionError("on-the-fly arrays nested too deeply")
+        R, op = self.R, e[0]
+        E = lambda x: self.ev(x, I, depth)  # noqa: E731
+        if op == "num":
+            return R(e[1]) if e[2] else e[1]
+        if op == "bool":
+            return e[1]
+        if op == "name":
+            n = e[1]
+            if n in self.S:
+                return self.S[n]
+            if self.k.kind == "parallel_indices" and n in self.k.indices:
+                return I[self.k.indices.index(n)]
+            if self.k.kind == "parallel" and n in ("ix", "iy", "iz")[:self.nd]:
+                return I["xyz".index(n[1])]
+            raise NameError(n)
+        if op == "neg":
+            return -E(e[1])
+        if op == "not":
+            return not E(e[1])
+        if op == "bin":
+            a, b = E(e[2]), E(e[3])
+            sym = e[1]
+            if sym == "*" and (isinstance(a, bool) or isinstance(b, bool)):
+                flag, x = (a, b) if isinstance(a, bool) else (b, a)
+                x = self.real(x)
+                return x if flag else R(math.copysign(0.0, float(x)))
+            if isinstance(a, int) and isinstance(b, int) and sym != "/":
+                return a + b if sym == "+" else a - b if sym == "-" else a * b
+            a, b = self.real(a), self.real(b)
+            return a + b if sym == "+" else a - b if sym == "-" else a * b if sym == "*" else a / b
+        if op == "pow":
+            x, n = E(e[1]), e[2]
+            if n[0] == "num" and not n[2] and n[1] in (2, 3):
+                x = self.real(x)
+                return x * x if n[1] == 2 else (x * x) * x
+            x, p = self.real(x), self.real(E(n))
+            return R(float(x) ** float(p))
+        if op == "cmp":
+            vals = [E(v) for v in e[2]]
+            for (sym, a, b) in zip(e[1], vals, vals[1:]):
+                ok = {"<": a < b, "<=": a <= b, ">": a > b, ">=": a >= b, "==": a == b, "!=": a != b}[sym]
+                if not ok:
+                    return False
+            return True
+        if op == "and":
+            return bool(E(e[1])) and bool(E(e[2]))
+        if op == "or":
+            return bool(E(e[1])) or bool(E(e[2]))
+        if op == "ifelse":
+            return E(e[2]) if E(e[1]) else E(e[3])
+        if op == "macro":
+            return self.macro(e[1], e[2], I, depth)
+        if op == "index":
+            shape = self.A[e[1]].shape + (1, 1)
+            idx = [int(self.ev(_subst_end(x, shape[d]), I, depth)) for d, x in enumerate(e[2])]
+            return self.load(e[1], idx, depth)
+        if op == "call":
+            f, args = e[1], e[2]
+            if f == "size":
+                a = self.A[args[0][1]]
+                d = E(args[1])
+                return a.shape[d - 1] if d <= a.ndim else 1
+            if f in ("max", "min"):
+                g = _jl_max if f == "max" else _jl_min
+                r = self.real(E(args[0]))
+                for x in args[1:]:
+                    r = g(r, self.real(E(x)))
+                return r
+            if f == "abs":
+                return abs(self.real(E(args[0])))
+            if f == "inv":
+                return R(1.0) / self.real(E(args[0]))
+            if f in ("one", "zero"):
+                return R(1.0 if f == "one" else 0.0)
+            if f == "ifelse":
+                return E(args[1]) if E(args[0]) else E(args[2])
+            if f in _FUN:
+                fn = _FUN[f][0 if R is float else 1]
+                return R(fn(self.real(E(args[0]))))
+            raise NameError(f)
+        raise ValueError(op)
+
+    def run(self, stmts, I):
+        for s in stmts:
+            if s[0] == "if":
+                self.run(s[2] if self.ev(s[1], I) else s[3], I)
+                continue
+            _, lhs, rhs = s
+            if lhs[0] == "macro":
+                sel, name = lhs[1], lhs[2]
+                if name in self.temps:
+                    continue
+                kind, _, inner = _decode(sel, self.nd)
+                a = self.A[name]
+                # @within: the thread index lies inside the selection of A
+                if any(I[d] > (a.shape[d] if d < a.ndim else 1) - (2 if d in inner else 0) for d in range(self.nd)):
+                    continue
+                v = self.real(self.ev(rhs, I))
+                idx = tuple(I[d] - 1 + (1 if d in inner else 0) for d in range(a.ndim))
+                a[idx] = v
+            elif lhs[0] == "index":
+                a = self.A[lhs[1]]
+                shape = a.shape + (1, 1)
+                idx = [int(self.ev(_subst_end(x, shape[d]), I)) for d, x in enumerate(lhs[2])]
+                v = self.real(self.ev(rhs, I))
+                for d in range(a.ndim):
+                    if not 1 <= idx[d] <= a.shape[d]:
+                        raise IndexError(f"BoundsError: {lhs[1]}{tuple(idx)} outside {a.shape}")
+                a[tuple(i - 1 for i in idx[:a.ndim])] = v
+            else:
+                raise SyntaxError("unsupported left-hand side")
+
+
+def _subst_end(e, n):
+    if e == ("name", "end"):
+        return ("num", n, False)
+    if isinstance(e, tuple):
+        return tuple(_subst_end(x, n) if isinstance(x, tuple) else
+                     ([_subst_end(y, n) for y in x] if isinstance(x, list) else x) for x in e)
+    return e
+
+
+def run(src, args, ndims=None, ranges=None):
+    """Run kernel `src` on numpy arrays / scalars `args` (arrays are modified in place, like the
+    device kernel). ranges: 1-based inclusive (start, stop) per dimension; default 1..max extent."""
+    k = parse(src)
+    if len(args) != len(k.argnames):
+        raise TypeError("argument count")
+    arrays = {n: a for n, a in zip(k.argnames, args) if isinstance(a, np.ndarray)}
+    dts = {a.dtype for a in arrays.values()}
+    assert len(dts) <= 1
+    R = np.float32 if dts == {np.dtype(np.float32)} else float
+    scalars = {}
+    for n, v in zip(k.argnames, args):
+        if not isinstance(v, np.ndarray):
+            scalars[n] = int(v) if isinstance(v, (int, np.integer)) and not isinstance(v, bool) else R(v)
+    nd = ndims or k.ndims_opt or max(a.ndim for a in arrays.values())
+    temps = {}
+    for s in k.body:
+        if s[0] == "assign" and s[1][0] == "macro" and s[1][2] not in arrays:
+            if s[1][1] != "all":
+                raise ValueError("on-the-fly arrays take @all")
+            temps[s[1][2]] = s[2]
+    ext = [max((a.shape[d] if d < a.ndim else 1) for a in arrays.values()) for d in range(3)]
+    lo, hi = [1, 1, 1], [ext[0] if nd >= 1 else 1, ext[1] if nd >= 2 else 1, ext[2] if nd >= 3 else 1]
+    if ranges is not None:
+        for d, r in enumerate(ranges):
+            lo[d], hi[d] = r
+    t = _Thread(k, arrays, scalars, temps, R, nd)
+    for iz in range(lo[2], hi[2] + 1):
+        for iy in range(lo[1], hi[1] + 1):
+            for ix in range(lo[0], hi[0] + 1):
+                t.run(k.body, (ix, iy, iz))

@@ -1,0 +1,185 @@
+// ps_jit.cu -- run-time compiled `@parallel` / `@parallel_indices` kernels.
+//
+// The host side (ps_gb300/jit.py) translates a kernel body written with the FiniteDifferences
+// macros (or with explicit indexing, for `@parallel_indices`) into CUDA C following the same rules
+// as the library's fixed kernels: the grid is the largest extent of the array arguments, every
+// statement is masked by `@within` of its left-hand selection, literals take the number type, and
+// there is no FMA contraction. Unless the kernel is defined with `inbounds=true`, every array access
+// is bounds-checked: an index outside the array skips the access and sets the kernel's error flag,
+// which a synchronous launch reads back and reports (Julia raises a BoundsError there). This file compiles that source with NVRTC for sm_103a
+// (`--fmad=false`), loads the cubin into the current context and launches its entry point with one
+// by-value argument block (ps_jit_args below; the generated source declares the same layout).
+//
+// Driver-API entry points (module load / launch) are looked up through the runtime like the TMA
+// encoder, so the library still links only the static runtime and NVRTC.
+#include <nvrtc.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ps_common.cuh"
+
+namespace ps {
+
+// By-value argument block of every generated kernel (identical layout in the generated source).
+constexpr int kJitMaxArrays = 32, kJitMaxScalars = 32;
+struct ps_jit_args {
+    void* a[kJitMaxArrays];
+    long long n[kJitMaxArrays][3];
+    double s[kJitMaxScalars];
+    long long lo[3];   // first thread index (0-based) per dimension
+    long long cnt[3];  // threads per dimension
+    int* err;          // out-of-bounds flag of the kernel (device memory, one int)
+};
+
+typedef CUresult (*ModuleLoadDataFn)(CUmodule*, const void*);
+typedef CUresult (*ModuleGetFunctionFn)(CUfunction*, CUmodule, const char*);
+typedef CUresult (*ModuleUnloadFn)(CUmodule);
+typedef CUresult (*LaunchKernelFn)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                                   CUstream, void**, void**);
+static ModuleLoadDataFn g_load = nullptr;
+static ModuleGetFunctionFn g_getfn = nullptr;
+static ModuleUnloadFn g_unload = nullptr;
+static LaunchKernelFn g_launch = nullptr;
+static std::mutex g_jit_mutex;
+
+template <typename F>
+static int driver_fn(const char* name, F* out) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return fail(PS_ERR_CUDA, "driver entry point %s unavailable", name);
+    }
+    *out = reinterpret_cast<F>(fn);
+    return PS_OK;
+}
+
+static int jit_driver() {
+    std::lock_guard<std::mutex> l(g_jit_mutex);
+    if (g_launch) return PS_OK;
+    PS_TRY(driver_fn("cuModuleLoadData", &g_load));
+    PS_TRY(driver_fn("cuModuleGetFunction", &g_getfn));
+    PS_TRY(driver_fn("cuModuleUnload", &g_unload));
+    PS_TRY(driver_fn("cuLaunchKernel", &g_launch));
+    return PS_OK;
+}
+
+struct JitKernel {
+    CUmodule mod = nullptr;
+    CUfunction fn = nullptr;
+    int device = -1;
+    int* err = nullptr;
+};
+
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" {
+
+int ps_jit_compile(const char* source, const char* entry, void** kernel) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    if (!source || !entry || !kernel) return fail(PS_ERR_NULL, "ps_jit_compile: NULL argument");
+    *kernel = nullptr;
+    PS_TRY(jit_driver());
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, source, "ps_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        return fail(PS_ERR_CUDA, "ps_jit_compile: nvrtcCreateProgram failed");
+    const char* opts[] = {"--gpu-architecture=sm_103a", "--fmad=false", "-std=c++17"};
+    const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
+    if (rc != NVRTC_SUCCESS) {
+        size_t n = 0;
+        nvrtcGetProgramLogSize(prog, &n);
+        std::string log(n, '\0');
+        if (n) nvrtcGetProgramLog(prog, &log[0]);
+        nvrtcDestroyProgram(&prog);
+        return fail(PS_ERR_ARG, "ps_jit_compile: %s: %.400s", nvrtcGetErrorString(rc), log.c_str());
+    }
+    size_t nbin = 0;
+    std::vector<char> bin;
+    if (nvrtcGetCUBINSize(prog, &nbin) == NVRTC_SUCCESS && nbin) {
+        bin.resize(nbin);
+        nvrtcGetCUBIN(prog, bin.data());
+    }
+    nvrtcDestroyProgram(&prog);
+    if (bin.empty()) return fail(PS_ERR_CUDA, "ps_jit_compile: NVRTC produced no cubin");
+    JitKernel* k = new JitKernel();
+    if (cudaMalloc(&k->err, sizeof(int)) != cudaSuccess || cudaMemset(k->err, 0, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        if (k->err) cudaFree(k->err);
+        delete k;
+        return fail(PS_ERR_NOMEM, "ps_jit_compile: cannot allocate the error flag");
+    }
+    CUresult r = g_load(&k->mod, bin.data());
+    if (r == CUDA_SUCCESS) r = g_getfn(&k->fn, k->mod, entry);
+    if (r != CUDA_SUCCESS) {
+        if (k->mod) g_unload(k->mod);
+        cudaFree(k->err);
+        delete k;
+        return fail(PS_ERR_CUDA, "ps_jit_compile: loading the module or entry %s failed (CUresult %d)", entry, (int)r);
+    }
+    cudaGetDevice(&k->device);
+    *kernel = k;
+    return PS_OK;
+}
+
+int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                  const int64_t lo[3], const int64_t count[3], void* stream, int sync) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    if (!kernel || !lo || !count) return fail(PS_ERR_NULL, "ps_jit_launch: NULL argument");
+    if (narrays < 0 || narrays > kJitMaxArrays || nscalars < 0 || nscalars > kJitMaxScalars ||
+        (narrays && !arrays) || (nscalars && !scalars))
+        return fail(PS_ERR_ARG, "ps_jit_launch: at most %d arrays and %d scalars", kJitMaxArrays, kJitMaxScalars);
+    JitKernel* k = static_cast<JitKernel*>(kernel);
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != k->device) return fail(PS_ERR_ARG, "ps_jit_launch: kernel compiled for device %d", k->device);
+    ps_jit_args g;
+    memset(&g, 0, sizeof(g));
+    for (int i = 0; i < narrays; i++) {
+        PS_TRY(check_array(arrays[i], "jit argument"));
+        if (i && arrays[i].dtype != arrays[0].dtype) return fail(PS_ERR_DTYPE, "ps_jit_launch: mixed dtypes");
+        g.a[i] = arrays[i].ptr;
+        for (int d = 0; d < 3; d++) g.n[i][d] = arrays[i].n[d];
+    }
+    for (int i = 0; i < nscalars; i++) g.s[i] = scalars[i];
+    for (int d = 0; d < 3; d++) {
+        if (lo[d] < 0 || count[d] < 0) return fail(PS_ERR_ARG, "ps_jit_launch: negative range");
+        g.lo[d] = lo[d];
+        g.cnt[d] = count[d];
+    }
+    g.err = k->err;
+    if (count[0] == 0 || count[1] == 0 || count[2] == 0) return PS_OK;
+    if (count[1] > 65535LL * 8 || count[2] > 65535) return fail(PS_ERR_SHAPE, "ps_jit_launch: grid too large");
+    const unsigned gx = (unsigned)((count[0] + 31) / 32), gy = (unsigned)((count[1] + 7) / 8), gz = (unsigned)count[2];
+    void* params[] = {&g};
+    const CUresult r = g_launch(k->fn, gx, gy, gz, 32, 8, 1, 0, static_cast<CUstream>(stream), params, nullptr);
+    if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "ps_jit_launch: cuLaunchKernel failed (CUresult %d)", (int)r);
+    PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), sync, "ps_jit_launch"));
+    if (!sync) return PS_OK;
+    int flag = 0;  // the stream is idle here; flags of earlier asynchronous launches are reported too
+    if (cudaMemcpy(&flag, k->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(PS_ERR_CUDA, "ps_jit_launch: reading the error flag failed");
+    if (flag) {
+        cudaMemset(k->err, 0, sizeof(int));
+        return fail(PS_ERR_ARG, "ps_jit_launch: out-of-bounds array access in the kernel (BoundsError)");
+    }
+    return PS_OK;
+}
+
+int ps_jit_destroy(void* kernel) {
+    if (!kernel) return PS_OK;
+    JitKernel* k = static_cast<JitKernel*>(kernel);
+    if (k->mod && g_unload) g_unload(k->mod);
+    if (k->err) cudaFree(k->err);
+    delete k;
+    return PS_OK;
+}
+
+}  // extern "C"

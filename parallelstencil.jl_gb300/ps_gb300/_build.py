@@ -67,7 +67,12 @@ def build(force: bool = False, jobs: int | None = None) -> str:
     newest = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs
+        # NVRTC (run-time compilation of @parallel kernel bodies) from the toolkit the library is built with
+        root = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+        cands = [os.path.join(root, d) for d in ("lib64", "targets/sbsa-linux/lib", "targets/x86_64-linux/lib", "lib")]
+        cudalib = next((d for d in cands if os.path.exists(os.path.join(d, "libnvrtc.so"))), cands[0])
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs + \
+            ["-L" + cudalib, "-lnvrtc", "-Xlinker", "-rpath", "-Xlinker", cudalib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

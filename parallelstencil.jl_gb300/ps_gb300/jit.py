@@ -1,0 +1,628 @@
+"""Run-time compiled ``@parallel`` / ``@parallel_indices`` kernels (any body, not only the fixed set).
+
+``parallel_kernel(src)`` takes a kernel written as in ParallelStencil.jl, e.g. (miniapps/
+ThermalConvection2D.jl:28-34)::
+
+    @parallel function compute_1!(Pt::Data.Array, τxx::Data.Array, ..., β::Data.Number, dx::Data.Number, dy::Data.Number)
+        @all(Pt)   = @all(Pt) - dτ_iter/β*@all(∇V)
+        @all(τxx)  = 2.0*@all(Eta)*(@d_xa(Vx)/dx  - 1.0/3.0*@all(∇V))
+        ...
+        return
+    end
+
+and generates CUDA C with the rules the reference applies when it parses such a body
+(src/parallel.jl:192-277, 654-680, 789-859; src/ParallelKernel/parallel.jl:400-418, 477-485, 795-798):
+
+- thread grid = the largest extent of the array arguments per dimension (or ``ranges``);
+- each ``@sel(A) = expr`` statement is masked by ``@within("@sel", A)`` and writes A at the thread
+  index shifted by the selection's inner offsets; the FiniteDifferences macros expand to the
+  reference's index patterns and operation orders (left-to-right sums, ``*0.5``, ``1.0/(..)*2.0``,
+  Julia's NaN-propagating ``max``/``min``);
+- a left-hand array that is not an argument is an on-the-fly temporary: its expression is inlined,
+  at the shifted index, wherever a later statement uses it;
+- floating literals take the array number type, ``x^2`` / ``x^3`` are products as Julia's literal
+  powers, ``Bool * x`` keeps Julia's signed zero, no FMA contraction (``--fmad=false``).
+
+``@parallel_indices (ix, iy[, iz]) function f!(...)`` bodies use explicit 1-based indexing,
+``size(A, d)``, comparisons and ``if (...) ... end``; the index names map to the grid dimensions.
+
+The CUDA C is compiled by the library (``ps_jit_compile``, NVRTC for sm_103a) and cached per
+source and number type.
+"""
+from __future__ import annotations
+
+import ast
+import ctypes
+import io
+import numbers
+import re
+import tokenize
+from dataclasses import dataclass, field
+
+from . import _lib
+from ._lib import PSArray
+from .core import ArgumentError, descriptor, require_initialized, stream_handle
+from .fd import AV, DIFF, DIFF2, HARM, LHS, MACROS, MAXLOC, MINLOC, SEL
+from .kernels import ranges_to_box
+
+_lib.register("ps_jit_compile", [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)])
+_lib.register("ps_jit_launch", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
+                                ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p, ctypes.c_int])
+_lib.register("ps_jit_destroy", [ctypes.c_void_p])
+
+MAX_ARRAYS = MAX_SCALARS = 32
+_MATH = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "sinh", "cosh", "atan", "asin", "acos", "log10",
+         "exp2", "cbrt"}
+
+
+# ---- reading Julia source ----------------------------------------------------------------
+def _ident(name: str) -> str:
+    """Julia identifier (Unicode allowed) -> Python identifier."""
+    return "".join(c if (c.isascii() and (c.isalnum() or c == "_")) else f"_u{ord(c):04x}_" for c in name)
+
+
+def _sanitize(text: str) -> str:
+    text = re.sub(r"#.*", "", text).replace("$", "")  # `$ix` interpolations name the index itself
+    for a, b in (("≤", "<="), ("≥", ">="), ("≠", "!=")):
+        text = text.replace(a, b)
+    out = []
+    for c in text:
+        out.append(c if c.isascii() else f"_u{ord(c):04x}_")
+    text = "".join(out)
+    text = re.sub(r"@(\w+)\s*\(", r"__m_\1(", text)
+    text = text.replace("^", "**").replace("&&", " and ").replace("||", " or ")
+    text = re.sub(r"!(?!=)", " not ", text)
+    text = re.sub(r"\btrue\b", "True", text)
+    return re.sub(r"\bfalse\b", "False", text)
+
+
+def _to_python(body: str) -> str:
+    """Julia statement / if-block structure -> indented Python source (the expressions are Python)."""
+    body = "\n".join(line.strip() for line in body.splitlines())  # Julia indentation carries no meaning
+    toks = [t for t in tokenize.generate_tokens(io.StringIO(body).readline)
+            if t.type not in (tokenize.COMMENT, tokenize.ENCODING)]
+    lines, cur, depth, indent = [], [], 0, 0
+
+    def flush():
+        nonlocal cur
+        s = tokenize.untokenize([(t.type, t.string) for t in cur]).strip() if cur else ""
+        # a left-hand selection `@all(A) = ...` becomes the assignable `__lhs_all[A] = ...`
+        s = re.sub(r"^__m_(\w+)\s*\(\s*(\w+)\s*\)\s*=(?!=)", r"__lhs_\1[\2] =", s)
+        if s and s != "return":
+            lines.append("    " * indent + s)
+        cur = []
+
+    i = 0
+    while i < len(toks):
+        t = toks[i]
+        if t.type == tokenize.OP and t.string in "([{":
+            depth += 1
+        elif t.type == tokenize.OP and t.string in ")]}":
+            depth -= 1
+        if depth == 0 and (t.type in (tokenize.NEWLINE, tokenize.NL, tokenize.ENDMARKER)
+                           or (t.type == tokenize.OP and t.string == ";")):
+            if not (cur and cur[-1].type == tokenize.OP and cur[-1].string in "+-*/=,<>"):
+                flush()
+            i += 1
+            continue
+        if depth == 0 and t.type == tokenize.NAME and t.string == "else" and not cur:
+            if lines and lines[-1].rstrip().endswith(":"):
+                lines.append("    " * indent + "pass")
+            lines.append("    " * (indent - 1) + "else:")
+            i += 1
+            continue
+        if depth == 0 and t.type == tokenize.NAME and t.string in ("if", "elseif") and not cur:
+            kw = "if"
+            if t.string == "elseif":  # closes the previous branch at the same level
+                if lines and lines[-1].rstrip().endswith(":"):
+                    lines.append("    " * indent + "pass")
+                indent -= 1
+                kw = "elif"
+            j, cond = i + 1, []
+            if toks[j].string == "(":  # the parenthesised condition of a one-line `if (...) stmt end`
+                d = 0
+                while True:
+                    d += toks[j].string == "("
+                    d -= toks[j].string == ")"
+                    cond.append(toks[j])
+                    j += 1
+                    if d == 0:
+                        break
+            else:
+                while toks[j].type not in (tokenize.NEWLINE, tokenize.NL) and toks[j].string != ";":
+                    cond.append(toks[j])
+                    j += 1
+            lines.append("    " * indent + kw + " " + tokenize.untokenize([(c.type, c.string) for c in cond]).strip() + ":")
+            indent += 1
+            i = j
+            continue
+        if depth == 0 and t.type == tokenize.NAME and t.string == "end":
+            flush()
+            if lines and lines[-1].rstrip().endswith(":"):
+                lines.append("    " * indent + "pass")
+            indent -= 1
+            i += 1
+            continue
+        if t.type in (tokenize.INDENT, tokenize.DEDENT):
+            i += 1
+            continue
+        cur.append(t)
+        i += 1
+    flush()
+    return "\n".join(lines) + "\n"
+
+
+@dataclass
+class KernelDef:
+    name: str
+    kind: str                  # "parallel" | "parallel_indices"
+    index_names: list          # parallel_indices: ["ix", "iy", ...]
+    arrays: list               # argument names (Python identifiers) of the arrays, in order
+    scalars: list
+    args: list                 # all argument names in order, ("array" | "scalar", name)
+    body: list                 # Python AST statements
+    source: str = ""
+    int_scalars: set = field(default_factory=set)  # scalars declared `::Integer` / `::Int*`
+    options: dict = field(default_factory=dict)    # keyword options before `function`
+
+
+# keyword options of `@parallel` / `@parallel_indices` definitions (src/parallel.jl:151-175,
+# src/ParallelKernel/parallel.jl:160-172); the memopt family changes how the reference schedules the
+# kernel, not its results, and is accepted without effect here
+_OPTIONS = {"ndims", "N", "inbounds", "padding", "memopt", "loopsize", "loopdim", "optvars", "optranges"}
+
+
+def _array_uses(tree) -> set:
+    """Names the body uses as arrays: FD macro operands, indexed names, `size(A, d)` operands and
+    left-hand selections."""
+    used = set()
+    for n in ast.walk(tree):
+        if isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and n.args and isinstance(n.args[0], ast.Name):
+            if n.func.id.startswith("__m_") or n.func.id in ("size", "eltype"):
+                used.add(n.args[0].id)
+        elif isinstance(n, ast.Subscript) and isinstance(n.value, ast.Name):
+            if n.value.id.startswith("__lhs_"):
+                if isinstance(n.slice, ast.Name):
+                    used.add(n.slice.id)
+            else:
+                used.add(n.value.id)
+    return used
+
+
+def parse(src: str) -> KernelDef:
+    """Parse a Julia `@parallel` / `@parallel_indices` function definition."""
+    m = re.search(r"@parallel(_indices)?\b(.*?)\bfunction\s+([^\s(]+)\s*\(", src, re.S)
+    if not m:
+        raise ArgumentError("expected `@parallel function name!(args...)` or `@parallel_indices (ix,...) function ...`")
+    kind = "parallel_indices" if m.group(1) else "parallel"
+    head, idx, options = m.group(2).strip(), [], {}
+    if kind == "parallel_indices":
+        mi = re.match(r"\(([^)]*)\)|([^\s=]+)(?=\s|$)", head)
+        if not mi:
+            raise ArgumentError("@parallel_indices: argument 'indices' must be a tuple of indices or a single index "
+                                "(e.g. (ix, iy, iz) or (ix, iy) or ix ).")
+        idx = [_ident(s.strip()) for s in (mi.group(1) if mi.group(1) is not None else mi.group(2)).split(",")
+               if s.strip()]
+        head = head[mi.end():].strip()
+        if not 1 <= len(idx) <= 3:
+            raise ArgumentError("@parallel_indices needs 1-3 index names")
+    for opt in head.split():
+        k, eq, v = opt.partition("=")
+        if not eq or k not in _OPTIONS:
+            raise ArgumentError(f"unsupported keyword argument in the kernel definition: {opt}")
+        options[k] = v
+    if options.get("padding", "false") != "false":
+        raise ArgumentError("padding=true is not supported by run-time compiled kernels")
+    if "ndims" in options:
+        if not options["ndims"].isdigit() or not 1 <= int(options["ndims"]) <= 3:
+            raise ArgumentError("ndims must be 1, 2 or 3")
+    if options.get("inbounds", "false") not in ("true", "false"):
+        raise ArgumentError("inbounds must be true or false")
+    # argument list: balanced parentheses after the name
+    i, d = m.end() - 1, 0
+    for j in range(i, len(src)):
+        d += src[j] == "("
+        d -= src[j] == ")"
+        if d == 0:
+            break
+    arglist, rest = src[i + 1:j], src[j + 1:]
+    rest = re.sub(r"^\s*where\s*(\{[^}]*\}|[^\n]*)", "", rest)  # `where T <: ...` clauses
+    rest = rest.rstrip()
+    if not rest.endswith("end"):
+        raise ArgumentError("kernel definition must end with `end`")
+    body = _to_python(_sanitize(rest[:-3]))
+    try:
+        tree = ast.parse(body)
+    except SyntaxError as e:
+        raise ArgumentError(f"cannot parse the kernel body: {e}") from None
+    used = _array_uses(tree)
+    args, arrays, scalars, ints = [], [], [], set()
+    for a in [s.strip() for s in arglist.split(",") if s.strip()]:
+        nm, _, ty = a.partition("::")
+        nm, ty = _ident(nm.strip()), ty.strip()
+        # number and array types decide; untyped arguments and type parameters follow their use in the body
+        if re.match(r"(Data\.Number|Real|AbstractFloat|Float\d*|Integer|U?Int\d*|Number)$", ty):
+            is_array = False
+        elif "Array" in ty or "Field" in ty:
+            is_array = True
+        else:
+            is_array = nm in used
+        args.append(("array" if is_array else "scalar", nm))
+        (arrays if is_array else scalars).append(nm)
+        if not is_array and re.match(r"(Integer|U?Int\d*)$", ty):
+            ints.add(nm)
+    if len(arrays) > MAX_ARRAYS or len(scalars) > MAX_SCALARS:
+        raise ArgumentError(f"at most {MAX_ARRAYS} arrays and {MAX_SCALARS} scalars")
+    for n in used - set(arrays):
+        if n in scalars:
+            raise ArgumentError(f"scalar argument {n} is used as an array")
+    return KernelDef(m.group(3), kind, idx, arrays, scalars, args, tree.body, src, ints, options)
+
+
+# ---- code generation -----------------------------------------------------------------------
+def _lit(v):
+    return f"((R){float(v)!r})"
+
+
+class _Gen:
+    def __init__(self, kd: KernelDef, ndims: int):
+        self.kd, self.nd = kd, ndims
+        self.macros = MACROS[ndims]
+        self.sels = LHS[ndims]
+        self.aidx = {n: i for i, n in enumerate(kd.arrays)}
+        self.sidx = {n: i for i, n in enumerate(kd.scalars)}
+        self.temps = {}  # temporary name -> (lhs inn mask, expression)
+        self.checked = kd.options.get("inbounds", "false") != "true"
+
+    # element of array `name` at 0-based integer index expressions (strings) per dimension
+    def at(self, name, ix):
+        k = self.aidx[name]
+        ix = list(ix) + ["0"] * (3 - len(ix))
+        return f"a{k}[({ix[0]}) + n{k}_0 * (({ix[1]}) + n{k}_1 * ({ix[2]}))]"
+
+    # read of that element; unless `inbounds=true`, an index outside the array sets the error flag
+    # and reads 0 (Julia's bounds check raises a BoundsError there)
+    def load(self, name, ix):
+        if not self.checked:
+            return self.at(name, ix)
+        k = self.aidx[name]
+        ix = list(ix) + ["0"] * (3 - len(ix))
+        return f"jl_ld(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)"
+
+    # value of array-or-temporary `name` at thread index + integer offset vector `o`
+    def val(self, name, o):
+        if name in self.temps:
+            li, e = self.temps[name]
+            return self.expr(e, tuple(o[d] - ((li >> d) & 1) for d in range(3)))
+        if name not in self.aidx:
+            raise ArgumentError(f"unknown array {name}")
+        t = ("tx", "ty", "tz")
+        return self.load(name, [f"{t[d]}+{o[d]}" if o[d] else t[d] for d in range(self.nd)])
+
+    def macro(self, mname, name, off):
+        if mname not in self.macros:
+            raise ArgumentError(f"unknown macro @{mname} for {self.nd}-D")
+        kind, opd, inn = self.macros[mname]
+        b = [off[d] + ((inn >> d) & 1) for d in range(3)]
+
+        def shift(d, s):
+            o = list(b)
+            o[d] += s
+            return self.val(name, o)
+
+        dims = [d for d in range(3) if (opd >> d) & 1]
+        if kind == SEL:
+            return self.val(name, b)
+        if kind == DIFF:
+            return f"({shift(dims[0], 1)} - {self.val(name, b)})"
+        if kind == DIFF2:
+            c = self.val(name, b)
+            return f"(({shift(dims[0], 1)} - {c}) - ({c} - {shift(dims[0], -1)}))"
+        if kind in (AV, HARM):
+            terms = []
+            for c in range(1 << len(dims)):
+                o = list(b)
+                for j, d in enumerate(dims):
+                    o[d] += (c >> j) & 1
+                v = self.val(name, o)
+                terms.append(f"((R)1.0 / {v})" if kind == HARM else v)
+            s = terms[0]
+            for t in terms[1:]:
+                s = f"({s} + {t})"
+            k = float(1 << len(dims))
+            return f"({s} * {_lit(1.0 / k)})" if kind == AV else f"(((R)1.0 / {s}) * {_lit(k)})"
+        if kind in (MAXLOC, MINLOC):
+            f = "jl_max" if kind == MAXLOC else "jl_min"
+            m = f"{f}({f}({shift(0, -1)}, {shift(0, 1)}), {self.val(name, b)})"
+            for d in range(1, self.nd):
+                m = f"{f}({m}, {f}({shift(d, -1)}, {shift(d, 1)}))"
+            return m
+        raise ArgumentError(f"macro @{mname} not supported")
+
+    def is_bool(self, e):
+        return isinstance(e, (ast.Compare, ast.BoolOp)) or (isinstance(e, ast.UnaryOp) and isinstance(e.op, ast.Not)) \
+            or (isinstance(e, ast.Constant) and isinstance(e.value, bool))
+
+    def expr(self, e, off=(0, 0, 0), ctx="real"):
+        E = lambda x, c=ctx: self.expr(x, off, c)  # noqa: E731
+        if isinstance(e, ast.Constant):
+            if isinstance(e.value, bool):
+                return "true" if e.value else "false"
+            if isinstance(e.value, int) and ctx != "real":
+                return str(e.value)
+            return _lit(e.value)
+        if isinstance(e, ast.Name):
+            if e.id in self.kd.index_names:
+                return f"((long long)t{'xyz'[self.kd.index_names.index(e.id)]} + 1)"
+            if e.id in self.sidx:
+                return f"s{self.sidx[e.id]}"
+            if self.kd.kind == "parallel" and e.id in ("ix", "iy", "iz")[:self.nd]:  # ParallelStencil.INDICES
+                return f"((long long)t{e.id[1]} + 1)"
+            raise ArgumentError(f"unknown name {e.id} in an expression")
+        if isinstance(e, ast.UnaryOp):
+            if isinstance(e.op, ast.USub):
+                return f"(-{E(e.operand)})"
+            if isinstance(e.op, ast.UAdd):
+                return E(e.operand)
+            if isinstance(e.op, ast.Not):
+                return f"(!{E(e.operand, 'auto')})"
+        if isinstance(e, ast.BinOp):
+            if isinstance(e.op, ast.Pow):
+                if isinstance(e.right, ast.Constant) and e.right.value in (2, 3) and not isinstance(e.right.value, bool):
+                    x = E(e.left)
+                    return f"({x} * {x})" if e.right.value == 2 else f"(({x} * {x}) * {x})"
+                return f"pow({E(e.left)}, (R)({E(e.right)}))"
+            ops = {ast.Add: "+", ast.Sub: "-", ast.Mult: "*", ast.Div: "/"}
+            if type(e.op) not in ops:
+                raise ArgumentError("unsupported operator")
+            if isinstance(e.op, ast.Mult) and (self.is_bool(e.left) or self.is_bool(e.right)):
+                b, x = (e.left, e.right) if self.is_bool(e.left) else (e.right, e.left)
+                return f"jl_bmul({E(b, 'auto')}, {E(x)})"
+            c = ctx if ctx != "real" else "real"
+            if isinstance(e.op, ast.Div):
+                c = "real"
+            return f"({E(e.left, c)} {ops[type(e.op)]} {E(e.right, c)})"
+        if isinstance(e, ast.Compare):
+            parts, left = [], e.left
+            for op, right in zip(e.ops, e.comparators):
+                sym = {ast.Lt: "<", ast.LtE: "<=", ast.Gt: ">", ast.GtE: ">=", ast.Eq: "==", ast.NotEq: "!="}[type(op)]
+                parts.append(f"({self.expr(left, off, 'auto')} {sym} {self.expr(right, off, 'auto')})")
+                left = right
+            return "(" + " && ".join(parts) + ")"
+        if isinstance(e, ast.BoolOp):
+            sym = " && " if isinstance(e.op, ast.And) else " || "
+            return "(" + sym.join(self.expr(v, off, "auto") for v in e.values) + ")"
+        if isinstance(e, ast.Call) and isinstance(e.func, ast.Name):
+            f = e.func.id
+            if f.startswith("__m_"):
+                if len(e.args) != 1 or not isinstance(e.args[0], ast.Name):
+                    raise ArgumentError(f"@{f[4:]} takes one array")
+                return self.macro(f[4:], e.args[0].id, off)
+            if f == "size":
+                a, d = e.args
+                return f"n{self.aidx[a.id]}_{int(d.value) - 1}"
+            if f in ("max", "min"):
+                r = E(e.args[0])
+                for x in e.args[1:]:
+                    r = f"jl_{f}({r}, {E(x)})"
+                return r
+            if f in ("one", "zero"):  # one(eltype(A)) etc.: the number type's 1 / 0
+                return "((R)1)" if f == "one" else "((R)0)"
+            if f == "ifelse":
+                c, a, b = e.args
+                return f"({E(c, 'auto')} ? {E(a)} : {E(b)})"
+            if f == "abs":
+                return f"fabs({E(e.args[0])})"
+            if f == "inv":
+                return f"((R)1.0 / {E(e.args[0])})"
+            if f in _MATH:
+                return f"{f}({E(e.args[0])})"
+            raise ArgumentError(f"unsupported function {f}")
+        if isinstance(e, ast.Subscript):
+            return self.load(*self.subscript(e, off))
+        raise ArgumentError(f"unsupported expression {ast.dump(e)[:80]}")
+
+    def subscript(self, e, off=(0, 0, 0)):
+        """`A[i, j, ...]` (1-based, Julia's `end` = size(A, d)) -> (A, 0-based index expressions)."""
+        if not isinstance(e.value, ast.Name) or e.value.id not in self.aidx:
+            raise ArgumentError("indexing applies to array arguments")
+        sl = e.slice.elts if isinstance(e.slice, ast.Tuple) else [e.slice]
+        if len(sl) > 3:
+            raise ArgumentError("at most 3 indices")
+
+        def last(node, d):
+            class _End(ast.NodeTransformer):
+                def visit_Name(self, n):
+                    if n.id == "end":
+                        return ast.Call(ast.Name("size", ast.Load()), [ast.Name(e.value.id, ast.Load()),
+                                                                       ast.Constant(d + 1)], [])
+                    return n
+            return _End().visit(node)
+
+        return e.value.id, [f"({self.expr(last(x, d), off, 'int')}) - 1" for d, x in enumerate(sl)]
+
+    def stmt(self, s, ind):
+        p = "    " * ind
+        if isinstance(s, ast.If):
+            out = [f"{p}if ({self.expr(s.test, ctx='auto')}) {{"]
+            for b in s.body:
+                out += self.stmt(b, ind + 1)
+            if s.orelse:
+                out.append(f"{p}}} else {{")
+                for b in s.orelse:
+                    out += self.stmt(b, ind + 1)
+            return out + [f"{p}}}"]
+        if isinstance(s, ast.Pass):
+            return []
+        if not isinstance(s, ast.Assign) or len(s.targets) != 1:
+            raise ArgumentError("kernel statements are assignments or if-blocks")
+        t = s.targets[0]
+        if isinstance(t, ast.Subscript) and isinstance(t.value, ast.Name) and t.value.id.startswith("__lhs_"):
+            sel, name = t.value.id[6:], t.slice.id
+            if sel not in self.sels:
+                raise ArgumentError(f"@{sel} cannot be a left-hand side")
+            li = self.sels[sel]
+            if name in self.temps:  # on-the-fly temporary: inlined where it is used
+                return []
+            k = self.aidx[name]
+            t3 = ("tx", "ty", "tz")
+            cond = " && ".join(f"{t3[d]} < n{k}_{d} - {2 * ((li >> d) & 1)}" for d in range(self.nd))
+            idx = [f"{t3[d]}+{(li >> d) & 1}" for d in range(self.nd)]
+            return [f"{p}if ({cond}) {self.at(name, idx)} = {self.expr(s.value)};"]
+        if isinstance(t, ast.Subscript):  # @parallel_indices: A[i, j] = expr
+            name, ix = self.subscript(t)
+            val = self.expr(s.value)
+            if not self.checked:
+                return [f"{p}{self.at(name, ix)} = (R)({val});"]
+            k = self.aidx[name]
+            ix = list(ix) + ["0"] * (3 - len(ix))
+            return [f"{p}jl_st(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err, (R)({val}));"]
+        raise ArgumentError("unsupported left-hand side")
+
+    def collect_temps(self):
+        """On-the-fly arrays: left-hand arrays that are not arguments (src/parallel.jl:789-819)."""
+        writes = {s.targets[0].slice.id for s in self.kd.body if _is_sel_assign(s)} & set(self.aidx)
+        for s in self.kd.body:
+            if not _is_sel_assign(s) or s.targets[0].slice.id in self.aidx:
+                continue
+            sel, name = s.targets[0].value.id[6:], s.targets[0].slice.id
+            names = {n.id for n in ast.walk(s.value) if isinstance(n, ast.Name)}
+            if sel != "all":
+                raise ArgumentError("unsupported kernel statements in @parallel kernel definition: partial assignments "
+                                    "are not possible for arrays that are not stored in global memory (arrays that "
+                                    "are not among the arguments of the kernel); use '@all' instead.")
+            if name in names:
+                raise ArgumentError("unsupported kernel statements in @parallel kernel definition: auto-dependency is "
+                                    "not possible for arrays that are not stored in global memory (arrays that are "
+                                    "not among the arguments of the kernel).")
+            if names & writes:
+                raise ArgumentError(f"unsupported kernel statements in @parallel kernel definition: the assignment of "
+                                    f"{name} should be done on the fly as it is not among the arguments of the kernel; "
+                                    f"however, this is not possible because it depends on at least one variable that "
+                                    f"is not read-only within the scope of the kernel (any of: {sorted(writes)}).")
+            self.temps[name] = (self.sels[sel], s.value)
+
+    def source(self, real):
+        kd = self.kd
+        self.collect_temps()
+        body = []
+        for s in kd.body:
+            body += self.stmt(s, 1)
+        decl = []
+        for name, k in self.aidx.items():
+            decl.append(f"    R* const a{k} = (R*)g.a[{k}];")
+            decl.append(f"    const long long n{k}_0 = g.n[{k}][0], n{k}_1 = g.n[{k}][1], n{k}_2 = g.n[{k}][2];")
+        for name, k in self.sidx.items():
+            ty = "long long" if name in kd.int_scalars else "R"
+            decl.append(f"    const {ty} s{k} = ({ty})g.s[{k}];")
+        return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}) -- generated by ps_gb300.jit
+typedef {real} R;
+struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; }};
+__device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
+    return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
+__device__ __forceinline__ R jl_ld(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
+    if (jl_in(n0, n1, n2, i, j, k)) return a[i + n0 * (j + n1 * k)];
+    atomicOr(err, 1); return (R)0; }}
+__device__ __forceinline__ void jl_st(R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err, R v) {{
+    if (jl_in(n0, n1, n2, i, j, k)) a[i + n0 * (j + n1 * k)] = v; else atomicOr(err, 1); }}
+__device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
+__device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
+__device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
+extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
+    const long long ux = blockIdx.x * (long long)blockDim.x + threadIdx.x, uy = blockIdx.y * (long long)blockDim.y + threadIdx.y, uz = blockIdx.z;
+    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) return;
+    const long long tx = g.lo[0] + ux, ty = g.lo[1] + uy, tz = g.lo[2] + uz;
+    (void)tx; (void)ty; (void)tz;
+{chr(10).join(decl)}
+{chr(10).join(body)}
+}}
+"""
+
+
+def _is_sel_assign(s):
+    t = s.targets[0] if isinstance(s, ast.Assign) and len(s.targets) == 1 else None
+    return isinstance(t, ast.Subscript) and isinstance(t.value, ast.Name) and t.value.id.startswith("__lhs_") \
+        and isinstance(t.slice, ast.Name)
+
+
+def generate(kd: KernelDef, ndims: int, dtype: str) -> str:
+    """CUDA C of kernel `kd` for `ndims`-D arrays of `dtype` ("double" or "float")."""
+    return _Gen(kd, ndims).source(dtype)
+
+
+# ---- kernels -----------------------------------------------------------------------------------
+def array_ndims(descs):
+    """Rank of a kernel's arrays (the largest; 2-D arrays have n[2] = 1, 1-D arrays n[1] = n[2] = 1)."""
+    return max((3 if d.n[2] > 1 else 2 if d.n[1] > 1 else 1) for d in descs) if descs else 1
+
+
+class JitKernel:
+    """A run-time compiled kernel; call it like `@parallel`: ``ps.parallel(k, *args)`` or ``k(*args)``.
+    ndims selects the FiniteDifferences{1,2,3}D macros (the reference's `@init_parallel_stencil`
+    ndims); None takes the rank of the array arguments."""
+
+    def __init__(self, src: str, ndims=None):
+        self.ndims = ndims
+        self.kd = parse(src)
+        self.name, self.nargs = self.kd.name, len(self.kd.args)
+        self._handles = {}
+
+    def source(self, ndims, dtype="double"):
+        return generate(self.kd, ndims, dtype)
+
+    def _handle(self, ndims, dtype):
+        key = (ndims, dtype)
+        if key not in self._handles:
+            h = ctypes.c_void_p()
+            _lib.call("ps_jit_compile", self.source(ndims, dtype).encode(), b"ps_jit_entry", ctypes.byref(h))
+            self._handles[key] = h
+        return self._handles[key]
+
+    def __call__(self, *args, ranges=None, stream=None, sync=True):
+        self.jit_launch(args, ranges, stream, sync)
+
+    def jit_launch(self, args, ranges=None, stream=None, sync=True):
+        require_initialized()
+        if len(args) != self.nargs:
+            raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
+        arrs, scal = [], []
+        for (kind, name), a in zip(self.kd.args, args):
+            if kind == "scalar" and not isinstance(a, numbers.Real):
+                raise ArgumentError(f"{self.name}: argument {name} is a scalar (obtained {type(a).__name__})")
+            (arrs if kind == "array" else scal).append(a)
+        descs = [descriptor(a) for a in arrs]
+        dt = {0: "double", 1: "float"}.get(descs[0].dtype) if descs else "double"
+        if dt is None or any(d.dtype != descs[0].dtype for d in descs):
+            raise ArgumentError("the array arguments must share one FP64 or FP32 type")
+        ndims = self.ndims or array_ndims(descs)
+        lo, cnt = [0, 0, 0], [1, 1, 1]
+        for d in range(ndims):
+            cnt[d] = max(int(x.n[d]) for x in descs) if descs else 1
+        if ranges is not None:  # Julia ranges: 1-based (start, stop) pairs, or python ranges over 0-based indices
+            lo, hi = ranges_to_box(ranges)
+            if min(lo) < 0:
+                raise ArgumentError("ranges must start at index 1 or above")
+            cnt = [max(0, hi[d] - lo[d]) for d in range(3)]
+        h = self._handle(ndims, dt)
+        A = (PSArray * max(1, len(descs)))(*descs)
+        S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
+        _lib.call("ps_jit_launch", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
+                  (ctypes.c_int64 * 3)(*cnt), stream_handle(stream), int(bool(sync)))
+
+    def __del__(self):
+        try:
+            for h in self._handles.values():
+                _lib.load().ps_jit_destroy(h)
+        except Exception:
+            pass
+
+
+_CACHE = {}
+
+
+def parallel_kernel(src: str, ndims=None) -> JitKernel:
+    """The `@parallel` / `@parallel_indices` function `src` as a run-time compiled kernel (cached)."""
+    if (src, ndims) not in _CACHE:
+        _CACHE[(src, ndims)] = JitKernel(src, ndims)
+    return _CACHE[(src, ndims)]

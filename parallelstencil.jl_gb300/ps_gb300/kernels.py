@@ -157,8 +157,9 @@ def from_source(body: str, ndims: int = 3):
     """Recognise a `@parallel` kernel body (statements separated by ';' or newlines).
 
     This is the pattern matching the `:GB300` package performs on kernel ASTs: known
-    bodies map to their libps_b200.so kernel; one-statement FD bodies map to ps_fd_apply.
-    Anything else raises ArgumentError (there is no generic code generator and no fallback).
+    bodies map to their hand-written libps_b200.so kernel; one-statement FD bodies map to
+    ps_fd_apply. Anything else raises ArgumentError: other bodies need their full definition
+    (argument order) and go through ps_gb300.parallel_kernel, the run-time compiler.
     """
     key = _normalise(body)
     if key in _NORMALISED:
@@ -171,6 +172,9 @@ def from_source(body: str, ndims: int = 3):
 def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True, fp64="ieee"):
     """`@parallel [ranges] [memopt=...] kernel!(args...)`."""
     require_initialized()
+    if hasattr(kernel, "jit_launch"):  # run-time compiled kernel (ps_gb300.jit); memopt does not change results
+        kernel.jit_launch(args, ranges, stream, sync)
+        return
     if isinstance(kernel, FdKernel):
         if ranges is not None or memopt:
             raise ArgumentError("FD operator kernels take no ranges/memopt")

@@ -1,0 +1,133 @@
+"""Kernel definitions (in ParallelStencil.jl's kernel language) shared by the run-time compilation
+tests. They are written for these tests: each one exercises a group of features the translator
+has to get right, with array sizes chosen so that every read of a thread inside its statement's
+`@within` mask is inside its array."""
+
+# 3-D heat step with on-the-fly fluxes (test/test_parallel.jl:411-434 tests this form)
+HEAT_FLUX = """@parallel function heat_flux_step!(Tnew, Told, Cinv, λ::Data.Number, Δt::Data.Number, rdx, rdy, rdz)
+    @all(fx)   = -λ*@d_xi(Told)*rdx           # on-the-fly arrays (not arguments)
+    @all(fy)   = -λ*@d_yi(Told)*rdy
+    @all(fz)   = -λ*@d_zi(Told)*rdz
+    @all(rate) = @inn(Cinv)*(-@d_xa(fx)*rdx - @d_ya(fy)*rdy - @d_za(fz)*rdz)
+    @inn(Tnew) = @inn(Told) + Δt*@all(rate)
+    return
+end"""
+
+# 3-D heat step, second differences (test/test_parallel.jl:521-563 tests this form)
+HEAT_LAP = """@parallel function heat_step!(Tnew, Told, Cinv, λ, Δt, rdx, rdy, rdz)
+    @inn(Tnew) = @inn(Told) + Δt*(λ*@inn(Cinv)*(@d2_xi(Told)*rdx^2 + @d2_yi(Told)*rdy^2 + @d2_zi(Told)*rdz^2))
+    return
+end"""
+
+# the same with divisions (examples/diffusion3D_novis_noperf.jl:10-13 is this form)
+HEAT_DIV = """@parallel function heat_div_step!(Tnew, Told, Cinv, lam, dt, dx, dy, dz)
+    @inn(Tnew) = @inn(Told) + dt*(lam*@inn(Cinv)*(@d2_xi(Told)/dx^2 + @d2_yi(Told)/dy^2 + @d2_zi(Told)/dz^2))
+    return
+end"""
+
+# 2-D staggered viscous stresses: @av, face differences, temporaries read by the same thread
+STRESS2D = """@parallel function stress2d!(Sxx, Syy, Sxy, divV, Vx, Vy, Eta, rdx::Data.Number, rdy::Data.Number)
+    @all(divV) = @d_xa(Vx)*rdx + @d_ya(Vy)*rdy
+    @all(Sxx)  = 2.0*@all(Eta)*(@d_xa(Vx)*rdx - 1.0/3.0*@all(divV))
+    @all(Syy)  = 2.0*@all(Eta)*(@d_ya(Vy)*rdy - 1.0/3.0*@all(divV))
+    @all(Sxy)  = 2.0*@av(Eta)*(0.5*(@d_yi(Vx)*rdy + @d_xi(Vy)*rdx))
+    return
+end"""
+
+# 2-D momentum residuals with @av_yi and damped rates
+MOMENTUM2D = """@parallel function momentum2d!(Rx, Ry, dVx, dVy, P, Sxx, Syy, Sxy, Rho, rdx, rdy, g, damp)
+    @all(Rx)  = @d_xi(Sxx)*rdx + @d_ya(Sxy)*rdy - @d_xi(P)*rdx
+    @all(Ry)  = @d_yi(Syy)*rdy + @d_xa(Sxy)*rdx - @d_yi(P)*rdy - g*@av_yi(Rho)
+    @all(dVx) = damp*@all(dVx) + @all(Rx)
+    @all(dVy) = damp*@all(dVy) + @all(Ry)
+    return
+end"""
+
+# 2-D velocity update on inner points with harmonic means and a local maximum
+VELOCITY2D = """@parallel function velocity2d!(Vx, Vy, dVx, dVy, Eta, Emax, h)
+    @all(Emax) = @maxloc(Eta)
+    @inn(Vx)   = @inn(Vx) + h/@harm_xi(Eta)*@all(dVx)
+    @inn(Vy)   = @inn(Vy) + h/@harm_yi(Eta)*@all(dVy)
+    return
+end"""
+
+# 2-D first-order upwind advection: explicit indices, chained comparisons, Bool * x
+UPWIND2D = """@parallel_indices (i, j) function upwind2d!(Tn, T, u, w, dt, rdx, rdy)
+    if (1 < i < size(T, 1) && 1 < j < size(T, 2))
+        Tn[i, j] = T[i, j] - dt*((u[i, j] > 0)*u[i, j]*(T[i, j] - T[i-1, j])*rdx +
+                                 (u[i, j] < 0)*u[i, j]*(T[i+1, j] - T[i, j])*rdx +
+                                 (w[i, j] > 0)*w[i, j]*(T[i, j] - T[i, j-1])*rdy +
+                                 (w[i, j] < 0)*w[i, j]*(T[i, j+1] - T[i, j])*rdy)
+    end
+    return
+end"""
+
+# 2-D insulated side walls: `end` inside indices, one index over the second dimension's range
+WALLS2D = """@parallel_indices (j) function walls2d!(T)
+    T[1, j]   = T[2, j]
+    T[end, j] = T[end-1, j]
+    return
+end"""
+
+# power-law permeability and exponential compaction (math library calls)
+COMPACTION = """@parallel function compaction!(Phi, K, Pe, phi0::Data.Number, n::Data.Number, lam::Data.Number)
+    @all(K)   = (@all(Phi)/phi0)^n
+    @all(Phi) = @all(Phi)*exp(-lam*@all(Pe))
+    return
+end"""
+
+# 3-D mixed operators: corner averages, harmonic and local maximum, second differences
+BLEND3D = """@parallel function blend3d!(Out, Q, B, D, s::Data.Number)
+    @all(Out) = @av_xyi(B) - s*@harm_zi(D) + @maxloc(B)*@d2_yi(D) + @av(Q)*@d_za(B)
+    return
+end"""
+
+# 3-D partial inner selection on the left-hand side
+FACES3D = """@parallel function faces3d!(W, B, D, s)
+    @inn_yz(W) = @inn_yz(B) + s*@av_za(D)
+    return
+end"""
+
+# 1-D rod
+ROD1D = """@parallel function rod1d!(U2, U, k)
+    @inn(U2) = @inn(U) + k*@d2(U)
+    return
+end"""
+
+# thread indices inside a @parallel body (test/test_parallel.jl:402-410 uses ParallelStencil.INDICES)
+LINEAR_INDEX = """@parallel function linear_index!(A)
+    @all(A) = $ix + ($iy-1)*size(A,1) + ($iz-1)*size(A,1)*size(A,2)
+    return
+end"""
+
+# elseif / else chains, ifelse, max/min, abs, integer scalar exponent
+BRANCHES2D = """@parallel_indices (ix, iy) inbounds=false function branches2d!(B, A, c::Integer, t)
+    if A[ix, iy] > t
+        B[ix, iy] = max(A[ix, iy], t) - abs(A[ix, iy])^c
+    elseif A[ix, iy] < -t
+        B[ix, iy] = min(A[ix, iy], -t) + ifelse(ix > iy, one(t), zero(t))
+    else
+        B[ix, iy] = sqrt(abs(A[ix, iy]))*(iy == 1 || ix == size(A, 1))
+    end
+    return
+end"""
+
+# 3-D explicit-index second difference along z (test/test_parallel.jl:466-479 tests this form)
+D2Z3D = """@parallel_indices (ix, iy, iz) memopt=true loopsize=3 function d2z3d!(A2, A)
+    if (iz > 1 && iz < size(A2, 3))
+        A2[ix, iy, iz] = A[ix, iy, iz+1] - 2*A[ix, iy, iz] + A[ix, iy, iz-1]
+    end
+    return
+end"""
+
+# reads one element past the end for the last thread (Julia raises a BoundsError)
+SHIFT_OOB = """@parallel_indices (i) function shift!(B, A)
+    B[i] = A[i+1]
+    return
+end"""
+
+# the same kernel compiled without bounds checks is only ever launched over safe ranges
+SHIFT_INBOUNDS = """@parallel_indices (i) inbounds=true function shift_inb!(B, A)
+    B[i] = A[i+1]
+    return
+end"""

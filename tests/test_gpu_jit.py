@@ -1,0 +1,221 @@
+"""GPU parity of run-time compiled kernels (ps_gb300.parallel_kernel: translated to CUDA C and
+compiled by NVRTC for sm_103a inside libps_b200.so) against the known-answer fixtures, the
+library's hand-written kernels and the CPU interpreter oracle/jit_reference.py.
+
+Bit-exact for + - * / comparisons, max/min and Bool*x in FP64 and FP32 (no FMA contraction on
+either side). Kernels that call the math library (exp; pow with a non-literal exponent) are
+compared with a tolerance of 4e-15 (FP64) / 2e-6 (FP32) relative to each value plus the same
+fraction of the largest value: the device's and the host's libm agree to a few ulp, not bit for bit."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import jit_kernels as K
+from conftest import DT
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def jr():
+    from oracle import jit_reference
+
+    return jit_reference
+
+
+def _dev(ps, a):
+    return ps.from_host(np.asfortranarray(a))
+
+
+def _fd_src(stmt):
+    return f"@parallel function fd_case!(R, A)\n    {stmt}\n    return\nend"
+
+
+def test_jit_every_fd_macro_fixture(ps, golden):
+    meta, arr = golden
+    for case in meta["fd"]:
+        Rexp = arr[case["key"] + "_R"]
+        R = ps.zeros(*Rexp.shape, dtype=DT[case["dtype"]])
+        k = ps.parallel_kernel(_fd_src(case["statement"]), ndims=case["ndims"])
+        ps.parallel(k, R, _dev(ps, arr[case["key"] + "_A"]))
+        assert np.array_equal(ps.to_host(R), Rexp), (case["key"], case["statement"])
+
+
+@pytest.mark.parametrize("src", [K.HEAT_FLUX, K.HEAT_LAP], ids=["flux_on_the_fly", "second_differences"])
+def test_jit_diffusion_fixtures(ps, golden, src):
+    meta, arr = golden
+    k = ps.parallel_kernel(src)
+    for case in meta["diffusion"]:
+        T, Ci, T2e = (arr[case["key"] + s] for s in ("_T", "_Ci", "_T2"))
+        T2 = ps.zeros(*T.shape, dtype=T.dtype.type)
+        k(T2, _dev(ps, T), _dev(ps, Ci), 1.0, 1.0, 1.0, 1.0, 1.0)
+        assert np.array_equal(ps.to_host(T2), T2e), case["key"]
+
+
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_jit_diffusion_project(ps, golden, dtn):
+    _, arr = golden
+    p = {k.split("_", 2)[2]: v for k, v in arr.items() if k.startswith(f"project8_{dtn}_")}
+    lam, dt_, dx, dy, dz = (float(v) for v in p["scalars"])
+    T, T2, Ci = _dev(ps, p["T0"]), _dev(ps, p["T0"]), _dev(ps, p["Ci"])
+    k = ps.parallel_kernel(K.HEAT_DIV)
+    for _ in range(3):
+        ps.parallel(k, T2, T, Ci, lam, dt_, dx, dy, dz)
+        T, T2 = T2, T
+    assert np.array_equal(ps.to_host(T), p["T"])
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("src,fixed", [(K.HEAT_FLUX, "diffusion3D_step_flux"), (K.HEAT_LAP, "diffusion3D_step_inv"),
+                                       (K.HEAT_DIV, "diffusion3D_step")])
+def test_jit_equals_hand_written_diffusion(ps, src, fixed, dt):
+    """The compiled body and the library's hand-written kernel for the same body agree bit for bit."""
+    rng = np.random.default_rng(21)
+    n = (37, 33, 29)
+    T, Ci = _dev(ps, rng.random(n).astype(dt)), _dev(ps, (rng.random(n) + 0.5).astype(dt))
+    sc = (0.7, 1e-3, 9.0, 11.0, 13.0)
+    A, B = ps.zeros(*n, dtype=dt), ps.zeros(*n, dtype=dt)
+    ps.parallel(ps.parallel_kernel(src), A, T, Ci, *sc)
+    for memopt in (False, True):
+        ps.fill_(B, 0.0)
+        ps.parallel(getattr(ps.kernels, fixed), B, T, Ci, *sc, memopt=memopt)
+        assert np.array_equal(ps.to_host(A), ps.to_host(B)), (fixed, memopt)
+
+
+def _pos(rng, shape, dt):
+    return (rng.random(shape) + 0.5).astype(dt)
+
+
+def _cases(dt):
+    rng = np.random.default_rng(7)
+    r = lambda *s: rng.standard_normal(s).astype(dt)  # noqa: E731
+    nx, ny, n3 = 21, 17, 12
+    return {
+        "STRESS2D": ([r(nx, ny), r(nx, ny), r(nx - 1, ny - 1), r(nx, ny), r(nx + 1, ny), r(nx, ny + 1),
+                      _pos(rng, (nx, ny), dt), 3.0, 5.0], None),
+        "MOMENTUM2D": ([r(nx - 1, ny - 2), r(nx - 2, ny - 1), r(nx - 1, ny - 2), r(nx - 2, ny - 1), r(nx, ny),
+                        r(nx, ny), r(nx, ny), r(nx - 1, ny - 1), r(nx, ny), 3.0, 5.0, 9.81, 0.9], None),
+        "VELOCITY2D": ([r(nx + 1, ny), r(nx, ny + 1), r(nx - 1, ny - 2), r(nx - 2, ny - 1), _pos(rng, (nx, ny), dt),
+                        r(nx - 2, ny - 2), 0.05], None),
+        "UPWIND2D": ([r(nx, ny), r(nx, ny), r(nx, ny), r(nx, ny), 0.01, 3.0, 5.0], None),
+        "WALLS2D": ([r(nx, ny)], [(1, ny)]),
+        "BLEND3D": ([r(n3 - 2, n3 - 2, n3 - 2), r(n3, n3, n3), r(n3, n3, n3), _pos(rng, (n3, n3, n3), dt), 0.3],
+                    None),
+        "FACES3D": ([r(n3, n3 - 1, n3 + 1), r(n3, n3 - 1, n3 + 1), r(n3, n3 - 1, n3 + 1), 0.25], None),
+        "ROD1D": ([r(29), r(29), 0.2], None),
+        "LINEAR_INDEX": ([np.zeros((4, 5, 6), dt)], None),
+        "D2Z3D": ([r(9, 7, 8), r(9, 7, 8)], None),
+        "COMPACTION": ([_pos(rng, (nx, ny), dt), r(nx, ny), r(nx, ny), 0.8, 3.0, 0.1], None),
+        "BRANCHES2D": ([r(nx, ny), r(nx, ny), 3, 0.5], None),
+    }
+
+
+_NDIMS = {"ROD1D": 1}
+_TOL = {"COMPACTION", "BRANCHES2D"}  # exp / pow
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("name", sorted(_cases(np.float64)))
+def test_jit_kernels_vs_interpreter(ps, jr, name, dt):
+    args, ranges = _cases(dt)[name]
+    src = getattr(K, name)
+    host = [a.copy() if isinstance(a, np.ndarray) else a for a in args]
+    jr.run(src, host, ndims=_NDIMS.get(name), ranges=ranges)
+    dev = [_dev(ps, a) if isinstance(a, np.ndarray) else a for a in args]
+    ps.parallel(ps.parallel_kernel(src, ndims=_NDIMS.get(name)), *dev, ranges=ranges)
+    for i, (h, d) in enumerate(zip(host, dev)):
+        if not isinstance(h, np.ndarray):
+            continue
+        got = ps.to_host(d)
+        assert got.dtype == dt
+        if name in _TOL:
+            rtol = 4e-15 if dt == np.float64 else 2e-6
+            # absolute part: a few ulp of the largest value (results formed by cancellation)
+            np.testing.assert_allclose(got, h, rtol=rtol, atol=rtol * np.abs(h).max(), err_msg=f"{name} arg {i}")
+        else:
+            assert np.array_equal(got, h), (name, i, np.abs(got - h).max())
+    assert any(isinstance(h, np.ndarray) and not np.array_equal(h, a) for h, a in zip(host, args))  # work was done
+
+
+def test_jit_ranges_select_a_box(ps, jr):
+    A = np.zeros((6, 5, 4))
+    jr.run(K.LINEAR_INDEX, [A], ranges=[(2, 4), (1, 3), (2, 2)])
+    D = ps.zeros(6, 5, 4)
+    ps.parallel(ps.parallel_kernel(K.LINEAR_INDEX), D, ranges=[(2, 4), (1, 3), (2, 2)])
+    assert np.array_equal(ps.to_host(D), A)
+    assert np.count_nonzero(A) == 9
+
+
+def test_jit_bounds_error_then_recovery(ps):
+    from ps_gb300._lib import PSError
+
+    n = 50
+    a = np.arange(n, dtype=np.float64)
+    A, B = _dev(ps, a), ps.zeros(n)
+    k = ps.parallel_kernel(K.SHIFT_OOB)
+    with pytest.raises(PSError, match="BoundsError") as e:
+        ps.parallel(k, B, A)
+    assert e.value.status == -1
+    ps.fill_(B, 0.0)
+    ps.parallel(k, B, A, ranges=[(1, n - 1)])  # the flag was cleared; a safe range passes
+    assert np.array_equal(ps.to_host(B)[:n - 1], a[1:])
+    C = ps.zeros(n)
+    ps.parallel(ps.parallel_kernel(K.SHIFT_INBOUNDS), C, A, ranges=[(1, n - 1)])
+    assert np.array_equal(ps.to_host(C), ps.to_host(B))
+
+
+def test_jit_async_on_a_stream(ps):
+    import torch
+
+    rng = np.random.default_rng(3)
+    T = rng.random((40, 30, 20))
+    Ci = rng.random((40, 30, 20)) + 0.5
+    k = ps.parallel_kernel(K.HEAT_LAP)
+    s = torch.cuda.Stream()
+    Td, Cd = _dev(ps, T), _dev(ps, Ci)
+    A, B = ps.zeros(40, 30, 20), ps.zeros(40, 30, 20)
+    ps.synchronize()
+    for _ in range(4):  # ping-pong, queued without synchronisation
+        ps.parallel_async(k, A, Td, Cd, 1.0, 0.01, 2.0, 2.0, 2.0, stream=s)
+        ps.parallel_async(k, B, A, Cd, 1.0, 0.01, 2.0, 2.0, 2.0, stream=s)
+        Td, A, B = B, Td, A
+    ps.synchronize(s)
+    R = _dev(ps, T)
+    X, Y = ps.zeros(40, 30, 20), ps.zeros(40, 30, 20)
+    for _ in range(4):
+        ps.parallel(k, X, R, Cd, 1.0, 0.01, 2.0, 2.0, 2.0)
+        ps.parallel(k, Y, X, Cd, 1.0, 0.01, 2.0, 2.0, 2.0)
+        R, X, Y = Y, R, X
+    assert np.array_equal(ps.to_host(Td), ps.to_host(R))
+
+
+def test_jit_c_abi_direct(ps):
+    """ps_jit_compile / ps_jit_launch with hand-written CUDA C (no translator), and the compile
+    error path through ps_last_error."""
+    from ps_gb300 import _lib
+    from ps_gb300._lib import PSArray
+    from ps_gb300.core import descriptor, stream_handle
+
+    src = b"""
+struct ps_jit_args { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err; };
+extern "C" __global__ void twice(const ps_jit_args g) {
+    long long i = g.lo[0] + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (threadIdx.y == 0 && i < g.lo[0] + g.cnt[0]) ((double*)g.a[0])[i] = g.s[0] * ((const double*)g.a[1])[i];
+}"""
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.ps_jit_compile(src, b"twice", ctypes.byref(h)) == 0
+    x = np.arange(100, dtype=np.float64)
+    X, Y = _dev(ps, x), ps.zeros(100)
+    arrs = (PSArray * 2)(descriptor(Y), descriptor(X))
+    sc = (ctypes.c_double * 1)(2.5)
+    rc = lib.ps_jit_launch(h, arrs, 2, sc, 1, (ctypes.c_int64 * 3)(0, 0, 0), (ctypes.c_int64 * 3)(100, 1, 1),
+                           stream_handle(None), 1)
+    assert rc == 0
+    assert np.array_equal(ps.to_host(Y), 2.5 * x)
+    assert lib.ps_jit_destroy(h) == 0
+    bad = ctypes.c_void_p()
+    assert lib.ps_jit_compile(b"extern \"C\" __global__ void k() { undeclared = 1; }", b"k", ctypes.byref(bad)) == -1
+    assert "undeclared" in _lib.last_error()
+    assert not bad.value

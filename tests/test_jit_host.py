@@ -1,0 +1,213 @@
+"""Run-time compiled kernels, host side (no GPU): the CPU interpreter that checks them is pinned
+against the known-answer fixtures, and the translator's parsing, argument rules, error messages and
+generated CUDA C are checked without launching anything."""
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import jit_kernels as K
+from conftest import DT
+
+REFERENCE = "/root/reference"  # read only when present (this container), to translate its miniapps
+
+
+@pytest.fixture(scope="module")
+def jr():
+    from oracle import jit_reference
+
+    return jit_reference
+
+
+@pytest.fixture(scope="module")
+def jit():
+    from ps_gb300 import jit
+
+    return jit
+
+
+def _fd_src(stmt):
+    return f"@parallel function fd_case!(R, A)\n    {stmt}\n    return\nend"
+
+
+# ---------------------------------------------------------------- the interpreter, pinned
+def test_interpreter_matches_every_fd_macro_fixture(jr, golden):
+    meta, arr = golden
+    assert len(meta["fd"]) > 150
+    for case in meta["fd"]:
+        Rexp = arr[case["key"] + "_R"]
+        R = np.zeros(Rexp.shape, dtype=Rexp.dtype)
+        jr.run(_fd_src(case["statement"]), [R, arr[case["key"] + "_A"].copy()], ndims=case["ndims"])
+        assert np.array_equal(R, Rexp), (case["key"], case["statement"])
+
+
+@pytest.mark.parametrize("src", [K.HEAT_FLUX, K.HEAT_LAP], ids=["flux_on_the_fly", "second_differences"])
+def test_interpreter_matches_diffusion_fixtures(jr, golden, src):
+    meta, arr = golden
+    for case in meta["diffusion"]:
+        T, Ci, T2e = (arr[case["key"] + s] for s in ("_T", "_Ci", "_T2"))
+        T2 = np.zeros_like(T)
+        jr.run(src, [T2, T.copy(), Ci.copy(), 1.0, 1.0, 1.0, 1.0, 1.0])
+        assert np.array_equal(T2, T2e), case["key"]
+        assert T2.dtype == DT[case["dtype"]]
+
+
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_interpreter_matches_diffusion_project(jr, golden, dtn):
+    _, arr = golden
+    p = {k.split("_", 2)[2]: v for k, v in arr.items() if k.startswith(f"project8_{dtn}_")}
+    lam, dt_, dx, dy, dz = (float(v) for v in p["scalars"])
+    T, T2 = p["T0"].copy(), p["T0"].copy()
+    for _ in range(3):
+        jr.run(K.HEAT_DIV, [T2, T, p["Ci"].copy(), lam, dt_, dx, dy, dz])
+        T, T2 = T2, T
+    assert np.array_equal(T, p["T"])
+
+
+def test_interpreter_explicit_indices_against_broadcasting(jr):
+    """Upwind advection and wall copies restated with numpy slicing."""
+    rng = np.random.default_rng(11)
+    nx, ny = 13, 9
+    T, u, w = rng.random((nx, ny)), rng.standard_normal((nx, ny)), rng.standard_normal((nx, ny))
+    Tn = np.full((nx, ny), -1.0)
+    dt, rdx, rdy = 0.1, 3.0, 2.5
+    jr.run(K.UPWIND2D, [Tn, T, u, w, dt, rdx, rdy])
+    c = (slice(1, -1), slice(1, -1))
+    Tc, uc, wc = T[c], u[c], w[c]
+    exp = Tc - dt * (np.where(uc > 0, uc, np.copysign(0.0, uc)) * (Tc - T[:-2, 1:-1]) * rdx
+                     + np.where(uc < 0, uc, np.copysign(0.0, uc)) * (T[2:, 1:-1] - Tc) * rdx
+                     + np.where(wc > 0, wc, np.copysign(0.0, wc)) * (Tc - T[1:-1, :-2]) * rdy
+                     + np.where(wc < 0, wc, np.copysign(0.0, wc)) * (T[1:-1, 2:] - Tc) * rdy)
+    assert np.array_equal(Tn[c], exp)
+    assert np.all(Tn[0] == -1.0) and np.all(Tn[:, -1] == -1.0)
+    W = rng.random((nx, ny))
+    W0 = W.copy()
+    jr.run(K.WALLS2D, [W], ranges=[(1, ny)])
+    assert np.array_equal(W[0], W0[1]) and np.array_equal(W[-1], W0[-2]) and np.array_equal(W[1:-1], W0[1:-1])
+
+
+def test_interpreter_julia_number_rules(jr):
+    """max/min propagate NaN and order signed zeros; Bool * x keeps the sign of zero; x^2 is x*x."""
+    A = np.array([[np.nan, -0.0, 0.0, 2.0]]).T.copy()
+    B = np.zeros_like(A)
+    src = """@parallel_indices (i, j) function rules!(B, A)
+        B[i, j] = max(A[i, j], 0.0) + (A[i, j] > 1)*(-0.0) + min(-0.0, 0.0)^2
+        return
+    end"""
+    jr.run(src, [B, A])
+    assert np.isnan(B[0, 0])
+    assert B[1, 0] == 0.0 and not np.signbit(B[1, 0])
+    assert B[3, 0] == 2.0
+
+
+def test_interpreter_bounds_error(jr):
+    A, B = np.arange(6.0), np.zeros(6)
+    with pytest.raises(IndexError, match="BoundsError"):
+        jr.run(K.SHIFT_OOB, [B, A])
+    B[:] = 0
+    jr.run(K.SHIFT_OOB, [B, A], ranges=[(1, 5)])
+    assert np.array_equal(B[:5], A[1:])
+
+
+def test_interpreter_linear_index_and_elseif(jr):
+    A = np.zeros((4, 5, 6))
+    jr.run(K.LINEAR_INDEX, [A])
+    ix, iy, iz = np.meshgrid(np.arange(1, 5), np.arange(1, 6), np.arange(1, 7), indexing="ij")
+    assert np.array_equal(A, ix + (iy - 1) * 4 + (iz - 1) * 20)
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((7, 6))
+    Y = np.zeros_like(X)
+    jr.run(K.BRANCHES2D, [Y, X, 3, 0.5])
+    i, j = np.meshgrid(np.arange(1, 8), np.arange(1, 7), indexing="ij")
+    exp = np.where(X > 0.5, np.maximum(X, 0.5) - (np.abs(X) * np.abs(X)) * np.abs(X),
+                   np.where(X < -0.5, np.minimum(X, -0.5) + (i > j),
+                            np.sqrt(np.abs(X)) * ((j == 1) | (i == 7))))
+    assert np.allclose(Y, exp, rtol=1e-15, atol=0)
+
+
+# ---------------------------------------------------------------- the translator
+def test_translator_argument_kinds(jit):
+    kd = jit.parse(K.HEAT_LAP)  # untyped arguments follow their use
+    assert kd.arrays == ["Tnew", "Told", "Cinv"] and kd.scalars == ["_u03bb_", "_u0394_t", "rdx", "rdy", "rdz"]
+    kd = jit.parse(K.BRANCHES2D)
+    assert kd.arrays == ["B", "A"] and kd.scalars == ["c", "t"] and kd.int_scalars == {"c"}
+    assert kd.kind == "parallel_indices" and kd.index_names == ["ix", "iy"] and kd.options == {"inbounds": "false"}
+    kd = jit.parse(K.D2Z3D)
+    assert kd.options == {"memopt": "true", "loopsize": "3"}
+    kd = jit.parse("@parallel function f!(A::Data.Array, B::Data.Array, c::T) where T <: Integer\n"
+                   "    @all(A) = @all(B)^c\n    return\nend")
+    assert kd.arrays == ["A", "B"] and kd.scalars == ["c"]
+
+
+@pytest.mark.parametrize("src,msg", [
+    ("@parallel function f!(A, B)\n @inn(t) = @all(B)\n @all(A) = @all(t)\n return\nend", "use '@all' instead"),
+    ("@parallel function f!(A, B)\n @all(t) = @all(t) + @all(B)\n @all(A) = @all(t)\n return\nend", "auto-dependency"),
+    ("@parallel function f!(A, B)\n @all(t) = @all(A)\n @all(A) = @all(t) + @all(B)\n return\nend", "not read-only"),
+    ("@parallel function f!(A, B)\n @all(A) = @d_qa(B)\n return\nend", "unknown macro"),
+    ("@parallel padding=true function f!(A, B)\n @all(A) = @all(B)\n return\nend", "padding"),
+    ("@parallel fancy=1 function f!(A, B)\n @all(A) = @all(B)\n return\nend", "unsupported keyword"),
+    ("@parallel function f!(A, s::Data.Number)\n @all(A) = @all(s)\n return\nend", "used as an array"),
+    ("@parallel_indices (i, j, k, l) function f!(A)\n A[i] = 1.0\n return\nend", "1-3 index"),
+])
+def test_translator_rejects(jit, src, msg):
+    from ps_gb300.core import ArgumentError
+
+    with pytest.raises(ArgumentError, match=re.escape(msg)):
+        jit.generate(jit.parse(src), 3 if "d_qa" not in src else 2, "double")
+
+
+def test_translator_generated_structure(jit):
+    src = jit.generate(jit.parse(K.HEAT_FLUX), 3, "double")
+    assert "extern \"C\" __global__ void ps_jit_entry(const ps_jit_args g)" in src
+    assert "fx" not in src.split("ps_jit_entry")[1]  # the on-the-fly arrays are inlined
+    assert src.count("jl_ld(") > 10  # bounds-checked reads by default
+    assert "tx < n0_0 - 2 && ty < n0_1 - 2 && tz < n0_2 - 2" in src  # @within("@inn", Tnew)
+    src = jit.generate(jit.parse(K.SHIFT_INBOUNDS), 1, "float")
+    assert "typedef float R;" in src and "jl_ld(a" not in src and "jl_st(a" not in src
+    src = jit.generate(jit.parse(K.BRANCHES2D), 2, "double")
+    assert "const long long s0 = (long long)g.s[0];" in src and "pow(" in src
+
+
+def _nvcc():
+    return shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
+
+
+@pytest.mark.skipif(_nvcc() is None, reason="nvcc not available")
+def test_generated_sources_compile_for_sm103a(jit, tmp_path):
+    """Every test kernel, FP64 and FP32, compiles as CUDA C for sm_103a (the same options NVRTC gets)."""
+    srcs = [(n, getattr(K, n)) for n in dir(K) if n.isupper()]
+    nd = {"ROD1D": 1, "SHIFT_OOB": 1, "SHIFT_INBOUNDS": 1, "WALLS2D": 2}
+    procs = []
+    for name, src in srcs:
+        ndims = nd.get(name, 2 if "2D" in name else 3)
+        for real in ("double", "float"):
+            f = tmp_path / f"{name}_{real}.cu"
+            f.write_text(jit.generate(jit.parse(src), ndims, real))
+            procs.append((f, subprocess.Popen([_nvcc(), "-arch=sm_103a", "-std=c++17", "--fmad=false", "-c", str(f),
+                                               "-o", str(f) + ".o"], stdout=subprocess.PIPE,
+                                              stderr=subprocess.STDOUT, text=True)))
+            if len(procs) % 8 == 0:
+                for _, p in procs[-8:]:
+                    p.wait()
+    for f, p in procs:
+        out = p.communicate()[0]
+        assert p.returncode == 0, (f.name, out[-2000:])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "miniapps")), reason="reference sources absent")
+def test_reference_miniapp_kernels_translate(jit):
+    """Every @parallel / @parallel_indices definition of the reference's miniapps translates."""
+    n = 0
+    for fn in sorted(os.listdir(os.path.join(REFERENCE, "miniapps"))):
+        if not fn.endswith(".jl"):
+            continue
+        with open(os.path.join(REFERENCE, "miniapps", fn), encoding="utf-8") as fh:
+            text = fh.read()
+        ndims = 3 if "3D" in fn else 2
+        for d in re.findall(r"^(@parallel(?:_indices)?[^\n]*function.*?^end)", text, re.S | re.M):
+            assert "ps_jit_entry" in jit.generate(jit.parse(d), ndims, "double"), (fn, d[:60])
+            n += 1
+    assert n >= 40
