@@ -33,6 +33,15 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 WORDS_FLUX_LAM = 4  # T read, T2 write, lam read, Ci read
+# the headline body as a run-time compiled kernel (ps_gb300.parallel_kernel), bounds-checked and not
+JIT_FLUX_LAM = """@parallel {opt}function diffusion3D_step!(T2, T, Ci, lam, dt, _dx, _dy, _dz)
+    @all(qx)   = -@av_xi(lam)*@d_xi(T)*_dx
+    @all(qy)   = -@av_yi(lam)*@d_yi(T)*_dy
+    @all(qz)   = -@av_zi(lam)*@d_zi(T)*_dz
+    @all(dTdt) = @inn(Ci)*(-@d_xa(qx)*_dx - @d_ya(qy)*_dy - @d_za(qz)*_dz)
+    @inn(T2)   = @inn(T) + dt*@all(dTdt)
+    return
+end"""
 WORDS_README = 3  # T read, T2 write, Ci read
 WORDS_MEMCOPY = 3
 NT_JOB = 50  # time steps of one diffusion job (the e2e unit)
@@ -202,7 +211,7 @@ def run_ours(a, world, rank, local):
             src, dst = bufs[i % 2], bufs[(i + 1) % 2]
             if kernel is ps.kernels.copy3D:
                 ps.parallel(kernel, dst, src, Ci, memopt=memopt, sync=False)
-            elif kernel is ps.kernels.diffusion3D_step_flux_lam:
+            elif kernel is ps.kernels.diffusion3D_step_flux_lam or hasattr(kernel, "jit_launch"):
                 ps.parallel(kernel, dst, src, Ci, lam, *scalars, memopt=memopt, sync=False, fp64=fp64)
             else:
                 ps.parallel(kernel, dst, src, Ci, 1.0, *scalars, memopt=memopt, sync=False, fp64=fp64)
@@ -292,6 +301,9 @@ def run_ours(a, world, rank, local):
             bench_kernel("diffusion3d_readme_f64_ieee_memopt", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx),
                          True, WORDS_README, n, np.float64, ieee_steps)
             bench_kernel("memcopy3d_f64", ps.kernels.copy3D, arrs64, (), False, WORDS_MEMCOPY, n, np.float64, a.steps)
+            for opt, tag in (("", "jit"), ("inbounds=true ", "jit_inbounds")):  # run-time compiled, IEEE FP64
+                bench_kernel(f"diffusion3d_flux_lam_f64_{tag}", ps.parallel_kernel(JIT_FLUX_LAM.format(opt=opt)),
+                             arrs64, (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
         # e2e: one diffusion job (NT_JOB steps) through the C ABI from pinned host buffers:
         # H2D of T, Ci, lam; NT_JOB steps; D2H of T -- all inside the timed region.
         lib = _lib.load()

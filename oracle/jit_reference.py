@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import math
 import re
+import threading
 
 import numpy as np
 
@@ -33,10 +34,12 @@ __all__ = ["parse", "run", "OracleKernel"]
 # ---------------------------------------------------------------- tokens
 _TOKEN = re.compile(r"""
     (?P<nl>\n) | (?P<ws>[ \t\r]+) | (?P<com>\#[^\n]*) |
+    (?P<hex>0x[0-9a-fA-F]+) |
     (?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eE][+-]?\d+)?(?:f0)?) |
     (?P<mac>@[A-Za-z_][A-Za-z0-9_]*) |
+    (?P<uop>÷|∈) |
     (?P<id>(?:[A-Za-z_]|[^\x00-\x7f])(?:[A-Za-z0-9_!]|[^\x00-\x7f])*) |
-    (?P<op>==|!=|<=|>=|&&|\|\||::|[-+*/^<>=!(),;\[\]?:.{}$])
+    (?P<op>==|!=|<=|>=|&&|\|\||::|[-+*/^<>=!(),;\[\]?:.{}$%])
 """, re.X)
 
 
@@ -47,6 +50,10 @@ def _tokens(text):
         kind, val = m.lastgroup, m.group()
         if kind in ("ws", "com") or val == "$":
             continue
+        if kind == "hex":
+            kind, val = "num", str(int(val, 16))
+        if kind == "uop":
+            kind = "op"
         if kind == "id" and val.endswith("!") and m.end() < len(text) and text[m.end()] == "=":
             # `a!=b`: the identifier does not own the `!`
             val = val[:-1]
@@ -109,14 +116,34 @@ class _P:
         tok = self.peek()
         if tok == ("id", "return"):
             self.next()
-            if self.peek()[0] not in ("nl", "eof") and self.peek()[1] != "end":
+            if self.peek()[0] not in ("nl", "eof") and self.peek()[1] not in ("end", "else", "elseif"):
                 self.expr()
-            return None
+            return ("return",)
         if tok == ("id", "if"):
             return self.if_stmt()
+        if tok == ("id", "for"):
+            self.next()
+            var = self.next()[1]
+            if self.next()[1] not in ("=", "in", "∈"):
+                raise SyntaxError("for v = a:b")
+            parts = [self.expr()]
+            while self.peek()[1] == ":":
+                self.next()
+                parts.append(self.expr())
+            body = self.block(("end",))
+            self.expect("end")
+            return ("for", var, parts, body)
+        if tok == ("id", "while"):
+            self.next()
+            cond = self.expr()
+            body = self.block(("end",))
+            self.expect("end")
+            return ("while", cond, body)
         lhs = self.expr()
+        if self.peek()[1] != "=" and lhs[0] == "mcall":
+            return ("do", lhs)  # @sync_threads()
         if self.peek()[1] != "=":
-            raise SyntaxError("kernel statements are assignments or if-blocks")
+            raise SyntaxError("kernel statements are assignments, if-blocks, loops or @sync_threads()")
         self.next()
         self.skip_nl()
         return ("assign", lhs, self.expr())
@@ -180,7 +207,7 @@ class _P:
 
     def term(self):
         a = self.unary()
-        while self.peek()[1] in ("*", "/"):
+        while self.peek()[1] in ("*", "/", "÷", "%"):
             op = self.next()[1]
             self.skip_nl()
             a = ("bin", op, a, self.unary())
@@ -209,13 +236,30 @@ class _P:
             return ("num", int(v), False)
         if tok[0] == "mac":
             self.expect("(")
-            name = self.next()
-            if name[0] != "id":
-                raise SyntaxError("a macro takes an array name")
+            args = []
+            while self.peek()[1] != ")":
+                args.append(self.expr())
+                if self.peek()[1] == ",":
+                    self.next()
             self.expect(")")
-            return ("macro", tok[1][1:], name[1])
+            if len(args) == 1 and args[0][0] == "name" and tok[1][1:] not in _KL:
+                return ("macro", tok[1][1:], args[0][1])  # FiniteDifferences macro on an array
+            node = ("mcall", tok[1][1:], args)
+            if self.peek()[1] == ".":  # @threadIdx().x
+                self.next()
+                node = ("attr", node, self.next()[1])
+            return node
         if tok[1] == "(":
             e = self.expr()
+            if self.peek()[1] == ",":  # a tuple (dims of @sharedMem)
+                items = [e]
+                while self.peek()[1] == ",":
+                    self.next()
+                    if self.peek()[1] == ")":
+                        break
+                    items.append(self.expr())
+                self.expect(")")
+                return ("tuple", items)
             self.expect(")")
             return e
         if tok[0] == "id":
@@ -241,6 +285,14 @@ class _P:
                 return ("bool", tok[1] == "true")
             return ("name", tok[1])
         raise SyntaxError(f"unexpected token {tok[1]!r}")
+
+
+# kernel-language macros (src/ParallelKernel/kernel_language.jl)
+_KL = {"threadIdx", "blockIdx", "blockDim", "gridDim", "sync_threads", "sharedMem", "warpsize", "laneid",
+       "active_mask", "shfl_sync", "shfl_up_sync", "shfl_down_sync", "shfl_xor_sync", "vote_any_sync",
+       "vote_all_sync", "vote_ballot_sync"}
+_COLL = {"sync_threads", "shfl_sync", "shfl_up_sync", "shfl_down_sync", "shfl_xor_sync", "vote_any_sync",
+         "vote_all_sync", "vote_ballot_sync"}
 
 
 class OracleKernel:
@@ -331,21 +383,68 @@ _FUN = {"exp": (math.exp, np.exp), "log": (math.log, np.log), "sqrt": (math.sqrt
         "log10": (math.log10, np.log10), "exp2": (lambda v: 2.0 ** v, np.exp2), "cbrt": (np.cbrt, np.cbrt)}
 
 
+class _Return(Exception):
+    """`return` inside a kernel: the thread is done."""
+
+
+class _Block:
+    """One thread block: indices, dynamic shared memory (zero-filled bytes) and, for kernels with
+    barriers, shuffles or votes, the synchronisation of its threads (each thread a Python thread)."""
+
+    def __init__(self, bidx, bdim, gdim, shmem, threaded):
+        self.bidx, self.bdim, self.gdim = bidx, bdim, gdim
+        self.buf = bytearray(int(shmem))
+        self.views = {}
+        nthr = bdim[0] * bdim[1] * bdim[2]
+        self.bar = threading.Barrier(nthr, timeout=60) if threaded else None
+        nw = (nthr + 31) // 32
+        self.warp_bars = [threading.Barrier(min(32, nthr - 32 * w), timeout=60) for w in range(nw)] if threaded else []
+        self.slots = [[None] * 32 for _ in range(nw)]
+
+    def shared(self, R, dims, offset):
+        key = (tuple(dims), offset)
+        if key not in self.views:
+            dt = np.dtype(np.float32 if R is np.float32 else np.float64)
+            need = offset + int(np.prod(dims)) * dt.itemsize
+            if offset < 0 or need > len(self.buf):
+                raise IndexError(f"BoundsError: @sharedMem{tuple(dims)} at offset {offset} exceeds shmem "
+                                 f"{len(self.buf)}")
+            self.views[key] = np.ndarray(tuple(dims), dtype=dt, buffer=self.buf, offset=offset, order="F")
+        return self.views[key]
+
+    def exchange(self, warp, lane, val):
+        """Every lane of the warp deposits its value; all lanes see all values."""
+        self.slots[warp][lane] = val
+        self.warp_bars[warp].wait()
+        snap = list(self.slots[warp])
+        self.warp_bars[warp].wait()
+        return snap
+
+
 class _Thread:
-    def __init__(self, k, arrays, scalars, temps, R, nd):
+    def __init__(self, k, arrays, scalars, temps, R, nd, blk=None, tid=(0, 0, 0)):
         self.k, self.A, self.S, self.temps, self.R, self.nd = k, arrays, scalars, temps, R, nd
+        self.blk, self.tid, self.loc = blk, tid, {}
+        if blk is not None:
+            lin = tid[0] + blk.bdim[0] * (tid[1] + blk.bdim[1] * tid[2])
+            self.warp, self.lane = divmod(lin, 32)
 
     def real(self, v):
         return self.R(v) if isinstance(v, (int, bool, float)) and not isinstance(v, self.R) else v
+
+    def array(self, name):
+        if name in self.loc and isinstance(self.loc[name], np.ndarray):
+            return self.loc[name]
+        return self.A[name]
 
     def load(self, name, idx, depth=0):
         """Array `name` at 1-based index tuple idx."""
         if name in self.temps:  # on-the-fly: its expression at this index
             return self.ev(self.temps[name], tuple(idx) + (1,) * (3 - len(idx)), depth + 1)
-        a = self.A[name]
+        a = self.array(name)
         idx = list(idx) + [1] * (a.ndim - len(idx))
         if len(idx) > a.ndim and any(i != 1 for i in idx[a.ndim:]):
-            raise IndexError(f"{name}{tuple(idx)}")
+            raise IndexError(f"BoundsError: {name}{tuple(idx)}")
         for d in range(a.ndim):
             if not 1 <= idx[d] <= a.shape[d]:
                 raise IndexError(f"BoundsError: {name}{tuple(idx)} outside {a.shape}")
@@ -385,6 +484,50 @@ class _Thread:
             return m
         raise KeyError(mname)
 
+    def kernel_language(self, name, args, I, depth):
+        """src/ParallelKernel/kernel_language.jl: 1-based thread/block indices, warps of 32 lanes."""
+        E = lambda x: self.ev(x, I, depth)  # noqa: E731
+        b = self.blk
+        if name == "sharedMem":
+            dims = E(args[1])
+            dims = list(dims) if isinstance(dims, list) else [dims]
+            off = int(E(args[2])) if len(args) > 2 else 0
+            return b.shared(self.R, [int(x) for x in dims], off)
+        if name == "warpsize":
+            return 32
+        if name == "laneid":
+            return self.lane + 1
+        if name == "active_mask":
+            return 0xFFFFFFFF
+        if name.startswith("vote"):
+            pred = bool(E(args[1]))
+            snap = b.exchange(self.warp, self.lane, pred)
+            mask = int(E(args[0]))
+            lanes = [i for i in range(32) if (mask >> i) & 1 and snap[i] is not None]
+            if name == "vote_any_sync":
+                return any(snap[i] for i in lanes)
+            if name == "vote_all_sync":
+                return all(snap[i] for i in lanes)
+            return sum(1 << i for i in lanes if snap[i])
+        if name.startswith("shfl"):
+            val = E(args[1])
+            x = int(E(args[2]))
+            w = int(E(args[3])) if len(args) > 3 else 32
+            snap = b.exchange(self.warp, self.lane, val)
+            lane, base = self.lane, self.lane - self.lane % w
+            if name == "shfl_sync":
+                src = base + (x - 1) % w
+            elif name == "shfl_up_sync":
+                src = lane - x if lane % w >= x else lane
+            elif name == "shfl_down_sync":
+                src = lane + x if lane % w + x < w else lane
+            else:  # xor: a partner outside the lane's partition returns the lane's own value
+                src = lane ^ x
+                src = src if src // w == lane // w else lane
+            v = snap[src] if src < 32 and snap[src] is not None else val
+            return v
+        raise NameError(name)
+
     def ev(self, e, I, depth=0):
         if depth > 64:
             raise RecursionError("on-the-fly arrays nested too deeply")
@@ -394,8 +537,12 @@ class _Thread:
             return R(e[1]) if e[2] else e[1]
         if op == "bool":
             return e[1]
+        if op == "tuple":
+            return [E(x) for x in e[1]]
         if op == "name":
             n = e[1]
+            if n in self.loc:
+                return self.loc[n]
             if n in self.S:
                 return self.S[n]
             if self.k.kind == "parallel_indices" and n in self.k.indices:
@@ -412,16 +559,25 @@ class _Thread:
             sym = e[1]
             if sym == "*" and (isinstance(a, bool) or isinstance(b, bool)):
                 flag, x = (a, b) if isinstance(a, bool) else (b, a)
+                if isinstance(x, int) and not isinstance(x, bool):
+                    return x if flag else 0
                 x = self.real(x)
                 return x if flag else R(math.copysign(0.0, float(x)))
             if isinstance(a, int) and isinstance(b, int) and sym != "/":
+                if sym in ("÷", "%"):  # truncating, like Julia's div and rem
+                    q = abs(a) // abs(b) * (1 if (a >= 0) == (b >= 0) else -1)
+                    return q if sym == "÷" else a - b * q
                 return a + b if sym == "+" else a - b if sym == "-" else a * b
             a, b = self.real(a), self.real(b)
+            if sym == "%":
+                return R(math.fmod(float(a), float(b)))
+            if sym == "÷":
+                return R(math.trunc(a / b))
             return a + b if sym == "+" else a - b if sym == "-" else a * b if sym == "*" else a / b
         if op == "pow":
             x, n = E(e[1]), e[2]
             if n[0] == "num" and not n[2] and n[1] in (2, 3):
-                x = self.real(x)
+                x = self.real(x) if not isinstance(x, int) else x
                 return x * x if n[1] == 2 else (x * x) * x
             x, p = self.real(x), self.real(E(n))
             return R(float(x) ** float(p))
@@ -440,24 +596,38 @@ class _Thread:
             return E(e[2]) if E(e[1]) else E(e[3])
         if op == "macro":
             return self.macro(e[1], e[2], I, depth)
+        if op == "mcall":
+            return self.kernel_language(e[1], e[2], I, depth)
+        if op == "attr":
+            name, field = e[1][1], e[2]
+            d = "xyz".index(field)
+            b = self.blk
+            return {"threadIdx": self.tid[d] + 1, "blockIdx": b.bidx[d] + 1, "blockDim": b.bdim[d],
+                    "gridDim": b.gdim[d]}[name]
         if op == "index":
-            shape = self.A[e[1]].shape + (1, 1)
+            shape = self.array(e[1]).shape + (1, 1)
             idx = [int(self.ev(_subst_end(x, shape[d]), I, depth)) for d, x in enumerate(e[2])]
             return self.load(e[1], idx, depth)
         if op == "call":
             f, args = e[1], e[2]
             if f == "size":
-                a = self.A[args[0][1]]
+                a = self.array(args[0][1])
                 d = E(args[1])
                 return a.shape[d - 1] if d <= a.ndim else 1
+            if f == "eltype":
+                return R
             if f in ("max", "min"):
+                vals = [E(x) for x in args]
+                if all(isinstance(v, int) and not isinstance(v, bool) for v in vals):
+                    return max(vals) if f == "max" else min(vals)
                 g = _jl_max if f == "max" else _jl_min
-                r = self.real(E(args[0]))
-                for x in args[1:]:
-                    r = g(r, self.real(E(x)))
+                r = self.real(vals[0])
+                for x in vals[1:]:
+                    r = g(r, self.real(x))
                 return r
             if f == "abs":
-                return abs(self.real(E(args[0])))
+                v = E(args[0])
+                return abs(v) if isinstance(v, int) else abs(self.real(v))
             if f == "inv":
                 return R(1.0) / self.real(E(args[0]))
             if f in ("one", "zero"):
@@ -472,11 +642,36 @@ class _Thread:
 
     def run(self, stmts, I):
         for s in stmts:
+            if s[0] == "return":
+                raise _Return()
             if s[0] == "if":
                 self.run(s[2] if self.ev(s[1], I) else s[3], I)
                 continue
+            if s[0] == "for":
+                _, var, parts, body = s
+                a, b = int(self.ev(parts[0], I)), int(self.ev(parts[-1], I))
+                st = int(self.ev(parts[1], I)) if len(parts) == 3 else 1
+                v = a
+                while (v <= b) if st > 0 else (v >= b):
+                    self.loc[var] = v
+                    self.run(body, I)
+                    v += st
+                continue
+            if s[0] == "while":
+                while self.ev(s[1], I):
+                    self.run(s[2], I)
+                continue
+            if s[0] == "do":
+                if s[1][1] != "sync_threads":
+                    raise SyntaxError(f"unsupported statement @{s[1][1]}")
+                self.blk.bar.wait()
+                continue
             _, lhs, rhs = s
-            if lhs[0] == "macro":
+            if lhs[0] == "name":  # local variable (a @sharedMem array or a number)
+                v = self.ev(rhs, I)
+                self.loc[lhs[1]] = v if isinstance(v, (np.ndarray, int)) and not isinstance(v, bool) \
+                    else self.real(v)
+            elif lhs[0] == "macro":
                 sel, name = lhs[1], lhs[2]
                 if name in self.temps:
                     continue
@@ -489,7 +684,7 @@ class _Thread:
                 idx = tuple(I[d] - 1 + (1 if d in inner else 0) for d in range(a.ndim))
                 a[idx] = v
             elif lhs[0] == "index":
-                a = self.A[lhs[1]]
+                a = self.array(lhs[1])
                 shape = a.shape + (1, 1)
                 idx = [int(self.ev(_subst_end(x, shape[d]), I)) for d, x in enumerate(lhs[2])]
                 v = self.real(self.ev(rhs, I))
@@ -510,9 +705,21 @@ def _subst_end(e, n):
     return e
 
 
-def run(src, args, ndims=None, ranges=None):
+def _uses(node, names):
+    if isinstance(node, tuple):
+        if node and node[0] == "mcall" and node[1] in names:
+            return True
+        return any(_uses(x, names) for x in node)
+    if isinstance(node, list):
+        return any(_uses(x, names) for x in node)
+    return False
+
+
+def run(src, args, ndims=None, ranges=None, nthreads=None, nblocks=None, shmem=0):
     """Run kernel `src` on numpy arrays / scalars `args` (arrays are modified in place, like the
-    device kernel). ranges: 1-based inclusive (start, stop) per dimension; default 1..max extent."""
+    device kernel). ranges: 1-based inclusive (start, stop) per dimension (dimensions not given
+    have one index); default 1..max extent, or nblocks .* nthreads. nthreads (default (32, 8, 1))
+    and shmem only matter for kernels that use the kernel language."""
     k = parse(src)
     if len(args) != len(k.argnames):
         raise TypeError("argument count")
@@ -531,13 +738,71 @@ def run(src, args, ndims=None, ranges=None):
             if s[1][1] != "all":
                 raise ValueError("on-the-fly arrays take @all")
             temps[s[1][2]] = s[2]
+    bdim = list(nthreads) + [1] * (3 - len(nthreads)) if nthreads else [32, 8, 1]
     ext = [max((a.shape[d] if d < a.ndim else 1) for a in arrays.values()) for d in range(3)]
-    lo, hi = [1, 1, 1], [ext[0] if nd >= 1 else 1, ext[1] if nd >= 2 else 1, ext[2] if nd >= 3 else 1]
+    lo, cnt = [1, 1, 1], [ext[0] if nd >= 1 else 1, ext[1] if nd >= 2 else 1, ext[2] if nd >= 3 else 1]
+    if nblocks is not None:
+        nb = list(nblocks) + [1] * (3 - len(nblocks))
+        cnt = [nb[d] * bdim[d] for d in range(3)]
     if ranges is not None:
+        lo, cnt = [1, 1, 1], [1, 1, 1]
         for d, r in enumerate(ranges):
-            lo[d], hi[d] = r
-    t = _Thread(k, arrays, scalars, temps, R, nd)
-    for iz in range(lo[2], hi[2] + 1):
-        for iy in range(lo[1], hi[1] + 1):
-            for ix in range(lo[0], hi[0] + 1):
-                t.run(k.body, (ix, iy, iz))
+            lo[d], cnt[d] = r[0], r[1] - r[0] + 1
+    threaded = _uses(k.body, _COLL) or any(s[0] == "do" for s in _walk_stmts(k.body))
+    if threaded and any(cnt[d] % bdim[d] for d in range(3)):
+        raise ValueError("a kernel with @sync_threads, shuffles or votes needs ranges that are a multiple of the "
+                         "thread block")
+    gdim = [-(-cnt[d] // bdim[d]) for d in range(3)]
+    for bz in range(gdim[2]):
+        for by in range(gdim[1]):
+            for bx in range(gdim[0]):
+                blk = _Block((bx, by, bz), bdim, gdim, shmem, threaded)
+                members = []
+                for tz in range(bdim[2]):
+                    for ty in range(bdim[1]):
+                        for tx in range(bdim[0]):
+                            u = (bx * bdim[0] + tx, by * bdim[1] + ty, bz * bdim[2] + tz)
+                            if any(u[d] >= cnt[d] for d in range(3)):
+                                continue
+                            I = tuple(lo[d] + u[d] for d in range(3))
+                            members.append((_Thread(k, arrays, scalars, temps, R, nd, blk, (tx, ty, tz)), I))
+                if not threaded:
+                    for t, I in members:
+                        try:
+                            t.run(k.body, I)
+                        except _Return:
+                            pass
+                    continue
+                errors = []
+
+                def work(t, I):
+                    try:
+                        t.run(k.body, I)
+                    except _Return:
+                        pass
+                    except BaseException as ex:  # a failing thread releases the others
+                        errors.append(ex)
+                        blk.bar.abort()
+                        for wb in blk.warp_bars:
+                            wb.abort()
+
+                ths = [threading.Thread(target=work, args=m) for m in members]
+                for th in ths:
+                    th.start()
+                for th in ths:
+                    th.join()
+                if errors:
+                    real = [x for x in errors if not isinstance(x, threading.BrokenBarrierError)]
+                    raise (real or errors)[0]
+
+
+def _walk_stmts(stmts):
+    for s in stmts:
+        yield s
+        if s[0] == "if" and len(s) == 4:
+            yield from _walk_stmts(s[2])
+            yield from _walk_stmts(s[3])
+        elif s[0] == "for":
+            yield from _walk_stmts(s[3])
+        elif s[0] == "while":
+            yield from _walk_stmts(s[2])

@@ -31,7 +31,8 @@ struct ps_jit_args {
     double s[kJitMaxScalars];
     long long lo[3];   // first thread index (0-based) per dimension
     long long cnt[3];  // threads per dimension
-    int* err;          // out-of-bounds flag of the kernel (device memory, one int)
+    int* err;          // error flags of the kernel (device memory, one int): 1 out of bounds, 2 partial block
+    long long smem;    // dynamic shared memory bytes of this launch (@sharedMem views are checked against it)
 };
 
 typedef CUresult (*ModuleLoadDataFn)(CUmodule*, const void*);
@@ -39,10 +40,12 @@ typedef CUresult (*ModuleGetFunctionFn)(CUfunction*, CUmodule, const char*);
 typedef CUresult (*ModuleUnloadFn)(CUmodule);
 typedef CUresult (*LaunchKernelFn)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
                                    CUstream, void**, void**);
+typedef CUresult (*FuncSetAttributeFn)(CUfunction, CUfunction_attribute, int);
 static ModuleLoadDataFn g_load = nullptr;
 static ModuleGetFunctionFn g_getfn = nullptr;
 static ModuleUnloadFn g_unload = nullptr;
 static LaunchKernelFn g_launch = nullptr;
+static FuncSetAttributeFn g_setattr = nullptr;
 static std::mutex g_jit_mutex;
 
 template <typename F>
@@ -64,6 +67,7 @@ static int jit_driver() {
     PS_TRY(driver_fn("cuModuleLoadData", &g_load));
     PS_TRY(driver_fn("cuModuleGetFunction", &g_getfn));
     PS_TRY(driver_fn("cuModuleUnload", &g_unload));
+    PS_TRY(driver_fn("cuFuncSetAttribute", &g_setattr));
     PS_TRY(driver_fn("cuLaunchKernel", &g_launch));
     return PS_OK;
 }
@@ -73,6 +77,7 @@ struct JitKernel {
     CUfunction fn = nullptr;
     int device = -1;
     int* err = nullptr;
+    int smem_opt_in = 48 * 1024;  // dynamic shared memory the function is currently allowed
 };
 
 }  // namespace ps
@@ -130,9 +135,21 @@ int ps_jit_compile(const char* source, const char* entry, void** kernel) {
 
 int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                   const int64_t lo[3], const int64_t count[3], void* stream, int sync) {
+    const int32_t threads[3] = {32, 8, 1};
+    return ps_jit_launch_ex(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, 0, stream, sync);
+}
+
+int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                     const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
+                     void* stream, int sync) {
     DeviceState* st = nullptr;
     PS_TRY(current_state(&st));
-    if (!kernel || !lo || !count) return fail(PS_ERR_NULL, "ps_jit_launch: NULL argument");
+    if (!kernel || !lo || !count || !threads) return fail(PS_ERR_NULL, "ps_jit_launch: NULL argument");
+    if (threads[0] < 1 || threads[1] < 1 || threads[2] < 1 || threads[2] > 64 ||
+        (int64_t)threads[0] * threads[1] * threads[2] > 1024 || threads[0] > 1024 || threads[1] > 1024)
+        return fail(PS_ERR_ARG, "ps_jit_launch: threads per block must be >= 1 and at most 1024 (z <= 64)");
+    if (shmem < 0 || shmem > 227 * 1024)
+        return fail(PS_ERR_ARG, "ps_jit_launch: shmem must be 0 to 232448 bytes (227 KB)");
     if (narrays < 0 || narrays > kJitMaxArrays || nscalars < 0 || nscalars > kJitMaxScalars ||
         (narrays && !arrays) || (nscalars && !scalars))
         return fail(PS_ERR_ARG, "ps_jit_launch: at most %d arrays and %d scalars", kJitMaxArrays, kJitMaxScalars);
@@ -155,11 +172,19 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
         g.cnt[d] = count[d];
     }
     g.err = k->err;
+    g.smem = shmem;
     if (count[0] == 0 || count[1] == 0 || count[2] == 0) return PS_OK;
-    if (count[1] > 65535LL * 8 || count[2] > 65535) return fail(PS_ERR_SHAPE, "ps_jit_launch: grid too large");
-    const unsigned gx = (unsigned)((count[0] + 31) / 32), gy = (unsigned)((count[1] + 7) / 8), gz = (unsigned)count[2];
+    const int64_t gx = (count[0] + threads[0] - 1) / threads[0], gy = (count[1] + threads[1] - 1) / threads[1],
+                  gz = (count[2] + threads[2] - 1) / threads[2];
+    if (gx > 2147483647LL || gy > 65535 || gz > 65535) return fail(PS_ERR_SHAPE, "ps_jit_launch: grid too large");
+    if (shmem > k->smem_opt_in) {
+        if (g_setattr(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)shmem) != CUDA_SUCCESS)
+            return fail(PS_ERR_ARG, "ps_jit_launch: %lld bytes of dynamic shared memory not available", (long long)shmem);
+        k->smem_opt_in = (int)shmem;
+    }
     void* params[] = {&g};
-    const CUresult r = g_launch(k->fn, gx, gy, gz, 32, 8, 1, 0, static_cast<CUstream>(stream), params, nullptr);
+    const CUresult r = g_launch(k->fn, (unsigned)gx, (unsigned)gy, (unsigned)gz, (unsigned)threads[0], (unsigned)threads[1],
+                                (unsigned)threads[2], (unsigned)shmem, static_cast<CUstream>(stream), params, nullptr);
     if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "ps_jit_launch: cuLaunchKernel failed (CUresult %d)", (int)r);
     PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), sync, "ps_jit_launch"));
     if (!sync) return PS_OK;
@@ -168,7 +193,9 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
         return fail(PS_ERR_CUDA, "ps_jit_launch: reading the error flag failed");
     if (flag) {
         cudaMemset(k->err, 0, sizeof(int));
-        return fail(PS_ERR_ARG, "ps_jit_launch: out-of-bounds array access in the kernel (BoundsError)");
+        if (flag & 1) return fail(PS_ERR_ARG, "ps_jit_launch: out-of-bounds array access in the kernel (BoundsError)");
+        return fail(PS_ERR_ARG, "ps_jit_launch: a kernel with @sync_threads, shuffles or votes needs ranges that are "
+                                "a multiple of the thread block; a partial block did not run");
     }
     return PS_OK;
 }

@@ -49,9 +49,15 @@ _lib.register("ps_jit_compile", [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTE
 _lib.register("ps_jit_launch", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
                                 ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p, ctypes.c_int])
+_lib.register("ps_jit_launch_ex", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
+                                   ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                   ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
+                                   ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
 MAX_ARRAYS = MAX_SCALARS = 32
+_COLLECTIVE = {"__m_shfl_sync", "__m_shfl_up_sync", "__m_shfl_down_sync", "__m_shfl_xor_sync", "__m_vote_any_sync",
+               "__m_vote_all_sync", "__m_vote_ballot_sync"}
 _MATH = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "sinh", "cosh", "atan", "asin", "acos", "log10",
          "exp2", "cbrt"}
 
@@ -64,7 +70,7 @@ def _ident(name: str) -> str:
 
 def _sanitize(text: str) -> str:
     text = re.sub(r"#.*", "", text).replace("$", "")  # `$ix` interpolations name the index itself
-    for a, b in (("≤", "<="), ("≥", ">="), ("≠", "!=")):
+    for a, b in (("≤", "<="), ("≥", ">="), ("≠", "!="), ("÷", "//"), ("∈", " in ")):
         text = text.replace(a, b)
     out = []
     for c in text:
@@ -75,6 +81,23 @@ def _sanitize(text: str) -> str:
     text = re.sub(r"!(?!=)", " not ", text)
     text = re.sub(r"\btrue\b", "True", text)
     return re.sub(r"\bfalse\b", "False", text)
+
+
+def _split_range(text: str) -> list:
+    """`a:b` / `a:s:b` (top-level colons) -> [a, b] / [a, s, b]."""
+    parts, d, cur = [], 0, ""
+    for c in text:
+        d += c in "([{"
+        d -= c in ")]}"
+        if c == ":" and d == 0:
+            parts.append(cur.strip())
+            cur = ""
+        else:
+            cur += c
+    parts.append(cur.strip())
+    if len(parts) not in (2, 3) or not all(parts):
+        raise ArgumentError(f"for loops run over a range a:b or a:s:b (obtained {text})")
+    return parts
 
 
 def _to_python(body: str) -> str:
@@ -89,7 +112,9 @@ def _to_python(body: str) -> str:
         s = tokenize.untokenize([(t.type, t.string) for t in cur]).strip() if cur else ""
         # a left-hand selection `@all(A) = ...` becomes the assignable `__lhs_all[A] = ...`
         s = re.sub(r"^__m_(\w+)\s*\(\s*(\w+)\s*\)\s*=(?!=)", r"__lhs_\1[\2] =", s)
-        if s and s != "return":
+        if s == "return" and indent == 0:
+            pass  # the closing `return` of the function body
+        elif s:
             lines.append("    " * indent + s)
         cur = []
 
@@ -129,11 +154,33 @@ def _to_python(body: str) -> str:
                     j += 1
                     if d == 0:
                         break
+                nxt = toks[j]
+                if (nxt.type == tokenize.OP and nxt.string not in ";([") or nxt.string in ("and", "or"):
+                    while toks[j].type not in (tokenize.NEWLINE, tokenize.NL) and toks[j].string != ";":
+                        cond.append(toks[j])  # `if (a) && (b)`: the condition goes on
+                        j += 1
             else:
                 while toks[j].type not in (tokenize.NEWLINE, tokenize.NL) and toks[j].string != ";":
                     cond.append(toks[j])
                     j += 1
             lines.append("    " * indent + kw + " " + tokenize.untokenize([(c.type, c.string) for c in cond]).strip() + ":")
+            indent += 1
+            i = j
+            continue
+        if depth == 0 and t.type == tokenize.NAME and t.string in ("for", "while") and not cur:
+            j, hdr = i + 1, []
+            while toks[j].type not in (tokenize.NEWLINE, tokenize.NL, tokenize.ENDMARKER) and toks[j].string != ";":
+                hdr.append(toks[j])
+                j += 1
+            text = tokenize.untokenize([(c.type, c.string) for c in hdr]).strip()
+            if t.string == "while":
+                lines.append("    " * indent + "while " + text + ":")
+            else:  # for v = a:b / a:s:b (also `in`, `∈`)
+                m = re.match(r"(\w+)\s*(?:=|\bin\b)\s*(.+)$", text)
+                if not m:
+                    raise ArgumentError(f"unsupported for-loop header: {text}")
+                parts = _split_range(m.group(2))
+                lines.append("    " * indent + f"for {m.group(1)} in __range({', '.join(parts)}):")
             indent += 1
             i = j
             continue
@@ -274,21 +321,16 @@ class _Gen:
         self.sidx = {n: i for i, n in enumerate(kd.scalars)}
         self.temps = {}  # temporary name -> (lhs inn mask, expression)
         self.checked = kd.options.get("inbounds", "false") != "true"
+        self.locals = {}   # local variable -> "int" | "real" | "shared"
+        self.shared = {}   # @sharedMem array -> index
+        self.kernel_language = False
+        self.uses_collectives = False  # @sync_threads, shuffles, votes
 
     # element of array `name` at 0-based integer index expressions (strings) per dimension
     def at(self, name, ix):
         k = self.aidx[name]
         ix = list(ix) + ["0"] * (3 - len(ix))
         return f"a{k}[({ix[0]}) + n{k}_0 * (({ix[1]}) + n{k}_1 * ({ix[2]}))]"
-
-    # read of that element; unless `inbounds=true`, an index outside the array sets the error flag
-    # and reads 0 (Julia's bounds check raises a BoundsError there)
-    def load(self, name, ix):
-        if not self.checked:
-            return self.at(name, ix)
-        k = self.aidx[name]
-        ix = list(ix) + ["0"] * (3 - len(ix))
-        return f"jl_ld(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)"
 
     # value of array-or-temporary `name` at thread index + integer offset vector `o`
     def val(self, name, o):
@@ -341,22 +383,66 @@ class _Gen:
         raise ArgumentError(f"macro @{mname} not supported")
 
     def is_bool(self, e):
-        return isinstance(e, (ast.Compare, ast.BoolOp)) or (isinstance(e, ast.UnaryOp) and isinstance(e.op, ast.Not)) \
-            or (isinstance(e, ast.Constant) and isinstance(e.value, bool))
+        return self.etype(e) == "bool"
+
+    # ---- types: "int" (Julia Int), "real" (the number type R), "bool"
+    def etype(self, e):
+        T = self.etype
+        if isinstance(e, ast.Constant):
+            return "bool" if isinstance(e.value, bool) else "int" if isinstance(e.value, int) else "real"
+        if isinstance(e, ast.Name):
+            if e.id in self.kd.index_names or (self.kd.kind == "parallel" and e.id in ("ix", "iy", "iz")):
+                return "int"
+            if e.id in self.sidx:
+                return "int" if e.id in self.kd.int_scalars else "real"
+            if e.id in self.locals:
+                return self.locals[e.id]
+            return "real"
+        if isinstance(e, ast.UnaryOp):
+            return "bool" if isinstance(e.op, ast.Not) else T(e.operand)
+        if isinstance(e, (ast.Compare, ast.BoolOp)):
+            return "bool"
+        if isinstance(e, ast.BinOp):
+            a, b = T(e.left), T(e.right)
+            if isinstance(e.op, ast.Div):
+                return "real"
+            if isinstance(e.op, ast.Mult) and "bool" in (a, b):
+                return b if a == "bool" else a
+            return "int" if a in ("int", "bool") and b in ("int", "bool") else "real"
+        if isinstance(e, ast.Attribute):
+            return "int"
+        if isinstance(e, ast.Call) and isinstance(e.func, ast.Name):
+            f = e.func.id
+            if f in ("size", "__m_warpsize", "__m_laneid", "__m_active_mask", "__m_vote_ballot_sync", "length"):
+                return "int"
+            if f in ("__m_vote_any_sync", "__m_vote_all_sync"):
+                return "bool"
+            if f in ("__m_shfl_sync", "__m_shfl_up_sync", "__m_shfl_down_sync", "__m_shfl_xor_sync"):
+                return T(e.args[1])
+            if f in ("max", "min", "abs"):
+                return "int" if all(T(a) == "int" for a in e.args) else "real"
+            if f == "ifelse":
+                return "int" if T(e.args[1]) == T(e.args[2]) == "int" else "real"
+            return "real"
+        return "real"
 
     def expr(self, e, off=(0, 0, 0), ctx="real"):
         E = lambda x, c=ctx: self.expr(x, off, c)  # noqa: E731
+        if ctx == "auto":
+            ctx = "int" if self.etype(e) in ("int", "bool") else "real"
         if isinstance(e, ast.Constant):
             if isinstance(e.value, bool):
                 return "true" if e.value else "false"
             if isinstance(e.value, int) and ctx != "real":
-                return str(e.value)
+                return f"{e.value}LL"
             return _lit(e.value)
         if isinstance(e, ast.Name):
             if e.id in self.kd.index_names:
                 return f"((long long)t{'xyz'[self.kd.index_names.index(e.id)]} + 1)"
             if e.id in self.sidx:
                 return f"s{self.sidx[e.id]}"
+            if e.id in self.locals and self.locals[e.id] != "shared":
+                return f"v_{e.id}"
             if self.kd.kind == "parallel" and e.id in ("ix", "iy", "iz")[:self.nd]:  # ParallelStencil.INDICES
                 return f"((long long)t{e.id[1]} + 1)"
             raise ArgumentError(f"unknown name {e.id} in an expression")
@@ -372,14 +458,22 @@ class _Gen:
                 if isinstance(e.right, ast.Constant) and e.right.value in (2, 3) and not isinstance(e.right.value, bool):
                     x = E(e.left)
                     return f"({x} * {x})" if e.right.value == 2 else f"(({x} * {x}) * {x})"
-                return f"pow({E(e.left)}, (R)({E(e.right)}))"
+                return f"pow({E(e.left, 'real')}, (R)({E(e.right, 'real')}))"
+            if isinstance(e.op, ast.Mult) and (self.is_bool(e.left) or self.is_bool(e.right)):
+                b, x = (e.left, e.right) if self.is_bool(e.left) else (e.right, e.left)
+                if self.etype(x) == "int":
+                    return f"((long long)({E(b, 'auto')}) * {E(x, 'int')})"
+                return f"jl_bmul({E(b, 'auto')}, {E(x, 'real')})"
+            if isinstance(e.op, (ast.FloorDiv, ast.Mod)):  # Julia ÷ and % (truncating)
+                if self.etype(e) == "int":
+                    return f"({E(e.left, 'int')} {'/' if isinstance(e.op, ast.FloorDiv) else '%'} {E(e.right, 'int')})"
+                if isinstance(e.op, ast.Mod):
+                    return f"fmod({E(e.left, 'real')}, {E(e.right, 'real')})"
+                return f"trunc({E(e.left, 'real')} / {E(e.right, 'real')})"
             ops = {ast.Add: "+", ast.Sub: "-", ast.Mult: "*", ast.Div: "/"}
             if type(e.op) not in ops:
                 raise ArgumentError("unsupported operator")
-            if isinstance(e.op, ast.Mult) and (self.is_bool(e.left) or self.is_bool(e.right)):
-                b, x = (e.left, e.right) if self.is_bool(e.left) else (e.right, e.left)
-                return f"jl_bmul({E(b, 'auto')}, {E(x)})"
-            c = ctx if ctx != "real" else "real"
+            c = "int" if (self.etype(e) == "int" and ctx != "real") else "real"
             if isinstance(e.op, ast.Div):
                 c = "real"
             return f"({E(e.left, c)} {ops[type(e.op)]} {E(e.right, c)})"
@@ -387,46 +481,103 @@ class _Gen:
             parts, left = [], e.left
             for op, right in zip(e.ops, e.comparators):
                 sym = {ast.Lt: "<", ast.LtE: "<=", ast.Gt: ">", ast.GtE: ">=", ast.Eq: "==", ast.NotEq: "!="}[type(op)]
-                parts.append(f"({self.expr(left, off, 'auto')} {sym} {self.expr(right, off, 'auto')})")
+                c = "int" if self.etype(left) in ("int", "bool") and self.etype(right) in ("int", "bool") else "real"
+                parts.append(f"({self.expr(left, off, c)} {sym} {self.expr(right, off, c)})")
                 left = right
             return "(" + " && ".join(parts) + ")"
         if isinstance(e, ast.BoolOp):
             sym = " && " if isinstance(e.op, ast.And) else " || "
             return "(" + sym.join(self.expr(v, off, "auto") for v in e.values) + ")"
+        if isinstance(e, ast.Attribute):  # @threadIdx().x etc. (1-based indices, like CUDA.jl)
+            v = e.value
+            if isinstance(v, ast.Call) and isinstance(v.func, ast.Name) and e.attr in ("x", "y", "z"):
+                f = v.func.id
+                base = {"__m_threadIdx": "threadIdx", "__m_blockIdx": "blockIdx", "__m_blockDim": "blockDim",
+                        "__m_gridDim": "gridDim"}.get(f)
+                if base:
+                    self.kernel_language = True
+                    plus = " + 1" if f in ("__m_threadIdx", "__m_blockIdx") else ""
+                    return f"((long long){base}.{e.attr}{plus})"
+            raise ArgumentError("unsupported attribute access")
         if isinstance(e, ast.Call) and isinstance(e.func, ast.Name):
             f = e.func.id
+            if f in _COLLECTIVE:
+                return self.collective(f, e.args, off)
+            if f == "__m_warpsize":
+                return "32LL"
+            if f == "__m_laneid":
+                self.kernel_language = True
+                return "((long long)jl_laneid() + 1)"
+            if f == "__m_active_mask":
+                self.kernel_language = True
+                return "((long long)__activemask())"
             if f.startswith("__m_"):
                 if len(e.args) != 1 or not isinstance(e.args[0], ast.Name):
                     raise ArgumentError(f"@{f[4:]} takes one array")
                 return self.macro(f[4:], e.args[0].id, off)
             if f == "size":
                 a, d = e.args
+                if a.id in self.shared:
+                    return f"sm{self.shared[a.id]}_n{int(d.value) - 1}"
                 return f"n{self.aidx[a.id]}_{int(d.value) - 1}"
+            if f == "length" and e.args[0].id in self.aidx:
+                k = self.aidx[e.args[0].id]
+                return f"(n{k}_0 * n{k}_1 * n{k}_2)"
             if f in ("max", "min"):
-                r = E(e.args[0])
+                if self.etype(e) == "int":
+                    r = E(e.args[0], "int")
+                    for x in e.args[1:]:
+                        r = f"{f}({r}, {E(x, 'int')})"
+                    return r
+                r = E(e.args[0], "real")
                 for x in e.args[1:]:
-                    r = f"jl_{f}({r}, {E(x)})"
+                    r = f"jl_{f}({r}, {E(x, 'real')})"
                 return r
+            if f == "abs":
+                return f"llabs({E(e.args[0], 'int')})" if self.etype(e) == "int" else f"fabs({E(e.args[0], 'real')})"
+            if f == "inv":
+                return f"((R)1.0 / {E(e.args[0], 'real')})"
             if f in ("one", "zero"):  # one(eltype(A)) etc.: the number type's 1 / 0
                 return "((R)1)" if f == "one" else "((R)0)"
             if f == "ifelse":
                 c, a, b = e.args
-                return f"({E(c, 'auto')} ? {E(a)} : {E(b)})"
-            if f == "abs":
-                return f"fabs({E(e.args[0])})"
-            if f == "inv":
-                return f"((R)1.0 / {E(e.args[0])})"
+                t = "int" if self.etype(e) == "int" else "real"
+                return f"({E(c, 'auto')} ? {E(a, t)} : {E(b, t)})"
             if f in _MATH:
-                return f"{f}({E(e.args[0])})"
+                return f"{f}({E(e.args[0], 'real')})"
             raise ArgumentError(f"unsupported function {f}")
         if isinstance(e, ast.Subscript):
             return self.load(*self.subscript(e, off))
         raise ArgumentError(f"unsupported expression {ast.dump(e)[:80]}")
 
+    def collective(self, f, args, off):
+        """Warp shuffles and votes (src/ParallelKernel/kernel_language.jl:123-193): lanes are 1-based."""
+        self.kernel_language = self.uses_collectives = True
+        E = lambda x, c: self.expr(x, off, c)  # noqa: E731
+        mask = f"(unsigned)({E(args[0], 'int')})"
+        if f.startswith("__m_vote"):
+            if len(args) != 2:
+                raise ArgumentError(f"@{f[4:]}(mask, predicate)")
+            fn = {"__m_vote_any_sync": "__any_sync", "__m_vote_all_sync": "__all_sync",
+                  "__m_vote_ballot_sync": "__ballot_sync"}[f]
+            r = f"{fn}({mask}, {E(args[1], 'auto')})"
+            return f"((long long){r})" if fn == "__ballot_sync" else f"({r} != 0)"
+        if len(args) not in (3, 4):
+            raise ArgumentError(f"@{f[4:]}(mask, val, lane_or_delta[, width])")
+        t = "long long" if self.etype(args[1]) == "int" else "R"
+        val = f"({t})({E(args[1], 'int' if t == 'long long' else 'real')})"
+        arg = f"(int)({E(args[2], 'int')})"
+        if f == "__m_shfl_sync":
+            arg = f"({arg} - 1)"
+        width = f", (int)({E(args[3], 'int')})" if len(args) == 4 else ""
+        fn = {"__m_shfl_sync": "__shfl_sync", "__m_shfl_up_sync": "__shfl_up_sync",
+              "__m_shfl_down_sync": "__shfl_down_sync", "__m_shfl_xor_sync": "__shfl_xor_sync"}[f]
+        return f"{fn}({mask}, {val}, {arg}{width})"
+
     def subscript(self, e, off=(0, 0, 0)):
         """`A[i, j, ...]` (1-based, Julia's `end` = size(A, d)) -> (A, 0-based index expressions)."""
-        if not isinstance(e.value, ast.Name) or e.value.id not in self.aidx:
-            raise ArgumentError("indexing applies to array arguments")
+        if not isinstance(e.value, ast.Name) or (e.value.id not in self.aidx and e.value.id not in self.shared):
+            raise ArgumentError("indexing applies to array arguments and @sharedMem arrays")
         sl = e.slice.elts if isinstance(e.slice, ast.Tuple) else [e.slice]
         if len(sl) > 3:
             raise ArgumentError("at most 3 indices")
@@ -442,6 +593,73 @@ class _Gen:
 
         return e.value.id, [f"({self.expr(last(x, d), off, 'int')}) - 1" for d, x in enumerate(sl)]
 
+    def smem_ref(self, name, ix):
+        j = self.shared[name]
+        ix = list(ix) + ["0"] * (3 - len(ix))
+        return f"sm{j}, sm{j}_n0, sm{j}_n1, sm{j}_n2, {ix[0]}, {ix[1]}, {ix[2]}, sm{j}_cap"
+
+    # read of an element; unless `inbounds=true`, an index outside the array sets the error flag and
+    # reads 0 (Julia's bounds check raises a BoundsError there)
+    def load(self, name, ix):
+        if name in self.shared:  # @sharedMem arrays are always bounds-checked (extents and the launch's shmem)
+            return f"jl_lds({self.smem_ref(name, ix)}, g.err)"
+        if not self.checked:
+            return self.at(name, ix)
+        k = self.aidx[name]
+        ix = list(ix) + ["0"] * (3 - len(ix))
+        return f"jl_ld(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)"
+
+    # ---- local variables of @parallel_indices bodies (Julia function scope: declared at the top)
+    def infer_locals(self, stmts):
+        for s in stmts:
+            if isinstance(s, ast.Assign) and len(s.targets) == 1 and isinstance(s.targets[0], ast.Name):
+                n = s.targets[0].id
+                if n in self.aidx or n in self.sidx or n in self.kd.index_names:
+                    raise ArgumentError(f"cannot assign to argument or index {n}")
+                v = s.value
+                if isinstance(v, ast.Call) and isinstance(v.func, ast.Name) and v.func.id == "__m_sharedMem":
+                    if n in self.locals:
+                        raise ArgumentError(f"@sharedMem array {n} is assigned twice")
+                    self.locals[n] = "shared"
+                    self.shared[n] = len(self.shared)
+                    continue
+                t = self.etype(v)
+                t = "int" if t == "bool" else t
+                if n in self.locals and self.locals[n] != t:
+                    if self.locals[n] == "shared":
+                        raise ArgumentError(f"@sharedMem array {n} is assigned twice")
+                    self.locals[n] = "real"  # Int and Float assignments: keep the wider type
+                else:
+                    self.locals.setdefault(n, t)
+            elif isinstance(s, ast.For):
+                self.locals.setdefault(s.target.id, "int")
+                self.infer_locals(s.body)
+            elif isinstance(s, (ast.If, ast.While)):
+                self.infer_locals(s.body)
+                self.infer_locals(s.orelse)
+
+    def shared_decl(self, name, call, p):
+        """`A = @sharedMem(T, dims[, offset])`: a view of the launch's dynamic shared memory."""
+        j = self.shared[name]
+        args = call.args
+        if len(args) not in (2, 3):
+            raise ArgumentError("@sharedMem(T, dims[, offset])")
+        ty = args[0]
+        ok = (isinstance(ty, ast.Call) and isinstance(ty.func, ast.Name) and ty.func.id == "eltype") or \
+            (isinstance(ty, ast.Attribute) and ty.attr == "Number") or \
+            (isinstance(ty, ast.Name) and ty.id in ("Float64", "Float32"))
+        if not ok:
+            raise ArgumentError("@sharedMem element type must be the kernel's number type (eltype(A), Data.Number)")
+        dims = args[1].elts if isinstance(args[1], ast.Tuple) else [args[1]]
+        if not 1 <= len(dims) <= 3:
+            raise ArgumentError("@sharedMem dims: 1 to 3 extents")
+        ext = [f"({self.expr(d, ctx='int')})" for d in dims] + ["1LL"] * (3 - len(dims))
+        offs = f"({self.expr(args[2], ctx='int')})" if len(args) == 3 else "0LL"
+        self.kernel_language = True
+        return [f"{p}sm{j}_off = {offs}; sm{j} = (R*)(ps_smem + (sm{j}_off > 0 ? sm{j}_off : 0));",
+                f"{p}sm{j}_n0 = {ext[0]}; sm{j}_n1 = {ext[1]}; sm{j}_n2 = {ext[2]};",
+                f"{p}sm{j}_cap = (g.smem - sm{j}_off) / (long long)sizeof(R);"]
+
     def stmt(self, s, ind):
         p = "    " * ind
         if isinstance(s, ast.If):
@@ -453,11 +671,44 @@ class _Gen:
                 for b in s.orelse:
                     out += self.stmt(b, ind + 1)
             return out + [f"{p}}}"]
+        if isinstance(s, ast.For):
+            it = s.iter
+            if not (isinstance(it, ast.Call) and isinstance(it.func, ast.Name) and it.func.id == "__range"):
+                raise ArgumentError("for loops run over a range a:b or a:s:b")
+            v = f"v_{s.target.id}"
+            a, b = self.expr(it.args[0], ctx="int"), self.expr(it.args[-1], ctx="int")
+            step = self.expr(it.args[1], ctx="int") if len(it.args) == 3 else "1LL"
+            out = [f"{p}{{ const long long st_ = {step}, hi_ = {b};",
+                   f"{p}for ({v} = {a}; st_ > 0 ? {v} <= hi_ : {v} >= hi_; {v} += st_) {{"]
+            for x in s.body:
+                out += self.stmt(x, ind + 1)
+            return out + [f"{p}}} }}"]
+        if isinstance(s, ast.While):
+            out = [f"{p}while ({self.expr(s.test, ctx='auto')}) {{"]
+            for x in s.body:
+                out += self.stmt(x, ind + 1)
+            return out + [f"{p}}}"]
         if isinstance(s, ast.Pass):
             return []
+        if isinstance(s, ast.Return):  # an early `return` inside a branch: this thread is done
+            if s.value is not None:
+                raise ArgumentError("kernels return nothing")
+            return [f"{p}return;"]
+        if isinstance(s, ast.Expr) and isinstance(s.value, ast.Call) and isinstance(s.value.func, ast.Name):
+            f = s.value.func.id
+            if f == "__m_sync_threads":
+                self.kernel_language = self.uses_collectives = True
+                return [f"{p}__syncthreads();"]
+            raise ArgumentError(f"unsupported statement {f}")
         if not isinstance(s, ast.Assign) or len(s.targets) != 1:
-            raise ArgumentError("kernel statements are assignments or if-blocks")
+            raise ArgumentError("kernel statements are assignments, if-blocks, loops or @sync_threads()")
         t = s.targets[0]
+        if isinstance(t, ast.Name):  # local variable
+            if self.locals.get(t.id) == "shared":
+                return self.shared_decl(t.id, s.value, p)
+            c = "int" if self.locals[t.id] == "int" else "real"
+            cast = "long long" if c == "int" else "R"
+            return [f"{p}v_{t.id} = ({cast})({self.expr(s.value, ctx=c)});"]
         if isinstance(t, ast.Subscript) and isinstance(t.value, ast.Name) and t.value.id.startswith("__lhs_"):
             sel, name = t.value.id[6:], t.slice.id
             if sel not in self.sels:
@@ -472,7 +723,9 @@ class _Gen:
             return [f"{p}if ({cond}) {self.at(name, idx)} = {self.expr(s.value)};"]
         if isinstance(t, ast.Subscript):  # @parallel_indices: A[i, j] = expr
             name, ix = self.subscript(t)
-            val = self.expr(s.value)
+            val = self.expr(s.value, ctx="real")
+            if name in self.shared:
+                return [f"{p}jl_sts({self.smem_ref(name, ix)}, g.err, (R)({val}));"]
             if not self.checked:
                 return [f"{p}{self.at(name, ix)} = (R)({val});"]
             k = self.aidx[name]
@@ -506,6 +759,7 @@ class _Gen:
     def source(self, real):
         kd = self.kd
         self.collect_temps()
+        self.infer_locals(kd.body)
         body = []
         for s in kd.body:
             body += self.stmt(s, 1)
@@ -516,9 +770,26 @@ class _Gen:
         for name, k in self.sidx.items():
             ty = "long long" if name in kd.int_scalars else "R"
             decl.append(f"    const {ty} s{k} = ({ty})g.s[{k}];")
+        for name, t in self.locals.items():
+            if t == "shared":
+                j = self.shared[name]
+                decl.append(f"    R* sm{j} = nullptr; long long sm{j}_off = 0, sm{j}_n0 = 0, sm{j}_n1 = 1, "
+                            f"sm{j}_n2 = 1, sm{j}_cap = 0;")
+            else:
+                decl.append(f"    {'long long' if t == 'int' else 'R'} v_{name} = 0;")
+        if self.uses_collectives:
+            # barriers, shuffles and votes need every thread of a block: a block that reaches past the
+            # ranges leaves as a whole before any of them (block-uniform) and reports it (flag 2)
+            guard = """    if ((blockIdx.x + 1LL) * blockDim.x > g.cnt[0] || (blockIdx.y + 1LL) * blockDim.y > g.cnt[1] ||
+        (blockIdx.z + 1LL) * blockDim.z > g.cnt[2]) {
+        if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicOr(g.err, 2);
+        return;
+    }"""
+        else:
+            guard = "    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) return;"
         return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}) -- generated by ps_gb300.jit
 typedef {real} R;
-struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; }};
+struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; }};
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ R jl_ld(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
@@ -526,14 +797,24 @@ __device__ __forceinline__ R jl_ld(const R* a, long long n0, long long n1, long 
     atomicOr(err, 1); return (R)0; }}
 __device__ __forceinline__ void jl_st(R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err, R v) {{
     if (jl_in(n0, n1, n2, i, j, k)) a[i + n0 * (j + n1 * k)] = v; else atomicOr(err, 1); }}
+__device__ __forceinline__ R jl_lds(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, long long cap, int* err) {{
+    const long long l = i + n0 * (j + n1 * k);
+    if (a && jl_in(n0, n1, n2, i, j, k) && l < cap) return a[l];
+    atomicOr(err, 1); return (R)0; }}
+__device__ __forceinline__ void jl_sts(R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, long long cap, int* err, R v) {{
+    const long long l = i + n0 * (j + n1 * k);
+    if (a && jl_in(n0, n1, n2, i, j, k) && l < cap) a[l] = v; else atomicOr(err, 1); }}
+__device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov.u32 %0, %%laneid;" : "=r"(l)); return l; }}
 __device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
 extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
-    const long long ux = blockIdx.x * (long long)blockDim.x + threadIdx.x, uy = blockIdx.y * (long long)blockDim.y + threadIdx.y, uz = blockIdx.z;
-    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) return;
+    extern __shared__ __align__(16) unsigned char ps_smem[];
+    const long long ux = blockIdx.x * (long long)blockDim.x + threadIdx.x, uy = blockIdx.y * (long long)blockDim.y + threadIdx.y;
+    const long long uz = blockIdx.z * (long long)blockDim.z + threadIdx.z;
+{guard}
     const long long tx = g.lo[0] + ux, ty = g.lo[1] + uy, tz = g.lo[2] + uz;
-    (void)tx; (void)ty; (void)tz;
+    (void)tx; (void)ty; (void)tz; (void)ps_smem;
 {chr(10).join(decl)}
 {chr(10).join(body)}
 }}
@@ -549,6 +830,12 @@ def _is_sel_assign(s):
 def generate(kd: KernelDef, ndims: int, dtype: str) -> str:
     """CUDA C of kernel `kd` for `ndims`-D arrays of `dtype` ("double" or "float")."""
     return _Gen(kd, ndims).source(dtype)
+
+
+def _generate_info(kd: KernelDef, ndims: int, dtype: str):
+    g = _Gen(kd, ndims)
+    src = g.source(dtype)
+    return src, g.uses_collectives
 
 
 # ---- kernels -----------------------------------------------------------------------------------
@@ -567,6 +854,7 @@ class JitKernel:
         self.kd = parse(src)
         self.name, self.nargs = self.kd.name, len(self.kd.args)
         self._handles = {}
+        self._collective = {}
 
     def source(self, ndims, dtype="double"):
         return generate(self.kd, ndims, dtype)
@@ -574,15 +862,19 @@ class JitKernel:
     def _handle(self, ndims, dtype):
         key = (ndims, dtype)
         if key not in self._handles:
+            src, self._collective[key] = _generate_info(self.kd, ndims, dtype)
             h = ctypes.c_void_p()
-            _lib.call("ps_jit_compile", self.source(ndims, dtype).encode(), b"ps_jit_entry", ctypes.byref(h))
+            _lib.call("ps_jit_compile", src.encode(), b"ps_jit_entry", ctypes.byref(h))
             self._handles[key] = h
         return self._handles[key]
 
-    def __call__(self, *args, ranges=None, stream=None, sync=True):
-        self.jit_launch(args, ranges, stream, sync)
+    def __call__(self, *args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None):
+        self.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem)
 
-    def jit_launch(self, args, ranges=None, stream=None, sync=True):
+    def jit_launch(self, args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None):
+        """Launch over `ranges` (default: the largest array extents; with `nblocks`, nblocks .* nthreads
+        threads) in blocks of `nthreads` (default (32, 8, 1)) with `shmem` bytes of dynamic shared
+        memory (src/ParallelKernel/parallel.jl:303-328)."""
         require_initialized()
         if len(args) != self.nargs:
             raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
@@ -599,16 +891,35 @@ class JitKernel:
         lo, cnt = [0, 0, 0], [1, 1, 1]
         for d in range(ndims):
             cnt[d] = max(int(x.n[d]) for x in descs) if descs else 1
+        threads = [1, 1, 1]
+        if nthreads is not None:
+            nthreads = tuple(int(x) for x in (nthreads if isinstance(nthreads, (tuple, list)) else (nthreads,)))
+            if not 1 <= len(nthreads) <= 3:
+                raise ArgumentError("nthreads: 1 to 3 dimensions")
+            threads[:len(nthreads)] = nthreads
+        else:
+            threads = [32, 8, 1]
+        if nblocks is not None:
+            if nthreads is None:
+                raise ArgumentError("nblocks needs nthreads")
+            nb = tuple(int(x) for x in (nblocks if isinstance(nblocks, (tuple, list)) else (nblocks,)))
+            nb = nb + (1,) * (3 - len(nb))
+            if ranges is None:
+                lo, cnt = [0, 0, 0], [nb[d] * threads[d] for d in range(3)]
         if ranges is not None:  # Julia ranges: 1-based (start, stop) pairs, or python ranges over 0-based indices
             lo, hi = ranges_to_box(ranges)
             if min(lo) < 0:
                 raise ArgumentError("ranges must start at index 1 or above")
             cnt = [max(0, hi[d] - lo[d]) for d in range(3)]
         h = self._handle(ndims, dt)
+        if self._collective[(ndims, dt)] and any(cnt[d] % threads[d] for d in range(3)):
+            raise ArgumentError("a kernel with @sync_threads, shuffles or votes needs ranges that are a multiple of "
+                                f"the thread block (ranges {cnt}, nthreads {threads})")
         A = (PSArray * max(1, len(descs)))(*descs)
         S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
-        _lib.call("ps_jit_launch", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
-                  (ctypes.c_int64 * 3)(*cnt), stream_handle(stream), int(bool(sync)))
+        _lib.call("ps_jit_launch_ex", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
+                  (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), stream_handle(stream),
+                  int(bool(sync)))
 
     def __del__(self):
         try:

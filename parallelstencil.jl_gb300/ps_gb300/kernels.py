@@ -169,12 +169,15 @@ def from_source(body: str, ndims: int = 3):
     raise ArgumentError("unsupported @parallel kernel body for the GB300 package")
 
 
-def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True, fp64="ieee"):
-    """`@parallel [ranges] [memopt=...] kernel!(args...)`."""
+def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True, fp64="ieee",
+             nblocks=None, nthreads=None, shmem=None):
+    """`@parallel [ranges] [nblocks nthreads] [memopt=...] [shmem=...] kernel!(args...)`."""
     require_initialized()
     if hasattr(kernel, "jit_launch"):  # run-time compiled kernel (ps_gb300.jit); memopt does not change results
-        kernel.jit_launch(args, ranges, stream, sync)
+        kernel.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem)
         return
+    if nblocks is not None or nthreads is not None or shmem is not None:
+        raise ArgumentError("nblocks / nthreads / shmem apply to run-time compiled kernels (parallel_kernel)")
     if isinstance(kernel, FdKernel):
         if ranges is not None or memopt:
             raise ArgumentError("FD operator kernels take no ranges/memopt")

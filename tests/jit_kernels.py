@@ -131,3 +131,90 @@ SHIFT_INBOUNDS = """@parallel_indices (i) inbounds=true function shift_inb!(B, A
     B[i] = A[i+1]
     return
 end"""
+
+# ---- kernel language (src/ParallelKernel/kernel_language.jl): blocks, shared memory, warps
+
+# 2-D heat step staged through a shared-memory tile with a one-cell halo, the pattern of
+# examples/diffusion2D_shmem_novis.jl (here with the barrier outside any branch)
+HEAT2D_TILE = """@parallel_indices (ix, iy) function heat2d_tile!(T2, T, Ci, lam, dt, rdx, rdy)
+    tx = @threadIdx().x + 1
+    ty = @threadIdx().y + 1
+    Tl = @sharedMem(eltype(T), (@blockDim().x + 2, @blockDim().y + 2))
+    Tl[tx, ty] = T[ix, iy]
+    if (ix > 1 && @threadIdx().x == 1) Tl[tx-1, ty] = T[ix-1, iy] end
+    if (ix < size(T, 1) && @threadIdx().x == @blockDim().x) Tl[tx+1, ty] = T[ix+1, iy] end
+    if (iy > 1 && @threadIdx().y == 1) Tl[tx, ty-1] = T[ix, iy-1] end
+    if (iy < size(T, 2) && @threadIdx().y == @blockDim().y) Tl[tx, ty+1] = T[ix, iy+1] end
+    @sync_threads()
+    if (1 < ix < size(T2, 1) && 1 < iy < size(T2, 2))
+        T2[ix, iy] = Tl[tx, ty] + dt*Ci[ix, iy]*lam*((Tl[tx+1, ty] - 2.0*Tl[tx, ty] + Tl[tx-1, ty])*rdx*rdx +
+                                                    (Tl[tx, ty+1] - 2.0*Tl[tx, ty] + Tl[tx, ty-1])*rdy*rdy)
+    end
+    return
+end"""
+
+# the same step without shared memory (the reference value for the tile kernel)
+HEAT2D_PLAIN = """@parallel_indices (ix, iy) function heat2d_plain!(T2, T, Ci, lam, dt, rdx, rdy)
+    if (1 < ix < size(T2, 1) && 1 < iy < size(T2, 2))
+        T2[ix, iy] = T[ix, iy] + dt*Ci[ix, iy]*lam*((T[ix+1, iy] - 2.0*T[ix, iy] + T[ix-1, iy])*rdx*rdx +
+                                                   (T[ix, iy+1] - 2.0*T[ix, iy] + T[ix, iy-1])*rdy*rdy)
+    end
+    return
+end"""
+
+# butterfly sum of each warp's 32 values (every lane ends with the same sum)
+WARP_SUMS = """@parallel_indices (i) function warp_sums!(S, A)
+    v = A[i]
+    o = 16
+    while o >= 1
+        v = v + @shfl_xor_sync(0xffffffff, v, o)
+        o = o ÷ 2
+    end
+    if @laneid() == 1
+        S[(i - 1) ÷ 32 + 1] = v
+    end
+    return
+end"""
+
+# broadcasts, shifts within 16-lane partitions, votes and ballots
+WARP_OPS = """@parallel_indices (i) function warp_ops!(B, C, D, A, t)
+    v = A[i]
+    first = @shfl_sync(0xffffffff, v, 1)
+    up = @shfl_up_sync(0xffffffff, v, 1)
+    down = @shfl_down_sync(0xffffffff, v, 2, 16)
+    anyhi = @vote_any_sync(0xffffffff, v > t)
+    allhi = @vote_all_sync(0xffffffff, v > -t)
+    bal = @vote_ballot_sync(0xffffffff, v > 0)
+    B[i] = first + up*anyhi - down
+    C[i] = allhi*1.0 + (bal % 1024)
+    D[i] = @laneid() + 100*@warpsize()
+    return
+end"""
+
+# loops and local variables: a box filter along x of half-width w
+BOX_X = """@parallel_indices (ix, iy) function box_x!(B, A, w::Integer)
+    s = 0.0
+    c = 0
+    for k = max(1, ix - w):min(size(A, 1), ix + w)
+        s = s + A[k, iy]
+        c = c + 1
+    end
+    B[ix, iy] = s / c
+    return
+end"""
+
+# block and thread coordinates of a 3-D launch
+BLOCK_IDS = """@parallel_indices (ix, iy, iz) function block_ids!(A)
+    A[ix, iy, iz] = @blockIdx().x + 10*@blockIdx().y + 100*@blockIdx().z +
+                    1000*(@threadIdx().x + @threadIdx().y*@blockDim().x) + 0.5*@gridDim().z
+    return
+end"""
+
+# an early `return` inside a branch ends the thread
+EARLY_RETURN = """@parallel_indices (i) function clip_tail!(B, A, m::Integer)
+    if i > m
+        return
+    end
+    B[i] = 2.0*A[i]
+    return
+end"""

@@ -83,6 +83,21 @@ def test_jit_equals_hand_written_diffusion(ps, src, fixed, dt):
         assert np.array_equal(ps.to_host(A), ps.to_host(B)), (fixed, memopt)
 
 
+@pytest.mark.parametrize("opt", ["", "inbounds=true "])
+def test_jit_equals_hand_written_flux_lam(ps, opt):
+    """The flux form with a conductivity array (face averages @av_xi(lam)) against the library kernel."""
+    import bench
+
+    rng = np.random.default_rng(8)
+    n = (35, 30, 27)
+    T, Ci, lam = (_dev(ps, rng.random(n) + c) for c in (0.0, 0.5, 1.0))
+    A, B = ps.zeros(*n), ps.zeros(*n)
+    sc = (1e-3, 9.0, 11.0, 13.0)
+    ps.parallel(ps.parallel_kernel(bench.JIT_FLUX_LAM.format(opt=opt)), A, T, Ci, lam, *sc)
+    ps.parallel(ps.kernels.diffusion3D_step_flux_lam, B, T, Ci, lam, *sc, memopt=True)
+    assert np.array_equal(ps.to_host(A), ps.to_host(B))
+
+
 def _pos(rng, shape, dt):
     return (rng.random(shape) + 0.5).astype(dt)
 
@@ -108,10 +123,11 @@ def _cases(dt):
         "D2Z3D": ([r(9, 7, 8), r(9, 7, 8)], None),
         "COMPACTION": ([_pos(rng, (nx, ny), dt), r(nx, ny), r(nx, ny), 0.8, 3.0, 0.1], None),
         "BRANCHES2D": ([r(nx, ny), r(nx, ny), 3, 0.5], None),
+        "EARLY_RETURN": ([r(40), r(40), 25], None),
     }
 
 
-_NDIMS = {"ROD1D": 1}
+_NDIMS = {"ROD1D": 1, "EARLY_RETURN": 1}
 _TOL = {"COMPACTION", "BRANCHES2D"}  # exp / pow
 
 
@@ -219,3 +235,98 @@ extern "C" __global__ void twice(const ps_jit_args g) {
     assert lib.ps_jit_compile(b"extern \"C\" __global__ void k() { undeclared = 1; }", b"k", ctypes.byref(bad)) == -1
     assert "undeclared" in _lib.last_error()
     assert not bad.value
+
+
+# ---------------------------------------------------------------- kernel language on the GPU
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+def test_jit_shared_memory_tile(ps, jr, dt):
+    rng = np.random.default_rng(4)
+    nx, ny = 256, 64
+    T, Ci = rng.random((nx, ny)).astype(dt), (rng.random((nx, ny)) + 0.5).astype(dt)
+    sc = (1.0, 1e-3, 7.0, 9.0)
+    host = np.zeros((nx, ny), dt)
+    jr.run(K.HEAT2D_PLAIN, [host, T, Ci, *sc])
+    A, B = ps.zeros(nx, ny, dtype=dt), ps.zeros(nx, ny, dtype=dt)
+    Td, Cd = _dev(ps, T), _dev(ps, Ci)
+    shmem = 34 * 10 * np.dtype(dt).itemsize
+    ps.parallel(ps.parallel_kernel(K.HEAT2D_TILE), A, Td, Cd, *sc, nthreads=(32, 8), shmem=shmem)
+    ps.parallel(ps.parallel_kernel(K.HEAT2D_PLAIN), B, Td, Cd, *sc)
+    assert np.array_equal(ps.to_host(A), host) and np.array_equal(ps.to_host(B), host)
+    # the interpreter runs the tile kernel block by block with real barriers (small case)
+    Ts, Cs = T[:64, :16].copy(), Ci[:64, :16].copy()
+    hs = np.zeros((64, 16), dt)
+    jr.run(K.HEAT2D_TILE, [hs, Ts, Cs, *sc], nthreads=(32, 8), shmem=shmem)
+    S = ps.zeros(64, 16, dtype=dt)
+    ps.parallel(ps.parallel_kernel(K.HEAT2D_TILE), S, _dev(ps, Ts), _dev(ps, Cs), *sc, nthreads=(32, 8), shmem=shmem)
+    assert np.array_equal(ps.to_host(S), hs)
+
+
+def test_jit_shared_memory_larger_than_48k(ps):
+    """Dynamic shared memory above the 48 KB default (the launch opts the function in)."""
+    rng = np.random.default_rng(9)
+    nx, ny = 256, 64
+    T, Ci = rng.random((nx, ny)), rng.random((nx, ny)) + 0.5
+    A, B = ps.zeros(nx, ny), ps.zeros(nx, ny)
+    sc = (1.0, 1e-3, 7.0, 9.0)
+    ps.parallel(ps.parallel_kernel(K.HEAT2D_TILE), A, _dev(ps, T), _dev(ps, Ci), *sc, nthreads=(32, 8),
+                shmem=100 * 1024)
+    ps.parallel(ps.parallel_kernel(K.HEAT2D_PLAIN), B, _dev(ps, T), _dev(ps, Ci), *sc)
+    assert np.array_equal(ps.to_host(A), ps.to_host(B))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+def test_jit_warp_shuffles_and_votes(ps, jr, dt):
+    rng = np.random.default_rng(6)
+    n = 1024
+    a = rng.standard_normal(n).astype(dt)
+    S = np.zeros(n // 32, dt)
+    jr.run(K.WARP_SUMS, [S, a], nthreads=(64,))
+    Sd = ps.zeros(n // 32, dtype=dt)
+    ps.parallel(ps.parallel_kernel(K.WARP_SUMS), Sd, _dev(ps, a), nthreads=(64,))
+    assert np.array_equal(ps.to_host(Sd), S)
+    B, C, D = (np.zeros(n, dt) for _ in range(3))
+    jr.run(K.WARP_OPS, [B, C, D, a, 1.5], nthreads=(64,))
+    Bd, Cd, Dd = (ps.zeros(n, dtype=dt) for _ in range(3))
+    ps.parallel(ps.parallel_kernel(K.WARP_OPS), Bd, Cd, Dd, _dev(ps, a), 1.5, nthreads=(64,))
+    for h, d in ((B, Bd), (C, Cd), (D, Dd)):
+        assert np.array_equal(ps.to_host(d), h)
+
+
+def test_jit_loops_locals_and_block_ids(ps, jr):
+    rng = np.random.default_rng(2)
+    A = rng.random((37, 9))
+    B = np.zeros_like(A)
+    jr.run(K.BOX_X, [B, A, 3])
+    Bd = ps.zeros(37, 9)
+    ps.parallel(ps.parallel_kernel(K.BOX_X), Bd, _dev(ps, A), 3)
+    assert np.array_equal(ps.to_host(Bd), B)
+    X = np.zeros((16, 8, 4))
+    jr.run(K.BLOCK_IDS, [X], nthreads=(8, 4, 2))
+    Xd = ps.zeros(16, 8, 4)
+    ps.parallel(ps.parallel_kernel(K.BLOCK_IDS), Xd, nthreads=(8, 4, 2))
+    assert np.array_equal(ps.to_host(Xd), X)
+    Y = ps.zeros(16, 8, 4)  # nblocks .* nthreads threads from index 1
+    ps.parallel(ps.parallel_kernel(K.BLOCK_IDS), Y, nblocks=(2, 2, 2), nthreads=(8, 4, 2))
+    assert np.array_equal(ps.to_host(Y), X)
+
+
+def test_jit_partial_blocks_with_barriers_are_refused(ps):
+    """A partial block of a kernel with barriers / shuffles never runs: the Python call refuses it,
+    and the kernel itself leaves block-uniformly before its first shuffle and reports it."""
+    from ps_gb300 import _lib
+    from ps_gb300._lib import PSArray
+    from ps_gb300.core import ArgumentError, descriptor, stream_handle
+
+    a = np.arange(100, dtype=np.float64)
+    A, S = _dev(ps, a), ps.zeros(4)
+    k = ps.parallel_kernel(K.WARP_SUMS)
+    with pytest.raises(ArgumentError, match="multiple of the thread block"):
+        ps.parallel(k, S, A, nthreads=(64,))
+    h = k._handle(1, "double")
+    arrs = (PSArray * 2)(descriptor(S), descriptor(A))
+    rc = _lib.load().ps_jit_launch_ex(h, arrs, 2, (ctypes.c_double * 1)(0.0), 0, (ctypes.c_int64 * 3)(0, 0, 0),
+                                      (ctypes.c_int64 * 3)(100, 1, 1), (ctypes.c_int32 * 3)(64, 1, 1), 0,
+                                      stream_handle(None), 1)
+    assert rc == -1 and "multiple of the thread block" in _lib.last_error()
+    ps.parallel(k, S, A, ranges=[(1, 64)], nthreads=(64,))  # a full block afterwards runs normally
+    assert np.allclose(ps.to_host(S)[:2], a[:64].reshape(2, 32).sum(axis=1))

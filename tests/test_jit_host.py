@@ -179,7 +179,8 @@ def _nvcc():
 def test_generated_sources_compile_for_sm103a(jit, tmp_path):
     """Every test kernel, FP64 and FP32, compiles as CUDA C for sm_103a (the same options NVRTC gets)."""
     srcs = [(n, getattr(K, n)) for n in dir(K) if n.isupper()]
-    nd = {"ROD1D": 1, "SHIFT_OOB": 1, "SHIFT_INBOUNDS": 1, "WALLS2D": 2}
+    nd = {"ROD1D": 1, "SHIFT_OOB": 1, "SHIFT_INBOUNDS": 1, "WALLS2D": 2, "WARP_SUMS": 1, "WARP_OPS": 1,
+          "EARLY_RETURN": 1, "BOX_X": 2}
     procs = []
     for name, src in srcs:
         ndims = nd.get(name, 2 if "2D" in name else 3)
@@ -211,3 +212,54 @@ def test_reference_miniapp_kernels_translate(jit):
             assert "ps_jit_entry" in jit.generate(jit.parse(d), ndims, "double"), (fn, d[:60])
             n += 1
     assert n >= 40
+
+
+# ---------------------------------------------------------------- kernel language in the interpreter
+def test_interpreter_shared_memory_tile_equals_plain(jr):
+    rng = np.random.default_rng(4)
+    nx, ny = 64, 16
+    T, Ci = rng.random((nx, ny)), rng.random((nx, ny)) + 0.5
+    A, B = np.zeros((nx, ny)), np.zeros((nx, ny))
+    sc = (1.0, 1e-3, 7.0, 9.0)
+    jr.run(K.HEAT2D_TILE, [A, T, Ci, *sc], nthreads=(32, 8), shmem=34 * 10 * 8)
+    jr.run(K.HEAT2D_PLAIN, [B, T, Ci, *sc])
+    assert np.array_equal(A, B) and np.count_nonzero(A) == (nx - 2) * (ny - 2)
+
+
+def test_interpreter_warp_shuffles_and_votes(jr):
+    rng = np.random.default_rng(6)
+    n = 128
+    a = rng.standard_normal(n)
+    S = np.zeros(n // 32)
+    jr.run(K.WARP_SUMS, [S, a], nthreads=(64,))
+    assert np.allclose(S, a.reshape(-1, 32).sum(axis=1), rtol=1e-14)
+    B, C, D = np.zeros(n), np.zeros(n), np.zeros(n)
+    jr.run(K.WARP_OPS, [B, C, D, a, 1.5], nthreads=(64,))
+    w = a.reshape(-1, 32)
+    lane = np.arange(32)
+    first = np.repeat(w[:, :1], 32, axis=1)
+    up = np.where(lane >= 1, np.roll(w, 1, axis=1), w)
+    down = np.where(lane % 16 + 2 < 16, np.roll(w, -2, axis=1), w)
+    anyhi = (w > 1.5).any(axis=1, keepdims=True)
+    allhi = (w > -1.5).all(axis=1, keepdims=True)
+    bal = ((w > 0) * (1 << lane)).sum(axis=1, keepdims=True) % 1024
+    assert np.array_equal(B.reshape(-1, 32), first + np.where(anyhi, up, np.copysign(0.0, up)) - down)
+    assert np.array_equal(C.reshape(-1, 32), allhi * 1.0 + bal + 0 * w)
+    assert np.array_equal(D.reshape(-1, 32), np.broadcast_to(lane + 1 + 3200.0, w.shape))
+    with pytest.raises(ValueError, match="multiple of the thread block"):
+        jr.run(K.WARP_SUMS, [S, a], ranges=[(1, 100)], nthreads=(64,))
+
+
+def test_interpreter_loops_and_block_ids(jr):
+    rng = np.random.default_rng(2)
+    A = rng.random((11, 5))
+    B = np.zeros_like(A)
+    jr.run(K.BOX_X, [B, A, 2])
+    exp = np.array([[A[max(0, i - 2):min(11, i + 3), j].sum() / (min(11, i + 3) - max(0, i - 2))
+                     for j in range(5)] for i in range(11)])
+    assert np.allclose(B, exp, rtol=1e-15)
+    X = np.zeros((16, 8, 4))
+    jr.run(K.BLOCK_IDS, [X], nthreads=(8, 4, 2))
+    i, j, k = np.meshgrid(np.arange(16), np.arange(8), np.arange(4), indexing="ij")
+    exp = (i // 8 + 1) + 10 * (j // 4 + 1) + 100 * (k // 2 + 1) + 1000 * ((i % 8 + 1) + (j % 4 + 1) * 8) + 0.5 * 2
+    assert np.array_equal(X, exp)
