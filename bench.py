@@ -562,6 +562,20 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": "gemm", "n": n, "steps": a.steps}))
         return
+    if a.only_run == "jit":  # the headline body, run-time compiled (IEEE FP64, bounds-checked), --steps steps
+        k = ps.parallel_kernel(JIT_FLUX_LAM.format(opt=""))
+        g = torch.Generator(device="cuda").manual_seed(2)
+        T = ps.empty(n, n, n)
+        T.copy_(torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64))
+        T2, lam, Ci = T.clone(), ps.empty(n, n, n), ps.ones(n, n, n)
+        lam.copy_(1 + 0.5 * torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64))
+        dx = 10.0 / (n - 1)
+        for i in range(a.steps):
+            src, dst = (T, T2) if i % 2 == 0 else (T2, T)
+            ps.parallel(k, dst, src, Ci, lam, dx * dx / 1.5 / 8.1, 1 / dx, 1 / dx, 1 / dx, sync=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"only_run": "jit", "n": n, "steps": a.steps}))
+        return
     g = torch.Generator(device="cuda")
     g.manual_seed(2)
     T = ps.empty(n, n, n)
@@ -592,9 +606,10 @@ def main():
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
-    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm"], default=None,
-                    help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or --steps "
-                         "calls of the tcgen05 GEMM on an --n cubed bf16 problem) and exit")
+    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit"], default=None,
+                    help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
+                         "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
+                         "problem) and exit")
     a = ap.parse_args()
     if a.only_run:
         only_run(a)
