@@ -348,6 +348,8 @@ def run_ours(a, world, rank, local):
             bench_kernel("diffusion3d_flux_lam_f32_plain", ps.kernels.diffusion3D_step_flux_lam, arrs32,
                          (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float32, a.steps)
             bench_kernel("memcopy3d_f32", ps.kernels.copy3D, arrs32, (), False, WORDS_MEMCOPY, n, np.float32, a.steps)
+            bench_kernel("diffusion3d_flux_lam_f32_jit", ps.parallel_kernel(JIT_FLUX_LAM.format(opt="")), arrs32,
+                         (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float32, a.steps)
             del arrs32
             torch.cuda.empty_cache()
             n2 = 256
@@ -368,6 +370,9 @@ def run_ours(a, world, rank, local):
         if warm:
             for r in (warm["fp64"], warm["mixed"]):
                 launches += int(r["seeds"] * (r["iters_zero_mean"] + r["iters_warm_mean"]))
+        adj = None if a.quick else bench_adjoint(ps, torch)
+        if adj:
+            launches += adj.pop("launches")
     clocks = clk.summary()
 
     value = world * b_head / t_head / 1e9
@@ -396,6 +401,7 @@ def run_ours(a, world, rank, local):
         "gpu_launches": launches,
         "stokes2d_time_to_tol": stokes,
         "warm_start_time_to_tol": warm,
+        "adjoint_gradient": adj,
         "clocks": clocks,
         "variants": results,
     }
@@ -481,6 +487,63 @@ def bench_warm_start(seeds, n=1023, tol=1e-8):
     return out
 
 
+def bench_adjoint(ps, torch, n=256, nt=200, every=20):
+    """The inverse-conductivity gradient: dL/dlam of L = 0.5||T_nt - T_obs||^2 through nt flux-lam
+    diffusion steps (n^3 FP64), checkpoints every `every` steps, reverse sweep with the hand-written
+    adjoint. lam = exp(0.3 g), g a seeded Gaussian random field (white noise, seed 4, convolved with
+    a Gaussian of sigma = 8 cells, unit variance); T_obs = the forward run with lam (1 + 0.05 h), h a
+    second field (seed 5); T0 = 1.7 exp(-|x - 5|^2) on [0, 10]^3."""
+    from ps_gb300 import adjoint
+
+    def grf(seed):
+        gen = torch.Generator(device="cuda").manual_seed(seed)
+        w = torch.randn((n, n, n), generator=gen, device="cuda", dtype=torch.float64)
+        k = torch.fft.fftfreq(n, device="cuda", dtype=torch.float64)
+        kx, ky, kz = torch.meshgrid(k, k, k, indexing="ij")
+        filt = torch.exp(-2 * (torch.pi * 8.0) ** 2 * (kx ** 2 + ky ** 2 + kz ** 2))  # Gaussian, sigma 8 cells
+        f = torch.fft.ifftn(torch.fft.fftn(w) * filt).real
+        return (f - f.mean()) / f.std()
+
+    def dev(t):  # torch (x, y, z) -> column-major device array
+        A = ps.empty(n, n, n)
+        A.copy_(t)
+        return A
+
+    x = torch.linspace(0, 10, n, device="cuda", dtype=torch.float64)
+    X, Y, Z = torch.meshgrid(x, x, x, indexing="ij")
+    T0 = dev(1.7 * torch.exp(-((X - 5) ** 2 + (Y - 5) ** 2 + (Z - 5) ** 2)))
+    del X, Y, Z
+    lam = dev(torch.exp(0.3 * grf(4)))
+    lam_obs = dev(torch.exp(0.3 * grf(4)) * (1 + 0.05 * grf(5)))
+    Ci = ps.ones(n, n, n)
+    h = ((n - 1) / 10.0,) * 3  # 1/dx
+    dt = (10.0 / (n - 1)) ** 2 / float(lam_obs.max()) / 8.1
+    torch.cuda.synchronize()
+    _, _, T_obs, _ = adjoint.misfit_gradient(T0, T0, Ci, lam_obs, dt, h, nt, return_final=True)
+    out = {"config": f"{n}^3 FP64, {nt} flux-lam steps, checkpoint every {every}, lam = exp(0.3 g) (Gaussian random "
+                     f"field, sigma 8 cells), T_obs from lam (1 + 0.05 h)", "launches": 0}
+    for fp64 in ("ieee", "split"):
+        adjoint.misfit_gradient(T0, T_obs, Ci, lam, dt, h, 2 * every, checkpoint_every=every, fp64=fp64)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss, g, st = adjoint.misfit_gradient(T0, T_obs, Ci, lam, dt, h, nt, checkpoint_every=every, fp64=fp64)
+        torch.cuda.synchronize()
+        t_grad = time.perf_counter() - t0
+        T, T2 = T0.clone(), T0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, T, T2, Ci, lam, dt, *h, nt, fp64=fp64, sync=False)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        out[fp64] = {"seconds_gradient": round(t_grad, 4), "seconds_forward": round(t_fwd, 4),
+                     "gradient_over_forward": round(t_grad / t_fwd, 3), "loss": loss,
+                     "checkpoints": st.checkpoints, "recomputed_steps": st.recomputed_steps,
+                     "grad_norm": float(g.norm())}
+        out["launches"] += 2 * nt + st.recomputed_steps + nt + 2
+        del T, T2, g
+    return out
+
+
 def _oracle_slab_steps(n, slab, steps, warmup):
     """Time the oracle's flux-lam diffusion step over a z-slab of an n^3 FP64 job."""
     import oracle
@@ -562,19 +625,28 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": "gemm", "n": n, "steps": a.steps}))
         return
-    if a.only_run == "jit":  # the headline body, run-time compiled (IEEE FP64, bounds-checked), --steps steps
+    if a.only_run in ("jit", "jit32"):  # the headline body, run-time compiled (IEEE, bounds-checked), --steps steps
+        dt_np = np.float32 if a.only_run == "jit32" else np.float64
+        tdt = torch.float32 if a.only_run == "jit32" else torch.float64
         k = ps.parallel_kernel(JIT_FLUX_LAM.format(opt=""))
         g = torch.Generator(device="cuda").manual_seed(2)
-        T = ps.empty(n, n, n)
-        T.copy_(torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64))
-        T2, lam, Ci = T.clone(), ps.empty(n, n, n), ps.ones(n, n, n)
-        lam.copy_(1 + 0.5 * torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64))
+        T = ps.empty(n, n, n, dtype=dt_np)
+        T.copy_(torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64).to(tdt))
+        T2, lam, Ci = T.clone(), ps.empty(n, n, n, dtype=dt_np), ps.ones(n, n, n, dtype=dt_np)
+        lam.copy_((1 + 0.5 * torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64)).to(tdt))
         dx = 10.0 / (n - 1)
-        for i in range(a.steps):
+        stream = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for i in range(a.steps + 1):
+            if i == 1:
+                e0.record(stream)
             src, dst = (T, T2) if i % 2 == 0 else (T2, T)
             ps.parallel(k, dst, src, Ci, lam, dx * dx / 1.5 / 8.1, 1 / dx, 1 / dx, 1 / dx, sync=False)
+        e1.record(stream)
         torch.cuda.synchronize()
-        print(json.dumps({"only_run": "jit", "n": n, "steps": a.steps}))
+        ms = e0.elapsed_time(e1) / max(1, a.steps)
+        print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps, "ms_per_step": round(ms, 4),
+                          "T_eff_GBs": round(WORDS_FLUX_LAM * n ** 3 * np.dtype(dt_np).itemsize / ms / 1e6, 1)}))
         return
     g = torch.Generator(device="cuda")
     g.manual_seed(2)
@@ -606,7 +678,7 @@ def main():
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
-    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit"], default=None,
+    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
                          "problem) and exit")

@@ -325,6 +325,15 @@ class _Gen:
         self.shared = {}   # @sharedMem array -> index
         self.kernel_language = False
         self.uses_collectives = False  # @sync_threads, shuffles, votes
+        self.table = None  # per-statement loads of an FD statement: (array, offsets) -> register
+        written = set()
+        for n in ast.walk(ast.Module(body=kd.body, type_ignores=[])):
+            if isinstance(n, ast.Assign):
+                for t in n.targets:
+                    if isinstance(t, ast.Subscript) and isinstance(t.value, ast.Name):
+                        written.add(t.slice.id if t.value.id.startswith("__lhs_") and isinstance(t.slice, ast.Name)
+                                    else t.value.id)
+        self.read_only = set(kd.arrays) - written  # read through the non-coherent cache (__ldg)
 
     # element of array `name` at 0-based integer index expressions (strings) per dimension
     def at(self, name, ix):
@@ -340,7 +349,33 @@ class _Gen:
         if name not in self.aidx:
             raise ArgumentError(f"unknown array {name}")
         t = ("tx", "ty", "tz")
+        if self.table is not None:  # FD statement: one register per distinct (array, offset)
+            key = (name, tuple(o[d] if d < self.nd else 0 for d in range(3)))
+            if key not in self.table:
+                self.table[key] = f"L{len(self.table)}"
+            return self.table[key]
         return self.load(name, [f"{t[d]}+{o[d]}" if o[d] else t[d] for d in range(self.nd)])
+
+    def fd_loads(self, p):
+        """Declarations of the statement's registered loads, and the bounds condition that covers
+        them all (per array: the stencil's largest offset in each dimension)."""
+        decl, box = [], {}
+        t3 = ("tx", "ty", "tz")
+        for (name, o), var in self.table.items():
+            k = self.aidx[name]
+            idx = [f"{t3[d]}+{o[d]}" if d < self.nd else "0" for d in range(3)]
+            ref = f"a{k}[({idx[0]}) + n{k}_0 * (({idx[1]}) + n{k}_1 * ({idx[2]}))]"
+            decl.append(f"{p}    const R {var} = " + (f"__ldg(&{ref});" if name in self.read_only else f"{ref};"))
+            lo, hi = box.setdefault(k, ([0] * 3, [0] * 3))
+            for d in range(self.nd):
+                lo[d], hi[d] = min(lo[d], o[d]), max(hi[d], o[d])
+        cond = []
+        for k, (lo, hi) in box.items():
+            for d in range(self.nd):
+                if lo[d] < 0:
+                    cond.append(f"{t3[d]} + {lo[d]} >= 0")
+                cond.append(f"{t3[d]} + {hi[d]} < n{k}_{d}")
+        return decl, " && ".join(cond)
 
     def macro(self, mname, name, off):
         if mname not in self.macros:
@@ -603,11 +638,12 @@ class _Gen:
     def load(self, name, ix):
         if name in self.shared:  # @sharedMem arrays are always bounds-checked (extents and the launch's shmem)
             return f"jl_lds({self.smem_ref(name, ix)}, g.err)"
+        ro = name in self.read_only
         if not self.checked:
-            return self.at(name, ix)
+            return f"__ldg(&{self.at(name, ix)})" if ro else self.at(name, ix)
         k = self.aidx[name]
         ix = list(ix) + ["0"] * (3 - len(ix))
-        return f"jl_ld(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)"
+        return f"jl_ld{'g' if ro else ''}(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)"
 
     # ---- local variables of @parallel_indices bodies (Julia function scope: declared at the top)
     def infer_locals(self, stmts):
@@ -720,7 +756,16 @@ class _Gen:
             t3 = ("tx", "ty", "tz")
             cond = " && ".join(f"{t3[d]} < n{k}_{d} - {2 * ((li >> d) & 1)}" for d in range(self.nd))
             idx = [f"{t3[d]}+{(li >> d) & 1}" for d in range(self.nd)]
-            return [f"{p}if ({cond}) {self.at(name, idx)} = {self.expr(s.value)};"]
+            self.table = {}
+            rhs = self.expr(s.value)
+            decl, box = self.fd_loads(p)
+            self.table = None
+            store = f"{p}    {self.at(name, idx)} = {rhs};"
+            if not self.checked or not box:
+                return [f"{p}if ({cond}) {{"] + decl + [store, f"{p}}}"]
+            # Julia's bounds check, once per statement: the whole stencil inside every array it reads
+            return [f"{p}if ({cond}) {{", f"{p}  if (!({box})) {{ atomicOr(g.err, 1); }} else {{"] + decl + \
+                [store, f"{p}  }}", f"{p}}}"]
         if isinstance(t, ast.Subscript):  # @parallel_indices: A[i, j] = expr
             name, ix = self.subscript(t)
             val = self.expr(s.value, ctx="real")
@@ -794,6 +839,9 @@ __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, 
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ R jl_ld(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
     if (jl_in(n0, n1, n2, i, j, k)) return a[i + n0 * (j + n1 * k)];
+    atomicOr(err, 1); return (R)0; }}
+__device__ __forceinline__ R jl_ldg(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
+    if (jl_in(n0, n1, n2, i, j, k)) return __ldg(&a[i + n0 * (j + n1 * k)]);
     atomicOr(err, 1); return (R)0; }}
 __device__ __forceinline__ void jl_st(R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err, R v) {{
     if (jl_in(n0, n1, n2, i, j, k)) a[i + n0 * (j + n1 * k)] = v; else atomicOr(err, 1); }}

@@ -163,10 +163,12 @@ def test_translator_generated_structure(jit):
     src = jit.generate(jit.parse(K.HEAT_FLUX), 3, "double")
     assert "extern \"C\" __global__ void ps_jit_entry(const ps_jit_args g)" in src
     assert "fx" not in src.split("ps_jit_entry")[1]  # the on-the-fly arrays are inlined
-    assert src.count("jl_ld(") > 10  # bounds-checked reads by default
+    body = src.split("ps_jit_entry")[1]
+    assert body.count("__ldg(") == 8  # the 8 distinct stencil points, each read once (read-only arrays)
+    assert "tx + 2 < n1_0" in body and "atomicOr(g.err, 1)" in body  # one bounds check per statement
     assert "tx < n0_0 - 2 && ty < n0_1 - 2 && tz < n0_2 - 2" in src  # @within("@inn", Tnew)
     src = jit.generate(jit.parse(K.SHIFT_INBOUNDS), 1, "float")
-    assert "typedef float R;" in src and "jl_ld(a" not in src and "jl_st(a" not in src
+    assert "typedef float R;" in src and "jl_ld(a" not in src and "jl_ldg(a" not in src and "jl_st(a" not in src
     src = jit.generate(jit.parse(K.BRANCHES2D), 2, "double")
     assert "const long long s0 = (long long)g.s[0];" in src and "pow(" in src
 
