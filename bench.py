@@ -348,8 +348,9 @@ def run_ours(a, world, rank, local):
             bench_kernel("diffusion3d_flux_lam_f32_plain", ps.kernels.diffusion3D_step_flux_lam, arrs32,
                          (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float32, a.steps)
             bench_kernel("memcopy3d_f32", ps.kernels.copy3D, arrs32, (), False, WORDS_MEMCOPY, n, np.float32, a.steps)
-            bench_kernel("diffusion3d_flux_lam_f32_jit", ps.parallel_kernel(JIT_FLUX_LAM.format(opt="")), arrs32,
-                         (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float32, a.steps)
+            for memopt, tag in ((False, "plain"), (True, "memopt")):
+                bench_kernel(f"diffusion3d_flux_lam_f32_jit_{tag}", ps.parallel_kernel(JIT_FLUX_LAM.format(opt="")),
+                             arrs32, (dt, _dx, _dx, _dx), memopt, WORDS_FLUX_LAM, n, np.float32, a.steps)
             del arrs32
             torch.cuda.empty_cache()
             n2 = 256
@@ -636,17 +637,22 @@ def only_run(a):
         lam.copy_((1 + 0.5 * torch.rand((n, n, n), generator=g, device="cuda", dtype=torch.float64)).to(tdt))
         dx = 10.0 / (n - 1)
         stream = torch.cuda.current_stream()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        for i in range(a.steps + 1):
-            if i == 1:
-                e0.record(stream)
-            src, dst = (T, T2) if i % 2 == 0 else (T2, T)
-            ps.parallel(k, dst, src, Ci, lam, dx * dx / 1.5 / 8.1, 1 / dx, 1 / dx, 1 / dx, sync=False)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / max(1, a.steps)
-        print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps, "ms_per_step": round(ms, 4),
-                          "T_eff_GBs": round(WORDS_FLUX_LAM * n ** 3 * np.dtype(dt_np).itemsize / ms / 1e6, 1)}))
+        res = {"only_run": a.only_run, "n": n, "steps": a.steps}
+        for memopt in (False, True):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            for i in range(a.steps + 1):
+                if i == 1:
+                    e0.record(stream)
+                src, dst = (T, T2) if i % 2 == 0 else (T2, T)
+                ps.parallel(k, dst, src, Ci, lam, dx * dx / 1.5 / 8.1, 1 / dx, 1 / dx, 1 / dx, sync=False,
+                            memopt=memopt, loopsize=a.loopsize)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / max(1, a.steps)
+            res["memopt" if memopt else "plain"] = {
+                "ms_per_step": round(ms, 4),
+                "T_eff_GBs": round(WORDS_FLUX_LAM * n ** 3 * np.dtype(dt_np).itemsize / ms / 1e6, 1)}
+        print(json.dumps(res))
         return
     g = torch.Generator(device="cuda")
     g.manual_seed(2)
@@ -677,6 +683,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--loopsize", type=int, default=0, help="z indices per thread of memopt run-time compiled kernels")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "

@@ -383,10 +383,10 @@ int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, 
  * contraction, and load it on the current device. `entry` is the extern "C" kernel, which takes
  * one argument block by value:
  *   struct { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err;
- *            long long smem; }
+ *            long long smem; long long zloop; }
  * (array pointers and extents, scalars, first thread index and thread counts per dimension, the
- * kernel's error flags -- one device int owned by the handle -- and the launch's dynamic shared
- * memory bytes).
+ * kernel's error flags -- one device int owned by the handle --, the launch's dynamic shared
+ * memory bytes and the z indices per thread of a z-sweep kernel).
  * Compile errors return PS_ERR_ARG with the compiler log in ps_last_error(). */
 int ps_jit_compile(const char* source, const char* entry, void** kernel);
 /* Launch a compiled kernel over count[0] x count[1] x count[2] threads starting at thread index
@@ -398,10 +398,12 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
 /* The same with explicit thread-block dimensions and dynamic shared memory bytes (up to 227 KB):
  * `@parallel nblocks nthreads shmem=... kernel!(...)` (src/ParallelKernel/parallel.jl:303-328,
  * 883-898). Kernels that use @sync_threads, warp shuffles or votes need count[d] to be a multiple of
- * threads[d]; a partial block leaves before its first barrier and the launch returns PS_ERR_ARG. */
+ * threads[d]; a partial block leaves before its first barrier and the launch returns PS_ERR_ARG.
+ * zloop > 1 (with threads[2] == 1) launches a z-sweep kernel (memopt, generated for it): each
+ * thread covers zloop consecutive z indices; 1 for every other kernel. */
 int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                      const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
-                     void* stream, int sync);
+                     int32_t zloop, void* stream, int sync);
 int ps_jit_destroy(void* kernel);
 
 /* ------------------------------------------------------------------------------------ */

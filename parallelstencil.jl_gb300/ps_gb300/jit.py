@@ -52,7 +52,7 @@ _lib.register("ps_jit_launch", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes
 _lib.register("ps_jit_launch_ex", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                    ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
-                                   ctypes.c_void_p, ctypes.c_int])
+                                   ctypes.c_int32, ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
 MAX_ARRAYS = MAX_SCALARS = 32
@@ -313,8 +313,13 @@ def _lit(v):
 
 
 class _Gen:
-    def __init__(self, kd: KernelDef, ndims: int):
+    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False):
         self.kd, self.nd = kd, ndims
+        # memopt: each thread sweeps g.zloop consecutive z indices and carries read-only stencil
+        # points it already holds to the next z (src/memopt.jl's register queue, in plain code)
+        self.zloop = bool(zloop) and kd.kind == "parallel" and ndims == 3
+        self.persist = []  # registers that live across the z sweep
+        self.nstmt = 0
         self.macros = MACROS[ndims]
         self.sels = LHS[ndims]
         self.aidx = {n: i for i, n in enumerate(kd.arrays)}
@@ -376,6 +381,36 @@ class _Gen:
                     cond.append(f"{t3[d]} + {lo[d]} >= 0")
                 cond.append(f"{t3[d]} + {hi[d]} < n{k}_{d}")
         return decl, " && ".join(cond)
+
+    def zloop_statement(self, p, cond, box, decl, store):
+        """An FD statement inside the z sweep: a read-only point whose z+1 neighbour was loaded at the
+        previous z comes from that register (valid while the statement ran at the previous z: its
+        mask and bounds conditions, once false along z, stay false)."""
+        j = self.nstmt
+        self.nstmt += 1
+        t3 = ("tx", "ty", "tz")
+        keys = self.table
+        loads, ups = [], []
+        for (name, o), var in keys.items():
+            k = self.aidx[name]
+            idx = [f"{t3[d]}+{o[d]}" for d in range(3)]
+            ref = f"a{k}[({idx[0]}) + n{k}_0 * (({idx[1]}) + n{k}_1 * ({idx[2]}))]"
+            ro = name in self.read_only
+            ld = f"__ldg(&{ref})" if ro else ref
+            nxt = (name, (o[0], o[1], o[2] + 1))
+            if ro and nxt in keys:
+                loads.append(f"{p}    const R {var} = pr{j} ? P{j}_{keys[nxt][1:]} : {ld};")
+            else:
+                loads.append(f"{p}    const R {var} = {ld};")
+            if ro and (name, (o[0], o[1], o[2] - 1)) in keys:
+                self.persist.append(f"    R P{j}_{var[1:]} = 0;")
+                ups.append(f"{p}    P{j}_{var[1:]} = {var};")
+        self.persist.append(f"    bool pr{j} = false;")
+        inner = loads + [store] + ups + [f"{p}    pr{j} = true;"]
+        if not self.checked or not box:
+            return [f"{p}if ({cond}) {{"] + inner + [f"{p}}} else pr{j} = false;"]
+        return [f"{p}if ({cond}) {{", f"{p}  if (!({box})) {{ atomicOr(g.err, 1); pr{j} = false; }} else {{"] + \
+            inner + [f"{p}  }}", f"{p}}} else pr{j} = false;"]
 
     def macro(self, mname, name, off):
         if mname not in self.macros:
@@ -759,8 +794,12 @@ class _Gen:
             self.table = {}
             rhs = self.expr(s.value)
             decl, box = self.fd_loads(p)
-            self.table = None
             store = f"{p}    {self.at(name, idx)} = {rhs};"
+            if self.zloop:
+                out = self.zloop_statement(p, cond, box, decl, store)
+                self.table = None
+                return out
+            self.table = None
             if not self.checked or not box:
                 return [f"{p}if ({cond}) {{"] + decl + [store, f"{p}}}"]
             # Julia's bounds check, once per statement: the whole stencil inside every array it reads
@@ -832,9 +871,20 @@ class _Gen:
     }"""
         else:
             guard = "    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) return;"
-        return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}) -- generated by ps_gb300.jit
+        zpre, zpost = "", ""
+        if self.zloop:  # blockDim.z == 1; block z covers g.zloop consecutive z indices
+            guard = "    if (ux >= g.cnt[0] || uy >= g.cnt[1]) return;"
+            zpre = "\n" + "\n".join(self.persist) + """
+    for (long long it_ = 0; it_ < g.zloop; ++it_) {
+    const long long uz = blockIdx.z * g.zloop + it_;
+    if (uz >= g.cnt[2]) break;
+    const long long tz = g.lo[2] + uz;"""
+            zpost = "    }"
+        pos = "const long long tx = g.lo[0] + ux, ty = g.lo[1] + uy" + ("" if self.zloop else ", tz = g.lo[2] + uz")
+        uzdecl = "" if self.zloop else "\n    const long long uz = blockIdx.z * (long long)blockDim.z + threadIdx.z;"
+        return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{', z sweep' if self.zloop else ''}) -- generated by ps_gb300.jit
 typedef {real} R;
-struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; }};
+struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long zloop; }};
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ R jl_ld(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
@@ -858,13 +908,13 @@ __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ?
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
 extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
     extern __shared__ __align__(16) unsigned char ps_smem[];
-    const long long ux = blockIdx.x * (long long)blockDim.x + threadIdx.x, uy = blockIdx.y * (long long)blockDim.y + threadIdx.y;
-    const long long uz = blockIdx.z * (long long)blockDim.z + threadIdx.z;
+    const long long ux = blockIdx.x * (long long)blockDim.x + threadIdx.x, uy = blockIdx.y * (long long)blockDim.y + threadIdx.y;{uzdecl}
 {guard}
-    const long long tx = g.lo[0] + ux, ty = g.lo[1] + uy, tz = g.lo[2] + uz;
-    (void)tx; (void)ty; (void)tz; (void)ps_smem;
-{chr(10).join(decl)}
+    {pos};
+    (void)ps_smem;
+{chr(10).join(decl)}{zpre}
 {chr(10).join(body)}
+{zpost}
 }}
 """
 
@@ -875,13 +925,14 @@ def _is_sel_assign(s):
         and isinstance(t.slice, ast.Name)
 
 
-def generate(kd: KernelDef, ndims: int, dtype: str) -> str:
-    """CUDA C of kernel `kd` for `ndims`-D arrays of `dtype` ("double" or "float")."""
-    return _Gen(kd, ndims).source(dtype)
+def generate(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False) -> str:
+    """CUDA C of kernel `kd` for `ndims`-D arrays of `dtype` ("double" or "float"); zloop: the memopt
+    variant (3-D `@parallel` kernels), each thread sweeping consecutive z indices."""
+    return _Gen(kd, ndims, zloop).source(dtype)
 
 
-def _generate_info(kd: KernelDef, ndims: int, dtype: str):
-    g = _Gen(kd, ndims)
+def _generate_info(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False):
+    g = _Gen(kd, ndims, zloop)
     src = g.source(dtype)
     return src, g.uses_collectives
 
@@ -907,22 +958,27 @@ class JitKernel:
     def source(self, ndims, dtype="double"):
         return generate(self.kd, ndims, dtype)
 
-    def _handle(self, ndims, dtype):
-        key = (ndims, dtype)
+    def _handle(self, ndims, dtype, zloop=False):
+        key = (ndims, dtype, bool(zloop))
         if key not in self._handles:
-            src, self._collective[key] = _generate_info(self.kd, ndims, dtype)
+            src, self._collective[key] = _generate_info(self.kd, ndims, dtype, zloop)
             h = ctypes.c_void_p()
             _lib.call("ps_jit_compile", src.encode(), b"ps_jit_entry", ctypes.byref(h))
             self._handles[key] = h
         return self._handles[key]
 
-    def __call__(self, *args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None):
-        self.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem)
+    def __call__(self, *args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None,
+                 memopt=None, loopsize=0):
+        self.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem, memopt=memopt,
+                        loopsize=loopsize)
 
-    def jit_launch(self, args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None):
+    def jit_launch(self, args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None,
+                   memopt=None, loopsize=0):
         """Launch over `ranges` (default: the largest array extents; with `nblocks`, nblocks .* nthreads
         threads) in blocks of `nthreads` (default (32, 8, 1)) with `shmem` bytes of dynamic shared
-        memory (src/ParallelKernel/parallel.jl:303-328)."""
+        memory (src/ParallelKernel/parallel.jl:303-328). memopt (default: the definition's
+        `memopt=`) runs 3-D `@parallel` kernels as z sweeps of `loopsize` (default 64, as
+        src/parallel.jl:532-543 for compute capability >= 9) indices per thread; same results."""
         require_initialized()
         if len(args) != self.nargs:
             raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
@@ -959,15 +1015,23 @@ class JitKernel:
             if min(lo) < 0:
                 raise ArgumentError("ranges must start at index 1 or above")
             cnt = [max(0, hi[d] - lo[d]) for d in range(3)]
-        h = self._handle(ndims, dt)
-        if self._collective[(ndims, dt)] and any(cnt[d] % threads[d] for d in range(3)):
+        want = memopt if memopt is not None else self.kd.options.get("memopt", "false") == "true"
+        zl = bool(want) and self.kd.kind == "parallel" and ndims == 3
+        zloop = 1
+        if zl:
+            zloop = int(loopsize or int(self.kd.options.get("loopsize", "0") or 0) or 64)  # 64: the reference's cc >= 9 default
+            if zloop < 1:
+                raise ArgumentError("loopsize must be positive")
+            threads[2] = 1
+        h = self._handle(ndims, dt, zl)
+        if self._collective[(ndims, dt, zl)] and any(cnt[d] % threads[d] for d in range(3)):
             raise ArgumentError("a kernel with @sync_threads, shuffles or votes needs ranges that are a multiple of "
                                 f"the thread block (ranges {cnt}, nthreads {threads})")
         A = (PSArray * max(1, len(descs)))(*descs)
         S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
         _lib.call("ps_jit_launch_ex", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
-                  (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), stream_handle(stream),
-                  int(bool(sync)))
+                  (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), zloop,
+                  stream_handle(stream), int(bool(sync)))
 
     def __del__(self):
         try:

@@ -218,3 +218,11 @@ EARLY_RETURN = """@parallel_indices (i) function clip_tail!(B, A, m::Integer)
     B[i] = 2.0*A[i]
     return
 end"""
+
+# two statements along z: the second reads (at its own index) what the first wrote, which the z
+# sweep must never carry in a register
+TWO3D = """@parallel function two3d!(A, C, B, s)
+    @all(A) = @d_za(B)*s + @av_zi(B)
+    @inn(C) = @inn(C) + @all(A)*@d2_zi(B)
+    return
+end"""

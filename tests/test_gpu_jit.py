@@ -214,7 +214,8 @@ def test_jit_c_abi_direct(ps):
     from ps_gb300.core import descriptor, stream_handle
 
     src = b"""
-struct ps_jit_args { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err; };
+struct ps_jit_args { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err;
+                     long long smem; long long zloop; };
 extern "C" __global__ void twice(const ps_jit_args g) {
     long long i = g.lo[0] + blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (threadIdx.y == 0 && i < g.lo[0] + g.cnt[0]) ((double*)g.a[0])[i] = g.s[0] * ((const double*)g.a[1])[i];
@@ -322,11 +323,68 @@ def test_jit_partial_blocks_with_barriers_are_refused(ps):
     k = ps.parallel_kernel(K.WARP_SUMS)
     with pytest.raises(ArgumentError, match="multiple of the thread block"):
         ps.parallel(k, S, A, nthreads=(64,))
-    h = k._handle(1, "double")
+    h = k._handle(1, "double")  # the handle the refused call compiled
     arrs = (PSArray * 2)(descriptor(S), descriptor(A))
     rc = _lib.load().ps_jit_launch_ex(h, arrs, 2, (ctypes.c_double * 1)(0.0), 0, (ctypes.c_int64 * 3)(0, 0, 0),
-                                      (ctypes.c_int64 * 3)(100, 1, 1), (ctypes.c_int32 * 3)(64, 1, 1), 0,
+                                      (ctypes.c_int64 * 3)(100, 1, 1), (ctypes.c_int32 * 3)(64, 1, 1), 0, 1,
                                       stream_handle(None), 1)
     assert rc == -1 and "multiple of the thread block" in _lib.last_error()
     ps.parallel(k, S, A, ranges=[(1, 64)], nthreads=(64,))  # a full block afterwards runs normally
     assert np.allclose(ps.to_host(S)[:2], a[:64].reshape(2, 32).sum(axis=1))
+
+
+# ---------------------------------------------------------------- memopt: z sweeps
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("name", ["HEAT_FLUX", "HEAT_LAP", "BLEND3D", "TWO3D", "FLUX_LAM"])
+def test_jit_memopt_z_sweep_is_bit_identical(ps, name, dt):
+    """memopt=true (z sweeps of 1, 3, 16 and 64 indices per thread, registers carried along z) gives
+    exactly the plain launch's result, on odd extents, with and without ranges."""
+    import bench
+
+    rng = np.random.default_rng(31)
+    n = (37, 33, 29)
+    src = bench.JIT_FLUX_LAM.format(opt="") if name == "FLUX_LAM" else getattr(K, name)
+    r = lambda *sh: _dev(ps, rng.standard_normal(sh).astype(dt))  # noqa: E731
+    p = lambda *sh: _dev(ps, (rng.random(sh) + 0.5).astype(dt))  # noqa: E731
+    if name == "BLEND3D":
+        ins, outs, sc = [r(*n), r(*n), p(*n)], [(n[0] - 2, n[1] - 2, n[2] - 2)], (0.3,)
+    elif name == "TWO3D":
+        ins, outs, sc = [r(*n)], [(n[0] - 2, n[1] - 2, n[2] - 1), n], (0.7,)
+    elif name == "FLUX_LAM":
+        ins, outs, sc = [r(*n), p(*n), p(*n)], [n], (1e-3, 9.0, 11.0, 13.0)
+    else:
+        ins, outs, sc = [r(*n), p(*n)], [n], (0.7, 1e-3, 9.0, 11.0, 13.0)
+    k = ps.parallel_kernel(src)
+
+    def launch(memopt, loopsize=0, ranges=None):
+        o = [ps.zeros(*sh, dtype=dt) for sh in outs]
+        if name == "TWO3D":
+            args = [o[0], o[1], ins[0], *sc]
+        else:
+            args = [*o, *ins, *sc]
+        ps.parallel(k, *args, memopt=memopt, loopsize=loopsize, ranges=ranges)
+        return [ps.to_host(x) for x in o]
+
+    ref = launch(False)
+    for ls in (1, 3, 16, 64):
+        got = launch(True, ls)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b), (name, ls)
+    box = [(2, 30), (3, 25), (4, 27)]
+    ref_box, got_box = launch(False, ranges=box), launch(True, 5, ranges=box)
+    for a, b in zip(got_box, ref_box):
+        assert np.array_equal(a, b), (name, "ranges")
+
+
+def test_jit_memopt_from_the_definition(ps):
+    """`@parallel memopt=true loopsize=3 function ...` selects the z sweep by itself."""
+    src = K.HEAT_LAP.replace("@parallel function", "@parallel memopt=true loopsize=3 function")
+    k = ps.parallel_kernel(src)
+    assert k.kd.options == {"memopt": "true", "loopsize": "3"}
+    rng = np.random.default_rng(2)
+    T, Ci = _dev(ps, rng.random((40, 21, 19))), _dev(ps, rng.random((40, 21, 19)) + 0.5)
+    A, B = ps.zeros(40, 21, 19), ps.zeros(40, 21, 19)
+    ps.parallel(k, A, T, Ci, 0.7, 1e-3, 9.0, 11.0, 13.0)
+    ps.parallel(ps.kernels.diffusion3D_step_inv, B, T, Ci, 0.7, 1e-3, 9.0, 11.0, 13.0, memopt=False)
+    assert np.array_equal(ps.to_host(A), ps.to_host(B))
+    assert (3, "double", True) in k._handles

@@ -192,6 +192,12 @@ def test_generated_sources_compile_for_sm103a(jit, tmp_path):
             procs.append((f, subprocess.Popen([_nvcc(), "-arch=sm_103a", "-std=c++17", "--fmad=false", "-c", str(f),
                                                "-o", str(f) + ".o"], stdout=subprocess.PIPE,
                                               stderr=subprocess.STDOUT, text=True)))
+            if real == "double" and ndims == 3 and src.lstrip().startswith("@parallel function"):
+                fz = tmp_path / f"{name}_zloop.cu"  # the memopt (z sweep) variant
+                fz.write_text(jit.generate(jit.parse(src), 3, "double", zloop=True))
+                procs.append((fz, subprocess.Popen([_nvcc(), "-arch=sm_103a", "-std=c++17", "--fmad=false", "-c",
+                                                    str(fz), "-o", str(fz) + ".o"], stdout=subprocess.PIPE,
+                                                   stderr=subprocess.STDOUT, text=True)))
             if len(procs) % 8 == 0:
                 for _, p in procs[-8:]:
                     p.wait()
@@ -265,3 +271,12 @@ def test_interpreter_loops_and_block_ids(jr):
     i, j, k = np.meshgrid(np.arange(16), np.arange(8), np.arange(4), indexing="ij")
     exp = (i // 8 + 1) + 10 * (j // 4 + 1) + 100 * (k // 2 + 1) + 1000 * ((i % 8 + 1) + (j % 4 + 1) * 8) + 0.5 * 2
     assert np.array_equal(X, exp)
+
+
+def test_translator_z_sweep_carries_only_read_only_points(jit):
+    src = jit.generate(jit.parse(K.TWO3D), 3, "double", zloop=True)
+    body = src.split("ps_jit_entry")[1]
+    assert "for (long long it_ = 0; it_ < g.zloop; ++it_)" in body
+    carried = re.findall(r"const R (L\d+) = pr(\d) \? P\d_\d+ : (.*?);", body)
+    assert carried and all("a2[" in ld for _, _, ld in carried)  # only B (argument 2) is read-only
+    assert "a0[" not in "".join(ld for _, _, ld in carried)  # A is written by the first statement
