@@ -134,6 +134,29 @@ def dist_setup():
     return world, rank, local
 
 
+def rank_ops(torch, dist, device):
+    """barrier() and max_over_ranks(x) of the replica runs: every rank times its own replica and the
+    job's time is the slowest rank's (NCCL between GPUs; gloo in the CPU tests of this path)."""
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def job_value(world, units_per_rank, seconds):
+    """Whole-job throughput of `world` replicas: the units all ranks processed over the slowest
+    rank's time (weak scaling: per-rank work fixed)."""
+    return world * units_per_rank / seconds
+
+
 def time_steps(torch, step_fn, steps, warmup, barrier, stream):
     for i in range(warmup):
         step_fn(i)
@@ -165,16 +188,7 @@ def run_ours(a, world, rank, local):
 
         dist.init_process_group("nccl")
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = rank_ops(torch, dist, "cuda")
 
     ps.init_parallel_stencil(ps.GB300, "Float64", 3, device=local)
     stream = torch.cuda.current_stream()
@@ -359,7 +373,35 @@ def run_ours(a, world, rank, local):
                          (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n2, np.float64, a.steps, fp64="split")
             bench_kernel("memcopy3d_f64_256", ps.kernels.copy3D, arrs256, (), False, WORDS_MEMCOPY, n2, np.float64,
                          a.steps)
-            del arrs256
+            dx2 = 10.0 / (n2 - 1)
+            sc2 = (dx2 * dx2 / 1.5 / 8.1, 1 / dx2, 1 / dx2, 1 / dx2)
+            bench_run("diffusion3d_flux_lam_f64_split_grid_run_256", ps.kernels.diffusion3D_step_flux_lam, arrs256,
+                      sc2, WORDS_FLUX_LAM, n2, np.float64, a.steps, "split_grid")
+            bench_kernel("diffusion3d_flux_lam_f64_ieee_memopt_256", ps.kernels.diffusion3D_step_flux_lam, arrs256,
+                         sc2, True, WORDS_FLUX_LAM, n2, np.float64, ieee_steps)
+            bench_kernel("diffusion3d_flux_lam_f64_ieee_plain_256", ps.kernels.diffusion3D_step_flux_lam, arrs256,
+                         sc2, False, WORDS_FLUX_LAM, n2, np.float64, ieee_steps)
+            # FP32 fields: error after 50 steps against the IEEE FP64 run (bit-identical to the oracle)
+            # from the same initial state
+            T, T2, lam, Ci = fields(np.float64, n2)
+            ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, T, T2, Ci, lam, *sc2, 50, fp64="ieee")
+            ref = T.clone()
+            del T, T2, lam, Ci
+            arrs256_32 = fields(np.float32, n2)
+            T, T2, lam, Ci = arrs256_32
+            ps.kernels.run(ps.kernels.diffusion3D_step_flux_lam, T, T2, Ci, lam, *sc2, 50)
+            fp32_err = float((T.double() - ref).abs().max() / ref.abs().max())
+            launches += 100
+            del ref
+            arrs256_32 = fields(np.float32, n2)
+            bench_kernel("diffusion3d_flux_lam_f32_memopt_256", ps.kernels.diffusion3D_step_flux_lam, arrs256_32,
+                         sc2, True, WORDS_FLUX_LAM, n2, np.float32, a.steps)
+            bench_kernel("diffusion3d_flux_lam_f32_plain_256", ps.kernels.diffusion3D_step_flux_lam, arrs256_32,
+                         sc2, False, WORDS_FLUX_LAM, n2, np.float32, a.steps)
+            bench_kernel("memcopy3d_f32_256", ps.kernels.copy3D, arrs256_32, (), False, WORDS_MEMCOPY, n2, np.float32,
+                         a.steps)
+            results["fp32_rel_err_vs_fp64_50_steps_256"] = fp32_err
+            del arrs256, arrs256_32
         if not a.quick:
             gemm = bench_gemm(torch)
             results["nn_gemm_bf16_8192"] = gemm
@@ -376,7 +418,7 @@ def run_ours(a, world, rank, local):
             launches += adj.pop("launches")
     clocks = clk.summary()
 
-    value = world * b_head / t_head / 1e9
+    value = job_value(world, b_head, t_head) / 1e9
     e2e_bytes = NT_JOB * b_head
     out = {
         "metric": "T_eff", "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": a.steps,
@@ -395,7 +437,7 @@ def run_ours(a, world, rank, local):
                      "frac": round((b_head / t_head / 1e9) / peak, 4), "peak_kind": f"{peak_kind} hbm_gbs (burst)",
                      "traffic": ncu_traffic("diffusion3d_grid_flux_lam_f64_512"),
                      "kernel": "diff3d_grid_tma<LAM,ISO>", "algorithmic_bytes_per_launch": b_head},
-        "e2e": {"value": round(world * e2e_bytes / t_e2e / 1e9, 2), "unit": "GB/s",
+        "e2e": {"value": round(job_value(world, e2e_bytes, t_e2e) / 1e9, 2), "unit": "GB/s",
                 "h2d_bytes_per_step": 4 * n ** 3 * 8, "d2h_bytes_per_step": n ** 3 * 8,
                 "step": f"one {NT_JOB}-step diffusion job from pinned host buffers through the C ABI",
                 "seconds_per_job": round(t_e2e, 5)},
