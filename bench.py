@@ -416,6 +416,9 @@ def run_ours(a, world, rank, local):
         adj = None if a.quick else bench_adjoint(ps, torch)
         if adj:
             launches += adj.pop("launches")
+        mini = None if a.quick else bench_miniapps(ps, torch, peak)
+        if mini:
+            launches += mini.pop("launches")
     clocks = clk.summary()
 
     value = job_value(world, b_head, t_head) / 1e9
@@ -445,6 +448,7 @@ def run_ours(a, world, rank, local):
         "stokes2d_time_to_tol": stokes,
         "warm_start_time_to_tol": warm,
         "adjoint_gradient": adj,
+        "miniapps": mini,
         "clocks": clocks,
         "variants": results,
     }
@@ -527,6 +531,77 @@ def bench_warm_start(seeds, n=1023, tol=1e-8):
         out[name] = r
     out["mixed_warm_over_fp64_zero"] = round(out["mixed"]["seconds_warm"] / out["fp64"]["seconds_zero"], 4)
     net.close()
+    return out
+
+
+def _events(torch, fn, reps):
+    """Seconds per call of fn() over `reps` calls (CUDA events on the current stream, after 3 warm-ups)."""
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def bench_miniapps(ps, torch, peak):
+    """T_eff of the miniapp iterations with each miniapp's own A_eff (words per cell per iteration):
+    Stokes2D 6 (Stokes2D.jl:128) at 1023^2, Stokes3D 8 (Stokes3D.jl:154) at 127^3 (the miniapp's
+    default) and 255^3, acoustic3D 8 (acoustic3D.jl:62) at 255^3 (its default); FP64 IEEE and FP32.
+    Fused iterations (one launch for Stokes2D, three for Stokes3D) and the miniapp's own launch
+    sequence with a synchronisation after each launch, as `@parallel` does (6 / 10 / 2 launches)."""
+    from ps_gb300 import stokes, stokes3d
+
+    out, launches = {}, 0
+    for dt, tag in ((np.float64, "f64"), (np.float32, "f32")):
+        es = np.dtype(dt).itemsize
+        n = 1023
+        Mus, Rog = stokes.inclusion_setup(n, n, 1.0, 1.0, musi=0.1, radius=0.1, dtype=dt)
+        g = stokes.Stokes2D(stokes.Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog, dtype=dt)
+        g.compute_timesteps()
+        t = _events(torch, lambda: g.iterate(20), 5) / 20
+        t1 = _events(torch, g.step_reference_sequence, 20)
+        out[f"stokes2d_{n}_{tag}"] = {"fused_ms": round(t * 1e3, 4), "T_eff_GBs": round(6 * es * n * n / t / 1e9, 1),
+                                      "six_kernels_ms": round(t1 * 1e3, 4),
+                                      "six_kernels_T_eff_GBs": round(6 * es * n * n / t1 / 1e9, 1)}
+        launches += 8 * 20 + 23 * 6
+        del g
+        for n in (127, 255):
+            Mus, Rog = stokes3d.inclusion_setup(n, n, n, dtype=dt)
+            g = stokes3d.Stokes3D(stokes3d.Stokes3DParams(n, n, n), Mus, Rog, dtype=dt)
+            g.compute_timesteps()
+            t = _events(torch, lambda: g.iterate(10), 3) / 10
+            t1 = _events(torch, g.step_reference_sequence, 10)
+            out[f"stokes3d_{n}_{tag}"] = {"fused_ms": round(t * 1e3, 4),
+                                          "T_eff_GBs": round(8 * es * n ** 3 / t / 1e9, 1),
+                                          "miniapp_sequence_ms": round(t1 * 1e3, 4),
+                                          "miniapp_sequence_T_eff_GBs": round(8 * es * n ** 3 / t1 / 1e9, 1)}
+            launches += 6 * 10 * 3 + 13 * 10
+            del g
+        n = 255
+        lx = 40.0
+        h = lx / (n - 1)
+        P = ps.zeros(n, n, n, dtype=dt)
+        Vx, Vy, Vz = ps.zeros(n + 1, n, n, dtype=dt), ps.zeros(n, n + 1, n, dtype=dt), ps.zeros(n, n, n + 1, dtype=dt)
+        ps.fill_(P, 1.0)
+        dts = h / 6.1
+
+        def acoustic_step():
+            ps.parallel(ps.kernels.acoustic3D_compute_V, Vx, Vy, Vz, P, dts, 1.0, h, h, h, sync=False)
+            ps.parallel(ps.kernels.acoustic3D_compute_P, P, Vx, Vy, Vz, dts, 1.0, h, h, h, sync=False)
+
+        t = _events(torch, acoustic_step, 50)
+        out[f"acoustic3d_{n}_{tag}"] = {"ms": round(t * 1e3, 4), "T_eff_GBs": round(8 * es * n ** 3 / t / 1e9, 1)}
+        launches += 2 * 53
+        del P, Vx, Vy, Vz
+    torch.cuda.empty_cache()
+    out["peak_hbm_gbs"] = peak
+    out["launches"] = launches
     return out
 
 
@@ -668,6 +743,38 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": "gemm", "n": n, "steps": a.steps}))
         return
+    if a.only_run in ("stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint"):  # --steps calls, size --n
+        from ps_gb300 import adjoint, stokes, stokes3d
+
+        if a.only_run == "stokes2d":  # fused PT iteration, FP64, n^2
+            Mus, Rog = stokes.inclusion_setup(n, n, 1.0, 1.0, musi=0.1, radius=0.1)
+            g = stokes.Stokes2D(stokes.Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog)
+            g.compute_timesteps()
+            g.iterate(a.steps)
+        elif a.only_run == "stokes3d":  # three-launch PT iteration, FP64, n^3
+            Mus, Rog = stokes3d.inclusion_setup(n, n, n)
+            g = stokes3d.Stokes3D(stokes3d.Stokes3DParams(n, n, n), Mus, Rog)
+            g.compute_timesteps()
+            g.iterate(a.steps)
+        elif a.only_run == "acoustic3d":
+            h = 40.0 / (n - 1)
+            P = ps.ones(n, n, n)
+            Vx, Vy, Vz = ps.zeros(n + 1, n, n), ps.zeros(n, n + 1, n), ps.zeros(n, n, n + 1)
+            for _ in range(a.steps):
+                ps.parallel(ps.kernels.acoustic3D_compute_V, Vx, Vy, Vz, P, h / 6.1, 1.0, h, h, h, sync=False)
+                ps.parallel(ps.kernels.acoustic3D_compute_P, P, Vx, Vy, Vz, h / 6.1, 1.0, h, h, h, sync=False)
+        elif a.only_run == "memcopy":
+            T, Ci, T2 = ps.ones(n, n, n), ps.ones(n, n, n), ps.zeros(n, n, n)
+            for _ in range(a.steps):
+                ps.parallel(ps.kernels.copy3D, T2, T, Ci, sync=False)
+        else:  # one adjoint step of the flux-lam diffusion step, FP64, n^3
+            T, Ci, lam = ps.ones(n, n, n), ps.ones(n, n, n), ps.fill(1.5, n, n, n)
+            lt, lt2, gl = ps.zeros(n, n, n), ps.ones(n, n, n), ps.zeros(n, n, n)
+            for _ in range(a.steps):
+                adjoint.adjoint_step(lt, lt2, T, Ci, lam, gl, 1e-4, 1.0, 1.0, 1.0, sync=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
+        return
     if a.only_run in ("jit", "jit32"):  # the headline body, run-time compiled (IEEE, bounds-checked), --steps steps
         dt_np = np.float32 if a.only_run == "jit32" else np.float64
         tdt = torch.float32 if a.only_run == "jit32" else torch.float64
@@ -727,7 +834,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--loopsize", type=int, default=0, help="z indices per thread of memopt run-time compiled kernels")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
-    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32"], default=None,
+    ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
+                                                 "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
                          "problem) and exit")
