@@ -419,6 +419,9 @@ def run_ours(a, world, rank, local):
         mini = None if a.quick else bench_miniapps(ps, torch, peak)
         if mini:
             launches += mini.pop("launches")
+        s3solve = None if a.quick else bench_stokes3d_solve(ps)
+        if s3solve:
+            launches += s3solve.pop("launches")
     clocks = clk.summary()
 
     value = job_value(world, b_head, t_head) / 1e9
@@ -449,6 +452,7 @@ def run_ours(a, world, rank, local):
         "warm_start_time_to_tol": warm,
         "adjoint_gradient": adj,
         "miniapps": mini,
+        "stokes3d_time_to_tol": s3solve,
         "clocks": clocks,
         "variants": results,
     }
@@ -602,6 +606,26 @@ def bench_miniapps(ps, torch, peak):
     torch.cuda.empty_cache()
     out["peak_hbm_gbs"] = peak
     out["launches"] = launches
+    return out
+
+
+def bench_stokes3d_solve(ps, n=127, tol=1e-6):
+    """The Stokes3D miniapp's solve (127^3, its inclusion, ε = 1e-6, Stokes3D.jl:73-84): wall time
+    to err < tol for the FP64 PT solver and for FP32 sweeps with FP64 defect correction."""
+    from ps_gb300 import stokes3d
+
+    out = {"config": f"{n}^3, the miniapp's setup (lx = 10, inclusion r = 1, viscosity 0.1, rho*g = 1), "
+                     f"err = max(mean|Rx|, mean|Ry|, mean|Rz|, mean|divV|) < {tol}, nout 500"}
+    for mode, name in ((0, "fp64"), (1, "mixed")):
+        Mus, Rog = stokes3d.inclusion_setup(n, n, n)
+        g = stokes3d.Stokes3D(stokes3d.Stokes3DParams(n, n, n), Mus, Rog)
+        g.compute_timesteps()
+        st = g.solve(tol=tol, nout=500, max_iter=400_000, max_seconds=120, mode=mode)
+        out[name] = {"seconds": round(st.seconds, 4), "iterations": int(st.iters), "outer": int(st.outer),
+                     "err": float(st.err), "converged": bool(st.converged)}
+        del g
+    out["mixed_over_fp64"] = round(out["mixed"]["seconds"] / out["fp64"]["seconds"], 4)
+    out["launches"] = 3 * (out["fp64"]["iterations"] + out["mixed"]["iterations"])
     return out
 
 

@@ -372,6 +372,14 @@ int ps_stokes3d_err(const ps_stokes3d_fields* f, double out_mean_abs[4], void* s
  * max_seconds (> 0), PS_ERR_NONFINITE on NaN/Inf residuals. */
 int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, double tol, int64_t max_iter,
                       int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
+/* The same solve in mixed precision (no counterpart in the reference; the Stokes3D form of
+ * ps_stokes2d_solve mode 1): FP32 PT sweeps on a correction with the FP64 residual of the state as
+ * source, FP64 residual (the reference's statements), FP64 update and convergence check with the
+ * reference's err. Uses library-owned FP32 scratch (26 arrays of the grid's size); stats->outer
+ * counts the FP64 corrections, stats->iters the FP32 sweeps. On return Rx, Ry, Rz, divV and the
+ * stresses hold the FP64 residual of the returned state. */
+int ps_stokes3d_solve_mixed(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, double tol, int64_t max_iter,
+                            int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Run-time compiled kernels: any `@parallel` body of FiniteDifferences macros, or a       */

@@ -46,8 +46,14 @@ struct S3A {
     T *Pt, *dtPt, *divV, *Vx, *Vy, *Vz, *txx, *tyy, *tzz, *txy, *txz, *tyz, *Rx, *Ry, *Rz, *dVx, *dVy, *dVz, *dtVx,
         *dtVy, *dtVz;
     const T *Mus, *Rog;
+    const T *fx, *fy, *fz, *fp;  // mode S3_DEFECT: FP64 residual of the outer state, rounded to T
     int64_t nx, ny, nz;
 };
+
+// Modes of the iteration kernels: the reference's iteration; the inner sweep of the mixed-precision
+// solver (PT on a correction: the outer state's residual is the source, buoyancy included in it);
+// the residual alone (no pseudo-time update) of the FP64 outer state.
+enum { S3_PLAIN = 0, S3_DEFECT = 1, S3_RESIDUAL = 2 };
 
 #define I3(a, b, c, n0, n1) ((int64_t)(a) + (int64_t)(n0) * ((int64_t)(b) + (int64_t)(n1) * (int64_t)(c)))
 
@@ -114,7 +120,7 @@ __device__ __forceinline__ void s3_tyz(const S3A<T>& a, const S3P<T>& p, int64_t
 
 // compute_dV! statements at residual index (x, y, z) and, with update_V, compute_V! at the same
 // index (it reads only the pseudo-velocity just written)
-template <typename T>
+template <typename T, int MODE = S3_PLAIN>
 __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z,
                                       bool update_V) {
     const int64_t nx = a.nx, ny = a.ny, nz = a.nz;
@@ -125,13 +131,16 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
         const T B = a.txy[I3(x, y + 1, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
         const T C = a.txz[I3(x, y, z + 1, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
         const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x, y + 1, z + 1, nx, ny)];
-        const T R = ((A / p.dx + B / p.dy) + C / p.dz) - P / p.dx;
+        T R = ((A / p.dx + B / p.dy) + C / p.dz) - P / p.dx;
+        if constexpr (MODE == S3_DEFECT) R = R + a.fx[r];
         a.Rx[r] = R;
-        const T dv = p.dampX * a.dVx[r] + R;
-        a.dVx[r] = dv;
-        if (update_V) {
-            const int64_t v = I3(x + 1, y + 1, z + 1, nx + 1, ny);
-            a.Vx[v] = a.Vx[v] + a.dtVx[r] * dv;
+        if constexpr (MODE != S3_RESIDUAL) {
+            const T dv = p.dampX * a.dVx[r] + R;
+            a.dVx[r] = dv;
+            if (update_V) {
+                const int64_t v = I3(x + 1, y + 1, z + 1, nx + 1, ny);
+                a.Vx[v] = a.Vx[v] + a.dtVx[r] * dv;
+            }
         }
     }
     if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
@@ -140,13 +149,16 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
         const T B = a.txy[I3(x + 1, y, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
         const T C = a.tyz[I3(x, y, z + 1, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
         const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y, z + 1, nx, ny)];
-        const T R = ((A / p.dy + B / p.dx) + C / p.dz) - P / p.dy;
+        T R = ((A / p.dy + B / p.dx) + C / p.dz) - P / p.dy;
+        if constexpr (MODE == S3_DEFECT) R = R + a.fy[r];
         a.Ry[r] = R;
-        const T dv = p.dampY * a.dVy[r] + R;
-        a.dVy[r] = dv;
-        if (update_V) {
-            const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny + 1);
-            a.Vy[v] = a.Vy[v] + a.dtVy[r] * dv;
+        if constexpr (MODE != S3_RESIDUAL) {
+            const T dv = p.dampY * a.dVy[r] + R;
+            a.dVy[r] = dv;
+            if (update_V) {
+                const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny + 1);
+                a.Vy[v] = a.Vy[v] + a.dtVy[r] * dv;
+            }
         }
     }
     if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
@@ -155,14 +167,21 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
         const T B = a.txz[I3(x + 1, y, z, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
         const T C = a.tyz[I3(x, y + 1, z, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
         const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y + 1, z, nx, ny)];
-        const T G = (a.Rog[I3(x + 1, y + 1, z, nx, ny)] + a.Rog[I3(x + 1, y + 1, z + 1, nx, ny)]) * T(0.5);
-        const T R = (((A / p.dz + B / p.dx) + C / p.dy) - P / p.dz) + G;
+        T R;
+        if constexpr (MODE == S3_DEFECT) {  // the buoyancy is part of the outer residual fz
+            R = (((A / p.dz + B / p.dx) + C / p.dy) - P / p.dz) + a.fz[r];
+        } else {
+            const T G = (a.Rog[I3(x + 1, y + 1, z, nx, ny)] + a.Rog[I3(x + 1, y + 1, z + 1, nx, ny)]) * T(0.5);
+            R = (((A / p.dz + B / p.dx) + C / p.dy) - P / p.dz) + G;
+        }
         a.Rz[r] = R;
-        const T dv = p.dampZ * a.dVz[r] + R;
-        a.dVz[r] = dv;
-        if (update_V) {
-            const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny);
-            a.Vz[v] = a.Vz[v] + a.dtVz[r] * dv;
+        if constexpr (MODE != S3_RESIDUAL) {
+            const T dv = p.dampZ * a.dVz[r] + R;
+            a.dVz[r] = dv;
+            if (update_V) {
+                const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny);
+                a.Vz[v] = a.Vz[v] + a.dtVz[r] * dv;
+            }
         }
     }
 }
@@ -273,13 +292,19 @@ __global__ void s3_bc_axis_k(T* A, int64_t n0, int64_t n1, int64_t n2, int ax) {
 // ---- iteration kernels ---------------------------------------------------------------------
 // compute_P! and compute_τ! of cell (x, y, z): τxx, τyy, τzz are written at the index whose ∇V
 // is this cell's, τxy, τxz, τyz at the cell's own index.
-template <typename T>
+template <typename T, int MODE = S3_PLAIN>
 __global__ void s3_Ptau_k(S3A<T> a, S3P<T> p) {
     S3_IDX;
     const int64_t c = I3(x, y, z, nx, ny);
     const T d = s3_divV(a, p, x, y, z);
-    a.divV[c] = d;
-    a.Pt[c] = a.Pt[c] - a.dtPt[c] * d;
+    if constexpr (MODE == S3_DEFECT) {  // the correction's continuity residual includes the outer one
+        const T dp = d + a.fp[c];
+        a.divV[c] = dp;
+        a.Pt[c] = a.Pt[c] - a.dtPt[c] * dp;
+    } else {
+        a.divV[c] = d;
+        if constexpr (MODE == S3_PLAIN) a.Pt[c] = a.Pt[c] - a.dtPt[c] * d;
+    }
     const T m = a.Mus[c];
     const bool iy = y >= 1 && y <= ny - 2, iz = z >= 1 && z <= nz - 2, ix = x >= 1 && x <= nx - 2;
     if (iy && iz)
@@ -296,10 +321,10 @@ __global__ void s3_Ptau_k(S3A<T> a, S3P<T> p) {
     if (x < nx - 2 && y < ny - 1 && z < nz - 1) s3_tyz(a, p, x, y, z);
 }
 
-template <typename T>
+template <typename T, int MODE = S3_PLAIN>
 __global__ void s3_dVV_k(S3A<T> a, S3P<T> p) {
     S3_IDX;
-    s3_dV(a, p, x, y, z, true);
+    s3_dV<T, MODE>(a, p, x, y, z, true);
 }
 
 // The loop body's six copies (bc_x!(Vy), bc_x!(Vz), bc_y!(Vx), bc_y!(Vz), bc_z!(Vx), bc_z!(Vy)):
@@ -326,6 +351,17 @@ __global__ void s3_bc_k(S3A<T> a) {
         s[ax1] = s[ax1] < 1 ? 1 : s[ax1] > n[ax1] - 2 ? n[ax1] - 2 : s[ax1];
         A[I3(i[0], i[1], i[2], n[0], n[1])] = A[I3(s[0], s[1], s[2], n[0], n[1])];
     }
+}
+
+// y32 = (float) x64 (rounding of the outer residual for the FP32 sweeps)
+__global__ void s3_to_f32(float* y, const double* x, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (float)x[i];
+}
+// x64 += (double) d32 (FP64 update of the outer state with the FP32 correction)
+__global__ void s3_axpy32(double* x, const float* d, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += (double)d[i];
 }
 
 __device__ __forceinline__ double s3_warp_sum(double v) {
@@ -392,6 +428,7 @@ template <typename T>
 static S3A<T> s3a(const ps_stokes3d_fields* f) {
     auto P = [](const ps_array& a) { return static_cast<T*>(a.ptr); };
     S3A<T> a;
+    a.fx = a.fy = a.fz = a.fp = nullptr;
     a.Pt = P(f->Pt);
     a.dtPt = P(f->dtauPt);
     a.divV = P(f->divV);
@@ -458,6 +495,21 @@ static void s3_iteration(const S3A<T>& a, const S3P<T>& p, cudaStream_t s) {
     s3_launch(S3_BC, a, p, s);
 }
 
+// the inner sweep of the mixed-precision solver (FP32 PT on the correction)
+static void s3_defect_iteration(const S3A<float>& a, const S3P<float>& p, cudaStream_t s) {
+    const dim3 b(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
+    s3_Ptau_k<float, S3_DEFECT><<<gc, b, 0, s>>>(a, p);
+    s3_dVV_k<float, S3_DEFECT><<<gc, b, 0, s>>>(a, p);
+    s3_launch(S3_BC, a, p, s);
+}
+
+// divV, the stresses and Rx, Ry, Rz of the FP64 state (the reference's statements, no update)
+static void s3_residual(const S3A<double>& a, const S3P<double>& p, cudaStream_t s) {
+    const dim3 b(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
+    s3_Ptau_k<double, S3_RESIDUAL><<<gc, b, 0, s>>>(a, p);
+    s3_dVV_k<double, S3_RESIDUAL><<<gc, b, 0, s>>>(a, p);
+}
+
 static int s3_entry(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, S3Kernel k, void* stream, int sync,
                     const char* what) {
     DeviceState* st = nullptr;
@@ -474,6 +526,143 @@ static int s3_entry(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, S3
 
 static double now_s3() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Mixed precision (the precision extension of the PT solvers, as ps_stokes2d_solve mode 1): FP32 PT
+// sweeps on the correction (δV, δP) with the FP64 residual of the outer state as source; FP64
+// residual, update and convergence check. The outer residual uses the reference's FP64 statements
+// (S3_RESIDUAL kernels) on the caller's arrays, so the final err is the reference's err of the
+// returned state.
+static int solve_mixed3(const ps_stokes3d_fields* f, const ps_stokes3d_params* pp, double tol, int64_t max_iter,
+                        int64_t nout, double max_seconds, double inner_rtol, double* red, ps_solve_stats* st,
+                        cudaStream_t s) {
+    const int64_t nx = f->Pt.n[0], ny = f->Pt.n[1], nz = f->Pt.n[2];
+    const int64_t nC = nx * ny * nz, nVx = (nx + 1) * ny * nz, nVy = nx * (ny + 1) * nz, nVz = nx * ny * (nz + 1);
+    const int64_t nRx = (nx - 1) * (ny - 2) * (nz - 2), nRy = (nx - 2) * (ny - 1) * (nz - 2),
+                  nRz = (nx - 2) * (ny - 2) * (nz - 1);
+    // float buffers, in this order: δVx δVy δVz δP dVx dVy dVz (zeroed before every inner sweep),
+    // txx tyy tzz txy txz tyz divV Rx Ry Rz, dtPt dtVx dtVy dtVz Mus, fx fy fz fp
+    const int64_t cnt[26] = {nVx, nVy, nVz, nC, nRx, nRy, nRz,
+                             numel(f->txx), numel(f->tyy), numel(f->tzz), numel(f->txy), numel(f->txz), numel(f->tyz),
+                             nC, nRx, nRy, nRz, nC, nRx, nRy, nRz, nC, nRx, nRy, nRz, nC};
+    size_t off[27];
+    off[0] = 0;
+    for (int k = 0; k < 26; k++) off[k + 1] = off[k] + ((cnt[k] * 4 + 255) / 256) * 256;
+    float* base = nullptr;
+    PS_CUDA_TRY(cudaMalloc(&base, off[26]));
+    auto F = [&](int k) { return reinterpret_cast<float*>(reinterpret_cast<char*>(base) + off[k]); };
+    S3A<float> a;
+    a.Vx = F(0); a.Vy = F(1); a.Vz = F(2); a.Pt = F(3);
+    a.dVx = F(4); a.dVy = F(5); a.dVz = F(6);
+    a.txx = F(7); a.tyy = F(8); a.tzz = F(9); a.txy = F(10); a.txz = F(11); a.tyz = F(12);
+    a.divV = F(13); a.Rx = F(14); a.Ry = F(15); a.Rz = F(16);
+    a.dtPt = F(17); a.dtVx = F(18); a.dtVy = F(19); a.dtVz = F(20);
+    a.Mus = F(21); a.Rog = nullptr;
+    a.fx = F(22); a.fy = F(23); a.fz = F(24); a.fp = F(25);
+    a.nx = nx; a.ny = ny; a.nz = nz;
+    const S3P<float> p32 = s3p<float>(*pp);
+    const S3P<double> p64 = s3p<double>(*pp);
+    const S3A<double> a64 = s3a<double>(f);
+    int rc = PS_OK;
+    cudaError_t e = cudaMemsetAsync(base, 0, off[26], s);
+    s3_to_f32<<<1024, 256, 0, s>>>(F(21), a64.Mus, nC);
+    s3_timesteps_k<float><<<g3(nx, ny, nz), dim3(32, 8, 1), 0, s>>>(a, p32);
+    // the corrections keep the free-slip copies of the state they are added to: give the state
+    // those copies first, as the first FP64 iteration would
+    s3_launch(S3_BC, a64, p64, s);
+    double* red_in = red;       // Σ|.| of the inner sweep (Rx, Ry, Rz, divV)
+    double* red_out = red + 4;  // of the FP64 outer residual
+    const int64_t n4[4] = {nRx, nRy, nRz, nC};
+    const dim3 gr((unsigned)std::max<int64_t>(1, std::min<int64_t>((nC + 1023) / 1024, 1024)), 4);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int64_t i = 0; i < nout; ++i) s3_defect_iteration(a, p32, s);
+        cudaMemsetAsync(red_in, 0, 4 * sizeof(double), s);
+        s3_sum_abs_k<float><<<gr, 256, 0, s>>>(a.Rx, nRx, a.Ry, nRy, a.Rz, nRz, a.divV, nC, red_in);
+        e = cudaStreamEndCapture(s, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) rc = cuda_fail(e, "ps_stokes3d_solve_mixed: graph capture");
+    const double t0 = now_s3();
+    double err = INFINITY, h[4];
+    int64_t it = 0, outer = 0;
+    auto norm = [&](const double* v) {
+        double m = 0;
+        for (int k = 0; k < 4; k++) m = std::max(m, v[k] / (double)n4[k]);
+        return m;
+    };
+    auto finite4 = [](const double* v) {
+        return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]) && std::isfinite(v[3]);
+    };
+    while (rc == PS_OK) {
+        // FP64 residual of the outer state; its rounding to FP32 is the inner sweeps' source
+        s3_residual(a64, p64, s);
+        cudaMemsetAsync(red_out, 0, 4 * sizeof(double), s);
+        s3_sum_abs_k<double><<<gr, 256, 0, s>>>(a64.Rx, nRx, a64.Ry, nRy, a64.Rz, nRz, a64.divV, nC, red_out);
+        s3_to_f32<<<1024, 256, 0, s>>>(F(22), a64.Rx, nRx);
+        s3_to_f32<<<1024, 256, 0, s>>>(F(23), a64.Ry, nRy);
+        s3_to_f32<<<1024, 256, 0, s>>>(F(24), a64.Rz, nRz);
+        s3_to_f32<<<1024, 256, 0, s>>>(F(25), a64.divV, nC);
+        e = cudaMemcpyAsync(h, red_out, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "ps_stokes3d_solve_mixed(residual)");
+            break;
+        }
+        if (!finite4(h)) {
+            err = NAN;
+            rc = fail(PS_ERR_NONFINITE, "ps_stokes3d_solve_mixed: non-finite FP64 residual");
+            break;
+        }
+        err = norm(h);
+        if (err < tol || it >= max_iter) break;
+        if (max_seconds > 0 && now_s3() - t0 > max_seconds) {
+            rc = fail(PS_ERR_TIMEOUT, "ps_stokes3d_solve_mixed: wall-clock limit reached (err %.3e)", err);
+            break;
+        }
+        ++outer;
+        cudaMemsetAsync(base, 0, off[7], s);  // δV, δP and the pseudo-velocities from zero
+        const double target = std::max(err * inner_rtol, tol * 0.25);
+        double ierr = INFINITY;
+        while (it < max_iter) {
+            e = cudaGraphLaunch(exec, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(h, red_in, sizeof(h), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "ps_stokes3d_solve_mixed(inner)");
+                break;
+            }
+            it += nout;
+            if (!finite4(h)) {
+                rc = fail(PS_ERR_NONFINITE, "ps_stokes3d_solve_mixed: non-finite FP32 residual");
+                break;
+            }
+            const double prev = ierr;
+            ierr = norm(h);
+            if (ierr < target) break;
+            if (ierr > 0.98 * prev && ierr < err * 0.5) break;  // FP32 floor reached
+        }
+        if (rc != PS_OK) break;
+        s3_axpy32<<<1024, 256, 0, s>>>(a64.Vx, a.Vx, nVx);
+        s3_axpy32<<<1024, 256, 0, s>>>(a64.Vy, a.Vy, nVy);
+        s3_axpy32<<<1024, 256, 0, s>>>(a64.Vz, a.Vz, nVz);
+        s3_axpy32<<<1024, 256, 0, s>>>(a64.Pt, a.Pt, nC);
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamSynchronize(s);
+    cudaFree(base);
+    cudaGetLastError();
+    st->iters = it;
+    st->outer = outer;
+    st->err = err;
+    st->seconds = now_s3() - t0;
+    st->converged = err < tol;
+    if (rc == PS_OK && !(err < tol))
+        rc = fail(PS_ERR_NOT_CONVERGED, "ps_stokes3d_solve_mixed: err %.3e after %lld iterations", err, (long long)it);
+    return rc;
 }
 
 }  // namespace ps
@@ -636,6 +825,29 @@ int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, 
     stats->converged = err < tol;
     if (rc == PS_OK && !(err < tol))
         rc = fail(PS_ERR_NOT_CONVERGED, "ps_stokes3d_solve: err %.3e after %lld iterations", err, (long long)it);
+    return rc;
+}
+
+int ps_stokes3d_solve_mixed(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, double tol, int64_t max_iter,
+                            int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    PS_TRY(check_fields3(f, false));
+    if (!p || !stats) return fail(PS_ERR_NULL, "NULL params / stats");
+    if (f->Pt.dtype != PS_F64) return fail(PS_ERR_DTYPE, "ps_stokes3d_solve_mixed: the arrays must be FP64");
+    if (nout < 1) return fail(PS_ERR_ARG, "nout must be >= 1");
+    if (!(tol > 0) || max_iter < 0) return fail(PS_ERR_ARG, "invalid tol / max_iter");
+    memset(stats, 0, sizeof(*stats));
+    cudaStream_t user = static_cast<cudaStream_t>(stream), s;
+    PS_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaEvent_t ev;
+    PS_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, user);
+    cudaStreamWaitEvent(s, ev, 0);
+    const int rc = solve_mixed3(f, p, tol, max_iter, nout, max_seconds, 1e-3, st->d_scratch, stats, s);
+    cudaStreamSynchronize(s);
+    cudaEventDestroy(ev);
+    cudaStreamDestroy(s);
     return rc;
 }
 

@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import PSArray
-from .core import descriptor, from_host, require_initialized, stream_handle, to_host, zeros
+from .core import ArgumentError, descriptor, from_host, require_initialized, stream_handle, to_host, zeros
 from .stokes import PSSolveStats
 
 FIELDS = ("Pt", "dtauPt", "divV", "Vx", "Vy", "Vz", "txx", "tyy", "tzz", "txy", "txz", "tyz", "Rx", "Ry", "Rz",
@@ -47,6 +47,8 @@ for _name in ("ps_bc_x3d", "ps_bc_y3d", "ps_bc_z3d"):
 _lib.register("ps_stokes3d_iterate", [_F, _PP, ctypes.c_int64, ctypes.c_void_p])
 _lib.register("ps_stokes3d_err", [_F, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p])
 _lib.register("ps_stokes3d_solve", [_F, _PP, ctypes.c_double, ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
+                                    ctypes.POINTER(PSSolveStats), ctypes.c_void_p])
+_lib.register("ps_stokes3d_solve_mixed", [_F, _PP, ctypes.c_double, ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
                                     ctypes.POINTER(PSSolveStats), ctypes.c_void_p])
 
 
@@ -151,12 +153,16 @@ class Stokes3D:
         _lib.call("ps_stokes3d_err", ctypes.byref(self._fields), out, stream_handle(stream))
         return max(out), tuple(out)
 
-    def solve(self, tol=1e-6, max_iter=100_000, nout=500, max_seconds=0.0, stream=None):
-        """PT solve to err < tol (FP64); returns PSSolveStats. Raises PSError if it does not converge."""
+    def solve(self, tol=1e-6, max_iter=100_000, nout=500, max_seconds=0.0, stream=None, mode=0):
+        """PT solve to err < tol; mode 0: FP64 (the reference's iteration), mode 1: FP32 sweeps on
+        FP64 defect corrections (ps_stokes3d_solve_mixed). Returns PSSolveStats; raises PSError if
+        it does not converge."""
+        if mode not in (0, 1):
+            raise ArgumentError("mode must be 0 (FP64) or 1 (FP32 + FP64 defect correction)")
         st = PSSolveStats()
-        rc = _lib.load().ps_stokes3d_solve(ctypes.byref(self._fields), ctypes.byref(self._p), float(tol),
-                                           int(max_iter), int(nout), float(max_seconds), ctypes.byref(st),
-                                           stream_handle(stream))
+        fn = _lib.load().ps_stokes3d_solve if mode == 0 else _lib.load().ps_stokes3d_solve_mixed
+        rc = fn(ctypes.byref(self._fields), ctypes.byref(self._p), float(tol), int(max_iter), int(nout),
+                float(max_seconds), ctypes.byref(st), stream_handle(stream))
         if rc != 0:
             err = _lib.PSError(rc, _lib.last_error())
             err.stats = st

@@ -127,3 +127,32 @@ def test_stokes3d_solver_reports_divergence(ps, oracle):
     with pytest.raises(PSError) as ei:
         g.solve(tol=1e-6, nout=100, max_iter=10_000)
     assert ei.value.status == -11
+
+
+def test_stokes3d_mixed_solver_matches_fp64(ps, oracle):
+    """FP32 sweeps + FP64 defect correction reach the same FP64 residual (the reference's err of the
+    returned state) and the same solution as the FP64 solver."""
+    n = (63, 63, 63)
+    g64, _ = _pair(ps, oracle, n, "f64")
+    gmx, _ = _pair(ps, oracle, n, "f64")
+    tol = 1e-8
+    s64 = g64.solve(tol=tol, nout=100, max_iter=200_000)
+    smx = gmx.solve(tol=tol, nout=100, max_iter=200_000, mode=1)
+    assert s64.converged and smx.converged and smx.outer >= 2
+    e, parts = gmx.err()  # the FP64 residual arrays the solver left for the returned state
+    assert e < tol and e == pytest.approx(smx.err, rel=1e-12)
+    diffs = {}
+    for k in ("Vx", "Vy", "Vz", "Pt"):
+        a, b = g64.host(k), gmx.host(k)
+        diffs[k] = np.abs(a - b).max() / np.abs(a).max()
+    print("stokes3d mixed vs fp64 relative max differences", diffs, s64.iters, smx.iters, smx.outer)
+    assert max(diffs.values()) < 1e-3, diffs
+
+
+def test_stokes3d_mixed_solver_refuses_fp32(ps, oracle):
+    from ps_gb300 import PSError
+
+    g, _ = _pair(ps, oracle, (15, 15, 15), "f32")
+    with pytest.raises(PSError) as e:
+        g.solve(tol=1e-6, mode=1)
+    assert e.value.status == -4
