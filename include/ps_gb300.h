@@ -412,6 +412,9 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
 int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                      const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
                      int32_t zloop, void* stream, int sync);
+/* Wait for `stream`, then report (and clear) the error flags left by earlier asynchronous launches
+ * of `kernel`, as a synchronous launch does. */
+int ps_jit_check(void* kernel, void* stream);
 int ps_jit_destroy(void* kernel);
 
 /* ------------------------------------------------------------------------------------ */

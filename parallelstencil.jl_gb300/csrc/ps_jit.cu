@@ -204,6 +204,24 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
     return PS_OK;
 }
 
+int ps_jit_check(void* kernel, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    if (!kernel) return fail(PS_ERR_NULL, "ps_jit_check: NULL kernel");
+    JitKernel* k = static_cast<JitKernel*>(kernel);
+    PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), 1, "ps_jit_check"));
+    int flag = 0;
+    if (cudaMemcpy(&flag, k->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(PS_ERR_CUDA, "ps_jit_check: reading the error flag failed");
+    if (flag) {
+        cudaMemset(k->err, 0, sizeof(int));
+        if (flag & 1) return fail(PS_ERR_ARG, "ps_jit_check: out-of-bounds array access in the kernel (BoundsError)");
+        return fail(PS_ERR_ARG, "ps_jit_check: a kernel with @sync_threads, shuffles or votes needs ranges that are "
+                                "a multiple of the thread block; a partial block did not run");
+    }
+    return PS_OK;
+}
+
 int ps_jit_destroy(void* kernel) {
     if (!kernel) return PS_OK;
     JitKernel* k = static_cast<JitKernel*>(kernel);

@@ -53,6 +53,7 @@ _lib.register("ps_jit_launch_ex", [ctypes.c_void_p, ctypes.POINTER(PSArray), cty
                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                    ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
                                    ctypes.c_int32, ctypes.c_void_p, ctypes.c_int])
+_lib.register("ps_jit_check", [ctypes.c_void_p, ctypes.c_void_p])
 _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
 MAX_ARRAYS = MAX_SCALARS = 32
@@ -992,9 +993,7 @@ class JitKernel:
         if dt is None or any(d.dtype != descs[0].dtype for d in descs):
             raise ArgumentError("the array arguments must share one FP64 or FP32 type")
         ndims = self.ndims or array_ndims(descs)
-        lo, cnt = [0, 0, 0], [1, 1, 1]
-        for d in range(ndims):
-            cnt[d] = max(int(x.n[d]) for x in descs) if descs else 1
+        lo, cnt = [0, 0, 0], self._extent(descs, ndims)
         threads = [1, 1, 1]
         if nthreads is not None:
             nthreads = tuple(int(x) for x in (nthreads if isinstance(nthreads, (tuple, list)) else (nthreads,)))
@@ -1032,6 +1031,21 @@ class JitKernel:
         _lib.call("ps_jit_launch_ex", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
                   (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), zloop,
                   stream_handle(stream), int(bool(sync)))
+
+    @staticmethod
+    def _extent(descs, ndims):
+        """The `@parallel` grid: the largest extent of the array arguments per dimension
+        (src/ParallelKernel/parallel.jl:785-798), 1 beyond ndims."""
+        return [max(int(x.n[d]) for x in descs) if descs and d < ndims else 1 for d in range(3)]
+
+    def grid_extent(self, args):
+        descs = [descriptor(a) for (kind, _), a in zip(self.kd.args, args) if kind == "array"]
+        return self._extent(descs, self.ndims or array_ndims(descs))
+
+    def check(self, stream=None):
+        """Wait for `stream` and raise what earlier asynchronous launches of this kernel flagged."""
+        for h in self._handles.values():
+            _lib.call("ps_jit_check", h, stream_handle(stream))
 
     def __del__(self):
         try:

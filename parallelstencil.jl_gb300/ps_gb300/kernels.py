@@ -224,14 +224,19 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
 
     The six boundary slabs run on a high-priority stream and the inner box on a normal
     stream (src/ParallelKernel/hide_communication.jl:177-258); `comm` runs on the host once
-    the boundary slabs are done. Only the diffusion kernels are split.
+    the boundary slabs are done. The diffusion kernels split inside the library
+    (ps_diffusion3d_step_split); run-time compiled kernels split by ranges on two streams.
     """
     require_initialized()
-    if not isinstance(kernel, Diffusion3D):
-        raise ArgumentError("@hide_communication is implemented for the diffusion3D kernels")
     bw = boundary_width if isinstance(boundary_width, (tuple, list)) else (boundary_width,) * 3
     if len(bw) != 3:
         raise ArgumentError("boundary_width must be an integer or a 3-tuple")
+    if hasattr(kernel, "jit_launch"):
+        _hide_communication_jit(tuple(int(b) for b in bw), kernel, args, comm, memopt, s_boundary, s_inner)
+        return
+    if not isinstance(kernel, Diffusion3D):
+        raise ArgumentError("@hide_communication is implemented for the diffusion3D kernels and for run-time "
+                            "compiled kernels")
     T2, T, Ci, lam_arr, lam, dt, hx, hy, hz = kernel.split_args(args)
     memopt = default_memopt() if memopt is None else memopt
     own = []
@@ -266,6 +271,41 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
             _lib.call("ps_stream_destroy", s)
     if errors:
         raise errors[0]
+
+
+def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner):
+    """The boundary/inner split for any run-time compiled kernel: the six boundary boxes of the
+    kernel's `@parallel` grid on a high-priority stream, the inner box on a normal one, `comm` on
+    the host once the boundary boxes are done, while the inner box runs."""
+    import torch
+
+    ms = kernel.grid_extent(args)
+    for d in range(3):
+        if bw[d] < 0:
+            raise ArgumentError("boundary width must be >= 0")
+        if not ms[d] > 2 * bw[d]:
+            raise ArgumentError("@hide_communication: length(ranges) > 2*boundary_width violated")
+        if ms[d] > 1 and bw[d] == 0:
+            raise ArgumentError("@hide_communication: boundary_width 0 in a dimension of length > 1")
+    # s_boundary / s_inner: torch streams (default: a new high-priority / normal-priority pair)
+    sb = s_boundary if s_boundary is not None else torch.cuda.Stream(priority=-1)
+    si = s_inner if s_inner is not None else torch.cuda.Stream(priority=0)
+    cur = torch.cuda.current_stream()
+    for s in (sb, si):
+        s.wait_stream(cur)
+    for lo, hi in get_ranges_outer(bw, ms):
+        kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], sb, False, memopt=memopt)
+    for lo, hi in get_ranges_inner(bw, ms):
+        kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], si, False, memopt=memopt)
+    sb.synchronize()
+    try:
+        if comm is not None:
+            comm()
+    finally:
+        si.synchronize()
+        cur.wait_stream(sb)
+        cur.wait_stream(si)
+    kernel.check(si)
 
 
 def get_ranges_outer(boundary_width, maxsize):

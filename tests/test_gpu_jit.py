@@ -388,3 +388,29 @@ def test_jit_memopt_from_the_definition(ps):
     ps.parallel(ps.kernels.diffusion3D_step_inv, B, T, Ci, 0.7, 1e-3, 9.0, 11.0, 13.0, memopt=False)
     assert np.array_equal(ps.to_host(A), ps.to_host(B))
     assert (3, "double", True) in k._handles
+
+
+@pytest.mark.parametrize("name", ["HEAT_FLUX", "TWO3D"])
+def test_jit_hide_communication_equals_one_launch(ps, name):
+    """@hide_communication with a run-time compiled kernel: the six boundary boxes and the inner box
+    on two streams give the one-launch result; comm runs once, after the boundary boxes."""
+    rng = np.random.default_rng(17)
+    n = (64, 40, 36)
+    k = ps.parallel_kernel(getattr(K, name))
+    if name == "HEAT_FLUX":
+        T, Ci = _dev(ps, rng.random(n)), _dev(ps, rng.random(n) + 0.5)
+        mk = lambda: [ps.zeros(*n)]  # noqa: E731
+        rest = [T, Ci, 0.7, 1e-3, 9.0, 11.0, 13.0]
+    else:
+        B = _dev(ps, rng.standard_normal(n))
+        mk = lambda: [ps.zeros(n[0] - 2, n[1] - 2, n[2] - 1), ps.zeros(*n)]  # noqa: E731
+        rest = [B, 0.7]
+    ref, out = mk(), mk()
+    ps.parallel(k, *ref, *rest)
+    calls = []
+    ps.hide_communication((16, 4, 2), k, (*out, *rest), comm=lambda: calls.append(1))
+    assert calls == [1]
+    for a, b in zip(ref, out):
+        assert np.array_equal(ps.to_host(a), ps.to_host(b))
+    with pytest.raises(ps.ArgumentError, match="boundary_width"):
+        ps.hide_communication((40, 4, 2), k, (*out, *rest))
