@@ -113,6 +113,11 @@ int ps_fill(ps_array a, double value, void* stream);
 /* Host <-> device copies of a whole array (`Data.Array(host)` / `Array(A)`). */
 int ps_copy_h2d(ps_array dst, const void* host_src, void* stream);
 int ps_copy_d2h(void* host_dst, ps_array src, void* stream);
+/* The same without waiting (stream-ordered; the host buffer must be page-locked for the copy to
+ * overlap other work), and a device-to-device copy of two arrays of one shape and dtype. */
+int ps_copy_h2d_async(ps_array dst, const void* host_src, void* stream);
+int ps_copy_d2h_async(void* host_dst, ps_array src, void* stream);
+int ps_copy_d2d_async(ps_array dst, ps_array src, void* stream);
 
 /* Streams of the `@hide_communication` split (CUDAExt/shared.jl:17-31): priority 1 =
  * high-priority non-blocking stream (boundary slabs), 0 = normal non-blocking stream. */

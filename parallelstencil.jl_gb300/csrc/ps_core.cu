@@ -283,6 +283,32 @@ int ps_copy_d2h(void* host_dst, ps_array src, void* stream) {
     return PS_OK;
 }
 
+int ps_copy_h2d_async(ps_array dst, const void* host_src, void* stream) {
+    PS_TRY(check_array(dst, "dst"));
+    if (!host_src) return fail(PS_ERR_NULL, "ps_copy_h2d_async: NULL host pointer");
+    PS_CUDA_TRY(cudaMemcpyAsync(dst.ptr, host_src, numel(dst) * elsize(dst.dtype), cudaMemcpyHostToDevice,
+                                static_cast<cudaStream_t>(stream)));
+    return PS_OK;
+}
+
+int ps_copy_d2h_async(void* host_dst, ps_array src, void* stream) {
+    PS_TRY(check_array(src, "src"));
+    if (!host_dst) return fail(PS_ERR_NULL, "ps_copy_d2h_async: NULL host pointer");
+    PS_CUDA_TRY(cudaMemcpyAsync(host_dst, src.ptr, numel(src) * elsize(src.dtype), cudaMemcpyDeviceToHost,
+                                static_cast<cudaStream_t>(stream)));
+    return PS_OK;
+}
+
+int ps_copy_d2d_async(ps_array dst, ps_array src, void* stream) {
+    PS_TRY(check_array(dst, "dst"));
+    PS_TRY(check_array(src, "src"));
+    PS_TRY(check_same_dtype(dst, src, "dst", "src"));
+    PS_TRY(check_shape(src, dst.n[0], dst.n[1], dst.n[2], "src"));
+    PS_CUDA_TRY(cudaMemcpyAsync(dst.ptr, src.ptr, numel(dst) * elsize(dst.dtype), cudaMemcpyDeviceToDevice,
+                                static_cast<cudaStream_t>(stream)));
+    return PS_OK;
+}
+
 int ps_stream_create(int priority, void** stream) {
     if (!stream) return fail(PS_ERR_NULL, "ps_stream_create: NULL output");
     int lo = 0, hi = 0;

@@ -64,6 +64,9 @@ SIGNATURES = {
     "ps_fill": [_A, _D, _P],
     "ps_copy_h2d": [_A, _P, _P],
     "ps_copy_d2h": [_P, _A, _P],
+    "ps_copy_h2d_async": [_A, _P, _P],
+    "ps_copy_d2h_async": [_P, _A, _P],
+    "ps_copy_d2d_async": [_A, _A, _P],
     "ps_stream_create": [_I, ctypes.POINTER(_P)],
     "ps_stream_destroy": [_P],
     "ps_synchronize": [_P],
