@@ -229,6 +229,12 @@ int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci
  * glam += (∂T2/∂lam)^T lamT2. T is the step's input state. All arrays n^3, one dtype. */
 int ps_diffusion3d_adjoint_step(ps_array lamT, ps_array lamT2, ps_array T, ps_array Ci, ps_array lam, ps_array glam,
                                 double dt, double hx, double hy, double hz, void* stream, int sync);
+/* The same with fp64_mode (ps_launch.fp64_mode values): PS_FP64_IEEE is the function above; any
+ * split mode evaluates the reverse step on FP32 pairs (FP64 arrays only; within ~1e-13 relative of
+ * the IEEE step). ps_diffusion3d_misfit_gradient uses this form with its cfg's fp64_mode. */
+int ps_diffusion3d_adjoint_step_ex(ps_array lamT, ps_array lamT2, ps_array T, ps_array Ci, ps_array lam,
+                                   ps_array glam, double dt, double hx, double hy, double hz, int32_t fp64_mode,
+                                   void* stream, int sync);
 
 typedef struct ps_adjoint_stats {
     double loss;               /* 0.5 * ||T_nt - T_obs||^2                  */

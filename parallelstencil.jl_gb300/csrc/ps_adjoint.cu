@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "ps_common.cuh"
+#include "ps_dd.cuh"
 
 namespace ps {
 
@@ -68,6 +69,61 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(T* __restrict__ lamT,
     }
 }
 
+// The same reverse step with FP64 arrays evaluated in split-FP32 arithmetic (fp64_mode != IEEE):
+// every input is split into an FP32 pair with integer operations, the sums and products of the
+// IEEE kernel above run on pairs (47-bit significands), and the results are applied in FP64 as
+// λ = (λ2 + acc.h) + acc.l and glam = (glam + g.h) + g.l. Same statement order as the IEEE kernel.
+__global__ void __launch_bounds__(256) adjoint_step_split_kernel(double* __restrict__ lamT,
+                                                                 const double* __restrict__ lamT2,
+                                                                 const double* __restrict__ Tn,
+                                                                 const double* __restrict__ Ci,
+                                                                 const double* __restrict__ lam,
+                                                                 double* __restrict__ glam, dd dt, dd hh0, dd hh1,
+                                                                 dd hh2, int64_t nx, int64_t ny, int64_t nz, int* err) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (i >= nx || j >= ny) return;
+    const dd hh[3] = {hh0, hh1, hh2};
+    const int64_t st[3] = {1, nx, nx * ny};
+    const int64_t ext[3] = {nx, ny, nz};
+    auto inner = [&](int64_t a, int64_t b, int64_t c) {
+        return a >= 1 && a <= nx - 2 && b >= 1 && b <= ny - 2 && c >= 1 && c <= nz - 2;
+    };
+    const dd zero = {0.0f, 0.0f};
+    bool big = false;
+    for (int64_t k = blockIdx.z; k < nz; k += gridDim.z) {
+        const int64_t c = i + nx * (j + ny * k);
+        const int64_t idx[3] = {i, j, k};
+        const bool inner_c = inner(i, j, k);
+        const dd mu_c = inner_c ? dd_mul(dd_mul(dt, dd_split(__ldg(Ci + c), big)), dd_split(__ldg(lamT2 + c), big))
+                                : zero;
+        const dd lc = dd_split(__ldg(lam + c), big), Tc = dd_split(__ldg(Tn + c), big);
+        dd acc = zero, g = zero;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+#pragma unroll
+            for (int sgn = -1; sgn <= 1; sgn += 2) {
+                const int64_t q = idx[d] + sgn;
+                if (q < 0 || q >= ext[d]) continue;
+                const int64_t nb = c + sgn * st[d];
+                const bool inner_n = inner(d == 0 ? q : i, d == 1 ? q : j, d == 2 ? q : k);
+                const dd mu_n = inner_n ? dd_mul(dd_mul(dt, dd_split(__ldg(Ci + nb), big)),
+                                                 dd_split(__ldg(lamT2 + nb), big))
+                                        : zero;
+                const dd kf = dd_scale(dd_add(lc, dd_split(__ldg(lam + nb), big)), 0.5f);
+                const dd Tnb = dd_split(__ldg(Tn + nb), big);
+                const dd mua = sgn > 0 ? mu_c : mu_n, mub = sgn > 0 ? mu_n : mu_c;
+                const dd Ta = sgn > 0 ? Tc : Tnb, Tb = sgn > 0 ? Tnb : Tc;
+                acc = dd_add(acc, dd_mul(dd_mul(hh[d], kf), dd_sub(mu_n, mu_c)));
+                g = dd_add(g, dd_mul(dd_mul(dd_scale(dd_sub(mua, mub), 0.5f), hh[d]), dd_sub(Tb, Ta)));
+            }
+        }
+        lamT[c] = inner_c ? (__ldg(lamT2 + c) + f32_to_f64(acc.h)) + f32_to_f64(acc.l) : 0.0;
+        glam[c] = (glam[c] + f32_to_f64(g.h)) + f32_to_f64(g.l);
+    }
+    if (big) atomicOr(err, DEV_ERR_RANGE);  // a magnitude outside the split range: reported at the next sync
+}
+
 // λ = (T - T_obs) on inner cells (0 on the boundary); loss += 0.5 Σ (T - T_obs)^2 over all cells.
 __global__ void misfit_kernel(double* __restrict__ lamT, const double* __restrict__ Tn, const double* __restrict__ Tobs,
                               int64_t nx, int64_t ny, int64_t nz, double* loss) {
@@ -91,12 +147,49 @@ static int check3(const ps_array& a, const ps_array& ref, const char* name) {
     return check_shape(a, ref.n[0], ref.n[1], ref.n[2], name);
 }
 
+// Library-owned scratch of the gradient (checkpoints, segment states, forward and adjoint buffers),
+// kept between calls (an inverse problem asks for many gradients of one size); freed by
+// ps_finalize.
+static void* g_adj_scratch = nullptr;
+static size_t g_adj_bytes = 0;
+
+void adjoint_free_scratch() {
+    if (g_adj_scratch) cudaFree(g_adj_scratch);
+    g_adj_scratch = nullptr;
+    g_adj_bytes = 0;
+}
+
+static int adjoint_scratch(size_t bytes, char** p) {
+    if (bytes > g_adj_bytes) {
+        adjoint_free_scratch();
+        if (cudaMalloc(&g_adj_scratch, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            g_adj_scratch = nullptr;
+            return fail(PS_ERR_NOMEM, "ps_diffusion3d_misfit_gradient: scratch allocation of %zu bytes failed", bytes);
+        }
+        g_adj_bytes = bytes;
+    }
+    *p = static_cast<char*>(g_adj_scratch);
+    return PS_OK;
+}
+
+static dd host_split(double x) {  // x = h + l to ~2^-48 relative (host side, for the coefficients)
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
 static int launch_adjoint_step(const ps_array& lamT, const ps_array& lamT2, const ps_array& Tn, const ps_array& Ci,
                                const ps_array& lam, const ps_array& glam, double dt, double hx, double hy, double hz,
-                               cudaStream_t s) {
+                               cudaStream_t s, int fp64_mode = PS_FP64_IEEE, int* d_err = nullptr) {
     dim3 blk(32, 8);
     dim3 grd((unsigned)((Tn.n[0] + 31) / 32), (unsigned)((Tn.n[1] + 7) / 8), (unsigned)std::min<int64_t>(Tn.n[2], 65535));
-    if (Tn.dtype == PS_F64)
+    if (Tn.dtype == PS_F64 && fp64_mode != PS_FP64_IEEE && d_err)
+        adjoint_step_split_kernel<<<grd, blk, 0, s>>>(
+            static_cast<double*>(lamT.ptr), static_cast<const double*>(lamT2.ptr), static_cast<const double*>(Tn.ptr),
+            static_cast<const double*>(Ci.ptr), static_cast<const double*>(lam.ptr), static_cast<double*>(glam.ptr),
+            host_split(dt), host_split(hx * hx), host_split(hy * hy), host_split(hz * hz), Tn.n[0], Tn.n[1], Tn.n[2],
+            d_err);
+    else if (Tn.dtype == PS_F64)
         adjoint_step_kernel<double><<<grd, blk, 0, s>>>(
             static_cast<double*>(lamT.ptr), static_cast<const double*>(lamT2.ptr), static_cast<const double*>(Tn.ptr),
             static_cast<const double*>(Ci.ptr), static_cast<const double*>(lam.ptr), static_cast<double*>(glam.ptr), dt,
@@ -117,6 +210,12 @@ extern "C" {
 
 int ps_diffusion3d_adjoint_step(ps_array lamT, ps_array lamT2, ps_array T, ps_array Ci, ps_array lam, ps_array glam,
                                 double dt, double hx, double hy, double hz, void* stream, int sync) {
+    return ps_diffusion3d_adjoint_step_ex(lamT, lamT2, T, Ci, lam, glam, dt, hx, hy, hz, PS_FP64_IEEE, stream, sync);
+}
+
+int ps_diffusion3d_adjoint_step_ex(ps_array lamT, ps_array lamT2, ps_array T, ps_array Ci, ps_array lam,
+                                   ps_array glam, double dt, double hx, double hy, double hz, int32_t fp64_mode,
+                                   void* stream, int sync) {
     DeviceState* st = nullptr;
     PS_TRY(current_state(&st));
     PS_TRY(check_array(T, "T"));
@@ -126,8 +225,9 @@ int ps_diffusion3d_adjoint_step(ps_array lamT, ps_array lamT2, ps_array T, ps_ar
     PS_TRY(check3(lam, T, "lam"));
     PS_TRY(check3(glam, T, "glam"));
     if (lamT.ptr == lamT2.ptr) return fail(PS_ERR_ARG, "λT and λT2 must be distinct arrays");
+    if (fp64_mode < PS_FP64_IEEE || fp64_mode > PS_FP64_SPLIT_GRID) return fail(PS_ERR_ARG, "unknown fp64_mode %d", fp64_mode);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    PS_TRY(launch_adjoint_step(lamT, lamT2, T, Ci, lam, glam, dt, hx, hy, hz, s));
+    PS_TRY(launch_adjoint_step(lamT, lamT2, T, Ci, lam, glam, dt, hx, hy, hz, s, fp64_mode, st->d_err));
     return finish_launch(s, sync, "ps_diffusion3d_adjoint_step");
 }
 
@@ -150,22 +250,16 @@ int ps_diffusion3d_misfit_gradient(ps_array T0, ps_array Tobs, ps_array Ci, ps_a
     const auto t0 = std::chrono::steady_clock::now();
     const int64_t ce = checkpoint_every, nseg = (nt + ce - 1) / ce;
     const size_t bytes = (size_t)numel(T0) * 8;
-    // scratch: nseg checkpoints, ce segment states, two forward buffers, two adjoint buffers
+    // scratch: nseg checkpoints, ce segment states, two forward buffers, two adjoint buffers, the loss
     const int64_t nbuf = nseg + ce + 4;
-    std::vector<void*> bufs(nbuf, nullptr);
-    double* d_loss = nullptr;
+    const size_t stride = (bytes + 255) / 256 * 256;
+    char* scr = nullptr;
+    PS_TRY(adjoint_scratch(stride * nbuf + 256, &scr));
+    double* d_loss = reinterpret_cast<double*>(scr + stride * nbuf);
     int rc = PS_OK;
-    for (int64_t b = 0; b < nbuf && rc == PS_OK; b++) {
-        if (cudaMalloc(&bufs[b], bytes) != cudaSuccess) {
-            cudaGetLastError();
-            rc = fail(PS_ERR_NOMEM, "ps_diffusion3d_misfit_gradient: scratch allocation failed (%lld arrays of %zu B)",
-                      (long long)nbuf, bytes);
-        }
-    }
-    if (rc == PS_OK && cudaMalloc(&d_loss, sizeof(double)) != cudaSuccess) rc = fail(PS_ERR_NOMEM, "loss scratch");
     auto arr = [&](int64_t b) {
         ps_array a = T0;
-        a.ptr = bufs[b];
+        a.ptr = scr + stride * b;
         return a;
     };
     auto ckpt = [&](int64_t sidx) { return arr(sidx); };
@@ -184,8 +278,10 @@ int ps_diffusion3d_misfit_gradient(ps_array T0, ps_array Tobs, ps_array Ci, ps_a
     int64_t recomputed = 0;
     double loss = 0.0;
     // ---- forward with checkpoints ----
+    // the steps write inner cells only: every state buffer gets T0's boundary values once
     if (rc == PS_OK) rc = copy(fA, T0);
-    if (rc == PS_OK) rc = copy(fB, T0);  // boundary values of the second buffer
+    if (rc == PS_OK) rc = copy(fB, T0);
+    for (int64_t j = 1; j < ce && j < nt && rc == PS_OK; j++) rc = copy(seg(j), T0);
     for (int64_t n = 0; n < nt && rc == PS_OK; n++) {
         if (n % ce == 0) rc = copy(ckpt(n / ce), fA);
         if (rc == PS_OK) rc = step(fB, fA);
@@ -206,12 +302,11 @@ int ps_diffusion3d_misfit_gradient(ps_array T0, ps_array Tobs, ps_array Ci, ps_a
         const int64_t n0 = sidx * ce, n1 = std::min(nt, n0 + ce);
         rc = copy(seg(0), ckpt(sidx));
         for (int64_t j = 1; j < n1 - n0 && rc == PS_OK; j++) {
-            rc = copy(seg(j), seg(j - 1));  // boundary values, then the step overwrites the interior
-            if (rc == PS_OK) rc = step(seg(j), seg(j - 1));
+            rc = step(seg(j), seg(j - 1));  // seg(j) holds the boundary values already
             recomputed++;
         }
         for (int64_t nn = n1 - 1; nn >= n0 && rc == PS_OK; nn--) {
-            rc = launch_adjoint_step(lB, lA, seg(nn - n0), Ci, lam, dL_dlam, dt, hx, hy, hz, s);
+            rc = launch_adjoint_step(lB, lA, seg(nn - n0), Ci, lam, dL_dlam, dt, hx, hy, hz, s, fp64_mode, st->d_err);
             std::swap(lA, lB);
         }
     }
@@ -222,9 +317,6 @@ int ps_diffusion3d_misfit_gradient(ps_array T0, ps_array Tobs, ps_array Ci, ps_a
     }
     if (rc == PS_OK) rc = finish_launch(s, 1, "ps_diffusion3d_misfit_gradient");
     cudaStreamSynchronize(s);
-    for (void* p : bufs)
-        if (p) cudaFree(p);
-    if (d_loss) cudaFree(d_loss);
     stats->loss = loss;
     stats->checkpoints = nseg;
     stats->recomputed_steps = recomputed;

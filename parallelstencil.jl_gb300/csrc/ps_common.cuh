@@ -45,6 +45,7 @@ int current_state(DeviceState** st);
 // Frees library-owned solver scratch (ps_finalize).
 void stokes2d_free_scratch();
 void diffusion_free_scratch();
+void adjoint_free_scratch();
 
 // Reads (and clears) the device error word after a synchronisation.
 int check_device_error(DeviceState* st, cudaStream_t s);

@@ -221,6 +221,7 @@ int ps_finalize(void) {
     cudaGetDevice(&cur);
     stokes2d_free_scratch();
     diffusion_free_scratch();
+    adjoint_free_scratch();
     for (int d = 0; d < kMaxDevices; d++) {
         DeviceState& st = g_dev[d];
         if (!st.ready) continue;

@@ -27,17 +27,21 @@ class PSAdjointStats(ctypes.Structure):
 
 _D = ctypes.c_double
 _lib.register("ps_diffusion3d_adjoint_step", [PSArray] * 6 + [_D] * 4 + [ctypes.c_void_p, ctypes.c_int])
+_lib.register("ps_diffusion3d_adjoint_step_ex", [PSArray] * 6 + [_D] * 4 + [ctypes.c_int32, ctypes.c_void_p,
+                                                                            ctypes.c_int])
 _lib.register("ps_diffusion3d_misfit_gradient",
               [PSArray] * 4 + [_D] * 4 + [ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(PSLaunch), PSArray, PSArray,
                                           ctypes.POINTER(PSAdjointStats), ctypes.c_void_p])
 
 
-def adjoint_step(lamT, lamT2, T, Ci, lam, glam, dt, hx, hy, hz, stream=None, sync=True):
-    """lamT = (∂T2/∂T)^T lamT2 (inner cells), glam += (∂T2/∂lam)^T lamT2 for T2 = step(T, lam)."""
+def adjoint_step(lamT, lamT2, T, Ci, lam, glam, dt, hx, hy, hz, stream=None, sync=True, fp64="ieee"):
+    """lamT = (∂T2/∂T)^T lamT2 (inner cells), glam += (∂T2/∂lam)^T lamT2 for T2 = step(T, lam);
+    fp64="split" evaluates it on FP32 pairs (FP64 arrays)."""
     require_initialized()
-    _lib.call("ps_diffusion3d_adjoint_step", descriptor(lamT), descriptor(lamT2), descriptor(T), descriptor(Ci),
-              descriptor(lam), descriptor(glam), float(dt), float(hx), float(hy), float(hz), stream_handle(stream),
-              int(bool(sync)))
+    cfg = _launch_cfg(False, 0, None, fp64)
+    _lib.call("ps_diffusion3d_adjoint_step_ex", descriptor(lamT), descriptor(lamT2), descriptor(T), descriptor(Ci),
+              descriptor(lam), descriptor(glam), float(dt), float(hx), float(hy), float(hz), int(cfg.fp64_mode),
+              stream_handle(stream), int(bool(sync)))
 
 
 def misfit_gradient(T0, T_obs, Ci, lam, dt, h, nt, checkpoint_every=20, memopt=True, fp64="ieee", stream=None,

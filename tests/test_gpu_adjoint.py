@@ -74,3 +74,21 @@ def test_misfit_gradient_finite_differences(ps):
         ad = float(np.sum(gh * v))
         worst = max(worst, abs(fd - ad) / max(abs(ad), 1e-30))
     assert worst < 1e-5, worst
+
+
+def test_adjoint_step_split_close_to_ieee(ps):
+    """The reverse step on FP32 pairs (FP64 arrays) against the IEEE one: ≤ 1e-13 relative max-norm."""
+    n = (45, 38, 33)
+    T0, Ci, lam, h, dt = _problem(n, seed=7)
+    rng = np.random.default_rng(2)
+    lamT2 = np.asfortranarray(rng.standard_normal(n) * 1e-3)
+    glam0 = np.asfortranarray(rng.standard_normal(n) * 1e-2)
+    out = {}
+    for fp64 in ("ieee", "split"):
+        dl, dg = ps.zeros(*n), ps.from_host(glam0)
+        ps.adjoint.adjoint_step(dl, ps.from_host(lamT2), ps.from_host(T0), ps.from_host(Ci), ps.from_host(lam), dg, dt,
+                                *h, fp64=fp64)
+        out[fp64] = (ps.to_host(dl), ps.to_host(dg))
+    for a, b in zip(out["ieee"], out["split"]):
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+    assert not np.array_equal(out["ieee"][0], out["split"][0])  # a different arithmetic really ran
