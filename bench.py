@@ -445,6 +445,12 @@ def run_ours(a, world, rank, local):
         s3solve = None if a.quick else bench_stokes3d_solve(ps)
         if s3solve:
             launches += s3solve.pop("launches")
+        fdm = None if a.quick else bench_fd_macros(ps, torch)
+        if fdm:
+            launches += fdm.pop("launches")
+        hide = None if a.quick else bench_hide_communication(ps, torch)
+        if hide:
+            launches += hide.pop("launches")
     clocks = clk.summary()
 
     value = job_value(world, b_head, t_head) / 1e9
@@ -479,6 +485,8 @@ def run_ours(a, world, rank, local):
         "adjoint_gradient": adj,
         "miniapps": mini,
         "stokes3d_time_to_tol": s3solve,
+        "fd_macros_512": fdm,
+        "hide_communication_512": hide,
         "clocks": clocks,
         "variants": results,
     }
@@ -633,6 +641,54 @@ def bench_miniapps(ps, torch, peak):
     out["peak_hbm_gbs"] = peak
     out["launches"] = launches
     return out
+
+
+# statement -> extent of R relative to A (n^3)
+FD_STATEMENTS = {"@all(R) = @d_xa(A)": (-1, 0, 0), "@inn(R) = @d2_zi(A)": (0, 0, 0), "@all(R) = @av(A)": (-1, -1, -1),
+                 "@all(R) = @harm_xya(A)": (-1, -1, 0), "@inn(R) = @maxloc(A)": (0, 0, 0),
+                 "@inn(R) = @av_yzi(A)": (0, 0, 0)}
+
+
+def bench_fd_macros(ps, torch, n=512):
+    """One-statement FiniteDifferences kernels (`@parallel f!(R, A) = (@<sel>(R) = @<op>(A))`) on
+    n^3 arrays through ps_fd_apply: T_eff with 2 words per cell (A read, R written), FP64 and FP32,
+    and the same statement as a run-time compiled kernel."""
+    out, launches = {}, 0
+    for dt, tag in ((np.float64, "f64"), (np.float32, "f32")):
+        A = ps.rand(n, n, n, dtype=dt, seed=4)
+        es = np.dtype(dt).itemsize
+        for stmt, off in FD_STATEMENTS.items():
+            R = ps.zeros(*(n + o for o in off), dtype=dt)
+            k = ps.fd_kernel(stmt)
+            t = _events(torch, lambda: ps.parallel(k, R, A, sync=False), 10)
+            j = ps.parallel_kernel(f"@parallel function f!(R, A)\n    {stmt}\n    return\nend")
+            tj = _events(torch, lambda: ps.parallel(j, R, A, sync=False), 10)
+            out[f"{stmt} {tag}"] = {"ms": round(t * 1e3, 4), "T_eff_GBs": round(2 * es * n ** 3 / t / 1e9, 1),
+                                    "jit_ms": round(tj * 1e3, 4), "jit_T_eff_GBs": round(2 * es * n ** 3 / tj / 1e9, 1)}
+            launches += 2 * 13
+            del R
+        del A
+    torch.cuda.empty_cache()
+    out["launches"] = launches
+    return out
+
+
+def bench_hide_communication(ps, torch, n=512, bw=(16, 2, 2)):
+    """`@hide_communication bw begin @parallel diffusion3D_step!(...); comm() end` at n^3 FP64 (IEEE,
+    memopt): the six boundary slabs on a high-priority stream, the inner box beside them, against
+    the same step in one launch; comm is empty, so the difference is the split's own cost."""
+    T = ps.rand(n, n, n, seed=2)
+    T2, Ci = ps.zeros(n, n, n), ps.ones(n, n, n)
+    h = (n - 1) / 10.0
+    args = (T2, T, Ci, 1.0, 1e-4, h, h, h)
+    k = ps.kernels.diffusion3D_step_inv
+    t1 = _events(torch, lambda: ps.parallel(k, *args, memopt=True, sync=False), 5)
+    t2 = _events(torch, lambda: ps.hide_communication(bw, k, args, comm=lambda: None, memopt=True), 5)
+    del T, T2, Ci
+    b = 3 * 8 * n ** 3
+    return {"boundary_width": list(bw), "one_launch_ms": round(t1 * 1e3, 4), "split_ms": round(t2 * 1e3, 4),
+            "one_launch_T_eff_GBs": round(b / t1 / 1e9, 1), "split_T_eff_GBs": round(b / t2 / 1e9, 1),
+            "launches": 8 * 8}
 
 
 def bench_stokes3d_solve(ps, n=127, tol=1e-6):
@@ -793,6 +849,14 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": "gemm", "n": n, "steps": a.steps}))
         return
+    if a.only_run == "fd":  # the FD-macro kernel of one statement, FP64, n^3, --steps calls
+        A, R = ps.rand(n, n, n, seed=4), ps.zeros(n, n, n)
+        k = ps.fd_kernel("@inn(R) = @d2_zi(A)")
+        for _ in range(a.steps):
+            ps.parallel(k, R, A, sync=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"only_run": "fd", "n": n, "steps": a.steps}))
+        return
     if a.only_run in ("stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint"):  # --steps calls, size --n
         from ps_gb300 import adjoint, stokes, stokes3d
 
@@ -885,7 +949,7 @@ def main():
     ap.add_argument("--loopsize", type=int, default=0, help="z indices per thread of memopt run-time compiled kernels")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
-                                                 "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint"], default=None,
+                                                 "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
                          "problem) and exit")

@@ -35,80 +35,106 @@ struct FdDesc {
     int64_t nR[3], nA[3], tmax[3];
 };
 
-template <typename T>
-__device__ __forceinline__ T fd_load(const T* A, const int64_t* nA, int64_t x, int64_t y, int64_t z) {
-    return A[x + nA[0] * (y + nA[1] * z)];
+// The operator of one macro, specialised at compile time on its kind and operated dimensions
+// (src/FiniteDifferences.jl: index patterns and operation orders), so the corners unroll into
+// register-indexed loads and the averaging weights are literals.
+__host__ __device__ constexpr int fd_dim(int opd, int j) {  // the j-th operated dimension
+    int n = 0;
+    for (int k = 0; k < 3; k++)
+        if ((opd >> k) & 1) {
+            if (n == j) return k;
+            n++;
+        }
+    return 0;
 }
+__host__ __device__ constexpr int fd_popc(int opd) { return (opd & 1) + ((opd >> 1) & 1) + ((opd >> 2) & 1); }
 
-template <typename T>
-__device__ T fd_eval(const FdDesc& d, const T* __restrict__ A, const int64_t t[3]) {
-    int64_t b[3];
-    for (int k = 0; k < 3; k++) b[k] = t[k] + ((d.inn >> k) & 1);
-    switch (d.kind) {
-    case PS_FD_SEL:
-        return fd_load(A, d.nA, b[0], b[1], b[2]);
-    case PS_FD_DIFF: {
-        int k = (d.opdims & 1) ? 0 : (d.opdims & 2) ? 1 : 2;
-        int64_t p[3] = {b[0], b[1], b[2]};
-        p[k] += 1;
-        return fd_load(A, d.nA, p[0], p[1], p[2]) - fd_load(A, d.nA, b[0], b[1], b[2]);
-    }
-    case PS_FD_DIFF2: {
-        int k = (d.opdims & 1) ? 0 : (d.opdims & 2) ? 1 : 2;
-        int64_t p[3] = {b[0], b[1], b[2]}, m[3] = {b[0], b[1], b[2]};
-        p[k] += 1;
-        m[k] -= 1;
-        T c = fd_load(A, d.nA, b[0], b[1], b[2]);
-        return (fd_load(A, d.nA, p[0], p[1], p[2]) - c) - (c - fd_load(A, d.nA, m[0], m[1], m[2]));
-    }
-    case PS_FD_AV:
-    case PS_FD_HARM: {
-        int dims[3], nd = 0;
-        for (int k = 0; k < 3; k++)
-            if ((d.opdims >> k) & 1) dims[nd++] = k;
-        int nc = 1 << nd;
+template <typename T, int KIND, int OPD>
+__device__ __forceinline__ T fd_eval_t(const T* __restrict__ A, int64_t c, const int64_t st[3]) {
+    if constexpr (KIND == PS_FD_SEL) {
+        return __ldg(A + c);
+    } else if constexpr (KIND == PS_FD_DIFF) {
+        const int64_t o = st[fd_dim(OPD, 0)];
+        return __ldg(A + c + o) - __ldg(A + c);
+    } else if constexpr (KIND == PS_FD_DIFF2) {
+        const int64_t o = st[fd_dim(OPD, 0)];
+        const T m = __ldg(A + c);
+        return (__ldg(A + c + o) - m) - (m - __ldg(A + c - o));
+    } else if constexpr (KIND == PS_FD_AV || KIND == PS_FD_HARM) {
+        constexpr int ND = fd_popc(OPD), NC = 1 << ND;
         T s = T(0);
-        for (int c = 0; c < nc; c++) {
-            int64_t p[3] = {b[0], b[1], b[2]};
-            for (int j = 0; j < nd; j++) p[dims[j]] += (c >> j) & 1;
-            T v = fd_load(A, d.nA, p[0], p[1], p[2]);
-            if (d.kind == PS_FD_HARM) v = T(1) / v;
-            s = (c == 0) ? v : s + v;
+#pragma unroll
+        for (int cc = 0; cc < NC; cc++) {  // first operated dimension fastest, as the macros list them
+            int64_t p = c;
+#pragma unroll
+            for (int j = 0; j < ND; j++)
+                if ((cc >> j) & 1) p += st[fd_dim(OPD, j)];
+            T v = __ldg(A + p);
+            if constexpr (KIND == PS_FD_HARM) v = T(1.0) / v;
+            s = cc == 0 ? v : s + v;
         }
-        if (d.kind == PS_FD_AV) return s * (T(1) / T(nc));
-        return (T(1) / s) * T(nc);
-    }
-    default: {  // maxloc / minloc
-        bool mx = d.kind == PS_FD_MAXLOC;
-        T m = T(0);
-        for (int k = 0; k < d.ndims; k++) {
-            int64_t p[3] = {b[0], b[1], b[2]}, q[3] = {b[0], b[1], b[2]};
-            p[k] -= 1;
-            q[k] += 1;
-            T lo = fd_load(A, d.nA, p[0], p[1], p[2]), hi = fd_load(A, d.nA, q[0], q[1], q[2]);
-            T pair = mx ? jl_max(lo, hi) : jl_min(lo, hi);
-            if (k == 0) {
-                T c = fd_load(A, d.nA, b[0], b[1], b[2]);
-                m = mx ? jl_max(pair, c) : jl_min(pair, c);
-            } else {
-                m = mx ? jl_max(m, pair) : jl_min(m, pair);
-            }
-        }
+        if constexpr (KIND == PS_FD_AV) return s * T(1.0 / NC);  // 0.5, 0.25, 0.125: exact literals
+        else return (T(1.0) / s) * T(NC);
+    } else {  // maxloc / minloc; OPD = ndims
+        constexpr bool MX = KIND == PS_FD_MAXLOC;
+        const auto f = [](T a, T b) { return MX ? jl_max(a, b) : jl_min(a, b); };
+        T m = f(f(__ldg(A + c - st[0]), __ldg(A + c + st[0])), __ldg(A + c));
+#pragma unroll
+        for (int k = 1; k < OPD; k++) m = f(m, f(__ldg(A + c - st[k]), __ldg(A + c + st[k])));
         return m;
     }
+}
+
+// Each thread evaluates FD_ZB consecutive z indices, their loads issued together (with one value
+// per thread in flight a one-point-per-thread kernel keeps too few bytes in flight for HBM).
+constexpr int FD_ZB = 4;
+
+template <typename T, int KIND, int OPD>
+__global__ void fd_apply_kernel(T* __restrict__ R, const T* __restrict__ A, FdDesc d) {
+    const int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (tx >= d.tmax[0] || ty >= d.tmax[1]) return;
+    const int64_t st[3] = {1, d.nA[0], d.nA[0] * d.nA[1]};
+    const int64_t bx = tx + (d.inn & 1), by = ty + ((d.inn >> 1) & 1), dz = (d.inn >> 2) & 1;
+    const int64_t rx = tx + (d.lhs_inn & 1), ry = ty + ((d.lhs_inn >> 1) & 1), rz0 = (d.lhs_inn >> 2) & 1;
+    const int64_t rs = d.nR[0] * d.nR[1];
+    for (int64_t z0 = (int64_t)blockIdx.z * FD_ZB; z0 < d.tmax[2]; z0 += (int64_t)gridDim.z * FD_ZB) {
+        T v[FD_ZB];
+#pragma unroll
+        for (int u = 0; u < FD_ZB; u++)
+            if (z0 + u < d.tmax[2]) v[u] = fd_eval_t<T, KIND, OPD>(A, bx + st[1] * by + st[2] * (z0 + u + dz), st);
+#pragma unroll
+        for (int u = 0; u < FD_ZB; u++)
+            if (z0 + u < d.tmax[2]) R[rx + d.nR[0] * ry + rs * (z0 + u + rz0)] = v[u];
     }
 }
 
 template <typename T>
-__global__ void fd_apply_kernel(T* __restrict__ R, const T* __restrict__ A, FdDesc d) {
-    int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
-    if (tx >= d.tmax[0] || ty >= d.tmax[1]) return;
-    for (int64_t tz = blockIdx.z; tz < d.tmax[2]; tz += gridDim.z) {
-        int64_t t[3] = {tx, ty, tz};
-        int64_t rx = tx + (d.lhs_inn & 1), ry = ty + ((d.lhs_inn >> 1) & 1), rz = tz + ((d.lhs_inn >> 2) & 1);
-        R[rx + d.nR[0] * (ry + d.nR[1] * rz)] = fd_eval(d, A, t);
+static int launch_fd(const FdDesc& d, T* R, const T* A, dim3 grd, dim3 blk, cudaStream_t s) {
+#define PS_FD_CASE(K, O) \
+    case O: fd_apply_kernel<T, K, O><<<grd, blk, 0, s>>>(R, A, d); return PS_OK;
+#define PS_FD_ONE_DIM(K) switch (d.opdims) { PS_FD_CASE(K, 1) PS_FD_CASE(K, 2) PS_FD_CASE(K, 4) }
+#define PS_FD_ANY_DIMS(K) \
+    switch (d.opdims) { PS_FD_CASE(K, 1) PS_FD_CASE(K, 2) PS_FD_CASE(K, 3) PS_FD_CASE(K, 4) PS_FD_CASE(K, 5) \
+                        PS_FD_CASE(K, 6) PS_FD_CASE(K, 7) }
+#define PS_FD_NDIMS(K) \
+    switch (d.ndims) { case 1: fd_apply_kernel<T, K, 1><<<grd, blk, 0, s>>>(R, A, d); return PS_OK; \
+                       case 2: fd_apply_kernel<T, K, 2><<<grd, blk, 0, s>>>(R, A, d); return PS_OK; \
+                       case 3: fd_apply_kernel<T, K, 3><<<grd, blk, 0, s>>>(R, A, d); return PS_OK; }
+    switch (d.kind) {
+    case PS_FD_SEL: fd_apply_kernel<T, PS_FD_SEL, 0><<<grd, blk, 0, s>>>(R, A, d); return PS_OK;
+    case PS_FD_DIFF: PS_FD_ONE_DIM(PS_FD_DIFF) break;
+    case PS_FD_DIFF2: PS_FD_ONE_DIM(PS_FD_DIFF2) break;
+    case PS_FD_AV: PS_FD_ANY_DIMS(PS_FD_AV) break;
+    case PS_FD_HARM: PS_FD_ANY_DIMS(PS_FD_HARM) break;
+    case PS_FD_MAXLOC: PS_FD_NDIMS(PS_FD_MAXLOC) break;
+    case PS_FD_MINLOC: PS_FD_NDIMS(PS_FD_MINLOC) break;
     }
+#undef PS_FD_CASE
+#undef PS_FD_ONE_DIM
+#undef PS_FD_ANY_DIMS
+#undef PS_FD_NDIMS
+    return fail(PS_ERR_ARG, "ps_fd_apply: unsupported operator (kind %d, dims %d)", d.kind, d.opdims);
 }
 
 // =======================================================================================
@@ -726,11 +752,11 @@ int ps_fd_apply(ps_fd_op op, int32_t lhs_inn, ps_array R, ps_array A, void* stre
     if (d.tmax[0] <= 0 || d.tmax[1] <= 0 || d.tmax[2] <= 0) return PS_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     dim3 blk(32, 8, 1);
-    dim3 grd = grid3(d.tmax[0], d.tmax[1], d.tmax[2], blk);
+    dim3 grd = grid3(d.tmax[0], d.tmax[1], (d.tmax[2] + FD_ZB - 1) / FD_ZB, blk);
     if (R.dtype == PS_F64)
-        fd_apply_kernel<double><<<grd, blk, 0, s>>>(static_cast<double*>(R.ptr), static_cast<const double*>(A.ptr), d);
+        PS_TRY(launch_fd<double>(d, static_cast<double*>(R.ptr), static_cast<const double*>(A.ptr), grd, blk, s));
     else
-        fd_apply_kernel<float><<<grd, blk, 0, s>>>(static_cast<float*>(R.ptr), static_cast<const float*>(A.ptr), d);
+        PS_TRY(launch_fd<float>(d, static_cast<float*>(R.ptr), static_cast<const float*>(A.ptr), grd, blk, s));
     return finish_launch(s, sync, "ps_fd_apply");
 }
 
