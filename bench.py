@@ -663,9 +663,11 @@ def bench_fd_macros(ps, torch, n=512):
             t = _events(torch, lambda: ps.parallel(k, R, A, sync=False), 10)
             j = ps.parallel_kernel(f"@parallel function f!(R, A)\n    {stmt}\n    return\nend")
             tj = _events(torch, lambda: ps.parallel(j, R, A, sync=False), 10)
+            tm = _events(torch, lambda: ps.parallel(j, R, A, sync=False, memopt=True), 10)
             out[f"{stmt} {tag}"] = {"ms": round(t * 1e3, 4), "T_eff_GBs": round(2 * es * n ** 3 / t / 1e9, 1),
-                                    "jit_ms": round(tj * 1e3, 4), "jit_T_eff_GBs": round(2 * es * n ** 3 / tj / 1e9, 1)}
-            launches += 2 * 13
+                                    "jit_ms": round(tj * 1e3, 4), "jit_T_eff_GBs": round(2 * es * n ** 3 / tj / 1e9, 1),
+                                    "jit_memopt_T_eff_GBs": round(2 * es * n ** 3 / tm / 1e9, 1)}
+            launches += 3 * 13
             del R
         del A
     torch.cuda.empty_cache()

@@ -978,8 +978,8 @@ class JitKernel:
         """Launch over `ranges` (default: the largest array extents; with `nblocks`, nblocks .* nthreads
         threads) in blocks of `nthreads` (default (32, 8, 1)) with `shmem` bytes of dynamic shared
         memory (src/ParallelKernel/parallel.jl:303-328). memopt (default: the definition's
-        `memopt=`) runs 3-D `@parallel` kernels as z sweeps of `loopsize` (default 64, as
-        src/parallel.jl:532-543 for compute capability >= 9) indices per thread; same results."""
+        `memopt=`, else true) runs 3-D `@parallel` kernels as z sweeps of `loopsize` (default 64,
+        as src/parallel.jl:532-543 for compute capability >= 9) indices per thread; same results."""
         require_initialized()
         if len(args) != self.nargs:
             raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
@@ -1014,7 +1014,10 @@ class JitKernel:
             if min(lo) < 0:
                 raise ArgumentError("ranges must start at index 1 or above")
             cnt = [max(0, hi[d] - lo[d]) for d in range(3)]
-        want = memopt if memopt is not None else self.kd.options.get("memopt", "false") == "true"
+        # the z sweep is the default schedule of 3-D @parallel kernels (bit-identical results, faster:
+        # a one-point-per-thread kernel keeps too few loads in flight); memopt=false keeps one point
+        # per thread, as the definition or the call may ask
+        want = memopt if memopt is not None else self.kd.options.get("memopt", "true") == "true"
         zl = bool(want) and self.kd.kind == "parallel" and ndims == 3
         zloop = 1
         if zl:
