@@ -318,6 +318,9 @@ def run_ours(a, world, rank, local):
             for opt, tag in (("", "jit"), ("inbounds=true ", "jit_inbounds")):  # run-time compiled, IEEE FP64
                 bench_kernel(f"diffusion3d_flux_lam_f64_{tag}", ps.parallel_kernel(JIT_FLUX_LAM.format(opt=opt)),
                              arrs64, (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
+            # the same run-time compiled body with its arithmetic on FP32 pairs (z sweep, default)
+            bench_kernel("diffusion3d_flux_lam_f64_jit_split", ps.parallel_kernel(JIT_FLUX_LAM.format(opt="")),
+                         arrs64, (dt, _dx, _dx, _dx), None, WORDS_FLUX_LAM, n, np.float64, a.steps, fp64="split")
         # e2e: diffusion jobs (NT_JOB steps each) through the C ABI from pinned host buffers: every
         # job copies its inputs T, Ci, lam host -> device, runs NT_JOB steps (T2 <- T on the device:
         # the run reads only T's boundary values from it) and copies T device -> host, all inside

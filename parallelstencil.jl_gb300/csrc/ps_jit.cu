@@ -31,7 +31,8 @@ struct ps_jit_args {
     double s[kJitMaxScalars];
     long long lo[3];   // first thread index (0-based) per dimension
     long long cnt[3];  // threads per dimension
-    int* err;          // error flags of the kernel (device memory, one int): 1 out of bounds, 2 partial block
+    int* err;          // error flags of the kernel (device memory, one int): 1 out of bounds, 2 partial block,
+                       // 4 a value outside the split FP64 range
     long long smem;    // dynamic shared memory bytes of this launch (@sharedMem views are checked against it)
     long long zloop;   // z indices per thread of a z-sweep (memopt) kernel; 1 otherwise
 };
@@ -198,6 +199,9 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
     if (flag) {
         cudaMemset(k->err, 0, sizeof(int));
         if (flag & 1) return fail(PS_ERR_ARG, "ps_jit_launch: out-of-bounds array access in the kernel (BoundsError)");
+        if (flag & 4)
+            return fail(PS_ERR_UNSUPPORTED, "ps_jit_launch: a value outside the split FP64 arithmetic's range "
+                                            "(|x| >= 2^128); run the kernel with fp64 = ieee");
         return fail(PS_ERR_ARG, "ps_jit_launch: a kernel with @sync_threads, shuffles or votes needs ranges that are "
                                 "a multiple of the thread block; a partial block did not run");
     }
@@ -216,6 +220,9 @@ int ps_jit_check(void* kernel, void* stream) {
     if (flag) {
         cudaMemset(k->err, 0, sizeof(int));
         if (flag & 1) return fail(PS_ERR_ARG, "ps_jit_check: out-of-bounds array access in the kernel (BoundsError)");
+        if (flag & 4)
+            return fail(PS_ERR_UNSUPPORTED, "ps_jit_check: a value outside the split FP64 arithmetic's range "
+                                            "(|x| >= 2^128); run the kernel with fp64 = ieee");
         return fail(PS_ERR_ARG, "ps_jit_check: a kernel with @sync_threads, shuffles or votes needs ranges that are "
                                 "a multiple of the thread block; a partial block did not run");
     }

@@ -314,8 +314,10 @@ def _lit(v):
 
 
 class _Gen:
-    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False):
+    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False, split: bool = False):
         self.kd, self.nd = kd, ndims
+        # FP64 arrays with the arithmetic on FP32 pairs (R = jd, storage E = double); see _JD below
+        self.split = bool(split)
         # memopt: each thread sweeps g.zloop consecutive z indices and carries read-only stencil
         # points it already holds to the next z (src/memopt.jl's register queue, in plain code)
         self.zloop = bool(zloop) and kd.kind == "parallel" and ndims == 3
@@ -362,6 +364,11 @@ class _Gen:
             return self.table[key]
         return self.load(name, [f"{t[d]}+{o[d]}" if o[d] else t[d] for d in range(self.nd)])
 
+    def wrap(self, ld):
+        """A value read from an FP64 array as the arithmetic type (an FP32 pair in split mode; a value
+        outside the pairs' range sets big_, reported with the next store)."""
+        return f"jd_in({ld}, big_)" if self.split else ld
+
     def fd_loads(self, p):
         """Declarations of the statement's registered loads, and the bounds condition that covers
         them all (per array: the stencil's largest offset in each dimension)."""
@@ -371,7 +378,7 @@ class _Gen:
             k = self.aidx[name]
             idx = [f"{t3[d]}+{o[d]}" if d < self.nd else "0" for d in range(3)]
             ref = f"a{k}[({idx[0]}) + n{k}_0 * (({idx[1]}) + n{k}_1 * ({idx[2]}))]"
-            decl.append(f"{p}    const R {var} = " + (f"__ldg(&{ref});" if name in self.read_only else f"{ref};"))
+            decl.append(f"{p}    const R {var} = " + self.wrap(f"__ldg(&{ref})" if name in self.read_only else ref) + ";")
             lo, hi = box.setdefault(k, ([0] * 3, [0] * 3))
             for d in range(self.nd):
                 lo[d], hi[d] = min(lo[d], o[d]), max(hi[d], o[d])
@@ -397,7 +404,7 @@ class _Gen:
             idx = [f"{t3[d]}+{o[d]}" for d in range(3)]
             ref = f"a{k}[({idx[0]}) + n{k}_0 * (({idx[1]}) + n{k}_1 * ({idx[2]}))]"
             ro = name in self.read_only
-            ld = f"__ldg(&{ref})" if ro else ref
+            ld = self.wrap(f"__ldg(&{ref})" if ro else ref)
             nxt = (name, (o[0], o[1], o[2] + 1))
             if ro and nxt in keys:
                 loads.append(f"{p}    const R {var} = pr{j} ? P{j}_{keys[nxt][1:]} : {ld};")
@@ -635,15 +642,18 @@ class _Gen:
             return f"((long long){r})" if fn == "__ballot_sync" else f"({r} != 0)"
         if len(args) not in (3, 4):
             raise ArgumentError(f"@{f[4:]}(mask, val, lane_or_delta[, width])")
-        t = "long long" if self.etype(args[1]) == "int" else "R"
+        t = "long long" if self.etype(args[1]) == "int" else "E"
         val = f"({t})({E(args[1], 'int' if t == 'long long' else 'real')})"
+        if t == "E":  # a real value is shuffled as the storage type (the pair's double in split mode)
+            val = f"({t})((R)({E(args[1], 'real')}))"
         arg = f"(int)({E(args[2], 'int')})"
         if f == "__m_shfl_sync":
             arg = f"({arg} - 1)"
         width = f", (int)({E(args[3], 'int')})" if len(args) == 4 else ""
         fn = {"__m_shfl_sync": "__shfl_sync", "__m_shfl_up_sync": "__shfl_up_sync",
               "__m_shfl_down_sync": "__shfl_down_sync", "__m_shfl_xor_sync": "__shfl_xor_sync"}[f]
-        return f"{fn}({mask}, {val}, {arg}{width})"
+        r = f"{fn}({mask}, {val}, {arg}{width})"
+        return f"((R)({r}))" if t == "E" else r
 
     def subscript(self, e, off=(0, 0, 0)):
         """`A[i, j, ...]` (1-based, Julia's `end` = size(A, d)) -> (A, 0-based index expressions)."""
@@ -673,13 +683,13 @@ class _Gen:
     # reads 0 (Julia's bounds check raises a BoundsError there)
     def load(self, name, ix):
         if name in self.shared:  # @sharedMem arrays are always bounds-checked (extents and the launch's shmem)
-            return f"jl_lds({self.smem_ref(name, ix)}, g.err)"
+            return self.wrap(f"jl_lds({self.smem_ref(name, ix)}, g.err)")
         ro = name in self.read_only
         if not self.checked:
-            return f"__ldg(&{self.at(name, ix)})" if ro else self.at(name, ix)
+            return self.wrap(f"__ldg(&{self.at(name, ix)})" if ro else self.at(name, ix))
         k = self.aidx[name]
         ix = list(ix) + ["0"] * (3 - len(ix))
-        return f"jl_ld{'g' if ro else ''}(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)"
+        return self.wrap(f"jl_ld{'g' if ro else ''}(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err)")
 
     # ---- local variables of @parallel_indices bodies (Julia function scope: declared at the top)
     def infer_locals(self, stmts):
@@ -728,9 +738,9 @@ class _Gen:
         ext = [f"({self.expr(d, ctx='int')})" for d in dims] + ["1LL"] * (3 - len(dims))
         offs = f"({self.expr(args[2], ctx='int')})" if len(args) == 3 else "0LL"
         self.kernel_language = True
-        return [f"{p}sm{j}_off = {offs}; sm{j} = (R*)(ps_smem + (sm{j}_off > 0 ? sm{j}_off : 0));",
+        return [f"{p}sm{j}_off = {offs}; sm{j} = (E*)(ps_smem + (sm{j}_off > 0 ? sm{j}_off : 0));",
                 f"{p}sm{j}_n0 = {ext[0]}; sm{j}_n1 = {ext[1]}; sm{j}_n2 = {ext[2]};",
-                f"{p}sm{j}_cap = (g.smem - sm{j}_off) / (long long)sizeof(R);"]
+                f"{p}sm{j}_cap = (g.smem - sm{j}_off) / (long long)sizeof(E);"]
 
     def stmt(self, s, ind):
         p = "    " * ind
@@ -795,7 +805,7 @@ class _Gen:
             self.table = {}
             rhs = self.expr(s.value)
             decl, box = self.fd_loads(p)
-            store = f"{p}    {self.at(name, idx)} = {rhs};"
+            store = f"{p}    {self.at(name, idx)} = (E)({rhs});" + (" if (big_) atomicOr(g.err, 4);" if self.split else "")
             if self.zloop:
                 out = self.zloop_statement(p, cond, box, decl, store)
                 self.table = None
@@ -809,13 +819,14 @@ class _Gen:
         if isinstance(t, ast.Subscript):  # @parallel_indices: A[i, j] = expr
             name, ix = self.subscript(t)
             val = self.expr(s.value, ctx="real")
+            chk = " if (big_) atomicOr(g.err, 4);" if self.split else ""
             if name in self.shared:
-                return [f"{p}jl_sts({self.smem_ref(name, ix)}, g.err, (R)({val}));"]
+                return [f"{p}jl_sts({self.smem_ref(name, ix)}, g.err, (E)((R)({val})));{chk}"]
             if not self.checked:
-                return [f"{p}{self.at(name, ix)} = (R)({val});"]
+                return [f"{p}{self.at(name, ix)} = (E)((R)({val}));{chk}"]
             k = self.aidx[name]
             ix = list(ix) + ["0"] * (3 - len(ix))
-            return [f"{p}jl_st(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err, (R)({val}));"]
+            return [f"{p}jl_st(a{k}, n{k}_0, n{k}_1, n{k}_2, {ix[0]}, {ix[1]}, {ix[2]}, g.err, (E)((R)({val})));{chk}"]
         raise ArgumentError("unsupported left-hand side")
 
     def collect_temps(self):
@@ -841,6 +852,13 @@ class _Gen:
                                     f"is not read-only within the scope of the kernel (any of: {sorted(writes)}).")
             self.temps[name] = (self.sels[sel], s.value)
 
+    def types(self, real):
+        if self.split:
+            if real != "double":
+                raise ArgumentError("fp64='split' applies to FP64 arrays")
+            return "typedef double E;" + _JD + "typedef jd R;"
+        return f"typedef {real} R;\ntypedef R E;"
+
     def source(self, real):
         kd = self.kd
         self.collect_temps()
@@ -848,17 +866,19 @@ class _Gen:
         body = []
         for s in kd.body:
             body += self.stmt(s, 1)
-        decl = []
+        decl = ["    bool big_ = false;"] if self.split else []
         for name, k in self.aidx.items():
-            decl.append(f"    R* const a{k} = (R*)g.a[{k}];")
+            decl.append(f"    E* const a{k} = (E*)g.a[{k}];")
             decl.append(f"    const long long n{k}_0 = g.n[{k}][0], n{k}_1 = g.n[{k}][1], n{k}_2 = g.n[{k}][2];")
         for name, k in self.sidx.items():
-            ty = "long long" if name in kd.int_scalars else "R"
-            decl.append(f"    const {ty} s{k} = ({ty})g.s[{k}];")
+            if name in kd.int_scalars:
+                decl.append(f"    const long long s{k} = (long long)g.s[{k}];")
+            else:
+                decl.append(f"    const R s{k} = {self.wrap(f'g.s[{k}]') if self.split else f'(R)g.s[{k}]'};")
         for name, t in self.locals.items():
             if t == "shared":
                 j = self.shared[name]
-                decl.append(f"    R* sm{j} = nullptr; long long sm{j}_off = 0, sm{j}_n0 = 0, sm{j}_n1 = 1, "
+                decl.append(f"    E* sm{j} = nullptr; long long sm{j}_off = 0, sm{j}_n0 = 0, sm{j}_n1 = 1, "
                             f"sm{j}_n2 = 1, sm{j}_cap = 0;")
             else:
                 decl.append(f"    {'long long' if t == 'int' else 'R'} v_{name} = 0;")
@@ -884,23 +904,23 @@ class _Gen:
         pos = "const long long tx = g.lo[0] + ux, ty = g.lo[1] + uy" + ("" if self.zloop else ", tz = g.lo[2] + uz")
         uzdecl = "" if self.zloop else "\n    const long long uz = blockIdx.z * (long long)blockDim.z + threadIdx.z;"
         return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{', z sweep' if self.zloop else ''}) -- generated by ps_gb300.jit
-typedef {real} R;
+{self.types(real)}
 struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long zloop; }};
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
-__device__ __forceinline__ R jl_ld(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
+__device__ __forceinline__ E jl_ld(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
     if (jl_in(n0, n1, n2, i, j, k)) return a[i + n0 * (j + n1 * k)];
-    atomicOr(err, 1); return (R)0; }}
-__device__ __forceinline__ R jl_ldg(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
+    atomicOr(err, 1); return (E)0; }}
+__device__ __forceinline__ E jl_ldg(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
     if (jl_in(n0, n1, n2, i, j, k)) return __ldg(&a[i + n0 * (j + n1 * k)]);
-    atomicOr(err, 1); return (R)0; }}
-__device__ __forceinline__ void jl_st(R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err, R v) {{
+    atomicOr(err, 1); return (E)0; }}
+__device__ __forceinline__ void jl_st(E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err, E v) {{
     if (jl_in(n0, n1, n2, i, j, k)) a[i + n0 * (j + n1 * k)] = v; else atomicOr(err, 1); }}
-__device__ __forceinline__ R jl_lds(const R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, long long cap, int* err) {{
+__device__ __forceinline__ E jl_lds(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, long long cap, int* err) {{
     const long long l = i + n0 * (j + n1 * k);
     if (a && jl_in(n0, n1, n2, i, j, k) && l < cap) return a[l];
-    atomicOr(err, 1); return (R)0; }}
-__device__ __forceinline__ void jl_sts(R* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, long long cap, int* err, R v) {{
+    atomicOr(err, 1); return (E)0; }}
+__device__ __forceinline__ void jl_sts(E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, long long cap, int* err, E v) {{
     const long long l = i + n0 * (j + n1 * k);
     if (a && jl_in(n0, n1, n2, i, j, k) && l < cap) a[l] = v; else atomicOr(err, 1); }}
 __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov.u32 %0, %%laneid;" : "=r"(l)); return l; }}
@@ -920,6 +940,79 @@ extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
 """
 
 
+# Split FP64 arithmetic for generated kernels: FP64 values as FP32 pairs (h + l, 47-bit
+# significands rounded to nearest; |x| < 2^128, magnitudes below 2^-126 flush to 0), split from
+# doubles with integer operations, sums by exact two-sums, products with FMA error terms, division
+# by one correction step, comparisons and math functions through FP64; results are written back as
+# FP64. Each operation is exact to ~2^-46 of its operands' magnitude.
+_JD = r"""
+__device__ __forceinline__ double jd_f64(float f) {  // exact float -> double with integer operations
+    const unsigned b = __float_as_uint(f);
+    unsigned hi = (((b >> 3) & 0x0FFFFFFFu) + 0x38000000u) | (b & 0x80000000u);
+    hi = (b & 0x7F800000u) ? hi : (b & 0x80000000u);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+__device__ __forceinline__ void jd_split2(double x, float& h, float& l, bool& big) {
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned t = hw & 0x7FFFFFFFu, sgn = hw & 0x80000000u;
+    const unsigned fb = __funnelshift_l(lw, hw, 3) ^ 0x40000000u;
+    h = __uint_as_float((fb & 0x7FFFFFFFu) | sgn);
+    // the next 23 bits, rounded to nearest at the 47th (an unbiased split)
+    const unsigned mi = ((lw >> 6) & 0x7FFFFFu) + ((lw >> 5) & 1u);
+    const float m = __uint_as_float(mi | 0x4B000000u) - 8388608.0f;
+    const unsigned sb = (((hw << 3) & 0xFF800000u) - 0xD7000000u) | sgn;
+    l = m * __uint_as_float(sb);
+    h = t < 0x38100000u ? 0.0f : h;
+    l = t < 0x3AF00000u ? 0.0f : l;
+    big |= t >= 0x47F00000u;
+}
+struct jd {
+    float h, l;
+    __device__ __forceinline__ jd() : h(0.0f), l(0.0f) {}
+    __device__ __forceinline__ jd(float h_, float l_) : h(h_), l(l_) {}
+    __device__ __forceinline__ jd(double x) { bool b = false; jd_split2(x, h, l, b); }
+    __device__ __forceinline__ jd(long long v) : jd((double)v) {}
+    __device__ __forceinline__ jd(int v) : jd((double)v) {}
+    __device__ __forceinline__ explicit operator double() const { return jd_f64(h) + jd_f64(l); }
+};
+__device__ __forceinline__ jd jd_in(double x, bool& big) { jd r; jd_split2(x, r.h, r.l, big); return r; }
+__device__ __forceinline__ jd jd_fast2(float s, float e) { const float h = s + e; return jd(h, e - (h - s)); }
+__device__ __forceinline__ jd operator+(jd a, jd b) {
+    const float s = a.h + b.h, bb = s - a.h, e = (a.h - (s - bb)) + (b.h - bb);
+    return jd_fast2(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ jd operator-(jd a) { return jd(-a.h, -a.l); }
+__device__ __forceinline__ jd operator-(jd a, jd b) { return a + (-b); }
+__device__ __forceinline__ jd operator*(jd a, jd b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return jd_fast2(p, e);
+}
+__device__ __forceinline__ jd operator/(jd a, jd b) {
+    const float q1 = a.h / b.h;
+    const jd r = a - jd(q1, 0.0f) * b;
+    return jd_fast2(q1, r.h / b.h);
+}
+__device__ __forceinline__ bool operator<(jd a, jd b) { return (double)a < (double)b; }
+__device__ __forceinline__ bool operator>(jd a, jd b) { return (double)a > (double)b; }
+__device__ __forceinline__ bool operator<=(jd a, jd b) { return (double)a <= (double)b; }
+__device__ __forceinline__ bool operator>=(jd a, jd b) { return (double)a >= (double)b; }
+__device__ __forceinline__ bool operator==(jd a, jd b) { return (double)a == (double)b; }
+__device__ __forceinline__ bool operator!=(jd a, jd b) { return (double)a != (double)b; }
+__device__ __forceinline__ bool signbit(jd a) { return signbit(a.h); }
+__device__ __forceinline__ bool isnan(jd a) { return isnan(a.h) || isnan(a.l); }
+__device__ __forceinline__ jd fabs(jd a) { return signbit(a.h) ? -a : a; }
+__device__ __forceinline__ jd copysign(jd a, jd b) { const jd m = fabs(a); return signbit(b.h) ? -m : m; }
+#define JD_F1(f) __device__ __forceinline__ jd f(jd a) { return jd(::f((double)a)); }
+JD_F1(exp) JD_F1(log) JD_F1(sqrt) JD_F1(sin) JD_F1(cos) JD_F1(tan) JD_F1(tanh) JD_F1(sinh) JD_F1(cosh)
+JD_F1(atan) JD_F1(asin) JD_F1(acos) JD_F1(log10) JD_F1(exp2) JD_F1(cbrt) JD_F1(trunc)
+__device__ __forceinline__ jd pow(jd a, jd b) { return jd(::pow((double)a, (double)b)); }
+__device__ __forceinline__ jd fmod(jd a, jd b) { return jd(::fmod((double)a, (double)b)); }
+"""
+
+
 def _is_sel_assign(s):
     t = s.targets[0] if isinstance(s, ast.Assign) and len(s.targets) == 1 else None
     return isinstance(t, ast.Subscript) and isinstance(t.value, ast.Name) and t.value.id.startswith("__lhs_") \
@@ -932,8 +1025,8 @@ def generate(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False) -> str:
     return _Gen(kd, ndims, zloop).source(dtype)
 
 
-def _generate_info(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False):
-    g = _Gen(kd, ndims, zloop)
+def _generate_info(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False, split: bool = False):
+    g = _Gen(kd, ndims, zloop, split)
     src = g.source(dtype)
     return src, g.uses_collectives
 
@@ -959,27 +1052,29 @@ class JitKernel:
     def source(self, ndims, dtype="double"):
         return generate(self.kd, ndims, dtype)
 
-    def _handle(self, ndims, dtype, zloop=False):
-        key = (ndims, dtype, bool(zloop))
+    def _handle(self, ndims, dtype, zloop=False, split=False):
+        key = (ndims, dtype, bool(zloop), bool(split))
         if key not in self._handles:
-            src, self._collective[key] = _generate_info(self.kd, ndims, dtype, zloop)
+            src, self._collective[key] = _generate_info(self.kd, ndims, dtype, zloop, split)
             h = ctypes.c_void_p()
             _lib.call("ps_jit_compile", src.encode(), b"ps_jit_entry", ctypes.byref(h))
             self._handles[key] = h
         return self._handles[key]
 
     def __call__(self, *args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None,
-                 memopt=None, loopsize=0):
+                 memopt=None, loopsize=0, fp64="ieee"):
         self.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem, memopt=memopt,
-                        loopsize=loopsize)
+                        loopsize=loopsize, fp64=fp64)
 
     def jit_launch(self, args, ranges=None, stream=None, sync=True, nblocks=None, nthreads=None, shmem=None,
-                   memopt=None, loopsize=0):
+                   memopt=None, loopsize=0, fp64="ieee"):
         """Launch over `ranges` (default: the largest array extents; with `nblocks`, nblocks .* nthreads
         threads) in blocks of `nthreads` (default (32, 8, 1)) with `shmem` bytes of dynamic shared
         memory (src/ParallelKernel/parallel.jl:303-328). memopt (default: the definition's
         `memopt=`, else true) runs 3-D `@parallel` kernels as z sweeps of `loopsize` (default 64,
-        as src/parallel.jl:532-543 for compute capability >= 9) indices per thread; same results."""
+        as src/parallel.jl:532-543 for compute capability >= 9) indices per thread; same results.
+        fp64="split" evaluates the arithmetic of FP64 kernels on FP32 pairs (each operation within
+        ~2^-46 of its operands' magnitude; GB300 issues FP32 at 64x the FP64 rate)."""
         require_initialized()
         if len(args) != self.nargs:
             raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
@@ -1025,8 +1120,11 @@ class JitKernel:
             if zloop < 1:
                 raise ArgumentError("loopsize must be positive")
             threads[2] = 1
-        h = self._handle(ndims, dt, zl)
-        if self._collective[(ndims, dt, zl)] and any(cnt[d] % threads[d] for d in range(3)):
+        if fp64 not in ("ieee", "split", "split_state", "split_grid"):
+            raise ArgumentError("fp64 must be 'ieee' or 'split'")
+        sp = fp64 != "ieee" and dt == "double"
+        h = self._handle(ndims, dt, zl, sp)
+        if self._collective[(ndims, dt, zl, sp)] and any(cnt[d] % threads[d] for d in range(3)):
             raise ArgumentError("a kernel with @sync_threads, shuffles or votes needs ranges that are a multiple of "
                                 f"the thread block (ranges {cnt}, nthreads {threads})")
         A = (PSArray * max(1, len(descs)))(*descs)

@@ -175,7 +175,7 @@ def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, s
     require_initialized()
     if hasattr(kernel, "jit_launch"):  # run-time compiled kernel (ps_gb300.jit); memopt does not change results
         kernel.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem, memopt=memopt,
-                          loopsize=loopsize)
+                          loopsize=loopsize, fp64=fp64)
         return
     if nblocks is not None or nthreads is not None or shmem is not None:
         raise ArgumentError("nblocks / nthreads / shmem apply to run-time compiled kernels (parallel_kernel)")

@@ -414,3 +414,65 @@ def test_jit_hide_communication_equals_one_launch(ps, name):
         assert np.array_equal(ps.to_host(a), ps.to_host(b))
     with pytest.raises(ps.ArgumentError, match="boundary_width"):
         ps.hide_communication((40, 4, 2), k, (*out, *rest))
+
+
+# ---------------------------------------------------------------- split FP64 arithmetic
+@pytest.mark.parametrize("name", sorted(_cases(np.float64)))
+def test_jit_split_fp64_close_to_ieee(ps, name):
+    """fp64="split" (FP64 arrays, arithmetic on FP32 pairs) against the IEEE run of the same kernel:
+    within 1e-12 of the largest output magnitude (each operation is exact to ~2^-46 of its
+    operands; the kernels here chain up to ~60 operations, some with cancellation)."""
+    args, ranges = _cases(np.float64)[name]
+    src = getattr(K, name)
+    k = ps.parallel_kernel(src, ndims=_NDIMS.get(name))
+    out = {}
+    for fp64 in ("ieee", "split"):
+        dev = [_dev(ps, a) if isinstance(a, np.ndarray) else a for a in args]
+        ps.parallel(k, *dev, ranges=ranges, fp64=fp64)
+        out[fp64] = [ps.to_host(d) for d in dev if not isinstance(d, (int, float))]
+    worst = 0.0
+    for a, b in zip(out["ieee"], out["split"]):
+        scale = max(np.abs(a).max(), 1e-300)
+        worst = max(worst, np.abs(a - b).max() / scale)
+    assert worst <= 1e-12, (name, worst)
+
+
+def test_jit_split_fp64_diffusion_run(ps):
+    """The headline body in split FP64 arithmetic: 1 step within 1e-13 and 20 steps within 1e-12 of the
+    IEEE run (relative max-norm), and really a different arithmetic."""
+    import bench
+
+    rng = np.random.default_rng(12)
+    n = (64, 48, 40)
+    T0, Ci, lam = rng.random(n), rng.random(n) + 0.5, rng.random(n) + 1.0
+    k = ps.parallel_kernel(bench.JIT_FLUX_LAM.format(opt=""))
+    sc = (1e-4, 20.0, 20.0, 20.0)
+    res = {}
+    for fp64 in ("ieee", "split"):
+        A, B = _dev(ps, T0), _dev(ps, T0)
+        dCi, dlam = _dev(ps, Ci), _dev(ps, lam)
+        for it in range(20):
+            ps.parallel(k, B, A, dCi, dlam, *sc, fp64=fp64)
+            A, B = B, A
+            if it == 0:
+                res[(fp64, 1)] = ps.to_host(A)
+        res[(fp64, 20)] = ps.to_host(A)
+    for nt, tol in ((1, 1e-13), (20, 1e-12)):
+        a, b = res[("ieee", nt)], res[("split", nt)]
+        err = np.abs(a - b).max() / np.abs(a).max()
+        assert err <= tol, (nt, err)
+    assert not np.array_equal(res[("ieee", 1)], res[("split", 1)])
+
+
+def test_jit_split_fp64_range_flag(ps):
+    """A value beyond the pairs' range (|x| >= 2^128) is reported, not silently wrong."""
+    from ps_gb300._lib import PSError
+
+    k = ps.parallel_kernel("@parallel function sc!(B, A, s)\n    @all(B) = s*@all(A)\n    return\nend")
+    A = _dev(ps, np.full((8, 8, 8), 1e40))
+    B = ps.zeros(8, 8, 8)
+    with pytest.raises(PSError, match="split FP64") as e:
+        ps.parallel(k, B, A, 2.0, fp64="split")
+    assert e.value.status == -12
+    ps.parallel(k, B, A, 2.0)  # IEEE: fine, and the flag was cleared
+    assert np.all(ps.to_host(B) == 2e40)
