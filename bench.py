@@ -575,6 +575,19 @@ def bench_warm_start(seeds, n=1023, tol=1e-8):
     return out
 
 
+# the acoustic3D update statements as kernel definitions (the bodies `from_source` recognises)
+ACOUSTIC_V = """@parallel function compute_V!(Vx, Vy, Vz, P, dt, ρ, dx, dy, dz)
+    @inn(Vx) = @inn(Vx) - dt/ρ*@d_xi(P)/dx
+    @inn(Vy) = @inn(Vy) - dt/ρ*@d_yi(P)/dy
+    @inn(Vz) = @inn(Vz) - dt/ρ*@d_zi(P)/dz
+    return
+end"""
+ACOUSTIC_P = """@parallel function compute_P!(P, Vx, Vy, Vz, dt, k, dx, dy, dz)
+    @all(P) = @all(P) - dt*k*(@d_xa(Vx)/dx + @d_ya(Vy)/dy + @d_za(Vz)/dz)
+    return
+end"""
+
+
 def _events(torch, fn, reps):
     """Seconds per call of fn() over `reps` calls (CUDA events on the current stream, after 3 warm-ups)."""
     for _ in range(3):
@@ -639,6 +652,18 @@ def bench_miniapps(ps, torch, peak):
         t = _events(torch, acoustic_step, 50)
         out[f"acoustic3d_{n}_{tag}"] = {"ms": round(t * 1e3, 4), "T_eff_GBs": round(8 * es * n ** 3 / t / 1e9, 1)}
         launches += 2 * 53
+        if dt == np.float64:  # the same two statements run-time compiled, IEEE and split FP64 arithmetic
+            kv = ps.parallel_kernel(ACOUSTIC_V)
+            kp = ps.parallel_kernel(ACOUSTIC_P)
+            for fp64 in ("ieee", "split"):
+                def jit_step():
+                    ps.parallel(kv, Vx, Vy, Vz, P, dts, 1.0, h, h, h, sync=False, fp64=fp64)
+                    ps.parallel(kp, P, Vx, Vy, Vz, dts, 1.0, h, h, h, sync=False, fp64=fp64)
+
+                tj = _events(torch, jit_step, 20)
+                out[f"acoustic3d_{n}_{tag}_jit_{fp64}"] = {"ms": round(tj * 1e3, 4),
+                                                           "T_eff_GBs": round(8 * es * n ** 3 / tj / 1e9, 1)}
+                launches += 2 * 23
         del P, Vx, Vy, Vz
     torch.cuda.empty_cache()
     out["peak_hbm_gbs"] = peak
@@ -947,7 +972,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--quick", action="store_true", help="headline + e2e only")
-    ap.add_argument("--e2e-jobs", type=int, default=8, help="diffusion jobs of the e2e measurement (pipelined)")
+    ap.add_argument("--e2e-jobs", type=int, default=16, help="diffusion jobs of the e2e measurement (pipelined)")
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ref-slab", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
