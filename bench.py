@@ -454,6 +454,9 @@ def run_ours(a, world, rank, local):
         hide = None if a.quick else bench_hide_communication(ps, torch)
         if hide:
             launches += hide.pop("launches")
+        sweep2d = None if a.quick else bench_sweep_2d(ps, torch)
+        if sweep2d:
+            launches += sweep2d.pop("launches")
     clocks = clk.summary()
 
     value = job_value(world, b_head, t_head) / 1e9
@@ -490,11 +493,14 @@ def run_ours(a, world, rank, local):
         "stokes3d_time_to_tol": s3solve,
         "fd_macros_512": fdm,
         "hide_communication_512": hide,
+        "memopt_2d_8192": sweep2d,
         "clocks": clocks,
         "variants": results,
     }
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(a, n)
+        if not a.quick:
+            out["cpu_baseline"]["miniapps"] = cpu_miniapps()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -680,7 +686,7 @@ FD_STATEMENTS = {"@all(R) = @d_xa(A)": (-1, 0, 0), "@inn(R) = @d2_zi(A)": (0, 0,
 def bench_fd_macros(ps, torch, n=512):
     """One-statement FiniteDifferences kernels (`@parallel f!(R, A) = (@<sel>(R) = @<op>(A))`) on
     n^3 arrays through ps_fd_apply: T_eff with 2 words per cell (A read, R written), FP64 and FP32,
-    and the same statement as a run-time compiled kernel."""
+    and the same statement as a run-time compiled kernel, one point per thread and as a z sweep."""
     out, launches = {}, 0
     for dt, tag in ((np.float64, "f64"), (np.float32, "f32")):
         A = ps.rand(n, n, n, dtype=dt, seed=4)
@@ -690,7 +696,7 @@ def bench_fd_macros(ps, torch, n=512):
             k = ps.fd_kernel(stmt)
             t = _events(torch, lambda: ps.parallel(k, R, A, sync=False), 10)
             j = ps.parallel_kernel(f"@parallel function f!(R, A)\n    {stmt}\n    return\nend")
-            tj = _events(torch, lambda: ps.parallel(j, R, A, sync=False), 10)
+            tj = _events(torch, lambda: ps.parallel(j, R, A, sync=False, memopt=False), 10)
             tm = _events(torch, lambda: ps.parallel(j, R, A, sync=False, memopt=True), 10)
             out[f"{stmt} {tag}"] = {"ms": round(t * 1e3, 4), "T_eff_GBs": round(2 * es * n ** 3 / t / 1e9, 1),
                                     "jit_ms": round(tj * 1e3, 4), "jit_T_eff_GBs": round(2 * es * n ** 3 / tj / 1e9, 1),
@@ -700,6 +706,36 @@ def bench_fd_macros(ps, torch, n=512):
         del A
     torch.cuda.empty_cache()
     out["launches"] = launches
+    return out
+
+
+HEAT2D = """@parallel function heat2d!(T2, T, Ci, lam, dt, _dx, _dy)
+    @inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)*_dx*_dx + @d2_yi(T)*_dy*_dy))
+    return
+end"""
+
+
+def bench_sweep_2d(ps, torch, n=8192):
+    """A 2-D `@parallel` diffusion step (FiniteDifferences2D, n^2, FP64 and FP32) run-time compiled:
+    one point per thread (memopt=false) against the y sweep (memopt=true, src/memopt.jl's loopdim 2);
+    T_eff with 3 words per cell (T and Ci read, T2 written)."""
+    out = {}
+    k = ps.parallel_kernel(HEAT2D)
+    for dt, tag in ((np.float64, "f64"), (np.float32, "f32")):
+        T = ps.rand(n, n, dtype=dt, seed=5)
+        T2, Ci = ps.zeros(n, n, dtype=dt), ps.ones(n, n, dtype=dt)
+        h = (n - 1) / 10.0
+        args = (T2, T, Ci, 1.0, 1e-4 / h ** 2, h, h)
+        b = 3 * np.dtype(dt).itemsize * n * n
+        row = {}
+        for name, memopt in (("plain", False), ("y_sweep", True)):
+            t = _events(torch, lambda: ps.parallel(k, *args, memopt=memopt, sync=False), 20)
+            row[f"{name}_ms"] = round(t * 1e3, 4)
+            row[f"{name}_T_eff_GBs"] = round(b / t / 1e9, 1)
+        out[f"heat2d_{n}_{tag}"] = row
+        del T, T2, Ci
+    torch.cuda.empty_cache()
+    out["launches"] = 2 * 2 * 23
     return out
 
 
@@ -833,6 +869,55 @@ def cpu_baseline(a, n):
     return {"value": round(teff, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port",
             "sample": f"{a.cpu_steps} steps of the oracle (C/OpenMP, -O3) over a {n}x{n}x{slab} z-slab of the "
                       f"{n}^3 FP64 flux-lam job ({secs * 1e3:.1f} ms/step)"}
+
+
+def cpu_miniapps(iters=10):
+    """The oracle's loop bodies of the miniapps timed on the host cores (FP64, the GPU lines' sizes
+    and A_eff): Stokes2D 1023^2, Stokes3D 127^3, acoustic3D 255^3; `iters` iterations each after one
+    untimed iteration."""
+    import oracle
+
+    from ps_gb300 import stokes, stokes3d
+
+    def timed(step):
+        step()
+        t0 = time.perf_counter()
+        for _ in range(iters):
+            step()
+        return (time.perf_counter() - t0) / iters
+
+    out = {}
+    n = 1023
+    Mus, Rog = stokes.inclusion_setup(n, n, 1.0, 1.0, musi=0.1, radius=0.1)
+    p = stokes.Stokes2DParams(n, n, 1.0, 1.0)
+    o = oracle.Stokes2D(n, n, p.dx, p.dy, Mus, Rog)
+    o.compute_timesteps()
+    t = timed(o.step)
+    out[f"stokes2d_{n}_f64"] = {"ms": round(t * 1e3, 3), "T_eff_GBs": round(6 * 8 * n * n / t / 1e9, 2)}
+    del o
+    n = 127
+    Mus, Rog = stokes3d.inclusion_setup(n, n, n)
+    p3 = stokes3d.Stokes3DParams(n, n, n)
+    o = oracle.Stokes3D(n, n, n, *p3.h, Mus, Rog)
+    o.compute_timesteps()
+    t = timed(o.step)
+    out[f"stokes3d_{n}_f64"] = {"ms": round(t * 1e3, 3), "T_eff_GBs": round(8 * 8 * n ** 3 / t / 1e9, 2)}
+    del o
+    n = 255
+    h = 40.0 / (n - 1)
+    P = np.asfortranarray(np.ones((n, n, n)))
+    Vx, Vy, Vz = (np.asfortranarray(np.zeros(s)) for s in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1)))
+    dts = h / 6.1
+
+    def acoustic_step():
+        oracle.acoustic3d_v(Vx, Vy, Vz, P, dts, 1.0, h, h, h)
+        oracle.acoustic3d_p(P, Vx, Vy, Vz, dts, 1.0, h, h, h)
+
+    t = timed(acoustic_step)
+    out[f"acoustic3d_{n}_f64"] = {"ms": round(t * 1e3, 3), "T_eff_GBs": round(8 * 8 * n ** 3 / t / 1e9, 2)}
+    out["cores"] = oracle.num_threads()
+    out["sample"] = f"{iters} iterations of each miniapp's loop body (C/OpenMP oracle, FP64)"
+    return out
 
 
 def run_reference(a, world, rank):

@@ -402,10 +402,10 @@ int ps_stokes3d_solve_mixed(const ps_stokes3d_fields* f, const ps_stokes3d_param
  * contraction, and load it on the current device. `entry` is the extern "C" kernel, which takes
  * one argument block by value:
  *   struct { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err;
- *            long long smem; long long zloop; }
+ *            long long smem; long long loop; }
  * (array pointers and extents, scalars, first thread index and thread counts per dimension, the
  * kernel's error flags -- one device int owned by the handle --, the launch's dynamic shared
- * memory bytes and the z indices per thread of a z-sweep kernel).
+ * memory bytes and the indices per thread of a sweep kernel).
  * Compile errors return PS_ERR_ARG with the compiler log in ps_last_error(). */
 int ps_jit_compile(const char* source, const char* entry, void** kernel);
 /* Launch a compiled kernel over count[0] x count[1] x count[2] threads starting at thread index
@@ -418,11 +418,13 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
  * `@parallel nblocks nthreads shmem=... kernel!(...)` (src/ParallelKernel/parallel.jl:303-328,
  * 883-898). Kernels that use @sync_threads, warp shuffles or votes need count[d] to be a multiple of
  * threads[d]; a partial block leaves before its first barrier and the launch returns PS_ERR_ARG.
- * zloop > 1 (with threads[2] == 1) launches a z-sweep kernel (memopt, generated for it): each
- * thread covers zloop consecutive z indices; 1 for every other kernel. */
+ * loop (NULL: 1, 1, 1) gives the indices per thread along each dimension: a sweep kernel (memopt,
+ * generated for it) has loop[d] > 1 in its sweep dimension d (z in 3-D, y in 2-D; src/memopt.jl's
+ * loopdim), with threads[d] == 1 there, and each thread covers loop[d] consecutive indices; every
+ * other kernel takes 1, 1, 1. */
 int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                      const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
-                     int32_t zloop, void* stream, int sync);
+                     const int32_t loop[3], void* stream, int sync);
 /* Wait for `stream`, then report (and clear) the error flags left by earlier asynchronous launches
  * of `kernel`, as a synchronous launch does. */
 int ps_jit_check(void* kernel, void* stream);

@@ -34,7 +34,7 @@ struct ps_jit_args {
     int* err;          // error flags of the kernel (device memory, one int): 1 out of bounds, 2 partial block,
                        // 4 a value outside the split FP64 range
     long long smem;    // dynamic shared memory bytes of this launch (@sharedMem views are checked against it)
-    long long zloop;   // z indices per thread of a z-sweep (memopt) kernel; 1 otherwise
+    long long loop;    // indices per thread along the sweep dimension of a sweep (memopt) kernel; 1 otherwise
 };
 
 typedef CUresult (*ModuleLoadDataFn)(CUmodule*, const void*);
@@ -138,12 +138,12 @@ int ps_jit_compile(const char* source, const char* entry, void** kernel) {
 int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                   const int64_t lo[3], const int64_t count[3], void* stream, int sync) {
     const int32_t threads[3] = {32, 8, 1};
-    return ps_jit_launch_ex(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, 0, 1, stream, sync);
+    return ps_jit_launch_ex(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, 0, nullptr, stream, sync);
 }
 
 int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                      const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
-                     int32_t zloop, void* stream, int sync) {
+                     const int32_t loop[3], void* stream, int sync) {
     DeviceState* st = nullptr;
     PS_TRY(current_state(&st));
     if (!kernel || !lo || !count || !threads) return fail(PS_ERR_NULL, "ps_jit_launch: NULL argument");
@@ -152,8 +152,15 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
         return fail(PS_ERR_ARG, "ps_jit_launch: threads per block must be >= 1 and at most 1024 (z <= 64)");
     if (shmem < 0 || shmem > 227 * 1024)
         return fail(PS_ERR_ARG, "ps_jit_launch: shmem must be 0 to 232448 bytes (227 KB)");
-    if (zloop < 1 || (zloop > 1 && threads[2] != 1))
-        return fail(PS_ERR_ARG, "ps_jit_launch: zloop must be >= 1, with threads[2] == 1 when > 1");
+    int32_t lp[3] = {1, 1, 1};
+    int nsweep = 0;
+    for (int d = 0; d < 3 && loop; d++) {
+        lp[d] = loop[d];
+        if (lp[d] < 1 || (lp[d] > 1 && threads[d] != 1))
+            return fail(PS_ERR_ARG, "ps_jit_launch: loop[%d] must be >= 1, with threads[%d] == 1 when > 1", d, d);
+        nsweep += lp[d] > 1;
+    }
+    if (nsweep > 1) return fail(PS_ERR_ARG, "ps_jit_launch: a sweep kernel loops along one dimension only");
     if (narrays < 0 || narrays > kJitMaxArrays || nscalars < 0 || nscalars > kJitMaxScalars ||
         (narrays && !arrays) || (nscalars && !scalars))
         return fail(PS_ERR_ARG, "ps_jit_launch: at most %d arrays and %d scalars", kJitMaxArrays, kJitMaxScalars);
@@ -177,10 +184,11 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
     }
     g.err = k->err;
     g.smem = shmem;
-    g.zloop = zloop;
+    g.loop = lp[0] * lp[1] * lp[2];  // the one loop count > 1, if any
     if (count[0] == 0 || count[1] == 0 || count[2] == 0) return PS_OK;
-    const int64_t gx = (count[0] + threads[0] - 1) / threads[0], gy = (count[1] + threads[1] - 1) / threads[1],
-                  gz = (count[2] + (int64_t)threads[2] * zloop - 1) / ((int64_t)threads[2] * zloop);
+    int64_t gd[3];
+    for (int d = 0; d < 3; d++) gd[d] = (count[d] + (int64_t)threads[d] * lp[d] - 1) / ((int64_t)threads[d] * lp[d]);
+    const int64_t gx = gd[0], gy = gd[1], gz = gd[2];
     if (gx > 2147483647LL || gy > 65535 || gz > 65535) return fail(PS_ERR_SHAPE, "ps_jit_launch: grid too large");
     if (shmem > k->smem_opt_in) {
         if (g_setattr(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)shmem) != CUDA_SUCCESS)

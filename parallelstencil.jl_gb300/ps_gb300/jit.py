@@ -52,11 +52,12 @@ _lib.register("ps_jit_launch", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes
 _lib.register("ps_jit_launch_ex", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                    ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
-                                   ctypes.c_int32, ctypes.c_void_p, ctypes.c_int])
+                                   ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_jit_check", [ctypes.c_void_p, ctypes.c_void_p])
 _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
 MAX_ARRAYS = MAX_SCALARS = 32
+RESIDENT_THREADS = 152 * 2048  # threads a GB300 holds at once (152 SMs x 2048)
 _COLLECTIVE = {"__m_shfl_sync", "__m_shfl_up_sync", "__m_shfl_down_sync", "__m_shfl_xor_sync", "__m_vote_any_sync",
                "__m_vote_all_sync", "__m_vote_ballot_sync"}
 _MATH = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "sinh", "cosh", "atan", "asin", "acos", "log10",
@@ -318,9 +319,11 @@ class _Gen:
         self.kd, self.nd = kd, ndims
         # FP64 arrays with the arithmetic on FP32 pairs (R = jd, storage E = double); see _JD below
         self.split = bool(split)
-        # memopt: each thread sweeps g.zloop consecutive z indices and carries read-only stencil
-        # points it already holds to the next z (src/memopt.jl's register queue, in plain code)
-        self.zloop = bool(zloop) and kd.kind == "parallel" and ndims == 3
+        # memopt: each thread sweeps g.loop consecutive indices of the last dimension (z in 3-D, y in
+        # 2-D) and carries read-only stencil points it already holds to the next index
+        # (src/memopt.jl's register queues for loopdim 3 and 2, in plain code)
+        self.zloop = bool(zloop) and kd.kind == "parallel" and ndims in (2, 3)
+        self.sweep = ndims - 1 if self.zloop else None
         self.persist = []  # registers that live across the z sweep
         self.nstmt = 0
         self.macros = MACROS[ndims]
@@ -391,9 +394,16 @@ class _Gen:
         return decl, " && ".join(cond)
 
     def zloop_statement(self, p, cond, box, decl, store):
-        """An FD statement inside the z sweep: a read-only point whose z+1 neighbour was loaded at the
-        previous z comes from that register (valid while the statement ran at the previous z: its
-        mask and bounds conditions, once false along z, stay false)."""
+        """An FD statement inside the sweep: a read-only point whose neighbour one index further along
+        the sweep was loaded at the previous index comes from that register (read-only values do not
+        change; the register is used only when the statement ran at the previous index)."""
+        sd = self.sweep
+
+        def along(o, s):
+            o = list(o)
+            o[sd] += s
+            return tuple(o)
+
         j = self.nstmt
         self.nstmt += 1
         t3 = ("tx", "ty", "tz")
@@ -405,12 +415,12 @@ class _Gen:
             ref = f"a{k}[({idx[0]}) + n{k}_0 * (({idx[1]}) + n{k}_1 * ({idx[2]}))]"
             ro = name in self.read_only
             ld = self.wrap(f"__ldg(&{ref})" if ro else ref)
-            nxt = (name, (o[0], o[1], o[2] + 1))
+            nxt = (name, along(o, 1))
             if ro and nxt in keys:
                 loads.append(f"{p}    const R {var} = pr{j} ? P{j}_{keys[nxt][1:]} : {ld};")
             else:
                 loads.append(f"{p}    const R {var} = {ld};")
-            if ro and (name, (o[0], o[1], o[2] - 1)) in keys:
+            if ro and (name, along(o, -1)) in keys:
                 self.persist.append(f"    R P{j}_{var[1:]} = 0;")
                 ups.append(f"{p}    P{j}_{var[1:]} = {var};")
         self.persist.append(f"    bool pr{j} = false;")
@@ -893,19 +903,23 @@ class _Gen:
         else:
             guard = "    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) return;"
         zpre, zpost = "", ""
-        if self.zloop:  # blockDim.z == 1; block z covers g.zloop consecutive z indices
-            guard = "    if (ux >= g.cnt[0] || uy >= g.cnt[1]) return;"
-            zpre = "\n" + "\n".join(self.persist) + """
-    for (long long it_ = 0; it_ < g.zloop; ++it_) {
-    const long long uz = blockIdx.z * g.zloop + it_;
-    if (uz >= g.cnt[2]) break;
-    const long long tz = g.lo[2] + uz;"""
+        u, t, c = ("ux", "uy", "uz"), ("tx", "ty", "tz"), "xyz"
+        grid = [d for d in range(3) if d != self.sweep]
+        udecl = ", ".join(f"{u[d]} = blockIdx.{c[d]} * (long long)blockDim.{c[d]} + threadIdx.{c[d]}" for d in grid)
+        if self.zloop:  # blockDim of the sweep dimension is 1; each block covers g.loop consecutive indices
+            sd = self.sweep
+            guard = "    if (" + " || ".join(f"{u[d]} >= g.cnt[{d}]" for d in grid) + ") return;"
+            zpre = "\n" + "\n".join(self.persist) + f"""
+    for (long long it_ = 0; it_ < g.loop; ++it_) {{
+    const long long {u[sd]} = blockIdx.{c[sd]} * g.loop + it_;
+    if ({u[sd]} >= g.cnt[{sd}]) break;
+    const long long {t[sd]} = g.lo[{sd}] + {u[sd]};"""
             zpost = "    }"
-        pos = "const long long tx = g.lo[0] + ux, ty = g.lo[1] + uy" + ("" if self.zloop else ", tz = g.lo[2] + uz")
-        uzdecl = "" if self.zloop else "\n    const long long uz = blockIdx.z * (long long)blockDim.z + threadIdx.z;"
-        return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{', z sweep' if self.zloop else ''}) -- generated by ps_gb300.jit
+        pos = "const long long " + ", ".join(f"{t[d]} = g.lo[{d}] + {u[d]}" for d in grid)
+        sweep = f", {c[self.sweep]} sweep" if self.zloop else ""
+        return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{sweep}) -- generated by ps_gb300.jit
 {self.types(real)}
-struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long zloop; }};
+struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long loop; }};
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ E jl_ld(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
@@ -929,7 +943,7 @@ __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ?
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
 extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
     extern __shared__ __align__(16) unsigned char ps_smem[];
-    const long long ux = blockIdx.x * (long long)blockDim.x + threadIdx.x, uy = blockIdx.y * (long long)blockDim.y + threadIdx.y;{uzdecl}
+    const long long {udecl};
 {guard}
     {pos};
     (void)ps_smem;
@@ -1021,7 +1035,8 @@ def _is_sel_assign(s):
 
 def generate(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False) -> str:
     """CUDA C of kernel `kd` for `ndims`-D arrays of `dtype` ("double" or "float"); zloop: the memopt
-    variant (3-D `@parallel` kernels), each thread sweeping consecutive z indices."""
+    variant (2-D and 3-D `@parallel` kernels), each thread sweeping consecutive indices of the last
+    dimension."""
     return _Gen(kd, ndims, zloop).source(dtype)
 
 
@@ -1071,8 +1086,10 @@ class JitKernel:
         """Launch over `ranges` (default: the largest array extents; with `nblocks`, nblocks .* nthreads
         threads) in blocks of `nthreads` (default (32, 8, 1)) with `shmem` bytes of dynamic shared
         memory (src/ParallelKernel/parallel.jl:303-328). memopt (default: the definition's
-        `memopt=`, else true) runs 3-D `@parallel` kernels as z sweeps of `loopsize` (default 64,
-        as src/parallel.jl:532-543 for compute capability >= 9) indices per thread; same results.
+        `memopt=`, else true) runs 2-D and 3-D `@parallel` kernels as sweeps along the last
+        dimension (src/memopt.jl, loopdim 2 and 3) of `loopsize` indices per thread -- by default
+        64, as src/parallel.jl:532-543 for compute capability >= 9, halved (down to 2) while the
+        launch would have fewer threads than the GPU holds at once -- with the same results.
         fp64="split" evaluates the arithmetic of FP64 kernels on FP32 pairs (each operation within
         ~2^-46 of its operands' magnitude; GB300 issues FP32 at 64x the FP64 rate)."""
         require_initialized()
@@ -1109,17 +1126,26 @@ class JitKernel:
             if min(lo) < 0:
                 raise ArgumentError("ranges must start at index 1 or above")
             cnt = [max(0, hi[d] - lo[d]) for d in range(3)]
-        # the z sweep is the default schedule of 3-D @parallel kernels (bit-identical results, faster:
-        # a one-point-per-thread kernel keeps too few loads in flight); memopt=false keeps one point
-        # per thread, as the definition or the call may ask
+        # the sweep is the default schedule of 2-D and 3-D @parallel kernels (bit-identical results,
+        # faster: a one-point-per-thread kernel keeps too few loads in flight); memopt=false keeps one
+        # point per thread, as the definition or the call may ask
         want = memopt if memopt is not None else self.kd.options.get("memopt", "true") == "true"
-        zl = bool(want) and self.kd.kind == "parallel" and ndims == 3
-        zloop = 1
+        zl = bool(want) and self.kd.kind == "parallel" and ndims in (2, 3)
+        loop = [1, 1, 1]
         if zl:
-            zloop = int(loopsize or int(self.kd.options.get("loopsize", "0") or 0) or 64)  # 64: the reference's cc >= 9 default
-            if zloop < 1:
+            sd = ndims - 1
+            if nthreads is None and ndims == 2:
+                threads = [128, 1, 1]
+            threads[sd] = 1
+            ls = int(loopsize or int(self.kd.options.get("loopsize", "0") or 0))
+            if ls < 0:
                 raise ArgumentError("loopsize must be positive")
-            threads[2] = 1
+            if not ls:
+                ls = 64  # the reference's default for compute capability >= 9
+                cols = cnt[0] * cnt[1] * cnt[2] // max(1, cnt[sd])
+                while ls > 2 and cols * -(-cnt[sd] // ls) < RESIDENT_THREADS:
+                    ls //= 2
+            loop[sd] = ls
         if fp64 not in ("ieee", "split", "split_state", "split_grid"):
             raise ArgumentError("fp64 must be 'ieee' or 'split'")
         sp = fp64 != "ieee" and dt == "double"
@@ -1130,7 +1156,7 @@ class JitKernel:
         A = (PSArray * max(1, len(descs)))(*descs)
         S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
         _lib.call("ps_jit_launch_ex", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
-                  (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), zloop,
+                  (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), (ctypes.c_int32 * 3)(*loop),
                   stream_handle(stream), int(bool(sync)))
 
     @staticmethod

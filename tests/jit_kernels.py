@@ -51,6 +51,12 @@ VELOCITY2D = """@parallel function velocity2d!(Vx, Vy, dVx, dVy, Eta, Emax, h)
     return
 end"""
 
+# 2-D heat diffusion with FiniteDifferences2D macros (the y sweep of memopt 2-D)
+HEAT2D_FD = """@parallel function heat2d_fd!(T2, T, Ci, lam, dt, _dx, _dy)
+    @inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)*_dx*_dx + @d2_yi(T)*_dy*_dy))
+    return
+end"""
+
 # 2-D first-order upwind advection: explicit indices, chained comparisons, Bool * x
 UPWIND2D = """@parallel_indices (i, j) function upwind2d!(Tn, T, u, w, dt, rdx, rdy)
     if (1 < i < size(T, 1) && 1 < j < size(T, 2))

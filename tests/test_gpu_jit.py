@@ -102,10 +102,10 @@ def _pos(rng, shape, dt):
     return (rng.random(shape) + 0.5).astype(dt)
 
 
-def _cases(dt):
+def _cases(dt, nx=21, ny=17):
     rng = np.random.default_rng(7)
     r = lambda *s: rng.standard_normal(s).astype(dt)  # noqa: E731
-    nx, ny, n3 = 21, 17, 12
+    n3 = 12
     return {
         "STRESS2D": ([r(nx, ny), r(nx, ny), r(nx - 1, ny - 1), r(nx, ny), r(nx + 1, ny), r(nx, ny + 1),
                       _pos(rng, (nx, ny), dt), 3.0, 5.0], None),
@@ -114,6 +114,7 @@ def _cases(dt):
         "VELOCITY2D": ([r(nx + 1, ny), r(nx, ny + 1), r(nx - 1, ny - 2), r(nx - 2, ny - 1), _pos(rng, (nx, ny), dt),
                         r(nx - 2, ny - 2), 0.05], None),
         "UPWIND2D": ([r(nx, ny), r(nx, ny), r(nx, ny), r(nx, ny), 0.01, 3.0, 5.0], None),
+        "HEAT2D_FD": ([r(nx, ny), r(nx, ny), _pos(rng, (nx, ny), dt), 0.7, 1e-3, 9.0, 11.0], None),
         "WALLS2D": ([r(nx, ny)], [(1, ny)]),
         "BLEND3D": ([r(n3 - 2, n3 - 2, n3 - 2), r(n3, n3, n3), r(n3, n3, n3), _pos(rng, (n3, n3, n3), dt), 0.3],
                     None),
@@ -215,7 +216,7 @@ def test_jit_c_abi_direct(ps):
 
     src = b"""
 struct ps_jit_args { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err;
-                     long long smem; long long zloop; };
+                     long long smem; long long loop; };
 extern "C" __global__ void twice(const ps_jit_args g) {
     long long i = g.lo[0] + blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (threadIdx.y == 0 && i < g.lo[0] + g.cnt[0]) ((double*)g.a[0])[i] = g.s[0] * ((const double*)g.a[1])[i];
@@ -326,7 +327,7 @@ def test_jit_partial_blocks_with_barriers_are_refused(ps):
     h = k._handle(1, "double")  # the handle the refused call compiled
     arrs = (PSArray * 2)(descriptor(S), descriptor(A))
     rc = _lib.load().ps_jit_launch_ex(h, arrs, 2, (ctypes.c_double * 1)(0.0), 0, (ctypes.c_int64 * 3)(0, 0, 0),
-                                      (ctypes.c_int64 * 3)(100, 1, 1), (ctypes.c_int32 * 3)(64, 1, 1), 0, 1,
+                                      (ctypes.c_int64 * 3)(100, 1, 1), (ctypes.c_int32 * 3)(64, 1, 1), 0, None,
                                       stream_handle(None), 1)
     assert rc == -1 and "multiple of the thread block" in _lib.last_error()
     ps.parallel(k, S, A, ranges=[(1, 64)], nthreads=(64,))  # a full block afterwards runs normally
@@ -373,6 +374,32 @@ def test_jit_memopt_z_sweep_is_bit_identical(ps, name, dt):
     box = [(2, 30), (3, 25), (4, 27)]
     ref_box, got_box = launch(False, ranges=box), launch(True, 5, ranges=box)
     for a, b in zip(got_box, ref_box):
+        assert np.array_equal(a, b), (name, "ranges")
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("name", ["STRESS2D", "MOMENTUM2D", "VELOCITY2D", "COMPACTION", "HEAT2D_FD"])
+def test_jit_memopt_y_sweep_is_bit_identical(ps, name, dt):
+    """2-D `@parallel` kernels with memopt=true (y sweeps of 1, 3, 16 and 64 indices per thread and the
+    default, read-only registers carried along y; src/memopt.jl's loopdim 2) give exactly the plain
+    launch's result, over several blocks in x and y, with explicit nthreads and with ranges."""
+    args, _ = _cases(dt, nx=300, ny=133)[name]
+    k = ps.parallel_kernel(getattr(K, name))
+
+    def launch(memopt, loopsize=0, ranges=None, nthreads=None):
+        dev = [_dev(ps, a) if isinstance(a, np.ndarray) else a for a in args]
+        ps.parallel(k, *dev, memopt=memopt, loopsize=loopsize, ranges=ranges, nthreads=nthreads)
+        return [ps.to_host(d) for d in dev if not isinstance(d, float)]
+
+    ref = launch(False)
+    for ls in (0, 1, 3, 16, 64):
+        for a, b in zip(launch(True, ls), ref):
+            assert np.array_equal(a, b), (name, ls)
+    assert (2, "double" if dt == np.float64 else "float", True, False) in k._handles
+    for a, b in zip(launch(True, 5, nthreads=(64, 4)), ref):  # the sweep dimension's threads become 1
+        assert np.array_equal(a, b), (name, "nthreads")
+    box = [(2, 250), (3, 120)]
+    for a, b in zip(launch(True, 7, ranges=box), launch(False, ranges=box)):
         assert np.array_equal(a, b), (name, "ranges")
 
 

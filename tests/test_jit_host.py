@@ -192,9 +192,9 @@ def test_generated_sources_compile_for_sm103a(jit, tmp_path):
             procs.append((f, subprocess.Popen([_nvcc(), "-arch=sm_103a", "-std=c++17", "--fmad=false", "-c", str(f),
                                                "-o", str(f) + ".o"], stdout=subprocess.PIPE,
                                               stderr=subprocess.STDOUT, text=True)))
-            if real == "double" and ndims == 3 and src.lstrip().startswith("@parallel function"):
-                fz = tmp_path / f"{name}_zloop.cu"  # the memopt (z sweep) variant
-                fz.write_text(jit.generate(jit.parse(src), 3, "double", zloop=True))
+            if real == "double" and ndims in (2, 3) and src.lstrip().startswith("@parallel function"):
+                fz = tmp_path / f"{name}_sweep.cu"  # the memopt variant (sweep along z in 3-D, y in 2-D)
+                fz.write_text(jit.generate(jit.parse(src), ndims, "double", zloop=True))
                 procs.append((fz, subprocess.Popen([_nvcc(), "-arch=sm_103a", "-std=c++17", "--fmad=false", "-c",
                                                     str(fz), "-o", str(fz) + ".o"], stdout=subprocess.PIPE,
                                                    stderr=subprocess.STDOUT, text=True)))
@@ -273,10 +273,23 @@ def test_interpreter_loops_and_block_ids(jr):
     assert np.array_equal(X, exp)
 
 
+def test_translator_y_sweep_of_2d_kernels(jit):
+    """memopt for 2-D `@parallel` kernels sweeps y (loopdim 2): blockIdx.y covers g.loop consecutive y
+    indices and the two T points one row further along y come from the previous row's registers."""
+    src = jit.generate(jit.parse(K.HEAT2D_FD), 2, "double", zloop=True)
+    body = src.split("ps_jit_entry")[1]
+    assert "const long long uy = blockIdx.y * g.loop + it_;" in body
+    assert "threadIdx.y" not in body
+    carried = re.findall(r"const R (L\d+) = pr(\d) \? P\d_\d+ : (.*?);", body)
+    assert len(carried) == 2 and all("a1[" in ld for _, _, ld in carried)  # T (argument 1) only
+    plain = jit.generate(jit.parse(K.HEAT2D_FD), 2, "double")
+    assert "g.loop" not in plain.split("ps_jit_entry")[1]
+
+
 def test_translator_z_sweep_carries_only_read_only_points(jit):
     src = jit.generate(jit.parse(K.TWO3D), 3, "double", zloop=True)
     body = src.split("ps_jit_entry")[1]
-    assert "for (long long it_ = 0; it_ < g.zloop; ++it_)" in body
+    assert "for (long long it_ = 0; it_ < g.loop; ++it_)" in body
     carried = re.findall(r"const R (L\d+) = pr(\d) \? P\d_\d+ : (.*?);", body)
     assert carried and all("a2[" in ld for _, _, ld in carried)  # only B (argument 2) is read-only
     assert "a0[" not in "".join(ld for _, _, ld in carried)  # A is written by the first statement
