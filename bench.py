@@ -702,6 +702,10 @@ def bench_fd_macros(ps, torch, n=512):
                                     "jit_ms": round(tj * 1e3, 4), "jit_T_eff_GBs": round(2 * es * n ** 3 / tj / 1e9, 1),
                                     "jit_memopt_T_eff_GBs": round(2 * es * n ** 3 / tm / 1e9, 1)}
             launches += 3 * 13
+            if dt == np.float64:  # FP64 arrays, arithmetic on FP32 pairs
+                tsp = _events(torch, lambda: ps.parallel(k, R, A, sync=False, fp64="split"), 10)
+                out[f"{stmt} {tag}"]["split_T_eff_GBs"] = round(2 * es * n ** 3 / tsp / 1e9, 1)
+                launches += 13
             del R
         del A
     torch.cuda.empty_cache()
@@ -964,13 +968,14 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": "gemm", "n": n, "steps": a.steps}))
         return
-    if a.only_run == "fd":  # the FD-macro kernel of one statement, FP64, n^3, --steps calls
-        A, R = ps.rand(n, n, n, seed=4), ps.zeros(n, n, n)
+    if a.only_run in ("fd", "fd32"):  # the FD-macro kernel of one statement, FP64 / FP32, n^3, --steps calls
+        dt = np.float32 if a.only_run == "fd32" else np.float64
+        A, R = ps.rand(n, n, n, dtype=dt, seed=4), ps.zeros(n, n, n, dtype=dt)
         k = ps.fd_kernel("@inn(R) = @d2_zi(A)")
         for _ in range(a.steps):
             ps.parallel(k, R, A, sync=False)
         torch.cuda.synchronize()
-        print(json.dumps({"only_run": "fd", "n": n, "steps": a.steps}))
+        print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
         return
     if a.only_run in ("stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint"):  # --steps calls, size --n
         from ps_gb300 import adjoint, stokes, stokes3d
@@ -1064,7 +1069,7 @@ def main():
     ap.add_argument("--loopsize", type=int, default=0, help="z indices per thread of memopt run-time compiled kernels")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
-                                                 "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd"], default=None,
+                                                 "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd", "fd32"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
                          "problem) and exit")

@@ -49,27 +49,28 @@ __host__ __device__ constexpr int fd_dim(int opd, int j) {  // the j-th operated
 }
 __host__ __device__ constexpr int fd_popc(int opd) { return (opd & 1) + ((opd >> 1) & 1) + ((opd >> 2) & 1); }
 
-template <typename T, int KIND, int OPD>
-__device__ __forceinline__ T fd_eval_t(const T* __restrict__ A, int64_t c, const int64_t st[3]) {
+// The macro's value from an accessor at(ox, oy, oz) of A relative to the point (offsets are
+// compile-time constants once the loops unroll).
+template <typename T, int KIND, int OPD, class F>
+__device__ __forceinline__ T fd_eval_f(F at) {
     if constexpr (KIND == PS_FD_SEL) {
-        return __ldg(A + c);
+        return at(0, 0, 0);
     } else if constexpr (KIND == PS_FD_DIFF) {
-        const int64_t o = st[fd_dim(OPD, 0)];
-        return __ldg(A + c + o) - __ldg(A + c);
+        constexpr int k = fd_dim(OPD, 0);
+        return at(k == 0, k == 1, k == 2) - at(0, 0, 0);
     } else if constexpr (KIND == PS_FD_DIFF2) {
-        const int64_t o = st[fd_dim(OPD, 0)];
-        const T m = __ldg(A + c);
-        return (__ldg(A + c + o) - m) - (m - __ldg(A + c - o));
+        constexpr int k = fd_dim(OPD, 0);
+        const T m = at(0, 0, 0);
+        return (at(k == 0, k == 1, k == 2) - m) - (m - at(-(k == 0), -(k == 1), -(k == 2)));
     } else if constexpr (KIND == PS_FD_AV || KIND == PS_FD_HARM) {
         constexpr int ND = fd_popc(OPD), NC = 1 << ND;
         T s = T(0);
 #pragma unroll
         for (int cc = 0; cc < NC; cc++) {  // first operated dimension fastest, as the macros list them
-            int64_t p = c;
+            int o[3] = {0, 0, 0};
 #pragma unroll
-            for (int j = 0; j < ND; j++)
-                if ((cc >> j) & 1) p += st[fd_dim(OPD, j)];
-            T v = __ldg(A + p);
+            for (int j = 0; j < ND; j++) o[fd_dim(OPD, j)] = (cc >> j) & 1;
+            T v = at(o[0], o[1], o[2]);
             if constexpr (KIND == PS_FD_HARM) v = T(1.0) / v;
             s = cc == 0 ? v : s + v;
         }
@@ -78,11 +79,32 @@ __device__ __forceinline__ T fd_eval_t(const T* __restrict__ A, int64_t c, const
     } else {  // maxloc / minloc; OPD = ndims
         constexpr bool MX = KIND == PS_FD_MAXLOC;
         const auto f = [](T a, T b) { return MX ? jl_max(a, b) : jl_min(a, b); };
-        T m = f(f(__ldg(A + c - st[0]), __ldg(A + c + st[0])), __ldg(A + c));
+        T m = f(f(at(-1, 0, 0), at(1, 0, 0)), at(0, 0, 0));
 #pragma unroll
-        for (int k = 1; k < OPD; k++) m = f(m, f(__ldg(A + c - st[k]), __ldg(A + c + st[k])));
+        for (int k = 1; k < OPD; k++) m = f(m, f(at(0, -(k == 1), -(k == 2)), at(0, k == 1, k == 2)));
         return m;
     }
+}
+
+// z offsets the macro reads (3-D): [fd_zlo, fd_zhi]; a window of zhi - zlo + 1 planes when > 1.
+template <int KIND, int OPD>
+__host__ __device__ constexpr int fd_zlo() {
+    return ((KIND == PS_FD_DIFF2 && OPD == 4) || ((KIND == PS_FD_MAXLOC || KIND == PS_FD_MINLOC) && OPD == 3)) ? -1 : 0;
+}
+template <int KIND, int OPD>
+__host__ __device__ constexpr int fd_zhi() {
+    return ((KIND == PS_FD_DIFF || KIND == PS_FD_DIFF2 || KIND == PS_FD_AV || KIND == PS_FD_HARM) && (OPD & 4)) ||
+                   ((KIND == PS_FD_MAXLOC || KIND == PS_FD_MINLOC) && OPD == 3)
+               ? 1 : 0;
+}
+// Whether the macro reads the point (ox, oy) of some plane (offsets -1..1).
+template <int KIND, int OPD>
+__host__ __device__ constexpr bool fd_reads_xy(int ox, int oy) {
+    if (KIND == PS_FD_SEL) return ox == 0 && oy == 0;
+    if (KIND == PS_FD_DIFF || KIND == PS_FD_AV || KIND == PS_FD_HARM)
+        return ox >= 0 && oy >= 0 && (ox == 0 || (OPD & 1)) && (oy == 0 || (OPD & 2));
+    if (KIND == PS_FD_DIFF2) return (ox == 0 || OPD == 1) && (oy == 0 || OPD == 2);
+    return ox == 0 || oy == 0;  // maxloc / minloc: the cross
 }
 
 // Each thread evaluates FD_ZB consecutive z indices, their loads issued together (with one value
@@ -102,27 +124,96 @@ __global__ void fd_apply_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
         T v[FD_ZB];
 #pragma unroll
         for (int u = 0; u < FD_ZB; u++)
-            if (z0 + u < d.tmax[2]) v[u] = fd_eval_t<T, KIND, OPD>(A, bx + st[1] * by + st[2] * (z0 + u + dz), st);
+            if (z0 + u < d.tmax[2]) {
+                const T* p = A + bx + st[1] * by + st[2] * (z0 + u + dz);
+                v[u] = fd_eval_f<T, KIND, OPD>([&](int ox, int oy, int oz) { return __ldg(p + ox + st[1] * oy + st[2] * oz); });
+            }
 #pragma unroll
         for (int u = 0; u < FD_ZB; u++)
             if (z0 + u < d.tmax[2]) R[rx + d.nR[0] * ry + rs * (z0 + u + rz0)] = v[u];
     }
 }
 
+// 3-D macros: each thread sweeps `zl` consecutive z indices, keeping a window of the planes' points
+// in registers, so every plane is loaded once per thread (4 loads per point instead of 8 for @av,
+// 5 instead of 7 for @maxloc); the same values in the same operation order as fd_apply_kernel.
+// Selections and differences (a few loads, little arithmetic) unroll the sweep 4 times to keep
+// more loads in flight; averages and extrema keep the compiler's own unrolling (each measured
+// fastest at 512^3 that way, against forced unrolling by 1, 2 and 4).
+template <typename T, int KIND, int OPD>
+__global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDesc d, int64_t zl) {
+    constexpr int ZLO = fd_zlo<KIND, OPD>(), ZN = fd_zhi<KIND, OPD>() - ZLO + 1;
+    constexpr bool UNR4 = KIND == PS_FD_SEL || KIND == PS_FD_DIFF || KIND == PS_FD_DIFF2;
+    const int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    const int64_t z0 = (int64_t)blockIdx.z * zl;
+    if (tx >= d.tmax[0] || ty >= d.tmax[1] || z0 >= d.tmax[2]) return;
+    const int64_t z1 = min(z0 + zl, d.tmax[2]);
+    const int64_t s1 = d.nA[0], s2 = d.nA[0] * d.nA[1];
+    const int64_t dz = (d.inn >> 2) & 1;
+    const T* p = A + tx + (d.inn & 1) + s1 * (ty + ((d.inn >> 1) & 1));
+    T* r = R + tx + (d.lhs_inn & 1) + d.nR[0] * (ty + ((d.lhs_inn >> 1) & 1));
+    const int64_t rs = d.nR[0] * d.nR[1], rz0 = (d.lhs_inn >> 2) & 1;
+    T W[ZN][9] = {};
+    auto load_plane = [&](T* w, int64_t z) {  // the points of plane z + dz the macro reads
+        const T* q = p + s2 * (z + dz);
+#pragma unroll
+        for (int oy = -1; oy <= 1; oy++)
+#pragma unroll
+            for (int ox = -1; ox <= 1; ox++)
+                if (fd_reads_xy<KIND, OPD>(ox, oy)) w[(oy + 1) * 3 + ox + 1] = __ldg(q + ox + s1 * oy);
+    };
+#pragma unroll
+    for (int k = 1; k < ZN; k++) load_plane(W[k], z0 + ZLO + k - 1);
+#define PS_FD_SWEEP_STEP                                                                                 \
+    {                                                                                                    \
+        _Pragma("unroll") for (int k = 0; k + 1 < ZN; k++)                                               \
+            _Pragma("unroll") for (int q = 0; q < 9; q++) W[k][q] = W[k + 1][q];                         \
+        load_plane(W[ZN - 1], z + ZLO + ZN - 1);                                                         \
+        r[rs * (z + rz0)] =                                                                              \
+            fd_eval_f<T, KIND, OPD>([&](int ox, int oy, int oz) { return W[oz - ZLO][(oy + 1) * 3 + ox + 1]; }); \
+    }
+    if constexpr (UNR4) {
+#pragma unroll 4
+        for (int64_t z = z0; z < z1; z++) PS_FD_SWEEP_STEP
+    } else {
+        for (int64_t z = z0; z < z1; z++) PS_FD_SWEEP_STEP  // the compiler's own unrolling
+    }
+#undef PS_FD_SWEEP_STEP
+}
+
+// Threads a GB300 holds at once (152 SMs x 2048): sweeps are shortened until a launch fills them.
+constexpr int64_t kResidentThreads = 152 * 2048;
+
+template <typename T, int K, int O>
+static void fd_launch_one(const FdDesc& d, T* R, const T* A, cudaStream_t s) {
+    const dim3 blk(32, 8, 1);
+    const unsigned gx = (unsigned)((d.tmax[0] + 31) / 32), gy = (unsigned)((d.tmax[1] + 7) / 8);
+    if (d.ndims == 3) {  // every 3-D macro sweeps z; 1-D and 2-D ones keep fd_apply_kernel
+        int64_t zl = 64;
+        while (zl > 2 && d.tmax[0] * d.tmax[1] * ((d.tmax[2] + zl - 1) / zl) < kResidentThreads) zl /= 2;
+        zl = std::max<int64_t>(zl, (d.tmax[2] + 65534) / 65535);
+        fd_sweep_kernel<T, K, O><<<dim3(gx, gy, (unsigned)((d.tmax[2] + zl - 1) / zl)), blk, 0, s>>>(R, A, d, zl);
+        return;
+    }
+    const unsigned gz = (unsigned)std::min<int64_t>((d.tmax[2] + FD_ZB - 1) / FD_ZB, 65535);
+    fd_apply_kernel<T, K, O><<<dim3(gx, gy, gz), blk, 0, s>>>(R, A, d);
+}
+
 template <typename T>
-static int launch_fd(const FdDesc& d, T* R, const T* A, dim3 grd, dim3 blk, cudaStream_t s) {
+static int launch_fd(const FdDesc& d, T* R, const T* A, cudaStream_t s) {
 #define PS_FD_CASE(K, O) \
-    case O: fd_apply_kernel<T, K, O><<<grd, blk, 0, s>>>(R, A, d); return PS_OK;
+    case O: fd_launch_one<T, K, O>(d, R, A, s); return PS_OK;
 #define PS_FD_ONE_DIM(K) switch (d.opdims) { PS_FD_CASE(K, 1) PS_FD_CASE(K, 2) PS_FD_CASE(K, 4) }
 #define PS_FD_ANY_DIMS(K) \
     switch (d.opdims) { PS_FD_CASE(K, 1) PS_FD_CASE(K, 2) PS_FD_CASE(K, 3) PS_FD_CASE(K, 4) PS_FD_CASE(K, 5) \
                         PS_FD_CASE(K, 6) PS_FD_CASE(K, 7) }
 #define PS_FD_NDIMS(K) \
-    switch (d.ndims) { case 1: fd_apply_kernel<T, K, 1><<<grd, blk, 0, s>>>(R, A, d); return PS_OK; \
-                       case 2: fd_apply_kernel<T, K, 2><<<grd, blk, 0, s>>>(R, A, d); return PS_OK; \
-                       case 3: fd_apply_kernel<T, K, 3><<<grd, blk, 0, s>>>(R, A, d); return PS_OK; }
+    switch (d.ndims) { case 1: fd_launch_one<T, K, 1>(d, R, A, s); return PS_OK; \
+                       case 2: fd_launch_one<T, K, 2>(d, R, A, s); return PS_OK; \
+                       case 3: fd_launch_one<T, K, 3>(d, R, A, s); return PS_OK; }
     switch (d.kind) {
-    case PS_FD_SEL: fd_apply_kernel<T, PS_FD_SEL, 0><<<grd, blk, 0, s>>>(R, A, d); return PS_OK;
+    case PS_FD_SEL: fd_launch_one<T, PS_FD_SEL, 0>(d, R, A, s); return PS_OK;
     case PS_FD_DIFF: PS_FD_ONE_DIM(PS_FD_DIFF) break;
     case PS_FD_DIFF2: PS_FD_ONE_DIM(PS_FD_DIFF2) break;
     case PS_FD_AV: PS_FD_ANY_DIMS(PS_FD_AV) break;
@@ -751,12 +842,10 @@ int ps_fd_apply(ps_fd_op op, int32_t lhs_inn, ps_array R, ps_array A, void* stre
     }
     if (d.tmax[0] <= 0 || d.tmax[1] <= 0 || d.tmax[2] <= 0) return PS_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    dim3 blk(32, 8, 1);
-    dim3 grd = grid3(d.tmax[0], d.tmax[1], (d.tmax[2] + FD_ZB - 1) / FD_ZB, blk);
     if (R.dtype == PS_F64)
-        PS_TRY(launch_fd<double>(d, static_cast<double*>(R.ptr), static_cast<const double*>(A.ptr), grd, blk, s));
+        PS_TRY(launch_fd<double>(d, static_cast<double*>(R.ptr), static_cast<const double*>(A.ptr), s));
     else
-        PS_TRY(launch_fd<float>(d, static_cast<float*>(R.ptr), static_cast<const float*>(A.ptr), grd, blk, s));
+        PS_TRY(launch_fd<float>(d, static_cast<float*>(R.ptr), static_cast<const float*>(A.ptr), s));
     return finish_launch(s, sync, "ps_fd_apply");
 }
 

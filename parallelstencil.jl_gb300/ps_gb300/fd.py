@@ -93,6 +93,18 @@ class FdKernel:
         _lib.call("ps_fd_apply", self.descriptor, self.lhs_inn, descriptor(R), descriptor(A), stream_handle(stream),
                   int(bool(sync)))
 
+    @property
+    def source(self) -> str:
+        """The kernel as a `@parallel` definition."""
+        return f"@parallel function fd!(R, A)\n    @{self.lhs}(R) = @{self.op}(A)\n    return\nend"
+
+    def launch_split(self, R, A, stream=None, sync=True) -> None:
+        """FP64 arrays, arithmetic on FP32 pairs: the definition run-time compiled with fp64="split"
+        (each operation within ~2^-46 of its operands' magnitude)."""
+        from .jit import parallel_kernel
+
+        parallel_kernel(self.source, self.ndims).jit_launch((R, A), None, stream, sync, fp64="split")
+
 
 def fd_kernel(statement: str, ndims: int = 3) -> FdKernel:
     """Parse a one-statement FD kernel body such as ``"@all(R) = @d_xa(A)"``."""

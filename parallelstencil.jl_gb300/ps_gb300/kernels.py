@@ -182,8 +182,13 @@ def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, s
     if isinstance(kernel, FdKernel):
         if ranges is not None or memopt:
             raise ArgumentError("FD operator kernels take no ranges/memopt")
+        if fp64 not in ("ieee", "split"):
+            raise ArgumentError("fp64 must be 'ieee' or 'split' for FD operator kernels")
         R, A = args
-        kernel.launch(R, A, stream=stream, sync=sync)
+        if fp64 == "split" and descriptor(R).dtype == 0:
+            kernel.launch_split(R, A, stream=stream, sync=sync)
+        else:
+            kernel.launch(R, A, stream=stream, sync=sync)
         return
     if not isinstance(kernel, Kernel):
         raise ArgumentError(f"not a GB300 kernel: {kernel!r}")

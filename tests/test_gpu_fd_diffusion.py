@@ -24,6 +24,59 @@ def test_fd_every_macro_known_answers(ps, golden):
         assert np.array_equal(ps.to_host(R), Rexp), (case["key"], case["statement"])
 
 
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_fd_z_sweeps_match_the_oracle(ps, oracle, dtn):
+    """3-D macros run as z sweeps with a register window of the planes they read; on a grid wide
+    enough for 64 z per thread (600 x 600 x 67: one full sweep and a ragged one) every 3-D macro
+    is bit-identical to the oracle, with `@all` and `@inn` left-hand sides."""
+    from ps_gb300.fd import LHS, MACROS
+
+    n = (600, 600, 67)
+    A = np.asfortranarray(np.random.default_rng(11).standard_normal(n).astype(DT[dtn]) + 3.0)
+    dA = _dev(ps, A)
+    done = 0
+    for op, (kind, opd, inn) in sorted(MACROS[3].items()):
+        for lhs in ("all", "inn"):
+            li = LHS[3][lhs]
+            shape = tuple(n[k] - ((inn >> k) & 1) - ((opd >> k) & 1) for k in range(3))
+            exp = np.asfortranarray(np.full(shape, -7.0, dtype=DT[dtn]))
+            oracle.fd_apply(kind, opd, inn, 3, li, exp, A)
+            R = _dev(ps, np.full(shape, -7.0, dtype=DT[dtn]))
+            ps.parallel(ps.fd_kernel(f"@{lhs}(R) = @{op}(A)"), R, dA)
+            assert np.array_equal(ps.to_host(R), exp), (op, lhs)
+            del R
+            done += 1
+    assert done == 2 * len(MACROS[3])
+
+
+def test_fd_split_fp64_close_to_the_oracle(ps, oracle):
+    """fp64="split" for FD operator kernels (FP64 arrays, arithmetic on FP32 pairs, the definition
+    run-time compiled): every 3-D macro within 1e-12 of the IEEE oracle (relative max-norm); FP32
+    arrays keep the hand-written kernel, bit-identical."""
+    from ps_gb300.fd import MACROS
+
+    n = (41, 37, 35)
+    A = np.asfortranarray(np.random.default_rng(12).random(n) + 0.5)
+    dA, dA32 = _dev(ps, A), _dev(ps, A.astype(np.float32))
+    for op, (kind, opd, inn) in sorted(MACROS[3].items()):
+        shape = tuple(n[k] - ((inn >> k) & 1) - ((opd >> k) & 1) for k in range(3))
+        exp = np.asfortranarray(np.full(shape, -7.0))
+        oracle.fd_apply(kind, opd, inn, 3, 0, exp, A)
+        R = _dev(ps, np.full(shape, -7.0))
+        k = ps.fd_kernel(f"@all(R) = @{op}(A)")
+        ps.parallel(k, R, dA, fp64="split")
+        got = ps.to_host(R)
+        err = np.abs(got - exp).max() / np.abs(exp).max()
+        assert err <= 1e-12, (op, err)
+        exp32 = np.asfortranarray(np.full(shape, -7.0, dtype=np.float32))
+        oracle.fd_apply(kind, opd, inn, 3, 0, exp32, np.asfortranarray(A.astype(np.float32)))
+        R32 = _dev(ps, np.full(shape, -7.0, dtype=np.float32))
+        ps.parallel(k, R32, dA32, fp64="split")
+        assert np.array_equal(ps.to_host(R32), exp32), op
+    with pytest.raises(ps.ArgumentError):
+        ps.parallel(ps.fd_kernel("@all(R) = @av(A)"), R, dA, fp64="split_grid")
+
+
 def test_fd_out_of_bounds_is_an_error(ps):
     R = ps.zeros(7, 5, 6)
     A = ps.zeros(7, 5, 6)  # @d_xa needs size(A,1) == size(R,1)+1
