@@ -34,7 +34,7 @@ struct GCfg {
     static constexpr int BBYTES = BN * G_BK * 2;
     static constexpr int STAGE = G_ABYTES + BBYTES;
     static constexpr int SMEM = S * STAGE + 1024 + 256;  // ring (1024-aligned) + barriers, TMEM slot, counters
-    static constexpr uint32_t TMEM = BN;                 // FP32 accumulator: one column per n
+    static constexpr uint32_t TMEM = BN;                 // FP32 accumulator: one column per n (two are allocated)
 };
 
 // tcgen05 instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M x N.
@@ -92,10 +92,39 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void mbar_arrive1(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// One output tile of the persistent schedule. Tiles go in bands of G_GROUP m blocks: within a
+// band, m block fastest, then n block; then the next band; the K split outermost. The CTAs in
+// flight then share a band of A (G_GROUP x 128 rows) and a few B blocks, which stay in L2
+// (m-fastest over the whole of M re-read all of A from DRAM for every n block of a large problem).
+constexpr int G_GROUP = 16;
+struct GTile {
+    int m0, n0, kb0, nkb;
+};
+__device__ __forceinline__ GTile gemm_tile(int t, int tiles_m, int tiles_n, int BN, int KB, int per) {
+    GTile g;
+    const int plane = tiles_m * tiles_n, zi = t / plane, r = t % plane;
+    const int band = r / (G_GROUP * tiles_n), in_band = r % (G_GROUP * tiles_n);
+    const int gm = min(G_GROUP, tiles_m - band * G_GROUP);  // m blocks in this band
+    const int mi = band * G_GROUP + in_band % gm, ni = in_band / gm;
+    g.m0 = mi * G_BM;
+    g.n0 = ni * BN;
+    g.kb0 = zi * per;
+    g.nkb = min(KB, g.kb0 + per) - g.kb0;
+    return g;
+}
+
+// Persistent, warp-specialised: one CTA per SM walks the tiles t = blockIdx.x, +gridDim.x, ...
+// warp 0 (one thread) feeds the shared-memory ring across tile boundaries, warp 1 (one thread)
+// issues the MMAs into one of two TMEM accumulators, and warps 2-5 drain the other accumulator
+// (tcgen05.ld, epilogue, global stores) while the next tile's MMAs run.
 template <int BN>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(192, 1)
     nn_gemm_tc(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, int64_t K,
-               int kb_per_split, GemmEpilogue e, int* __restrict__ err) {
+               int kb_per_split, int tiles_m, int tiles_n, int ntiles, GemmEpilogue e, int* __restrict__ err) {
     using C = GCfg<BN>;
     constexpr int G_S = C::S, G_STAGE = C::STAGE;
     extern __shared__ unsigned char smem_raw[];
@@ -103,14 +132,14 @@ __global__ void __launch_bounds__(128, 1)
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + G_S * G_STAGE);
     uint64_t* empty = full + G_S;
-    uint64_t* done = empty + G_S;
+    uint64_t* tfull = empty + G_S;  // [2] accumulator ready (MMA -> epilogue)
+    uint64_t* tempty = tfull + 2;   // [2] accumulator drained (epilogue warps -> MMA)
+    uint64_t* done = tempty + 2;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-    int* counts = reinterpret_cast<int*>(tmem_slot + 1);  // [0] copies issued, [1] stages consumed
+    int* counts = reinterpret_cast<int*>(tmem_slot + 1);  // [0] stages filled, [1] stages consumed
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * G_BM, n0 = blockIdx.y * BN;
     const int KB = (int)((K + G_BK - 1) / G_BK);
-    const int kb0 = blockIdx.z * kb_per_split;
-    const int nkb = min(KB, kb0 + kb_per_split) - kb0;
+    const int per = kb_per_split;
 
     if (threadIdx.x == 0) {
         prefetch_tensormap(&mA);
@@ -119,89 +148,156 @@ __global__ void __launch_bounds__(128, 1)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 4);  // one arrival per epilogue warp
+        }
         mbar_init(done, 1);
+        counts[0] = counts[1] = 0;
         fence_mbar_init();
     }
-    if (warp == 0) tc_alloc(tmem_slot, C::TMEM);
+    if (warp == 0) tc_alloc(tmem_slot, 2 * C::TMEM);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
     if (threadIdx.x == 0) {  // TMA producer
-        int i = 0;
-        for (; i < nkb; i++) {
-            const int s = i % G_S;
-            // stage s was last read by the MMAs of k-block i - G_S: its empty barrier's (i/G_S - 1)th phase
-            if (i >= G_S && !mbar_wait_bounded(&empty[s], ((i / G_S) - 1) & 1)) break;
-            unsigned char* st = smem + s * G_STAGE;
-            mbar_arrive_expect_tx(&full[s], G_STAGE);
-            tma_load_2d(st, &mA, &full[s], (kb0 + i) * G_BK, m0);
-            tma_load_2d(st + G_ABYTES, &mB, &full[s], (kb0 + i) * G_BK, n0);
-        }
-        counts[0] = i;
-        if (i < nkb) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
-    } else if (threadIdx.x == 32) {  // MMA issuer
-        constexpr uint32_t idesc = umma_idesc_bf16(G_BM, BN);
-        int i = 0;
-        for (; i < nkb; i++) {
-            const int s = i % G_S;
-            if (!mbar_wait_bounded(&full[s], (i / G_S) & 1)) break;
-            tc_fence_after();
-            const uint32_t sa = smem_u32(smem + s * G_STAGE);
-            const uint64_t da = umma_desc_sw128(sa), db = umma_desc_sw128(sa + G_ABYTES);
-#pragma unroll
-            for (int k = 0; k < G_BK / 16; k++)  // K = 16 per MMA: +32 bytes along the swizzled row
-                tc_mma(tmem, da + 2 * k, db + 2 * k, idesc, (i > 0 || k > 0) ? 1u : 0u);
-            tc_commit(&empty[s]);
-        }
-        counts[1] = i;
-        if (i < nkb) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
-        tc_commit(done);  // arrives when every MMA issued above has completed
-    }
-    __syncwarp();
-    const bool have = mbar_wait_bounded(done, 0);
-    tc_fence_after();
-    __syncthreads();  // counts[] visible; every warp converged before the collective tcgen05.ld
-    if (!have) {
-        if (threadIdx.x == 0) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
-    } else if (nkb > 0) {
-        const int row = warp * 32 + lane;
-        const int64_t gm = (int64_t)m0 + row;
-        const bool row_ok = gm < e.M;
-        for (int c = 0; c < BN; c += 16) {
-            float v[16];
-            tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);  // whole warp, no divergence
-            if (!row_ok) continue;
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int64_t gn = (int64_t)n0 + c + j;
-                if (gn >= e.N) break;
-                float x = v[j] * e.alpha;
-                if (e.bias) x += e.bias[gn];
-                if (e.relu) x = fmaxf(x, 0.0f);
-                const int64_t o = gm * e.ldc + gn;
-                if (e.out_bf16)
-                    e.outh[o] = __float2bfloat16_rn(x);
-                else if (e.atomic)
-                    atomicAdd(e.outf + o, x);
-                else
-                    e.outf[o] = x;
+        int it = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            const GTile g = gemm_tile(t, tiles_m, tiles_n, BN, KB, per);
+            for (int i = 0; i < g.nkb; i++, it++) {
+                const int s = it % G_S;
+                // stage s was last read by the MMAs of ring step it - G_S: its empty barrier's (it/G_S - 1)th phase
+                if (it >= G_S && !mbar_wait_bounded(&empty[s], ((it / G_S) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                unsigned char* st = smem + s * G_STAGE;
+                mbar_arrive_expect_tx(&full[s], G_STAGE);
+                tma_load_2d(st, &mA, &full[s], (g.kb0 + i) * G_BK, g.m0);
+                tma_load_2d(st + G_ABYTES, &mB, &full[s], (g.kb0 + i) * G_BK, g.n0);
             }
         }
+        counts[0] = it;
+        if (!ok) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+    } else if (threadIdx.x == 32) {  // MMA issuer
+        constexpr uint32_t idesc = umma_idesc_bf16(G_BM, BN);
+        int it = 0, j = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, j++) {
+            const GTile g = gemm_tile(t, tiles_m, tiles_n, BN, KB, per);
+            const int acc = j & 1, use = j >> 1;
+            // the epilogue must have drained this accumulator's previous tile (its (use-1)th phase)
+            if (use >= 1 && !mbar_wait_bounded(&tempty[acc], (use - 1) & 1)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)(acc * BN);
+            for (int i = 0; i < g.nkb; i++, it++) {
+                const int s = it % G_S;
+                if (!mbar_wait_bounded(&full[s], (it / G_S) & 1)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + s * G_STAGE);
+                const uint64_t da = umma_desc_sw128(sa), db = umma_desc_sw128(sa + G_ABYTES);
+#pragma unroll
+                for (int k = 0; k < G_BK / 16; k++)  // K = 16 per MMA: +32 bytes along the swizzled row
+                    tc_mma(d, da + 2 * k, db + 2 * k, idesc, (i > 0 || k > 0) ? 1u : 0u);
+                tc_commit(&empty[s]);
+            }
+            if (!ok) break;
+            tc_commit(&tfull[acc]);  // arrives when this tile's MMAs have completed
+        }
+        counts[1] = it;
+        if (!ok) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+        tc_commit(done);  // arrives when every MMA issued above has completed
+    } else if (warp >= 2) {  // epilogue: warp w reads TMEM lanes (tile rows) 32 (w % 4) .. + 31
+        const int q = warp & 3, row = q * 32 + lane;
+        int j = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
+            const GTile g = gemm_tile(t, tiles_m, tiles_n, BN, KB, per);
+            const int acc = j & 1, use = j >> 1;
+            // warp-uniform: tcgen05.ld below is a warp-collective instruction
+            if (!__all_sync(0xffffffffu, mbar_wait_bounded(&tfull[acc], use & 1))) {
+                if (lane == 0) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+                break;
+            }
+            tc_fence_after();
+            const int64_t gm = (int64_t)g.m0 + row;
+            const bool row_ok = gm < e.M && g.nkb > 0;
+            const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+            for (int c = 0; c < BN; c += 16) {
+                float v[16];
+                tc_ld16(tl + (uint32_t)c, v);  // whole warp, no divergence
+                if (!row_ok) continue;
+                const int64_t gn0 = (int64_t)g.n0 + c;
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++) {
+                    float x = v[jj] * e.alpha;
+                    if (e.bias && gn0 + jj < e.N) x += e.bias[gn0 + jj];
+                    if (e.relu) x = fmaxf(x, 0.0f);
+                    v[jj] = x;
+                }
+                const int64_t o = gm * e.ldc + gn0;
+                if (gn0 + 16 <= e.N && !e.atomic) {  // 16 columns in range: vector stores where aligned
+                    if (e.out_bf16) {
+                        __nv_bfloat16* p = e.outh + o;
+                        if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+                            uint4 w[2];
+                            __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(w);
+#pragma unroll
+                            for (int jj = 0; jj < 8; jj++) h[jj] = __floats2bfloat162_rn(v[2 * jj], v[2 * jj + 1]);
+                            reinterpret_cast<uint4*>(p)[0] = w[0];
+                            reinterpret_cast<uint4*>(p)[1] = w[1];
+                            continue;
+                        }
+                    } else {
+                        float* p = e.outf + o;
+                        if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+#pragma unroll
+                            for (int jj = 0; jj < 4; jj++)
+                                reinterpret_cast<float4*>(p)[jj] =
+                                    make_float4(v[4 * jj], v[4 * jj + 1], v[4 * jj + 2], v[4 * jj + 3]);
+                            continue;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++) {
+                    if (gn0 + jj >= e.N) break;
+                    if (e.out_bf16)
+                        e.outh[o + jj] = __float2bfloat16_rn(v[jj]);
+                    else if (e.atomic)
+                        atomicAdd(e.outf + o + jj, v[jj]);
+                    else
+                        e.outf[o + jj] = v[jj];
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&tempty[acc]);
+        }
     }
+    __syncwarp();
+    if (!mbar_wait_bounded(done, 0) && threadIdx.x == 0) atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+    tc_fence_after();
+    __syncthreads();  // counts[] visible
     if (threadIdx.x == 0 && counts[1] < counts[0])  // a wait gave up: drain the copies still in flight
         for (int j = counts[1]; j < counts[0]; j++) mbar_wait_bounded(&full[j % G_S], (j / G_S) & 1);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc_dealloc(tmem, C::TMEM);
+    if (warp == 0) tc_dealloc(tmem, 2 * C::TMEM);
 }
 
 template <int BN>
 static int nn_gemm_bn(const void* A, int64_t M, const void* B, int64_t N, int64_t K, const GemmEpilogue& e,
                       int split, cudaStream_t s, int* d_err) {
     using C = GCfg<BN>;
-    if (M > ((int64_t)65535 * 32768) || N > 65535LL * BN) return fail(PS_ERR_SHAPE, "nn_gemm: matrix too large");
     CUtensorMap mA, mB;
     PS_TRY(encode_bf16_rows_sw128(&mA, A, (uint64_t)K, (uint64_t)M, G_BK, G_BM));
     PS_TRY(encode_bf16_rows_sw128(&mB, B, (uint64_t)K, (uint64_t)N, G_BK, BN));
@@ -215,8 +311,14 @@ static int nn_gemm_bn(const void* A, int64_t M, const void* B, int64_t N, int64_
     if (split > 1 && (!e.atomic || e.out_bf16 || e.bias || e.relu))
         return fail(PS_ERR_ARG, "nn_gemm: split-K needs a plain FP32 atomic epilogue");
     const int per = (KB + split - 1) / split;
-    const dim3 grid((unsigned)((M + G_BM - 1) / G_BM), (unsigned)((N + BN - 1) / BN), (unsigned)((KB + per - 1) / per));
-    nn_gemm_tc<BN><<<grid, 128, C::SMEM, s>>>(mA, mB, K, per, e, d_err);
+    const int64_t tiles_m = (M + G_BM - 1) / G_BM, tiles_n = (N + BN - 1) / BN, splits = (KB + per - 1) / per;
+    const int64_t ntiles = tiles_m * tiles_n * splits;
+    if (ntiles > 0x7FFFFFFF - 65536) return fail(PS_ERR_SHAPE, "nn_gemm: matrix too large");
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = (int)std::min<int64_t>(ntiles, std::max(1, sms));  // one CTA per SM (shared memory)
+    nn_gemm_tc<BN><<<grid, 192, C::SMEM, s>>>(mA, mB, K, per, (int)tiles_m, (int)tiles_n, (int)ntiles, e, d_err);
     PS_CUDA_TRY(cudaGetLastError());
     return PS_OK;
 }

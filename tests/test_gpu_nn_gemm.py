@@ -11,8 +11,11 @@ def _ref(A, B):
     return A.float().cpu() @ B.float().cpu().T
 
 
+# the last three have more tiles than a GB300 has SMs: each persistent CTA runs two or three tiles
+# through both TMEM accumulators
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 128, 128), (300, 77, 200), (1000, 3, 32), (128, 256, 512),
-                                   (4096, 64, 288), (77, 130, 8)])
+                                   (4096, 64, 288), (77, 130, 8), (8269, 1300, 200), (40000, 96, 72),
+                                   (2048, 2560, 1000)])
 def test_gemm_fp32_out(ps, M, N, K):
     import torch
 
@@ -33,7 +36,7 @@ def test_gemm_bias_relu_bf16(ps):
 
     from ps_gb300 import nn
 
-    M, N, K = 1500, 96, 576
+    M, N, K = 9000, 520, 576  # 213 tiles of 128 x 256: more than one per SM
     g = torch.Generator(device="cuda").manual_seed(3)
     A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
     B = (0.05 * torch.randn(N, K, device="cuda", generator=g)).to(torch.bfloat16)
@@ -47,13 +50,14 @@ def test_gemm_bias_relu_bf16(ps):
     assert (got == 0).any() and (got > 0).any()
 
 
-@pytest.mark.parametrize("split", [1, 3, 8])
-def test_gemm_split_k_accumulate(ps, split):
+@pytest.mark.parametrize("split,M,N,K", [(1, 64, 288, 8192), (3, 64, 288, 8192), (8, 64, 288, 8192),
+                                         (2, 4096, 1024, 1024)])
+def test_gemm_split_k_accumulate(ps, split, M, N, K):
+    """The weight-gradient shape (few output tiles, long K) and a split over 256 tiles."""
     import torch
 
     from ps_gb300 import nn
 
-    M, N, K = 64, 288, 8192  # the weight-gradient shape: few output tiles, long K
     g = torch.Generator(device="cuda").manual_seed(5)
     A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
     B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
