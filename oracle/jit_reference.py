@@ -312,7 +312,8 @@ def parse(src: str) -> OracleKernel:
         mi = re.match(r"\(([^)]*)\)|(\S+)", head)
         indices = [s.strip() for s in (mi.group(1) if mi.group(1) is not None else mi.group(2)).split(",") if s.strip()]
         head = head[mi.end():]
-    opts = dict(o.split("=", 1) for o in head.split())
+    # key=value options; values may hold blanks inside parentheses (optvars=(A, B))
+    opts = dict(o.split("=", 1) for o in re.findall(r"\w+=(?:\((?:[^()]|\([^()]*\))*\)|\S+)", head))
     depth, j = 0, m.end() - 1
     for j in range(m.end() - 1, len(src)):
         depth += src[j] == "("

@@ -239,6 +239,24 @@ def _array_uses(tree) -> set:
     return used
 
 
+def _split_options(head: str):
+    """`key=value` items separated by blanks outside parentheses (values such as
+    `optvars=(A, B)` or `optranges=(A=(-1:1, 0:0, 0:0),)` contain blanks)."""
+    items, cur, depth = [], "", 0
+    for ch in head:
+        depth += ch in "([{"
+        depth -= ch in ")]}"
+        if ch.isspace() and depth == 0:
+            if cur:
+                items.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    if depth != 0:
+        raise ArgumentError(f"unbalanced parentheses in the kernel definition's options: {head}")
+    return items + ([cur] if cur else [])
+
+
 def parse(src: str) -> KernelDef:
     """Parse a Julia `@parallel` / `@parallel_indices` function definition."""
     m = re.search(r"@parallel(_indices)?\b(.*?)\bfunction\s+([^\s(]+)\s*\(", src, re.S)
@@ -256,7 +274,7 @@ def parse(src: str) -> KernelDef:
         head = head[mi.end():].strip()
         if not 1 <= len(idx) <= 3:
             raise ArgumentError("@parallel_indices needs 1-3 index names")
-    for opt in head.split():
+    for opt in _split_options(head):
         k, eq, v = opt.partition("=")
         if not eq or k not in _OPTIONS:
             raise ArgumentError(f"unsupported keyword argument in the kernel definition: {opt}")

@@ -137,6 +137,12 @@ def test_translator_argument_kinds(jit):
     assert kd.kind == "parallel_indices" and kd.index_names == ["ix", "iy"] and kd.options == {"inbounds": "false"}
     kd = jit.parse(K.D2Z3D)
     assert kd.options == {"memopt": "true", "loopsize": "3"}
+    kd = jit.parse("@parallel memopt=true loopsize=3 optvars=(A, B) optranges=(A=(0:0, 0:0, 0:0), B=(0:0,0:0,0:0)) "
+                   "function f!(A2, A, B)\n    @all(A2) = @all(A) + @all(B)\n    return\nend")
+    assert kd.options == {"memopt": "true", "loopsize": "3", "optvars": "(A, B)",
+                          "optranges": "(A=(0:0, 0:0, 0:0), B=(0:0,0:0,0:0))"}
+    with pytest.raises(jit.ArgumentError):
+        jit.parse("@parallel optvars=(A, B function f!(A)\n    @all(A) = 1.0\n    return\nend")
     kd = jit.parse("@parallel function f!(A::Data.Array, B::Data.Array, c::T) where T <: Integer\n"
                    "    @all(A) = @all(B)^c\n    return\nend")
     assert kd.arrays == ["A", "B"] and kd.scalars == ["c"]
