@@ -39,12 +39,14 @@ _TOKEN = re.compile(r"""
     (?P<mac>@[A-Za-z_][A-Za-z0-9_]*) |
     (?P<uop>÷|∈) |
     (?P<id>(?:[A-Za-z_]|[^\x00-\x7f])(?:[A-Za-z0-9_!]|[^\x00-\x7f])*) |
-    (?P<op>==|!=|<=|>=|&&|\|\||::|[-+*/^<>=!(),;\[\]?:.{}$%])
+    (?P<op>==|!=|<=|>=|&&|\|\||::|\+=|-=|\*=|/=|[-+*/^<>=!(),;\[\]?:.{}$%])
 """, re.X)
 
 
 def _tokens(text):
     text = text.replace("≤", "<=").replace("≥", ">=").replace("≠", "!=")
+    # module-qualified macros (FiniteDifferences2D.@inn) are the macros themselves
+    text = re.sub(r"\b(?:ParallelStencil\.)?(?:FiniteDifferences[123]D\.)?(?=@)", "", text)
     out, depth = [], 0
     for m in _TOKEN.finditer(text):
         kind, val = m.lastgroup, m.group()
@@ -140,6 +142,10 @@ class _P:
             self.expect("end")
             return ("while", cond, body)
         lhs = self.expr()
+        if self.peek()[1] in ("+=", "-=", "*=", "/="):  # a op= b is a = a op b
+            op = self.next()[1][0]
+            self.skip_nl()
+            return ("assign", lhs, ("bin", op, lhs, self.expr()))
         if self.peek()[1] != "=" and lhs[0] == "mcall":
             return ("do", lhs)  # @sync_threads()
         if self.peek()[1] != "=":
@@ -320,13 +326,20 @@ def parse(src: str) -> OracleKernel:
         depth -= src[j] == ")"
         if depth == 0:
             break
-    argnames = [a.split("::")[0].strip() for a in src[m.end():j].split(",") if a.strip()]
+    # arguments: commas outside brackets separate them (A::Data.Array{T,N} is one)
+    argnames = [a.split("::")[0].strip() for a in re.split(r",(?![^{(\[]*[})\]])", src[m.end():j]) if a.strip()]
     rest = src[j + 1:].strip()
     rest = re.sub(r"^where\s*(\{[^}]*\}|[^\n]*)", "", rest).strip()
     assert rest.endswith("end")
-    p = _P(_tokens(rest[:-3]))
+    body_text = rest[:-3]
+    if len(indices) == 1 and re.fullmatch(r"\w+\.\.\.", indices[0]):
+        # (I...): the index tuple; A[I...] indexes A at the thread's own point
+        indices = ["..."]
+        body_text = re.sub(r"\b\w+\.\.\.", " __splat__ ", body_text)
+    p = _P(_tokens(body_text))
     body = p.block(())
-    return OracleKernel(m.group(3), kind, indices, argnames, body, int(opts["ndims"]) if "ndims" in opts else None)
+    nd = opts.get("ndims", "").strip("()")
+    return OracleKernel(m.group(3), kind, indices, argnames, body, int(nd) if nd.isdigit() else None)
 
 
 # ---------------------------------------------------------------- FiniteDifferences macros by name
@@ -607,6 +620,8 @@ class _Thread:
                     "gridDim": b.gdim[d]}[name]
         if op == "index":
             shape = self.array(e[1]).shape + (1, 1)
+            if len(e[2]) == 1 and e[2][0] == ("name", "__splat__"):
+                return self.load(e[1], list(I[:self.array(e[1]).ndim]), depth)
             idx = [int(self.ev(_subst_end(x, shape[d]), I, depth)) for d, x in enumerate(e[2])]
             return self.load(e[1], idx, depth)
         if op == "call":
@@ -617,6 +632,8 @@ class _Thread:
                 return a.shape[d - 1] if d <= a.ndim else 1
             if f == "eltype":
                 return R
+            if f == "sizeof":  # sizeof(eltype(A))
+                return 8 if R is float else 4
             if f in ("max", "min"):
                 vals = [E(x) for x in args]
                 if all(isinstance(v, int) and not isinstance(v, bool) for v in vals):
@@ -687,7 +704,10 @@ class _Thread:
             elif lhs[0] == "index":
                 a = self.array(lhs[1])
                 shape = a.shape + (1, 1)
-                idx = [int(self.ev(_subst_end(x, shape[d]), I)) for d, x in enumerate(lhs[2])]
+                if len(lhs[2]) == 1 and lhs[2][0] == ("name", "__splat__"):
+                    idx = list(I[:a.ndim])
+                else:
+                    idx = [int(self.ev(_subst_end(x, shape[d]), I)) for d, x in enumerate(lhs[2])]
                 v = self.real(self.ev(rhs, I))
                 for d in range(a.ndim):
                     if not 1 <= idx[d] <= a.shape[d]:

@@ -32,6 +32,7 @@ source and number type.
 from __future__ import annotations
 
 import ast
+import copy
 import ctypes
 import io
 import numbers
@@ -78,6 +79,9 @@ def _sanitize(text: str) -> str:
     for c in text:
         out.append(c if c.isascii() else f"_u{ord(c):04x}_")
     text = "".join(out)
+    text = re.sub(r"\b(\w+)\.\.\.", r"__splat_\1", text)  # A[I...]
+    # module-qualified macros (FiniteDifferences2D.@inn) are the macros themselves
+    text = re.sub(r"\b(?:ParallelStencil\.)?(?:FiniteDifferences[123]D\.)?(?=@)", "", text)
     text = re.sub(r"@(\w+)\s*\(", r"__m_\1(", text)
     text = text.replace("^", "**").replace("&&", " and ").replace("||", " or ")
     text = re.sub(r"!(?!=)", " not ", text)
@@ -214,12 +218,16 @@ class KernelDef:
     source: str = ""
     int_scalars: set = field(default_factory=set)  # scalars declared `::Integer` / `::Int*`
     options: dict = field(default_factory=dict)    # keyword options before `function`
+    splat: str = ""            # `@parallel_indices (I...)`: the index tuple's name (indices of any rank)
 
 
 # keyword options of `@parallel` / `@parallel_indices` definitions (src/parallel.jl:151-175,
 # src/ParallelKernel/parallel.jl:160-172); the memopt family changes how the reference schedules the
 # kernel, not its results, and is accepted without effect here
-_OPTIONS = {"ndims", "N", "inbounds", "padding", "memopt", "loopsize", "loopdim", "optvars", "optranges"}
+# optvars / optranges / optimize_halo_read tune src/memopt.jl's caching; the sweep here carries every
+# read-only point and reads halos directly, so they are accepted and change nothing
+_OPTIONS = {"ndims", "N", "inbounds", "padding", "memopt", "loopsize", "loopdim", "optvars", "optranges",
+            "optimize_halo_read"}
 
 
 def _array_uses(tree) -> set:
@@ -237,6 +245,32 @@ def _array_uses(tree) -> set:
             else:
                 used.add(n.value.id)
     return used
+
+
+class _AugAssign(ast.NodeTransformer):
+    """`a op= b` is `a = a op b` (Julia lowers it so)."""
+
+    def visit_AugAssign(self, n):
+        load = copy.deepcopy(n.target)
+        for x in ast.walk(load):
+            if hasattr(x, "ctx"):
+                x.ctx = ast.Load()
+        load.ctx = ast.Load()
+        return ast.copy_location(ast.Assign(targets=[n.target], value=ast.BinOp(left=load, op=n.op, right=n.value)), n)
+
+
+def _split_commas(text: str):
+    """Items separated by commas outside brackets (`A::Data.Array{T,N}, B` is two arguments)."""
+    items, cur, depth = [], "", 0
+    for ch in text:
+        depth += ch in "([{"
+        depth -= ch in ")]}"
+        if ch == "," and depth == 0:
+            items.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    return items + [cur]
 
 
 def _split_options(head: str):
@@ -263,17 +297,21 @@ def parse(src: str) -> KernelDef:
     if not m:
         raise ArgumentError("expected `@parallel function name!(args...)` or `@parallel_indices (ix,...) function ...`")
     kind = "parallel_indices" if m.group(1) else "parallel"
-    head, idx, options = m.group(2).strip(), [], {}
+    head, idx, options, splat = m.group(2).strip(), [], {}, ""
     if kind == "parallel_indices":
         mi = re.match(r"\(([^)]*)\)|([^\s=]+)(?=\s|$)", head)
         if not mi:
             raise ArgumentError("@parallel_indices: argument 'indices' must be a tuple of indices or a single index "
                                 "(e.g. (ix, iy, iz) or (ix, iy) or ix ).")
-        idx = [_ident(s.strip()) for s in (mi.group(1) if mi.group(1) is not None else mi.group(2)).split(",")
-               if s.strip()]
+        names = [s.strip() for s in (mi.group(1) if mi.group(1) is not None else mi.group(2)).split(",") if s.strip()]
         head = head[mi.end():].strip()
-        if not 1 <= len(idx) <= 3:
-            raise ArgumentError("@parallel_indices needs 1-3 index names")
+        ms = re.fullmatch(r"(\w+)\.\.\.", names[0]) if len(names) == 1 else None
+        if ms:  # (I...): as many indices as the arrays have dimensions, used as A[I...]
+            splat = _ident(ms.group(1))
+        else:
+            idx = [_ident(s) for s in names]
+            if not 1 <= len(idx) <= 3:
+                raise ArgumentError("@parallel_indices needs 1-3 index names")
     for opt in _split_options(head):
         k, eq, v = opt.partition("=")
         if not eq or k not in _OPTIONS:
@@ -281,9 +319,10 @@ def parse(src: str) -> KernelDef:
         options[k] = v
     if options.get("padding", "false") != "false":
         raise ArgumentError("padding=true is not supported by run-time compiled kernels")
-    if "ndims" in options:
-        if not options["ndims"].isdigit() or not 1 <= int(options["ndims"]) <= 3:
-            raise ArgumentError("ndims must be 1, 2 or 3")
+    if "ndims" in options:  # one rank, or a tuple of ranks the definition serves (ndims=(2,3))
+        nds = options["ndims"].strip("()").split(",")
+        if not all(x.strip().isdigit() and 1 <= int(x) <= 3 for x in nds if x.strip()):
+            raise ArgumentError("ndims must be 1, 2 or 3 (or a tuple of them)")
     if options.get("inbounds", "false") not in ("true", "false"):
         raise ArgumentError("inbounds must be true or false")
     # argument list: balanced parentheses after the name
@@ -300,12 +339,12 @@ def parse(src: str) -> KernelDef:
         raise ArgumentError("kernel definition must end with `end`")
     body = _to_python(_sanitize(rest[:-3]))
     try:
-        tree = ast.parse(body)
+        tree = ast.fix_missing_locations(_AugAssign().visit(ast.parse(body)))
     except SyntaxError as e:
         raise ArgumentError(f"cannot parse the kernel body: {e}") from None
     used = _array_uses(tree)
     args, arrays, scalars, ints = [], [], [], set()
-    for a in [s.strip() for s in arglist.split(",") if s.strip()]:
+    for a in [s.strip() for s in _split_commas(arglist) if s.strip()]:
         nm, _, ty = a.partition("::")
         nm, ty = _ident(nm.strip()), ty.strip()
         # number and array types decide; untyped arguments and type parameters follow their use in the body
@@ -324,7 +363,7 @@ def parse(src: str) -> KernelDef:
     for n in used - set(arrays):
         if n in scalars:
             raise ArgumentError(f"scalar argument {n} is used as an array")
-    return KernelDef(m.group(3), kind, idx, arrays, scalars, args, tree.body, src, ints, options)
+    return KernelDef(m.group(3), kind, idx, arrays, scalars, args, tree.body, src, ints, options, splat)
 
 
 # ---- code generation -----------------------------------------------------------------------
@@ -519,7 +558,8 @@ class _Gen:
             return "int"
         if isinstance(e, ast.Call) and isinstance(e.func, ast.Name):
             f = e.func.id
-            if f in ("size", "__m_warpsize", "__m_laneid", "__m_active_mask", "__m_vote_ballot_sync", "length"):
+            if f in ("size", "__m_warpsize", "__m_laneid", "__m_active_mask", "__m_vote_ballot_sync", "length",
+                     "sizeof"):
                 return "int"
             if f in ("__m_vote_any_sync", "__m_vote_all_sync"):
                 return "bool"
@@ -626,6 +666,8 @@ class _Gen:
                 if a.id in self.shared:
                     return f"sm{self.shared[a.id]}_n{int(d.value) - 1}"
                 return f"n{self.aidx[a.id]}_{int(d.value) - 1}"
+            if f == "sizeof":  # sizeof(eltype(A)): bytes per element of the kernel's number type
+                return "((long long)sizeof(E))"
             if f == "length" and e.args[0].id in self.aidx:
                 k = self.aidx[e.args[0].id]
                 return f"(n{k}_0 * n{k}_1 * n{k}_2)"
@@ -688,6 +730,10 @@ class _Gen:
         if not isinstance(e.value, ast.Name) or (e.value.id not in self.aidx and e.value.id not in self.shared):
             raise ArgumentError("indexing applies to array arguments and @sharedMem arrays")
         sl = e.slice.elts if isinstance(e.slice, ast.Tuple) else [e.slice]
+        if len(sl) == 1 and isinstance(sl[0], ast.Name) and sl[0].id.startswith("__splat_"):
+            if not self.kd.splat or sl[0].id != "__splat_" + self.kd.splat:
+                raise ArgumentError(f"{sl[0].id[8:]}... is not the kernel's index tuple")
+            return e.value.id, ["tx", "ty", "tz"][:self.nd]  # A[I...]: the thread's own point
         if len(sl) > 3:
             raise ArgumentError("at most 3 indices")
 

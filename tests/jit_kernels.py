@@ -57,6 +57,38 @@ HEAT2D_FD = """@parallel function heat2d_fd!(T2, T, Ci, lam, dt, _dx, _dy)
     return
 end"""
 
+# compound assignments on array elements (Julia lowers `a op= b` to `a = a op b`)
+AUGASSIGN = """@parallel_indices (ix) function augassign!(A, B, a)
+    A[ix] += a * B[ix] * 100.65
+    A[ix] -= 1.5
+    A[ix] *= 2
+    A[ix] /= 3
+    return
+end"""
+
+# module-qualified FD macros and the memopt options of a 2-D y sweep
+QUALIFIED2D = """@parallel ndims=2 memopt=true optvars=B loopdim=2 loopsize=3 function qualified2d!(A2, B)
+    FiniteDifferences2D.@inn(A2) = FiniteDifferences2D.@d2_yi(B)
+    return
+end"""
+
+# an index tuple of any rank: (I...) with A[I...], for 2-D and 3-D arrays (ndims=(2,3))
+SPLAT_COPY = """@parallel_indices (I...) ndims=(2,3) N=ndims function splat_copy!(B::Data.Array{T,N}, A::Data.Array{T,N}, c::T) where {T}
+    B[I...] = c * A[I...]
+    return
+end"""
+
+# a @sharedMem view at a byte offset given with sizeof(eltype(A))
+SMEM_OFFSET = """@parallel_indices (ix,iy) function smem_offset!(B, A)
+    tx  = @threadIdx().x
+    ty  = @threadIdx().y
+    A_l = @sharedMem(eltype(A), (@blockDim().x, @blockDim().y), 2*@blockDim().x*sizeof(eltype(A)))
+    A_l[tx,ty] = A[ix,iy]
+    @sync_threads()
+    B[ix,iy] = A_l[@blockDim().x+1-tx,ty]
+    return
+end"""
+
 # 2-D first-order upwind advection: explicit indices, chained comparisons, Bool * x
 UPWIND2D = """@parallel_indices (i, j) function upwind2d!(Tn, T, u, w, dt, rdx, rdy)
     if (1 < i < size(T, 1) && 1 < j < size(T, 2))

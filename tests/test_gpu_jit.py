@@ -114,6 +114,9 @@ def _cases(dt, nx=21, ny=17):
         "VELOCITY2D": ([r(nx + 1, ny), r(nx, ny + 1), r(nx - 1, ny - 2), r(nx - 2, ny - 1), _pos(rng, (nx, ny), dt),
                         r(nx - 2, ny - 2), 0.05], None),
         "UPWIND2D": ([r(nx, ny), r(nx, ny), r(nx, ny), r(nx, ny), 0.01, 3.0, 5.0], None),
+        "AUGASSIGN": ([r(40), r(40), 0.3], None),
+        "QUALIFIED2D": ([r(nx, ny), r(nx, ny)], None),
+        "SPLAT_COPY": ([r(nx, ny), r(nx, ny), 1.5], None),
         "HEAT2D_FD": ([r(nx, ny), r(nx, ny), _pos(rng, (nx, ny), dt), 0.7, 1e-3, 9.0, 11.0], None),
         "WALLS2D": ([r(nx, ny)], [(1, ny)]),
         "BLEND3D": ([r(n3 - 2, n3 - 2, n3 - 2), r(n3, n3, n3), r(n3, n3, n3), _pos(rng, (n3, n3, n3), dt), 0.3],
@@ -128,7 +131,7 @@ def _cases(dt, nx=21, ny=17):
     }
 
 
-_NDIMS = {"ROD1D": 1, "EARLY_RETURN": 1}
+_NDIMS = {"ROD1D": 1, "EARLY_RETURN": 1, "AUGASSIGN": 1}
 _TOL = {"COMPACTION", "BRANCHES2D"}  # exp / pow
 
 
@@ -274,6 +277,29 @@ def test_jit_shared_memory_larger_than_48k(ps):
                 shmem=100 * 1024)
     ps.parallel(ps.parallel_kernel(K.HEAT2D_PLAIN), B, _dev(ps, T), _dev(ps, Ci), *sc)
     assert np.array_equal(ps.to_host(A), ps.to_host(B))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
+def test_jit_shared_memory_offset_and_splat_3d(ps, jr, dt):
+    """A @sharedMem view at a byte offset (2 blockDim.x elements, sizeof(eltype(A))) reversing
+    each block's rows in x, and the (I...) kernel on 3-D arrays; both against the interpreter."""
+    rng = np.random.default_rng(8)
+    A = rng.random((64, 16)).astype(dt)
+    nt = (16, 4)
+    shmem = (16 * 4 + 2 * 16) * np.dtype(dt).itemsize
+    host = np.zeros((64, 16), dt)
+    jr.run(K.SMEM_OFFSET, [host, A], nthreads=nt, shmem=shmem)
+    exp = A.reshape(4, 16, 16)[:, ::-1, :].reshape(64, 16)  # x reversed within each 16-wide block
+    assert np.array_equal(host, exp)
+    B = ps.zeros(64, 16, dtype=dt)
+    ps.parallel(ps.parallel_kernel(K.SMEM_OFFSET), B, _dev(ps, A), nthreads=nt, shmem=shmem)
+    assert np.array_equal(ps.to_host(B), exp)
+    X = rng.random((9, 7, 5)).astype(dt)
+    Y = ps.zeros(9, 7, 5, dtype=dt)
+    ps.parallel(ps.parallel_kernel(K.SPLAT_COPY), Y, _dev(ps, X), 1.5)
+    hy = np.zeros((9, 7, 5), dt)
+    jr.run(K.SPLAT_COPY, [hy, X, 1.5])
+    assert np.array_equal(ps.to_host(Y), hy) and np.array_equal(hy, (dt(1.5) * X).astype(dt))
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
