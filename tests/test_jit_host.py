@@ -228,6 +228,28 @@ def test_reference_miniapp_kernels_translate(jit):
     assert n >= 40
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "examples")), reason="reference sources absent")
+def test_reference_example_kernels_translate(jit):
+    """Every top-level @parallel / @parallel_indices definition of the reference's examples and test
+    projects translates, except those over CellArrays and NamedTuples of arrays (not built)."""
+    n = 0
+    roots = [os.path.join(REFERENCE, "examples"), os.path.join(REFERENCE, "test", "test_projects")]
+    for root in roots:
+        for dirpath, _, files in os.walk(root):
+            for fn in sorted(files):
+                if not fn.endswith(".jl") or "CellArray" in fn or "NamedArrayTuple" in fn:
+                    continue
+                with open(os.path.join(dirpath, fn), encoding="utf-8") as fh:
+                    text = fh.read()
+                ndims = 2 if "2D" in fn else 1 if "1D" in fn else 3
+                for d in re.findall(r"^(@parallel(?:_indices)?[^\n]*function.*?^end)", text, re.S | re.M):
+                    kd = jit.parse(d)
+                    for nd in ((2, 3) if kd.splat else (ndims,)):
+                        assert "ps_jit_entry" in jit.generate(kd, nd, "double"), (fn, d[:60])
+                    n += 1
+    assert n >= 15
+
+
 # ---------------------------------------------------------------- kernel language in the interpreter
 def test_interpreter_shared_memory_tile_equals_plain(jr):
     rng = np.random.default_rng(4)
