@@ -754,11 +754,16 @@ def bench_hide_communication(ps, torch, n=512, bw=(16, 2, 2)):
     k = ps.kernels.diffusion3D_step_inv
     t1 = _events(torch, lambda: ps.parallel(k, *args, memopt=True, sync=False), 5)
     t2 = _events(torch, lambda: ps.hide_communication(bw, k, args, comm=lambda: None, memopt=True), 5)
+    # the same with the arithmetic on FP32 pairs (fp64="split"), one launch and split
+    t3 = _events(torch, lambda: ps.parallel(k, *args, memopt=True, sync=False, fp64="split"), 5)
+    t4 = _events(torch, lambda: ps.hide_communication(bw, k, args, comm=lambda: None, memopt=True, fp64="split"), 5)
     del T, T2, Ci
     b = 3 * 8 * n ** 3
     return {"boundary_width": list(bw), "one_launch_ms": round(t1 * 1e3, 4), "split_ms": round(t2 * 1e3, 4),
             "one_launch_T_eff_GBs": round(b / t1 / 1e9, 1), "split_T_eff_GBs": round(b / t2 / 1e9, 1),
-            "launches": 8 * 8}
+            "fp64_split_one_launch_ms": round(t3 * 1e3, 4), "fp64_split_split_ms": round(t4 * 1e3, 4),
+            "fp64_split_one_launch_T_eff_GBs": round(b / t3 / 1e9, 1),
+            "fp64_split_split_T_eff_GBs": round(b / t4 / 1e9, 1), "launches": 8 * 16}
 
 
 def bench_stokes3d_solve(ps, n=127, tol=1e-6):

@@ -707,7 +707,12 @@ static int launch_diffusion(const ps_array& T2, const ps_array& Tin, const ps_ar
     if (wx <= 0 || wy <= 0 || wz <= 0) return PS_OK;
     const T* lp = lam ? static_cast<const T*>(lam->ptr) : nullptr;
     int L = loopsize > 0 ? loopsize : kDefaultLoopsize;
-    if (memopt) {
+    // A box under half a z-sweep tile wide (x) or high (y) -- e.g. 16-cell boundary slabs of
+    // @hide_communication -- would leave most of each tile's threads idle; those run one point per
+    // thread instead, in blocks no wider than the box (same results: every kernel here is
+    // bit-identical).
+    constexpr int64_t kSweepTileX = 32 * (16 / (int64_t)sizeof(T));
+    if (memopt && 2 * wx >= kSweepTileX && wy >= 4) {
         bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
         if (tma) return launch_zsweep_tma<T, FORM, 8, 4>(T2, Tin, Ci, lam, p, cb, loopsize, s, d_err);
         dim3 blk(32, 4, 1);
@@ -717,7 +722,9 @@ static int launch_diffusion(const ps_array& T2, const ps_array& Tin, const ps_ar
                                                             T2.n[2], cb, L);
         return PS_OK;
     }
-    dim3 blk(32, 8, 1);
+    unsigned bxw = 32;  // full warps for boxes narrower than 32 in x: a warp spans several y rows
+    while (bxw > 1 && bxw / 2 >= wx) bxw /= 2;
+    dim3 blk(bxw, 256 / bxw, 1);
     diff3d_plain<T, FORM><<<grid3(wx, wy, wz, blk), blk, 0, s>>>(static_cast<T*>(T2.ptr),
                                                                  static_cast<const T*>(Tin.ptr),
                                                                  static_cast<const T*>(Ci.ptr), lp, p, T2.n[0],
@@ -929,17 +936,34 @@ int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci
     }
     if (!any_gt1) return fail(PS_ERR_SHAPE, "@hide_communication: all ranges have length 1");
     cudaStream_t sb = static_cast<cudaStream_t>(s_boundary), si = static_cast<cudaStream_t>(s_inner);
+    // Boundary widths below (lw) and above (hw) the inner box. With the z-sweep kernels the x and y
+    // slabs are widened to whole sweep tiles (x: 64 FP64 / 128 FP32 cells from an even cell, y: 8
+    // rows): a slab narrower than a tile costs the whole tile anyway, and an inner box that starts
+    // mid-tile costs one more tile column. The boundary boxes then hold a superset of the requested
+    // boundary cells (all computed before `comm`), the inner box the rest; each cell is computed once.
+    int64_t lw[3] = {bw[0], bw[1], bw[2]}, hw[3] = {bw[0], bw[1], bw[2]};
+    if (memopt) {
+        const int64_t W = (T2.dtype == PS_F64 || fp64_mode != PS_FP64_IEEE) ? 64 : 128;
+        const int64_t a = ((bw[0] + W) / W) * W - 1;           // cells [1, a + 1): ends at a tile edge
+        const int64_t b = ms[0] + 1 - ((ms[0] + 1 - bw[0]) / W) * W;  // first cell on a tile edge
+        if (bw[0] > 0 && a >= bw[0] && b >= bw[0] && ms[0] > a + b) {
+            lw[0] = a;
+            hw[0] = b;
+        }
+        const int64_t y = ((bw[1] + 7) / 8) * 8;
+        if (bw[1] > 0 && ms[1] > 2 * y) lw[1] = hw[1] = y;
+    }
     // get_ranges_outer / get_ranges_inner (src/ParallelKernel/hide_communication.jl:350-394), 3-D case,
     // converted to 0-based half-open boxes.
     Box outer[6] = {
-        {{0, bw[1], bw[2]}, {bw[0], ms[1] - bw[1], ms[2] - bw[2]}},
-        {{0, 0, 0}, {ms[0], ms[1], bw[2]}},
-        {{0, 0, ms[2] - bw[2]}, {ms[0], ms[1], ms[2]}},
-        {{ms[0] - bw[0], bw[1], bw[2]}, {ms[0], ms[1] - bw[1], ms[2] - bw[2]}},
-        {{0, 0, bw[2]}, {ms[0], bw[1], ms[2] - bw[2]}},
-        {{0, ms[1] - bw[1], bw[2]}, {ms[0], ms[1], ms[2] - bw[2]}},
+        {{0, lw[1], lw[2]}, {lw[0], ms[1] - hw[1], ms[2] - hw[2]}},
+        {{0, 0, 0}, {ms[0], ms[1], lw[2]}},
+        {{0, 0, ms[2] - hw[2]}, {ms[0], ms[1], ms[2]}},
+        {{ms[0] - hw[0], lw[1], lw[2]}, {ms[0], ms[1] - hw[1], ms[2] - hw[2]}},
+        {{0, 0, lw[2]}, {ms[0], lw[1], ms[2] - hw[2]}},
+        {{0, ms[1] - hw[1], lw[2]}, {ms[0], ms[1], ms[2] - hw[2]}},
     };
-    Box inner = {{bw[0], bw[1], bw[2]}, {ms[0] - bw[0], ms[1] - bw[1], ms[2] - bw[2]}};
+    Box inner = {{lw[0], lw[1], lw[2]}, {ms[0] - hw[0], ms[1] - hw[1], ms[2] - hw[2]}};
     for (int i = 0; i < 6; i++) {
         bool empty = false;
         for (int d = 0; d < 3; d++) empty |= outer[i].hi[d] <= outer[i].lo[d];

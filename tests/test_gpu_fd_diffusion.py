@@ -157,12 +157,13 @@ def test_diffusion_explicit_ranges(ps, oracle, memopt):
     assert np.array_equal(ps.to_host(T2), ref)
 
 
+@pytest.mark.parametrize("n", [(128, 64, 48), (200, 40, 24)])
 @pytest.mark.parametrize("memopt", [False, True])
 @pytest.mark.parametrize("form", [1, 3])
-def test_hide_communication_split_equals_full(ps, oracle, memopt, form):
+def test_hide_communication_split_equals_full(ps, oracle, memopt, form, n):
     """src/ParallelKernel/test_hide_communication.jl: split computation == serial computation;
-    the communication callback runs once, after the boundary slabs."""
-    n = (128, 64, 48)
+    the communication callback runs once, after the boundary slabs. At 200 cells in x the x slabs
+    are widened to whole 64-cell sweep tiles (63 + 73 threads), at 128 they are not."""
     rng = np.random.default_rng(21)
     T = np.asfortranarray(rng.random(n))
     Ci = np.asfortranarray(rng.random(n))
@@ -176,6 +177,21 @@ def test_hide_communication_split_equals_full(ps, oracle, memopt, form):
                                           5.0, 5.0, 5.0), comm=lambda: calls.append(1), memopt=memopt)
     assert calls == [1]
     assert np.array_equal(ps.to_host(T2), ref)
+
+
+@pytest.mark.parametrize("form", [1, 3])
+def test_hide_communication_split_fp64_equals_one_launch(ps, form):
+    """fp64="split": the boundary slabs and the inner box give the one launch's values bit for bit
+    (each cell's arithmetic does not depend on the box it is computed in)."""
+    n = (200, 40, 24)
+    rng = np.random.default_rng(22)
+    T, Ci, lam = rng.random(n), rng.random(n), 1 + 0.5 * rng.random(n)
+    k = ps.kernels.diffusion3D_step_inv if form == 1 else ps.kernels.diffusion3D_step_flux_lam
+    args = lambda T2: (T2, _dev(ps, T), _dev(ps, Ci), _dev(ps, lam) if form == 3 else 1.0, 1e-4, 5.0, 5.0, 5.0)  # noqa: E731
+    A, B = ps.zeros(*n), ps.zeros(*n)
+    ps.parallel(k, *args(A), memopt=True, fp64="split")
+    ps.hide_communication((16, 2, 2), k, args(B), comm=lambda: None, memopt=True, fp64="split")
+    assert np.array_equal(ps.to_host(A), ps.to_host(B))
 
 
 def test_hide_communication_invalid_width(ps):
