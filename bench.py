@@ -42,6 +42,11 @@ JIT_FLUX_LAM = """@parallel {opt}function diffusion3D_step!(T2, T, Ci, lam, dt, 
     @inn(T2)   = @inn(T) + dt*@all(dTdt)
     return
 end"""
+# the @hide_communication example's step (examples/diffusion3D_multigpucpu_hidecomm_novis.jl:12-15)
+JIT_DIFF_INV = """@parallel function diffusion3D_step!(T2, T, Ci, lam, dt, _dx, _dy, _dz)
+    @inn(T2) = @inn(T) + dt*(lam*@inn(Ci)*(@d2_xi(T)*_dx^2 + @d2_yi(T)*_dy^2 + @d2_zi(T)*_dz^2))
+    return
+end"""
 WORDS_README = 3  # T read, T2 write, Ci read
 WORDS_MEMCOPY = 3
 NT_JOB = 50  # time steps of one diffusion job (the e2e unit)
@@ -757,13 +762,19 @@ def bench_hide_communication(ps, torch, n=512, bw=(16, 2, 2)):
     # the same with the arithmetic on FP32 pairs (fp64="split"), one launch and split
     t3 = _events(torch, lambda: ps.parallel(k, *args, memopt=True, sync=False, fp64="split"), 5)
     t4 = _events(torch, lambda: ps.hide_communication(bw, k, args, comm=lambda: None, memopt=True, fp64="split"), 5)
+    # the same step as a run-time compiled kernel (split FP64 arithmetic), one launch and split
+    j = ps.parallel_kernel(JIT_DIFF_INV)
+    t5 = _events(torch, lambda: ps.parallel(j, *args, sync=False, fp64="split"), 5)
+    t6 = _events(torch, lambda: ps.hide_communication(bw, j, args, comm=lambda: None, fp64="split"), 5)
     del T, T2, Ci
     b = 3 * 8 * n ** 3
-    return {"boundary_width": list(bw), "one_launch_ms": round(t1 * 1e3, 4), "split_ms": round(t2 * 1e3, 4),
+    return {"boundary_width": list(bw), "jit_fp64_split_one_launch_ms": round(t5 * 1e3, 4),
+            "jit_fp64_split_split_ms": round(t6 * 1e3, 4),
+            "one_launch_ms": round(t1 * 1e3, 4), "split_ms": round(t2 * 1e3, 4),
             "one_launch_T_eff_GBs": round(b / t1 / 1e9, 1), "split_T_eff_GBs": round(b / t2 / 1e9, 1),
             "fp64_split_one_launch_ms": round(t3 * 1e3, 4), "fp64_split_split_ms": round(t4 * 1e3, 4),
             "fp64_split_one_launch_T_eff_GBs": round(b / t3 / 1e9, 1),
-            "fp64_split_split_T_eff_GBs": round(b / t4 / 1e9, 1), "launches": 8 * 16}
+            "fp64_split_split_T_eff_GBs": round(b / t4 / 1e9, 1), "launches": 8 * 24}
 
 
 def bench_stokes3d_solve(ps, n=127, tol=1e-6):

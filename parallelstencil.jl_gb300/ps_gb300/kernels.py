@@ -237,7 +237,7 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
     if len(bw) != 3:
         raise ArgumentError("boundary_width must be an integer or a 3-tuple")
     if hasattr(kernel, "jit_launch"):
-        _hide_communication_jit(tuple(int(b) for b in bw), kernel, args, comm, memopt, s_boundary, s_inner)
+        _hide_communication_jit(tuple(int(b) for b in bw), kernel, args, comm, memopt, s_boundary, s_inner, fp64)
         return
     if not isinstance(kernel, Diffusion3D):
         raise ArgumentError("@hide_communication is implemented for the diffusion3D kernels and for run-time "
@@ -278,7 +278,7 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
         raise errors[0]
 
 
-def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner):
+def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner, fp64="ieee"):
     """The boundary/inner split for any run-time compiled kernel: the six boundary boxes of the
     kernel's `@parallel` grid on a high-priority stream, the inner box on a normal one, `comm` on
     the host once the boundary boxes are done, while the inner box runs."""
@@ -298,10 +298,19 @@ def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner)
     cur = torch.cuda.current_stream()
     for s in (sb, si):
         s.wait_stream(cur)
-    for lo, hi in get_ranges_outer(bw, ms):
-        kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], sb, False, memopt=memopt)
-    for lo, hi in get_ranges_inner(bw, ms):
-        kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], si, False, memopt=memopt)
+    # x and y slabs widened to whole thread blocks (32 x 8): a 16-wide x slab would leave half of
+    # every warp idle, and an inner box starting mid-block would cost one more block column; the
+    # boundary boxes then hold a superset of the requested boundary (all computed before `comm`)
+    lw, hw = list(bw), list(bw)
+    for d, blk in ((0, 32), (1, 8)):
+        a = -(-bw[d] // blk) * blk  # lower slab [0, a)
+        b = ms[d] - (ms[d] - bw[d]) // blk * blk  # upper slab [ms - b, ms) from a block edge
+        if bw[d] > 0 and ms[d] > a + b:
+            lw[d], hw[d] = a, b
+    for lo, hi in get_ranges_outer(lw, ms, hw):
+        kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], sb, False, memopt=memopt, fp64=fp64)
+    for lo, hi in get_ranges_inner(lw, ms, hw):
+        kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], si, False, memopt=memopt, fp64=fp64)
     sb.synchronize()
     try:
         if comm is not None:
@@ -313,21 +322,24 @@ def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner)
     kernel.check(si)
 
 
-def get_ranges_outer(boundary_width, maxsize):
+def get_ranges_outer(boundary_width, maxsize, upper_width=None):
     """The six boundary boxes of `@hide_communication` (3-D), 0-based half-open
-    (src/ParallelKernel/hide_communication.jl:350-381)."""
+    (src/ParallelKernel/hide_communication.jl:350-381); `upper_width`: the widths at the upper ends
+    when they differ from the lower ones."""
     bw, ms = boundary_width, maxsize
+    uw = bw if upper_width is None else upper_width
     boxes = [
-        ((0, bw[1], bw[2]), (bw[0], ms[1] - bw[1], ms[2] - bw[2])),
+        ((0, bw[1], bw[2]), (bw[0], ms[1] - uw[1], ms[2] - uw[2])),
         ((0, 0, 0), (ms[0], ms[1], bw[2])),
-        ((0, 0, ms[2] - bw[2]), (ms[0], ms[1], ms[2])),
-        ((ms[0] - bw[0], bw[1], bw[2]), (ms[0], ms[1] - bw[1], ms[2] - bw[2])),
-        ((0, 0, bw[2]), (ms[0], bw[1], ms[2] - bw[2])),
-        ((0, ms[1] - bw[1], bw[2]), (ms[0], ms[1], ms[2] - bw[2])),
+        ((0, 0, ms[2] - uw[2]), (ms[0], ms[1], ms[2])),
+        ((ms[0] - uw[0], bw[1], bw[2]), (ms[0], ms[1] - uw[1], ms[2] - uw[2])),
+        ((0, 0, bw[2]), (ms[0], bw[1], ms[2] - uw[2])),
+        ((0, ms[1] - uw[1], bw[2]), (ms[0], ms[1], ms[2] - uw[2])),
     ]
     return [b for b in boxes if all(h > l for l, h in zip(*b))]
 
 
-def get_ranges_inner(boundary_width, maxsize):
+def get_ranges_inner(boundary_width, maxsize, upper_width=None):
     bw, ms = boundary_width, maxsize
-    return [((bw[0], bw[1], bw[2]), (ms[0] - bw[0], ms[1] - bw[1], ms[2] - bw[2]))]
+    uw = bw if upper_width is None else upper_width
+    return [((bw[0], bw[1], bw[2]), (ms[0] - uw[0], ms[1] - uw[1], ms[2] - uw[2]))]

@@ -131,6 +131,12 @@ def test_hide_communication_ranges_match_reference_formula():
         assert len(outer) == 6
         # the z-boundary slabs come second and third, as the reference's split of comm calls assumes
         assert outer[1][1][2] == bw[2] and outer[2][0][2] == ms[2] - bw[2]
+        # different widths at the upper ends (slabs widened to thread blocks) still tile the grid
+        uw = (bw[0] + 3, bw[1] + 1, bw[2])
+        cover[:] = 0
+        for lo, hi in get_ranges_outer(bw, ms, uw) + get_ranges_inner(bw, ms, uw):
+            cover[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] += 1
+        assert np.all(cover == 1)
 
 
 def test_ranges_to_box():

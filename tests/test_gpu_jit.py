@@ -444,11 +444,12 @@ def test_jit_memopt_from_the_definition(ps):
 
 
 @pytest.mark.parametrize("name", ["HEAT_FLUX", "TWO3D"])
-def test_jit_hide_communication_equals_one_launch(ps, name):
+@pytest.mark.parametrize("n", [(64, 40, 36), (100, 40, 36)])
+def test_jit_hide_communication_equals_one_launch(ps, name, n):
     """@hide_communication with a run-time compiled kernel: the six boundary boxes and the inner box
-    on two streams give the one-launch result; comm runs once, after the boundary boxes."""
+    on two streams give the one-launch result; comm runs once, after the boundary boxes. At 100
+    in x the x slabs are widened to whole 32-thread blocks, at 64 they are not."""
     rng = np.random.default_rng(17)
-    n = (64, 40, 36)
     k = ps.parallel_kernel(getattr(K, name))
     if name == "HEAT_FLUX":
         T, Ci = _dev(ps, rng.random(n)), _dev(ps, rng.random(n) + 0.5)
@@ -466,7 +467,14 @@ def test_jit_hide_communication_equals_one_launch(ps, name):
     for a, b in zip(ref, out):
         assert np.array_equal(ps.to_host(a), ps.to_host(b))
     with pytest.raises(ps.ArgumentError, match="boundary_width"):
-        ps.hide_communication((40, 4, 2), k, (*out, *rest))
+        ps.hide_communication((n[0] // 2, 4, 2), k, (*out, *rest))
+    # split FP64 arithmetic through the boxes: the one split launch's values
+    ref2, out2 = mk(), mk()
+    ps.parallel(k, *ref2, *rest, fp64="split")
+    ps.hide_communication((16, 4, 2), k, (*out2, *rest), comm=None, fp64="split")
+    for a, b in zip(ref2, out2):
+        assert np.array_equal(ps.to_host(a), ps.to_host(b))
+    assert not np.array_equal(ps.to_host(ref2[-1]), ps.to_host(ref[-1]))
 
 
 # ---------------------------------------------------------------- split FP64 arithmetic
