@@ -849,7 +849,8 @@ def bench_adjoint(ps, torch, n=256, nt=200, every=20):
                      "gradient_over_forward": round(t_grad / t_fwd, 3), "loss": loss,
                      "checkpoints": st.checkpoints, "recomputed_steps": st.recomputed_steps,
                      "grad_norm": float(g.norm())}
-        out["launches"] += 2 * nt + st.recomputed_steps + nt + 2
+        # forward and recomputed steps, adjoint steps (split: a pair pass before each), misfit
+        out["launches"] += 2 * nt + st.recomputed_steps + nt * (2 if fp64 == "split" else 1) + 2
         del T, T2, g
     return out
 

@@ -73,31 +73,52 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(T* __restrict__ lamT,
 // every input is split into an FP32 pair with integer operations, the sums and products of the
 // IEEE kernel above run on pairs (47-bit significands), and the results are applied in FP64 as
 // λ = (λ2 + acc.h) + acc.l and glam = (glam + g.h) + g.l. Same statement order as the IEEE kernel.
+// Two passes: adjoint_pairs_kernel splits T and lam and forms μ = (dt Ci) λT2 once per cell into
+// pair arrays; adjoint_step_split_kernel reads the seven points' pairs from them (each value was
+// split and each μ multiplied seven times when one pass did everything: 1.35 ms per 256^3 step).
+__global__ void __launch_bounds__(256) adjoint_pairs_kernel(float2* __restrict__ Tp, float2* __restrict__ Lp,
+                                                            float2* __restrict__ Mp, const double* __restrict__ lamT2,
+                                                            const double* __restrict__ Tn, const double* __restrict__ Ci,
+                                                            const double* __restrict__ lam, dd dt, int64_t nx,
+                                                            int64_t ny, int64_t nz, int* err) {
+    bool big = false;
+    const int64_t n = nx * ny * nz;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+        const bool inner = i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2 && k >= 1 && k <= nz - 2;
+        const dd t = dd_split(__ldg(Tn + c), big), l = dd_split(__ldg(lam + c), big);
+        dd mu = {0.0f, 0.0f};
+        if (inner) mu = dd_mul(dd_mul(dt, dd_split(__ldg(Ci + c), big)), dd_split(__ldg(lamT2 + c), big));
+        Tp[c] = make_float2(t.h, t.l);
+        Lp[c] = make_float2(l.h, l.l);
+        Mp[c] = make_float2(mu.h, mu.l);
+    }
+    if (big) atomicOr(err, DEV_ERR_RANGE);  // a magnitude outside the split range: reported at the next sync
+}
+
 __global__ void __launch_bounds__(256) adjoint_step_split_kernel(double* __restrict__ lamT,
                                                                  const double* __restrict__ lamT2,
-                                                                 const double* __restrict__ Tn,
-                                                                 const double* __restrict__ Ci,
-                                                                 const double* __restrict__ lam,
-                                                                 double* __restrict__ glam, dd dt, dd hh0, dd hh1,
-                                                                 dd hh2, int64_t nx, int64_t ny, int64_t nz, int* err) {
+                                                                 const float2* __restrict__ Tp,
+                                                                 const float2* __restrict__ Lp,
+                                                                 const float2* __restrict__ Mp,
+                                                                 double* __restrict__ glam, dd hh0, dd hh1, dd hh2,
+                                                                 int64_t nx, int64_t ny, int64_t nz) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t j = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
     if (i >= nx || j >= ny) return;
     const dd hh[3] = {hh0, hh1, hh2};
     const int64_t st[3] = {1, nx, nx * ny};
     const int64_t ext[3] = {nx, ny, nz};
-    auto inner = [&](int64_t a, int64_t b, int64_t c) {
-        return a >= 1 && a <= nx - 2 && b >= 1 && b <= ny - 2 && c >= 1 && c <= nz - 2;
-    };
     const dd zero = {0.0f, 0.0f};
-    bool big = false;
+    auto pr = [](const float2* a, int64_t c) {
+        const float2 v = __ldg(a + c);
+        return dd{v.x, v.y};
+    };
     for (int64_t k = blockIdx.z; k < nz; k += gridDim.z) {
         const int64_t c = i + nx * (j + ny * k);
         const int64_t idx[3] = {i, j, k};
-        const bool inner_c = inner(i, j, k);
-        const dd mu_c = inner_c ? dd_mul(dd_mul(dt, dd_split(__ldg(Ci + c), big)), dd_split(__ldg(lamT2 + c), big))
-                                : zero;
-        const dd lc = dd_split(__ldg(lam + c), big), Tc = dd_split(__ldg(Tn + c), big);
+        const bool inner_c = i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2 && k >= 1 && k <= nz - 2;
+        const dd mu_c = pr(Mp, c), lc = pr(Lp, c), Tc = pr(Tp, c);
         dd acc = zero, g = zero;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -106,12 +127,9 @@ __global__ void __launch_bounds__(256) adjoint_step_split_kernel(double* __restr
                 const int64_t q = idx[d] + sgn;
                 if (q < 0 || q >= ext[d]) continue;
                 const int64_t nb = c + sgn * st[d];
-                const bool inner_n = inner(d == 0 ? q : i, d == 1 ? q : j, d == 2 ? q : k);
-                const dd mu_n = inner_n ? dd_mul(dd_mul(dt, dd_split(__ldg(Ci + nb), big)),
-                                                 dd_split(__ldg(lamT2 + nb), big))
-                                        : zero;
-                const dd kf = dd_scale(dd_add(lc, dd_split(__ldg(lam + nb), big)), 0.5f);
-                const dd Tnb = dd_split(__ldg(Tn + nb), big);
+                const dd mu_n = pr(Mp, nb);  // zero off the inner cells
+                const dd kf = dd_scale(dd_add(lc, pr(Lp, nb)), 0.5f);
+                const dd Tnb = pr(Tp, nb);
                 const dd mua = sgn > 0 ? mu_c : mu_n, mub = sgn > 0 ? mu_n : mu_c;
                 const dd Ta = sgn > 0 ? Tc : Tnb, Tb = sgn > 0 ? Tnb : Tc;
                 acc = dd_add(acc, dd_mul(dd_mul(hh[d], kf), dd_sub(mu_n, mu_c)));
@@ -121,7 +139,6 @@ __global__ void __launch_bounds__(256) adjoint_step_split_kernel(double* __restr
         lamT[c] = inner_c ? (__ldg(lamT2 + c) + f32_to_f64(acc.h)) + f32_to_f64(acc.l) : 0.0;
         glam[c] = (glam[c] + f32_to_f64(g.h)) + f32_to_f64(g.l);
     }
-    if (big) atomicOr(err, DEV_ERR_RANGE);  // a magnitude outside the split range: reported at the next sync
 }
 
 // λ = (T - T_obs) on inner cells (0 on the boundary); loss += 0.5 Σ (T - T_obs)^2 over all cells.
@@ -153,10 +170,32 @@ static int check3(const ps_array& a, const ps_array& ref, const char* name) {
 static void* g_adj_scratch = nullptr;
 static size_t g_adj_bytes = 0;
 
+// Pair arrays of the split reverse step (T, lam, μ: 3 x 8 bytes per cell), grow-only.
+static void* g_adj_pairs = nullptr;
+static size_t g_adj_pairs_bytes = 0;
+
 void adjoint_free_scratch() {
     if (g_adj_scratch) cudaFree(g_adj_scratch);
     g_adj_scratch = nullptr;
     g_adj_bytes = 0;
+    if (g_adj_pairs) cudaFree(g_adj_pairs);
+    g_adj_pairs = nullptr;
+    g_adj_pairs_bytes = 0;
+}
+
+static int adjoint_pairs(size_t bytes, char** p) {
+    if (bytes > g_adj_pairs_bytes) {
+        if (g_adj_pairs) cudaFree(g_adj_pairs);
+        g_adj_pairs = nullptr;
+        g_adj_pairs_bytes = 0;
+        if (cudaMalloc(&g_adj_pairs, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(PS_ERR_NOMEM, "adjoint step: pair scratch of %zu bytes failed", bytes);
+        }
+        g_adj_pairs_bytes = bytes;
+    }
+    *p = static_cast<char*>(g_adj_pairs);
+    return PS_OK;
 }
 
 static int adjoint_scratch(size_t bytes, char** p) {
@@ -183,13 +222,25 @@ static int launch_adjoint_step(const ps_array& lamT, const ps_array& lamT2, cons
                                cudaStream_t s, int fp64_mode = PS_FP64_IEEE, int* d_err = nullptr) {
     dim3 blk(32, 8);
     dim3 grd((unsigned)((Tn.n[0] + 31) / 32), (unsigned)((Tn.n[1] + 7) / 8), (unsigned)std::min<int64_t>(Tn.n[2], 65535));
-    if (Tn.dtype == PS_F64 && fp64_mode != PS_FP64_IEEE && d_err)
+    if (Tn.dtype == PS_F64 && fp64_mode != PS_FP64_IEEE && d_err) {
+        const int64_t n = Tn.n[0] * Tn.n[1] * Tn.n[2];
+        char* pp = nullptr;
+        PS_TRY(adjoint_pairs((size_t)n * 3 * sizeof(float2), &pp));
+        float2* Tp = reinterpret_cast<float2*>(pp);
+        float2 *Lp = Tp + n, *Mp = Lp + n;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 8));
+        adjoint_pairs_kernel<<<g, 256, 0, s>>>(Tp, Lp, Mp, static_cast<const double*>(lamT2.ptr),
+                                               static_cast<const double*>(Tn.ptr), static_cast<const double*>(Ci.ptr),
+                                               static_cast<const double*>(lam.ptr), host_split(dt), Tn.n[0], Tn.n[1],
+                                               Tn.n[2], d_err);
         adjoint_step_split_kernel<<<grd, blk, 0, s>>>(
-            static_cast<double*>(lamT.ptr), static_cast<const double*>(lamT2.ptr), static_cast<const double*>(Tn.ptr),
-            static_cast<const double*>(Ci.ptr), static_cast<const double*>(lam.ptr), static_cast<double*>(glam.ptr),
-            host_split(dt), host_split(hx * hx), host_split(hy * hy), host_split(hz * hz), Tn.n[0], Tn.n[1], Tn.n[2],
-            d_err);
-    else if (Tn.dtype == PS_F64)
+            static_cast<double*>(lamT.ptr), static_cast<const double*>(lamT2.ptr), Tp, Lp, Mp,
+            static_cast<double*>(glam.ptr), host_split(hx * hx), host_split(hy * hy), host_split(hz * hz), Tn.n[0],
+            Tn.n[1], Tn.n[2]);
+    } else if (Tn.dtype == PS_F64)
         adjoint_step_kernel<double><<<grd, blk, 0, s>>>(
             static_cast<double*>(lamT.ptr), static_cast<const double*>(lamT2.ptr), static_cast<const double*>(Tn.ptr),
             static_cast<const double*>(Ci.ptr), static_cast<const double*>(lam.ptr), static_cast<double*>(glam.ptr), dt,
