@@ -347,19 +347,34 @@ def run_ours(a, world, rank, local):
         cfg.fp64_mode = 3  # state on the fixed grid, as the headline
         P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
 
+        # where a job's time goes: CUDA events around its copies, the host time of the (blocking) run
+        phases = {"h2d": [], "d2h": [], "run": []}
+
+        def timed_copy(kind, k, fn):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(streams[k])
+            fn()
+            e1.record(streams[k])
+            phases[kind].append((e0, e1))
+
         def h2d(k):
             dT, _, dCi, dlam = (descriptor(x) for x in sets[k])
             s = stream_handle(streams[k])
-            for d, h in ((dT, hT), (dCi, hCi), (dlam, hlam)):
-                _lib.check(lib.ps_copy_h2d_async(d, P(h), s))
+
+            def copies():
+                for d, h in ((dT, hT), (dCi, hCi), (dlam, hlam)):
+                    _lib.check(lib.ps_copy_h2d_async(d, P(h), s))
+            timed_copy("h2d", k, copies)
 
         def run_and_d2h(k):
             dT, dT2, dCi, dlam = (descriptor(x) for x in sets[k])
             s = stream_handle(streams[k])
             _lib.check(lib.ps_copy_d2d_async(dT2, dT, s))
+            t0_ = time.perf_counter()
             _lib.check(lib.ps_diffusion3d_run(3, dT, dT2, dCi, dlam, 0.0, dt, _dx, _dx, _dx, NT_JOB, ctypes.byref(cfg),
                                               s))
-            _lib.check(lib.ps_copy_d2h_async(P(hout[k]), dT, s))
+            phases["run"].append(time.perf_counter() - t0_)
+            timed_copy("d2h", k, lambda: _lib.check(lib.ps_copy_d2h_async(P(hout[k]), dT, s)))
 
         def jobs_run(jobs):
             h2d(0)
@@ -379,9 +394,15 @@ def run_ours(a, world, rank, local):
         t_job1 = time.perf_counter() - t0
         jobs = max(1, a.e2e_jobs)
         torch.cuda.synchronize()
+        for v in phases.values():
+            v.clear()
         t0 = time.perf_counter()
         jobs_run(jobs)
         t_e2e = max_over_ranks((time.perf_counter() - t0) / jobs)
+        e2e_phases = {f"{kind}_ms_median": round(float(np.median([e0.elapsed_time(e1) for e0, e1 in phases[kind]])), 3)
+                      for kind in ("h2d", "d2h")}
+        e2e_phases["run_ms_median"] = round(float(np.median(phases["run"])) * 1e3, 3)
+        e2e_phases["run_ms_max"] = round(float(np.max(phases["run"])) * 1e3, 3)
         launches += (jobs + 2) * NT_JOB
         del hostbufs, hT, hCi, hlam, hout, sets
         if not a.quick:
@@ -489,7 +510,7 @@ def run_ours(a, world, rank, local):
                         f"buffers, {NT_JOB} steps, T device -> host; {max(1, a.e2e_jobs)} jobs, two device buffer "
                         f"sets on two streams (one job's copies overlap the other's steps)",
                 "seconds_per_job": round(t_e2e, 5), "seconds_one_job_alone": round(t_job1, 5),
-                "one_job_alone_GBs": round(e2e_bytes / t_job1 / 1e9, 2)},
+                "one_job_alone_GBs": round(e2e_bytes / t_job1 / 1e9, 2), "phases": e2e_phases},
         "gpu_launches": launches,
         "stokes2d_time_to_tol": stokes,
         "warm_start_time_to_tol": warm,
