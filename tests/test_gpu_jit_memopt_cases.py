@@ -5,7 +5,9 @@ compiled and launched with memopt=true, against the expected arrays those tests 
 broadcasting -- restated here with numpy slices in the same operation order. Inputs are the tests'
 `(ix + (iy-1) nx + (iz-1) nx ny)^3` fields (times 1, 2, 3), so every value is an integer below
 2^53 and the bar is exact equality, as in the reference. Grid sizes: the tests' (32, 8, 8) and
-the ragged (33, 7, 8) and (31, 7, 9) their comments list."""
+the ragged (33, 7, 8) and (31, 7, 9) their comments list. The 2-D testset (:1084-1195: y second
+differences in index and FD-macro form, a mixed x/y stencil over two arrays, optranges, loopsize
+and optimize_halo_read) runs the same way at (32, 8), (33, 7) and (300, 131)."""
 import numpy as np
 import pytest
 
@@ -256,3 +258,73 @@ def test_memopt_two_and_three_arrays(ps, n):
     ref = np.zeros(n)
     ref[I, I, I] = c + ((Bx[1:, I, I] - Bx[:-1, I, I]) * s) + _lap(B3)[1]
     assert np.array_equal(T2, ref)
+
+
+# ---------------------------------------------------------------- 2-D (test/test_parallel.jl:1084-1195)
+D2Y_2D_IDX = """@parallel_indices (ix, iy) ndims=2 memopt=true loopdim=2 function d2_memopt_indices!(A2, A)
+    if (1 < iy < size(A2, 2))
+        A2[ix, iy] = A[ix, iy + 1] - 2 * A[ix, iy] + A[ix, iy - 1]
+    end
+    return
+end"""
+
+D2YI_2D_FD = """@parallel ndims=2 memopt=true optvars=B loopdim=2 function d2_memopt_kernel!(A2, B)
+    @inn(A2) = @d2_yi(B)
+    return
+end"""
+
+MIXED_2D = """@parallel_indices (ix, iy) ndims=2 memopt=true loopdim=2 optvars=A function mixed_memopt_indices!(A2, A, B)
+    if (1 < ix < size(A2, 1) && 1 < iy < size(A2, 2))
+        A2[ix, iy] = (A[ix, iy + 1] - 2 * A[ix, iy] + A[ix, iy - 1]) + (B[ix + 1, iy] - 2 * B[ix, iy] + B[ix - 1, iy])
+    end
+    return
+end"""
+
+RANGED_2D = """@parallel_indices (ix, iy) ndims=2 memopt=true loopdim=2 optvars=A optranges=(A=(0:0, -1:1, 0:0),) function ranged_memopt_indices!(A2, A)
+    if (1 < iy < size(A2, 2))
+        A2[ix, iy] = A[ix, iy + 1] - 2 * A[ix, iy] + A[ix, iy - 1]
+    end
+    return
+end"""
+
+LOOP4_2D = """@parallel_indices (ix, iy) ndims=2 memopt=true loopdim=2 loopsize=4 function loopsize_memopt_indices!(A2, A)
+    if (1 < iy < size(A2, 2))
+        A2[ix, iy] = A[ix, iy + 1] - 2 * A[ix, iy] + A[ix, iy - 1]
+    end
+    return
+end"""
+
+HALO_2D = """@parallel_indices (ix, iy) ndims=2 memopt=true loopdim=2 optvars=A optranges=(A=(0:0, -1:1, 0:0),) optimize_halo_read=false function halo_read_memopt_indices!(A2, A)
+    if (1 < iy < size(A2, 2))
+        A2[ix, iy] = A[ix, iy + 1] - 2 * A[ix, iy] + A[ix, iy - 1]
+    end
+    return
+end"""
+
+
+def cube2(shape):
+    n = int(np.prod(shape))
+    return np.asfortranarray(np.arange(1, n + 1, dtype=np.float64).reshape(shape, order="F") ** 3)
+
+
+@pytest.mark.parametrize("n", [(32, 8), (33, 7), (300, 131)])
+def test_memopt_2d_cases(ps, n):
+    """The 2-D memopt kernels (y sweeps for the `@parallel` one), exact against the tests' broadcast
+    expectations, at the tests' (32, 8), a ragged size and one with several blocks per dimension."""
+    A = cube2(n)
+    ref = np.zeros(n)
+    ref[:, 1:-1] = A[:, 2:] - 2 * A[:, 1:-1] + A[:, :-2]
+    for src in (D2Y_2D_IDX, RANGED_2D, LOOP4_2D, HALO_2D):
+        A2, _ = _run(ps, src, [np.zeros(n), A])
+        assert np.array_equal(A2, ref), src[:60]
+    A2, _ = _run(ps, D2YI_2D_FD, [np.zeros(n), A])
+    r2 = np.zeros(n)
+    r2[1:-1, 1:-1] = A[1:-1, 2:] - 2 * A[1:-1, 1:-1] + A[1:-1, :-2]
+    # @d2_yi is (B[y+1] - B) - (B - B[y-1]); the expectation's `B+ - 2B + B-` is the same integer
+    assert np.array_equal(A2, r2)
+    i, j = np.meshgrid(np.arange(1, n[0] + 1), np.arange(1, n[1] + 1), indexing="ij")
+    B = np.asfortranarray((2 * i - j).astype(np.float64))
+    A2, _, _ = _run(ps, MIXED_2D, [np.zeros(n), A, B])
+    r3 = np.zeros(n)
+    r3[1:-1, 1:-1] = (A[1:-1, 2:] - 2 * A[1:-1, 1:-1] + A[1:-1, :-2]) + (B[2:, 1:-1] - 2 * B[1:-1, 1:-1] + B[:-2, 1:-1])
+    assert np.array_equal(A2, r3)
