@@ -59,6 +59,19 @@ _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
 MAX_ARRAYS = MAX_SCALARS = 32
 RESIDENT_THREADS = 152 * 2048  # threads a GB300 holds at once (152 SMs x 2048)
+# kernel-language macros (src/ParallelKernel/kernel_language.jl): a kernel that uses any of them
+# keeps one point per thread (a sweep would change what @threadIdx, @sharedMem and barriers see)
+_KERNEL_LANGUAGE = {"__m_" + m for m in ("threadIdx", "blockIdx", "blockDim", "gridDim", "sharedMem", "sync_threads",
+                                         "warpsize", "laneid", "active_mask", "shfl_sync", "shfl_up_sync",
+                                         "shfl_down_sync", "shfl_xor_sync", "vote_any_sync", "vote_all_sync",
+                                         "vote_ballot_sync")}
+
+
+def uses_kernel_language(kd) -> bool:
+    return any(isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and n.func.id in _KERNEL_LANGUAGE
+               for n in ast.walk(ast.Module(body=kd.body, type_ignores=[])))
+
+
 _COLLECTIVE = {"__m_shfl_sync", "__m_shfl_up_sync", "__m_shfl_down_sync", "__m_shfl_xor_sync", "__m_vote_any_sync",
                "__m_vote_all_sync", "__m_vote_ballot_sync"}
 _MATH = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "sinh", "cosh", "atan", "asin", "acos", "log10",
@@ -379,7 +392,7 @@ class _Gen:
         # memopt: each thread sweeps g.loop consecutive indices of the last dimension (z in 3-D, y in
         # 2-D) and carries read-only stencil points it already holds to the next index
         # (src/memopt.jl's register queues for loopdim 3 and 2, in plain code)
-        self.zloop = bool(zloop) and kd.kind == "parallel" and ndims in (2, 3)
+        self.zloop = bool(zloop) and kd.kind == "parallel" and ndims in (2, 3) and not uses_kernel_language(kd)
         self.sweep = ndims - 1 if self.zloop else None
         self.persist = []  # registers that live across the z sweep
         self.nstmt = 0
@@ -1124,6 +1137,7 @@ class JitKernel:
     def __init__(self, src: str, ndims=None):
         self.ndims = ndims
         self.kd = parse(src)
+        self._kernel_language = uses_kernel_language(self.kd)
         self.name, self.nargs = self.kd.name, len(self.kd.args)
         self._handles = {}
         self._collective = {}
@@ -1194,7 +1208,7 @@ class JitKernel:
         # faster: a one-point-per-thread kernel keeps too few loads in flight); memopt=false keeps one
         # point per thread, as the definition or the call may ask
         want = memopt if memopt is not None else self.kd.options.get("memopt", "true") == "true"
-        zl = bool(want) and self.kd.kind == "parallel" and ndims in (2, 3)
+        zl = bool(want) and self.kd.kind == "parallel" and ndims in (2, 3) and not self._kernel_language
         loop = [1, 1, 1]
         if zl:
             sd = ndims - 1

@@ -321,3 +321,14 @@ def test_translator_z_sweep_carries_only_read_only_points(jit):
     carried = re.findall(r"const R (L\d+) = pr(\d) \? P\d_\d+ : (.*?);", body)
     assert carried and all("a2[" in ld for _, _, ld in carried)  # only B (argument 2) is read-only
     assert "a0[" not in "".join(ld for _, _, ld in carried)  # A is written by the first statement
+
+
+def test_kernel_language_keeps_one_point_per_thread(jit):
+    """A `@parallel` kernel that uses the kernel language (@threadIdx, @sharedMem, barriers, shuffles)
+    is not turned into a sweep: what those see must stay the launch's own thread layout."""
+    src = ("@parallel function kl!(A, B)\n    @all(A) = @all(B) * @threadIdx().x\n    @sync_threads()\n"
+           "    return\nend")
+    kd = jit.parse(src)
+    assert jit.uses_kernel_language(kd)
+    assert "g.loop" not in jit.generate(kd, 3, "double", zloop=True).split("ps_jit_entry")[1]
+    assert not jit.uses_kernel_language(jit.parse(K.HEAT_FLUX))
