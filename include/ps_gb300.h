@@ -213,7 +213,9 @@ typedef int (*ps_comm_fn)(void* ctx);
  * slabs of width bw run on s_boundary, the inner box on s_inner; comm (may be NULL) runs
  * after the boundary slabs finish and before the inner box is waited for. On return both
  * streams are synchronised. cfg supplies memopt and fp64_mode (its ranges are ignored).
- * Result identical to ps_diffusion3d_step. */
+ * With memopt the x and y slabs are widened to whole z-sweep tiles when the grid allows it
+ * (x: 64 cells for FP64 / 128 for FP32 from an even cell, y: 8 rows), so the boundary phase
+ * computes a superset of the bw-wide boundary. Result identical to ps_diffusion3d_step. */
 int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr,
                               double lam, double dt, double hx, double hy, double hz,
                               const ps_launch* cfg, const int64_t bw[3], void* s_boundary, void* s_inner,
