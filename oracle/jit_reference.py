@@ -336,10 +336,40 @@ def parse(src: str) -> OracleKernel:
         # (I...): the index tuple; A[I...] indexes A at the thread's own point
         indices = ["..."]
         body_text = re.sub(r"\b\w+\.\.\.", " __splat__ ", body_text)
+    # one-line local functions `f(a, b) = [return] expr`: inlined at their calls
+    fns = {}
+    for fm in re.finditer(r"^[ \t]*(\w+)[ \t]*\(([\w \t,]*)\)[ \t]*=(?!=)[ \t]*(?:return[ \t]+)?(.+)$", body_text, re.M):
+        fns[fm.group(1)] = ([a.strip() for a in fm.group(2).split(",") if a.strip()], _P(_tokens(fm.group(3))).expr())
+    body_text = re.sub(r"^[ \t]*\w+[ \t]*\([\w \t,]*\)[ \t]*=(?!=)[^\n]*$", "", body_text, flags=re.M)
     p = _P(_tokens(body_text))
-    body = p.block(())
+    body = _inline(p.block(()), fns) if fns else p.block(())
     nd = opts.get("ndims", "").strip("()")
     return OracleKernel(m.group(3), kind, indices, argnames, body, int(nd) if nd.isdigit() else None)
+
+
+def _inline(node, fns):
+    """Replace calls of local functions by their expression with the parameters bound."""
+    if isinstance(node, list):
+        return [_inline(x, fns) for x in node]
+    if not isinstance(node, tuple):
+        return node
+    node = tuple(_inline(x, fns) for x in node)
+    if len(node) == 3 and node[0] == "call" and node[1] in fns:
+        params, expr = fns[node[1]]
+        bind = dict(zip(params, node[2]))
+
+        def sub(x):
+            if isinstance(x, list):
+                return [sub(y) for y in x]
+            if not isinstance(x, tuple):
+                return x
+            if x[0] == "name" and x[1] in bind:
+                return bind[x[1]]
+            if x[0] == "index" and x[1] in bind and bind[x[1]][0] == "name":
+                return ("index", bind[x[1]][1], sub(x[2]))
+            return tuple(sub(y) for y in x)
+        return _inline(sub(expr), fns)
+    return node
 
 
 # ---------------------------------------------------------------- FiniteDifferences macros by name

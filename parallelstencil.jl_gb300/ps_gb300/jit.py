@@ -260,6 +260,46 @@ def _array_uses(tree) -> set:
     return used
 
 
+_LOCAL_FN = re.compile(r"^[ \t]*(?!__m_)(\w+)[ \t]*\(([\w \t,]*)\)[ \t]*=(?!=)[ \t]*(?:return[ \t]+)?(.+)$", re.M)
+
+
+def _local_functions(text: str):
+    """One-line local function definitions in a kernel body (`f(a, b) = [return] expr`): removed
+    from the statements and returned as name -> (parameters, expression), for inlining at each call."""
+    fns = {}
+
+    def take(m):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip()]
+        try:
+            expr = ast.parse(m.group(3).strip(), mode="eval").body
+        except SyntaxError as e:
+            raise ArgumentError(f"cannot parse the local function {m.group(1)}: {e}") from None
+        fns[m.group(1)] = (params, expr)
+        return ""
+    return _LOCAL_FN.sub(take, text), fns
+
+
+class _Inline(ast.NodeTransformer):
+    """Calls of local functions replaced by their expression, parameters bound to the arguments."""
+
+    def __init__(self, fns):
+        self.fns = fns
+
+    def visit_Call(self, n):
+        self.generic_visit(n)
+        if isinstance(n.func, ast.Name) and n.func.id in self.fns:
+            params, expr = self.fns[n.func.id]
+            if len(params) != len(n.args):
+                raise ArgumentError(f"local function {n.func.id} takes {len(params)} arguments")
+            bind = dict(zip(params, n.args))
+
+            class _Bind(ast.NodeTransformer):
+                def visit_Name(self, m):
+                    return copy.deepcopy(bind[m.id]) if m.id in bind else m
+            return self.visit(_Bind().visit(copy.deepcopy(expr)))
+        return n
+
+
 class _AugAssign(ast.NodeTransformer):
     """`a op= b` is `a = a op b` (Julia lowers it so)."""
 
@@ -350,9 +390,10 @@ def parse(src: str) -> KernelDef:
     rest = rest.rstrip()
     if not rest.endswith("end"):
         raise ArgumentError("kernel definition must end with `end`")
-    body = _to_python(_sanitize(rest[:-3]))
+    text, local_fns = _local_functions(_sanitize(rest[:-3]))
+    body = _to_python(text)
     try:
-        tree = ast.fix_missing_locations(_AugAssign().visit(ast.parse(body)))
+        tree = ast.fix_missing_locations(_Inline(local_fns).visit(_AugAssign().visit(ast.parse(body))))
     except SyntaxError as e:
         raise ArgumentError(f"cannot parse the kernel body: {e}") from None
     used = _array_uses(tree)
@@ -632,10 +673,11 @@ class _Gen:
             ops = {ast.Add: "+", ast.Sub: "-", ast.Mult: "*", ast.Div: "/"}
             if type(e.op) not in ops:
                 raise ArgumentError("unsupported operator")
-            c = "int" if (self.etype(e) == "int" and ctx != "real") else "real"
-            if isinstance(e.op, ast.Div):
-                c = "real"
-            return f"({E(e.left, c)} {ops[type(e.op)]} {E(e.right, c)})"
+            if self.etype(e) == "int" and not isinstance(e.op, ast.Div):
+                # Julia: Int op Int is an Int, converted once where a real value is wanted
+                v = f"({E(e.left, 'int')} {ops[type(e.op)]} {E(e.right, 'int')})"
+                return f"((R){v})" if ctx == "real" else v
+            return f"({E(e.left, 'real')} {ops[type(e.op)]} {E(e.right, 'real')})"
         if isinstance(e, ast.Compare):
             parts, left = [], e.left
             for op, right in zip(e.ops, e.comparators):

@@ -89,6 +89,19 @@ SMEM_OFFSET = """@parallel_indices (ix,iy) function smem_offset!(B, A)
     return
 end"""
 
+# a one-line local function, inlined at its call (test/ParallelKernel/test_parallel.jl)
+LOCAL_FN = """@parallel_indices (ix,iy,iz) function write_indices!(A)
+    compute_indices(A) = return ix + (iy-1)*size(A,1) + (iz-1)*size(A,1)*size(A,2)
+    A[ix,iy,iz] = compute_indices(A)
+    return
+end"""
+
+# an Int expression stored into a real array: computed as Int, converted once (as Julia does)
+INT_EXPR2D = """@parallel_indices (ix, iy) function int_expr2d!(A)
+    A[ix, iy] = ix + (iy - 1) * size(A, 1)
+    return
+end"""
+
 # 2-D first-order upwind advection: explicit indices, chained comparisons, Bool * x
 UPWIND2D = """@parallel_indices (i, j) function upwind2d!(Tn, T, u, w, dt, rdx, rdy)
     if (1 < i < size(T, 1) && 1 < j < size(T, 2))

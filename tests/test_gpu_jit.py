@@ -115,6 +115,7 @@ def _cases(dt, nx=21, ny=17):
                         r(nx - 2, ny - 2), 0.05], None),
         "UPWIND2D": ([r(nx, ny), r(nx, ny), r(nx, ny), r(nx, ny), 0.01, 3.0, 5.0], None),
         "AUGASSIGN": ([r(40), r(40), 0.3], None),
+        "LOCAL_FN": ([np.zeros((6, 5, 4), dt)], None),
         "QUALIFIED2D": ([r(nx, ny), r(nx, ny)], None),
         "SPLAT_COPY": ([r(nx, ny), r(nx, ny), 1.5], None),
         "HEAT2D_FD": ([r(nx, ny), r(nx, ny), _pos(rng, (nx, ny), dt), 0.7, 1e-3, 9.0, 11.0], None),
@@ -277,6 +278,16 @@ def test_jit_shared_memory_larger_than_48k(ps):
                 shmem=100 * 1024)
     ps.parallel(ps.parallel_kernel(K.HEAT2D_PLAIN), B, _dev(ps, T), _dev(ps, Ci), *sc)
     assert np.array_equal(ps.to_host(A), ps.to_host(B))
+
+
+def test_jit_int_expression_converted_once(ps):
+    """`A[ix, iy] = ix + (iy - 1) * size(A, 1)` into FP32 beyond 2^24: the Int value rounded once to
+    Float32, as Julia converts it (real arithmetic on the parts would round the product and the sum)."""
+    n = (5003, 4001)
+    A = ps.zeros(*n, dtype=np.float32)
+    ps.parallel(ps.parallel_kernel(K.INT_EXPR2D), A)
+    i, j = np.meshgrid(np.arange(1, n[0] + 1, dtype=np.int64), np.arange(1, n[1] + 1, dtype=np.int64), indexing="ij")
+    assert np.array_equal(ps.to_host(A), (i + (j - 1) * n[0]).astype(np.float32))
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["f64", "f32"])
