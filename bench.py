@@ -86,7 +86,11 @@ class ClockSampler:
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # the raw samples: PS_BENCH_CLOCKS_DIR if set, else the system's temporary directory
+        import tempfile
+
+        d = os.environ.get("PS_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
