@@ -332,3 +332,44 @@ def test_kernel_language_keeps_one_point_per_thread(jit):
     assert jit.uses_kernel_language(kd)
     assert "g.loop" not in jit.generate(kd, 3, "double", zloop=True).split("ps_jit_entry")[1]
     assert not jit.uses_kernel_language(jit.parse(K.HEAT_FLUX))
+
+
+def test_interpreter_language_additions(jr):
+    """Compound assignment, module-qualified macros, (I...) index tuples, local functions and Int
+    expressions, on the interpreter against numpy."""
+    rng = np.random.default_rng(3)
+    A, B = rng.random(12), rng.random(12)
+    A0 = A.copy()
+    jr.run(K.AUGASSIGN, [A, B, 0.3])
+    assert np.array_equal(A, (((A0 + 0.3 * B * 100.65) - 1.5) * 2) / 3)
+    Bq = np.asfortranarray(rng.random((7, 6)))
+    A2 = np.zeros((7, 6), order="F")
+    jr.run(K.QUALIFIED2D, [A2, Bq])
+    exp = np.zeros((7, 6))
+    exp[1:-1, 1:-1] = (Bq[1:-1, 2:] - Bq[1:-1, 1:-1]) - (Bq[1:-1, 1:-1] - Bq[1:-1, :-2])
+    assert np.array_equal(A2, exp)
+    for shape in ((7, 5), (4, 3, 5)):
+        X = np.asfortranarray(rng.random(shape))
+        Y = np.zeros(shape, order="F")
+        jr.run(K.SPLAT_COPY, [Y, X, 1.5])
+        assert np.array_equal(Y, 1.5 * X)
+    L = np.zeros((6, 5, 4), order="F")
+    jr.run(K.LOCAL_FN, [L])
+    assert np.array_equal(L, np.arange(1, 121, dtype=float).reshape((6, 5, 4), order="F"))
+    F = np.zeros((9, 7), dtype=np.float32, order="F")
+    jr.run(K.INT_EXPR2D, [F])
+    assert np.array_equal(F, np.arange(1, 64, dtype=np.float32).reshape((9, 7), order="F"))
+
+
+def test_translator_language_additions(jit):
+    """The same kernels translate; local functions leave no call behind, `I...` indexes with the
+    thread's own indices, Int expressions stay Int until the store."""
+    for name, nd in (("AUGASSIGN", 1), ("QUALIFIED2D", 2), ("SPLAT_COPY", 2), ("SPLAT_COPY", 3), ("LOCAL_FN", 3),
+                     ("INT_EXPR2D", 2)):
+        src = jit.generate(jit.parse(getattr(K, name)), nd, "float")
+        assert "ps_jit_entry" in src
+    body = jit.generate(jit.parse(K.LOCAL_FN), 3, "double").split("ps_jit_entry")[1]
+    assert "compute_indices" not in body
+    body = jit.generate(jit.parse(K.INT_EXPR2D), 2, "float").split("ps_jit_entry")[1]
+    assert "- 1LL" in body and "(R)1.0" not in body
+    assert jit.parse(K.SPLAT_COPY).splat == "I"
