@@ -76,12 +76,16 @@ __device__ __forceinline__ T fd_eval_f(F at) {
         }
         if constexpr (KIND == PS_FD_AV) return s * T(1.0 / NC);  // 0.5, 0.25, 0.125: exact literals
         else return (T(1.0) / s) * T(NC);
-    } else {  // maxloc / minloc; OPD = ndims
+    } else {  // maxloc / minloc; OPD = ndims, or 5: a 2-D macro laid out as (nx, 1, ny) (y as z)
         constexpr bool MX = KIND == PS_FD_MAXLOC;
         const auto f = [](T a, T b) { return MX ? jl_max(a, b) : jl_min(a, b); };
         T m = f(f(at(-1, 0, 0), at(1, 0, 0)), at(0, 0, 0));
+        if constexpr (OPD == 5) {
+            m = f(m, f(at(0, 0, -1), at(0, 0, 1)));
+        } else {
 #pragma unroll
-        for (int k = 1; k < OPD; k++) m = f(m, f(at(0, -(k == 1), -(k == 2)), at(0, k == 1, k == 2)));
+            for (int k = 1; k < OPD; k++) m = f(m, f(at(0, -(k == 1), -(k == 2)), at(0, k == 1, k == 2)));
+        }
         return m;
     }
 }
@@ -89,12 +93,13 @@ __device__ __forceinline__ T fd_eval_f(F at) {
 // z offsets the macro reads (3-D): [fd_zlo, fd_zhi]; a window of zhi - zlo + 1 planes when > 1.
 template <int KIND, int OPD>
 __host__ __device__ constexpr int fd_zlo() {
-    return ((KIND == PS_FD_DIFF2 && OPD == 4) || ((KIND == PS_FD_MAXLOC || KIND == PS_FD_MINLOC) && OPD == 3)) ? -1 : 0;
+    return ((KIND == PS_FD_DIFF2 && OPD == 4) || ((KIND == PS_FD_MAXLOC || KIND == PS_FD_MINLOC) && (OPD == 3 || OPD == 5)))
+               ? -1 : 0;
 }
 template <int KIND, int OPD>
 __host__ __device__ constexpr int fd_zhi() {
     return ((KIND == PS_FD_DIFF || KIND == PS_FD_DIFF2 || KIND == PS_FD_AV || KIND == PS_FD_HARM) && (OPD & 4)) ||
-                   ((KIND == PS_FD_MAXLOC || KIND == PS_FD_MINLOC) && OPD == 3)
+                   ((KIND == PS_FD_MAXLOC || KIND == PS_FD_MINLOC) && (OPD == 3 || OPD == 5))
                ? 1 : 0;
 }
 // Whether the macro reads the point (ox, oy) of some plane (offsets -1..1).
@@ -104,7 +109,7 @@ __host__ __device__ constexpr bool fd_reads_xy(int ox, int oy) {
     if (KIND == PS_FD_DIFF || KIND == PS_FD_AV || KIND == PS_FD_HARM)
         return ox >= 0 && oy >= 0 && (ox == 0 || (OPD & 1)) && (oy == 0 || (OPD & 2));
     if (KIND == PS_FD_DIFF2) return (ox == 0 || OPD == 1) && (oy == 0 || OPD == 2);
-    return ox == 0 || oy == 0;  // maxloc / minloc: the cross
+    return OPD == 5 ? oy == 0 : (ox == 0 || oy == 0);  // maxloc / minloc: the cross
 }
 
 // Each thread evaluates FD_ZB consecutive z indices, their loads issued together (with one value
@@ -187,8 +192,9 @@ constexpr int64_t kResidentThreads = 152 * 2048;
 
 template <typename T, int K, int O>
 static void fd_launch_one(const FdDesc& d, T* R, const T* A, cudaStream_t s) {
-    const dim3 blk(32, 8, 1);
-    const unsigned gx = (unsigned)((d.tmax[0] + 31) / 32), gy = (unsigned)((d.tmax[1] + 7) / 8);
+    // a 2-D macro arrives here as a 3-D one over (nx, 1, ny): rows of 128 threads sweep "z" (= y)
+    const dim3 blk = d.tmax[1] == 1 ? dim3(128, 1, 1) : dim3(32, 8, 1);
+    const unsigned gx = (unsigned)((d.tmax[0] + blk.x - 1) / blk.x), gy = (unsigned)((d.tmax[1] + blk.y - 1) / blk.y);
     if (d.ndims == 3) {  // every 3-D macro sweeps z; 1-D and 2-D ones keep fd_apply_kernel
         int64_t zl = 64;
         while (zl > 2 && d.tmax[0] * d.tmax[1] * ((d.tmax[2] + zl - 1) / zl) < kResidentThreads) zl /= 2;
@@ -218,8 +224,12 @@ static int launch_fd(const FdDesc& d, T* R, const T* A, cudaStream_t s) {
     case PS_FD_DIFF2: PS_FD_ONE_DIM(PS_FD_DIFF2) break;
     case PS_FD_AV: PS_FD_ANY_DIMS(PS_FD_AV) break;
     case PS_FD_HARM: PS_FD_ANY_DIMS(PS_FD_HARM) break;
-    case PS_FD_MAXLOC: PS_FD_NDIMS(PS_FD_MAXLOC) break;
-    case PS_FD_MINLOC: PS_FD_NDIMS(PS_FD_MINLOC) break;
+    case PS_FD_MAXLOC:
+        if (d.opdims == 5) { fd_launch_one<T, PS_FD_MAXLOC, 5>(d, R, A, s); return PS_OK; }
+        PS_FD_NDIMS(PS_FD_MAXLOC) break;
+    case PS_FD_MINLOC:
+        if (d.opdims == 5) { fd_launch_one<T, PS_FD_MINLOC, 5>(d, R, A, s); return PS_OK; }
+        PS_FD_NDIMS(PS_FD_MINLOC) break;
     }
 #undef PS_FD_CASE
 #undef PS_FD_ONE_DIM
@@ -848,6 +858,18 @@ int ps_fd_apply(ps_fd_op op, int32_t lhs_inn, ps_array R, ps_array A, void* stre
             return fail(PS_ERR_SHAPE, "ps_fd_apply: the operator reads outside A along dimension %d", k);
     }
     if (d.tmax[0] <= 0 || d.tmax[1] <= 0 || d.tmax[2] <= 0) return PS_OK;
+    if (op.ndims == 2) {
+        // (nx, ny) is laid out as (nx, 1, ny): the 2-D macro is the 3-D one with y as z (the same
+        // points in the same operation order; @maxloc / @minloc as OPD 5), so it runs as a sweep
+        // along y with a register window
+        auto yz = [](int m) { return (m & 1) | ((m & 2) << 1); };
+        d.ndims = 3;
+        d.opdims = yz(d.opdims);
+        d.inn = yz(d.inn);
+        d.lhs_inn = yz(d.lhs_inn);
+        d.nR[2] = d.nR[1], d.nA[2] = d.nA[1], d.tmax[2] = d.tmax[1];
+        d.nR[1] = d.nA[1] = d.tmax[1] = 1;
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (R.dtype == PS_F64)
         PS_TRY(launch_fd<double>(d, static_cast<double*>(R.ptr), static_cast<const double*>(A.ptr), s));

@@ -49,6 +49,25 @@ def test_fd_z_sweeps_match_the_oracle(ps, oracle, dtn):
     assert done == 2 * len(MACROS[3])
 
 
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_fd_2d_y_sweeps_match_the_oracle(ps, oracle, dtn):
+    """2-D macros run as the 3-D sweep over (nx, 1, ny) (y as z): every 2-D macro at 700 x 600 is
+    bit-identical to the oracle, `@all` and `@inn`."""
+    from ps_gb300.fd import LHS, MACROS
+
+    n = (700, 600)
+    A = np.asfortranarray(np.random.default_rng(13).standard_normal(n).astype(DT[dtn]) + 3.0)
+    dA = _dev(ps, A)
+    for op, (kind, opd, inn) in sorted(MACROS[2].items()):
+        for lhs in ("all", "inn"):
+            shape = tuple(n[k] - ((inn >> k) & 1) - ((opd >> k) & 1) for k in range(2))
+            exp = np.asfortranarray(np.full(shape, -7.0, dtype=DT[dtn]))
+            oracle.fd_apply(kind, opd, inn, 2, LHS[2][lhs], exp, A)
+            R = _dev(ps, np.full(shape, -7.0, dtype=DT[dtn]))
+            ps.parallel(ps.fd_kernel(f"@{lhs}(R) = @{op}(A)", 2), R, dA)
+            assert np.array_equal(ps.to_host(R), exp), (op, lhs)
+
+
 def test_fd_split_fp64_close_to_the_oracle(ps, oracle):
     """fp64="split" for FD operator kernels (FP64 arrays, arithmetic on FP32 pairs, the definition
     run-time compiled): every 3-D macro within 1e-12 of the IEEE oracle (relative max-norm); FP32
