@@ -298,15 +298,7 @@ def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner,
     cur = torch.cuda.current_stream()
     for s in (sb, si):
         s.wait_stream(cur)
-    # x and y slabs widened to whole thread blocks (32 x 8): a 16-wide x slab would leave half of
-    # every warp idle, and an inner box starting mid-block would cost one more block column; the
-    # boundary boxes then hold a superset of the requested boundary (all computed before `comm`)
-    lw, hw = list(bw), list(bw)
-    for d, blk in ((0, 32), (1, 8)):
-        a = -(-bw[d] // blk) * blk  # lower slab [0, a)
-        b = ms[d] - (ms[d] - bw[d]) // blk * blk  # upper slab [ms - b, ms) from a block edge
-        if bw[d] > 0 and ms[d] > a + b:
-            lw[d], hw[d] = a, b
+    lw, hw = widened_widths(bw, ms)
     for lo, hi in get_ranges_outer(lw, ms, hw):
         kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], sb, False, memopt=memopt, fp64=fp64)
     for lo, hi in get_ranges_inner(lw, ms, hw):
@@ -320,6 +312,20 @@ def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner,
         cur.wait_stream(sb)
         cur.wait_stream(si)
     kernel.check(si)
+
+
+def widened_widths(bw, ms, blocks=(32, 8)):
+    """Lower and upper boundary widths with the x and y slabs widened to whole thread blocks
+    (default 32 x 8) where the grid allows it: a 16-wide x slab would leave half of every warp idle,
+    and an inner box starting mid-block would cost one more block column. The boundary boxes then
+    hold a superset of the requested boundary (all computed before `comm`)."""
+    lw, hw = list(bw), list(bw)
+    for d, blk in enumerate(blocks):
+        a = -(-bw[d] // blk) * blk  # lower slab [0, a)
+        b = ms[d] - (ms[d] - bw[d]) // blk * blk  # upper slab [ms - b, ms) from a block edge
+        if bw[d] > 0 and ms[d] > a + b:
+            lw[d], hw[d] = a, b
+    return lw, hw
 
 
 def get_ranges_outer(boundary_width, maxsize, upper_width=None):

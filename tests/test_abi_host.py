@@ -165,3 +165,23 @@ def test_column_major_check():
     assert is_column_major((4, 5, 6), (1, 4, 20))
     assert not is_column_major((4, 5, 6), (30, 6, 1))
     assert is_column_major((1, 5, 6), (99, 1, 5))
+
+
+def test_hide_communication_widened_slabs():
+    """Slabs widened to whole thread blocks: at least the requested widths, the inner box starting
+    and ending on block edges, the boxes still tiling the grid; left alone where the grid is too
+    small."""
+    from ps_gb300.kernels import get_ranges_inner, get_ranges_outer, widened_widths
+
+    for ms, bw in [((512, 512, 512), (16, 2, 2)), ((100, 40, 36), (16, 4, 2)), ((64, 40, 36), (16, 4, 2)),
+                   ((300, 131, 7), (3, 1, 1))]:
+        lw, hw = widened_widths(bw, ms)
+        assert all(lw[d] >= bw[d] and hw[d] >= bw[d] for d in range(3)) and lw[2] == hw[2] == bw[2]
+        for d, blk in ((0, 32), (1, 8)):
+            if (lw[d], hw[d]) != (bw[d], bw[d]):
+                assert lw[d] % blk == 0 and (ms[d] - hw[d]) % blk == 0 and ms[d] > lw[d] + hw[d]
+        cover = np.zeros(ms, dtype=np.int8)
+        for lo, hi in get_ranges_outer(lw, ms, hw) + get_ranges_inner(lw, ms, hw):
+            cover[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] += 1
+        assert np.all(cover == 1)
+    assert widened_widths((16, 4, 2), (64, 40, 36))[0][0] == 16  # 64 cells: no room to widen x
