@@ -373,3 +373,23 @@ def test_translator_language_additions(jit):
     body = jit.generate(jit.parse(K.INT_EXPR2D), 2, "float").split("ps_jit_entry")[1]
     assert "- 1LL" in body and "(R)1.0" not in body
     assert jit.parse(K.SPLAT_COPY).splat == "I"
+
+
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+def test_interpreter_and_c_oracle_agree(jr, oracle, dtn):
+    """The two independent CPU restatements -- the C oracle's FD kernels and the interpreter of kernel
+    definitions -- agree bit for bit on random fields for every 2-D and 3-D macro, `@all` and `@inn`
+    left-hand sides (the golden fixtures pin each at one size; this crosses them at others)."""
+    from ps_gb300.fd import LHS, MACROS
+
+    dt = DT[dtn]
+    for nd, n in ((3, (9, 8, 7)), (2, (11, 6))):
+        A = np.asfortranarray(np.random.default_rng(nd).standard_normal(n).astype(dt) + 2.0)
+        for op, (kind, opd, inn) in sorted(MACROS[nd].items()):
+            for lhs in ("all", "inn"):
+                shape = tuple(n[k] - ((inn >> k) & 1) - ((opd >> k) & 1) for k in range(nd))
+                c = np.asfortranarray(np.full(shape, -7.0, dtype=dt))
+                oracle.fd_apply(kind, opd, inn, nd, LHS[nd][lhs], c, A)
+                p = np.asfortranarray(np.full(shape, -7.0, dtype=dt))
+                jr.run(f"@parallel function f!(R, A)\n    @{lhs}(R) = @{op}(A)\n    return\nend", [p, A], ndims=nd)
+                assert np.array_equal(c, p, equal_nan=True), (nd, op, lhs)
