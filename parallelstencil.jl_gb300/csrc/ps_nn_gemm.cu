@@ -2,17 +2,20 @@
 // start's convolutions: D[M][N] = A[M][K] * B[N][K]^T, A and B bf16 row-major (K contiguous), FP32
 // accumulation in tensor memory (TMEM).
 //
-// One CTA of 128 threads computes a 128 x BN tile of D (BN = 128, or 256 when N > 128):
-//   - warp 0 (one thread) streams 128 x 64 / BN x 64 tiles of A and B into a 6-stage (BN = 256: 4) ring with
-//     TMA (cp.async.bulk.tensor.2d, 128-byte swizzle, zero fill past the matrix edges, so M, N and
-//     K need no padding beyond K % 8 == 0), refilling a stage as soon as its "empty" mbarrier says
-//     the MMAs that read it are done;
+// Persistent: one CTA of 192 threads per SM walks the 128 x BN output tiles of D (BN = 128, or 256
+// when N > 128; K splits as further tiles), in bands of 16 m blocks for L2 reuse:
+//   - warp 0 (one thread) streams 128 x 64 / BN x 64 tiles of A and B into a 6-stage (BN = 256: 4)
+//     ring with TMA (cp.async.bulk.tensor.2d, 128-byte swizzle, zero fill past the matrix edges, so
+//     M, N and K need no padding beyond K % 8 == 0), across tile boundaries, refilling a stage as
+//     soon as its "empty" mbarrier says the MMAs that read it are done;
 //   - warp 1 (one thread) waits for each stage's "full" mbarrier and issues tcgen05.mma
-//     (kind::f16, M = 128, N = BN, K = 16) on it; tcgen05.commit arrives on the stage's "empty"
-//     mbarrier when those MMAs have read it;
-//   - all four warps then read the accumulator with tcgen05.ld (warp w owns TMEM lanes / tile
-//     rows 32w..32w+31) and apply the epilogue: + bias[n], ReLU, store as bf16 or FP32, or add
-//     into FP32 output with atomics (split-K over blockIdx.z).
+//     (kind::f16, M = 128, N = BN, K = 16) into one of two TMEM accumulators; tcgen05.commit
+//     arrives on the stage's "empty" mbarrier when those MMAs have read it, and on the
+//     accumulator's "full" mbarrier when the tile is done;
+//   - warps 2-5 read the other accumulator with tcgen05.ld (warp w owns TMEM lanes / tile rows
+//     32 (w % 4) .. + 31) and apply the epilogue -- + bias[n], ReLU, store as bf16 or FP32 (vector
+//     stores where aligned), or add into FP32 output with atomics (split-K) -- while the next
+//     tile's MMAs run, then release the accumulator.
 // Every mbarrier wait is bounded: on a timeout the kernel raises DEV_ERR_TMA_TIMEOUT, drains
 // the copies it issued, frees its TMEM columns and returns.
 #include <cuda_bf16.h>
