@@ -1,10 +1,14 @@
 // ps_stencil3d.cu -- FD operators, memcopy3D and diffusion3D kernels of libps_b200.so.
 //
 // Kernels:
-//   fd_apply_kernel      one-statement `@parallel` kernels of every FiniteDifferences macro
-//                        (src/FiniteDifferences.jl:54-61, 160-185, 328-394)
+//   fd_sweep_kernel      one-statement `@parallel` kernels of every 3-D and 2-D FiniteDifferences
+//                        macro (src/FiniteDifferences.jl:160-185, 328-394): z sweeps with a register
+//                        window of the planes the macro reads (2-D: the same over (nx, 1, ny))
+//   fd_apply_kernel      the same for 1-D macros (src/FiniteDifferences.jl:54-61), FD_ZB points
+//                        per thread
 //   memcopy_flat/_box    `@all(T2) = @all(T) + @all(Ci)` (examples/memcopy3D.jl:10-13)
-//   diff3d_plain         diffusion step, one thread per cell (`memopt=false`)
+//   diff3d_plain         diffusion step, one thread per cell (`memopt=false`, and boxes under half
+//                        a sweep tile, e.g. @hide_communication's thin boundary slabs)
 //   diff3d_zsweep_tma    diffusion step, z-sweep with TMA-staged x-y planes in a shared-memory
 //                        ring and register-rotated z neighbours (`memopt=true`; the reference's
 //                        memopt codegen is src/memopt.jl:190-573)
