@@ -24,10 +24,16 @@ and generates CUDA C with the rules the reference applies when it parses such a 
   powers, ``Bool * x`` keeps Julia's signed zero, no FMA contraction (``--fmad=false``).
 
 ``@parallel_indices (ix, iy[, iz]) function f!(...)`` bodies use explicit 1-based indexing,
-``size(A, d)``, comparisons and ``if (...) ... end``; the index names map to the grid dimensions.
+``size(A, d)``, comparisons, ``if``/``elseif``/``else``, ``for``/``while`` loops, compound
+assignments and one-line local functions; the index names (or an index tuple ``(I...)`` used as
+``A[I...]``) map to the grid dimensions; Int subexpressions stay Int until a real value is needed.
+The kernel language (``@threadIdx`` ... ``@sharedMem``, ``@sync_threads``, shuffles, votes) is
+translated for ``nblocks`` / ``nthreads`` / ``shmem`` launches.
 
-The CUDA C is compiled by the library (``ps_jit_compile``, NVRTC for sm_103a) and cached per
-source and number type.
+memopt (the default for 2-D and 3-D ``@parallel`` kernels without kernel-language calls) sweeps
+the last dimension with read-only neighbours carried in registers; ``fp64="split"`` evaluates FP64
+kernels on FP32 pairs. The CUDA C is compiled by the library (``ps_jit_compile``, NVRTC for
+sm_103a) and cached per source, rank, number type, sweep and arithmetic.
 """
 from __future__ import annotations
 
