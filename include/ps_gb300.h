@@ -316,7 +316,9 @@ int ps_stokes2d_iterate(const ps_stokes2d_fields* f, const ps_stokes2d_params* p
  * ((nx+1)*ny + nx*(ny+1) + nx*ny) * sizeof(T), each term rounded up to 256 bytes, must not exceed
  * 16 MiB (about 830 x 830 cells in FP64); larger grids return PS_ERR_SHAPE. The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress, with that device current),
- * so make that first call before any stream capture. All calls share the one array and it keeps
+ * so make that first call before any stream capture. The address is cached until ps_finalize,
+ * which forgets it: a caller that resets the device (cudaDeviceReset) calls ps_finalize first, and
+ * the next call looks the address up again. All calls share the one array and it keeps
  * the last call's contents (every element a call reads is written by that call first): calls that
  * overlap on the GPU (concurrent streams, several host threads) race. Allocates nothing; results
  * are bit-identical to ps_stokes2d_iterate. Synchronises. */

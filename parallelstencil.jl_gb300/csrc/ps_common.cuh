@@ -44,9 +44,12 @@ struct DeviceState {
 int current_state(DeviceState** st);
 // Frees library-owned solver scratch (ps_finalize).
 void stokes2d_free_scratch();
+void stokes2d_static_forget();  // drop the cached device addresses of the static scratch array
 void diffusion_free_scratch();
 void adjoint_free_scratch();
 
+// Copies `bytes` (<= 256 through pinned staging) from device memory on stream s and synchronises s.
+int read_device_words(void* dst, const void* src, size_t bytes, cudaStream_t s);
 // Reads (and clears) the device error word after a synchronisation.
 int check_device_error(DeviceState* st, cudaStream_t s);
 
@@ -142,6 +145,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this thread's generic-proxy shared-memory writes before later async-proxy (TMA) accesses
+// of the same bytes (a staged slot rewritten in place and later refilled by a TMA load).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)

@@ -46,10 +46,39 @@ int current_state(DeviceState** st) {
     return PS_OK;
 }
 
+// A small pinned staging buffer per host thread for reading device flags and norms: a copy into
+// pageable memory goes through the driver's own staging and can queue behind large copies of other
+// streams. Freed when the thread exits.
+namespace {
+struct PinnedWords {
+    void* p = nullptr;
+    bool tried = false;
+    ~PinnedWords() {
+        if (p) cudaFreeHost(p);
+    }
+};
+thread_local PinnedWords t_pinned;
+constexpr size_t kPinnedWordBytes = 256;
+}  // namespace
+
+int read_device_words(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (!t_pinned.tried) {
+        t_pinned.tried = true;
+        if (cudaMallocHost(&t_pinned.p, kPinnedWordBytes) != cudaSuccess) {
+            cudaGetLastError();
+            t_pinned.p = nullptr;
+        }
+    }
+    void* stage = (t_pinned.p && bytes <= kPinnedWordBytes) ? t_pinned.p : dst;
+    PS_CUDA_TRY(cudaMemcpyAsync(stage, src, bytes, cudaMemcpyDeviceToHost, s));
+    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (stage != dst) memcpy(dst, stage, bytes);
+    return PS_OK;
+}
+
 int check_device_error(DeviceState* st, cudaStream_t s) {
     int h = 0;
-    PS_CUDA_TRY(cudaMemcpyAsync(&h, st->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    PS_CUDA_TRY(cudaStreamSynchronize(s));
+    PS_TRY(read_device_words(&h, st->d_err, sizeof(int), s));
     if (h != DEV_ERR_NONE) {
         int zero = 0;
         PS_CUDA_TRY(cudaMemcpyAsync(st->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
@@ -222,6 +251,7 @@ int ps_finalize(void) {
     stokes2d_free_scratch();
     diffusion_free_scratch();
     adjoint_free_scratch();
+    stokes2d_static_forget();
     for (int d = 0; d < kMaxDevices; d++) {
         DeviceState& st = g_dev[d];
         if (!st.ready) continue;

@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
                 }
             }
         }
+        if constexpr (NCONV > 0) fence_proxy_async_smem();  // the slot is refilled by TMA after a later barrier
     };
     auto ld2 = [&](const double* plane, int off) {
         float2 v = *reinterpret_cast<const float2*>(plane + off);
@@ -395,7 +396,7 @@ int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, co
 
 // Run header in library scratch (written by the setup kernels on the device).
 struct GridRun {
-    unsigned long long maxT, maxL;  // bit patterns of max|T|, max|lam| (non-negative doubles order as integers)
+    unsigned long long maxT, maxL;  // max|T|, max|lam| as (largest high word << 32) | (any low word != 0)
     int shT, shL;                   // grid units = value * 2^sh
     int bad;                        // a value left the grid range: the run is redone with split pairs
     int pad;
@@ -417,6 +418,38 @@ __device__ __forceinline__ dd gface(dd Ta, dd Tb, dd la, dd lb) {
     }
 }
 
+// A double as a grid pair (h, l): v * 2^sh = h + l, h integer-valued, |l| <= 1/2. Non-finite
+// values set `bad`.
+__device__ __forceinline__ float2 to_grid(double v, int sh, bool& bad) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0x7FF) {
+        bad = true;
+        return make_float2(0.f, 0.f);
+    }
+    if (e == 0 || e + sh <= 0) return make_float2(0.f, 0.f);  // below 2^-1022 grid units
+    const double x = __longlong_as_double(b + ((long long)sh << 52));  // v * 2^sh, |x| < 2^23
+    bool big = false;
+    const dd d = dd_split(x, big);
+    const float h = rintf(d.h);
+    return make_float2(h, (d.h - h) + d.l);
+}
+
+// The run's coefficient scale g as a float pair (Ci pairs are Ci * g).
+__device__ __forceinline__ dd g_pair(double g) {
+    dd gd;
+    gd.h = (float)g;
+    gd.l = (float)(g - (double)gd.h);
+    return gd;
+}
+
+// Ci as the value pair of Ci * g; magnitudes outside FP32's range set `big`.
+__device__ __forceinline__ dd ci_pair(double c, dd gd, bool& big) {
+    const dd r = dd_norm(dd_mul(dd_split(c, big), gd));
+    big |= !(fabsf(r.h) < 0x1p127f);
+    return r;
+}
+
 // Exact double of the grid value (h + l) * 2^-sh (h, l floats; values below 2^-1022 -> 0).
 __device__ __forceinline__ double grid_to_f64(double y, int sh) {
     const long long b = __double_as_longlong(y);
@@ -427,12 +460,23 @@ __device__ __forceinline__ double grid_to_f64(double y, int sh) {
 // One step on grid pairs: T, lam as (h, l) grid pairs, Ci as value pairs of Ci * G * u_lam; T2 as
 // grid pairs, or (OUT64, the last step of a run) as IEEE doubles. Every launch returns at once when
 // an earlier kernel of the run flagged a value outside the grid (the run is then redone).
-template <bool LAM, bool ISO, int TY, int S, int MINB, bool OUT64>
+//
+// IN64 (the first step of a run of two or more steps): T, lam and Ci are the caller's FP64 arrays.
+// Each staged plane of T and lam is converted to grid pairs in place in shared memory (own cells by
+// their thread, the x-y halo by assigned threads), and the step also writes its own cells' lam grid
+// pairs and Ci value pairs to Lout / Cout for the later steps, so the run never converts T, lam or
+// Ci in separate passes. The conversions are the setup kernels' functions, so the run's results do
+// not depend on which step converted a value.
+template <bool LAM, bool ISO, int TY, int S, int MINB, bool OUT64, bool IN64>
 __global__ void __launch_bounds__(32 * TY, MINB)
     diff3d_grid_tma(const __grid_constant__ CUtensorMap mT, const __grid_constant__ CUtensorMap mL,
                     const __grid_constant__ CUtensorMap mC, void* __restrict__ T2v, SplitParams p, int64_t nx,
-                    int64_t ny, Box cb, int L, int* __restrict__ err, GridRun* __restrict__ run) {
+                    int64_t ny, Box cb, int L, int* __restrict__ err, GridRun* __restrict__ run,
+                    float4* __restrict__ Lout, float4* __restrict__ Cout) {
+    static_assert(!(IN64 && OUT64), "a one-step run converts its input first");
     using C = SplitCfg<LAM, TY, S>;
+    constexpr int NHALO = IN64 ? C::HALO * (LAM ? 2 : 1) : 0;
+    constexpr int HPT = NHALO > 0 ? (NHALO + 32 * TY - 1) / (32 * TY) : 1;
     if (*reinterpret_cast<volatile int*>(&run->bad)) return;
     const int sh = run->shT;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -472,6 +516,7 @@ __global__ void __launch_bounds__(32 * TY, MINB)
     const bool row_in = gy >= cb.lo[1] && gy < cb.hi[1];
     const bool in0 = row_in && gx >= cb.lo[0] && gx < cb.hi[0];
     const bool in1 = row_in && gx + 1 >= cb.lo[0] && gx + 1 < cb.hi[0];
+    const bool in_array = gx < nx && gy < ny;  // gx even, nx even: the pair (gx, gx+1) is in the array
     auto ld1 = [](const unsigned char* b, int off) {
         const float2 v = reinterpret_cast<const float2*>(b)[off];
         return dd{v.x, v.y};
@@ -482,17 +527,70 @@ __global__ void __launch_bounds__(32 * TY, MINB)
         v[1] = dd{t.z, t.w};
     };
 
+    // IN64: this thread's halo values (byte offsets inside a stage; -1 = none): columns 1 and PW-2
+    // of every row, then rows 0 and PH-1 of the interior columns; T first, then lam
+    int hoff[HPT];
+    int shL = 0;
+    dd gd{0.f, 0.f};
+    if constexpr (IN64) {
+        shL = run->shL;
+        gd = g_pair(run->g);
+#pragma unroll
+        for (int r = 0; r < HPT; r++) {
+            const int h = tid + r * 32 * TY;
+            const int a = h % C::HALO;
+            const int idx = a < 2 * C::PH ? (a % C::PH) * C::PW + (a < C::PH ? 1 : C::PW - 2)
+                                          : ((a - 2 * C::PH) < SP_TX ? 0 : (C::PH - 1)) * C::PW + 2 +
+                                                ((a - 2 * C::PH) % SP_TX);
+            hoff[r] = h < NHALO ? (h < C::HALO ? 0 : C::PLANE) + idx * 8 : -1;
+        }
+    }
     bool bad = false, timed_out = false;
+    // IN64: converts plane q of T (and lam) in place: own cells (returned) and this thread's halo
+    auto convert = [&](int q, dd* Tn, dd* ln) {
+        unsigned char* b = slot(q);
+        double* tp = reinterpret_cast<double*>(b);
+        const double2 rt = *reinterpret_cast<const double2*>(tp + own);
+        const float2 t0 = to_grid(rt.x, sh, bad), t1 = to_grid(rt.y, sh, bad);
+        *reinterpret_cast<float4*>(tp + own) = make_float4(t0.x, t0.y, t1.x, t1.y);
+        Tn[0] = dd{t0.x, t0.y};
+        Tn[1] = dd{t1.x, t1.y};
+        if constexpr (LAM) {
+            double* lp = reinterpret_cast<double*>(b + C::PLANE);
+            const double2 rl = *reinterpret_cast<const double2*>(lp + own);
+            const float2 l0 = to_grid(rl.x, shL, bad), l1 = to_grid(rl.y, shL, bad);
+            *reinterpret_cast<float4*>(lp + own) = make_float4(l0.x, l0.y, l1.x, l1.y);
+            ln[0] = dd{l0.x, l0.y};
+            ln[1] = dd{l1.x, l1.y};
+        }
+#pragma unroll
+        for (int r = 0; r < HPT; r++) {
+            if (hoff[r] >= 0) {
+                double* v = reinterpret_cast<double*>(b + hoff[r]);
+                *reinterpret_cast<float2*>(v) = to_grid(*v, hoff[r] >= C::PLANE ? shL : sh, bad);
+            }
+        }
+        fence_proxy_async_smem();  // the slot is refilled by TMA after a later barrier
+    };
+
     dd Tc[2], lc[2], Tz[2], lz[2], Fzm[2];
     timed_out |= !mbar_wait_bounded(&bar[0], 0);
     timed_out |= !mbar_wait_bounded(&bar[1], 0);
     {
         dd T0[2], l0[2];
-        ld2(slot(0), own, T0);
-        ld2(slot(1), own, Tc);
-        if constexpr (LAM) {
-            ld2(slot(0) + C::PLANE, own, l0);
-            ld2(slot(1) + C::PLANE, own, lc);
+        if constexpr (IN64) {
+            if (!timed_out) {
+                convert(0, T0, l0);
+                convert(1, Tc, lc);
+            }
+            __syncthreads();  // plane 1's halo is read by the neighbours in the first z step
+        } else {
+            ld2(slot(0), own, T0);
+            ld2(slot(1), own, Tc);
+            if constexpr (LAM) {
+                ld2(slot(0) + C::PLANE, own, l0);
+                ld2(slot(1) + C::PLANE, own, lc);
+            }
         }
 #pragma unroll
         for (int j = 0; j < 2; j++) Fzm[j] = gface<LAM>(T0[j], Tc[j], l0[j], lc[j]);
@@ -502,13 +600,31 @@ __global__ void __launch_bounds__(32 * TY, MINB)
         const int q = k + 2;
         timed_out |= !mbar_wait_bounded(&bar[q % S], (q / S) & 1);
         const unsigned char* bz = slot(q);
-        ld2(bz, own, Tz);
-        if constexpr (LAM) ld2(bz + C::PLANE, own, lz);
+        if constexpr (IN64) {
+            // plane q is read by the other threads only in the next z step, after barrier B below
+            if (!timed_out) convert(q, Tz, lz);
+        } else {
+            ld2(bz, own, Tz);
+            if constexpr (LAM) ld2(bz + C::PLANE, own, lz);
+        }
         float2* faceY = faceY0 + (k & 1) * (TY + 1) * SP_TX;
         const unsigned char* tp = slot(k + 1);
         const unsigned char* lp = tp + C::PLANE;
+        const int64_t gz = Z0 + k;
+        const int64_t o = gx + nx * (gy + ny * gz);
         dd Fx[3], Fym[2], Fzp[2], ci[2];
-        ld2(tp + C::PLANE * (LAM ? 2 : 1), ly * SP_TX + 2 * lx, ci);
+        if constexpr (IN64) {
+            const double2 rc = *reinterpret_cast<const double2*>(
+                reinterpret_cast<const double*>(tp + C::PLANE * (LAM ? 2 : 1)) + ly * SP_TX + 2 * lx);
+            ci[0] = ci_pair(rc.x, gd, bad);
+            ci[1] = ci_pair(rc.y, gd, bad);
+            if (in_array) {  // the later steps' lam and Ci pairs of this thread's cells
+                Cout[o / 2] = make_float4(ci[0].h, ci[0].l, ci[1].h, ci[1].l);
+                if constexpr (LAM) Lout[o / 2] = make_float4(lc[0].h, lc[0].l, lc[1].h, lc[1].l);
+            }
+        } else {
+            ld2(tp + C::PLANE * (LAM ? 2 : 1), ly * SP_TX + 2 * lx, ci);
+        }
         {
             const dd Txm = ld1(tp, own - 1), Txp = ld1(tp, own + 2);
             dd lxm{0.f, 0.f}, lxp{0.f, 0.f};
@@ -538,7 +654,7 @@ __global__ void __launch_bounds__(32 * TY, MINB)
         }
 #pragma unroll
         for (int j = 0; j < 2; j++) Fzp[j] = gface<LAM>(Tc[j], Tz[j], lc[j], lz[j]);
-        // y faces published; planes <= k+1 are no longer read
+        // B: y faces published; planes <= k+1 are no longer read
         if (__syncthreads_or(timed_out)) {
             if (tid == 0) {
                 atomicOr(err, DEV_ERR_TMA_TIMEOUT);
@@ -586,8 +702,6 @@ __global__ void __launch_bounds__(32 * TY, MINB)
                 out[j] = make_float2(h2, l2 - q1);
             }
         }
-        const int64_t gz = Z0 + k;
-        const int64_t o = gx + nx * (gy + ny * gz);
         if constexpr (OUT64) {
             double* dst = static_cast<double*>(T2v) + o;
             if (in0 && in1)
@@ -615,11 +729,15 @@ __global__ void __launch_bounds__(32 * TY, MINB)
     if (__syncthreads_or(bad) && tid == 0) atomicOr(&run->bad, 1);
 }
 
-// Boundary cells (the six faces) of a grid state copied from a to b: b's interior is written by
-// the first step, its boundary is read from the second step on.
-__global__ void grid_faces_kernel(const float2* __restrict__ a, float2* __restrict__ b, int64_t nx, int64_t ny,
-                                  int64_t nz, const GridRun* r) {
+// Boundary cells (the six faces) of T converted to grid pairs into both run states a and b, and of
+// lam (if given) into the lam pairs: the first step of a run (IN64) writes the inner cells of b, of
+// lam's pairs and of Ci's pairs, so these faces are the rest of what the later steps read.
+__global__ void grid_faces64_kernel(const double* __restrict__ T, float2* __restrict__ a, float2* __restrict__ b,
+                                    const double* __restrict__ lam, float2* __restrict__ lg, int64_t nx, int64_t ny,
+                                    int64_t nz, GridRun* r) {
     if (r->bad) return;
+    const int shT = r->shT, shL = r->shL;
+    bool bad = false;
     const int f = blockIdx.y;  // 0,1: z faces; 2,3: y faces; 4,5: x faces
     const int64_t n0 = f < 4 ? nx : ny, n1 = f < 2 ? ny : nz;
     const int64_t fixed = (f & 1) ? (f < 2 ? nz : f < 4 ? ny : nx) - 1 : 0;
@@ -627,30 +745,66 @@ __global__ void grid_faces_kernel(const float2* __restrict__ a, float2* __restri
         const int64_t u = i % n0, v = i / n0;
         const int64_t ix = f < 4 ? u : fixed, iy = f < 2 ? v : f < 4 ? fixed : u, iz = f < 2 ? fixed : v;
         const int64_t o = ix + nx * (iy + ny * iz);
-        b[o] = a[o];
+        const float2 t = to_grid(T[o], shT, bad);
+        a[o] = t;
+        b[o] = t;
+        if (lam) lg[o] = to_grid(lam[o], shL, bad);
     }
+    if (bad) atomicOr(&r->bad, 1);
 }
 
 // The setup kernels below run on TMA-eligible arrays (nx even), so they work on pairs of values
 // (16-byte accesses); n2 = numel / 2.
 
-// max |a[i]| as a bit pattern (atomicMax over warps)
-__global__ void absmax_bits_kernel(const double2* __restrict__ a, int64_t n2, unsigned long long* out) {
-    unsigned long long m = 0;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += stride) {
-        const double2 v = __ldcs(a + i);
-        const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
-        const unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
-        m = b0 > m ? b0 : m;
-        m = b1 > m ? b1 : m;
+// max |a[i]| reduced to what the grid needs: the largest high word (sign cleared: it carries the
+// exponent) and whether any low word is nonzero, composed as (max_hi << 32) | any_lo. The result
+// has the exponent of max |a[i]| and is zero exactly when every a[i] is zero.
+struct AbsmaxBits {
+    unsigned hi = 0, lo = 0;
+    __device__ __forceinline__ void add(double2 v) {
+        hi = max(hi, max((unsigned)__double2hiint(v.x) & 0x7FFFFFFFu, (unsigned)__double2hiint(v.y) & 0x7FFFFFFFu));
+        lo |= (unsigned)__double2loint(v.x) | (unsigned)__double2loint(v.y);
     }
+    __device__ __forceinline__ void publish(unsigned long long* out) {
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, m, o);
-        m = t > m ? t : m;
+        for (int o = 16; o; o >>= 1) {
+            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+            lo |= __shfl_xor_sync(0xFFFFFFFFu, lo, o);
+        }
+        const unsigned long long m = ((unsigned long long)hi << 32) | (lo ? 1ull : 0ull);
+        if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
     }
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+};
+
+// max |a[i]| and max |b[i]| (b may be NULL) in one pass over both arrays. A persistent grid (4 CTAs
+// of 256 threads per SM, all resident) walks the pairs with four 16-byte loads per array in flight
+// per thread.
+constexpr int kAbsmaxUnroll = 4;
+__global__ void __launch_bounds__(256, 4)
+    absmax2_bits_kernel(const double2* __restrict__ a, const double2* __restrict__ b, int64_t n2,
+                        unsigned long long* out_a, unsigned long long* out_b) {
+    AbsmaxBits ma, mb;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; i + (kAbsmaxUnroll - 1) * stride < n2; i += kAbsmaxUnroll * stride) {
+        double2 va[kAbsmaxUnroll], vb[kAbsmaxUnroll];
+#pragma unroll
+        for (int u = 0; u < kAbsmaxUnroll; u++) va[u] = __ldcs(a + i + u * stride);
+        if (b) {
+#pragma unroll
+            for (int u = 0; u < kAbsmaxUnroll; u++) vb[u] = __ldcs(b + i + u * stride);
+#pragma unroll
+            for (int u = 0; u < kAbsmaxUnroll; u++) mb.add(vb[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kAbsmaxUnroll; u++) ma.add(va[u]);
+    }
+    for (; i < n2; i += stride) {
+        ma.add(__ldcs(a + i));
+        if (b) mb.add(__ldcs(b + i));
+    }
+    ma.publish(out_a);
+    if (b) mb.publish(out_b);
 }
 
 // Grid exponent of a maximum: largest magnitude < 2^23 grid units. Maxima outside
@@ -678,21 +832,6 @@ __global__ void grid_setup_kernel(GridRun* r, double G, int has_lam) {
     r->g = g;
 }
 
-__device__ __forceinline__ float2 to_grid(double v, int sh, bool& bad) {
-    const long long b = __double_as_longlong(v);
-    const int e = (int)((b >> 52) & 0x7FF);
-    if (e == 0x7FF) {
-        bad = true;
-        return make_float2(0.f, 0.f);
-    }
-    if (e == 0 || e + sh <= 0) return make_float2(0.f, 0.f);  // below 2^-1022 grid units
-    const double x = __longlong_as_double(b + ((long long)sh << 52));  // v * 2^sh, |x| < 2^23
-    bool big = false;
-    const dd d = dd_split(x, big);
-    const float h = rintf(d.h);
-    return make_float2(h, (d.h - h) + d.l);
-}
-
 // T -> grid pairs (lam_grid = 0) or lam -> grid pairs (lam_grid = 1)
 __global__ void to_grid_kernel(const double2* __restrict__ in, float4* __restrict__ a, int64_t n2, GridRun* r,
                                int lam_grid) {
@@ -711,26 +850,26 @@ __global__ void to_grid_kernel(const double2* __restrict__ in, float4* __restric
 // Ci -> value pairs of Ci * g
 __global__ void ci_grid_kernel(const double2* __restrict__ in, float4* __restrict__ out, int64_t n2, GridRun* r) {
     if (r->bad) return;
-    const double g = r->g;
-    dd gd;
-    gd.h = (float)g;
-    gd.l = (float)(g - (double)gd.h);
+    const dd gd = g_pair(r->g);
     bool big = false;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += stride) {
         const double2 v = __ldcs(in + i);
-        const dd c0 = dd_norm(dd_mul(dd_split(v.x, big), gd)), c1 = dd_norm(dd_mul(dd_split(v.y, big), gd));
-        big |= !(fabsf(c0.h) < 0x1p127f) || !(fabsf(c1.h) < 0x1p127f);
+        const dd c0 = ci_pair(v.x, gd, big), c1 = ci_pair(v.y, gd, big);
         out[i] = make_float4(c0.h, c0.l, c1.h, c1.l);
     }
     if (big) atomicOr(&r->bad, 1);
 }
 
-template <bool LAM, bool ISO, bool OUT64>
+// One step of a grid run. IN64 (first step): Tin, Cs and Ls are the caller's FP64 T, Ci and lam,
+// and the step writes the lam / Ci pairs of its cells to Lout / Cout.
+template <bool LAM, bool ISO, bool OUT64, bool IN64>
 static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps_array* Ls, const ps_array& T2,
-                               const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, GridRun* run) {
+                               const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, GridRun* run,
+                               void* Lout, void* Cout) {
     constexpr int TY = 8, S = 4, MINB = 3;
     using C = SplitCfg<LAM, TY, S>;
+    auto kernel = diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64, IN64>;
     CUtensorMap mT, mL, mC;
     PS_TRY(encode_plane_map(&mT, Tin, C::PW, C::PH));
     if (LAM)
@@ -740,30 +879,38 @@ static int launch_grid_variant(const ps_array& Tin, const ps_array& Cs, const ps
     PS_TRY(encode_plane_map(&mC, Cs, SP_TX, TY));
     static bool attr = false;
     if (!attr) {
-        PS_CUDA_TRY(cudaFuncSetAttribute(diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+        PS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
         attr = true;
     }
     const int64_t x0 = cb.lo[0] & ~(int64_t)1;
     dim3 blk(32, TY, 1);
     const int64_t bx = (cb.hi[0] - x0 + SP_TX - 1) / SP_TX, by = (cb.hi[1] - cb.lo[1] + TY - 1) / TY;
     if (L <= 0) {
-        static const int occ = resident_ctas(diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64>, 32 * TY, C::SMEM);
+        static const int occ = resident_ctas(kernel, 32 * TY, C::SMEM);
         DeviceState* st = nullptr;
         PS_TRY(current_state(&st));
         L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
     }
     dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
-    diff3d_grid_tma<LAM, ISO, TY, S, MINB, OUT64><<<grd, blk, C::SMEM, s>>>(mT, mL, mC, T2.ptr, p, T2.n[0], T2.n[1],
-                                                                           cb, L, d_err, run);
+    kernel<<<grd, blk, C::SMEM, s>>>(mT, mL, mC, T2.ptr, p, T2.n[0], T2.n[1], cb, L, d_err, run,
+                                     static_cast<float4*>(Lout), static_cast<float4*>(Cout));
     return PS_OK;
 }
 
+enum GridStep { GRID_FIRST64 = 0, GRID_MIDDLE = 1, GRID_LAST64 = 2 };
+
 template <bool LAM, bool ISO>
-static int launch_grid_step(bool last, const ps_array& Tin, const ps_array& Cs, const ps_array* Ls, const ps_array& T2,
-                            const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err, GridRun* run) {
-    return last ? launch_grid_variant<LAM, ISO, true>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run)
-                : launch_grid_variant<LAM, ISO, false>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run);
+static int launch_grid_step(GridStep kind, const ps_array& Tin, const ps_array& Cs, const ps_array* Ls,
+                            const ps_array& T2, const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err,
+                            GridRun* run, void* Lout = nullptr, void* Cout = nullptr) {
+    switch (kind) {
+    case GRID_FIRST64:
+        return launch_grid_variant<LAM, ISO, false, true>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run, Lout, Cout);
+    case GRID_LAST64:
+        return launch_grid_variant<LAM, ISO, true, false>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run, nullptr, nullptr);
+    default:
+        return launch_grid_variant<LAM, ISO, false, false>(Tin, Cs, Ls, T2, p, cb, L, s, d_err, run, nullptr, nullptr);
+    }
 }
 
 // ---- multi-step runs -------------------------------------------------------------------
@@ -776,8 +923,14 @@ __global__ void split_pairs_kernel(const double* __restrict__ in, double* __rest
     if (big) atomicOr(err, DEV_ERR_RANGE);
 }
 
-__global__ void join_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n) {
+// Final state of a split-pair run back to doubles, inner cells only: the boundary cells of T keep
+// their initial values exactly (a split pair holds only 24 bits of magnitudes below 2^-80).
+__global__ void join_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t nx, int64_t ny,
+                                  int64_t nz) {
+    const int64_t n = nx * ny * nz;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t x = i % nx, y = (i / nx) % ny, z = i / (nx * ny);
+        if (x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1) continue;
         const double v = in[i];
         out[i] = f32_to_f64(__int_as_float(__double2loint(v))) + f32_to_f64(__int_as_float(__double2hiint(v)));
     }
@@ -857,36 +1010,54 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
         const int g = st->num_sms * 8;
         PS_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(GridRun), s));
         const int64_t n2 = n / 2;  // nx is even (TMA eligibility)
-        absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(T.ptr), n2, &r->maxT);
-        if (has_lam) absmax_bits_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(lam_arr.ptr), n2, &r->maxL);
+        absmax2_bits_kernel<<<st->num_sms * 4, 256, 0, s>>>(static_cast<const double2*>(T.ptr),
+                                              has_lam ? static_cast<const double2*>(lam_arr.ptr) : nullptr, n2,
+                                              &r->maxT, &r->maxL);
         grid_setup_kernel<<<1, 1, 0, s>>>(r, G, has_lam ? 1 : 0);
-        // T2's boundary values are T's (the documented precondition): Sb gets Sa's faces
-        to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(T.ptr), static_cast<float4*>(Sa.ptr), n2, r, 0);
-        grid_faces_kernel<<<dim3(st->num_sms, 6), 256, 0, s>>>(static_cast<const float2*>(Sa.ptr),
-                                                               static_cast<float2*>(Sb.ptr), T.n[0], T.n[1], T.n[2], r);
-        if (has_lam)
-            to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(lam_arr.ptr), static_cast<float4*>(Ls.ptr), n2,
-                                             r, 1);
-        ci_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(Ci.ptr), static_cast<float4*>(Cs.ptr), n2, r);
-        A = Sa;
-        B = Sb;
-        for (int64_t it = 0; it < nt; ++it) {
-            const bool last = it == nt - 1;  // the last step writes T as IEEE doubles
-            const ps_array& out = last ? T : B;
-            int rc;
+        auto step = [&](GridStep kind, const ps_array& Tin, const ps_array& Cin, const ps_array* Lin,
+                        const ps_array& out) {
+            const ps_array* lin = has_lam ? Lin : nullptr;
+            void* lout = has_lam ? Ls.ptr : nullptr;
             if (form == PS_DIFF_FLUX_LAM)
-                rc = iso ? launch_grid_step<true, true>(last, A, Cs, &Ls, out, p, cells, L, s, st->d_err, r)
-                         : launch_grid_step<true, false>(last, A, Cs, &Ls, out, p, cells, L, s, st->d_err, r);
-            else
-                rc = iso ? launch_grid_step<false, true>(last, A, Cs, nullptr, out, p, cells, L, s, st->d_err, r)
-                         : launch_grid_step<false, false>(last, A, Cs, nullptr, out, p, cells, L, s, st->d_err, r);
-            PS_TRY(rc);
+                return iso ? launch_grid_step<true, true>(kind, Tin, Cin, lin, out, p, cells, L, s, st->d_err, r, lout,
+                                                          Cs.ptr)
+                           : launch_grid_step<true, false>(kind, Tin, Cin, lin, out, p, cells, L, s, st->d_err, r,
+                                                           lout, Cs.ptr);
+            return iso ? launch_grid_step<false, true>(kind, Tin, Cin, nullptr, out, p, cells, L, s, st->d_err, r,
+                                                       nullptr, Cs.ptr)
+                       : launch_grid_step<false, false>(kind, Tin, Cin, nullptr, out, p, cells, L, s, st->d_err, r,
+                                                        nullptr, Cs.ptr);
+        };
+        if (nt >= 2) {
+            // the first step reads the caller's FP64 T, lam and Ci and converts them as it stages
+            // them (writing the lam / Ci pairs of its cells); the boundary faces are converted here
+            grid_faces64_kernel<<<dim3(st->num_sms, 6), 256, 0, s>>>(
+                static_cast<const double*>(T.ptr), static_cast<float2*>(Sa.ptr), static_cast<float2*>(Sb.ptr),
+                has_lam ? static_cast<const double*>(lam_arr.ptr) : nullptr, static_cast<float2*>(Ls.ptr), T.n[0],
+                T.n[1], T.n[2], r);
+            PS_TRY(step(GRID_FIRST64, T, Ci, &lam_arr, Sb));
+            A = Sb;
+            B = Sa;
+        } else {
+            // one step: convert first (the step writes T itself)
+            to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(T.ptr), static_cast<float4*>(Sa.ptr), n2, r,
+                                             0);
+            if (has_lam)
+                to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(lam_arr.ptr),
+                                                 static_cast<float4*>(Ls.ptr), n2, r, 1);
+            ci_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(Ci.ptr), static_cast<float4*>(Cs.ptr), n2,
+                                             r);
+            A = Sa;
+            B = Sb;
+        }
+        for (int64_t it = nt >= 2 ? 1 : 0; it < nt; ++it) {
+            const bool last = it == nt - 1;  // the last step writes T as IEEE doubles
+            PS_TRY(step(last ? GRID_LAST64 : GRID_MIDDLE, A, Cs, &Ls, last ? T : B));
             std::swap(A, B);
         }
         PS_CUDA_TRY(cudaGetLastError());
         int bad = 0;
-        PS_CUDA_TRY(cudaMemcpyAsync(&bad, &r->bad, sizeof(int), cudaMemcpyDeviceToHost, s));
-        PS_CUDA_TRY(cudaStreamSynchronize(s));
+        PS_TRY(read_device_words(&bad, &r->bad, sizeof(int), s));
         if (bad) {  // a value outside the grid's range: redo the run with value-relative split pairs
             ps_launch c2 = cfg ? *cfg : ps_launch{};
             c2.memopt = memopt;
@@ -930,7 +1101,8 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
             std::swap(A, B);
         }
         if (state) {
-            join_pairs_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(A.ptr), static_cast<double*>(T.ptr), n);
+            join_pairs_kernel<<<g, 256, 0, s>>>(static_cast<const double*>(A.ptr), static_cast<double*>(T.ptr), T.n[0],
+                                                T.n[1], T.n[2]);
             A = T;
         }
     }

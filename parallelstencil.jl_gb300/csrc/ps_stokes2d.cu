@@ -993,7 +993,9 @@ int ps_stokes2d_solve(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, 
 // The array is file-scope, kStaticScratchBytes (16 MiB) on every device that loads the library,
 // held until process exit. Host code must not pass the array's name to a kernel (on the host it
 // is only a stand-in symbol): its device address is looked up once per device with
-// cudaGetSymbolAddress, on the first call on that device, with that device current.
+// cudaGetSymbolAddress, on the first call on that device, with that device current, and cached.
+// The cache belongs to the device's current context: ps_finalize clears it, so that after a
+// context is torn down (ps_finalize, then cudaDeviceReset) the next call looks the address up again.
 // =======================================================================================
 namespace ps {
 
@@ -1018,6 +1020,11 @@ static int static_scratch(void** out) {
     }
     *out = g_static_scratch_addr[dev];
     return PS_OK;
+}
+
+void stokes2d_static_forget() {
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    for (int d = 0; d < kStaticMaxDevices; d++) g_static_scratch_addr[d] = nullptr;
 }
 
 static size_t round256(size_t b) { return (b + 255) / 256 * 256; }

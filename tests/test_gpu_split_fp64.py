@@ -23,6 +23,11 @@ def relerr(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
+def faces_untouched(got, T0):
+    """The six boundary faces hold the initial values exactly (the steps write inner cells only)."""
+    return all(np.array_equal(np.take(got, i, axis=d), np.take(T0, i, axis=d)) for d in range(3) for i in (0, -1))
+
+
 @pytest.mark.parametrize("n", [(64, 40, 36), (130, 66, 70), (256, 24, 9), (66, 66, 66)])
 @pytest.mark.parametrize("form", [0, 1, 2, 3])
 def test_split_one_step_vs_oracle(ps, oracle, n, form):
@@ -136,6 +141,7 @@ def test_run_driver_vs_oracle_loop(ps, oracle, nt, fp64, form):
         assert np.array_equal(got, a)
     else:
         assert relerr(got, a) <= 1e-12
+        assert faces_untouched(got, T)
 
 
 def test_run_driver_odd_size_falls_back(ps, oracle):
@@ -153,9 +159,10 @@ def test_run_driver_odd_size_falls_back(ps, oracle):
 
 @pytest.mark.parametrize("n", [(64, 64, 64), (64, 34, 30)])
 @pytest.mark.parametrize("form", [0, 1, 2, 3])
-@pytest.mark.parametrize("nt", [1, 20])
+@pytest.mark.parametrize("nt", [1, 20, 50, 100])
 def test_grid_run_vs_oracle_loop(ps, oracle, n, form, nt):
-    """fp64 = split_grid (state on a fixed power-of-two grid): isotropic (cubic) and anisotropic spacing."""
+    """fp64 = split_grid (state on a fixed power-of-two grid): isotropic (cubic) and anisotropic spacing,
+    up to the 100 steps of the diffusion examples' time loop."""
     T, Ci, lam, hs, dt = _setup(n, form, seed=20 + form)
     a, b = T.copy(order="F"), T.copy(order="F")
     for _ in range(nt):
@@ -165,8 +172,10 @@ def test_grid_run_vs_oracle_loop(ps, oracle, n, form, nt):
     dT, dT2 = ps.from_host(T), ps.from_host(T)
     ps.kernels.run(k, dT, dT2, ps.from_host(Ci), ps.from_host(lam) if form == 3 else 1.3, dt, *hs, nt,
                    fp64="split_grid")
-    e = relerr(ps.to_host(dT), a)
+    got = ps.to_host(dT)
+    e = relerr(got, a)
     assert e <= 1e-12, e
+    assert faces_untouched(got, T)
 
 
 @pytest.mark.parametrize("shift,scale,lscale", [(-0.5, 1e-30, 1e5), (3.0, 7.0e20, 1e-7), (0.0, 1.0, 1.0)])

@@ -12,7 +12,9 @@ import pytest
 import jit_kernels as K
 from conftest import DT
 
-REFERENCE = "/root/reference"  # read only when present (this container), to translate its miniapps
+# the reference's source tree (ParallelStencil.jl) named by PS_REFERENCE_DIR: the tests that translate
+# its miniapps and examples are skipped when it is unset
+REFERENCE = os.environ.get("PS_REFERENCE_DIR", "")
 
 
 @pytest.fixture(scope="module")
@@ -212,7 +214,7 @@ def test_generated_sources_compile_for_sm103a(jit, tmp_path):
         assert p.returncode == 0, (f.name, out[-2000:])
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "miniapps")), reason="reference sources absent")
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "miniapps")), reason="PS_REFERENCE_DIR unset")
 def test_reference_miniapp_kernels_translate(jit):
     """Every @parallel / @parallel_indices definition of the reference's miniapps translates."""
     n = 0
@@ -228,7 +230,7 @@ def test_reference_miniapp_kernels_translate(jit):
     assert n >= 40
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "examples")), reason="reference sources absent")
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "examples")), reason="PS_REFERENCE_DIR unset")
 def test_reference_example_kernels_translate(jit):
     """Every top-level @parallel / @parallel_indices definition of the reference's examples and test
     projects translates, except those over CellArrays and NamedTuples of arrays (not built)."""

@@ -17,12 +17,12 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("Pt", "Vx", "Vy", "divV", "txx", "tyy", "txy", "Rx", "Ry", "dVxdtau", "dVydtau")
 
 
-def _pair(ps, nx, ny):
+def _pair(ps, nx, ny, dtype=np.float64):
     from ps_gb300.stokes import Stokes2D, Stokes2DParams, inclusion_setup
 
-    Mus, Rog = inclusion_setup(nx, ny, 1.0, 1.0, musi=0.1)
-    a = Stokes2D(Stokes2DParams(nx, ny, 1.0, 1.0), Mus, Rog)
-    b = Stokes2D(Stokes2DParams(nx, ny, 1.0, 1.0), Mus, Rog)
+    Mus, Rog = inclusion_setup(nx, ny, 1.0, 1.0, musi=0.1, dtype=dtype)
+    a = Stokes2D(Stokes2DParams(nx, ny, 1.0, 1.0), Mus, Rog, dtype=dtype)
+    b = Stokes2D(Stokes2DParams(nx, ny, 1.0, 1.0), Mus, Rog, dtype=dtype)
     a.compute_timesteps()
     b.compute_timesteps()
     return a, b
@@ -36,15 +36,30 @@ def _static(ps, s, n_iter):
                                                    stream_handle(None))
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("n", [(63, 47), (130, 97)])
-def test_static_scratch_iteration_matches_allocating_entry_point(ps, n):
-    ref, new = _pair(ps, *n)
+def test_static_scratch_iteration_matches_allocating_entry_point(ps, n, dtype):
+    ref, new = _pair(ps, *n, dtype=dtype)
     for n_iter in (7, 6):  # two calls in a row; odd then even iteration counts
         ref.iterate(n_iter)
         assert _static(ps, new, n_iter) == 0
         for k in FIELDS:
             assert np.array_equal(new.host(k), ref.host(k)), (n, n_iter, k)
     assert np.abs(new.host("Vy")).max() > 0
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_static_scratch_larger_grid_then_smaller(ps, dtype):
+    """The buffer offsets inside the shared array depend on the grid: a call on a smaller grid after
+    one on a larger grid (the array still holding the larger call's fields) gives the allocating
+    entry point's result as well."""
+    for n in ((130, 97), (63, 47)):
+        ref, new = _pair(ps, *n, dtype=dtype)
+        for n_iter in (5, 4):
+            ref.iterate(n_iter)
+            assert _static(ps, new, n_iter) == 0
+            for k in FIELDS:
+                assert np.array_equal(new.host(k), ref.host(k)), (n, n_iter, k)
 
 
 def test_static_scratch_rejects_grids_beyond_its_size(ps):
