@@ -339,6 +339,53 @@ int ps_stokes2d_err(const ps_stokes2d_fields* f, double out_mean_abs[3], void* s
 int ps_stokes2d_solve(const ps_stokes2d_fields* f, const ps_stokes2d_params* p, int32_t mode, double tol,
                       int64_t max_iter, int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
 
+/* Stokes2D with an accelerated pseudo-transient (APT) iteration whose pseudo-time steps come from
+ * the local viscosity maximum Musτ = @maxloc(Mus) -- the reference's idiom for heterogeneous
+ * coefficients (miniapps/HydroMech2D.jl:27). The miniapp's damped iteration (above) diverges at a
+ * viscosity contrast of 1e-3; this one keeps its arrays and statements (∇V, P, τ, R, V, the
+ * free-slip copies) but relaxes the stresses in pseudo-time (τ is state):
+ *   ∇V = @d_xa(Vx)*_dx + @d_ya(Vy)*_dy;  Pt = Pt - kP*∇V
+ *   τxx = aτ*τxx + bτ*(@d_xa(Vx)*_dx - ∇V/3);  τyy likewise;  τxy = aτc*τxy + bτc*ε̇xy
+ *   Rx, Ry as in Stokes2D.jl:33-34 (times _dx, _dy);  V = V + dτV*R;  bc_y!(Vx), bc_x!(Vy)
+ * with dτρ = Vpdt*max_lxy/Re/Musτ, Gdτ = Vpdt^2/dτρ/(r+2), kP = r*Gdτ, aτ = 1/(Gdτ/Mus+1),
+ * bτ = 2*Gdτ*aτ (cells); corners: the smallest Gdτ of the four cells, μ = @av(Mus); faces:
+ * dτV = the smaller dτρ of the two cells. Arrays: the miniapp's (shapes as ps_stokes2d_fields)
+ * plus Must, kP, aT, bT: (nx, ny); aTc, bTc: (nx-1, ny-1); dtVx: (nx-1, ny-2); dtVy: (nx-2, ny-1).
+ * No counterpart kernel exists in the reference; its oracle is the C restatement of these
+ * statements. */
+typedef struct ps_stokes2d_apt_fields {
+    ps_array Pt, divV, Vx, Vy, txx, tyy, txy, Rx, Ry, Mus, Rog;
+    ps_array Must, kP, aT, bT, aTc, bTc, dtVx, dtVy;
+} ps_stokes2d_apt_fields;
+
+/* dx, dy; Vpdt = CFL*min(dx,dy) (CFL = 0.9/sqrt(2)); Re (16π); r (1); max_lxy = max(lx, ly). */
+typedef struct ps_stokes2d_apt_params {
+    double dx, dy, Vpdt, Re, r, max_lxy;
+} ps_stokes2d_apt_params;
+
+/* Musτ and the coefficient arrays from Mus (FP64 arithmetic; FP32 arrays hold the rounded values). */
+int ps_stokes2d_apt_coefficients(const ps_stokes2d_apt_fields* f, const ps_stokes2d_apt_params* p, void* stream,
+                                 int sync);
+/* n_iter APT iterations in place (two kernels each); divV, Rx, Ry hold the last iteration's
+ * values. Bit-identical to the oracle's statements. Synchronises. */
+int ps_stokes2d_apt_iterate(const ps_stokes2d_apt_fields* f, const ps_stokes2d_apt_params* p, int64_t n_iter,
+                            void* stream);
+/* FP64 residual of the state (Vx, Vy, Pt) with the stresses at their pseudo-time steady state
+ * τ = 2μ(ε̇ - ∇V/3): writes txx, tyy, txy, divV, Rx, Ry and returns mean|Rx|, mean|Ry|, mean|∇V|.
+ * FP64 fields only. Synchronises. */
+int ps_stokes2d_apt_residual(const ps_stokes2d_apt_fields* f, const ps_stokes2d_apt_params* p, double out_mean_abs[3],
+                             void* stream);
+/* APT solve from the current state (coefficients recomputed from Mus) until the FP64 residual
+ * err = max(mean|Rx|, mean|Ry|, mean|∇V|) < tol, checked every nout iterations.
+ *   mode 0: FP64 APT iterations (the stresses are state).
+ *   mode 1: FP32 APT sweeps on the correction (δV, δP, δτ) driven by the FP64 residual of the
+ *           state (defect correction); residual, update and convergence check in FP64.
+ * FP64 fields. On return divV, Rx, Ry hold the FP64 residual of the final state (mode 1 also
+ * writes its steady-state stresses into txx, tyy, txy). Returns PS_ERR_NOT_CONVERGED at max_iter,
+ * PS_ERR_TIMEOUT after max_seconds (> 0), PS_ERR_NONFINITE on NaN/Inf residuals. */
+int ps_stokes2d_apt_solve(const ps_stokes2d_apt_fields* f, const ps_stokes2d_apt_params* p, int32_t mode, double tol,
+                          int64_t max_iter, int64_t nout, double max_seconds, ps_solve_stats* stats, void* stream);
+
 /* ------------------------------------------------------------------------------------ */
 /* Stokes3D miniapp (miniapps/Stokes3D.jl): the PT kernels of the 3-D analogue.          */
 /* ------------------------------------------------------------------------------------ */

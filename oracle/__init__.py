@@ -204,6 +204,64 @@ class Stokes2D:
         return max(m), tuple(m)
 
 
+class Stokes2DAPT:
+    """The accelerated pseudo-transient Stokes2D iteration (pseudo-time steps from @maxloc(Mus))
+    run by the oracle; same field names as ps_gb300.stokes.Stokes2DAPT. Coefficients are computed
+    in FP64 from the field's own Mus values and rounded for FP32 fields."""
+
+    SHAPES = {"Pt": (0, 0), "divV": (0, 0), "Vx": (1, 0), "Vy": (0, 1), "txx": (0, 0), "tyy": (0, 0),
+              "txy": (-1, -1), "Rx": (-1, -2), "Ry": (-2, -1), "Must": (0, 0), "kP": (0, 0), "aT": (0, 0),
+              "bT": (0, 0), "aTc": (-1, -1), "bTc": (-1, -1), "dtVx": (-1, -2), "dtVy": (-2, -1)}
+    COEFFS = ("Must", "kP", "aT", "bT", "aTc", "bTc", "dtVx", "dtVy")
+
+    def __init__(self, nx, ny, dx, dy, Mus, Rog, Re, r, Vpdt, max_lxy, dtype=np.float64):
+        self.nx, self.ny, self.dtype = nx, ny, np.dtype(dtype)
+        self.a = {k: np.asfortranarray(np.zeros((nx + e[0], ny + e[1]), dtype=dtype)) for k, e in self.SHAPES.items()}
+        self.a["Mus"] = np.asfortranarray(Mus.astype(dtype))
+        self.a["Rog"] = np.asfortranarray(Rog.astype(dtype))
+        self._dx, self._dy = 1.0 / dx, 1.0 / dy
+        c64 = {k: np.asfortranarray(np.zeros((nx + self.SHAPES[k][0], ny + self.SHAPES[k][1]))) for k in self.COEFFS}
+        m64 = np.asfortranarray(self.a["Mus"].astype(np.float64))  # the field's own values, widened
+        _check(lib().orc_stokes2d_apt_coeffs(*[_ptr(c64[k]) for k in self.COEFFS], _ptr(m64), ctypes.c_int64(nx),
+                                             ctypes.c_int64(ny), ctypes.c_double(Vpdt), ctypes.c_double(Re),
+                                             ctypes.c_double(r), ctypes.c_double(max_lxy)), "stokes2d_apt_coeffs")
+        for k in self.COEFFS:
+            self.a[k][...] = c64[k].astype(dtype)
+
+    def __getitem__(self, k):
+        return self.a[k]
+
+    def step(self):
+        R, a, i64 = _real(self.dtype), self.a, ctypes.c_int64
+        names = ("Vx", "Vy", "Pt", "txx", "tyy", "txy", "divV", "Rx", "Ry", "kP", "aT", "bT", "aTc", "bTc", "dtVx",
+                 "dtVy", "Rog")
+        _check(_fn("orc_stokes2d_apt_step", self.dtype)(*[_ptr(a[k]) for k in names], i64(self.nx), i64(self.ny),
+                                                          R(self._dx), R(self._dy)), "stokes2d_apt_step")
+
+    def err(self):
+        """max(mean|Rx|, mean|Ry|, mean|∇V|) of the last iteration (Stokes2D.jl:119-120)."""
+        m = [float(np.mean(np.abs(self.a[k]))) for k in ("Rx", "Ry", "divV")]
+        return max(m), tuple(m)
+
+    def residual(self):
+        """FP64 residual of the current state with the stresses at their steady state: returns
+        max(mean|Rx|, mean|Ry|, mean|∇V|) and the arrays (FP64 fields only)."""
+        if self.dtype != np.float64:
+            raise ValueError("the residual is computed on FP64 fields")
+        nx, ny = self.nx, self.ny
+        out = {k: np.asfortranarray(np.zeros((nx + e[0], ny + e[1]))) for k, e in
+               (("Rx", (-1, -2)), ("Ry", (-2, -1)), ("divV", (0, 0)), ("txx", (0, 0)), ("tyy", (0, 0)),
+                ("txy", (-1, -1)))}
+        a = self.a
+        _check(lib().orc_stokes2d_apt_residual(*[_ptr(out[k]) for k in ("Rx", "Ry", "divV", "txx", "tyy", "txy")],
+                                                 _ptr(a["Vx"]), _ptr(a["Vy"]), _ptr(a["Pt"]), _ptr(a["Mus"]),
+                                                 _ptr(a["Rog"]), ctypes.c_int64(nx), ctypes.c_int64(ny),
+                                                 ctypes.c_double(self._dx), ctypes.c_double(self._dy)),
+               "stokes2d_apt_residual")
+        m = [float(np.mean(np.abs(out[k]))) for k in ("Rx", "Ry", "divV")]
+        return max(m), out
+
+
 STOKES3D_SHAPES = {  # extents relative to (nx, ny, nz) = size(Pt) (miniapps/Stokes3D.jl:89-110)
     "Pt": (0, 0, 0), "dtauPt": (0, 0, 0), "divV": (0, 0, 0), "Vx": (1, 0, 0), "Vy": (0, 1, 0), "Vz": (0, 0, 1),
     "txx": (0, -2, -2), "tyy": (-2, 0, -2), "tzz": (-2, -2, 0), "txy": (-1, -1, -2), "txz": (-1, -2, -1),

@@ -398,6 +398,171 @@ int SFX(orc_bc_y2d)(REAL* A, int64_t n0, int64_t n1) {
     }
     return ORC_OK;
 }
+/* ------------------------------------------------------------------------------------- */
+/* Stokes2D, accelerated pseudo-transient (APT) iteration with pseudo-time steps from the   */
+/* local viscosity maximum. No counterpart kernel in the reference: its Stokes2D miniapp's  */
+/* damped iteration (above) diverges at viscosity contrasts of 1e-3; this scheme keeps the  */
+/* miniapp's staggered arrays and statements (∇V, P, τ, R, V, free-slip copies) but relaxes */
+/* the stresses in pseudo-time, with every local pseudo-time step taken from @maxloc(Mus)   */
+/* (the reference's own idiom for heterogeneous coefficients, miniapps/HydroMech2D.jl:27):  */
+/*   Musτ = Mus; @inn(Musτ) = @maxloc(Mus)                                                 */
+/*   dτρ = ((Vpdτ*max_lxy)/Re)/Musτ, Gdτ = ((Vpdτ*Vpdτ)/dτρ)/(r+2)        (cells)           */
+/*   kP = r*Gdτ, aτ = 1/(Gdτ/Mus + 1), bτ = (2*Gdτ)*aτ                    (cells)           */
+/*   corner: Gc = min of the four cells' Gdτ, μc = @av(Mus), aτc, bτc as above             */
+/*   face pseudo-steps: dτVx, dτVy = min of the two cells' dτρ                              */
+/* One iteration (all differences times 1/dx, 1/dy):                                       */
+/*   ∇V = dVx*_dx + dVy*_dy;  P = P - kP*∇V                                                 */
+/*   τxx = aτ*τxx + bτ*(dVx*_dx - ∇V*(1/3));  τyy likewise;  τxy = aτc*τxy + bτc*εxy        */
+/*   Rx = (dτxx*_dx + dτxy*_dy) - dP*_dx;  Ry = ((dτyy*_dy + dτxy*_dx) - dP*_dy) + @av_yi(Rog)*/
+/*   V = V + dτV*R;  bc_y!(Vx), bc_x!(Vy)                                                   */
+/* The coefficients are computed in FP64 from the field's own Mus values (FP32 arrays hold  */
+/* their FP64 values rounded).                                                              */
+/* ------------------------------------------------------------------------------------- */
+#define I2(a, b, n0) ((int64_t)(a) + (int64_t)(n0) * (int64_t)(b))
+#ifndef ORC_APT_COEFFS_DEFINED
+#define ORC_APT_COEFFS_DEFINED
+/* Coefficient arrays from Mus (FP64 only). Must: (nx, ny); kP, aT, bT: (nx, ny);
+ * aTc, bTc: (nx-1, ny-1); dtVx: (nx-1, ny-2); dtVy: (nx-2, ny-1). */
+int orc_stokes2d_apt_coeffs(double* Must, double* kP, double* aT, double* bT, double* aTc, double* bTc, double* dtVx,
+                            double* dtVy, const double* Mus, int64_t nx, int64_t ny, double Vpdt, double Re, double r,
+                            double max_lxy) {
+    if (nx < 3 || ny < 3) return ORC_ERR_SHAPE;
+    const int64_t n = nx * ny;
+    double* G = (double*)malloc((size_t)n * sizeof(double));
+    double* R = (double*)malloc((size_t)n * sizeof(double));
+    if (!G || !R) {
+        free(G);
+        free(R);
+        return ORC_ERR_ARG;
+    }
+    memcpy(Must, Mus, (size_t)n * sizeof(double));
+    for (int64_t iy = 1; iy < ny - 1; iy++)
+        for (int64_t ix = 1; ix < nx - 1; ix++) {
+            /* @maxloc (src/FiniteDifferences.jl:189-190): max(max(max(W, E), C), max(S, N)) */
+            double a = jl_max_f64(Mus[I2(ix - 1, iy, nx)], Mus[I2(ix + 1, iy, nx)]);
+            a = jl_max_f64(a, Mus[I2(ix, iy, nx)]);
+            Must[I2(ix, iy, nx)] = jl_max_f64(a, jl_max_f64(Mus[I2(ix, iy - 1, nx)], Mus[I2(ix, iy + 1, nx)]));
+        }
+    const double c0 = (Vpdt * max_lxy) / Re, v2 = Vpdt * Vpdt, rp2 = r + 2.0;
+    for (int64_t i = 0; i < n; i++) {
+        R[i] = c0 / Must[i];
+        G[i] = (v2 / R[i]) / rp2;
+        kP[i] = r * G[i];
+        aT[i] = 1.0 / (G[i] / Mus[i] + 1.0);
+        bT[i] = (2.0 * G[i]) * aT[i];
+    }
+    for (int64_t iy = 0; iy < ny - 1; iy++)
+        for (int64_t ix = 0; ix < nx - 1; ix++) {
+            double g = jl_min_f64(jl_min_f64(G[I2(ix, iy, nx)], G[I2(ix + 1, iy, nx)]),
+                                  jl_min_f64(G[I2(ix, iy + 1, nx)], G[I2(ix + 1, iy + 1, nx)]));
+            double mc = (((Mus[I2(ix, iy, nx)] + Mus[I2(ix + 1, iy, nx)]) + Mus[I2(ix, iy + 1, nx)]) +
+                         Mus[I2(ix + 1, iy + 1, nx)]) * 0.25;
+            double a = 1.0 / (g / mc + 1.0);
+            aTc[I2(ix, iy, nx - 1)] = a;
+            bTc[I2(ix, iy, nx - 1)] = (2.0 * g) * a;
+        }
+    for (int64_t iy = 0; iy < ny - 2; iy++)
+        for (int64_t ix = 0; ix < nx - 1; ix++)
+            dtVx[I2(ix, iy, nx - 1)] = jl_min_f64(R[I2(ix, iy + 1, nx)], R[I2(ix + 1, iy + 1, nx)]);
+    for (int64_t iy = 0; iy < ny - 1; iy++)
+        for (int64_t ix = 0; ix < nx - 2; ix++)
+            dtVy[I2(ix, iy, nx - 2)] = jl_min_f64(R[I2(ix + 1, iy, nx)], R[I2(ix + 1, iy + 1, nx)]);
+    free(G);
+    free(R);
+    return ORC_OK;
+}
+
+/* The FP64 residual of a state (Vx, Vy, Pt) with the stresses at their pseudo-time steady
+ * state, τ = 2μ(ε̇ - ∇V/3) (μ = Mus at cells, @av(Mus) at corners): Rx (nx-1, ny-2),
+ * Ry (nx-2, ny-1), divV (nx, ny); txx, tyy, txy receive those stresses. */
+int orc_stokes2d_apt_residual(double* Rx, double* Ry, double* divV, double* txx, double* tyy, double* txy,
+                              const double* Vx, const double* Vy, const double* Pt, const double* Mus,
+                              const double* Rog, int64_t nx, int64_t ny, double _dx, double _dy) {
+    const double third = 1.0 / 3.0;
+    for (int64_t iy = 0; iy < ny; iy++)
+        for (int64_t ix = 0; ix < nx; ix++) {
+            int64_t c = I2(ix, iy, nx);
+            double dvx = Vx[I2(ix + 1, iy, nx + 1)] - Vx[I2(ix, iy, nx + 1)];
+            double dvy = Vy[I2(ix, iy + 1, nx)] - Vy[I2(ix, iy, nx)];
+            double d = dvx * _dx + dvy * _dy;
+            double td = d * third;
+            divV[c] = d;
+            txx[c] = (2.0 * Mus[c]) * (dvx * _dx - td);
+            tyy[c] = (2.0 * Mus[c]) * (dvy * _dy - td);
+            if (ix < nx - 1 && iy < ny - 1) {
+                double mc = (((Mus[I2(ix, iy, nx)] + Mus[I2(ix + 1, iy, nx)]) + Mus[I2(ix, iy + 1, nx)]) +
+                             Mus[I2(ix + 1, iy + 1, nx)]) * 0.25;
+                double e = 0.5 * ((Vx[I2(ix + 1, iy + 1, nx + 1)] - Vx[I2(ix + 1, iy, nx + 1)]) * _dy +
+                                  (Vy[I2(ix + 1, iy + 1, nx)] - Vy[I2(ix, iy + 1, nx)]) * _dx);
+                txy[I2(ix, iy, nx - 1)] = (2.0 * mc) * e;
+            }
+        }
+    for (int64_t iy = 0; iy < ny - 2; iy++)
+        for (int64_t ix = 0; ix < nx - 1; ix++)
+            Rx[I2(ix, iy, nx - 1)] = ((txx[I2(ix + 1, iy + 1, nx)] - txx[I2(ix, iy + 1, nx)]) * _dx +
+                                      (txy[I2(ix, iy + 1, nx - 1)] - txy[I2(ix, iy, nx - 1)]) * _dy) -
+                                     (Pt[I2(ix + 1, iy + 1, nx)] - Pt[I2(ix, iy + 1, nx)]) * _dx;
+    for (int64_t iy = 0; iy < ny - 1; iy++)
+        for (int64_t ix = 0; ix < nx - 2; ix++)
+            Ry[I2(ix, iy, nx - 2)] = (((tyy[I2(ix + 1, iy + 1, nx)] - tyy[I2(ix + 1, iy, nx)]) * _dy +
+                                       (txy[I2(ix + 1, iy, nx - 1)] - txy[I2(ix, iy, nx - 1)]) * _dx) -
+                                      (Pt[I2(ix + 1, iy + 1, nx)] - Pt[I2(ix + 1, iy, nx)]) * _dy) +
+                                     (Rog[I2(ix + 1, iy, nx)] + Rog[I2(ix + 1, iy + 1, nx)]) * 0.5;
+    return ORC_OK;
+}
+#endif
+
+/* One APT iteration in place (cells and corners, then faces and the free-slip copies). */
+int SFX(orc_stokes2d_apt_step)(REAL* Vx, REAL* Vy, REAL* Pt, REAL* txx, REAL* tyy, REAL* txy, REAL* divV, REAL* Rx,
+                               REAL* Ry, const REAL* kP, const REAL* aT, const REAL* bT, const REAL* aTc,
+                               const REAL* bTc, const REAL* dtVx, const REAL* dtVy, const REAL* Rog, int64_t nx,
+                               int64_t ny, REAL _dx, REAL _dy) {
+    const REAL third = (REAL)(1.0 / 3.0), h = (REAL)0.5;
+#pragma omp parallel for schedule(static)
+    for (int64_t iy = 0; iy < ny; iy++)
+        for (int64_t ix = 0; ix < nx; ix++) {
+            int64_t c = I2(ix, iy, nx);
+            REAL dvx = Vx[I2(ix + 1, iy, nx + 1)] - Vx[I2(ix, iy, nx + 1)];
+            REAL dvy = Vy[I2(ix, iy + 1, nx)] - Vy[I2(ix, iy, nx)];
+            REAL d = dvx * _dx + dvy * _dy;
+            REAL td = d * third;
+            divV[c] = d;
+            Pt[c] = Pt[c] - kP[c] * d;
+            txx[c] = aT[c] * txx[c] + bT[c] * (dvx * _dx - td);
+            tyy[c] = aT[c] * tyy[c] + bT[c] * (dvy * _dy - td);
+            if (ix < nx - 1 && iy < ny - 1) {
+                int64_t k = I2(ix, iy, nx - 1);
+                REAL e = h * ((Vx[I2(ix + 1, iy + 1, nx + 1)] - Vx[I2(ix + 1, iy, nx + 1)]) * _dy +
+                              (Vy[I2(ix + 1, iy + 1, nx)] - Vy[I2(ix, iy + 1, nx)]) * _dx);
+                txy[k] = aTc[k] * txy[k] + bTc[k] * e;
+            }
+        }
+#pragma omp parallel for schedule(static)
+    for (int64_t iy = 0; iy < ny - 1; iy++)
+        for (int64_t ix = 0; ix < nx - 1; ix++) {
+            if (iy < ny - 2) {
+                int64_t k = I2(ix, iy, nx - 1);
+                REAL R = ((txx[I2(ix + 1, iy + 1, nx)] - txx[I2(ix, iy + 1, nx)]) * _dx +
+                          (txy[I2(ix, iy + 1, nx - 1)] - txy[I2(ix, iy, nx - 1)]) * _dy) -
+                         (Pt[I2(ix + 1, iy + 1, nx)] - Pt[I2(ix, iy + 1, nx)]) * _dx;
+                Rx[k] = R;
+                Vx[I2(ix + 1, iy + 1, nx + 1)] = Vx[I2(ix + 1, iy + 1, nx + 1)] + dtVx[k] * R;
+            }
+            if (ix < nx - 2) {
+                int64_t k = I2(ix, iy, nx - 2);
+                REAL R = (((tyy[I2(ix + 1, iy + 1, nx)] - tyy[I2(ix + 1, iy, nx)]) * _dy +
+                           (txy[I2(ix + 1, iy, nx - 1)] - txy[I2(ix, iy, nx - 1)]) * _dx) -
+                          (Pt[I2(ix + 1, iy + 1, nx)] - Pt[I2(ix + 1, iy, nx)]) * _dy) +
+                         (Rog[I2(ix + 1, iy, nx)] + Rog[I2(ix + 1, iy + 1, nx)]) * h;
+                Ry[k] = R;
+                Vy[I2(ix + 1, iy + 1, nx)] = Vy[I2(ix + 1, iy + 1, nx)] + dtVy[k] * R;
+            }
+        }
+    SFX(orc_bc_y2d)(Vx, nx + 1, ny);
+    SFX(orc_bc_x2d)(Vy, nx, ny + 1);
+    return ORC_OK;
+}
+
 #undef I2
 
 #undef OIDX

@@ -80,6 +80,39 @@ class Stokes2DParams:
                                 self.Ptsc, min(self.dx, self.dy) ** 2, max(self.nx, self.ny))
 
 
+@dataclass
+class Stokes2DAPTParams:
+    """Numerics of the accelerated pseudo-transient iteration (pseudo-time steps from the local
+    viscosity maximum): Vpdτ = CFL * min(dx, dy), dτρ = Vpdτ * max(lx, ly) / Re / Musτ,
+    Gdτ = Vpdτ^2 / dτρ / (r + 2). Re = 16π converged fastest on a circular inclusion of viscosity
+    ratio 1e-3 (127^2 and 255^2: 16400 and 28600 iterations to 1e-8; 5π, the constant-viscosity
+    choice, needed about twice as many)."""
+
+    nx: int
+    ny: int
+    lx: float = 10.0
+    ly: float = 10.0
+    Re: float = 16.0 * np.pi
+    r: float = 1.0
+    CFL: float = 0.9 / np.sqrt(2.0)
+
+    @property
+    def dx(self):
+        return self.lx / (self.nx - 1)
+
+    @property
+    def dy(self):
+        return self.ly / (self.ny - 1)
+
+    @property
+    def Vpdt(self):
+        return min(self.dx, self.dy) * self.CFL
+
+    @property
+    def max_lxy(self):
+        return max(self.lx, self.ly)
+
+
 def inclusion_setup(nx, ny, lx=10.0, ly=10.0, mus0=1.0, musi=0.1, rhogi=1.0, radius=None, dtype=np.float64):
     """Mus, Rog of Stokes2D.jl:94-99: a circular inclusion at the centre (Radc < r^2).
 
@@ -167,6 +200,81 @@ class Stokes2D:
         rc = _lib.load().ps_stokes2d_solve(ctypes.byref(self._fields), ctypes.byref(self._p), int(mode), float(tol),
                                            int(max_iter), int(nout), float(max_seconds), ctypes.byref(st),
                                            stream_handle(stream))
+        if rc != 0:
+            err = _lib.PSError(rc, _lib.last_error())
+            err.stats = st
+            raise err
+        return st
+
+
+APT_FIELDS = ("Pt", "divV", "Vx", "Vy", "txx", "tyy", "txy", "Rx", "Ry", "Mus", "Rog", "Must", "kP", "aT", "bT", "aTc",
+              "bTc", "dtVx", "dtVy")
+
+
+class PSStokes2DAPTFields(ctypes.Structure):
+    _fields_ = [(n, PSArray) for n in APT_FIELDS]
+
+
+class PSStokes2DAPTParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("dx", "dy", "Vpdt", "Re", "r", "max_lxy")]
+
+
+_FA = ctypes.POINTER(PSStokes2DAPTFields)
+_PA = ctypes.POINTER(PSStokes2DAPTParams)
+_lib.register("ps_stokes2d_apt_coefficients", [_FA, _PA, ctypes.c_void_p, ctypes.c_int])
+_lib.register("ps_stokes2d_apt_iterate", [_FA, _PA, ctypes.c_int64, ctypes.c_void_p])
+_lib.register("ps_stokes2d_apt_residual", [_FA, _PA, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p])
+_lib.register("ps_stokes2d_apt_solve", [_FA, _PA, ctypes.c_int32, ctypes.c_double, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_double, ctypes.POINTER(PSSolveStats), ctypes.c_void_p])
+
+
+class Stokes2DAPT:
+    """The Stokes2D arrays with the accelerated pseudo-transient iteration whose pseudo-time steps
+    come from @maxloc(Mus) (ps_stokes2d_apt_*): the miniapp's arrays plus the coefficient arrays
+    Must, kP, aT, bT (cells), aTc, bTc (corners), dtVx, dtVy (faces)."""
+
+    def __init__(self, params: Stokes2DAPTParams, Mus: np.ndarray, Rog: np.ndarray, dtype=np.float64):
+        require_initialized()
+        nx, ny = params.nx, params.ny
+        self.params, self.dtype = params, dtype
+        shapes = {"Pt": (nx, ny), "divV": (nx, ny), "Vx": (nx + 1, ny), "Vy": (nx, ny + 1), "txx": (nx, ny),
+                  "tyy": (nx, ny), "txy": (nx - 1, ny - 1), "Rx": (nx - 1, ny - 2), "Ry": (nx - 2, ny - 1),
+                  "Must": (nx, ny), "kP": (nx, ny), "aT": (nx, ny), "bT": (nx, ny), "aTc": (nx - 1, ny - 1),
+                  "bTc": (nx - 1, ny - 1), "dtVx": (nx - 1, ny - 2), "dtVy": (nx - 2, ny - 1)}
+        self.arrays = {k: zeros(*v, dtype=dtype) for k, v in shapes.items()}
+        self.arrays["Mus"] = from_host(np.asarray(Mus, dtype=dtype))
+        self.arrays["Rog"] = from_host(np.asarray(Rog, dtype=dtype))
+        self._fields = PSStokes2DAPTFields(*[descriptor(self.arrays[n]) for n in APT_FIELDS])
+        p = params
+        self._p = PSStokes2DAPTParams(p.dx, p.dy, p.Vpdt, p.Re, p.r, p.max_lxy)
+
+    def __getitem__(self, name):
+        return self.arrays[name]
+
+    def host(self, name) -> np.ndarray:
+        return to_host(self.arrays[name])
+
+    def coefficients(self, stream=None, sync=True):
+        _lib.call("ps_stokes2d_apt_coefficients", ctypes.byref(self._fields), ctypes.byref(self._p),
+                  stream_handle(stream), int(bool(sync)))
+
+    def iterate(self, n_iter: int, stream=None):
+        _lib.call("ps_stokes2d_apt_iterate", ctypes.byref(self._fields), ctypes.byref(self._p), int(n_iter),
+                  stream_handle(stream))
+
+    def residual(self, stream=None):
+        """FP64 residual of the state with the stresses at their steady state: (err, (means))."""
+        out = (ctypes.c_double * 3)()
+        _lib.call("ps_stokes2d_apt_residual", ctypes.byref(self._fields), ctypes.byref(self._p), out,
+                  stream_handle(stream))
+        return max(out), tuple(out)
+
+    def solve(self, tol=1e-8, mode=MODE_FP64, max_iter=10_000_000, nout=200, max_seconds=0.0, stream=None):
+        """APT solve to err < tol (FP64 residual); returns PSSolveStats. Raises PSError otherwise."""
+        st = PSSolveStats()
+        rc = _lib.load().ps_stokes2d_apt_solve(ctypes.byref(self._fields), ctypes.byref(self._p), int(mode),
+                                               float(tol), int(max_iter), int(nout), float(max_seconds),
+                                               ctypes.byref(st), stream_handle(stream))
         if rc != 0:
             err = _lib.PSError(rc, _lib.last_error())
             err.stats = st
