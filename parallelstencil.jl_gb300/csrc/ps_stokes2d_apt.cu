@@ -590,13 +590,18 @@ static int apt_solve_mixed(const ps_stokes2d_apt_fields* f, const ps_stokes2d_ap
         apt_convert_k<float, double><<<g, 256, 0, s>>>(F(18), AP<double>(f->Ry), n_y);
         cudaMemsetAsync(c + off[7], 0, off[13] - off[7], s);  // δVx, δVy, δP, δτ from zero
         const double target = std::max(err * inner_rtol, tol * 0.25);
-        // APT residuals oscillate while they decay: the sweep stops at the target, or when the
-        // best error has not improved by 2 % for 10 checks (FP32 stagnation)
+        // APT residuals oscillate while they decay, and pseudo-time waves need ~n iterations to
+        // cross the grid: the sweep stops at the target, or -- after at least 20 n iterations --
+        // when the best error has not improved by 2 % over the last 4 n iterations (FP32
+        // stagnation), n = max(nx, ny)
+        const int64_t nmax = std::max(nx, ny), min_sweep = 20 * nmax;
+        const int64_t stale_checks = std::max<int64_t>(10, (4 * nmax + nout - 1) / nout);
         double ierr = INFINITY, best = INFINITY;
-        int stale = 0;
+        int64_t stale = 0, swept = 0;
         while (it < max_iter) {
             PS_CUDA_TRY(cudaGraphLaunch(gr.exec, s));
             it += nout;
+            swept += nout;
             PS_TRY(read_device_words(h, red_in, sizeof(h), s));
             ierr = apt_err(h, nx, ny);
             if (std::isnan(ierr)) break;
@@ -604,7 +609,7 @@ static int apt_solve_mixed(const ps_stokes2d_apt_fields* f, const ps_stokes2d_ap
             if (ierr < 0.98 * best) {
                 best = ierr;
                 stale = 0;
-            } else if (++stale >= 10) {
+            } else if (++stale >= stale_checks && swept >= min_sweep) {
                 break;
             }
             if (max_seconds > 0 && apt_now() - t0 > max_seconds) break;
