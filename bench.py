@@ -890,7 +890,7 @@ def bench_adjoint(ps, torch, n=256, nt=200, every=20):
     _, _, T_obs, _ = adjoint.misfit_gradient(T0, T0, Ci, lam_obs, dt, h, nt, return_final=True)
     out = {"config": f"{n}^3 FP64, {nt} flux-lam steps, checkpoint every {every}, lam = exp(0.3 g) (Gaussian random "
                      f"field, sigma 8 cells), T_obs from lam (1 + 0.05 h)", "launches": 0}
-    for fp64 in ("ieee", "split"):
+    for fp64 in ("ieee", "split", "split_grid"):
         adjoint.misfit_gradient(T0, T_obs, Ci, lam, dt, h, 2 * every, checkpoint_every=every, fp64=fp64)  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -907,9 +907,15 @@ def bench_adjoint(ps, torch, n=256, nt=200, every=20):
                      "gradient_over_forward": round(t_grad / t_fwd, 3), "loss": loss,
                      "checkpoints": st.checkpoints, "recomputed_steps": st.recomputed_steps,
                      "grad_norm": float(g.norm())}
-        # forward and recomputed steps, adjoint steps (split: a pair pass before each), misfit
-        out["launches"] += 2 * nt + st.recomputed_steps + nt * (2 if fp64 == "split" else 1) + 2
+        if fp64 == "ieee":
+            g_ieee = g.clone()
+        else:
+            out[fp64]["gradient_err_vs_ieee"] = float((g - g_ieee).abs().max() / g_ieee.abs().max())
+        # forward and recomputed steps, adjoint steps (split: a pair pass before each; grid: the glam
+        # kernel and the adjoint state's step), misfit
+        out["launches"] += 2 * nt + st.recomputed_steps + nt * (1 if fp64 == "ieee" else 2) + 2
         del T, T2, g
+    del g_ieee
     return out
 
 
@@ -1052,6 +1058,24 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
         return
+    if a.only_run == "adjoint_grid":  # the misfit gradient on fixed grids, n^3, --steps steps, 2 segments
+        from ps_gb300 import adjoint
+
+        x = torch.linspace(0, 10, n, device="cuda", dtype=torch.float64)
+        T0 = ps.empty(n, n, n)
+        T0.copy_(1.7 * torch.exp(-((x[:, None, None] - 5) ** 2 + (x[None, :, None] - 5) ** 2 +
+                                   (x[None, None, :] - 5) ** 2)))
+        lam = ps.fill(1.2, n, n, n)
+        Ci = ps.ones(n, n, n)
+        h = ((n - 1) / 10.0,) * 3
+        dt = (10.0 / (n - 1)) ** 2 / 1.2 / 8.1
+        T_obs = ps.empty(n, n, n)
+        T_obs.copy_(T0 * 0.9)
+        adjoint.misfit_gradient(T0, T_obs, Ci, lam, dt, h, a.steps, checkpoint_every=max(1, a.steps // 2),
+                                fp64="split_grid")
+        torch.cuda.synchronize()
+        print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
+        return
     if a.only_run in ("stokes2d_apt", "stokes2d_apt32"):  # --steps accelerated PT iterations, n^2, ratio 1e-3
         from ps_gb300 import stokes
 
@@ -1156,7 +1180,7 @@ def main():
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
                                                  "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd", "fd32",
-                                                 "stokes2d_apt", "stokes2d_apt32"], default=None,
+                                                 "stokes2d_apt", "stokes2d_apt32", "adjoint_grid"], default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
                          "problem) and exit")

@@ -940,10 +940,17 @@ __global__ void join_pairs_kernel(const double* __restrict__ in, double* __restr
 static void* g_run_scratch = nullptr;
 static size_t g_run_bytes = 0;
 
+// Grow-only scratch of the fixed-grid misfit gradient (freed by ps_finalize).
+static void* g_grad_scratch = nullptr;
+static size_t g_grad_bytes = 0;
+
 void diffusion_free_scratch() {
     if (g_run_scratch) cudaFree(g_run_scratch);
     g_run_scratch = nullptr;
     g_run_bytes = 0;
+    if (g_grad_scratch) cudaFree(g_grad_scratch);
+    g_grad_scratch = nullptr;
+    g_grad_bytes = 0;
 }
 
 static int run_scratch(size_t bytes, char** p) {
@@ -957,6 +964,210 @@ static int run_scratch(size_t bytes, char** p) {
         g_run_bytes = bytes;
     }
     *p = static_cast<char*>(g_run_scratch);
+    return PS_OK;
+}
+
+// =======================================================================================
+// Misfit gradient on the fixed grid (ps_diffusion3d_misfit_gradient with PS_FP64_SPLIT_GRID).
+//
+// The flux-form step with a conductivity array is T' = T + dt Ci L T with L symmetric, so its
+// adjoint is λ = λ' + L μ' with μ = dt Ci λ (zero off the inner cells), and μ itself obeys
+// μ = μ' + dt Ci L μ': the same step as the forward one. The reverse sweep therefore runs the
+// forward grid kernel on μ (its own power-of-two grid, fixed from max|μ_nt|; the step is a
+// diffusion, so |μ| does not grow) and one more kernel per step accumulates
+//   glam[c] += Σ over the faces (a, b = a + e_d) of c of -1/2 hh_d (μ_b - μ_a)(T_b - T_a)
+// from μ_{n+1} and the forward state T_n (both grid pairs: the differences of their integer
+// parts are exact), summed on FP32 pairs and added to glam in FP64. The forward states and the
+// checkpoints are grid pairs of the forward run's grid. If any value leaves its grid, the caller
+// redoes the gradient with value-relative split pairs.
+// =======================================================================================
+
+// glam accumulation, one thread per (x, y) column and a z chunk; neighbours through L1/L2.
+__global__ void __launch_bounds__(256) glam_grid_kernel(const float2* __restrict__ M, const float2* __restrict__ Tg,
+                                                        double* __restrict__ glam, dd c0, dd c1, dd c2, int64_t nx,
+                                                        int64_t ny, int64_t nz, int L, const GridRun* __restrict__ run,
+                                                        const GridRun* __restrict__ mrun) {
+    if (run->bad || mrun->bad) return;
+    const int sh = mrun->shT + run->shT;  // μ in 2^-shμ, T in 2^-shT grid units
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, j = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
+    if (i >= nx || j >= ny) return;
+    const int64_t z0 = (int64_t)blockIdx.z * L, z1 = min(nz, z0 + L);
+    const int64_t sy = nx, sz = nx * ny;
+    auto ld = [](const float2* a, int64_t o) {
+        const float2 v = __ldg(a + o);
+        return dd{v.x, v.y};
+    };
+    // product of two grid differences (b - a) of μ and T, on pairs
+    auto face = [](dd ma, dd mb, dd ta, dd tb) {
+        const dd Dm{mb.h - ma.h, mb.l - ma.l};  // high parts: integers, exact
+        const dd Dt{tb.h - ta.h, tb.l - ta.l};
+        return dd_mul(Dm, Dt);
+    };
+    const dd zero{0.f, 0.f};
+    int64_t o = i + nx * (j + ny * z0);
+    dd mp = z0 > 0 ? ld(M, o - sz) : zero, tp = z0 > 0 ? ld(Tg, o - sz) : zero;
+    dd mc = ld(M, o), tc = ld(Tg, o);
+    for (int64_t k = z0; k < z1; ++k, o += sz) {
+        const bool up = k + 1 < nz;
+        const dd mn = up ? ld(M, o + sz) : zero, tn = up ? ld(Tg, o + sz) : zero;
+        dd sx = zero, sy_ = zero, szz = zero;
+        if (i > 0) sx = dd_add(sx, face(ld(M, o - 1), mc, ld(Tg, o - 1), tc));
+        if (i + 1 < nx) sx = dd_add(sx, face(mc, ld(M, o + 1), tc, ld(Tg, o + 1)));
+        if (j > 0) sy_ = dd_add(sy_, face(ld(M, o - sy), mc, ld(Tg, o - sy), tc));
+        if (j + 1 < ny) sy_ = dd_add(sy_, face(mc, ld(M, o + sy), tc, ld(Tg, o + sy)));
+        if (k > 0) szz = dd_add(szz, face(mp, mc, tp, tc));
+        if (up) szz = dd_add(szz, face(mc, mn, tc, tn));
+        dd g = dd_mul(c0, sx);
+        g = dd_add(g, dd_mul(c1, sy_));
+        g = dd_add(g, dd_mul(c2, szz));
+        const double y = f32_to_f64(g.h) + f32_to_f64(g.l);
+        glam[o] = glam[o] + grid_to_f64(y, sh);
+        mp = mc;
+        tp = tc;
+        mc = mn;
+        tc = tn;
+    }
+}
+
+// FP64 state from grid pairs (every cell): (h + l) 2^-sh
+__global__ void grid_state_to_f64_kernel(const float2* __restrict__ S, double* __restrict__ out, int64_t n,
+                                         const GridRun* __restrict__ r) {
+    if (r->bad) return;
+    const int sh = r->shT;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = S[c];
+        out[c] = grid_to_f64(f32_to_f64(v.x) + f32_to_f64(v.y), sh);
+    }
+}
+
+// μ_nt = dt Ci (T_nt - T_obs) on inner cells, 0 elsewhere; loss += 1/2 Σ (T_nt - T_obs)^2 (all cells)
+__global__ void grid_misfit_kernel(double* mu, const double* Tn,
+                                   const double* __restrict__ Tobs, const double* __restrict__ Ci, double dt, int64_t nx,
+                                   int64_t ny, int64_t nz, double* __restrict__ loss) {
+    double s = 0.0;
+    const int64_t n = nx * ny * nz;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+        const double r = Tn[c] - Tobs[c];
+        s += 0.5 * r * r;
+        const bool inner = i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2 && k >= 1 && k <= nz - 2;
+        mu[c] = inner ? dt * Ci[c] * r : 0.0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
+}
+
+int grid_misfit_gradient(const ps_array& T0, const ps_array& Tobs, const ps_array& Ci, const ps_array& lam, double dt,
+                         double hx, double hy, double hz, int64_t nt, int64_t ce, const ps_array& glam,
+                         const ps_array& T_final, double* loss, int64_t* recomputed, bool* redo, cudaStream_t s) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    *redo = false;
+    *recomputed = 0;
+    const int64_t n = numel(T0), n2 = n / 2, nseg = (nt + ce - 1) / ce;
+    const size_t bytes = (size_t)n * 8, stride = (bytes + 255) / 256 * 256;
+    const int64_t nbuf = 7 + nseg + ce;  // Cs, Ls, fA, fB, μA, μB, μ64, checkpoints, segment states
+    if (stride * nbuf + 512 > g_grad_bytes) {
+        if (g_grad_scratch) cudaFree(g_grad_scratch);
+        g_grad_scratch = nullptr;
+        g_grad_bytes = 0;
+        if (cudaMalloc(&g_grad_scratch, stride * nbuf + 512) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(PS_ERR_NOMEM, "ps_diffusion3d_misfit_gradient: grid scratch of %zu bytes failed",
+                        stride * nbuf + 512);
+        }
+        g_grad_bytes = stride * nbuf + 512;
+    }
+    char* scr = static_cast<char*>(g_grad_scratch);
+    GridRun* r = reinterpret_cast<GridRun*>(scr);         // the forward's grid (T, lam)
+    GridRun* rm = reinterpret_cast<GridRun*>(scr + 256);  // the adjoint's grid (μ)
+    double* d_loss = reinterpret_cast<double*>(scr + 128);
+    auto arr = [&](int64_t b) {
+        ps_array a = T0;
+        a.ptr = scr + 512 + stride * b;
+        return a;
+    };
+    ps_array Cs = arr(0), Ls = arr(1), fA = arr(2), fB = arr(3), mA = arr(4), mB = arr(5), mu64 = arr(6);
+    auto ckpt = [&](int64_t i) { return arr(7 + i); };
+    auto seg = [&](int64_t j) { return arr(7 + nseg + j); };
+    SplitParams p{};
+    double G;
+    const bool iso = split_coeffs(PS_DIFF_FLUX_LAM, 0.0, dt, hx, hy, hz, &p, &G);
+    const Box cells = {{1, 1, 1}, {T0.n[0] - 1, T0.n[1] - 1, T0.n[2] - 1}};
+    const int g = st->num_sms * 8;
+    auto copy = [&](const ps_array& dst, const ps_array& src) {
+        return cudaMemcpyAsync(dst.ptr, src.ptr, bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                   ? PS_OK
+                   : fail(PS_ERR_CUDA, "device copy failed");
+    };
+    auto step = [&](const ps_array& in, const ps_array& out) {
+        return iso ? launch_grid_step<true, true>(GRID_MIDDLE, in, Cs, &Ls, out, p, cells, 0, s, st->d_err, r)
+                   : launch_grid_step<true, false>(GRID_MIDDLE, in, Cs, &Ls, out, p, cells, 0, s, st->d_err, r);
+    };
+    // setup: grids of T and lam, pairs of lam and Ci, the first state
+    PS_CUDA_TRY(cudaMemsetAsync(scr, 0, 512, s));
+    absmax2_bits_kernel<<<st->num_sms * 4, 256, 0, s>>>(static_cast<const double2*>(T0.ptr),
+                                                        static_cast<const double2*>(lam.ptr), n2, &r->maxT, &r->maxL);
+    grid_setup_kernel<<<1, 1, 0, s>>>(r, G, 1);
+    to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(T0.ptr), static_cast<float4*>(fA.ptr), n2, r, 0);
+    to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(lam.ptr), static_cast<float4*>(Ls.ptr), n2, r, 1);
+    ci_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(Ci.ptr), static_cast<float4*>(Cs.ptr), n2, r);
+    // every state buffer holds T0's boundary values (the steps write inner cells only)
+    PS_TRY(copy(fB, fA));
+    for (int64_t j = 1; j < ce && j < nt; j++) PS_TRY(copy(seg(j), fA));
+    // forward with checkpoints
+    for (int64_t it = 0; it < nt; it++) {
+        if (it % ce == 0) PS_TRY(copy(ckpt(it / ce), fA));
+        PS_TRY(step(fA, fB));
+        std::swap(fA, fB);
+    }
+    // T_nt in FP64, the misfit, μ_nt on its own grid
+    grid_state_to_f64_kernel<<<g, 256, 0, s>>>(static_cast<const float2*>(fA.ptr), static_cast<double*>(mu64.ptr), n, r);
+    if (T_final.ptr) PS_TRY(copy(T_final, mu64));
+    grid_misfit_kernel<<<g, 256, 0, s>>>(static_cast<double*>(mu64.ptr), static_cast<const double*>(mu64.ptr),
+                                         static_cast<const double*>(Tobs.ptr), static_cast<const double*>(Ci.ptr), dt,
+                                         T0.n[0], T0.n[1], T0.n[2], d_loss);
+    absmax2_bits_kernel<<<st->num_sms * 4, 256, 0, s>>>(static_cast<const double2*>(mu64.ptr), nullptr, n2, &rm->maxT,
+                                                        nullptr);
+    grid_setup_kernel<<<1, 1, 0, s>>>(rm, 1.0, 0);
+    to_grid_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(mu64.ptr), static_cast<float4*>(mA.ptr), n2, rm, 0);
+    PS_CUDA_TRY(cudaMemsetAsync(mB.ptr, 0, bytes, s));  // μ is zero on the boundary cells
+    PS_CUDA_TRY(cudaMemsetAsync(glam.ptr, 0, bytes, s));
+    // glam coefficients: -1/2 hh_d; the grid scales 2^-(shμ + shT) are applied in FP64 per cell
+    dd c[3];
+    const double h[3] = {hx, hy, hz};
+    for (int d = 0; d < 3; d++) split_const(c[d], -0.5 * (h[d] * h[d]));
+    const dim3 blk(32, 8);
+    const int Lz = 16;
+    const dim3 grd((unsigned)((T0.n[0] + 31) / 32), (unsigned)((T0.n[1] + 7) / 8), (unsigned)((T0.n[2] + Lz - 1) / Lz));
+    // reverse sweep over the segments
+    for (int64_t sidx = nseg - 1; sidx >= 0; sidx--) {
+        const int64_t n0 = sidx * ce, n1 = std::min(nt, n0 + ce);
+        PS_TRY(copy(seg(0), ckpt(sidx)));
+        for (int64_t j = 1; j < n1 - n0; j++) {
+            PS_TRY(step(seg(j - 1), seg(j)));
+            (*recomputed)++;
+        }
+        for (int64_t nn = n1 - 1; nn >= n0; nn--) {
+            glam_grid_kernel<<<grd, blk, 0, s>>>(static_cast<const float2*>(mA.ptr),
+                                                 static_cast<const float2*>(seg(nn - n0).ptr),
+                                                 static_cast<double*>(glam.ptr), c[0], c[1], c[2], T0.n[0],
+                                                 T0.n[1], T0.n[2], Lz, r, rm);
+            if (nn > 0) {
+                PS_TRY(step(mA, mB));
+                std::swap(mA, mB);
+            }
+        }
+    }
+    PS_CUDA_TRY(cudaGetLastError());
+    GridRun hr[2];
+    double hl;
+    PS_TRY(read_device_words(hr, scr, sizeof(GridRun), s));
+    PS_TRY(read_device_words(hr + 1, rm, sizeof(GridRun), s));
+    PS_TRY(read_device_words(&hl, d_loss, sizeof(double), s));
+    *loss = hl;
+    *redo = (hr[0].bad | hr[1].bad) != 0;
     return PS_OK;
 }
 

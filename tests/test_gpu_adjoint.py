@@ -52,7 +52,47 @@ def test_misfit_gradient_vs_oracle_32(ps, oracle, fp64):
     assert np.abs(gg - g_ref).max() <= max(tol, 1e-13) * np.abs(g_ref).max()
 
 
-def test_misfit_gradient_finite_differences(ps):
+@pytest.mark.parametrize("n", [(64, 64, 64), (64, 40, 36)])
+def test_misfit_gradient_split_grid_vs_ieee(ps, n):
+    """The forward and reverse sweeps on fixed power-of-two grids (the adjoint state μ = dt Ci λ
+    on its own grid) against the IEEE gradient: loss and gradient within 1e-12 relative max-norm."""
+    T0, Ci, lam, h, dt = _problem(n, seed=11)
+    rng = np.random.default_rng(12)
+    nt = 40
+    dT0, dCi, dlam = ps.from_host(T0), ps.from_host(Ci), ps.from_host(lam)
+    lam_obs = ps.from_host(np.asfortranarray(lam * (1 + 0.05 * rng.standard_normal(n))))
+    _, _, T_obs, _ = ps.adjoint.misfit_gradient(dT0, dT0, dCi, lam_obs, dt, h, nt, return_final=True)
+    out = {}
+    for fp64 in ("ieee", "split_grid"):
+        loss, g, Tf, st = ps.adjoint.misfit_gradient(dT0, T_obs, dCi, dlam, dt, h, nt, checkpoint_every=8, fp64=fp64,
+                                                     return_final=True)
+        assert st.checkpoints == 5 and st.recomputed_steps == nt - 5
+        out[fp64] = (loss, ps.to_host(g), ps.to_host(Tf))
+    (la, ga, Ta), (lb, gb, Tb) = out["ieee"], out["split_grid"]
+    assert abs(la - lb) <= 1e-12 * la, (la, lb)
+    assert np.abs(ga - gb).max() <= 1e-12 * np.abs(ga).max(), np.abs(ga - gb).max() / np.abs(ga).max()
+    assert np.abs(Ta - Tb).max() <= 1e-12 * np.abs(Ta).max()
+    assert not np.array_equal(ga, gb)  # a different arithmetic really ran
+
+
+def test_misfit_gradient_split_grid_falls_back(ps):
+    """Odd nx (no TMA) and an unstable dt (values leave the grid) both run the split-pair gradient."""
+    for n, f in (((33, 20, 18), 1.0), ((64, 40, 36), 12.0)):
+        T0, Ci, lam, h, dt = _problem(n, seed=13)
+        dt = dt * f
+        dT0, dCi, dlam = ps.from_host(T0), ps.from_host(Ci), ps.from_host(lam)
+        T_obs = ps.from_host(np.asfortranarray(T0 * 0.9))
+        res = {}
+        for fp64 in ("split", "split_grid"):
+            loss, g, st = ps.adjoint.misfit_gradient(dT0, T_obs, dCi, dlam, dt, h, 6, checkpoint_every=3, fp64=fp64)
+            res[fp64] = (loss, ps.to_host(g))
+        la, lb = res["split"][0], res["split_grid"][0]  # the loss is an atomic sum: order may differ
+        assert la == lb or abs(la - lb) <= 1e-14 * abs(la), (la, lb)
+        assert np.array_equal(res["split"][1], res["split_grid"][1], equal_nan=True)
+
+
+@pytest.mark.parametrize("fp64", ["ieee", "split_grid"])
+def test_misfit_gradient_finite_differences(ps, fp64):
     """Central finite differences on 16 random directions (the inverse problem's check)."""
     n = (48, 48, 48)
     T0, Ci, lam, h, dt = _problem(n, seed=5)
@@ -62,7 +102,8 @@ def test_misfit_gradient_finite_differences(ps):
     lam_obs = lam * (1 + 0.05 * rng.standard_normal(n))
     _, _, T_obs, _ = ps.adjoint.misfit_gradient(dT0, dT0, dCi, ps.from_host(np.asfortranarray(lam_obs)), dt, h, nt,
                                                 return_final=True)
-    loss, g, st = ps.adjoint.misfit_gradient(dT0, T_obs, dCi, ps.from_host(lam), dt, h, nt, checkpoint_every=4)
+    loss, g, st = ps.adjoint.misfit_gradient(dT0, T_obs, dCi, ps.from_host(lam), dt, h, nt, checkpoint_every=4,
+                                             fp64=fp64)
     gh = ps.to_host(g)
     worst = 0.0
     for _ in range(16):
