@@ -85,7 +85,8 @@ typedef struct ps_launch {
  * most 2^23 grid units plus a low part), which makes differences and conductivity sums exact in
  * one FP32 operation. Rounding <= 1.5 * 2^-47 of max|T| per step. If a value leaves the grid's
  * range (max|T| growing past its initial power of two), the run is redone in
- * PS_FP64_SPLIT_STATE; this mode therefore synchronises the stream before returning.
+ * PS_FP64_SPLIT_STATE by kernels enqueued behind it that run only when the grid run flagged
+ * that, so the call stays asynchronous.
  * Single steps (ps_diffusion3d_step) treat both multi-step modes as PS_FP64_SPLIT. */
 enum { PS_FP64_IEEE = 0, PS_FP64_SPLIT = 1, PS_FP64_SPLIT_STATE = 2, PS_FP64_SPLIT_GRID = 3 };
 
@@ -199,8 +200,9 @@ int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_a
  * holds the state after nt steps (the boundary values of T and T2 must agree, as in the
  * examples' `T2 .= T`); T2's interior is workspace. cfg->memopt and cfg->fp64_mode apply; with
  * PS_FP64_SPLIT / PS_FP64_SPLIT_STATE the static arrays lam and Ci are split once per call into
- * library scratch (grow-only, freed by ps_finalize), so each step converts only T (SPLIT) or
- * nothing (SPLIT_STATE). Asynchronous on `stream`. */
+ * library scratch (grow-only, one per device and stream, freed by ps_finalize), so each step
+ * converts only T (SPLIT) or nothing (SPLIT_STATE). Asynchronous on `stream` in every mode; runs
+ * on different streams may overlap on the GPU. */
 int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_array Ci, ps_array lam_arr, double lam, double dt,
                        double hx, double hy, double hz, int64_t nt, const ps_launch* cfg, void* stream);
 

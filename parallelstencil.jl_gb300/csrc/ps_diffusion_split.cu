@@ -21,6 +21,8 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "ps_common.cuh"
 #include "ps_dd.cuh"
@@ -68,7 +70,11 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
                                                                   const __grid_constant__ CUtensorMap mL,
                                                                   const __grid_constant__ CUtensorMap mC,
                                                                   double* __restrict__ T2, SplitParams p, int64_t nx,
-                                                                  int64_t ny, Box cb, int L, int* __restrict__ err) {
+                                                                  int64_t ny, Box cb, int L, int* __restrict__ err,
+                                                                  const int* __restrict__ pred) {
+    // pred (may be NULL): the launch runs only if *pred is set -- the device-side fallback of a
+    // fixed-grid run whose values left the grid
+    if (pred && !*reinterpret_cast<const volatile int*>(pred)) return;
     using C = SplitCfg<LAM, TY, S>;
     // staged arrays converted in place each step: T (unless STATE) and lam (unless PRE)
     constexpr int NCONV = (STATE ? 0 : 1) + ((LAM && !PRE) ? 1 : 0);
@@ -295,7 +301,8 @@ static void split_const(dd& d, double v) {
 
 template <bool LAM, bool ISO, bool PRE, bool STATE>
 static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const ps_array* lam, const ps_array& T2,
-                                const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err) {
+                                const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err,
+                                const int* pred) {
     constexpr int TY = 8, S = 4, MINB = 3;
     using C = SplitCfg<LAM, TY, S>;
     CUtensorMap mT, mL, mC;
@@ -322,19 +329,19 @@ static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const p
     }
     dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
     diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE><<<grd, blk, C::SMEM, s>>>(
-        mT, mL, mC, static_cast<double*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err);
+        mT, mL, mC, static_cast<double*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err, pred);
     return PS_OK;
 }
 
 template <bool LAM, bool ISO>
 static int launch_split_flags(bool pre, bool state, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                               const ps_array& T2, const SplitParams& p, const Box& cb, int L, cudaStream_t s,
-                              int* d_err) {
+                              int* d_err, const int* pred) {
     if (pre)
-        return state ? launch_split_variant<LAM, ISO, true, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err)
-                     : launch_split_variant<LAM, ISO, true, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err);
-    return state ? launch_split_variant<LAM, ISO, false, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err)
-                 : launch_split_variant<LAM, ISO, false, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err);
+        return state ? launch_split_variant<LAM, ISO, true, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
+                     : launch_split_variant<LAM, ISO, true, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
+    return state ? launch_split_variant<LAM, ISO, false, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
+                 : launch_split_variant<LAM, ISO, false, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
 }
 
 // Per-dimension coefficients of the forms (split into p->c) and the common factor g: the
@@ -362,7 +369,7 @@ static bool split_coeffs(int form, double lam_s, double dt, double hx, double hy
 // then uses the IEEE kernels).
 static int launch_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                         double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L, bool pre,
-                        bool state, cudaStream_t s, int* d_err) {
+                        bool state, cudaStream_t s, int* d_err, const int* pred = nullptr) {
     bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
     if (!tma || T2.dtype != PS_F64) return PS_ERR_UNSUPPORTED;
     SplitParams p{};
@@ -370,10 +377,10 @@ static int launch_split(int form, const ps_array& T2, const ps_array& Tin, const
     const bool iso = split_coeffs(form, lam_s, dt, hx, hy, hz, &p, &g);
     split_const(p.g, g);
     if (form == PS_DIFF_FLUX_LAM)
-        return iso ? launch_split_flags<true, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err)
-                   : launch_split_flags<true, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err);
-    return iso ? launch_split_flags<false, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err)
-               : launch_split_flags<false, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err);
+        return iso ? launch_split_flags<true, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
+                   : launch_split_flags<true, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
+    return iso ? launch_split_flags<false, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
+               : launch_split_flags<false, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
 }
 
 int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
@@ -914,7 +921,9 @@ static int launch_grid_step(GridStep kind, const ps_array& Tin, const ps_array& 
 }
 
 // ---- multi-step runs -------------------------------------------------------------------
-__global__ void split_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n, int* err) {
+__global__ void split_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n, int* err,
+                                   const int* __restrict__ pred = nullptr) {
+    if (pred && !*reinterpret_cast<const volatile int*>(pred)) return;
     bool big = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         dd d = dd_split(in[i], big);
@@ -926,7 +935,8 @@ __global__ void split_pairs_kernel(const double* __restrict__ in, double* __rest
 // Final state of a split-pair run back to doubles, inner cells only: the boundary cells of T keep
 // their initial values exactly (a split pair holds only 24 bits of magnitudes below 2^-80).
 __global__ void join_pairs_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t nx, int64_t ny,
-                                  int64_t nz) {
+                                  int64_t nz, const int* __restrict__ pred = nullptr) {
+    if (pred && !*reinterpret_cast<const volatile int*>(pred)) return;
     const int64_t n = nx * ny * nz;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t x = i % nx, y = (i / nx) % ny, z = i / (nx * ny);
@@ -936,34 +946,57 @@ __global__ void join_pairs_kernel(const double* __restrict__ in, double* __restr
     }
 }
 
-// Grow-only scratch for the split pairs of lam, Ci and the run state (freed by ps_finalize).
-static void* g_run_scratch = nullptr;
-static size_t g_run_bytes = 0;
+// out = in (n 8-byte words) when *pred is set
+__global__ void copy_words_if_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n,
+                                     const int* __restrict__ pred) {
+    if (!*reinterpret_cast<const volatile int*>(pred)) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+// Grow-only scratch for the split pairs of lam, Ci and the run state, one per device and stream:
+// a run is asynchronous, so runs on different streams may execute at the same time (freed by
+// ps_finalize).
+struct RunScratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+static std::mutex g_run_mutex;
+static std::map<std::pair<int, cudaStream_t>, RunScratch> g_run_scratch;  // (device, stream)
 
 // Grow-only scratch of the fixed-grid misfit gradient (freed by ps_finalize).
 static void* g_grad_scratch = nullptr;
 static size_t g_grad_bytes = 0;
 
 void diffusion_free_scratch() {
-    if (g_run_scratch) cudaFree(g_run_scratch);
-    g_run_scratch = nullptr;
-    g_run_bytes = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_run_mutex);
+        for (auto& kv : g_run_scratch)
+            if (kv.second.ptr) cudaFree(kv.second.ptr);
+        g_run_scratch.clear();
+    }
     if (g_grad_scratch) cudaFree(g_grad_scratch);
     g_grad_scratch = nullptr;
     g_grad_bytes = 0;
 }
 
-static int run_scratch(size_t bytes, char** p) {
-    if (bytes > g_run_bytes) {
-        diffusion_free_scratch();
-        if (cudaMalloc(&g_run_scratch, bytes) != cudaSuccess) {
+static int run_scratch(size_t bytes, char** p, cudaStream_t s) {
+    int dev = 0;
+    PS_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_run_mutex);
+    RunScratch& r = g_run_scratch[{dev, s}];
+    if (bytes > r.bytes) {
+        if (r.ptr) cudaFree(r.ptr);  // waits for the work that used it
+        r.ptr = nullptr;
+        r.bytes = 0;
+        if (cudaMalloc(&r.ptr, bytes) != cudaSuccess) {
             cudaGetLastError();
-            g_run_scratch = nullptr;
+            r.ptr = nullptr;
             return fail(PS_ERR_NOMEM, "ps_diffusion3d_run: scratch allocation of %zu bytes failed", bytes);
         }
-        g_run_bytes = bytes;
+        r.bytes = bytes;
     }
-    *p = static_cast<char*>(g_run_scratch);
+    *p = static_cast<char*>(r.ptr);
     return PS_OK;
 }
 
@@ -972,9 +1005,9 @@ static int run_scratch(size_t bytes, char** p) {
 //
 // The flux-form step with a conductivity array is T' = T + dt Ci L T with L symmetric, so its
 // adjoint is λ = λ' + L μ' with μ = dt Ci λ (zero off the inner cells), and μ itself obeys
-// μ = μ' + dt Ci L μ': the same step as the forward one. The reverse sweep therefore runs the
-// forward grid kernel on μ (its own power-of-two grid, fixed from max|μ_nt|; the step is a
-// diffusion, so |μ| does not grow) and one more kernel per step accumulates
+// μ = μ' + dt Ci L μ': the same step as the forward one. Each reverse step is one sweep
+// (diff3d_grid_adj_tma) that applies that step to μ (its own power-of-two grid, fixed from
+// max|μ_nt|; the step is a diffusion, so |μ| does not grow) and accumulates
 //   glam[c] += Σ over the faces (a, b = a + e_d) of c of -1/2 hh_d (μ_b - μ_a)(T_b - T_a)
 // from μ_{n+1} and the forward state T_n (both grid pairs: the differences of their integer
 // parts are exact), summed on FP32 pairs and added to glam in FP64. The forward states and the
@@ -982,51 +1015,324 @@ static int run_scratch(size_t bytes, char** p) {
 // redoes the gradient with value-relative split pairs.
 // =======================================================================================
 
-// glam accumulation, one thread per (x, y) column and a z chunk; neighbours through L1/L2.
-__global__ void __launch_bounds__(256) glam_grid_kernel(const float2* __restrict__ M, const float2* __restrict__ Tg,
-                                                        double* __restrict__ glam, dd c0, dd c1, dd c2, int64_t nx,
-                                                        int64_t ny, int64_t nz, int L, const GridRun* __restrict__ run,
-                                                        const GridRun* __restrict__ mrun) {
-    if (run->bad || mrun->bad) return;
-    const int sh = mrun->shT + run->shT;  // μ in 2^-shμ, T in 2^-shT grid units
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, j = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
-    if (i >= nx || j >= ny) return;
-    const int64_t z0 = (int64_t)blockIdx.z * L, z1 = min(nz, z0 + L);
-    const int64_t sy = nx, sz = nx * ny;
-    auto ld = [](const float2* a, int64_t o) {
-        const float2 v = __ldg(a + o);
+// ---- fused reverse step ------------------------------------------------------------------
+// One z-sweep that does both halves of a reverse step: μ_out = μ_in + (dt Ci) L μ_in on the inner
+// cells (the forward grid step applied to μ, same operations as diff3d_grid_tma) and
+// glam += Σ_faces -1/2 hh_d Dμ DT from μ_in and the forward state T_n, for the cells of the rows
+// 1 .. ny-2 and planes 1 .. nz-2 (every x); glam_boundary_kernel does rows 0, ny-1 and planes 0,
+// nz-1. Planes of μ, lam, T_n (with their x-y halo) and of Ci are staged by TMA; y-face terms go
+// through shared memory, z-face terms through registers.
+template <int TY, int S>
+struct AdjCfg {
+    static constexpr int PW = SP_TX + 4;
+    static constexpr int PH = TY + 2;
+    static constexpr int PLANE = ((PW * PH * 8 + 127) / 128) * 128;
+    static constexpr int CIB = SP_TX * TY * 8;
+    static constexpr int STAGE = 3 * PLANE + CIB;  // μ, lam, T_n, Ci
+    static constexpr uint32_t TX_BYTES = (uint32_t)(3 * PW * PH * 8 + SP_TX * TY * 8);
+    static constexpr int FACE = (TY + 1) * SP_TX * 8;
+    static constexpr int SMEM = S * STAGE + 4 * FACE + 8 * S;  // K·Dμ and Dμ·DT of the y faces, 2 buffers each
+};
+
+// K·D of a face from its difference D (the operations of gface<true>)
+__device__ __forceinline__ dd grid_kd(dd D, dd la, dd lb) {
+    const float Kh = la.h + lb.h, Kl = la.l + lb.l;
+    const float pr = Kh * D.h;
+    float e = fmaf(Kh, D.h, -pr);
+    e = fmaf(Kh, D.l, e);
+    e = fmaf(Kl, D.h, e);
+    return {pr, e};
+}
+__device__ __forceinline__ dd grid_diff(dd a, dd b) { return {b.h - a.h, b.l - a.l}; }  // b - a, high part exact
+
+template <bool ISO, int TY, int S>
+__global__ void __launch_bounds__(32 * TY, 2)
+    diff3d_grid_adj_tma(const __grid_constant__ CUtensorMap mM, const __grid_constant__ CUtensorMap mL,
+                        const __grid_constant__ CUtensorMap mC, const __grid_constant__ CUtensorMap mT,
+                        float2* __restrict__ Mout, double* __restrict__ glam, SplitParams p, dd gc0, dd gc1, dd gc2,
+                        int64_t nx, int64_t ny, Box cb, int L, int* __restrict__ err, GridRun* __restrict__ run,
+                        const GridRun* __restrict__ mrun) {
+    using C = AdjCfg<TY, S>;
+    if (*reinterpret_cast<volatile int*>(&run->bad) || mrun->bad) return;
+    const int sh = mrun->shT + run->shT;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2* faceY0 = reinterpret_cast<float2*>(smem + S * C::STAGE);
+    float2* wY0 = reinterpret_cast<float2*>(smem + S * C::STAGE + 2 * C::FACE);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + 4 * C::FACE);
+
+    const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
+    const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
+    const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
+    const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
+    const int nk = min(L, (int)cb.hi[2] - Z0);
+    const int nq = nk + 2;
+
+    auto slot = [&](int q) { return smem + (q % S) * C::STAGE; };
+    if (tid == 0) {
+        prefetch_tensormap(&mM);
+        prefetch_tensormap(&mL);
+        prefetch_tensormap(&mC);
+        prefetch_tensormap(&mT);
+        for (int s = 0; s < S; s++) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int next_q = 0;
+    auto issue = [&](int q) {
+        unsigned char* b = slot(q);
+        int s = q % S, z = Z0 - 1 + q;
+        mbar_arrive_expect_tx(&bar[s], C::TX_BYTES);
+        tma_load_3d(b, &mM, &bar[s], X0 - 2, Y0 - 1, z);
+        tma_load_3d(b + C::PLANE, &mL, &bar[s], X0 - 2, Y0 - 1, z);
+        tma_load_3d(b + 2 * C::PLANE, &mT, &bar[s], X0 - 2, Y0 - 1, z);
+        tma_load_3d(b + 3 * C::PLANE, &mC, &bar[s], X0, Y0, z);
+    };
+    if (tid == 0)
+        for (; next_q < min(S, nq); ++next_q) issue(next_q);
+
+    const int own = (1 + ly) * C::PW + 2 + 2 * lx;
+    const int64_t gx = X0 + 2 * lx, gy = Y0 + ly;
+    const bool row_in = gy >= cb.lo[1] && gy < cb.hi[1];
+    const bool in0 = row_in && gx >= cb.lo[0] && gx < cb.hi[0];
+    const bool in1 = row_in && gx + 1 >= cb.lo[0] && gx + 1 < cb.hi[0];
+    const bool glam_row = gx < nx && gy >= 1 && gy < ny - 1;  // rows 0 and ny-1: glam_boundary_kernel
+    auto ld1 = [](const unsigned char* b, int off) {
+        const float2 v = reinterpret_cast<const float2*>(b)[off];
         return dd{v.x, v.y};
     };
-    // product of two grid differences (b - a) of μ and T, on pairs
-    auto face = [](dd ma, dd mb, dd ta, dd tb) {
-        const dd Dm{mb.h - ma.h, mb.l - ma.l};  // high parts: integers, exact
-        const dd Dt{tb.h - ta.h, tb.l - ta.l};
-        return dd_mul(Dm, Dt);
+    auto ld2 = [](const unsigned char* b, int off, dd* v) {
+        const float4 t = *reinterpret_cast<const float4*>(reinterpret_cast<const float2*>(b) + off);
+        v[0] = dd{t.x, t.y};
+        v[1] = dd{t.z, t.w};
     };
-    const dd zero{0.f, 0.f};
-    int64_t o = i + nx * (j + ny * z0);
-    dd mp = z0 > 0 ? ld(M, o - sz) : zero, tp = z0 > 0 ? ld(Tg, o - sz) : zero;
-    dd mc = ld(M, o), tc = ld(Tg, o);
-    for (int64_t k = z0; k < z1; ++k, o += sz) {
-        const bool up = k + 1 < nz;
-        const dd mn = up ? ld(M, o + sz) : zero, tn = up ? ld(Tg, o + sz) : zero;
-        dd sx = zero, sy_ = zero, szz = zero;
-        if (i > 0) sx = dd_add(sx, face(ld(M, o - 1), mc, ld(Tg, o - 1), tc));
-        if (i + 1 < nx) sx = dd_add(sx, face(mc, ld(M, o + 1), tc, ld(Tg, o + 1)));
-        if (j > 0) sy_ = dd_add(sy_, face(ld(M, o - sy), mc, ld(Tg, o - sy), tc));
-        if (j + 1 < ny) sy_ = dd_add(sy_, face(mc, ld(M, o + sy), tc, ld(Tg, o + sy)));
-        if (k > 0) szz = dd_add(szz, face(mp, mc, tp, tc));
-        if (up) szz = dd_add(szz, face(mc, mn, tc, tn));
-        dd g = dd_mul(c0, sx);
-        g = dd_add(g, dd_mul(c1, sy_));
-        g = dd_add(g, dd_mul(c2, szz));
-        const double y = f32_to_f64(g.h) + f32_to_f64(g.l);
-        glam[o] = glam[o] + grid_to_f64(y, sh);
-        mp = mc;
-        tp = tc;
-        mc = mn;
-        tc = tn;
+
+    bool bad = false, timed_out = false;
+    dd Mc[2], lc[2], Nc[2], Mz[2], lz[2], Nz[2], Fzm[2], Wzm[2];
+    timed_out |= !mbar_wait_bounded(&bar[0], 0);
+    timed_out |= !mbar_wait_bounded(&bar[1], 0);
+    {
+        dd M0[2], l0[2], N0[2];
+        ld2(slot(0), own, M0);
+        ld2(slot(1), own, Mc);
+        ld2(slot(0) + C::PLANE, own, l0);
+        ld2(slot(1) + C::PLANE, own, lc);
+        ld2(slot(0) + 2 * C::PLANE, own, N0);
+        ld2(slot(1) + 2 * C::PLANE, own, Nc);
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const dd D = grid_diff(M0[j], Mc[j]);
+            Fzm[j] = grid_kd(D, l0[j], lc[j]);
+            Wzm[j] = dd_mul(D, grid_diff(N0[j], Nc[j]));
+        }
     }
+
+    for (int k = 0; k < nk; ++k) {
+        const int q = k + 2;
+        const int64_t gz = Z0 + k;
+        const int64_t o = gx + nx * (gy + ny * gz);
+        // glam of this plane: loaded first, so its latency hides behind the face arithmetic
+        double2 gv = make_double2(0.0, 0.0);
+        if (glam_row) gv = *reinterpret_cast<const double2*>(glam + o);
+        timed_out |= !mbar_wait_bounded(&bar[q % S], (q / S) & 1);
+        const unsigned char* bz = slot(q);
+        ld2(bz, own, Mz);
+        ld2(bz + C::PLANE, own, lz);
+        ld2(bz + 2 * C::PLANE, own, Nz);
+        float2* faceY = faceY0 + (k & 1) * (TY + 1) * SP_TX;
+        float2* wY = wY0 + (k & 1) * (TY + 1) * SP_TX;
+        const unsigned char* mp = slot(k + 1);
+        const unsigned char* lp = mp + C::PLANE;
+        const unsigned char* np = mp + 2 * C::PLANE;
+        dd Fx[3], Wx[3], Fym[2], Wym[2], Fzp[2], Wzp[2], ci[2];
+        ld2(mp + 3 * C::PLANE, ly * SP_TX + 2 * lx, ci);
+        {
+            const dd Mxm = ld1(mp, own - 1), Mxp = ld1(mp, own + 2);
+            const dd lxm = ld1(lp, own - 1), lxp = ld1(lp, own + 2);
+            const dd Nxm = ld1(np, own - 1), Nxp = ld1(np, own + 2);
+            const dd D0 = grid_diff(Mxm, Mc[0]), D1 = grid_diff(Mc[0], Mc[1]), D2 = grid_diff(Mc[1], Mxp);
+            Fx[0] = grid_kd(D0, lxm, lc[0]);
+            Fx[1] = grid_kd(D1, lc[0], lc[1]);
+            Fx[2] = grid_kd(D2, lc[1], lxp);
+            Wx[0] = dd_mul(D0, grid_diff(Nxm, Nc[0]));
+            Wx[1] = dd_mul(D1, grid_diff(Nc[0], Nc[1]));
+            Wx[2] = dd_mul(D2, grid_diff(Nc[1], Nxp));
+        }
+        {
+            dd mb[2], lb[2], nb[2];
+            ld2(mp, own - C::PW, mb);
+            ld2(lp, own - C::PW, lb);
+            ld2(np, own - C::PW, nb);
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const dd D = grid_diff(mb[j], Mc[j]);
+                Fym[j] = grid_kd(D, lb[j], lc[j]);
+                Wym[j] = dd_mul(D, grid_diff(nb[j], Nc[j]));
+            }
+            *reinterpret_cast<float4*>(faceY + ly * SP_TX + 2 * lx) = make_float4(Fym[0].h, Fym[0].l, Fym[1].h, Fym[1].l);
+            *reinterpret_cast<float4*>(wY + ly * SP_TX + 2 * lx) = make_float4(Wym[0].h, Wym[0].l, Wym[1].h, Wym[1].l);
+        }
+        if (ly == TY - 1) {
+            dd ma[2], la[2], na[2];
+            ld2(mp, own + C::PW, ma);
+            ld2(lp, own + C::PW, la);
+            ld2(np, own + C::PW, na);
+            dd f[2], w[2];
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const dd D = grid_diff(Mc[j], ma[j]);
+                f[j] = grid_kd(D, lc[j], la[j]);
+                w[j] = dd_mul(D, grid_diff(Nc[j], na[j]));
+            }
+            *reinterpret_cast<float4*>(faceY + TY * SP_TX + 2 * lx) = make_float4(f[0].h, f[0].l, f[1].h, f[1].l);
+            *reinterpret_cast<float4*>(wY + TY * SP_TX + 2 * lx) = make_float4(w[0].h, w[0].l, w[1].h, w[1].l);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const dd D = grid_diff(Mc[j], Mz[j]);
+            Fzp[j] = grid_kd(D, lc[j], lz[j]);
+            Wzp[j] = dd_mul(D, grid_diff(Nc[j], Nz[j]));
+        }
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0) {
+                atomicOr(err, DEV_ERR_TMA_TIMEOUT);
+                for (int r = q + 1; r < next_q; ++r) mbar_wait_bounded(&bar[r % S], (r / S) & 1);
+            }
+            return;
+        }
+        if (tid == 0)
+            for (; next_q < min(nq, k + 2 + S); ++next_q) issue(next_q);
+        const float4 fa = *reinterpret_cast<const float4*>(faceY + (ly + 1) * SP_TX + 2 * lx);
+        const float4 wa = *reinterpret_cast<const float4*>(wY + (ly + 1) * SP_TX + 2 * lx);
+        const dd Fyp[2] = {dd{fa.x, fa.y}, dd{fa.z, fa.w}};
+        const dd Wyp[2] = {dd{wa.x, wa.y}, dd{wa.z, wa.w}};
+        float2 out[2];
+        double gout[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            dd Sm;
+            if constexpr (ISO) {
+                Sm = dd_sub(Fx[j + 1], Fx[j]);
+                Sm = dd_add(Sm, Fyp[j]);
+                Sm = dd_sub(Sm, Fym[j]);
+                Sm = dd_add(Sm, Fzp[j]);
+                Sm = dd_sub(Sm, Fzm[j]);
+            } else {
+                Sm = dd_mul(p.c[0], dd_sub(Fx[j + 1], Fx[j]));
+                Sm = dd_add(Sm, dd_mul(p.c[1], dd_sub(Fyp[j], Fym[j])));
+                Sm = dd_add(Sm, dd_mul(p.c[2], dd_sub(Fzp[j], Fzm[j])));
+            }
+            const dd d = dd_mul(ci[j], Sm);
+            constexpr float Mg = 12582912.0f;
+            const float q0 = (d.h + Mg) - Mg;
+            float l2 = (d.h - q0) + d.l;
+            l2 = l2 + Mc[j].l;
+            const float q1 = (l2 + Mg) - Mg;
+            const float h2 = (Mc[j].h + q0) + q1;
+            bad |= !(fabsf(h2) <= 8388608.0f);
+            out[j] = make_float2(h2, l2 - q1);
+            // glam: the six faces of the cell, by dimension
+            dd g = dd_mul(gc0, dd_add(Wx[j], Wx[j + 1]));
+            g = dd_add(g, dd_mul(gc1, dd_add(Wym[j], Wyp[j])));
+            g = dd_add(g, dd_mul(gc2, dd_add(Wzm[j], Wzp[j])));
+            gout[j] = grid_to_f64(f32_to_f64(g.h) + f32_to_f64(g.l), sh);
+        }
+        {
+            float2* dst = Mout + o;
+            if (in0 && in1)
+                *reinterpret_cast<float4*>(dst) = make_float4(out[0].x, out[0].y, out[1].x, out[1].y);
+            else {
+                if (in0) dst[0] = out[0];
+                if (in1) dst[1] = out[1];
+            }
+        }
+        if (glam_row) {
+            gv.x = gv.x + gout[0];
+            gv.y = gv.y + gout[1];
+            *reinterpret_cast<double2*>(glam + o) = gv;
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            Mc[j] = Mz[j];
+            lc[j] = lz[j];
+            Nc[j] = Nz[j];
+            Fzm[j] = Fzp[j];
+            Wzm[j] = Wzp[j];
+        }
+    }
+    if (__syncthreads_or(bad) && tid == 0) atomicOr(&run->bad, 1);
+}
+
+// glam of the cells in the planes z = 0, nz-1 and the rows y = 0, ny-1 (the rest is done by
+// diff3d_grid_adj_tma): the same face sums from global loads, one thread per cell.
+__global__ void glam_boundary_kernel(const float2* __restrict__ M, const float2* __restrict__ Tg,
+                                     double* __restrict__ glam, dd gc0, dd gc1, dd gc2, int64_t nx, int64_t ny,
+                                     int64_t nz, const GridRun* __restrict__ run, const GridRun* __restrict__ mrun) {
+    if (run->bad || mrun->bad) return;
+    const int sh = mrun->shT + run->shT;
+    const int f = blockIdx.y;  // 0, 1: planes z = 0, nz-1 (all x, y); 2, 3: rows y = 0, ny-1 (z = 1 .. nz-2)
+    const int64_t n0 = nx, n1 = f < 2 ? ny : nz - 2;
+    const int64_t sy = nx, sz = nx * ny;
+    auto ld = [](const float2* a, int64_t o) {
+        const float2 v = a[o];
+        return dd{v.x, v.y};
+    };
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n0 * n1; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t x = t % n0, v = t / n0;
+        const int64_t y = f < 2 ? v : (f == 2 ? 0 : ny - 1), z = f < 2 ? (f == 0 ? 0 : nz - 1) : v + 1;
+        const int64_t o = x + nx * (y + ny * z);
+        const dd mc = ld(M, o), tc = ld(Tg, o);
+        dd s3[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        const int64_t pos[3] = {x, y, z}, ext[3] = {nx, ny, nz}, st[3] = {1, sy, sz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (pos[d] > 0) {
+                const int64_t nb = o - st[d];
+                s3[d] = dd_add(s3[d], dd_mul(grid_diff(ld(M, nb), mc), grid_diff(ld(Tg, nb), tc)));
+            }
+            if (pos[d] + 1 < ext[d]) {
+                const int64_t nb = o + st[d];
+                s3[d] = dd_add(s3[d], dd_mul(grid_diff(mc, ld(M, nb)), grid_diff(tc, ld(Tg, nb))));
+            }
+        }
+        dd g = dd_mul(gc0, s3[0]);
+        g = dd_add(g, dd_mul(gc1, s3[1]));
+        g = dd_add(g, dd_mul(gc2, s3[2]));
+        glam[o] = glam[o] + grid_to_f64(f32_to_f64(g.h) + f32_to_f64(g.l), sh);
+    }
+}
+
+template <bool ISO>
+static int launch_grid_adj(const ps_array& Min, const ps_array& Ls, const ps_array& Cs, const ps_array& Tn,
+                           const ps_array& Mout, const ps_array& glam, const SplitParams& p, const dd gc[3],
+                           const Box& cb, cudaStream_t s, int* d_err, GridRun* run, const GridRun* mrun) {
+    constexpr int TY = 8, S = 4;
+    using C = AdjCfg<TY, S>;
+    auto kernel = diff3d_grid_adj_tma<ISO, TY, S>;
+    CUtensorMap mM, mL, mC, mT;
+    PS_TRY(encode_plane_map(&mM, Min, C::PW, C::PH));
+    PS_TRY(encode_plane_map(&mL, Ls, C::PW, C::PH));
+    PS_TRY(encode_plane_map(&mT, Tn, C::PW, C::PH));
+    PS_TRY(encode_plane_map(&mC, Cs, SP_TX, TY));
+    static bool attr = false;
+    if (!attr) {
+        PS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+        attr = true;
+    }
+    const int64_t x0 = cb.lo[0] & ~(int64_t)1;
+    const int64_t bx = (cb.hi[0] - x0 + SP_TX - 1) / SP_TX, by = (cb.hi[1] - cb.lo[1] + TY - 1) / TY;
+    static const int occ = resident_ctas(kernel, 32 * TY, C::SMEM);
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    const int L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
+    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    kernel<<<grd, dim3(32, TY, 1), C::SMEM, s>>>(mM, mL, mC, mT, static_cast<float2*>(Mout.ptr),
+                                                static_cast<double*>(glam.ptr), p, gc[0], gc[1], gc[2], Mout.n[0],
+                                                Mout.n[1], cb, L, d_err, run, mrun);
+    const int64_t nmax = std::max(Mout.n[0] * Mout.n[1], Mout.n[0] * Mout.n[2]);
+    glam_boundary_kernel<<<dim3((unsigned)std::min<int64_t>((nmax + 255) / 256, st->num_sms * 4), 4), 256, 0, s>>>(
+        static_cast<const float2*>(Min.ptr), static_cast<const float2*>(Tn.ptr), static_cast<double*>(glam.ptr),
+        gc[0], gc[1], gc[2], Mout.n[0], Mout.n[1], Mout.n[2], run, mrun);
+    return PS_OK;
 }
 
 // FP64 state from grid pairs (every cell): (h + l) 2^-sh
@@ -1138,9 +1444,6 @@ int grid_misfit_gradient(const ps_array& T0, const ps_array& Tobs, const ps_arra
     dd c[3];
     const double h[3] = {hx, hy, hz};
     for (int d = 0; d < 3; d++) split_const(c[d], -0.5 * (h[d] * h[d]));
-    const dim3 blk(32, 8);
-    const int Lz = 16;
-    const dim3 grd((unsigned)((T0.n[0] + 31) / 32), (unsigned)((T0.n[1] + 7) / 8), (unsigned)((T0.n[2] + Lz - 1) / Lz));
     // reverse sweep over the segments
     for (int64_t sidx = nseg - 1; sidx >= 0; sidx--) {
         const int64_t n0 = sidx * ce, n1 = std::min(nt, n0 + ce);
@@ -1150,14 +1453,11 @@ int grid_misfit_gradient(const ps_array& T0, const ps_array& Tobs, const ps_arra
             (*recomputed)++;
         }
         for (int64_t nn = n1 - 1; nn >= n0; nn--) {
-            glam_grid_kernel<<<grd, blk, 0, s>>>(static_cast<const float2*>(mA.ptr),
-                                                 static_cast<const float2*>(seg(nn - n0).ptr),
-                                                 static_cast<double*>(glam.ptr), c[0], c[1], c[2], T0.n[0],
-                                                 T0.n[1], T0.n[2], Lz, r, rm);
-            if (nn > 0) {
-                PS_TRY(step(mA, mB));
-                std::swap(mA, mB);
-            }
+            // glam from μ_{nn+1} and T_nn, and μ_nn, in one sweep
+            PS_TRY(iso ? launch_grid_adj<true>(mA, Ls, Cs, seg(nn - n0), mB, glam, p, c, cells, s, st->d_err, r, rm)
+                       : launch_grid_adj<false>(mA, Ls, Cs, seg(nn - n0), mB, glam, p, c, cells, s, st->d_err, r,
+                                                rm));
+            std::swap(mA, mB);
         }
     }
     PS_CUDA_TRY(cudaGetLastError());
@@ -1205,10 +1505,13 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
     ps_array A = T, B = T2;
     if (split && mode == PS_FP64_SPLIT_GRID && nt > 0) {
         // state, lam and Ci as grid / value pairs in scratch; T is written only by the final
-        // conversion, which the device skips when a value left the grid range
+        // conversion, which the device skips when a value left the grid range. The fallback (the
+        // same run on value-relative split pairs) is enqueued behind the grid run with every
+        // kernel predicated on the run's flag, so the call stays asynchronous; its pairs live in
+        // four more scratch arrays.
         char* scr = nullptr;
         const size_t head = 256;
-        PS_TRY(run_scratch(head + bytes * ((has_lam ? 1 : 0) + 3), &scr));
+        PS_TRY(run_scratch(head + bytes * ((has_lam ? 1 : 0) + 3 + 4), &scr, s));
         GridRun* r = reinterpret_cast<GridRun*>(scr);
         ps_array Cs = Ci, Ls = lam_arr, Sa = T, Sb = T;
         Cs.ptr = scr + head;
@@ -1266,15 +1569,35 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
             PS_TRY(step(last ? GRID_LAST64 : GRID_MIDDLE, A, Cs, &Ls, last ? T : B));
             std::swap(A, B);
         }
-        PS_CUDA_TRY(cudaGetLastError());
-        int bad = 0;
-        PS_TRY(read_device_words(&bad, &r->bad, sizeof(int), s));
-        if (bad) {  // a value outside the grid's range: redo the run with value-relative split pairs
-            ps_launch c2 = cfg ? *cfg : ps_launch{};
-            c2.memopt = memopt;
-            c2.fp64_mode = PS_FP64_SPLIT_STATE;
-            return ps_diffusion3d_run(form, T, T2, Ci, lam_arr, lam, dt, hx, hy, hz, nt, &c2, stream);
+        // the fallback: a PS_FP64_SPLIT_STATE run from T (left untouched by a flagged grid run),
+        // each launch returning at once unless the flag is set
+        const int* pred = &r->bad;
+        char* fb = scr + head + bytes * ((has_lam ? 1 : 0) + 3);
+        ps_array C2 = Ci, L2 = lam_arr, Fa = T, Fb = T;
+        C2.ptr = fb;
+        L2.ptr = fb + bytes;
+        Fa.ptr = fb + 2 * bytes;
+        Fb.ptr = fb + 3 * bytes;
+        // small grids (one CTA per SM for the elementwise kernels, whole-z sweeps for the steps:
+        // results do not depend on the sweep length), so the launches cost little when skipped
+        const int gp = st->num_sms;
+        const int Lz = (int)(cells.hi[2] - cells.lo[2]);
+        split_pairs_kernel<<<gp, 256, 0, s>>>(static_cast<const double*>(Ci.ptr), static_cast<double*>(C2.ptr), n,
+                                              st->d_err, pred);
+        if (has_lam)
+            split_pairs_kernel<<<gp, 256, 0, s>>>(static_cast<const double*>(lam_arr.ptr),
+                                                  static_cast<double*>(L2.ptr), n, st->d_err, pred);
+        split_pairs_kernel<<<gp, 256, 0, s>>>(static_cast<const double*>(T.ptr), static_cast<double*>(Fa.ptr), n,
+                                              st->d_err, pred);
+        copy_words_if_kernel<<<gp, 256, 0, s>>>(static_cast<const double*>(Fa.ptr), static_cast<double*>(Fb.ptr), n,
+                                                pred);
+        for (int64_t it = 0; it < nt; ++it) {
+            PS_TRY(launch_split(form, Fb, Fa, C2, has_lam ? &L2 : nullptr, lam, dt, hx, hy, hz, cells, Lz, true, true,
+                                s, st->d_err, pred));
+            std::swap(Fa, Fb);
         }
+        join_pairs_kernel<<<gp, 256, 0, s>>>(static_cast<const double*>(Fa.ptr), static_cast<double*>(T.ptr), T.n[0],
+                                             T.n[1], T.n[2], pred);
         return finish_launch(s, 0, "ps_diffusion3d_run");
     }
     if (!split) {
@@ -1287,7 +1610,7 @@ extern "C" int ps_diffusion3d_run(int32_t form, ps_array T, ps_array T2, ps_arra
         const bool state = mode == PS_FP64_SPLIT_STATE;
         char* scr = nullptr;
         const size_t need = bytes * ((has_lam ? 2 : 1) + (state ? 2 : 0));
-        PS_TRY(run_scratch(need, &scr));
+        PS_TRY(run_scratch(need, &scr, s));
         ps_array Cs = Ci, Ls = lam_arr, Sa = T, Sb = T;
         Cs.ptr = scr;
         if (has_lam) Ls.ptr = scr + bytes;
