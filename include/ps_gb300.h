@@ -104,6 +104,12 @@ const char* ps_last_error(void);
 int ps_abi_version(void);
 /* Number of CUDA devices visible (0 without a driver). Needs no ps_init. */
 int ps_device_count(int* count);
+/* Self-check of the kernels' division by a number known on the host (Markstein's method: one
+ * multiply and four FMAs, correctly rounded) against the IEEE division a / b on the device.
+ * PS_F32: every significand of 12 binades (from 2^-126 to 2^127) with both signs plus special
+ * values; PS_F64: n dividends from a seeded hash plus special values. *mismatches = the number
+ * of results whose bits differ (NaNs compare equal). Synchronises. */
+int ps_check_division(double b, int32_t dtype, int64_t n, uint64_t seed, int64_t* mismatches, void* stream);
 
 /* `@zeros(nx,ny,nz)` allocation (src/ParallelKernel/allocators.jl:279-293,
  * CUDAExt/allocators.jl:3): zero-filled device array owned by the caller. */
@@ -265,6 +271,22 @@ int ps_acoustic3d_v(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
 /* `@all(P) = @all(P) - dt*k*(@d_xa(Vx)/dx + @d_ya(Vy)/dy + @d_za(Vz)/dz)`. */
 int ps_acoustic3d_p(ps_array P, ps_array Vx, ps_array Vy, ps_array Vz,
                     double dt, double k, double dx, double dy, double dz, void* stream, int sync);
+/* One time step of the miniapp's loop (acoustic3D.jl:55-56: compute_V! then compute_P!) as one
+ * kernel that reads (Vx, Vy, Vz, P) and writes the new state into (Vx2, Vy2, Vz2, P2): every value,
+ * faces outside @inn copied. 8 words per cell instead of the 12 of the two launches. The output
+ * arrays must not overlap each other or the inputs (PS_ERR_ARG). fp64_mode: PS_FP64_IEEE
+ * (bit-identical to ps_acoustic3d_v + ps_acoustic3d_p; FP32 arrays take only this) or
+ * PS_FP64_SPLIT (FP64 arrays, arithmetic on FP32 pairs, ~2^-46 relative rounding per step). */
+int ps_acoustic3d_step(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
+                       ps_array Vx2, ps_array Vy2, ps_array Vz2, ps_array P2,
+                       double dt, double rho, double k, double dx, double dy, double dz,
+                       int32_t fp64_mode, void* stream, int sync);
+/* nt steps of the miniapp's time loop on (Vx, Vy, Vz, P) in place: ps_acoustic3d_step alternating
+ * between the caller's arrays and a second set in library scratch (grow-only, one per device and
+ * stream, freed by ps_finalize); odd nt ends with a copy back. Asynchronous on `stream`. */
+int ps_acoustic3d_run(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
+                      double dt, double rho, double k, double dx, double dy, double dz,
+                      int64_t nt, int32_t fp64_mode, void* stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Stokes2D pseudo-transient solver (miniapps/Stokes2D.jl).                              */
@@ -455,10 +477,12 @@ int ps_stokes3d_solve_mixed(const ps_stokes3d_fields* f, const ps_stokes3d_param
  * contraction, and load it on the current device. `entry` is the extern "C" kernel, which takes
  * one argument block by value:
  *   struct { void* a[32]; long long n[32][3]; double s[32]; long long lo[3]; long long cnt[3]; int* err;
- *            long long smem; long long loop; }
+ *            long long smem; long long loop; unsigned* ocnt; int ord[10]; }
  * (array pointers and extents, scalars, first thread index and thread counts per dimension, the
  * kernel's error flags -- one device int owned by the handle --, the launch's dynamic shared
- * memory bytes and the indices per thread of a sweep kernel).
+ * memory bytes, the indices per thread of a sweep kernel, and the block order of a boundary-first
+ * launch: a host-mapped counter, NULL otherwise, and blocks per axis, boundary blocks at the low and
+ * high end of each axis and their count).
  * Compile errors return PS_ERR_ARG with the compiler log in ps_last_error(). */
 int ps_jit_compile(const char* source, const char* entry, void** kernel);
 /* Launch a compiled kernel over count[0] x count[1] x count[2] threads starting at thread index
@@ -478,6 +502,17 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
 int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                      const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
                      const int32_t loop[3], void* stream, int sync);
+/* `@hide_communication bw begin @parallel kernel!(...); comm() end` for a run-time compiled
+ * `@parallel` kernel over its full grid (count threads from index 0; threads and loop as for
+ * ps_jit_launch_ex; no dynamic shared memory, no barriers, shuffles or votes). One launch on
+ * `stream` whose first blocks take the tiles holding the boundary indices t < bw or t >= count - bw
+ * (the reference's ranges_outer, src/ParallelKernel/hide_communication.jl:350-394); each such block
+ * counts itself in host-mapped memory after its stores, and `comm` runs on this thread as soon as
+ * all have, while the inner blocks still run. Returns after the launch completes, with the
+ * kernel's flags reported as by a synchronous launch. */
+int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars,
+                              int32_t nscalars, const int64_t count[3], const int32_t threads[3], const int32_t loop[3],
+                              const int64_t bw[3], ps_comm_fn comm, void* comm_ctx, void* stream);
 /* Wait for `stream`, then report (and clear) the error flags left by earlier asynchronous launches
  * of `kernel`, as a synchronous launch does. */
 int ps_jit_check(void* kernel, void* stream);

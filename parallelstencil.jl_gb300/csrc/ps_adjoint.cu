@@ -25,7 +25,7 @@ namespace ps {
 
 int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam,
                   double lam_s, double dt, double hx, double hy, double hz, const Box& thread_box, int memopt,
-                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err);
+                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err, HideReq* hr = nullptr);
 int grid_misfit_gradient(const ps_array& T0, const ps_array& Tobs, const ps_array& Ci, const ps_array& lam, double dt,
                          double hx, double hy, double hz, int64_t nt, int64_t ce, const ps_array& glam,
                          const ps_array& T_final, double* loss, int64_t* recomputed, bool* redo, cudaStream_t s);

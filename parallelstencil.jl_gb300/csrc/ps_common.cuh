@@ -47,6 +47,7 @@ void stokes2d_free_scratch();
 void stokes2d_static_forget();  // drop the cached device addresses of the static scratch array
 void diffusion_free_scratch();
 void adjoint_free_scratch();
+void acoustic_free_scratch();
 
 // Copies `bytes` (<= 256 through pinned staging) from device memory on stream s and synchronises s.
 int read_device_words(void* dst, const void* src, size_t bytes, cudaStream_t s);
@@ -113,6 +114,140 @@ inline int resident_ctas(K kernel, int threads, int smem) {
         n = 1;
     }
     return n;
+}
+
+// ---------------------------------------------------------------------------------------
+// Boundary-first tile order (`@hide_communication` in one launch).
+// ---------------------------------------------------------------------------------------
+// A z-sweep launch over TX x TY x TZ tiles (x tile columns, y tile rows, z chunks) can run as a
+// 1-D grid whose first `nb` CTAs take the tiles holding boundary cells -- bx0 / bx1 tile columns
+// at the low / high x end, by0 / by1 rows, bz0 / bz1 chunks -- and the rest the inner block. Each
+// boundary CTA, once its stores are done, increments `counter` (host-mapped memory); the host
+// calls the communication when the counter reaches nb, while the inner tiles still run. The
+// kernel never waits on the host. counter == NULL: an ordinary launch (blockIdx is the tile).
+struct TileOrder {
+    unsigned* counter;
+    int TX, TY, TZ;
+    int bx0, bx1, by0, by1, bz0, bz1;
+    int nb;
+};
+// Host: the order of a TX x TY x TZ tile launch whose tiles start at cell lo + t * tile (per
+// axis) over the cells [lo, end); boundary cells are c < lo_end or c >= hi_start.
+TileOrder make_tile_order(const int64_t ntiles[3], const int64_t lo[3], const int64_t tile[3], const int64_t end[3],
+                          const int64_t lo_end[3], const int64_t hi_start[3], unsigned* counter);
+// What a caller asks of a boundary-first launch (the launcher fills nb).
+struct HideReq {
+    int64_t lo_end[3], hi_start[3];
+    unsigned* counter;
+    int nb;
+};
+// Host: the thread's host-mapped progress word (allocated on first use; NULL pointers if the
+// device cannot map host memory).
+int progress_word(volatile unsigned** host, unsigned** dev);
+
+__device__ __forceinline__ uint3 ordered_tile(const TileOrder& o) {
+    if (!o.counter) return make_uint3(blockIdx.x, blockIdx.y, blockIdx.z);
+    int i = (int)blockIdx.x;
+    const int IX = o.TX - o.bx0 - o.bx1, IY = o.TY - o.by0 - o.by1;
+    if (i >= o.nb) {  // the inner block, x fastest
+        i -= o.nb;
+        return make_uint3(o.bx0 + i % IX, o.by0 + (i / IX) % IY, o.bz0 + i / (IX * IY));
+    }
+    const int layer = o.TX * o.TY;
+    const int nzfull = (o.bz0 + o.bz1) * layer;
+    if (i < nzfull) {  // whole layers at both z ends
+        const int l = i / layer, r = i % layer;
+        return make_uint3(r % o.TX, r / o.TX, l < o.bz0 ? l : o.TZ - o.bz1 + (l - o.bz0));
+    }
+    i -= nzfull;  // the frames of the middle layers: whole rows at both y ends, then column ends
+    const int frame = layer - IX * IY;
+    const int z = o.bz0 + i / frame;
+    int r = i % frame;
+    const int nyfull = (o.by0 + o.by1) * o.TX;
+    if (r < nyfull) {
+        const int row = r / o.TX;
+        return make_uint3(r % o.TX, row < o.by0 ? row : o.TY - o.by1 + (row - o.by0), z);
+    }
+    r -= nyfull;
+    const int ex = o.bx0 + o.bx1, c = r % ex;
+    return make_uint3(c < o.bx0 ? c : o.TX - o.bx1 + (c - o.bx0), o.by0 + r / ex, z);
+}
+
+// Called by every thread of a CTA after its last global store (plain stores only).
+__device__ __forceinline__ void ordered_tile_done(const TileOrder& o) {
+    if (!o.counter || (int)blockIdx.x >= o.nb) return;  // uniform over the CTA
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+        __threadfence_system();
+        atomicAdd_system(o.counter, 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Division by a number known on the host, correctly rounded.
+// ---------------------------------------------------------------------------------------
+// Markstein's method (P. W. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Develop. 34 (1990) 111-119): with y = RN(1/b) and a quotient
+// q within one ulp of a/b, the remainder r = a - b q is exact in one FMA and RN(q + r y) = RN(a/b).
+// The first quotient RN(a y) can be 1.5 ulps off, so one FMA correction brings it within an ulp and
+// a second gives the correctly rounded quotient: 1 multiply + 4 FMAs against the general division's
+// reciprocal iteration and slow-path test. Dividends outside [lo, hi] (tiny, huge, non-finite; zero
+// is a * y, with the quotient's sign) take the IEEE division; for divisors outside [2^-20, 2^20]
+// (FP32) or [2^-60, 2^60] (FP64) the host sets lo > hi and every division takes it. Results equal
+// a / b bit for bit (checked against the IEEE division by ps_check_division).
+template <typename T>
+struct DivC {
+    T b, y, lo, hi;
+};
+template <typename T>
+inline DivC<T> make_div(T b) {
+    const T lim = sizeof(T) == 4 ? (T)0x1p20 : (T)0x1p60;
+    const T a = b < 0 ? -b : b;
+    DivC<T> d;
+    d.b = b;
+    if (a >= 1 / lim && a <= lim) {
+        d.y = (T)1 / b;
+        d.lo = sizeof(T) == 4 ? (T)0x1p-70 : (T)0x1p-900;
+        d.hi = sizeof(T) == 4 ? (T)0x1p70 : (T)0x1p900;
+    } else {
+        d.y = 0;
+        d.lo = 1;
+        d.hi = 0;
+    }
+    return d;
+}
+__device__ __forceinline__ float div_c(float a, const DivC<float>& d) {
+    const float aa = fabsf(a);
+    if (aa >= d.lo && aa <= d.hi) {
+        float q = a * d.y;
+        float r = fmaf(-q, d.b, a);
+        q = fmaf(r, d.y, q);
+        r = fmaf(-q, d.b, a);
+        return fmaf(r, d.y, q);
+    }
+    return (aa == 0.0f && d.lo <= d.hi) ? a * d.y : a / d.b;
+}
+__device__ __forceinline__ double div_c(double a, const DivC<double>& d) {
+    const double aa = fabs(a);
+    if (aa >= d.lo && aa <= d.hi) {
+        double q = a * d.y;
+        double r = fma(-q, d.b, a);
+        q = fma(r, d.y, q);
+        r = fma(-q, d.b, a);
+        return fma(r, d.y, q);
+    }
+    return (aa == 0.0 && d.lo <= d.hi) ? a * d.y : a / d.b;
+}
+
+// a / h for statement helpers used with a plain divisor (host or device) or a DivC (device)
+template <typename T>
+__host__ __device__ __forceinline__ T dvd(T a, T h) {
+    return a / h;
+}
+template <typename T>
+__device__ __forceinline__ T dvd(T a, const DivC<T>& h) {
+    return div_c(a, h);
 }
 
 // ---------------------------------------------------------------------------------------

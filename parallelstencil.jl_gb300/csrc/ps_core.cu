@@ -61,6 +61,71 @@ thread_local PinnedWords t_pinned;
 constexpr size_t kPinnedWordBytes = 256;
 }  // namespace
 
+namespace {
+struct MappedWord {
+    unsigned* h = nullptr;
+    bool tried = false;
+    ~MappedWord() {
+        if (h) cudaFreeHost(h);
+    }
+};
+thread_local MappedWord t_mapped;
+}  // namespace
+
+int progress_word(volatile unsigned** host, unsigned** dev) {
+    *host = nullptr;
+    *dev = nullptr;
+    if (!t_mapped.tried) {
+        t_mapped.tried = true;
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, 64, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+            cudaGetLastError();
+            return PS_OK;
+        }
+        t_mapped.h = static_cast<unsigned*>(p);
+    }
+    if (!t_mapped.h) return PS_OK;
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, t_mapped.h, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return PS_OK;
+    }
+    *host = t_mapped.h;
+    *dev = static_cast<unsigned*>(d);
+    return PS_OK;
+}
+
+TileOrder make_tile_order(const int64_t ntiles[3], const int64_t lo[3], const int64_t tile[3], const int64_t end[3],
+                          const int64_t lo_end[3], const int64_t hi_start[3], unsigned* counter) {
+    int64_t b0[3], b1[3];
+    for (int d = 0; d < 3; ++d) {
+        // tiles holding a cell c < lo_end[d], and tiles holding a cell c >= hi_start[d]
+        b0[d] = lo_end[d] > lo[d] ? (lo_end[d] - lo[d] + tile[d] - 1) / tile[d] : 0;
+        const int64_t first_hi = hi_start[d] > lo[d] ? (hi_start[d] - lo[d]) / tile[d] : 0;
+        b1[d] = hi_start[d] < end[d] ? ntiles[d] - first_hi : 0;
+        if (b0[d] > ntiles[d]) b0[d] = ntiles[d];
+        if (b1[d] < 0) b1[d] = 0;
+        if (b0[d] + b1[d] >= ntiles[d]) {  // every tile along this axis holds boundary cells
+            b0[d] = ntiles[d];
+            b1[d] = 0;
+        }
+    }
+    TileOrder o{};
+    o.counter = counter;
+    o.TX = (int)ntiles[0];
+    o.TY = (int)ntiles[1];
+    o.TZ = (int)ntiles[2];
+    o.bx0 = (int)b0[0];
+    o.bx1 = (int)b1[0];
+    o.by0 = (int)b0[1];
+    o.by1 = (int)b1[1];
+    o.bz0 = (int)b0[2];
+    o.bz1 = (int)b1[2];
+    const int64_t inner = (ntiles[0] - b0[0] - b1[0]) * (ntiles[1] - b0[1] - b1[1]) * (ntiles[2] - b0[2] - b1[2]);
+    o.nb = (int)(ntiles[0] * ntiles[1] * ntiles[2] - inner);
+    return o;
+}
+
 int read_device_words(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     if (!t_pinned.tried) {
         t_pinned.tried = true;
@@ -186,11 +251,94 @@ int encode_bf16_rows_sw128(CUtensorMap* map, const void* ptr, uint64_t cols, uin
     return PS_OK;
 }
 
+// ps_check_division: div_c against the IEEE division. Dividend i: FP32 -- significand i mod 2^23,
+// exponent and sign from i / 2^23 (every significand in each listed binade, both signs); FP64 --
+// a hashed 52-bit significand, exponent and sign from the hash too. The first 64 indices are
+// special values (zeros, subnormals, extremes, infinities, NaN).
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+__constant__ int c_exp32[12] = {-126, -100, -71, -70, -69, -1, 0, 1, 69, 70, 71, 127};
+__constant__ int c_exp64[12] = {-1022, -950, -901, -900, -899, -1, 0, 1, 899, 900, 901, 1023};
+
+template <typename T>
+__device__ T special_dividend(int i) {
+    const T v[16] = {(T)0, -(T)0, (T)1, -(T)1, (T)INFINITY, -(T)INFINITY, (T)NAN,
+                     sizeof(T) == 4 ? (T)1e-40f : (T)1e-310, sizeof(T) == 4 ? (T)-1e-45f : (T)-4e-324,
+                     sizeof(T) == 4 ? (T)3.4e38f : (T)1.7e308, sizeof(T) == 4 ? (T)1.17549435e-38f : (T)2.2250738585072014e-308,
+                     (T)3, (T)0.1, (T)-7.5, (T)1e10, (T)-1e-10};
+    return v[i & 15];
+}
+
+__global__ void check_div32_kernel(DivC<float> d, unsigned long long* bad) {
+    const int64_t n = 12LL * 2 * (1LL << 23);
+    unsigned long long local = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float a;
+        if (i < 64) {
+            a = special_dividend<float>((int)i);
+        } else {
+            const unsigned m = (unsigned)(i & ((1 << 23) - 1));
+            const int64_t k = i >> 23;
+            const int e = c_exp32[(k >> 1) % 12];
+            a = ldexpf(1.0f + (float)m * 0x1p-23f, e) * ((k & 1) ? -1.0f : 1.0f);
+        }
+        const float q1 = div_c(a, d), q2 = a / d.b;
+        if (__float_as_uint(q1) != __float_as_uint(q2) && !(isnan(q1) && isnan(q2))) ++local;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+__global__ void check_div64_kernel(DivC<double> d, int64_t n, uint64_t seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a;
+        if (i < 64) {
+            a = special_dividend<double>((int)i);
+        } else {
+            const uint64_t h = mix64(seed ^ (uint64_t)i * 0x9e3779b97f4a7c15ull);
+            const int e = c_exp64[(h >> 52) % 12];
+            a = ldexp(1.0 + (double)(h & ((1ull << 52) - 1)) * 0x1p-52, e) * ((h >> 63) ? -1.0 : 1.0);
+        }
+        const double q1 = div_c(a, d), q2 = a / d.b;
+        if (__double_as_longlong(q1) != __double_as_longlong(q2) && !(isnan(q1) && isnan(q2))) ++local;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
 }  // namespace ps
 
 using namespace ps;
 
 extern "C" {
+
+int ps_check_division(double b, int32_t dtype, int64_t n, uint64_t seed, int64_t* mismatches, void* stream) {
+    DeviceState* st = nullptr;
+    PS_TRY(current_state(&st));
+    if (!mismatches) return fail(PS_ERR_NULL, "ps_check_division: NULL output");
+    if (dtype != PS_F32 && dtype != PS_F64) return fail(PS_ERR_DTYPE, "ps_check_division: dtype %d", dtype);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned long long* bad = nullptr;
+    PS_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&bad), sizeof(*bad), s));
+    PS_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(*bad), s));
+    const unsigned grid = (unsigned)st->num_sms * 8;
+    if (dtype == PS_F32)
+        check_div32_kernel<<<grid, 256, 0, s>>>(make_div<float>((float)b), bad);
+    else
+        check_div64_kernel<<<grid, 256, 0, s>>>(make_div<double>(b), n, seed, bad);
+    unsigned long long h = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(bad, s);
+    if (e != cudaSuccess) return cuda_fail(e, "ps_check_division");
+    *mismatches = (int64_t)h;
+    return PS_OK;
+}
 
 int ps_abi_version(void) { return PS_ABI_VERSION; }
 
@@ -251,6 +399,7 @@ int ps_finalize(void) {
     stokes2d_free_scratch();
     diffusion_free_scratch();
     adjoint_free_scratch();
+    acoustic_free_scratch();
     stokes2d_static_forget();
     for (int d = 0; d < kMaxDevices; d++) {
         DeviceState& st = g_dev[d];

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
                                                                   const __grid_constant__ CUtensorMap mC,
                                                                   double* __restrict__ T2, SplitParams p, int64_t nx,
                                                                   int64_t ny, Box cb, int L, int* __restrict__ err,
-                                                                  const int* __restrict__ pred) {
+                                                                  const int* __restrict__ pred, TileOrder ord) {
     // pred (may be NULL): the launch runs only if *pred is set -- the device-side fallback of a
     // fixed-grid run whose values left the grid
     if (pred && !*reinterpret_cast<const volatile int*>(pred)) return;
@@ -85,9 +85,10 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * C::STAGE + 2 * C::FACE);
 
     const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
-    const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + blockIdx.x * SP_TX;
-    const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
-    const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
+    const uint3 tile = ordered_tile(ord);
+    const int X0 = (int)(cb.lo[0] & ~(int64_t)1) + (int)tile.x * SP_TX;
+    const int Y0 = (int)cb.lo[1] + (int)tile.y * TY;
+    const int Z0 = (int)cb.lo[2] + (int)tile.z * L;
     const int nk = min(L, (int)cb.hi[2] - Z0);
     const int nq = nk + 2;
 
@@ -291,6 +292,7 @@ __global__ void __launch_bounds__(32 * TY, MINB) diff3d_split_tma(const __grid_c
         rawTc = rawTz;
     }
     if (__syncthreads_or(big) && tid == 0) atomicOr(err, DEV_ERR_RANGE);
+    ordered_tile_done(ord);
 }
 
 static void split_const(dd& d, double v) {
@@ -302,7 +304,7 @@ static void split_const(dd& d, double v) {
 template <bool LAM, bool ISO, bool PRE, bool STATE>
 static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const ps_array* lam, const ps_array& T2,
                                 const SplitParams& p, const Box& cb, int L, cudaStream_t s, int* d_err,
-                                const int* pred) {
+                                const int* pred, HideReq* hr) {
     constexpr int TY = 8, S = 4, MINB = 3;
     using C = SplitCfg<LAM, TY, S>;
     CUtensorMap mT, mL, mC;
@@ -327,21 +329,30 @@ static int launch_split_variant(const ps_array& Tin, const ps_array& Ci, const p
         PS_TRY(current_state(&st));
         L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
     }
-    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    const int64_t bz = (cb.hi[2] - cb.lo[2] + L - 1) / L;
+    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)bz);
+    TileOrder ord{};
+    if (hr) {  // boundary tiles first, as one 1-D grid
+        const int64_t nt[3] = {bx, by, bz}, lo[3] = {x0, cb.lo[1], cb.lo[2]}, tl[3] = {SP_TX, TY, L};
+        const int64_t end[3] = {cb.hi[0], cb.hi[1], cb.hi[2]};
+        ord = make_tile_order(nt, lo, tl, end, hr->lo_end, hr->hi_start, hr->counter);
+        hr->nb = ord.nb;
+        grd = dim3((unsigned)(bx * by * bz), 1, 1);
+    }
     diff3d_split_tma<LAM, ISO, TY, S, MINB, PRE, STATE><<<grd, blk, C::SMEM, s>>>(
-        mT, mL, mC, static_cast<double*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err, pred);
+        mT, mL, mC, static_cast<double*>(T2.ptr), p, T2.n[0], T2.n[1], cb, L, d_err, pred, ord);
     return PS_OK;
 }
 
 template <bool LAM, bool ISO>
 static int launch_split_flags(bool pre, bool state, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                               const ps_array& T2, const SplitParams& p, const Box& cb, int L, cudaStream_t s,
-                              int* d_err, const int* pred) {
+                              int* d_err, const int* pred, HideReq* hr) {
     if (pre)
-        return state ? launch_split_variant<LAM, ISO, true, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
-                     : launch_split_variant<LAM, ISO, true, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
-    return state ? launch_split_variant<LAM, ISO, false, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
-                 : launch_split_variant<LAM, ISO, false, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
+        return state ? launch_split_variant<LAM, ISO, true, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr)
+                     : launch_split_variant<LAM, ISO, true, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr);
+    return state ? launch_split_variant<LAM, ISO, false, true>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr)
+                 : launch_split_variant<LAM, ISO, false, false>(Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr);
 }
 
 // Per-dimension coefficients of the forms (split into p->c) and the common factor g: the
@@ -369,7 +380,7 @@ static bool split_coeffs(int form, double lam_s, double dt, double hx, double hy
 // then uses the IEEE kernels).
 static int launch_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                         double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L, bool pre,
-                        bool state, cudaStream_t s, int* d_err, const int* pred = nullptr) {
+                        bool state, cudaStream_t s, int* d_err, const int* pred = nullptr, HideReq* hr = nullptr) {
     bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
     if (!tma || T2.dtype != PS_F64) return PS_ERR_UNSUPPORTED;
     SplitParams p{};
@@ -377,16 +388,16 @@ static int launch_split(int form, const ps_array& T2, const ps_array& Tin, const
     const bool iso = split_coeffs(form, lam_s, dt, hx, hy, hz, &p, &g);
     split_const(p.g, g);
     if (form == PS_DIFF_FLUX_LAM)
-        return iso ? launch_split_flags<true, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
-                   : launch_split_flags<true, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
-    return iso ? launch_split_flags<false, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred)
-               : launch_split_flags<false, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred);
+        return iso ? launch_split_flags<true, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr)
+                   : launch_split_flags<true, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr);
+    return iso ? launch_split_flags<false, true>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr)
+               : launch_split_flags<false, false>(pre, state, Tin, Ci, lam, T2, p, cb, L, s, d_err, pred, hr);
 }
 
 int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                            double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
-                           cudaStream_t s, int* d_err) {
-    return launch_split(form, T2, Tin, Ci, lam, lam_s, dt, hx, hy, hz, cb, L, false, false, s, d_err);
+                           cudaStream_t s, int* d_err, HideReq* hr) {
+    return launch_split(form, T2, Tin, Ci, lam, lam_s, dt, hx, hy, hz, cb, L, false, false, s, d_err, nullptr, hr);
 }
 
 // =======================================================================================
@@ -1478,7 +1489,7 @@ using namespace ps;
 namespace ps {
 int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam,
                   double lam_s, double dt, double hx, double hy, double hz, const Box& thread_box, int memopt,
-                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err);
+                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err, HideReq* hr = nullptr);
 int diffusion_args(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam);
 }
 

@@ -15,6 +15,7 @@
 #include <nvrtc.h>
 #include <string.h>
 
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -35,6 +36,9 @@ struct ps_jit_args {
                        // 4 a value outside the split FP64 range
     long long smem;    // dynamic shared memory bytes of this launch (@sharedMem views are checked against it)
     long long loop;    // indices per thread along the sweep dimension of a sweep (memopt) kernel; 1 otherwise
+    unsigned* ocnt;    // boundary-first launch (ps_jit_hide_communication): host-mapped count of finished
+                       // boundary blocks; NULL for an ordinary launch
+    int ord[10];       // its tile order: blocks per axis, boundary blocks at both ends of each axis, their count
 };
 
 typedef CUresult (*ModuleLoadDataFn)(CUmodule*, const void*);
@@ -141,9 +145,15 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
     return ps_jit_launch_ex(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, 0, nullptr, stream, sync);
 }
 
-int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
-                     const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
-                     const int32_t loop[3], void* stream, int sync) {
+}  // extern "C"
+
+namespace ps {
+
+// Validates a launch and fills its argument block and grid (gd: blocks per axis; all zero when a
+// count is zero).
+static int jit_prepare(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                       const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
+                       const int32_t loop[3], JitKernel** kout, ps_jit_args* g, int64_t gd[3], int32_t lp[3]) {
     DeviceState* st = nullptr;
     PS_TRY(current_state(&st));
     if (!kernel || !lo || !count || !threads) return fail(PS_ERR_NULL, "ps_jit_launch: NULL argument");
@@ -152,7 +162,7 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
         return fail(PS_ERR_ARG, "ps_jit_launch: threads per block must be >= 1 and at most 1024 (z <= 64)");
     if (shmem < 0 || shmem > 227 * 1024)
         return fail(PS_ERR_ARG, "ps_jit_launch: shmem must be 0 to 232448 bytes (227 KB)");
-    int32_t lp[3] = {1, 1, 1};
+    lp[0] = lp[1] = lp[2] = 1;
     int nsweep = 0;
     for (int d = 0; d < 3 && loop; d++) {
         lp[d] = loop[d];
@@ -168,51 +178,135 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
     int dev = -1;
     cudaGetDevice(&dev);
     if (dev != k->device) return fail(PS_ERR_ARG, "ps_jit_launch: kernel compiled for device %d", k->device);
-    ps_jit_args g;
-    memset(&g, 0, sizeof(g));
+    memset(g, 0, sizeof(*g));
     for (int i = 0; i < narrays; i++) {
         PS_TRY(check_array(arrays[i], "jit argument"));
         if (i && arrays[i].dtype != arrays[0].dtype) return fail(PS_ERR_DTYPE, "ps_jit_launch: mixed dtypes");
-        g.a[i] = arrays[i].ptr;
-        for (int d = 0; d < 3; d++) g.n[i][d] = arrays[i].n[d];
+        g->a[i] = arrays[i].ptr;
+        for (int d = 0; d < 3; d++) g->n[i][d] = arrays[i].n[d];
     }
-    for (int i = 0; i < nscalars; i++) g.s[i] = scalars[i];
+    for (int i = 0; i < nscalars; i++) g->s[i] = scalars[i];
     for (int d = 0; d < 3; d++) {
         if (lo[d] < 0 || count[d] < 0) return fail(PS_ERR_ARG, "ps_jit_launch: negative range");
-        g.lo[d] = lo[d];
-        g.cnt[d] = count[d];
+        g->lo[d] = lo[d];
+        g->cnt[d] = count[d];
     }
-    g.err = k->err;
-    g.smem = shmem;
-    g.loop = lp[0] * lp[1] * lp[2];  // the one loop count > 1, if any
-    if (count[0] == 0 || count[1] == 0 || count[2] == 0) return PS_OK;
-    int64_t gd[3];
-    for (int d = 0; d < 3; d++) gd[d] = (count[d] + (int64_t)threads[d] * lp[d] - 1) / ((int64_t)threads[d] * lp[d]);
-    const int64_t gx = gd[0], gy = gd[1], gz = gd[2];
-    if (gx > 2147483647LL || gy > 65535 || gz > 65535) return fail(PS_ERR_SHAPE, "ps_jit_launch: grid too large");
+    g->err = k->err;
+    g->smem = shmem;
+    g->loop = lp[0] * lp[1] * lp[2];  // the one loop count > 1, if any
+    for (int d = 0; d < 3; d++)
+        gd[d] = count[0] == 0 || count[1] == 0 || count[2] == 0
+                    ? 0
+                    : (count[d] + (int64_t)threads[d] * lp[d] - 1) / ((int64_t)threads[d] * lp[d]);
     if (shmem > k->smem_opt_in) {
         if (g_setattr(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)shmem) != CUDA_SUCCESS)
             return fail(PS_ERR_ARG, "ps_jit_launch: %lld bytes of dynamic shared memory not available", (long long)shmem);
         k->smem_opt_in = (int)shmem;
     }
-    void* params[] = {&g};
-    const CUresult r = g_launch(k->fn, (unsigned)gx, (unsigned)gy, (unsigned)gz, (unsigned)threads[0], (unsigned)threads[1],
-                                (unsigned)threads[2], (unsigned)shmem, static_cast<CUstream>(stream), params, nullptr);
-    if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "ps_jit_launch: cuLaunchKernel failed (CUresult %d)", (int)r);
-    PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), sync, "ps_jit_launch"));
-    if (!sync) return PS_OK;
-    int flag = 0;  // the stream is idle here; flags of earlier asynchronous launches are reported too
+    *kout = k;
+    return PS_OK;
+}
+
+// Reads (and clears) the kernel's error flags; the stream is idle.
+static int jit_flags(JitKernel* k, const char* what) {
+    int flag = 0;
     if (cudaMemcpy(&flag, k->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return fail(PS_ERR_CUDA, "ps_jit_launch: reading the error flag failed");
+        return fail(PS_ERR_CUDA, "%s: reading the error flag failed", what);
     if (flag) {
         cudaMemset(k->err, 0, sizeof(int));
-        if (flag & 1) return fail(PS_ERR_ARG, "ps_jit_launch: out-of-bounds array access in the kernel (BoundsError)");
+        if (flag & 1) return fail(PS_ERR_ARG, "%s: out-of-bounds array access in the kernel (BoundsError)", what);
         if (flag & 4)
-            return fail(PS_ERR_UNSUPPORTED, "ps_jit_launch: a value outside the split FP64 arithmetic's range "
-                                            "(|x| >= 2^128); run the kernel with fp64 = ieee");
-        return fail(PS_ERR_ARG, "ps_jit_launch: a kernel with @sync_threads, shuffles or votes needs ranges that are "
-                                "a multiple of the thread block; a partial block did not run");
+            return fail(PS_ERR_UNSUPPORTED, "%s: a value outside the split FP64 arithmetic's range "
+                                            "(|x| >= 2^128); run the kernel with fp64 = ieee", what);
+        return fail(PS_ERR_ARG, "%s: a kernel with @sync_threads, shuffles or votes needs ranges that are "
+                                "a multiple of the thread block; a partial block did not run", what);
     }
+    return PS_OK;
+}
+
+static int jit_cu_launch(JitKernel* k, unsigned gx, unsigned gy, unsigned gz, const int32_t threads[3], int64_t shmem,
+                         ps_jit_args* g, void* stream) {
+    void* params[] = {g};
+    const CUresult r = g_launch(k->fn, gx, gy, gz, (unsigned)threads[0], (unsigned)threads[1], (unsigned)threads[2],
+                                (unsigned)shmem, static_cast<CUstream>(stream), params, nullptr);
+    if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "ps_jit_launch: cuLaunchKernel failed (CUresult %d)", (int)r);
+    return PS_OK;
+}
+
+}  // namespace ps
+
+extern "C" {
+
+int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                     const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
+                     const int32_t loop[3], void* stream, int sync) {
+    JitKernel* k = nullptr;
+    ps_jit_args g;
+    int64_t gd[3];
+    int32_t lp[3];
+    PS_TRY(jit_prepare(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, shmem, loop, &k, &g, gd, lp));
+    if (gd[0] == 0) return PS_OK;
+    if (gd[0] > 2147483647LL || gd[1] > 65535 || gd[2] > 65535) return fail(PS_ERR_SHAPE, "ps_jit_launch: grid too large");
+    PS_TRY(jit_cu_launch(k, (unsigned)gd[0], (unsigned)gd[1], (unsigned)gd[2], threads, shmem, &g, stream));
+    PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), sync, "ps_jit_launch"));
+    if (!sync) return PS_OK;
+    return jit_flags(k, "ps_jit_launch");  // flags of earlier asynchronous launches are reported too
+}
+
+int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars,
+                              int32_t nscalars, const int64_t count[3], const int32_t threads[3], const int32_t loop[3],
+                              const int64_t bw[3], ps_comm_fn comm, void* comm_ctx, void* stream) {
+    const int64_t lo[3] = {0, 0, 0};
+    JitKernel* k = nullptr;
+    ps_jit_args g;
+    int64_t gd[3];
+    int32_t lp[3];
+    PS_TRY(jit_prepare(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, 0, loop, &k, &g, gd, lp));
+    if (!bw) return fail(PS_ERR_NULL, "ps_jit_hide_communication: NULL boundary width");
+    for (int d = 0; d < 3; d++) {  // validate_ranges_args (src/ParallelKernel/hide_communication.jl:396-403)
+        if (bw[d] < 0) return fail(PS_ERR_ARG, "boundary width must be >= 0");
+        if (!(count[d] > 2 * bw[d]))
+            return fail(PS_ERR_SHAPE, "@hide_communication: length(ranges) > 2*boundary_width violated");
+        if (count[d] > 1 && bw[d] == 0)
+            return fail(PS_ERR_SHAPE, "@hide_communication: boundary_width 0 in a dimension of length > 1");
+    }
+    if (gd[0] == 0) return PS_OK;
+    if (gd[0] * gd[1] * gd[2] > 2147483647LL) return fail(PS_ERR_SHAPE, "ps_jit_hide_communication: grid too large");
+    volatile unsigned* hc = nullptr;
+    unsigned* dc = nullptr;
+    PS_TRY(progress_word(&hc, &dc));
+    if (!dc) return fail(PS_ERR_UNSUPPORTED, "ps_jit_hide_communication: no host-mapped memory on this device");
+    // tiles: thread blocks (times the sweep length); boundary: thread indices t < bw or t >= count - bw,
+    // the reference's ranges_outer (src/ParallelKernel/hide_communication.jl:350-394)
+    const int64_t tl[3] = {(int64_t)threads[0] * lp[0], (int64_t)threads[1] * lp[1], (int64_t)threads[2] * lp[2]};
+    const int64_t end[3] = {count[0], count[1], count[2]}, hi[3] = {count[0] - bw[0], count[1] - bw[1], count[2] - bw[2]};
+    const TileOrder o = make_tile_order(gd, lo, tl, end, bw, hi, dc);
+    g.ocnt = dc;
+    const int ov[10] = {o.TX, o.TY, o.TZ, o.bx0, o.bx1, o.by0, o.by1, o.bz0, o.bz1, o.nb};
+    memcpy(g.ord, ov, sizeof(ov));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    *hc = 0u;
+    PS_TRY(jit_cu_launch(k, (unsigned)(gd[0] * gd[1] * gd[2]), 1, 1, threads, 0, &g, stream));
+    PS_TRY(finish_launch(s, 0, "ps_jit_hide_communication"));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (unsigned spin = 1; *hc < (unsigned)o.nb; ++spin) {
+        if (spin % 256 == 0) {
+            cudaError_t q = cudaStreamQuery(s);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return cuda_fail(q, "ps_jit_hide_communication");
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60)) {
+                PS_CUDA_TRY(cudaStreamSynchronize(s));
+                break;
+            }
+        }
+    }
+    const bool boundary_done = *hc >= (unsigned)o.nb;
+    int crc = PS_OK;
+    if (comm && boundary_done) crc = comm(comm_ctx);
+    PS_TRY(finish_launch(s, 1, "ps_jit_hide_communication(sync)"));
+    PS_TRY(jit_flags(k, "ps_jit_hide_communication"));
+    if (!boundary_done) return fail(PS_ERR_TIMEOUT, "ps_jit_hide_communication: boundary blocks not reported done");
+    if (crc != PS_OK) return fail(crc, "ps_jit_hide_communication: communication callback returned %d", crc);
     return PS_OK;
 }
 
@@ -222,19 +316,7 @@ int ps_jit_check(void* kernel, void* stream) {
     if (!kernel) return fail(PS_ERR_NULL, "ps_jit_check: NULL kernel");
     JitKernel* k = static_cast<JitKernel*>(kernel);
     PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), 1, "ps_jit_check"));
-    int flag = 0;
-    if (cudaMemcpy(&flag, k->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return fail(PS_ERR_CUDA, "ps_jit_check: reading the error flag failed");
-    if (flag) {
-        cudaMemset(k->err, 0, sizeof(int));
-        if (flag & 1) return fail(PS_ERR_ARG, "ps_jit_check: out-of-bounds array access in the kernel (BoundsError)");
-        if (flag & 4)
-            return fail(PS_ERR_UNSUPPORTED, "ps_jit_check: a value outside the split FP64 arithmetic's range "
-                                            "(|x| >= 2^128); run the kernel with fp64 = ieee");
-        return fail(PS_ERR_ARG, "ps_jit_check: a kernel with @sync_threads, shuffles or votes needs ranges that are "
-                                "a multiple of the thread block; a partial block did not run");
-    }
-    return PS_OK;
+    return jit_flags(k, "ps_jit_check");
 }
 
 int ps_jit_destroy(void* kernel) {

@@ -18,6 +18,8 @@
 // order, so FP64 results are bit-identical to the reference's CPU path.
 #include <algorithm>
 
+#include <chrono>
+
 #include "ps_common.cuh"
 
 namespace ps {
@@ -317,6 +319,7 @@ __global__ void memcopy_box(T* __restrict__ T2, const T* __restrict__ Tin, const
 template <typename T>
 struct DiffParams {
     T lam, dt, hx, hy, hz;
+    DivC<T> q[3];  // the divisors hx*hx, hy*hy, hz*hz of the `/dx^2` form
 };
 
 // One cell of the diffusion statement in form FORM (see ps_diffusion_form). Operation order
@@ -330,7 +333,7 @@ __device__ __forceinline__ T diff_cell(const DiffParams<T>& p, T Tc, T Txm, T Tx
         T d2z = (Tzp - Tc) - (Tc - Tzm);
         T s;
         if constexpr (FORM == PS_DIFF_DIV)
-            s = (d2x / (p.hx * p.hx) + d2y / (p.hy * p.hy)) + d2z / (p.hz * p.hz);
+            s = (div_c(d2x, p.q[0]) + div_c(d2y, p.q[1])) + div_c(d2z, p.q[2]);
         else
             s = (d2x * (p.hx * p.hx) + d2y * (p.hy * p.hy)) + d2z * (p.hz * p.hz);
         return Tc + p.dt * ((p.lam * ci) * s);
@@ -404,7 +407,8 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
                                                              const __grid_constant__ CUtensorMap mL,
                                                              const __grid_constant__ CUtensorMap mC,
                                                              T* __restrict__ T2, DiffParams<T> p, int64_t nx,
-                                                             int64_t ny, Box cb, int L, int* __restrict__ err) {
+                                                             int64_t ny, Box cb, int L, int* __restrict__ err,
+                                                             TileOrder ord) {
     using Z = ZSweep<T, FORM, TY, S>;
     constexpr int VEC = Z::VEC;
     using V = typename Vec<T>::type;
@@ -412,9 +416,10 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * Z::STAGE_BYTES);
 
     const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
-    const int X0 = (int)(cb.lo[0] & ~(int64_t)(VEC - 1)) + blockIdx.x * Z::TX;
-    const int Y0 = (int)cb.lo[1] + blockIdx.y * TY;
-    const int Z0 = (int)cb.lo[2] + blockIdx.z * L;
+    const uint3 tile = ordered_tile(ord);
+    const int X0 = (int)(cb.lo[0] & ~(int64_t)(VEC - 1)) + (int)tile.x * Z::TX;
+    const int Y0 = (int)cb.lo[1] + (int)tile.y * TY;
+    const int Z0 = (int)cb.lo[2] + (int)tile.z * L;
     const int nk = min(L, (int)cb.hi[2] - Z0);
     const int nq = nk + 2;  // planes Z0-1 .. Z0+nk
 
@@ -561,6 +566,7 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
         if (tid == 0)
             for (; next_q < min(nq, k + 2 + S); ++next_q) issue(next_q);
     }
+    ordered_tile_done(ord);
 }
 
 // --- z-sweep with thread-loaded planes (fallback for non-TMA-eligible arrays) ----------
@@ -618,7 +624,7 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_smem(T* __restrict__ T2
 // =======================================================================================
 template <typename T>
 __global__ void acoustic_v_kernel(T* __restrict__ Vx, T* __restrict__ Vy, T* __restrict__ Vz, const T* __restrict__ P,
-                                  int64_t nx, int64_t ny, int64_t nz, T dtr, T dx, T dy, T dz) {
+                                  int64_t nx, int64_t ny, int64_t nz, T dtr, DivC<T> dx, DivC<T> dy, DivC<T> dz) {
     // grid = (nx+1, ny+1, nz+1); each statement masked by @inn of its left-hand array.
     int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
@@ -628,25 +634,25 @@ __global__ void acoustic_v_kernel(T* __restrict__ Vx, T* __restrict__ Vy, T* __r
         if (tx < nx - 1 && ty < ny - 2 && tz < nz - 2) {  // @inn(Vx): Vx is (nx+1, ny, nz)
             int64_t v = (tx + 1) + (nx + 1) * ((ty + 1) + ny * (tz + 1));
             int64_t pc = (tx + 1) + sy * (ty + 1) + sz * (tz + 1);
-            Vx[v] = Vx[v] - (dtr * (P[pc] - P[pc - 1])) / dx;
+            Vx[v] = Vx[v] - div_c(dtr * (P[pc] - P[pc - 1]), dx);
         }
         if (tx < nx - 2 && ty < ny - 1 && tz < nz - 2) {  // @inn(Vy): Vy is (nx, ny+1, nz)
             int64_t v = (tx + 1) + nx * ((ty + 1) + (ny + 1) * (tz + 1));
             int64_t pc = (tx + 1) + sy * (ty + 1) + sz * (tz + 1);
-            Vy[v] = Vy[v] - (dtr * (P[pc] - P[pc - sy])) / dy;
+            Vy[v] = Vy[v] - div_c(dtr * (P[pc] - P[pc - sy]), dy);
         }
         if (tx < nx - 2 && ty < ny - 2 && tz < nz - 1) {  // @inn(Vz): Vz is (nx, ny, nz+1)
             int64_t v = (tx + 1) + nx * ((ty + 1) + ny * (tz + 1));
             int64_t pc = (tx + 1) + sy * (ty + 1) + sz * (tz + 1);
-            Vz[v] = Vz[v] - (dtr * (P[pc] - P[pc - sz])) / dz;
+            Vz[v] = Vz[v] - div_c(dtr * (P[pc] - P[pc - sz]), dz);
         }
     }
 }
 
 template <typename T>
 __global__ void acoustic_p_kernel(T* __restrict__ P, const T* __restrict__ Vx, const T* __restrict__ Vy,
-                                  const T* __restrict__ Vz, int64_t nx, int64_t ny, int64_t nz, T dtk, T dx, T dy,
-                                  T dz) {
+                                  const T* __restrict__ Vz, int64_t nx, int64_t ny, int64_t nz, T dtk, DivC<T> dx,
+                                  DivC<T> dy, DivC<T> dz) {
     int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
     if (ix >= nx || iy >= ny) return;
@@ -655,7 +661,7 @@ __global__ void acoustic_p_kernel(T* __restrict__ P, const T* __restrict__ Vx, c
         T ay = Vy[ix + nx * ((iy + 1) + (ny + 1) * iz)] - Vy[ix + nx * (iy + (ny + 1) * iz)];
         T az = Vz[ix + nx * (iy + ny * (iz + 1))] - Vz[ix + nx * (iy + ny * iz)];
         int64_t pc = ix + nx * (iy + ny * iz);
-        P[pc] = P[pc] - dtk * ((ax / dx + ay / dy) + az / dz);
+        P[pc] = P[pc] - dtk * ((div_c(ax, dx) + div_c(ay, dy)) + div_c(az, dz));
     }
 }
 
@@ -669,12 +675,13 @@ static dim3 grid3(int64_t wx, int64_t wy, int64_t wz, dim3 blk) {
 
 template <typename T>
 static DiffParams<T> diff_params(double lam, double dt, double hx, double hy, double hz) {
-    return DiffParams<T>{(T)lam, (T)dt, (T)hx, (T)hy, (T)hz};
+    const T x = (T)hx, y = (T)hy, z = (T)hz;
+    return DiffParams<T>{(T)lam, (T)dt, x, y, z, {make_div((T)(x * x)), make_div((T)(y * y)), make_div((T)(z * z))}};
 }
 
 int launch_diffusion_split(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                            double lam_s, double dt, double hx, double hy, double hz, const Box& cb, int L,
-                           cudaStream_t s, int* d_err);
+                           cudaStream_t s, int* d_err, HideReq* hr = nullptr);
 
 // z-sweep length (`loopsize`) of the shared-memory fallback when none is given: the reference
 // uses 64 on compute capability >= 9 (src/parallel.jl:532-543). The TMA z-sweeps choose theirs
@@ -683,7 +690,8 @@ static constexpr int kDefaultLoopsize = 64;
 
 template <typename T, int FORM, int TY, int S>
 static int launch_zsweep_tma(const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
-                             const DiffParams<T>& p, const Box& cb, int L, cudaStream_t s, int* d_err) {
+                             const DiffParams<T>& p, const Box& cb, int L, cudaStream_t s, int* d_err,
+                             HideReq* hr = nullptr) {
     using Z = ZSweep<T, FORM, TY, S>;
     CUtensorMap mT, mL, mC;
     PS_TRY(encode_plane_map(&mT, Tin, Z::PW, Z::PH));
@@ -707,18 +715,32 @@ static int launch_zsweep_tma(const ps_array& T2, const ps_array& Tin, const ps_a
         PS_TRY(current_state(&st));
         L = auto_loopsize(bx * by, cb.hi[2] - cb.lo[2], (int64_t)occ * st->num_sms);
     }
-    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)((cb.hi[2] - cb.lo[2] + L - 1) / L));
+    const int64_t bz = (cb.hi[2] - cb.lo[2] + L - 1) / L;
+    dim3 grd((unsigned)bx, (unsigned)by, (unsigned)bz);
+    TileOrder ord{};
+    if (hr) {  // boundary tiles first, as one 1-D grid
+        const int64_t nt[3] = {bx, by, bz}, lo[3] = {x0, cb.lo[1], cb.lo[2]}, tl[3] = {Z::TX, TY, L};
+        const int64_t end[3] = {cb.hi[0], cb.hi[1], cb.hi[2]};
+        ord = make_tile_order(nt, lo, tl, end, hr->lo_end, hr->hi_start, hr->counter);
+        hr->nb = ord.nb;
+        grd = dim3((unsigned)(bx * by * bz), 1, 1);
+    }
     diff3d_zsweep_tma<T, FORM, TY, S><<<grd, blk, Z::SMEM, s>>>(mT, mL, mC, static_cast<T*>(T2.ptr), p, T2.n[0],
-                                                                T2.n[1], cb, L, d_err);
+                                                                T2.n[1], cb, L, d_err, ord);
     return PS_OK;
 }
 
 template <typename T, int FORM>
 static int launch_diffusion(const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array* lam,
                             const DiffParams<T>& p, const Box& cb, int memopt, int loopsize, cudaStream_t s,
-                            int* d_err) {
+                            int* d_err, HideReq* hr = nullptr) {
     const int64_t wx = cb.hi[0] - cb.lo[0], wy = cb.hi[1] - cb.lo[1], wz = cb.hi[2] - cb.lo[2];
-    if (wx <= 0 || wy <= 0 || wz <= 0) return PS_OK;
+    if (wx <= 0 || wy <= 0 || wz <= 0) return hr ? PS_ERR_UNSUPPORTED : PS_OK;
+    if (hr) {  // boundary-first launches exist for the TMA z-sweep only
+        const bool tma = tma_eligible(T2) && tma_eligible(Tin) && tma_eligible(Ci) && (!lam || tma_eligible(*lam));
+        if (!memopt || !tma) return PS_ERR_UNSUPPORTED;
+        return launch_zsweep_tma<T, FORM, 8, 4>(T2, Tin, Ci, lam, p, cb, loopsize, s, d_err, hr);
+    }
     const T* lp = lam ? static_cast<const T*>(lam->ptr) : nullptr;
     int L = loopsize > 0 ? loopsize : kDefaultLoopsize;
     // A box under half a z-sweep tile wide (x) or high (y) -- e.g. 16-cell boundary slabs of
@@ -749,13 +771,18 @@ static int launch_diffusion(const ps_array& T2, const ps_array& Tin, const ps_ar
 template <typename T>
 static int dispatch_diffusion(int form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci,
                               const ps_array* lam, double lam_s, double dt, double hx, double hy, double hz,
-                              const Box& cb, int memopt, int loopsize, cudaStream_t s, int* d_err) {
+                              const Box& cb, int memopt, int loopsize, cudaStream_t s, int* d_err,
+                              HideReq* hr = nullptr) {
     DiffParams<T> p = diff_params<T>(lam_s, dt, hx, hy, hz);
     switch (form) {
-    case PS_DIFF_DIV: return launch_diffusion<T, PS_DIFF_DIV>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err);
-    case PS_DIFF_MUL: return launch_diffusion<T, PS_DIFF_MUL>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err);
-    case PS_DIFF_FLUX: return launch_diffusion<T, PS_DIFF_FLUX>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err);
-    case PS_DIFF_FLUX_LAM: return launch_diffusion<T, PS_DIFF_FLUX_LAM>(T2, Tin, Ci, lam, p, cb, memopt, loopsize, s, d_err);
+    case PS_DIFF_DIV:
+        return launch_diffusion<T, PS_DIFF_DIV>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err, hr);
+    case PS_DIFF_MUL:
+        return launch_diffusion<T, PS_DIFF_MUL>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err, hr);
+    case PS_DIFF_FLUX:
+        return launch_diffusion<T, PS_DIFF_FLUX>(T2, Tin, Ci, nullptr, p, cb, memopt, loopsize, s, d_err, hr);
+    case PS_DIFF_FLUX_LAM:
+        return launch_diffusion<T, PS_DIFF_FLUX_LAM>(T2, Tin, Ci, lam, p, cb, memopt, loopsize, s, d_err, hr);
     }
     return fail(PS_ERR_ARG, "ps_diffusion3d_step: unknown form %d", form);
 }
@@ -793,17 +820,18 @@ static Box inner_cells(const Box& tb, const int64_t n[3]) {
 
 int diffusion_box(int32_t form, const ps_array& T2, const ps_array& Tin, const ps_array& Ci, const ps_array& lam,
                   double lam_s, double dt, double hx, double hy, double hz, const Box& thread_box, int memopt,
-                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err) {
+                  int loopsize, int fp64_mode, cudaStream_t s, int* d_err, HideReq* hr = nullptr) {
     Box cb = inner_cells(thread_box, T2.n);
     const ps_array* lp = form == PS_DIFF_FLUX_LAM ? &lam : nullptr;
-    if (cb.hi[0] <= cb.lo[0] || cb.hi[1] <= cb.lo[1] || cb.hi[2] <= cb.lo[2]) return PS_OK;
+    if (cb.hi[0] <= cb.lo[0] || cb.hi[1] <= cb.lo[1] || cb.hi[2] <= cb.lo[2]) return hr ? PS_ERR_UNSUPPORTED : PS_OK;
     if (T2.dtype == PS_F64 && fp64_mode == PS_FP64_SPLIT) {
-        int rc = launch_diffusion_split(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, loopsize, s, d_err);
-        if (rc != PS_ERR_UNSUPPORTED) return rc;  // not TMA-eligible: IEEE kernels below
+        int rc = launch_diffusion_split(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, loopsize, s, d_err, hr);
+        if (rc != PS_ERR_UNSUPPORTED || hr) return rc;  // not TMA-eligible: IEEE kernels below
     }
     if (T2.dtype == PS_F64)
-        return dispatch_diffusion<double>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err);
-    return dispatch_diffusion<float>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err);
+        return dispatch_diffusion<double>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err,
+                                          hr);
+    return dispatch_diffusion<float>(form, T2, Tin, Ci, lp, lam_s, dt, hx, hy, hz, cb, memopt, loopsize, s, d_err, hr);
 }
 
 }  // namespace ps
@@ -943,6 +971,65 @@ int ps_diffusion3d_step(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_a
     return finish_launch(s, sync, "ps_diffusion3d_step");
 }
 
+}  // extern "C"
+
+namespace ps {
+namespace {
+thread_local cudaEvent_t t_order_event = nullptr;
+}
+
+// The boundary-first launch of ps_diffusion3d_step_split (memopt, TMA-eligible arrays); returns
+// PS_ERR_UNSUPPORTED (nothing launched) when it does not apply.
+static int ordered_step(int32_t form, const ps_array& T2, const ps_array& T, const ps_array& Ci,
+                        const ps_array& lam_arr, double lam, double dt, double hx, double hy, double hz,
+                        const int64_t bw[3], int fp64_mode, cudaStream_t sb, cudaStream_t si, ps_comm_fn comm,
+                        void* comm_ctx, DeviceState* st) {
+    volatile unsigned* hc = nullptr;
+    unsigned* dc = nullptr;
+    PS_TRY(progress_word(&hc, &dc));
+    if (!dc) return PS_ERR_UNSUPPORTED;
+    HideReq hr{};
+    for (int d = 0; d < 3; ++d) {
+        hr.lo_end[d] = bw[d] + 1;
+        hr.hi_start[d] = T2.n[d] - 1 - bw[d];
+    }
+    hr.counter = dc;
+    if (sb != si) {  // the launch follows the work already queued on both streams
+        if (!t_order_event) PS_CUDA_TRY(cudaEventCreateWithFlags(&t_order_event, cudaEventDisableTiming));
+        PS_CUDA_TRY(cudaEventRecord(t_order_event, sb));
+        PS_CUDA_TRY(cudaStreamWaitEvent(si, t_order_event, 0));
+    }
+    *hc = 0u;
+    const Box full = {{0, 0, 0}, {T2.n[0], T2.n[1], T2.n[2]}};
+    int rc = diffusion_box(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, full, 1, 0, fp64_mode, si, st->d_err, &hr);
+    if (rc != PS_OK) return rc;
+    PS_TRY(finish_launch(si, 0, "ps_diffusion3d_step_split"));
+    // wait for the boundary tiles (bounded; a kernel that ended early is reported by the sync below)
+    const auto t0 = std::chrono::steady_clock::now();
+    for (unsigned spin = 1; *hc < (unsigned)hr.nb; ++spin) {
+        if (spin % 256 == 0) {
+            cudaError_t q = cudaStreamQuery(si);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return cuda_fail(q, "ps_diffusion3d_step_split");
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60)) {
+                PS_CUDA_TRY(cudaStreamSynchronize(si));
+                break;
+            }
+        }
+    }
+    const bool boundary_done = *hc >= (unsigned)hr.nb;
+    int crc = PS_OK;
+    if (comm && boundary_done) crc = comm(comm_ctx);
+    PS_TRY(finish_launch(si, 1, "ps_diffusion3d_step_split(sync)"));
+    if (!boundary_done) return fail(PS_ERR_TIMEOUT, "ps_diffusion3d_step_split: boundary tiles not reported done");
+    if (crc != PS_OK) return fail(crc, "ps_diffusion3d_step_split: communication callback returned %d", crc);
+    return PS_OK;
+}
+
+}  // namespace ps
+
+extern "C" {
+
 int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci, ps_array lam_arr, double lam,
                               double dt, double hx, double hy, double hz, const ps_launch* cfg, const int64_t bw[3],
                               void* s_boundary, void* s_inner, ps_comm_fn comm, void* comm_ctx) {
@@ -962,6 +1049,16 @@ int ps_diffusion3d_step_split(int32_t form, ps_array T2, ps_array T, ps_array Ci
     }
     if (!any_gt1) return fail(PS_ERR_SHAPE, "@hide_communication: all ranges have length 1");
     cudaStream_t sb = static_cast<cudaStream_t>(s_boundary), si = static_cast<cudaStream_t>(s_inner);
+    if (memopt) {
+        // One TMA z-sweep launch on s_inner whose first CTAs take the tiles holding boundary cells
+        // (cells 1 .. bw and n-1-bw .. n-2 of each axis: the reference's boundary ranges, whose
+        // high end in @inn(T2) cells is n-bw+1 .. n-2, plus the planes a halo exchange sends).
+        // Each such CTA counts itself in host-mapped memory after its stores; `comm` runs once
+        // all have, while the inner tiles still run. No second launch, no tile cut twice.
+        int rc = ordered_step(form, T2, T, Ci, lam_arr, lam, dt, hx, hy, hz, bw, fp64_mode, sb, si, comm, comm_ctx,
+                              st);
+        if (rc != PS_ERR_UNSUPPORTED) return rc;  // otherwise the boundary slabs as separate launches below
+    }
     // Boundary widths below (lw) and above (hw) the inner box. With the z-sweep kernels the x and y
     // slabs are widened to whole sweep tiles (x: 64 FP64 / 128 FP32 cells from an even cell, y: 8
     // rows): a slab narrower than a tile costs the whole tile anyway, and an inner box that starts
@@ -1028,11 +1125,13 @@ int ps_acoustic3d_v(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P, double dt
     if (P.dtype == PS_F64)
         acoustic_v_kernel<double><<<grd, blk, 0, s>>>(static_cast<double*>(Vx.ptr), static_cast<double*>(Vy.ptr),
                                                       static_cast<double*>(Vz.ptr), static_cast<const double*>(P.ptr),
-                                                      nx, ny, nz, dt / rho, dx, dy, dz);
+                                                      nx, ny, nz, dt / rho, make_div(dx), make_div(dy),
+                                                      make_div(dz));
     else
         acoustic_v_kernel<float><<<grd, blk, 0, s>>>(static_cast<float*>(Vx.ptr), static_cast<float*>(Vy.ptr),
                                                      static_cast<float*>(Vz.ptr), static_cast<const float*>(P.ptr), nx,
-                                                     ny, nz, (float)dt / (float)rho, (float)dx, (float)dy, (float)dz);
+                                                     ny, nz, (float)dt / (float)rho, make_div((float)dx),
+                                                     make_div((float)dy), make_div((float)dz));
     return finish_launch(s, sync, "ps_acoustic3d_v");
 }
 
@@ -1057,11 +1156,13 @@ int ps_acoustic3d_p(ps_array P, ps_array Vx, ps_array Vy, ps_array Vz, double dt
     if (P.dtype == PS_F64)
         acoustic_p_kernel<double><<<grd, blk, 0, s>>>(static_cast<double*>(P.ptr), static_cast<const double*>(Vx.ptr),
                                                       static_cast<const double*>(Vy.ptr),
-                                                      static_cast<const double*>(Vz.ptr), nx, ny, nz, dt * k, dx, dy, dz);
+                                                      static_cast<const double*>(Vz.ptr), nx, ny, nz, dt * k,
+                                                      make_div(dx), make_div(dy), make_div(dz));
     else
         acoustic_p_kernel<float><<<grd, blk, 0, s>>>(static_cast<float*>(P.ptr), static_cast<const float*>(Vx.ptr),
                                                      static_cast<const float*>(Vy.ptr), static_cast<const float*>(Vz.ptr),
-                                                     nx, ny, nz, (float)dt * (float)k, (float)dx, (float)dy, (float)dz);
+                                                     nx, ny, nz, (float)dt * (float)k, make_div((float)dx),
+                                                     make_div((float)dy), make_div((float)dz));
     return finish_launch(s, sync, "ps_acoustic3d_p");
 }
 

@@ -41,36 +41,39 @@ template <typename T>
 __host__ __device__ __forceinline__ T s2_dtPt(T Ptsc, T mus, T max_nxy) {
     return ((Ptsc * T(4.1)) * mus) / max_nxy;
 }
-template <typename T>
-__host__ __device__ __forceinline__ T s2_divV(T vx0, T vx1, T vy0, T vy1, T dx, T dy) {
-    return (vx1 - vx0) / dx + (vy1 - vy0) / dy;
+// H: the divisor's type -- T, or DivC<T> (the correctly rounded division by a host-known number)
+template <typename T, typename H>
+__host__ __device__ __forceinline__ T s2_divV(T vx0, T vx1, T vy0, T vy1, H dx, H dy) {
+    return dvd(vx1 - vx0, dx) + dvd(vy1 - vy0, dy);
 }
-template <typename T>
-__host__ __device__ __forceinline__ T s2_tau_nn(T mus, T v0, T v1, T divV, T h) {
-    return (T(2.0) * mus) * ((v1 - v0) / h - (T(1.0) / T(3.0)) * divV);
+template <typename T, typename H>
+__host__ __device__ __forceinline__ T s2_tau_nn(T mus, T v0, T v1, T divV, H h) {
+    return (T(2.0) * mus) * (dvd(v1 - v0, h) - (T(1.0) / T(3.0)) * divV);
 }
-template <typename T>
-__host__ __device__ __forceinline__ T s2_tau_xy(T m00, T m10, T m01, T m11, T dyVx, T dxVy, T dx, T dy) {
+template <typename T, typename H>
+__host__ __device__ __forceinline__ T s2_tau_xy(T m00, T m10, T m01, T m11, T dyVx, T dxVy, H dx, H dy) {
     T av = (((m00 + m10) + m01) + m11) * T(0.25);
-    return (T(2.0) * av) * (T(0.5) * (dyVx / dy + dxVy / dx));
+    return (T(2.0) * av) * (T(0.5) * (dvd(dyVx, dy) + dvd(dxVy, dx)));
 }
-template <typename T>
-__host__ __device__ __forceinline__ T s2_Rx(T txx_l, T txx_r, T txy_b, T txy_t, T p_l, T p_r, T dx, T dy) {
-    return ((txx_r - txx_l) / dx + (txy_t - txy_b) / dy) - (p_r - p_l) / dx;
+template <typename T, typename H>
+__host__ __device__ __forceinline__ T s2_Rx(T txx_l, T txx_r, T txy_b, T txy_t, T p_l, T p_r, H dx, H dy) {
+    return (dvd(txx_r - txx_l, dx) + dvd(txy_t - txy_b, dy)) - dvd(p_r - p_l, dx);
 }
-template <typename T>
-__host__ __device__ __forceinline__ T s2_Ry_core(T tyy_b, T tyy_t, T txy_l, T txy_r, T p_b, T p_t, T dx, T dy) {
-    return ((tyy_t - tyy_b) / dy + (txy_r - txy_l) / dx) - (p_t - p_b) / dy;
+template <typename T, typename H>
+__host__ __device__ __forceinline__ T s2_Ry_core(T tyy_b, T tyy_t, T txy_l, T txy_r, T p_b, T p_t, H dx, H dy) {
+    return (dvd(tyy_t - tyy_b, dy) + dvd(txy_r - txy_l, dx)) - dvd(p_t - p_b, dy);
 }
 
 template <typename T>
 struct S2P {
-    T dx, dy, dampX, dampY, Vsc, Ptsc, min_dxy2, max_nxy;
+    DivC<T> dx, dy;
+    T dampX, dampY, Vsc, Ptsc, min_dxy2, max_nxy;
 };
 
 template <typename T>
 static S2P<T> s2p(const ps_stokes2d_params& p) {
-    return S2P<T>{(T)p.dx, (T)p.dy, (T)p.dampX, (T)p.dampY, (T)p.Vsc, (T)p.Ptsc, (T)p.min_dxy2, (T)p.max_nxy};
+    return S2P<T>{make_div((T)p.dx), make_div((T)p.dy), (T)p.dampX,    (T)p.dampY,
+                  (T)p.Vsc,          (T)p.Ptsc,         (T)p.min_dxy2, (T)p.max_nxy};
 }
 
 #define A2(a, i, j, n0) (a)[(int64_t)(i) + (int64_t)(n0) * (int64_t)(j)]

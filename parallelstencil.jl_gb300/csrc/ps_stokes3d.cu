@@ -30,13 +30,14 @@ namespace ps {
 
 template <typename T>
 struct S3P {
-    T dx, dy, dz, dampX, dampY, dampZ, Vsc, Ptsc, min_dxyz2, max_nxyz;
+    DivC<T> dx, dy, dz;  // divisors of the statements (correctly rounded division by host numbers)
+    T dampX, dampY, dampZ, Vsc, Ptsc, min_dxyz2, max_nxyz;
 };
 
 template <typename T>
 static S3P<T> s3p(const ps_stokes3d_params& p) {
-    return S3P<T>{(T)p.dx,   (T)p.dy,  (T)p.dz,   (T)p.dampX,     (T)p.dampY,
-                  (T)p.dampZ, (T)p.Vsc, (T)p.Ptsc, (T)p.min_dxyz2, (T)p.max_nxyz};
+    return S3P<T>{make_div((T)p.dx), make_div((T)p.dy), make_div((T)p.dz), (T)p.dampX,     (T)p.dampY,
+                  (T)p.dampZ,        (T)p.Vsc,          (T)p.Ptsc,         (T)p.min_dxyz2, (T)p.max_nxyz};
 }
 
 // Device pointers of the miniapp's arrays (sizes relative to (nx, ny, nz) = size(Pt) as in
@@ -71,20 +72,20 @@ __device__ __forceinline__ T s3_dtPt(T Ptsc, T m, T mn) {
 template <typename T>
 __device__ __forceinline__ T s3_divV(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
     const int64_t nx = a.nx, ny = a.ny;
-    return ((a.Vx[I3(x + 1, y, z, nx + 1, ny)] - a.Vx[I3(x, y, z, nx + 1, ny)]) / p.dx +
-            (a.Vy[I3(x, y + 1, z, nx, ny + 1)] - a.Vy[I3(x, y, z, nx, ny + 1)]) / p.dy) +
-           (a.Vz[I3(x, y, z + 1, nx, ny)] - a.Vz[I3(x, y, z, nx, ny)]) / p.dz;
+    return (div_c(a.Vx[I3(x + 1, y, z, nx + 1, ny)] - a.Vx[I3(x, y, z, nx + 1, ny)], p.dx) +
+            div_c(a.Vy[I3(x, y + 1, z, nx, ny + 1)] - a.Vy[I3(x, y, z, nx, ny + 1)], p.dy)) +
+           div_c(a.Vz[I3(x, y, z + 1, nx, ny)] - a.Vz[I3(x, y, z, nx, ny)], p.dz);
 }
 // 2.0*μ*(dV/h - 1.0/3.0*∇V)
 template <typename T>
-__device__ __forceinline__ T s3_tnn(T m, T v1, T v0, T h, T d) {
-    return (T(2.0) * m) * ((v1 - v0) / h - (T(1.0) / T(3.0)) * d);
+__device__ __forceinline__ T s3_tnn(T m, T v1, T v0, const DivC<T>& h, T d) {
+    return (T(2.0) * m) * (div_c(v1 - v0, h) - (T(1.0) / T(3.0)) * d);
 }
 // 2.0*@av_..i(μ)*(0.5*(a/ha + b/hb)), the four μ in the macro's order
 template <typename T>
-__device__ __forceinline__ T s3_tsh(T m0, T m1, T m2, T m3, T a, T ha, T b, T hb) {
+__device__ __forceinline__ T s3_tsh(T m0, T m1, T m2, T m3, T a, const DivC<T>& ha, T b, const DivC<T>& hb) {
     const T av = (((m0 + m1) + m2) + m3) * T(0.25);
-    return (T(2.0) * av) * (T(0.5) * (a / ha + b / hb));
+    return (T(2.0) * av) * (T(0.5) * (div_c(a, ha) + div_c(b, hb)));
 }
 
 template <typename T>
@@ -131,7 +132,7 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
         const T B = a.txy[I3(x, y + 1, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
         const T C = a.txz[I3(x, y, z + 1, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
         const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x, y + 1, z + 1, nx, ny)];
-        T R = ((A / p.dx + B / p.dy) + C / p.dz) - P / p.dx;
+        T R = ((div_c(A, p.dx) + div_c(B, p.dy)) + div_c(C, p.dz)) - div_c(P, p.dx);
         if constexpr (MODE == S3_DEFECT) R = R + a.fx[r];
         a.Rx[r] = R;
         if constexpr (MODE != S3_RESIDUAL) {
@@ -149,7 +150,7 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
         const T B = a.txy[I3(x + 1, y, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
         const T C = a.tyz[I3(x, y, z + 1, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
         const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y, z + 1, nx, ny)];
-        T R = ((A / p.dy + B / p.dx) + C / p.dz) - P / p.dy;
+        T R = ((div_c(A, p.dy) + div_c(B, p.dx)) + div_c(C, p.dz)) - div_c(P, p.dy);
         if constexpr (MODE == S3_DEFECT) R = R + a.fy[r];
         a.Ry[r] = R;
         if constexpr (MODE != S3_RESIDUAL) {
@@ -169,10 +170,10 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
         const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y + 1, z, nx, ny)];
         T R;
         if constexpr (MODE == S3_DEFECT) {  // the buoyancy is part of the outer residual fz
-            R = (((A / p.dz + B / p.dx) + C / p.dy) - P / p.dz) + a.fz[r];
+            R = (((div_c(A, p.dz) + div_c(B, p.dx)) + div_c(C, p.dy)) - div_c(P, p.dz)) + a.fz[r];
         } else {
             const T G = (a.Rog[I3(x + 1, y + 1, z, nx, ny)] + a.Rog[I3(x + 1, y + 1, z + 1, nx, ny)]) * T(0.5);
-            R = (((A / p.dz + B / p.dx) + C / p.dy) - P / p.dz) + G;
+            R = (((div_c(A, p.dz) + div_c(B, p.dx)) + div_c(C, p.dy)) - div_c(P, p.dz)) + G;
         }
         a.Rz[r] = R;
         if constexpr (MODE != S3_RESIDUAL) {

@@ -59,6 +59,7 @@ SIGNATURES = {
     "ps_last_error": [],
     "ps_abi_version": [],
     "ps_device_count": [ctypes.POINTER(_I)],
+    "ps_check_division": [_D, _I32, _I64, ctypes.c_uint64, ctypes.POINTER(_I64), _P],
     "ps_alloc": [ctypes.POINTER(_A), _I32, _I64, _I64, _I64],
     "ps_free": [ctypes.POINTER(_A)],
     "ps_fill": [_A, _D, _P],
@@ -78,6 +79,8 @@ SIGNATURES = {
                                   COMM_FN, _P],
     "ps_acoustic3d_v": [_A, _A, _A, _A, _D, _D, _D, _D, _D, _P, _I],
     "ps_acoustic3d_p": [_A, _A, _A, _A, _D, _D, _D, _D, _D, _P, _I],
+    "ps_acoustic3d_step": [_A] * 8 + [_D] * 6 + [_I32, _P, _I],
+    "ps_acoustic3d_run": [_A] * 4 + [_D] * 6 + [_I64, _I32, _P],
 }
 _RESTYPES = {"ps_last_error": ctypes.c_char_p}
 

@@ -60,6 +60,11 @@ _lib.register("ps_jit_launch_ex", [ctypes.c_void_p, ctypes.POINTER(PSArray), cty
                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                    ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
                                    ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p, ctypes.c_int])
+_lib.register("ps_jit_hide_communication", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
+                                            _lib.COMM_FN, ctypes.c_void_p, ctypes.c_void_p])
 _lib.register("ps_jit_check", [ctypes.c_void_p, ctypes.c_void_p])
 _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
@@ -1020,8 +1025,8 @@ class _Gen:
         if self.uses_collectives:
             # barriers, shuffles and votes need every thread of a block: a block that reaches past the
             # ranges leaves as a whole before any of them (block-uniform) and reports it (flag 2)
-            guard = """    if ((blockIdx.x + 1LL) * blockDim.x > g.cnt[0] || (blockIdx.y + 1LL) * blockDim.y > g.cnt[1] ||
-        (blockIdx.z + 1LL) * blockDim.z > g.cnt[2]) {
+            guard = """    if ((bi.x + 1LL) * blockDim.x > g.cnt[0] || (bi.y + 1LL) * blockDim.y > g.cnt[1] ||
+        (bi.z + 1LL) * blockDim.z > g.cnt[2]) {
         if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicOr(g.err, 2);
         return;
     }"""
@@ -1030,13 +1035,13 @@ class _Gen:
         zpre, zpost = "", ""
         u, t, c = ("ux", "uy", "uz"), ("tx", "ty", "tz"), "xyz"
         grid = [d for d in range(3) if d != self.sweep]
-        udecl = ", ".join(f"{u[d]} = blockIdx.{c[d]} * (long long)blockDim.{c[d]} + threadIdx.{c[d]}" for d in grid)
+        udecl = ", ".join(f"{u[d]} = bi.{c[d]} * (long long)blockDim.{c[d]} + threadIdx.{c[d]}" for d in grid)
         if self.zloop:  # blockDim of the sweep dimension is 1; each block covers g.loop consecutive indices
             sd = self.sweep
             guard = "    if (" + " || ".join(f"{u[d]} >= g.cnt[{d}]" for d in grid) + ") return;"
             zpre = "\n" + "\n".join(self.persist) + f"""
     for (long long it_ = 0; it_ < g.loop; ++it_) {{
-    const long long {u[sd]} = blockIdx.{c[sd]} * g.loop + it_;
+    const long long {u[sd]} = bi.{c[sd]} * g.loop + it_;
     if ({u[sd]} >= g.cnt[{sd}]) break;
     const long long {t[sd]} = g.lo[{sd}] + {u[sd]};"""
             zpost = "    }"
@@ -1044,7 +1049,8 @@ class _Gen:
         sweep = f", {c[self.sweep]} sweep" if self.zloop else ""
         return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{sweep}) -- generated by ps_gb300.jit
 {self.types(real)}
-struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long loop; }};
+struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long loop; unsigned* ocnt; int ord[10]; }};
+{_BLOCK_ORDER}
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ E jl_ld(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
@@ -1066,7 +1072,7 @@ __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov
 __device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
-extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
+__device__ __forceinline__ void ps_jit_body(const ps_jit_args& g, const uint3 bi) {{
     extern __shared__ __align__(16) unsigned char ps_smem[];
     const long long {udecl};
 {guard}
@@ -1076,6 +1082,42 @@ extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
 {chr(10).join(body)}
 {zpost}
 }}
+extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
+    ps_jit_body(g, jl_block(g));
+    jl_block_done(g);
+}}
+"""
+
+
+# Block order of a boundary-first launch (ps_jit_hide_communication): with g.ocnt set, the 1-D
+# grid's first ord[9] blocks take the tiles holding boundary indices -- whole layers at both ends of
+# z, then whole rows at both ends of y, then column ends of x -- the rest the inner block; each
+# boundary block counts itself in host-mapped memory once its stores are done.
+_BLOCK_ORDER = r"""
+__device__ __forceinline__ uint3 jl_block(const ps_jit_args& g) {
+    if (!g.ocnt) return blockIdx;
+    const int TX = g.ord[0], TY = g.ord[1], TZ = g.ord[2], bx0 = g.ord[3], bx1 = g.ord[4], by0 = g.ord[5],
+              by1 = g.ord[6], bz0 = g.ord[7], bz1 = g.ord[8], nb = g.ord[9];
+    int i = (int)blockIdx.x;
+    const int IX = TX - bx0 - bx1, IY = TY - by0 - by1;
+    if (i >= nb) { i -= nb; return make_uint3(bx0 + i % IX, by0 + (i / IX) % IY, bz0 + i / (IX * IY)); }
+    const int layer = TX * TY, nzfull = (bz0 + bz1) * layer;
+    if (i < nzfull) { const int l = i / layer, r = i % layer; return make_uint3(r % TX, r / TX, l < bz0 ? l : TZ - bz1 + (l - bz0)); }
+    i -= nzfull;
+    const int frame = layer - IX * IY, z = bz0 + i / frame;
+    int r = i % frame;
+    const int nyfull = (by0 + by1) * TX;
+    if (r < nyfull) { const int row = r / TX; return make_uint3(r % TX, row < by0 ? row : TY - by1 + (row - by0), z); }
+    r -= nyfull;
+    const int ex = bx0 + bx1, c = r % ex;
+    return make_uint3(c < bx0 ? c : TX - bx1 + (c - bx0), by0 + r / ex, z);
+}
+__device__ __forceinline__ void jl_block_done(const ps_jit_args& g) {
+    if (!g.ocnt || (int)blockIdx.x >= g.ord[9]) return;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) { __threadfence_system(); atomicAdd_system(g.ocnt, 1u); }
+}
 """
 
 
@@ -1218,6 +1260,29 @@ class JitKernel:
         launch would have fewer threads than the GPU holds at once -- with the same results.
         fp64="split" evaluates the arithmetic of FP64 kernels on FP32 pairs (each operation within
         ~2^-46 of its operands' magnitude; GB300 issues FP32 at 64x the FP64 rate)."""
+        h, A, nA, S, nS, lo, cnt, threads, shmem, loop = self._config(args, ranges, nblocks, nthreads, shmem, memopt,
+                                                                     loopsize, fp64)
+        _lib.call("ps_jit_launch_ex", h, A, nA, S, nS, (ctypes.c_int64 * 3)(*lo), (ctypes.c_int64 * 3)(*cnt),
+                  (ctypes.c_int32 * 3)(*threads), int(shmem or 0), (ctypes.c_int32 * 3)(*loop), stream_handle(stream),
+                  int(bool(sync)))
+
+    def hide_eligible(self):
+        """A `@parallel` kernel without kernel-language calls (block / thread indices, shared memory,
+        barriers, shuffles, votes): its blocks can run in any order, so ps_jit_hide_communication
+        may launch the boundary tiles first."""
+        return self.kd.kind == "parallel" and not self._kernel_language
+
+    def hide_communication(self, args, bw, comm_fn, stream=None, memopt=None, loopsize=0, fp64="ieee"):
+        """One boundary-first launch over the kernel's full grid (ps_jit_hide_communication); comm_fn
+        (a ps_comm_fn) runs once the boundary tiles are done."""
+        h, A, nA, S, nS, lo, cnt, threads, shmem, loop = self._config(args, None, None, None, None, memopt, loopsize,
+                                                                     fp64)
+        _lib.call("ps_jit_hide_communication", h, A, nA, S, nS, (ctypes.c_int64 * 3)(*cnt),
+                  (ctypes.c_int32 * 3)(*threads), (ctypes.c_int32 * 3)(*loop), (ctypes.c_int64 * 3)(*bw), comm_fn,
+                  None, stream_handle(stream))
+
+    def _config(self, args, ranges, nblocks, nthreads, shmem, memopt, loopsize, fp64):
+        """Handle, argument arrays and launch geometry of one launch (see jit_launch)."""
         require_initialized()
         if len(args) != self.nargs:
             raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
@@ -1281,9 +1346,7 @@ class JitKernel:
                                 f"the thread block (ranges {cnt}, nthreads {threads})")
         A = (PSArray * max(1, len(descs)))(*descs)
         S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
-        _lib.call("ps_jit_launch_ex", h, A, len(descs), S, len(scal), (ctypes.c_int64 * 3)(*lo),
-                  (ctypes.c_int64 * 3)(*cnt), (ctypes.c_int32 * 3)(*threads), int(shmem or 0), (ctypes.c_int32 * 3)(*loop),
-                  stream_handle(stream), int(bool(sync)))
+        return h, A, len(descs), S, len(scal), lo, cnt, threads, shmem, loop
 
     @staticmethod
     def _extent(descs, ndims):

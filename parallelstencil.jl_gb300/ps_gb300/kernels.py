@@ -217,6 +217,34 @@ def run(kernel, T, T2, Ci, lam, dt, hx, hy, hz, nt, *, memopt=True, loopsize=0, 
         synchronize(stream)
 
 
+def acoustic3d_step(Vx, Vy, Vz, P, Vx2, Vy2, Vz2, P2, dt, rho, k, dx, dy, dz, *, fp64="ieee", stream=None,
+                    sync=True):
+    """One step of the acoustic3D time loop (`@parallel compute_V!(...)`, `@parallel compute_P!(...)`,
+    miniapps/acoustic3D.jl:55-56) as one kernel (ps_acoustic3d_step): reads (Vx, Vy, Vz, P), writes
+    the new state into (Vx2, Vy2, Vz2, P2). fp64 = "ieee" (bit-identical) or "split" (FP32 pairs)."""
+    require_initialized()
+    if fp64 not in ("ieee", "split"):
+        raise ArgumentError(f"fp64 must be 'ieee' or 'split' (obtained {fp64!r})")
+    _lib.call("ps_acoustic3d_step", *(descriptor(a) for a in (Vx, Vy, Vz, P, Vx2, Vy2, Vz2, P2)), float(dt),
+              float(rho), float(k), float(dx), float(dy), float(dz), FP64_MODES[fp64], stream_handle(stream),
+              int(bool(sync)))
+
+
+def acoustic3d_run(Vx, Vy, Vz, P, dt, rho, k, dx, dy, dz, nt, *, fp64="ieee", stream=None, sync=True):
+    """`for it = 1:nt; @parallel compute_V!(...); @parallel compute_P!(...); end` in place on
+    (Vx, Vy, Vz, P) (ps_acoustic3d_run: one fused kernel per step, a second state set in library
+    scratch)."""
+    require_initialized()
+    if fp64 not in ("ieee", "split"):
+        raise ArgumentError(f"fp64 must be 'ieee' or 'split' (obtained {fp64!r})")
+    _lib.call("ps_acoustic3d_run", *(descriptor(a) for a in (Vx, Vy, Vz, P)), float(dt), float(rho), float(k),
+              float(dx), float(dy), float(dz), int(nt), FP64_MODES[fp64], stream_handle(stream))
+    if sync:
+        from .core import synchronize
+
+        synchronize(stream)
+
+
 def parallel_async(kernel, *args, **kw):
     """`@parallel_async kernel!(args...)`: no synchronisation."""
     kw["sync"] = False
@@ -244,15 +272,15 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
                             "compiled kernels")
     T2, T, Ci, lam_arr, lam, dt, hx, hy, hz = kernel.split_args(args)
     memopt = default_memopt() if memopt is None else memopt
-    own = []
-    if s_boundary is None:
-        s_boundary = ctypes.c_void_p()
-        _lib.call("ps_stream_create", 1, ctypes.byref(s_boundary))
-        own.append(s_boundary)
-    if s_inner is None:
-        s_inner = ctypes.c_void_p()
-        _lib.call("ps_stream_create", 0, ctypes.byref(s_inner))
-        own.append(s_inner)
+    sb_def, si_def = _hide_streams()
+    if s_boundary is None or s_inner is None:  # the default pair follows the work queued on the current stream
+        import torch
+
+        cur = torch.cuda.current_stream()
+        for st in (sb_def, si_def):
+            st.wait_stream(cur)
+    s_boundary = stream_handle(s_boundary if s_boundary is not None else sb_def)
+    s_inner = stream_handle(s_inner if s_inner is not None else si_def)
     errors = []
 
     def _cb(_ctx):
@@ -267,15 +295,25 @@ def hide_communication(boundary_width, kernel, args, comm=None, *, memopt=None, 
     cb = _lib.COMM_FN(_cb)
     bw_arr = (ctypes.c_int64 * 3)(*[int(b) for b in bw])
     cfg = _launch_cfg(memopt, 0, None, fp64)
-    try:
-        _lib.call("ps_diffusion3d_step_split", kernel.form, descriptor(T2), descriptor(T), descriptor(Ci),
-                  descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), ctypes.byref(cfg),
-                  bw_arr, s_boundary, s_inner, cb, None)
-    finally:
-        for s in own:
-            _lib.call("ps_stream_destroy", s)
+    _lib.call("ps_diffusion3d_step_split", kernel.form, descriptor(T2), descriptor(T), descriptor(Ci),
+              descriptor(lam_arr), float(lam), float(dt), float(hx), float(hy), float(hz), ctypes.byref(cfg),
+              bw_arr, s_boundary, s_inner, cb, None)
     if errors:
         raise errors[0]
+
+
+_HIDE_STREAMS = {}
+
+
+def _hide_streams():
+    """The default (boundary, inner) stream pair of the current device: a high-priority and a
+    normal-priority torch stream, created once (streams outlive the calls that use them)."""
+    import torch
+
+    dev = torch.cuda.current_device()
+    if dev not in _HIDE_STREAMS:
+        _HIDE_STREAMS[dev] = (torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=0))
+    return _HIDE_STREAMS[dev]
 
 
 def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner, fp64="ieee"):
@@ -292,12 +330,33 @@ def _hide_communication_jit(bw, kernel, args, comm, memopt, s_boundary, s_inner,
             raise ArgumentError("@hide_communication: length(ranges) > 2*boundary_width violated")
         if ms[d] > 1 and bw[d] == 0:
             raise ArgumentError("@hide_communication: boundary_width 0 in a dimension of length > 1")
-    # s_boundary / s_inner: torch streams (default: a new high-priority / normal-priority pair)
-    sb = s_boundary if s_boundary is not None else torch.cuda.Stream(priority=-1)
-    si = s_inner if s_inner is not None else torch.cuda.Stream(priority=0)
+    # s_boundary / s_inner: torch streams (default: the device's high-priority / normal-priority pair)
+    sb_def, si_def = _hide_streams()
+    sb = s_boundary if s_boundary is not None else sb_def
+    si = s_inner if s_inner is not None else si_def
     cur = torch.cuda.current_stream()
     for s in (sb, si):
         s.wait_stream(cur)
+    if kernel.hide_eligible():  # one boundary-first launch on s_inner (after s_boundary's queued work)
+        si.wait_stream(sb)
+        errors = []
+
+        def _cb(_ctx):
+            try:
+                if comm is not None:
+                    comm()
+                return 0
+            except Exception as e:  # noqa: BLE001 - reported after the call
+                errors.append(e)
+                return -1
+
+        try:
+            kernel.hide_communication(args, bw, _lib.COMM_FN(_cb), si, memopt=memopt, fp64=fp64)
+        finally:
+            cur.wait_stream(si)
+        if errors:
+            raise errors[0]
+        return
     lw, hw = widened_widths(bw, ms)
     for lo, hi in get_ranges_outer(lw, ms, hw):
         kernel.jit_launch(args, [range(lo[d], hi[d]) for d in range(3)], sb, False, memopt=memopt, fp64=fp64)

@@ -213,6 +213,38 @@ def test_hide_communication_split_fp64_equals_one_launch(ps, form):
     assert np.array_equal(ps.to_host(A), ps.to_host(B))
 
 
+@pytest.mark.parametrize("memopt,fp64", [(True, "ieee"), (True, "split"), (False, "ieee")])
+def test_hide_communication_boundary_is_done_when_comm_runs(ps, oracle, memopt, fp64):
+    """What `comm` sees: a full copy of T2 taken inside the callback holds the final values on the
+    boundary cells. memopt (one boundary-first launch, each boundary tile counted in host-mapped
+    memory): cells 1 .. bw and n-1-bw .. n-2 of every axis; the separate slab launches: the
+    reference's ranges, cells 1 .. bw and n-bw+1 .. n-2 (src/ParallelKernel/hide_communication.jl:350-394)."""
+    n, bw = (256, 96, 80), (16, 2, 2)
+    rng = np.random.default_rng(23)
+    T, Ci, lam = (np.asfortranarray(a) for a in (rng.random(n), rng.random(n), 1 + 0.5 * rng.random(n)))
+    ref = np.asfortranarray(np.zeros(n))
+    oracle.diffusion3d_step(3, ref, T, Ci, lam, 1.0, 1e-4, 5.0, 5.0, 5.0)
+    T2 = ps.zeros(*n)
+    snaps = []
+    ps.hide_communication(bw, ps.kernels.diffusion3D_step_flux_lam, (T2, _dev(ps, T), _dev(ps, Ci), _dev(ps, lam),
+                                                                     1e-4, 5.0, 5.0, 5.0),
+                          comm=lambda: snaps.append(ps.to_host(T2)), memopt=memopt, fp64=fp64)
+    final = ps.to_host(T2)
+    if fp64 == "ieee":
+        assert np.array_equal(final, ref)
+    snap = snaps[0]
+    inner = [np.arange(1, m - 1) for m in n]
+    for d in range(3):
+        hi0 = n[d] - 1 - bw[d] if memopt else n[d] - bw[d] + 1
+        for cells in (np.arange(1, bw[d] + 1), np.arange(hi0, n[d] - 1)):
+            if cells.size == 0:
+                continue
+            idx = list(inner)
+            idx[d] = cells
+            sel = np.ix_(*idx)
+            assert np.array_equal(snap[sel], final[sel]), (d, cells[0])
+
+
 def test_hide_communication_invalid_width(ps):
     T = ps.zeros(16, 16, 16)
     with pytest.raises(ps.PSError):

@@ -488,6 +488,34 @@ def test_jit_hide_communication_equals_one_launch(ps, name, n):
     assert not np.array_equal(ps.to_host(ref2[-1]), ps.to_host(ref[-1]))
 
 
+@pytest.mark.parametrize("fp64", ["ieee", "split"])
+def test_jit_hide_communication_boundary_is_done_when_comm_runs(ps, fp64):
+    """The boundary-first launch of a run-time compiled kernel: a full copy of T2 taken inside the
+    callback holds the final values on the boundary cells of the reference's ranges (thread indices
+    t < bw or t >= n - bw, i.e. @inn cells 1 .. bw and n-bw+1 .. n-2)."""
+    n, bw = (256, 96, 80), (16, 2, 2)
+    rng = np.random.default_rng(19)
+    k = ps.parallel_kernel(K.HEAT_FLUX)
+    assert k.hide_eligible()
+    T, Ci = _dev(ps, rng.random(n)), _dev(ps, rng.random(n) + 0.5)
+    rest = [T, Ci, 0.7, 1e-3, 9.0, 11.0, 13.0]
+    ref, out = ps.zeros(*n), ps.zeros(*n)
+    ps.parallel(k, ref, *rest, fp64=fp64)
+    snaps = []
+    ps.hide_communication(bw, k, (out, *rest), comm=lambda: snaps.append(ps.to_host(out)), fp64=fp64)
+    final = ps.to_host(out)
+    assert np.array_equal(final, ps.to_host(ref))
+    inner = [np.arange(1, m - 1) for m in n]
+    for d in range(3):
+        for cells in (np.arange(1, bw[d] + 1), np.arange(n[d] - bw[d] + 1, n[d] - 1)):
+            if cells.size == 0:
+                continue
+            idx = list(inner)
+            idx[d] = cells
+            sel = np.ix_(*idx)
+            assert np.array_equal(snaps[0][sel], final[sel]), (d, cells[0])
+
+
 # ---------------------------------------------------------------- split FP64 arithmetic
 @pytest.mark.parametrize("name", sorted(_cases(np.float64)))
 def test_jit_split_fp64_close_to_ieee(ps, name):
