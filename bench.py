@@ -687,6 +687,20 @@ def _events(torch, fn, reps):
     return e0.elapsed_time(e1) / 1e3 / reps
 
 
+def acoustic_fields(ps, n, dt, seed=3):
+    """Vx, Vy, Vz, P of the acoustic3D miniapp at n^3 on a 40^3 box: its Gaussian pressure
+    (acoustic3D.jl:39) plus seeded noise of 1e-3 on every array, so that no difference is zero
+    (a zero quotient takes a shorter path in the divisions)."""
+    h, lx = 40.0 / (n - 1), 40.0
+    c = (np.arange(n) * h - 0.5 * lx) ** 2
+    P0 = np.exp(-(c[:, None, None] + c[None, :, None] + c[None, None, :]))
+    rng = np.random.default_rng(seed)
+    P = ps.from_host(np.asfortranarray((P0 + 1e-3 * rng.random((n, n, n))).astype(dt)))
+    V = [ps.from_host(np.asfortranarray((1e-3 * rng.standard_normal(sh)).astype(dt)))
+         for sh in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))]
+    return V[0], V[1], V[2], P
+
+
 def bench_miniapps(ps, torch, peak):
     """T_eff of the miniapp iterations with each miniapp's own A_eff (words per cell per iteration):
     Stokes2D 6 (Stokes2D.jl:128) at 1023^2, Stokes3D 8 (Stokes3D.jl:154) at 127^3 (the miniapp's
@@ -722,16 +736,8 @@ def bench_miniapps(ps, torch, peak):
             launches += 6 * 10 * 3 + 13 * 10
             del g
         n = 255
-        lx = 40.0
-        h = lx / (n - 1)
-        # the miniapp's Gaussian pressure (acoustic3D.jl:39) plus seeded noise of 1e-3 on every array,
-        # so that no difference is zero (zero quotients take a shorter path in the divisions)
-        c = (np.arange(n) * h - 0.5 * lx) ** 2
-        P0 = np.exp(-(c[:, None, None] + c[None, :, None] + c[None, None, :]))
-        rng = np.random.default_rng(3)
-        P = ps.from_host(np.asfortranarray((P0 + 1e-3 * rng.random((n, n, n))).astype(dt)))
-        Vx, Vy, Vz = (ps.from_host(np.asfortranarray((1e-3 * rng.standard_normal(sh)).astype(dt)))
-                      for sh in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1)))
+        h = 40.0 / (n - 1)
+        Vx, Vy, Vz, P = acoustic_fields(ps, n, dt)
         dts = h / 6.1
 
         def acoustic_step():
@@ -1177,8 +1183,7 @@ def only_run(a):
             dtp = np.float32 if a.only_run.endswith("32") else np.float64
             fp64 = "split" if a.only_run.endswith("split") else "ieee"
             h = 40.0 / (n - 1)
-            sets = [[ps.ones(n + 1, n, n, dtype=dtp), ps.ones(n, n + 1, n, dtype=dtp), ps.ones(n, n, n + 1, dtype=dtp),
-                     ps.ones(n, n, n, dtype=dtp)] for _ in range(2)]
+            sets = [list(acoustic_fields(ps, n, dtp, seed=3 + i)) for i in range(2)]
             for it in range(a.steps):
                 ps.kernels.acoustic3d_step(*sets[it % 2], *sets[1 - it % 2], h / 6.1, 1.0, 1.0, h, h, h, fp64=fp64,
                                            sync=False)

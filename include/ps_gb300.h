@@ -506,9 +506,10 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
  * `@parallel` kernel over its full grid (count threads from index 0; threads and loop as for
  * ps_jit_launch_ex; no dynamic shared memory, no barriers, shuffles or votes). One launch on
  * `stream` whose first blocks take the tiles holding the boundary indices t < bw or t >= count - bw
- * (the reference's ranges_outer, src/ParallelKernel/hide_communication.jl:350-394); each such block
- * counts itself in host-mapped memory after its stores, and `comm` runs on this thread as soon as
- * all have, while the inner blocks still run. Returns after the launch completes, with the
+ * (the reference's ranges_outer, src/ParallelKernel/hide_communication.jl:350-394); each warp of
+ * such a block counts itself in host-mapped memory after its stores, and `comm` runs on this thread
+ * as soon as all have, while the inner blocks still run. The kernel must be the boundary-first
+ * variant of the definition (ps_gb300/jit.py generates it with the order decode and the count). Returns after the launch completes, with the
  * kernel's flags reported as by a synchronous launch. */
 int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars,
                               int32_t nscalars, const int64_t count[3], const int32_t threads[3], const int32_t loop[3],

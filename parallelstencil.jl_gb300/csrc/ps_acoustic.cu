@@ -25,6 +25,7 @@
 // (ps_dd.cuh): values split on load with integer operations, the constants (dt/ρ)/h and (dt·k)/h
 // folded into one product per term (three-float constants), each new value stored as the old
 // FP64 value plus the pair increment, summed in FP64.
+#include <algorithm>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -38,7 +39,6 @@ namespace ps {
 namespace {
 
 constexpr int ACU_W = 8;  // warps per CTA
-constexpr int ACU_K = 1;  // y rows per warp (2 and 4 measured slower: registers cost occupancy)
 
 template <typename S>
 struct AcuArrays {
@@ -117,148 +117,138 @@ struct AcuSplit {
     }
 };
 
-template <class AR, int K>
+// One y row per warp (each Vy face between two rows is computed by both: two rows per warp measured
+// slower, their registers cost occupancy). I: the index type of element offsets (int when every
+// array has fewer than 2^31 elements). Offsets advance by the plane strides along the sweep.
+template <class AR, typename I>
 __global__ void __launch_bounds__(32 * ACU_W, 4) acoustic_step_kernel(AcuArrays<typename AR::S> a,
                                                                     typename AR::C c, int Lz, int* err) {
     using S = typename AR::S;
     using V = typename AR::V;
     const int lane = threadIdx.x;
-    const int64_t nx = a.nx, ny = a.ny, nz = a.nz;
-    const int64_t yb = ((int64_t)blockIdx.y * ACU_W + threadIdx.y) * K;
-    if (yb >= ny) return;  // whole warps only: no block-wide synchronisation follows
-    const int64_t x = (int64_t)blockIdx.x * 32 + lane;
-    const int64_t z0 = (int64_t)blockIdx.z * Lz;
-    const int64_t z1 = z0 + Lz < nz ? z0 + Lz : nz;
+    const I nx = (I)a.nx, ny = (I)a.ny, nz = (I)a.nz;
+    const I y = (I)blockIdx.y * ACU_W + (I)threadIdx.y;
+    if (y >= ny) return;  // whole warps only: no block-wide synchronisation follows
+    const I x = (I)blockIdx.x * 32 + lane;
+    const I z0 = (I)blockIdx.z * Lz;
+    const I z1 = z0 + Lz < nz ? z0 + Lz : nz;
     const bool xv = x < nx;
-    const int64_t sP = nx * ny;         // P and Vz planes; P, Vy and Vz rows have pitch nx
-    const int64_t rX = nx + 1, sX = (nx + 1) * ny;
-    const int64_t sY = nx * (ny + 1);
-    const bool xin = x >= 1 && x <= nx - 2;  // the x range of @inn(Vy), @inn(Vz)
-    const bool edge_lo = lane == 0 && xv && x >= 1;          // loads P(x-1)
-    const bool edge_hi = xv && (lane == 31 || x == nx - 1);  // computes the Vx face x+1 itself
+    const I sP = nx * ny, sX = (nx + 1) * ny, sY = nx * (ny + 1);  // plane strides: P and Vz, Vx, Vy
+    // the x-y parts of the @inn masks
+    const bool xin = x >= 1 && x <= nx - 2, yin = y >= 1 && y <= ny - 2;
+    const bool m_vx = x >= 1 && yin;              // Vx face x (x <= nx - 1 holds)
+    const bool m_vx1 = x + 1 <= nx - 1 && yin;    // Vx face x + 1
+    const bool m_vy0 = xin && y >= 1;             // Vy face y (y <= ny - 1 holds)
+    const bool m_vy1 = xin && y + 1 <= ny - 1;    // Vy face y + 1
+    const bool m_vz = xin && yin;
+    const bool ld_lo = xv && y >= 1, ld_hi = xv && y + 1 < ny;
+    const bool e_lo = lane == 0 && xv && x >= 1;           // loads P(x-1)
+    const bool e_p31 = lane == 31 && xv && x + 1 < nx;     // loads P(x+1)
+    const bool e_hi = xv && (lane == 31 || x == nx - 1);   // computes the Vx face x + 1 itself
+    const bool last_x = x == nx - 1, last_y = y == ny - 1;
     bool big = false;
 
-    bool rv[K], yin[K];
-#pragma unroll
-    for (int r = 0; r < K; ++r) {
-        rv[r] = xv && yb + r < ny;
-        yin[r] = yb + r >= 1 && yb + r <= ny - 2;
+    I oP = x + nx * y + sP * z0;        // P(x, y, z) and the Vz face below it
+    I oX = x + (nx + 1) * y + sX * z0;  // Vx face x
+    I oY = x + nx * y + sY * z0;        // Vy face y
+    // carried state: P(z) (value and arithmetic form) and the new Vz on face z
+    S pr = xv ? a.P[oP] : S(0);
+    V pc = AR::in(pr, big);
+    V vzc;
+    {
+        const S vo = xv ? a.Vz[oP] : S(0);
+        const bool inner = m_vz && z0 >= 1;
+        const S pm = (xv && inner) ? a.P[oP - sP] : S(0);
+        vzc = inner ? AR::add(AR::in(vo, big), AR::vdel(pc, AR::in(pm, big), c, 2)) : AR::in(vo, big);
+        if (xv && z0 == 0) a.Vz2[oP] = vo;  // face 0 is outside @inn(Vz)
     }
 
-    // The carried state at z0: P(z0) (value and arithmetic form) and the new Vz on face z0.
-    S pr[K];
-    V pc[K], vzc[K];
-#pragma unroll
-    for (int r = 0; r < K; ++r) {
-        const int64_t cell = x + nx * (yb + r) + sP * z0;
-        pr[r] = rv[r] ? a.P[cell] : S(0);
-        const S vo = rv[r] ? a.Vz[cell] : S(0);
-        pc[r] = AR::in(pr[r], big);
-        const bool inner = xin && yin[r] && z0 >= 1;
-        const S pm = (rv[r] && inner) ? a.P[cell - sP] : S(0);
-        vzc[r] = inner ? AR::add(AR::in(vo, big), AR::vdel(pc[r], AR::in(pm, big), c, 2)) : AR::in(vo, big);
-        if (rv[r] && z0 == 0) a.Vz2[cell] = vo;  // face 0 is outside @inn(Vz)
-    }
-
-    for (int64_t z = z0; z < z1; ++z) {
+    // the own-cell loads run one plane ahead: P(z+1), the Vz face z+1, the Vx and Vy faces of z
+    S f_pn = (xv && z0 + 1 < nz) ? a.P[oP + sP] : S(0);
+    S f_vzo = xv ? a.Vz[oP + sP] : S(0);
+    S f_vxo = xv ? a.Vx[oX] : S(0);
+    S f_vy0 = xv ? a.Vy[oY] : S(0);
+    for (I z = z0; z < z1; ++z, oP += sP, oX += sX, oY += sY) {
         const bool zin = z >= 1 && z <= nz - 2;  // the z range of @inn(Vx), @inn(Vy)
-        const bool has_next = z + 1 < nz;
-        // loads of this plane
-        S pn[K], vzo[K], vxo[K], vyo[K + 1], xe_p[K], xe_v[K];
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-            const int64_t cell = x + nx * (yb + r) + sP * z;
-            const int64_t fx = x + rX * (yb + r) + sX * z;
-            pn[r] = (rv[r] && has_next) ? a.P[cell + sP] : S(0);
-            vzo[r] = rv[r] ? a.Vz[cell + sP] : S(0);  // face z+1 <= nz
-            vxo[r] = rv[r] ? a.Vx[fx] : S(0);
-            // lane 0: P(x-1); lane 31: P(x+1) and the Vx face x+1; x = nx-1: the last Vx face
-            xe_p[r] = (rv[r] && (edge_lo || (lane == 31 && x + 1 < nx))) ? a.P[lane == 0 ? cell - 1 : cell + 1] : S(0);
-            xe_v[r] = (rv[r] && edge_hi) ? a.Vx[fx + 1] : S(0);
+        const S pn = f_pn, vzo = f_vzo, vxo = f_vxo, vy0 = f_vy0;
+        if (z + 1 < z1) {
+            f_pn = (xv && z + 2 < nz) ? a.P[oP + 2 * sP] : S(0);
+            f_vzo = xv ? a.Vz[oP + 2 * sP] : S(0);  // face z + 2 <= nz
+            f_vxo = xv ? a.Vx[oX + sX] : S(0);
+            f_vy0 = xv ? a.Vy[oY + sY] : S(0);
         }
-#pragma unroll
-        for (int r = 0; r <= K; ++r) vyo[r] = (xv && yb + r <= ny) ? a.Vy[x + nx * (yb + r) + sY * z] : S(0);
-        const S p_lo = (xv && yb >= 1) ? a.P[x + nx * (yb - 1) + sP * z] : S(0);
-        const S p_hi = (xv && yb + K < ny) ? a.P[x + nx * (yb + K) + sP * z] : S(0);
+        const S vy1 = xv ? a.Vy[oY + nx] : S(0);   // face y + 1 <= ny
+        const S plo = ld_lo ? a.P[oP - nx] : S(0);
+        const S phi = ld_hi ? a.P[oP + nx] : S(0);
+        const S xep = (e_lo || e_p31) ? a.P[lane == 0 ? oP - 1 : oP + 1] : S(0);
+        const S xev = e_hi ? a.Vx[oX + 1] : S(0);
 
-        // new Vy on the K+1 faces yb .. yb+K
-        V vyn[K + 1];
-#pragma unroll
-        for (int r = 0; r <= K; ++r) {
-            const int64_t f = yb + r;
-            const bool inner = xin && f >= 1 && f <= ny - 1 && zin;
-            const V vo = AR::in(vyo[r], big);
-            S st = vyo[r];
-            if (inner) {
-                const V pa = r < K ? pc[r] : AR::in(p_hi, big);
-                const V pb = r > 0 ? pc[r - 1] : AR::in(p_lo, big);
-                const V dl = AR::vdel(pa, pb, c, 1);
-                vyn[r] = AR::add(vo, dl);
-                st = AR::store(vyo[r], vyn[r], dl);
-            } else {
-                vyn[r] = vo;
-            }
-            const bool mine = r < K ? f <= ny : f == ny;  // face ny: the warp of the last row
-            if (xv && mine) a.Vy2[x + nx * f + sY * z] = st;
+        // Vy on faces y and y + 1
+        V vyn0 = AR::in(vy0, big), vyn1 = AR::in(vy1, big);
+        S st0 = vy0;
+        if (m_vy0 && zin) {
+            const V dl = AR::vdel(pc, AR::in(plo, big), c, 1);
+            vyn0 = AR::add(vyn0, dl);
+            st0 = AR::store(vy0, vyn0, dl);
         }
-
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-            const int64_t y = yb + r;
-            const int64_t cell = x + nx * y + sP * z;
-            const int64_t fx = x + rX * y + sX * z;
-            // Vx on face x (this lane) and face x+1 (the next lane, or computed here at the edges)
-            V pxm = AR::shfl_up(pc[r]);
-            if (lane == 0) pxm = AR::in(xe_p[r], big);
-            const bool in_x = x >= 1 && x <= nx - 1 && y >= 1 && y <= ny - 2 && zin;
-            const V vxo_v = AR::in(vxo[r], big);
-            const V dlx = AR::vdel(pc[r], pxm, c, 0);
-            const V vxn = in_x ? AR::add(vxo_v, dlx) : vxo_v;
-            V vxp = AR::shfl_down(vxn);
-            if (edge_hi) {
-                const bool in_x1 = x + 1 <= nx - 1 && y >= 1 && y <= ny - 2 && zin;
-                const V vo1 = AR::in(xe_v[r], big);
-                vxp = in_x1 ? AR::add(vo1, AR::vdel(AR::in(xe_p[r], big), pc[r], c, 0)) : vo1;
-                if (rv[r] && x == nx - 1) a.Vx2[fx + 1] = xe_v[r];  // face nx is outside @inn(Vx)
-            }
-            // Vz on face z+1
-            const bool in_z = xin && yin[r] && z + 1 <= nz - 1;
-            const V vzo_v = AR::in(vzo[r], big);
-            const V pnv = AR::in(pn[r], big);
-            const V dlz = AR::vdel(pnv, pc[r], c, 2);
-            const V vzn = in_z ? AR::add(vzo_v, dlz) : vzo_v;
-            // P
-            const V dlp = AR::pdel(AR::sub(vxp, vxn), AR::sub(vyn[r + 1], vyn[r]), AR::sub(vzn, vzc[r]), c);
-            if (rv[r]) {
-                a.Vx2[fx] = in_x ? AR::store(vxo[r], vxn, dlx) : vxo[r];
-                a.Vz2[cell + sP] = in_z ? AR::store(vzo[r], vzn, dlz) : vzo[r];
-                a.P2[cell] = AR::store(pr[r], AR::add(pc[r], dlp), dlp);
-            }
-            vzc[r] = vzn;
-            pc[r] = pnv;
-            pr[r] = pn[r];
+        if (m_vy1 && zin) {
+            const V dl = AR::vdel(AR::in(phi, big), pc, c, 1);
+            vyn1 = AR::add(vyn1, dl);
+            if (last_y) a.Vy2[oY + nx] = AR::store(vy1, vyn1, dl);
+        } else if (xv && last_y) {
+            a.Vy2[oY + nx] = vy1;  // face ny is outside @inn(Vy)
         }
+        // Vx on face x (this lane) and face x + 1 (the next lane, or computed here at the edges)
+        V pxm = AR::shfl_up(pc);
+        if (lane == 0) pxm = AR::in(xep, big);
+        const bool in_x = m_vx && zin;
+        const V vxo_v = AR::in(vxo, big);
+        const V dlx = AR::vdel(pc, pxm, c, 0);
+        const V vxn = in_x ? AR::add(vxo_v, dlx) : vxo_v;
+        V vxp = AR::shfl_down(vxn);
+        if (e_hi) {
+            const V vo1 = AR::in(xev, big);
+            vxp = (m_vx1 && zin) ? AR::add(vo1, AR::vdel(AR::in(xep, big), pc, c, 0)) : vo1;
+            if (last_x) a.Vx2[oX + 1] = xev;  // face nx is outside @inn(Vx)
+        }
+        // Vz on face z + 1
+        const bool in_z = m_vz && z + 1 <= nz - 1;
+        const V vzo_v = AR::in(vzo, big);
+        const V pnv = AR::in(pn, big);
+        const V dlz = AR::vdel(pnv, pc, c, 2);
+        const V vzn = in_z ? AR::add(vzo_v, dlz) : vzo_v;
+        // P
+        const V dlp = AR::pdel(AR::sub(vxp, vxn), AR::sub(vyn1, vyn0), AR::sub(vzn, vzc), c);
+        if (xv) {
+            a.Vy2[oY] = st0;
+            a.Vx2[oX] = in_x ? AR::store(vxo, vxn, dlx) : vxo;
+            a.Vz2[oP + sP] = in_z ? AR::store(vzo, vzn, dlz) : vzo;
+            a.P2[oP] = AR::store(pr, AR::add(pc, dlp), dlp);
+        }
+        vzc = vzn;
+        pc = pnv;
+        pr = pn;
     }
     if (big) atomicOr(err, DEV_ERR_RANGE);
 }
 
-template <class AR, int K>
-int launch_acoustic_k(const ps_array& Vx, const ps_array& Vy, const ps_array& Vz, const ps_array& P, const ps_array& Vx2,
-                    const ps_array& Vy2, const ps_array& Vz2, const ps_array& P2, const typename AR::C& c,
-                    const DeviceState* st, cudaStream_t s) {
+template <class AR, typename I>
+int launch_acoustic_i(const ps_array& Vx, const ps_array& Vy, const ps_array& Vz, const ps_array& P, const ps_array& Vx2,
+                      const ps_array& Vy2, const ps_array& Vz2, const ps_array& P2, const typename AR::C& c,
+                      const DeviceState* st, cudaStream_t s) {
     using S = typename AR::S;
     AcuArrays<S> a{static_cast<const S*>(Vx.ptr), static_cast<const S*>(Vy.ptr), static_cast<const S*>(Vz.ptr),
                    static_cast<const S*>(P.ptr), static_cast<S*>(Vx2.ptr), static_cast<S*>(Vy2.ptr),
                    static_cast<S*>(Vz2.ptr), static_cast<S*>(P2.ptr), P.n[0], P.n[1], P.n[2]};
     const dim3 blk(32, ACU_W, 1);
-    const int64_t gx = (a.nx + 31) / 32, gy = (a.ny + ACU_W * K - 1) / (ACU_W * K);
+    const int64_t gx = (a.nx + 31) / 32, gy = (a.ny + ACU_W - 1) / ACU_W;
     if (gx > 0x7FFFFFFF || gy > 65535) return fail(PS_ERR_SHAPE, "ps_acoustic3d_step: grid too large");
     static int slots_per_sm = 0;  // per instantiation
-    if (slots_per_sm == 0) slots_per_sm = resident_ctas(acoustic_step_kernel<AR, K>, 32 * ACU_W, 0);
+    if (slots_per_sm == 0) slots_per_sm = resident_ctas(acoustic_step_kernel<AR, I>, 32 * ACU_W, 0);
     int Lz = auto_loopsize(gx * gy, a.nz, (int64_t)slots_per_sm * st->num_sms);
     if ((a.nz + Lz - 1) / Lz > 65535) Lz = (int)((a.nz + 65534) / 65535);
     const dim3 grd((unsigned)gx, (unsigned)gy, (unsigned)((a.nz + Lz - 1) / Lz));
-    acoustic_step_kernel<AR, K><<<grd, blk, 0, s>>>(a, c, Lz, st->d_err);
+    acoustic_step_kernel<AR, I><<<grd, blk, 0, s>>>(a, c, Lz, st->d_err);
     return PS_OK;
 }
 
@@ -266,7 +256,12 @@ template <class AR>
 int launch_acoustic(const ps_array& Vx, const ps_array& Vy, const ps_array& Vz, const ps_array& P, const ps_array& Vx2,
                     const ps_array& Vy2, const ps_array& Vz2, const ps_array& P2, const typename AR::C& c,
                     const DeviceState* st, cudaStream_t s) {
-    return launch_acoustic_k<AR, ACU_K>(Vx, Vy, Vz, P, Vx2, Vy2, Vz2, P2, c, st, s);
+    // 32-bit element offsets when every offset the kernel forms stays below 2^31 (the largest
+    // array, plus a plane of slack for the offsets one plane ahead)
+    const int64_t big = std::max(std::max(numel(Vx), numel(Vy)), numel(Vz)) + 2 * (P.n[0] + 1) * (P.n[1] + 1);
+    if (big < ((int64_t)1 << 31))
+        return launch_acoustic_i<AR, int>(Vx, Vy, Vz, P, Vx2, Vy2, Vz2, P2, c, st, s);
+    return launch_acoustic_i<AR, int64_t>(Vx, Vy, Vz, P, Vx2, Vy2, Vz2, P2, c, st, s);
 }
 
 // x as h + l + r (three floats); x itself is given as the exact sum hi + lo of two doubles

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "ps_gb300.h"
 
 namespace ps {
@@ -194,8 +196,10 @@ __device__ __forceinline__ void ordered_tile_done(const TileOrder& o) {
 // a second gives the correctly rounded quotient: 1 multiply + 4 FMAs against the general division's
 // reciprocal iteration and slow-path test. Dividends outside [lo, hi] (tiny, huge, non-finite; zero
 // is a * y, with the quotient's sign) take the IEEE division; for divisors outside [2^-20, 2^20]
-// (FP32) or [2^-60, 2^60] (FP64) the host sets lo > hi and every division takes it. Results equal
-// a / b bit for bit (checked against the IEEE division by ps_check_division).
+// (FP32) or [2^-60, 2^60] (FP64) the host sets lo > hi and every division takes it. lo keeps the
+// quotient normal and the remainder a - bq, a multiple of 2^(e(a) - 2p + 1), representable
+// (subnormal remainders are exact); hi keeps a*y and the quotient finite. Results equal a / b bit
+// for bit (checked against the IEEE division by ps_check_division).
 template <typename T>
 struct DivC {
     T b, y, lo, hi;
@@ -208,7 +212,7 @@ inline DivC<T> make_div(T b) {
     d.b = b;
     if (a >= 1 / lim && a <= lim) {
         d.y = (T)1 / b;
-        d.lo = sizeof(T) == 4 ? (T)0x1p-70 : (T)0x1p-900;
+        d.lo = sizeof(T) == 4 ? (T)0x1p-100 : (T)0x1p-960;
         d.hi = sizeof(T) == 4 ? (T)0x1p70 : (T)0x1p900;
     } else {
         d.y = 0;
@@ -248,6 +252,30 @@ __host__ __device__ __forceinline__ T dvd(T a, T h) {
 template <typename T>
 __device__ __forceinline__ T dvd(T a, const DivC<T>& h) {
     return div_c(a, h);
+}
+
+// ---------------------------------------------------------------------------------------
+// Programmatic dependent launch: a kernel launched with launch_dependent() may start while the
+// kernel before it on the stream finishes its last wave; it waits in grid_dependency_wait() (a
+// no-op in an ordinary launch) until that kernel has completed and its stores are visible, so
+// every read of data the previous kernel wrote must come after the wait.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dependents_may_launch() { asm volatile("griddepcontrol.launch_dependents;"); }
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                    Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // ---------------------------------------------------------------------------------------

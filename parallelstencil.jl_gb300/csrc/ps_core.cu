@@ -262,8 +262,8 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
     x *= 0x94d049bb133111ebull;
     return x ^ (x >> 31);
 }
-__constant__ int c_exp32[12] = {-126, -100, -71, -70, -69, -1, 0, 1, 69, 70, 71, 127};
-__constant__ int c_exp64[12] = {-1022, -950, -901, -900, -899, -1, 0, 1, 899, 900, 901, 1023};
+__constant__ int c_exp32[12] = {-126, -101, -100, -99, -70, -1, 0, 1, 69, 70, 71, 127};
+__constant__ int c_exp64[12] = {-1022, -961, -960, -959, -900, -1, 0, 1, 899, 900, 901, 1023};
 
 template <typename T>
 __device__ T special_dividend(int i) {

@@ -170,6 +170,8 @@ __device__ __forceinline__ void apt_block_add(double v0, double* out0, double v1
 // (pressure driven by ∇δV + ∇V of the outer state). STORE: write ∇V (and add Σ|∇V| to red).
 template <typename T, bool DEFECT, bool STORE>
 __global__ void __launch_bounds__(256) apt_cells_k(AptArrays<T> a) {
+    grid_dependency_wait();  // V of the previous iteration's faces kernel
+    grid_dependents_may_launch();
     const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
     const int64_t nx = a.nx, ny = a.ny;
     const T third = (T)(1.0 / 3.0), h = (T)0.5;
@@ -206,6 +208,8 @@ __global__ void __launch_bounds__(256) apt_cells_k(AptArrays<T> a) {
 // Σ|Rx|, Σ|Ry| to red).
 template <typename T, bool DEFECT, bool STORE, bool UPDATE>
 __global__ void __launch_bounds__(256) apt_faces_k(AptArrays<T> a) {
+    grid_dependency_wait();  // τ and Pt of the cells kernel
+    grid_dependents_may_launch();
     const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
     const int64_t nx = a.nx, ny = a.ny;
     const T h = (T)0.5;
@@ -379,11 +383,22 @@ static AptArrays<T> apt_arrays(const ps_stokes2d_apt_fields* f, const ps_stokes2
 }
 
 template <typename T, bool DEFECT, bool STORE>
-static void apt_launch_iteration(const AptArrays<T>& a, cudaStream_t s) {
+static void apt_launch_iteration(const AptArrays<T>& a, cudaStream_t s, bool after_kernel = true) {
     const dim3 blk(32, 8);
     const dim3 grd = apt_grid(a.nx, a.ny, blk);
-    apt_cells_k<T, DEFECT, STORE><<<grd, blk, 0, s>>>(a);
-    apt_faces_k<T, DEFECT, STORE, true><<<grd, blk, 0, s>>>(a);
+    // each kernel may start while the kernel before it ends (programmatic dependent launch; it waits
+    // for that kernel's stores before reading); after_kernel = false: the stream's last operation
+    // is not one of these kernels (a memset, a copy, the start of a captured graph)
+    if (!after_kernel) {
+        apt_cells_k<T, DEFECT, STORE><<<grd, blk, 0, s>>>(a);
+    } else if (launch_dependent(apt_cells_k<T, DEFECT, STORE>, grd, blk, 0, s, a) != cudaSuccess) {
+        cudaGetLastError();
+        apt_cells_k<T, DEFECT, STORE><<<grd, blk, 0, s>>>(a);
+    }
+    if (launch_dependent(apt_faces_k<T, DEFECT, STORE, true>, grd, blk, 0, s, a) != cudaSuccess) {
+        cudaGetLastError();
+        apt_faces_k<T, DEFECT, STORE, true><<<grd, blk, 0, s>>>(a);
+    }
 }
 
 template <typename T>
@@ -429,9 +444,9 @@ struct AptGraph {
             if (store_last && it == nout - 1) {
                 AptArrays<T> b = a;
                 b.red = red;
-                apt_launch_iteration<T, DEFECT, true>(b, s);
+                apt_launch_iteration<T, DEFECT, true>(b, s, it > 0);
             } else {
-                apt_launch_iteration<T, DEFECT, false>(a, s);
+                apt_launch_iteration<T, DEFECT, false>(a, s, it > 0);
             }
         }
         PS_CUDA_TRY(cudaStreamEndCapture(s, &graph));
@@ -660,9 +675,9 @@ int ps_stokes2d_apt_iterate(const ps_stokes2d_apt_fields* f, const ps_stokes2d_a
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     for (int64_t it = 0; it < n_iter; ++it) {
         if (f->Pt.dtype == PS_F64)
-            apt_launch_iteration<double, false, true>(apt_arrays<double>(f, p), s);
+            apt_launch_iteration<double, false, true>(apt_arrays<double>(f, p), s, it > 0);
         else
-            apt_launch_iteration<float, false, true>(apt_arrays<float>(f, p), s);
+            apt_launch_iteration<float, false, true>(apt_arrays<float>(f, p), s, it > 0);
     }
     return finish_launch(s, 1, "ps_stokes2d_apt_iterate");
 }

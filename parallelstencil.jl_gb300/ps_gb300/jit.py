@@ -437,8 +437,12 @@ def _lit(v):
 
 
 class _Gen:
-    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False, split: bool = False):
+    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False, split: bool = False, ordered: bool = False):
         self.kd, self.nd = kd, ndims
+        # the boundary-first variant (ps_jit_hide_communication): its block index comes from the
+        # launch's tile order, and every warp counts itself in host-mapped memory at the end
+        self.ordered = bool(ordered)
+        self.exit = "goto ps_done_;" if self.ordered else "return;"
         # FP64 arrays with the arithmetic on FP32 pairs (R = jd, storage E = double); see _JD below
         self.split = bool(split)
         # memopt: each thread sweeps g.loop consecutive indices of the last dimension (z in 3-D, y in
@@ -915,7 +919,7 @@ class _Gen:
         if isinstance(s, ast.Return):  # an early `return` inside a branch: this thread is done
             if s.value is not None:
                 raise ArgumentError("kernels return nothing")
-            return [f"{p}return;"]
+            return [f"{p}{self.exit}"]
         if isinstance(s, ast.Expr) and isinstance(s.value, ast.Call) and isinstance(s.value.func, ast.Name):
             f = s.value.func.id
             if f == "__m_sync_threads":
@@ -1022,35 +1026,39 @@ class _Gen:
                             f"sm{j}_n2 = 1, sm{j}_cap = 0;")
             else:
                 decl.append(f"    {'long long' if t == 'int' else 'R'} v_{name} = 0;")
+        bi = "bi" if self.ordered else "blockIdx"
         if self.uses_collectives:
             # barriers, shuffles and votes need every thread of a block: a block that reaches past the
             # ranges leaves as a whole before any of them (block-uniform) and reports it (flag 2)
-            guard = """    if ((bi.x + 1LL) * blockDim.x > g.cnt[0] || (bi.y + 1LL) * blockDim.y > g.cnt[1] ||
-        (bi.z + 1LL) * blockDim.z > g.cnt[2]) {
+            guard = f"""    if (({bi}.x + 1LL) * blockDim.x > g.cnt[0] || ({bi}.y + 1LL) * blockDim.y > g.cnt[1] ||
+        ({bi}.z + 1LL) * blockDim.z > g.cnt[2]) {{
         if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomicOr(g.err, 2);
-        return;
-    }"""
+        {self.exit}
+    }}"""
         else:
-            guard = "    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) return;"
+            guard = f"    if (ux >= g.cnt[0] || uy >= g.cnt[1] || uz >= g.cnt[2]) {self.exit}"
         zpre, zpost = "", ""
         u, t, c = ("ux", "uy", "uz"), ("tx", "ty", "tz"), "xyz"
         grid = [d for d in range(3) if d != self.sweep]
-        udecl = ", ".join(f"{u[d]} = bi.{c[d]} * (long long)blockDim.{c[d]} + threadIdx.{c[d]}" for d in grid)
+        udecl = ", ".join(f"{u[d]} = {bi}.{c[d]} * (long long)blockDim.{c[d]} + threadIdx.{c[d]}" for d in grid)
         if self.zloop:  # blockDim of the sweep dimension is 1; each block covers g.loop consecutive indices
             sd = self.sweep
-            guard = "    if (" + " || ".join(f"{u[d]} >= g.cnt[{d}]" for d in grid) + ") return;"
+            guard = "    if (" + " || ".join(f"{u[d]} >= g.cnt[{d}]" for d in grid) + f") {self.exit}"
             zpre = "\n" + "\n".join(self.persist) + f"""
     for (long long it_ = 0; it_ < g.loop; ++it_) {{
-    const long long {u[sd]} = bi.{c[sd]} * g.loop + it_;
+    const long long {u[sd]} = {bi}.{c[sd]} * g.loop + it_;
     if ({u[sd]} >= g.cnt[{sd}]) break;
     const long long {t[sd]} = g.lo[{sd}] + {u[sd]};"""
             zpost = "    }"
         pos = "const long long " + ", ".join(f"{t[d]} = g.lo[{d}] + {u[d]}" for d in grid)
+        # the boundary-first variant: the body in a block that a finished thread jumps past, then the count
+        head = "    const uint3 bi = jl_block(g);\n    {\n" if self.ordered else ""
+        tail = "    }\nps_done_:\n    jl_block_done(g);\n" if self.ordered else ""
         sweep = f", {c[self.sweep]} sweep" if self.zloop else ""
         return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{sweep}) -- generated by ps_gb300.jit
 {self.types(real)}
 struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long loop; unsigned* ocnt; int ord[10]; }};
-{_BLOCK_ORDER}
+{_BLOCK_ORDER if self.ordered else ""}
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ E jl_ld(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
@@ -1072,30 +1080,25 @@ __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov
 __device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
-__device__ __forceinline__ void ps_jit_body(const ps_jit_args& g, const uint3 bi) {{
+extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
     extern __shared__ __align__(16) unsigned char ps_smem[];
-    const long long {udecl};
+{head}    const long long {udecl};
 {guard}
     {pos};
     (void)ps_smem;
 {chr(10).join(decl)}{zpre}
 {chr(10).join(body)}
 {zpost}
-}}
-extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
-    ps_jit_body(g, jl_block(g));
-    jl_block_done(g);
-}}
+{tail}}}
 """
 
 
-# Block order of a boundary-first launch (ps_jit_hide_communication): with g.ocnt set, the 1-D
-# grid's first ord[9] blocks take the tiles holding boundary indices -- whole layers at both ends of
-# z, then whole rows at both ends of y, then column ends of x -- the rest the inner block; each
+# Block order of the boundary-first variant (ps_jit_hide_communication): the 1-D grid's first
+# ord[9] blocks take the tiles holding boundary indices -- whole layers at both ends of z, then
+# whole rows at both ends of y, then column ends of x -- the rest the inner block; each warp of a
 # boundary block counts itself in host-mapped memory once its stores are done.
 _BLOCK_ORDER = r"""
 __device__ __forceinline__ uint3 jl_block(const ps_jit_args& g) {
-    if (!g.ocnt) return blockIdx;
     const int TX = g.ord[0], TY = g.ord[1], TZ = g.ord[2], bx0 = g.ord[3], bx1 = g.ord[4], by0 = g.ord[5],
               by1 = g.ord[6], bz0 = g.ord[7], bz1 = g.ord[8], nb = g.ord[9];
     int i = (int)blockIdx.x;
@@ -1113,10 +1116,11 @@ __device__ __forceinline__ uint3 jl_block(const ps_jit_args& g) {
     return make_uint3(c < bx0 ? c : TX - bx1 + (c - bx0), by0 + r / ex, z);
 }
 __device__ __forceinline__ void jl_block_done(const ps_jit_args& g) {
-    if (!g.ocnt || (int)blockIdx.x >= g.ord[9]) return;
+    if ((int)blockIdx.x >= g.ord[9]) return;
     __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) { __threadfence_system(); atomicAdd_system(g.ocnt, 1u); }
+    __syncwarp();
+    const unsigned t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    if ((t & 31u) == 0) { __threadfence_system(); atomicAdd_system(g.ocnt, 1u); }
 }
 """
 
@@ -1207,8 +1211,9 @@ def generate(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False) -> str:
     return _Gen(kd, ndims, zloop).source(dtype)
 
 
-def _generate_info(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False, split: bool = False):
-    g = _Gen(kd, ndims, zloop, split)
+def _generate_info(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False, split: bool = False,
+                   ordered: bool = False):
+    g = _Gen(kd, ndims, zloop, split, ordered)
     src = g.source(dtype)
     return src, g.uses_collectives
 
@@ -1235,10 +1240,10 @@ class JitKernel:
     def source(self, ndims, dtype="double"):
         return generate(self.kd, ndims, dtype)
 
-    def _handle(self, ndims, dtype, zloop=False, split=False):
-        key = (ndims, dtype, bool(zloop), bool(split))
+    def _handle(self, ndims, dtype, zloop=False, split=False, ordered=False):
+        key = (ndims, dtype, bool(zloop), bool(split)) + (("ordered",) if ordered else ())
         if key not in self._handles:
-            src, self._collective[key] = _generate_info(self.kd, ndims, dtype, zloop, split)
+            src, self._collective[key] = _generate_info(self.kd, ndims, dtype, zloop, split, ordered)
             h = ctypes.c_void_p()
             _lib.call("ps_jit_compile", src.encode(), b"ps_jit_entry", ctypes.byref(h))
             self._handles[key] = h
@@ -1276,12 +1281,12 @@ class JitKernel:
         """One boundary-first launch over the kernel's full grid (ps_jit_hide_communication); comm_fn
         (a ps_comm_fn) runs once the boundary tiles are done."""
         h, A, nA, S, nS, lo, cnt, threads, shmem, loop = self._config(args, None, None, None, None, memopt, loopsize,
-                                                                     fp64)
+                                                                     fp64, ordered=True)
         _lib.call("ps_jit_hide_communication", h, A, nA, S, nS, (ctypes.c_int64 * 3)(*cnt),
                   (ctypes.c_int32 * 3)(*threads), (ctypes.c_int32 * 3)(*loop), (ctypes.c_int64 * 3)(*bw), comm_fn,
                   None, stream_handle(stream))
 
-    def _config(self, args, ranges, nblocks, nthreads, shmem, memopt, loopsize, fp64):
+    def _config(self, args, ranges, nblocks, nthreads, shmem, memopt, loopsize, fp64, ordered=False):
         """Handle, argument arrays and launch geometry of one launch (see jit_launch)."""
         require_initialized()
         if len(args) != self.nargs:
@@ -1340,8 +1345,9 @@ class JitKernel:
         if fp64 not in ("ieee", "split", "split_state", "split_grid"):
             raise ArgumentError("fp64 must be 'ieee' or 'split'")
         sp = fp64 != "ieee" and dt == "double"
-        h = self._handle(ndims, dt, zl, sp)
-        if self._collective[(ndims, dt, zl, sp)] and any(cnt[d] % threads[d] for d in range(3)):
+        h = self._handle(ndims, dt, zl, sp, ordered)
+        if self._collective[(ndims, dt, zl, sp) + (("ordered",) if ordered else ())] and \
+                any(cnt[d] % threads[d] for d in range(3)):
             raise ArgumentError("a kernel with @sync_threads, shuffles or votes needs ranges that are a multiple of "
                                 f"the thread block (ranges {cnt}, nthreads {threads})")
         A = (PSArray * max(1, len(descs)))(*descs)

@@ -170,8 +170,8 @@ def test_translator_rejects(jit, src, msg):
 def test_translator_generated_structure(jit):
     src = jit.generate(jit.parse(K.HEAT_FLUX), 3, "double")
     assert "extern \"C\" __global__ void ps_jit_entry(const ps_jit_args g)" in src
-    assert "fx" not in src.split("void ps_jit_body")[1]  # the on-the-fly arrays are inlined
-    body = src.split("void ps_jit_body")[1]
+    assert "fx" not in src.split("ps_jit_entry")[1]  # the on-the-fly arrays are inlined
+    body = src.split("ps_jit_entry")[1]
     assert body.count("__ldg(") == 8  # the 8 distinct stencil points, each read once (read-only arrays)
     assert "tx + 2 < n1_0" in body and "atomicOr(g.err, 1)" in body  # one bounds check per statement
     assert "tx < n0_0 - 2 && ty < n0_1 - 2 && tz < n0_2 - 2" in src  # @within("@inn", Tnew)
@@ -307,18 +307,18 @@ def test_translator_y_sweep_of_2d_kernels(jit):
     """memopt for 2-D `@parallel` kernels sweeps y (loopdim 2): blockIdx.y covers g.loop consecutive y
     indices and the two T points one row further along y come from the previous row's registers."""
     src = jit.generate(jit.parse(K.HEAT2D_FD), 2, "double", zloop=True)
-    body = src.split("void ps_jit_body")[1]
-    assert "const long long uy = bi.y * g.loop + it_;" in body
+    body = src.split("ps_jit_entry")[1]
+    assert "const long long uy = blockIdx.y * g.loop + it_;" in body
     assert "threadIdx.y" not in body
     carried = re.findall(r"const R (L\d+) = pr(\d) \? P\d_\d+ : (.*?);", body)
     assert len(carried) == 2 and all("a1[" in ld for _, _, ld in carried)  # T (argument 1) only
     plain = jit.generate(jit.parse(K.HEAT2D_FD), 2, "double")
-    assert "g.loop" not in plain.split("void ps_jit_body")[1]
+    assert "g.loop" not in plain.split("ps_jit_entry")[1]
 
 
 def test_translator_z_sweep_carries_only_read_only_points(jit):
     src = jit.generate(jit.parse(K.TWO3D), 3, "double", zloop=True)
-    body = src.split("void ps_jit_body")[1]
+    body = src.split("ps_jit_entry")[1]
     assert "for (long long it_ = 0; it_ < g.loop; ++it_)" in body
     carried = re.findall(r"const R (L\d+) = pr(\d) \? P\d_\d+ : (.*?);", body)
     assert carried and all("a2[" in ld for _, _, ld in carried)  # only B (argument 2) is read-only
@@ -332,7 +332,7 @@ def test_kernel_language_keeps_one_point_per_thread(jit):
            "    return\nend")
     kd = jit.parse(src)
     assert jit.uses_kernel_language(kd)
-    assert "g.loop" not in jit.generate(kd, 3, "double", zloop=True).split("void ps_jit_body")[1]
+    assert "g.loop" not in jit.generate(kd, 3, "double", zloop=True).split("ps_jit_entry")[1]
     assert not jit.uses_kernel_language(jit.parse(K.HEAT_FLUX))
 
 
@@ -370,9 +370,9 @@ def test_translator_language_additions(jit):
                      ("INT_EXPR2D", 2)):
         src = jit.generate(jit.parse(getattr(K, name)), nd, "float")
         assert "ps_jit_entry" in src
-    body = jit.generate(jit.parse(K.LOCAL_FN), 3, "double").split("void ps_jit_body")[1]
+    body = jit.generate(jit.parse(K.LOCAL_FN), 3, "double").split("ps_jit_entry")[1]
     assert "compute_indices" not in body
-    body = jit.generate(jit.parse(K.INT_EXPR2D), 2, "float").split("void ps_jit_body")[1]
+    body = jit.generate(jit.parse(K.INT_EXPR2D), 2, "float").split("ps_jit_entry")[1]
     assert "- 1LL" in body and "(R)1.0" not in body
     assert jit.parse(K.SPLAT_COPY).splat == "I"
 
