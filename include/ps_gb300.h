@@ -283,7 +283,8 @@ int ps_acoustic3d_step(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
                        int32_t fp64_mode, void* stream, int sync);
 /* nt steps of the miniapp's time loop on (Vx, Vy, Vz, P) in place: ps_acoustic3d_step alternating
  * between the caller's arrays and a second set in library scratch (grow-only, one per device and
- * stream, freed by ps_finalize); odd nt ends with a copy back. Asynchronous on `stream`. */
+ * stream, freed by ps_finalize); odd nt ends with a copy back. IEEE FP64 (FP64-pipe bound, where
+ * the two kernels are faster) runs ps_acoustic3d_v / _p in place. Asynchronous on `stream`. */
 int ps_acoustic3d_run(ps_array Vx, ps_array Vy, ps_array Vz, ps_array P,
                       double dt, double rho, double k, double dx, double dy, double dz,
                       int64_t nt, int32_t fp64_mode, void* stream);
@@ -506,9 +507,9 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
  * `@parallel` kernel over its full grid (count threads from index 0; threads and loop as for
  * ps_jit_launch_ex; no dynamic shared memory, no barriers, shuffles or votes). One launch on
  * `stream` whose first blocks take the tiles holding the boundary indices t < bw or t >= count - bw
- * (the reference's ranges_outer, src/ParallelKernel/hide_communication.jl:350-394); each warp of
- * such a block counts itself in host-mapped memory after its stores, and `comm` runs on this thread
- * as soon as all have, while the inner blocks still run. The kernel must be the boundary-first
+ * (the reference's ranges_outer, src/ParallelKernel/hide_communication.jl:350-394); each such block
+ * counts itself in host-mapped memory after its stores, and `comm` runs on this thread as soon as
+ * all have, while the inner blocks still run. The kernel must be the boundary-first
  * variant of the definition (ps_gb300/jit.py generates it with the order decode and the count). Returns after the launch completes, with the
  * kernel's flags reported as by a synchronous launch. */
 int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars,

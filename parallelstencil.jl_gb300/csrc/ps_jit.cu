@@ -285,8 +285,7 @@ int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narr
     const int ov[10] = {o.TX, o.TY, o.TZ, o.bx0, o.bx1, o.by0, o.by1, o.bz0, o.bz1, o.nb};
     memcpy(g.ord, ov, sizeof(ov));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // each warp of a boundary block counts itself (no block-wide barrier in the generated kernel)
-    const unsigned need = (unsigned)o.nb * (unsigned)(((int64_t)threads[0] * threads[1] * threads[2] + 31) / 32);
+    const unsigned need = (unsigned)o.nb;  // each boundary block counts itself once
     *hc = 0u;
     PS_TRY(jit_cu_launch(k, (unsigned)(gd[0] * gd[1] * gd[2]), 1, 1, threads, 0, &g, stream));
     PS_TRY(finish_launch(s, 0, "ps_jit_hide_communication"));

@@ -76,10 +76,13 @@ def test_acoustic3d_fused_step_equals_the_two_kernels(ps, oracle, dtn, n):
         assert np.array_equal(ps.to_host(d), a)
 
 
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
 @pytest.mark.parametrize("nt", [7, 8])
-def test_acoustic3d_run_in_place(ps, oracle, nt):
+def test_acoustic3d_run_in_place(ps, oracle, nt, dtn):
+    """ps_acoustic3d_run: FP32 alternates with the library's second set (odd nt copies back), IEEE
+    FP64 runs the two kernels in place; both equal the oracle's loop bit for bit."""
     n = (40, 35, 45)
-    P, (Vx, Vy, Vz), (dx, dy, dz), dts = _acoustic_setup(n, np.float64, seed=5)
+    P, (Vx, Vy, Vz), (dx, dy, dz), dts = _acoustic_setup(n, DT[dtn], seed=5)
     d = [ps.from_host(a) for a in (Vx, Vy, Vz, P)]
     for _ in range(nt):
         oracle.acoustic3d_v(Vx, Vy, Vz, P, dts, 1.0, dx, dy, dz)
