@@ -1158,7 +1158,7 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
         return
-    if a.only_run in ("stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "acoustic3d_fused",
+    if a.only_run in ("stokes2d", "stokes3d", "stokes3d_fused32", "acoustic3d", "memcopy", "adjoint", "acoustic3d_fused",
                       "acoustic3d_fused32", "acoustic3d_fused_split"):  # --steps calls, size --n
         from ps_gb300 import adjoint, stokes, stokes3d
 
@@ -1167,11 +1167,12 @@ def only_run(a):
             g = stokes.Stokes2D(stokes.Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog)
             g.compute_timesteps()
             g.iterate(a.steps)
-        elif a.only_run == "stokes3d":  # three-launch PT iteration, FP64, n^3
-            Mus, Rog = stokes3d.inclusion_setup(n, n, n)
-            g = stokes3d.Stokes3D(stokes3d.Stokes3DParams(n, n, n), Mus, Rog)
+        elif a.only_run in ("stokes3d", "stokes3d_fused32"):  # PT iterations, FP64 three launches / FP32 one
+            dtp = np.float32 if a.only_run.endswith("32") else np.float64
+            Mus, Rog = stokes3d.inclusion_setup(n, n, n, dtype=dtp)
+            g = stokes3d.Stokes3D(stokes3d.Stokes3DParams(n, n, n), Mus, Rog, dtype=dtp)
             g.compute_timesteps()
-            g.iterate(a.steps)
+            g.iterate(a.steps, one_launch=a.only_run.endswith("32"))
         elif a.only_run == "acoustic3d":
             h = 40.0 / (n - 1)
             P = ps.ones(n, n, n)
@@ -1268,7 +1269,8 @@ def main():
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
                                                  "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd", "fd32",
                                                  "stokes2d_apt", "stokes2d_apt32", "adjoint_grid", "acoustic3d_fused",
-                                                 "acoustic3d_fused32", "acoustic3d_fused_split", "hide", "miniapps"], default=None,
+                                                 "acoustic3d_fused32", "acoustic3d_fused_split", "hide", "miniapps", "stokes3d_fused32"],
+                    default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
                          "problem) and exit")

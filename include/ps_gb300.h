@@ -448,6 +448,13 @@ int ps_bc_z3d(ps_array A, void* stream, int sync);
  * compute_V!, six bc calls) in three launches each, bit-identical to the reference's sequence.
  * Synchronises. */
 int ps_stokes3d_iterate(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, int64_t n_iter, void* stream);
+/* The same with a choice of schedule. one_launch = 0: three kernels per iteration (compute_P! +
+ * compute_τ!, compute_dV! + compute_V!, the six free-slip copies), every array stored each
+ * iteration. one_launch = 1: pairs of single-kernel iterations (the state through a second set in
+ * library scratch, grow-only, one per device and stream; ∇V, τ and R kept on chip), then the storing
+ * kernels for the last one or two iterations; every array ends bit-identical to one_launch = 0. */
+int ps_stokes3d_iterate_ex(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, int64_t n_iter,
+                           int32_t one_launch, void* stream);
 
 /* mean(abs.(Rx)), mean(abs.(Ry)), mean(abs.(Rz)), mean(abs.(∇V)) of the stored arrays
  * (Stokes3D.jl:145-146), accumulated in FP64. */

@@ -50,6 +50,7 @@ void stokes2d_static_forget();  // drop the cached device addresses of the stati
 void diffusion_free_scratch();
 void adjoint_free_scratch();
 void acoustic_free_scratch();
+void stokes3d_free_scratch();
 
 // Copies `bytes` (<= 256 through pinned staging) from device memory on stream s and synchronises s.
 int read_device_words(void* dst, const void* src, size_t bytes, cudaStream_t s);

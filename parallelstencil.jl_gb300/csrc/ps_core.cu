@@ -400,6 +400,7 @@ int ps_finalize(void) {
     diffusion_free_scratch();
     adjoint_free_scratch();
     acoustic_free_scratch();
+    stokes3d_free_scratch();
     stokes2d_static_forget();
     for (int d = 0; d < kMaxDevices; d++) {
         DeviceState& st = g_dev[d];

@@ -23,6 +23,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <utility>
+#include <mutex>
+#include <map>
 
 #include "ps_common.cuh"
 
@@ -354,6 +357,207 @@ __global__ void s3_bc_k(S3A<T> a) {
     }
 }
 
+// ---- one launch per iteration ----------------------------------------------------------------
+// s3_fused_k runs compute_P!, compute_τ!, compute_dV!, compute_V! and the six free-slip copies of
+// one iteration (Stokes3D.jl:131-137) as one z-sweep. The state moves from (V, Pt) to (V2, Pt2):
+// neighbouring CTAs read each other's old V and Pt while writing their own. dVdτ is updated in
+// place (each value only at its own face). The stresses, ∇V and R live in registers and shared
+// memory only: per cell 20 words move (V, Pt, dτPt, Mus, Rog, dVdτ, dτV read, V2, Pt2, dVdτ
+// written) against ~40 for the kernels that store them.
+//
+// Block: 32 x S3F_TY threads at positions X = 30 bx - 1 + tx, Y = (S3F_TY - 2) by - 1 + ty; the
+// outer ring only computes the quantities its neighbours need. A position holds the cell (X, Y, k),
+// the faces Vx (X, Y, k) (low x side of cell X), Vy (X, Y, k) and Vz (X, Y, k) (low z side), the
+// x-y edge at the cell's low-x low-y corner (τxy) and, one level up, the x-z and y-z edges at its
+// low-x / low-y side between planes k and k+1 (τxz, τyz). Per plane k: (1) every thread computes
+// the plane-k quantities of its position and the level-(k+1/2) edges; (2) Rx, Ry of the faces in
+// plane k and Rz of the Vz face k (between cells k-1 and k) from its own values and those of the
+// neighbours in shared memory; (3) the updates and the free-slip copies: the thread of an inner
+// face writes the boundary faces that copy it (s3_bc_k's clamped source), faces outside the
+// updated range keep their old value. Bit-identical to the one-to-one kernels (same operations on
+// the same operands, in the reference's order).
+constexpr int S3F_TY = 16;
+
+template <typename T>
+struct S3Out {
+    T *Vx, *Vy, *Vz, *Pt;
+};
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(32 * S3F_TY) s3_fused_k(S3A<T> a, S3Out<T> o, S3P<T> p, int Lz) {
+    static_assert(MODE == S3_PLAIN || MODE == S3_DEFECT, "update modes only");
+    __shared__ T sPt[S3F_TY][32], sTxx[S3F_TY][32], sTyy[S3F_TY][32], sTxy[S3F_TY][32];
+    __shared__ T sLxz[2][S3F_TY][32], sLyz[2][S3F_TY][32];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t nx = a.nx, ny = a.ny, nz = a.nz;
+    const int64_t X = (int64_t)blockIdx.x * 30 - 1 + tx, Y = (int64_t)blockIdx.y * (S3F_TY - 2) - 1 + ty;
+    const int64_t z0 = (int64_t)blockIdx.z * Lz, z1 = z0 + Lz < nz + 1 ? z0 + Lz : nz + 1;
+    const bool own = tx >= 1 && tx <= 30 && ty >= 1 && ty <= S3F_TY - 2;
+    const T* M = a.Mus;
+    // existence of this position's objects in x-y
+    const bool pos = X >= 0 && Y >= 0;
+    const bool cell_xy = pos && X < nx && Y < ny;
+    const bool vx_xy = pos && X <= nx && Y < ny, vy_xy = pos && X < nx && Y <= ny;
+    const bool xin = X >= 1 && X <= nx - 2, yin = Y >= 1 && Y <= ny - 2;
+    const bool txy_xy = X >= 1 && X <= nx - 1 && Y >= 1 && Y <= ny - 1;
+    const bool txz_xy = X >= 1 && X <= nx - 1 && yin;  // τxz at (X-1, Y-1, .)
+    const bool tyz_xy = xin && Y >= 1 && Y <= ny - 1;  // τyz at (X-1, Y-1, .)
+    auto VX = [&](int64_t x, int64_t y, int64_t z) { return I3(x, y, z, nx + 1, ny); };
+    auto VY = [&](int64_t x, int64_t y, int64_t z) { return I3(x, y, z, nx, ny + 1); };
+    auto VZ = [&](int64_t x, int64_t y, int64_t z) { return I3(x, y, z, nx, ny); };
+    auto C3 = [&](int64_t x, int64_t y, int64_t z) { return I3(x, y, z, nx, ny); };
+
+    // carried along z: own V faces of plane k, Mus of plane k at (X,Y), (X-1,Y), (X,Y-1); from
+    // plane k-1: τzz and the new Pt of the own cell, Rog; the own edges of level k-1/2
+    T vx = 0, vy = 0, vz = 0, m00 = 0, m10 = 0, m01 = 0;
+    T tzz_m = 0, pt_m = 0, rog_m = 0, lxz_m = 0, lyz_m = 0;
+    const int64_t kb = z0 >= 1 ? z0 - 1 : 0;  // plane k0-1 is recomputed for Rz of face k0
+    if (kb < nz) {
+        if (vx_xy) vx = a.Vx[VX(X, Y, kb)];
+        if (vy_xy) vy = a.Vy[VY(X, Y, kb)];
+        if (cell_xy) vz = a.Vz[VZ(X, Y, kb)];
+        if (cell_xy) m00 = M[C3(X, Y, kb)];
+        if (X >= 1 && X <= nx && Y >= 0 && Y < ny) m10 = M[C3(X - 1, Y, kb)];
+        if (Y >= 1 && Y <= ny && X >= 0 && X < nx) m01 = M[C3(X, Y - 1, kb)];
+    }
+    for (int64_t k = kb; k < z1; ++k) {
+        const bool plane = k < nz;  // plane k holds cells (k = nz: only the Vz faces k)
+        const bool out = own && k >= z0;
+        // ---- loads of plane k+1 (own faces and Mus) and the neighbour values of plane k
+        T vx_n = 0, vy_n = 0, vz_n = 0, m00_n = 0, m10_n = 0, m01_n = 0, m11 = 0;
+        T vx_r = 0, vy_u = 0, vx_d = 0, vy_l = 0, vzl_n = 0, vzd_n = 0;
+        if (plane) {
+            if (vx_xy && k + 1 < nz) vx_n = a.Vx[VX(X, Y, k + 1)];
+            if (vy_xy && k + 1 < nz) vy_n = a.Vy[VY(X, Y, k + 1)];
+            if (cell_xy) vz_n = a.Vz[VZ(X, Y, k + 1)];  // face k+1 <= nz
+            if (cell_xy && k + 1 < nz) m00_n = M[C3(X, Y, k + 1)];
+            if (X >= 1 && X <= nx && Y >= 0 && Y < ny && k + 1 < nz) m10_n = M[C3(X - 1, Y, k + 1)];
+            if (Y >= 1 && Y <= ny && X >= 0 && X < nx && k + 1 < nz) m01_n = M[C3(X, Y - 1, k + 1)];
+            if (X >= 1 && Y >= 1 && X <= nx && Y <= ny) m11 = M[C3(X - 1, Y - 1, k)];
+            if (cell_xy) {
+                vx_r = a.Vx[VX(X + 1, Y, k)];
+                vy_u = a.Vy[VY(X, Y + 1, k)];
+            }
+            if (txy_xy) {
+                vx_d = a.Vx[VX(X, Y - 1, k)];
+                vy_l = a.Vy[VY(X - 1, Y, k)];
+            }
+            if (txz_xy && k + 1 < nz) vzl_n = a.Vz[VZ(X - 1, Y, k + 1)];
+            if (tyz_xy && k + 1 < nz) vzd_n = a.Vz[VZ(X, Y - 1, k + 1)];
+        }
+        // ---- plane-k quantities of this position and its level-(k+1/2) edges
+        T pt_new = 0, d = 0, txx = 0, tyy = 0, tzz = 0, txy = 0, lxz = 0, lyz = 0, rog = 0;
+        if (plane && cell_xy) {
+            const int64_t c = C3(X, Y, k);
+            d = (div_c(vx_r - vx, p.dx) + div_c(vy_u - vy, p.dy)) + div_c(vz_n - vz, p.dz);
+            T dp = d;
+            if constexpr (MODE == S3_DEFECT) dp = d + a.fp[c];
+            pt_new = a.Pt[c] - a.dtPt[c] * dp;
+            if constexpr (MODE == S3_PLAIN) rog = a.Rog[c];
+            if (yin && k >= 1 && k <= nz - 2) txx = s3_tnn(m00, vx_r, vx, p.dx, d);
+            if (xin && k >= 1 && k <= nz - 2) tyy = s3_tnn(m00, vy_u, vy, p.dy, d);
+            if (xin && yin) tzz = s3_tnn(m00, vz_n, vz, p.dz, d);
+        }
+        if (plane && txy_xy && k >= 1 && k <= nz - 2)
+            txy = s3_tsh(m11, m01, m10, m00, vx - vx_d, p.dy, vy - vy_l, p.dx);
+        if (plane && txz_xy && k <= nz - 2) lxz = s3_tsh(m10, m00, m10_n, m00_n, vx_n - vx, p.dz, vz_n - vzl_n, p.dx);
+        if (plane && tyz_xy && k <= nz - 2) lyz = s3_tsh(m01, m00, m01_n, m00_n, vy_n - vy, p.dz, vz_n - vzd_n, p.dy);
+        __syncthreads();  // A: the previous plane's neighbour reads are done
+        sPt[ty][tx] = pt_new;
+        sTxx[ty][tx] = txx;
+        sTyy[ty][tx] = tyy;
+        sTxy[ty][tx] = txy;
+        sLxz[k & 1][ty][tx] = lxz;
+        sLyz[k & 1][ty][tx] = lyz;
+        __syncthreads();  // B: plane k and level k+1/2 published
+        if (out) {
+            // compute_dV! / compute_V! of the faces of this position (r: index of R, dVdτ, dτV)
+            const int64_t r = I3(X - 1, Y - 1, k - 1, nx - 1, ny - 2);
+            T ux = vx;  // the updated Vx face (X, Y, k): old value outside @inn
+            if (plane && X >= 1 && X <= nx - 1 && yin && k >= 1 && k <= nz - 2) {
+                const T A = txx - sTxx[ty][tx - 1], B = sTxy[ty + 1][tx] - txy, Cc = lxz - lxz_m;
+                const T P = pt_new - sPt[ty][tx - 1];
+                T R = ((div_c(A, p.dx) + div_c(B, p.dy)) + div_c(Cc, p.dz)) - div_c(P, p.dx);
+                if constexpr (MODE == S3_DEFECT) R = R + a.fx[r];
+                const T dv = p.dampX * a.dVx[r] + R;
+                a.dVx[r] = dv;
+                ux = vx + a.dtVx[r] * dv;
+            }
+            T uy = vy;
+            if (plane && xin && Y >= 1 && Y <= ny - 1 && k >= 1 && k <= nz - 2) {
+                const int64_t ry = I3(X - 1, Y - 1, k - 1, nx - 2, ny - 1);
+                const T A = tyy - sTyy[ty - 1][tx], B = sTxy[ty][tx + 1] - txy, Cc = lyz - lyz_m;
+                const T P = pt_new - sPt[ty - 1][tx];
+                T R = ((div_c(A, p.dy) + div_c(B, p.dx)) + div_c(Cc, p.dz)) - div_c(P, p.dy);
+                if constexpr (MODE == S3_DEFECT) R = R + a.fy[ry];
+                const T dv = p.dampY * a.dVy[ry] + R;
+                a.dVy[ry] = dv;
+                uy = vy + a.dtVy[ry] * dv;
+            }
+            T uz = vz;
+            if (xin && yin && k >= 1 && k <= nz - 1) {
+                const int64_t rz = I3(X - 1, Y - 1, k - 1, nx - 2, ny - 2);
+                const T A = tzz - tzz_m;
+                const T B = sLxz[(k - 1) & 1][ty][tx + 1] - lxz_m, Cc = sLyz[(k - 1) & 1][ty + 1][tx] - lyz_m;
+                const T P = pt_new - pt_m;
+                T R;
+                if constexpr (MODE == S3_DEFECT) {
+                    R = (((div_c(A, p.dz) + div_c(B, p.dx)) + div_c(Cc, p.dy)) - div_c(P, p.dz)) + a.fz[rz];
+                } else {
+                    const T G = (rog_m + rog) * T(0.5);
+                    R = (((div_c(A, p.dz) + div_c(B, p.dx)) + div_c(Cc, p.dy)) - div_c(P, p.dz)) + G;
+                }
+                const T dv = p.dampZ * a.dVz[rz] + R;
+                a.dVz[rz] = dv;
+                uz = vz + a.dtVz[rz] * dv;
+            }
+            // the new state and the free-slip copies (bc_y!(Vx), bc_z!(Vx), bc_x!(Vy), bc_z!(Vy),
+            // bc_x!(Vz), bc_y!(Vz)): the source of a copied face is the face with its copied axes
+            // clamped into [1, n-2]; that source's thread writes it
+            if (plane && vx_xy && yin && k >= 1 && k <= nz - 2) {
+                const int ny0 = Y == 1 ? 1 : 0, ny1 = Y == ny - 2 ? 1 : 0, nz0 = k == 1 ? 1 : 0, nz1 = k == nz - 2 ? 1 : 0;
+                for (int dy = -ny0; dy <= ny1; ++dy)
+                    for (int dz = -nz0; dz <= nz1; ++dz) o.Vx[VX(X, Y + dy, k + dz)] = ux;
+            }
+            if (plane && vy_xy && xin && k >= 1 && k <= nz - 2) {
+                const int nx0 = X == 1 ? 1 : 0, nx1 = X == nx - 2 ? 1 : 0, nz0 = k == 1 ? 1 : 0, nz1 = k == nz - 2 ? 1 : 0;
+                for (int dx = -nx0; dx <= nx1; ++dx)
+                    for (int dz = -nz0; dz <= nz1; ++dz) o.Vy[VY(X + dx, Y, k + dz)] = uy;
+            }
+            if (cell_xy && xin && yin) {  // Vz faces k = 0 .. nz
+                const int nx0 = X == 1 ? 1 : 0, nx1 = X == nx - 2 ? 1 : 0, ny0 = Y == 1 ? 1 : 0, ny1 = Y == ny - 2 ? 1 : 0;
+                for (int dx = -nx0; dx <= nx1; ++dx)
+                    for (int dy = -ny0; dy <= ny1; ++dy) o.Vz[VZ(X + dx, Y + dy, k)] = uz;
+            }
+            if (plane && cell_xy) o.Pt[C3(X, Y, k)] = pt_new;
+        }
+        // ---- carry to plane k+1
+        tzz_m = tzz;
+        pt_m = pt_new;
+        rog_m = rog;
+        lxz_m = lxz;
+        lyz_m = lyz;
+        vx = vx_n;
+        vy = vy_n;
+        vz = vz_n;
+        m00 = m00_n;
+        m10 = m10_n;
+        m01 = m01_n;
+    }
+}
+
+template <typename T, int MODE>
+static void s3_fused_launch(const S3A<T>& a, const S3Out<T>& o, const S3P<T>& p, cudaStream_t s) {
+    static int occ = 0;
+    if (!occ) occ = resident_ctas(s3_fused_k<T, MODE>, 32 * S3F_TY, 0);
+    DeviceState* st = nullptr;
+    current_state(&st);
+    const int64_t gx = (a.nx + 1 + 29) / 30, gy = (a.ny + 1 + S3F_TY - 3) / (S3F_TY - 2);
+    int Lz = auto_loopsize(gx * gy, a.nz + 1, (int64_t)occ * (st ? st->num_sms : 152));
+    const dim3 grd((unsigned)gx, (unsigned)gy, (unsigned)((a.nz + 1 + Lz - 1) / Lz));
+    s3_fused_k<T, MODE><<<grd, dim3(32, S3F_TY, 1), 0, s>>>(a, o, p, Lz);
+}
+
 // y32 = (float) x64 (rounding of the outer residual for the FP32 sweeps)
 __global__ void s3_to_f32(float* y, const double* x, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -489,19 +693,32 @@ static void s3_launch(S3Kernel k, const S3A<T>& a, const S3P<T>& p, cudaStream_t
     }
 }
 
-template <typename T>
-static void s3_iteration(const S3A<T>& a, const S3P<T>& p, cudaStream_t s) {
-    s3_launch(S3_PTAU, a, p, s);
-    s3_launch(S3_DVV, a, p, s);
-    s3_launch(S3_BC, a, p, s);
-}
-
-// the inner sweep of the mixed-precision solver (FP32 PT on the correction)
-static void s3_defect_iteration(const S3A<float>& a, const S3P<float>& p, cudaStream_t s) {
-    const dim3 b(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
-    s3_Ptau_k<float, S3_DEFECT><<<gc, b, 0, s>>>(a, p);
-    s3_dVV_k<float, S3_DEFECT><<<gc, b, 0, s>>>(a, p);
-    s3_launch(S3_BC, a, p, s);
+// n iterations of MODE on the state (a.Vx, a.Vy, a.Vz, a.Pt): pairs of one-launch iterations
+// through the second set B (the state is back in a's arrays after each pair), then the remaining
+// one or two iterations as the three kernels that also store ∇V, τ and R (the reference's loop
+// body leaves them, and the solvers' residual norms read them). With n >= 1 the last iteration
+// always stores. B.Vx.. B.Pt: arrays of the shapes of a's.
+template <typename T, int MODE>
+static void s3_iterations(const S3A<T>& a, const S3Out<T>& B, const S3P<T>& p, int64_t n, cudaStream_t s,
+                          bool one_launch) {
+    if (n <= 0) return;
+    const int64_t pairs = one_launch ? (n - 1) / 2 : 0;
+    S3A<T> b = a;
+    b.Vx = B.Vx;
+    b.Vy = B.Vy;
+    b.Vz = B.Vz;
+    b.Pt = B.Pt;
+    const S3Out<T> toB{B.Vx, B.Vy, B.Vz, B.Pt}, toA{a.Vx, a.Vy, a.Vz, a.Pt};
+    for (int64_t i = 0; i < pairs; ++i) {
+        s3_fused_launch<T, MODE>(a, toB, p, s);
+        s3_fused_launch<T, MODE>(b, toA, p, s);
+    }
+    const dim3 b3(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
+    for (int64_t i = 2 * pairs; i < n; ++i) {
+        s3_Ptau_k<T, MODE><<<gc, b3, 0, s>>>(a, p);
+        s3_dVV_k<T, MODE><<<gc, b3, 0, s>>>(a, p);
+        s3_launch(S3_BC, a, p, s);
+    }
 }
 
 // divV, the stresses and Rx, Ry, Rz of the FP64 state (the reference's statements, no update)
@@ -509,6 +726,40 @@ static void s3_residual(const S3A<double>& a, const S3P<double>& p, cudaStream_t
     const dim3 b(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
     s3_Ptau_k<double, S3_RESIDUAL><<<gc, b, 0, s>>>(a, p);
     s3_dVV_k<double, S3_RESIDUAL><<<gc, b, 0, s>>>(a, p);
+}
+
+// Library scratch of the iterate entry point: grow-only, one per device and stream.
+struct S3Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+static std::mutex g_s3_mutex;
+static std::map<std::pair<int, cudaStream_t>, S3Scratch> g_s3_scratch;
+
+static int s3_scratch(size_t bytes, char** out, cudaStream_t s) {
+    int dev = 0;
+    PS_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_s3_mutex);
+    S3Scratch& sc = g_s3_scratch[{dev, s}];
+    if (sc.bytes < bytes) {
+        if (sc.ptr) {
+            PS_CUDA_TRY(cudaStreamSynchronize(s));
+            PS_CUDA_TRY(cudaFree(sc.ptr));
+            sc.ptr = nullptr;
+            sc.bytes = 0;
+        }
+        PS_CUDA_TRY(cudaMalloc(&sc.ptr, bytes));
+        sc.bytes = bytes;
+    }
+    *out = static_cast<char*>(sc.ptr);
+    return PS_OK;
+}
+
+void stokes3d_free_scratch() {
+    std::lock_guard<std::mutex> lk(g_s3_mutex);
+    for (auto& kv : g_s3_scratch)
+        if (kv.second.ptr) cudaFree(kv.second.ptr);
+    g_s3_scratch.clear();
 }
 
 static int s3_entry(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, S3Kernel k, void* stream, int sync,
@@ -542,15 +793,16 @@ static int solve_mixed3(const ps_stokes3d_fields* f, const ps_stokes3d_params* p
     const int64_t nRx = (nx - 1) * (ny - 2) * (nz - 2), nRy = (nx - 2) * (ny - 1) * (nz - 2),
                   nRz = (nx - 2) * (ny - 2) * (nz - 1);
     // float buffers, in this order: δVx δVy δVz δP dVx dVy dVz (zeroed before every inner sweep),
-    // txx tyy tzz txy txz tyz divV Rx Ry Rz, dtPt dtVx dtVy dtVz Mus, fx fy fz fp
-    const int64_t cnt[26] = {nVx, nVy, nVz, nC, nRx, nRy, nRz,
+    // txx tyy tzz txy txz tyz divV Rx Ry Rz, dtPt dtVx dtVy dtVz Mus, fx fy fz fp, and the second
+    // set δVx δVy δVz δP of the one-launch sweeps
+    const int64_t cnt[30] = {nVx, nVy, nVz, nC, nRx, nRy, nRz,
                              numel(f->txx), numel(f->tyy), numel(f->tzz), numel(f->txy), numel(f->txz), numel(f->tyz),
-                             nC, nRx, nRy, nRz, nC, nRx, nRy, nRz, nC, nRx, nRy, nRz, nC};
-    size_t off[27];
+                             nC, nRx, nRy, nRz, nC, nRx, nRy, nRz, nC, nRx, nRy, nRz, nC, nVx, nVy, nVz, nC};
+    size_t off[31];
     off[0] = 0;
-    for (int k = 0; k < 26; k++) off[k + 1] = off[k] + ((cnt[k] * 4 + 255) / 256) * 256;
+    for (int k = 0; k < 30; k++) off[k + 1] = off[k] + ((cnt[k] * 4 + 255) / 256) * 256;
     float* base = nullptr;
-    PS_CUDA_TRY(cudaMalloc(&base, off[26]));
+    PS_CUDA_TRY(cudaMalloc(&base, off[30]));
     auto F = [&](int k) { return reinterpret_cast<float*>(reinterpret_cast<char*>(base) + off[k]); };
     S3A<float> a;
     a.Vx = F(0); a.Vy = F(1); a.Vz = F(2); a.Pt = F(3);
@@ -565,7 +817,8 @@ static int solve_mixed3(const ps_stokes3d_fields* f, const ps_stokes3d_params* p
     const S3P<double> p64 = s3p<double>(*pp);
     const S3A<double> a64 = s3a<double>(f);
     int rc = PS_OK;
-    cudaError_t e = cudaMemsetAsync(base, 0, off[26], s);
+    const S3Out<float> B32{F(26), F(27), F(28), F(29)};
+    cudaError_t e = cudaMemsetAsync(base, 0, off[30], s);
     s3_to_f32<<<1024, 256, 0, s>>>(F(21), a64.Mus, nC);
     s3_timesteps_k<float><<<g3(nx, ny, nz), dim3(32, 8, 1), 0, s>>>(a, p32);
     // the corrections keep the free-slip copies of the state they are added to: give the state
@@ -579,7 +832,7 @@ static int solve_mixed3(const ps_stokes3d_fields* f, const ps_stokes3d_params* p
     cudaGraphExec_t exec = nullptr;
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        for (int64_t i = 0; i < nout; ++i) s3_defect_iteration(a, p32, s);
+        s3_iterations<float, S3_DEFECT>(a, B32, p32, nout, s, false);
         cudaMemsetAsync(red_in, 0, 4 * sizeof(double), s);
         s3_sum_abs_k<float><<<gr, 256, 0, s>>>(a.Rx, nRx, a.Ry, nRy, a.Rz, nRz, a.divV, nC, red_in);
         e = cudaStreamEndCapture(s, &graph);
@@ -709,17 +962,46 @@ int ps_bc_y3d(ps_array A, void* stream, int sync) { return bc3(A, stream, sync, 
 int ps_bc_z3d(ps_array A, void* stream, int sync) { return bc3(A, stream, sync, 2, "ps_bc_z3d"); }
 
 int ps_stokes3d_iterate(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, int64_t n_iter, void* stream) {
+    return ps_stokes3d_iterate_ex(f, p, n_iter, 0, stream);
+}
+
+int ps_stokes3d_iterate_ex(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, int64_t n_iter,
+                           int32_t one_launch, void* stream) {
     DeviceState* st = nullptr;
     PS_TRY(current_state(&st));
     PS_TRY(check_fields3(f, true));
     if (!p) return fail(PS_ERR_NULL, "NULL params");
     if (n_iter < 0) return fail(PS_ERR_ARG, "n_iter must be >= 0");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    for (int64_t it = 0; it < n_iter; ++it) {
-        if (f->Pt.dtype == PS_F64)
-            s3_iteration<double>(s3a<double>(f), s3p<double>(*p), s);
-        else
-            s3_iteration<float>(s3a<float>(f), s3p<float>(*p), s);
+    if (n_iter == 0) return PS_OK;
+    if (!one_launch) {  // the three storing kernels per iteration, in place
+        for (int64_t it = 0; it < n_iter; ++it) {
+            if (f->Pt.dtype == PS_F64)
+                s3_iterations<double, S3_PLAIN>(s3a<double>(f), S3Out<double>{}, s3p<double>(*p), 1, s, false);
+            else
+                s3_iterations<float, S3_PLAIN>(s3a<float>(f), S3Out<float>{}, s3p<float>(*p), 1, s, false);
+        }
+        return finish_launch(s, 1, "ps_stokes3d_iterate");
+    }
+    // the second state set of the one-launch iterations (grow-only library scratch per device and stream)
+    const size_t es = elsize(f->Pt.dtype);
+    const size_t nb[4] = {(size_t)numel(f->Vx) * es, (size_t)numel(f->Vy) * es, (size_t)numel(f->Vz) * es,
+                          (size_t)numel(f->Pt) * es};
+    size_t off[4], total = 0;
+    for (int i = 0; i < 4; ++i) {
+        off[i] = total;
+        total += (nb[i] + 255) / 256 * 256;
+    }
+    char* base = nullptr;
+    PS_TRY(s3_scratch(total, &base, s));
+    if (f->Pt.dtype == PS_F64) {
+        const S3Out<double> B{reinterpret_cast<double*>(base + off[0]), reinterpret_cast<double*>(base + off[1]),
+                              reinterpret_cast<double*>(base + off[2]), reinterpret_cast<double*>(base + off[3])};
+        s3_iterations<double, S3_PLAIN>(s3a<double>(f), B, s3p<double>(*p), n_iter, s, one_launch != 0);
+    } else {
+        const S3Out<float> B{reinterpret_cast<float*>(base + off[0]), reinterpret_cast<float*>(base + off[1]),
+                             reinterpret_cast<float*>(base + off[2]), reinterpret_cast<float*>(base + off[3])};
+        s3_iterations<float, S3_PLAIN>(s3a<float>(f), B, s3p<float>(*p), n_iter, s, one_launch != 0);
     }
     return finish_launch(s, 1, "ps_stokes3d_iterate");
 }
@@ -775,9 +1057,23 @@ int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, 
     const dim3 gr((unsigned)std::max<int64_t>(1, std::min<int64_t>((n[3] + 1023) / 1024, 1024)), 4);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    // the second state set of the one-launch iterations
+    const size_t nb[4] = {(size_t)numel(f->Vx) * 8, (size_t)numel(f->Vy) * 8, (size_t)numel(f->Vz) * 8,
+                          (size_t)numel(f->Pt) * 8};
+    char* bbase = nullptr;
+    cudaError_t e = cudaMalloc(&bbase, (nb[0] + nb[1] + nb[2] + nb[3] + 1024));
+    S3Out<double> B{};
     if (e == cudaSuccess) {
-        for (int64_t i = 0; i < nout; ++i) s3_iteration<double>(a, pp, s);
+        size_t o = 0;
+        double** dst[4] = {&B.Vx, &B.Vy, &B.Vz, &B.Pt};
+        for (int i = 0; i < 4; ++i) {
+            *dst[i] = reinterpret_cast<double*>(bbase + o);
+            o += (nb[i] + 255) / 256 * 256;
+        }
+        e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    }
+    if (e == cudaSuccess) {
+        s3_iterations<double, S3_PLAIN>(a, B, pp, nout, s, false);
         cudaMemsetAsync(red, 0, 4 * sizeof(double), s);
         s3_sum_abs_k<double><<<gr, 256, 0, s>>>(a.Rx, n[0], a.Ry, n[1], a.Rz, n[2], a.divV, n[3], red);
         e = cudaStreamEndCapture(s, &graph);
@@ -816,6 +1112,7 @@ int ps_stokes3d_solve(const ps_stokes3d_fields* f, const ps_stokes3d_params* p, 
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     cudaStreamSynchronize(s);
+    if (bbase) cudaFree(bbase);
     cudaEventDestroy(ev);
     cudaStreamDestroy(s);
     cudaGetLastError();

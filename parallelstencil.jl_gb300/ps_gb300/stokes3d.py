@@ -45,6 +45,7 @@ for _name in ("ps_stokes3d_timesteps", "ps_stokes3d_compute_P", "ps_stokes3d_com
 for _name in ("ps_bc_x3d", "ps_bc_y3d", "ps_bc_z3d"):
     _lib.register(_name, [PSArray, ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_stokes3d_iterate", [_F, _PP, ctypes.c_int64, ctypes.c_void_p])
+_lib.register("ps_stokes3d_iterate_ex", [_F, _PP, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p])
 _lib.register("ps_stokes3d_err", [_F, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p])
 _lib.register("ps_stokes3d_solve", [_F, _PP, ctypes.c_double, ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
                                     ctypes.POINTER(PSSolveStats), ctypes.c_void_p])
@@ -144,9 +145,11 @@ class Stokes3D:
         for which, name in self.BC_SEQUENCE:
             self.bc(which, name)
 
-    def iterate(self, n_iter: int, stream=None):
-        _lib.call("ps_stokes3d_iterate", ctypes.byref(self._fields), ctypes.byref(self._p), int(n_iter),
-                  stream_handle(stream))
+    def iterate(self, n_iter: int, stream=None, one_launch=False):
+        """n_iter iterations of the miniapp's loop body (ps_stokes3d_iterate_ex); one_launch: pairs of
+        single-kernel iterations, ending with the storing kernels (bit-identical results)."""
+        _lib.call("ps_stokes3d_iterate_ex", ctypes.byref(self._fields), ctypes.byref(self._p), int(n_iter),
+                  int(bool(one_launch)), stream_handle(stream))
 
     def err(self, stream=None):
         out = (ctypes.c_double * 4)()

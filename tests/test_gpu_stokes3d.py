@@ -47,9 +47,11 @@ def test_stokes3d_golden(ps, golden, dtn):
 @pytest.mark.parametrize("dtn", ["f64", "f32"])
 @pytest.mark.parametrize("n", [(15, 13, 11), (34, 20, 17), (33, 33, 33)])
 def test_stokes3d_iterate_matches_oracle(ps, oracle, dtn, n):
-    """Three launches per iteration (fused P+τ, fused dV+V, all six copies) == the reference's loop."""
+    """Three launches per iteration (fused P+τ, fused dV+V, all six copies) == the reference's loop;
+    so do pairs of one-launch iterations (s3_fused_k) followed by the storing kernels."""
     g, o = _pair(ps, oracle, n, dtn)
-    g.iterate(25)
+    g.iterate(12)
+    g.iterate(13, one_launch=True)
     for _ in range(25):
         o.step()
     _same(g, o, STATE)
@@ -58,6 +60,25 @@ def test_stokes3d_iterate_matches_oracle(ps, oracle, dtn, n):
     rtol = 1e-12 if dtn == "f64" else 1e-5
     assert np.allclose(parts_g, parts_o, rtol=rtol, atol=0), (parts_g, parts_o)
     assert eg > 0
+
+
+@pytest.mark.parametrize("dtn", ["f64", "f32"])
+@pytest.mark.parametrize("n,iters", [((61, 29, 100), 5), ((31, 15, 7), 6), ((3, 3, 3), 4)])
+def test_stokes3d_one_launch_iterations_random_state(ps, oracle, dtn, n, iters):
+    """`iterate` runs pairs of one-launch iterations (s3_fused_k: the state through a second set,
+    the stresses and residuals in registers and shared memory) and ends with the storing kernels:
+    from a random state, every array equals the oracle's loop bit for bit. The sizes give several
+    blocks in x and y, several z sweeps, and the smallest grid."""
+    g, o = _pair(ps, oracle, n, dtn)
+    rng = np.random.default_rng(8)
+    for k in ("Pt", "Vx", "Vy", "Vz", "dVxdtau", "dVydtau", "dVzdtau"):
+        v = np.asfortranarray((0.1 * rng.standard_normal(o[k].shape)).astype(DT[dtn]))
+        o[k][...] = v
+        g[k].copy_(ps.from_host(v))
+    g.iterate(iters, one_launch=True)
+    for _ in range(iters):
+        o.step()
+    _same(g, o, STATE)
 
 
 def test_stokes3d_one_to_one_kernels_random_state(ps, oracle):
