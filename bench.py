@@ -896,6 +896,8 @@ def bench_hide_communication(ps, torch, n=512, bw=(16, 2, 2)):
     j = ps.parallel_kernel(JIT_DIFF_INV)
     out["jit_fp64_split_one_launch_ms"] = round(_events(torch, lambda: ps.parallel(j, *args, sync=False,
                                                                                    fp64="split"), 5) * 1e3, 4)
+    out["jit_fp64_split_one_launch_sync_ms"] = round(_events(torch, lambda: ps.parallel(j, *args, sync=True,
+                                                                                        fp64="split"), 5) * 1e3, 4)
     out["jit_fp64_split_split_ms"] = round(_events(torch, lambda: ps.hide_communication(
         bw, j, args, comm=lambda: None, fp64="split"), 5) * 1e3, 4)
     out["jit_fp64_split_payload_split_ms"] = round(_events(torch, lambda: ps.hide_communication(

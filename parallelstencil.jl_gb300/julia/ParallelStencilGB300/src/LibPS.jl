@@ -160,6 +160,21 @@ acoustic3d_p!(P, Vx, Vy, Vz, dt, k, dx, dy, dz; stream = CUDA.stream(), sync = t
     check(ccall((:ps_acoustic3d_p, lib), Cint,
                 (PSArray, PSArray, PSArray, PSArray, Cdouble, Cdouble, Cdouble, Cdouble, Cdouble, Ptr{Cvoid}, Cint),
                 desc(P), desc(Vx), desc(Vy), desc(Vz), dt, k, dx, dy, dz, stream_ptr(stream), Cint(sync)))
+# both statements in one kernel, old state -> new state (fp64_mode 0 IEEE, 1 FP32 pairs on FP64 arrays)
+acoustic3d_step!(Vx, Vy, Vz, P, Vx2, Vy2, Vz2, P2, dt, rho, k, dx, dy, dz; fp64_mode = 0, stream = CUDA.stream(),
+                 sync = true) =
+    check(ccall((:ps_acoustic3d_step, lib), Cint,
+                (PSArray, PSArray, PSArray, PSArray, PSArray, PSArray, PSArray, PSArray, Cdouble, Cdouble, Cdouble,
+                 Cdouble, Cdouble, Cdouble, Int32, Ptr{Cvoid}, Cint),
+                desc(Vx), desc(Vy), desc(Vz), desc(P), desc(Vx2), desc(Vy2), desc(Vz2), desc(P2), dt, rho, k, dx, dy,
+                dz, Int32(fp64_mode), stream_ptr(stream), Cint(sync)))
+# the miniapp's time loop in place (acoustic3D.jl:55-56)
+acoustic3d_run!(Vx, Vy, Vz, P, dt, rho, k, dx, dy, dz, nt; fp64_mode = 0, stream = CUDA.stream()) =
+    check(ccall((:ps_acoustic3d_run, lib), Cint,
+                (PSArray, PSArray, PSArray, PSArray, Cdouble, Cdouble, Cdouble, Cdouble, Cdouble, Cdouble, Int64, Int32,
+                 Ptr{Cvoid}),
+                desc(Vx), desc(Vy), desc(Vz), desc(P), dt, rho, k, dx, dy, dz, Int64(nt), Int32(fp64_mode),
+                stream_ptr(stream)))
 
 # ---- Stokes2D (miniapps/Stokes2D.jl) -------------------------------------------------------
 struct Stokes2DFields
@@ -276,9 +291,10 @@ for (jl, c) in ((:bc_x3d!, :ps_bc_x3d), (:bc_y3d!, :ps_bc_y3d), (:bc_z3d!, :ps_b
         check(ccall(($(QuoteNode(c)), lib), Cint, (PSArray, Ptr{Cvoid}, Cint), desc(A), stream_ptr(stream),
                     Cint(sync)))
 end
-stokes3d_iterate!(f::Stokes3DFields, p::Stokes3DParams, n_iter; stream = CUDA.stream()) =
-    check(ccall((:ps_stokes3d_iterate, lib), Cint, (Ref{Stokes3DFields}, Ref{Stokes3DParams}, Int64, Ptr{Cvoid}),
-                f, p, Int64(n_iter), stream_ptr(stream)))
+stokes3d_iterate!(f::Stokes3DFields, p::Stokes3DParams, n_iter; one_launch = false, stream = CUDA.stream()) =
+    check(ccall((:ps_stokes3d_iterate_ex, lib), Cint,
+                (Ref{Stokes3DFields}, Ref{Stokes3DParams}, Int64, Int32, Ptr{Cvoid}),
+                f, p, Int64(n_iter), Int32(one_launch), stream_ptr(stream)))
 function stokes3d_solve!(f::Stokes3DFields, p::Stokes3DParams, tol, max_iter, nout; mixed = false,
                          max_seconds = 0.0, stream = CUDA.stream())
     st = Ref(SolveStats(0, 0, 0.0, 0.0, 0, 0))
