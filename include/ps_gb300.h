@@ -512,7 +512,8 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
                      const int32_t loop[3], void* stream, int sync);
 /* `@hide_communication bw begin @parallel kernel!(...); comm() end` for a run-time compiled
  * `@parallel` kernel over its full grid (count threads from index 0; threads and loop as for
- * ps_jit_launch_ex; no dynamic shared memory, no barriers, shuffles or votes). One launch on
+ * ps_jit_launch_ex, at most 256 threads per block; no dynamic shared memory, no barriers, shuffles
+ * or votes). One launch on
  * `stream` whose first blocks take the tiles holding the boundary indices t < bw or t >= count - bw
  * (the reference's ranges_outer, src/ParallelKernel/hide_communication.jl:350-394); each such block
  * counts itself in host-mapped memory after its stores, and `comm` runs on this thread as soon as

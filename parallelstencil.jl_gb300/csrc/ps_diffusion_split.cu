@@ -1064,6 +1064,7 @@ __global__ void __launch_bounds__(32 * TY, 2)
                         int64_t nx, int64_t ny, Box cb, int L, int* __restrict__ err, GridRun* __restrict__ run,
                         const GridRun* __restrict__ mrun) {
     using C = AdjCfg<TY, S>;
+    grid_dependents_may_launch();  // glam_boundary_kernel of this step runs beside this kernel
     if (*reinterpret_cast<volatile int*>(&run->bad) || mrun->bad) return;
     const int sh = mrun->shT + run->shT;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1339,10 +1340,19 @@ static int launch_grid_adj(const ps_array& Min, const ps_array& Ls, const ps_arr
     kernel<<<grd, dim3(32, TY, 1), C::SMEM, s>>>(mM, mL, mC, mT, static_cast<float2*>(Mout.ptr),
                                                 static_cast<double*>(glam.ptr), p, gc[0], gc[1], gc[2], Mout.n[0],
                                                 Mout.n[1], cb, L, d_err, run, mrun);
+    // The boundary rows and planes of glam run beside the kernel above (programmatic dependent
+    // launch without a wait): they read μ and T_n, which the step before completed, and write glam
+    // cells the kernel above does not touch. The next step's launch waits for both.
     const int64_t nmax = std::max(Mout.n[0] * Mout.n[1], Mout.n[0] * Mout.n[2]);
-    glam_boundary_kernel<<<dim3((unsigned)std::min<int64_t>((nmax + 255) / 256, st->num_sms * 4), 4), 256, 0, s>>>(
-        static_cast<const float2*>(Min.ptr), static_cast<const float2*>(Tn.ptr), static_cast<double*>(glam.ptr),
-        gc[0], gc[1], gc[2], Mout.n[0], Mout.n[1], Mout.n[2], run, mrun);
+    const dim3 gb((unsigned)std::min<int64_t>((nmax + 255) / 256, st->num_sms * 4), 4);
+    if (launch_dependent(glam_boundary_kernel, gb, dim3(256), 0, s, static_cast<const float2*>(Min.ptr),
+                         static_cast<const float2*>(Tn.ptr), static_cast<double*>(glam.ptr), gc[0], gc[1], gc[2],
+                         Mout.n[0], Mout.n[1], Mout.n[2], static_cast<const GridRun*>(run), mrun) != cudaSuccess) {
+        cudaGetLastError();
+        glam_boundary_kernel<<<gb, 256, 0, s>>>(static_cast<const float2*>(Min.ptr), static_cast<const float2*>(Tn.ptr),
+                                                static_cast<double*>(glam.ptr), gc[0], gc[1], gc[2], Mout.n[0],
+                                                Mout.n[1], Mout.n[2], run, mrun);
+    }
     return PS_OK;
 }
 

@@ -263,6 +263,8 @@ int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narr
     int32_t lp[3];
     PS_TRY(jit_prepare(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, 0, loop, &k, &g, gd, lp));
     if (!bw) return fail(PS_ERR_NULL, "ps_jit_hide_communication: NULL boundary width");
+    if ((int64_t)threads[0] * threads[1] * threads[2] > 256)
+        return fail(PS_ERR_ARG, "ps_jit_hide_communication: blocks of at most 256 threads");
     for (int d = 0; d < 3; d++) {  // validate_ranges_args (src/ParallelKernel/hide_communication.jl:396-403)
         if (bw[d] < 0) return fail(PS_ERR_ARG, "boundary width must be >= 0");
         if (!(count[d] > 2 * bw[d]))

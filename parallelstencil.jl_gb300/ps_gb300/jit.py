@@ -1053,6 +1053,9 @@ class _Gen:
         pos = "const long long " + ", ".join(f"{t[d]} = g.lo[{d}] + {u[d]}" for d in grid)
         # the boundary-first variant: the body in a block that a finished thread jumps past, then the count
         head = "    const uint3 bi = jl_block(g);\n    {\n" if self.ordered else ""
+        # the ordered block index and the count raise register use (56 -> 72 for the diffusion step in
+        # split FP64, 4 -> 3 blocks per SM); its launches use blocks of <= 256 threads
+        bounds = "__launch_bounds__(256, 4) " if self.ordered else ""
         tail = "    }\nps_done_:\n    jl_block_done(g);\n" if self.ordered else ""
         sweep = f", {c[self.sweep]} sweep" if self.zloop else ""
         return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{sweep}) -- generated by ps_gb300.jit
@@ -1080,7 +1083,7 @@ __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov
 __device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
-extern "C" __global__ void ps_jit_entry(const ps_jit_args g) {{
+extern "C" __global__ void {bounds}ps_jit_entry(const ps_jit_args g) {{
     extern __shared__ __align__(16) unsigned char ps_smem[];
 {head}    const long long {udecl};
 {guard}
