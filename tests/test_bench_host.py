@@ -1,5 +1,5 @@
 """The CPU legs of bench.py, run here on the host cores (no GPU): the headline's CPU baseline (the
-oracle on a z-slab of the 512^3 job), the miniapp loop bodies timed beside the GPU lines, and the
+oracle over the whole job), the miniapp loop bodies timed beside the GPU lines, and the
 reference arm's JSON line. They run at the end of every GPU benchmark, so a failure here would cost
 the whole line."""
 import argparse
@@ -8,6 +8,8 @@ import io
 import json
 import os
 import sys
+
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
@@ -25,11 +27,14 @@ def test_cpu_baseline_and_miniapps():
     assert mini["cores"] >= 1
 
 
-def test_reference_arm_line():
-    a = argparse.Namespace(n=64, ref_slab=16, steps=1, warmup=0)
+@pytest.mark.parametrize("slab", [0, 16])
+def test_reference_arm_line(slab):
+    a = argparse.Namespace(n=64, ref_slab=slab, steps=1, warmup=0)
     buf = io.StringIO()
     with contextlib.redirect_stdout(buf):
         bench.run_reference(a, 1, 0)
     line = json.loads(buf.getvalue().strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["metric"] == "T_eff" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    # the default (slab 0) times the whole job, so the line names no sample
+    assert ("z-slab" in line["config"]["workload"]) == (slab > 0)
