@@ -502,6 +502,9 @@ def run_ours(a, world, rank, local):
         sweep2d = None if a.quick else bench_sweep_2d(ps, torch)
         if sweep2d:
             launches += sweep2d.pop("launches")
+        adg = None if a.quick else bench_ad(ps, torch)
+        if adg:
+            launches += adg.pop("launches")
     clocks = clk.summary()
 
     value = job_value(world, b_head, t_head) / 1e9
@@ -550,6 +553,7 @@ def run_ours(a, world, rank, local):
         "fd_macros_512": fdm,
         "hide_communication_512": hide,
         "memopt_2d_8192": sweep2d,
+        "ad_kernels_256": adg,
         "clocks": clocks,
         "variants": results,
     }
@@ -815,6 +819,48 @@ def bench_fd_macros(ps, torch, n=512):
             del R
         del A
     torch.cuda.empty_cache()
+    out["launches"] = launches
+    return out
+
+
+def bench_ad(ps, torch, n=256):
+    """`@parallel ∇` of the flux-lam step (JIT_FLUX_LAM, IEEE) at n^3: the generated reverse kernel
+    (∇=(T2->T2̄, T->T̄, lam->lam̄): the primal step, T2̄ taken, T̄ and lam̄ gathered with atomic
+    additions) and forward kernel (tangents of T and lam) against the hand-written adjoint step
+    (ps_diffusion3d_adjoint_step); FP64, plus the reverse kernel in FP32. Bytes: reverse 8 words per
+    cell at least (T, Ci, lam, T2̄ read, T2 written, T2̄ zeroed, T̄ and lam̄ updated), forward 7
+    (T, Ci, lam, T̄, lam̄ read; T2, T2̄ written), hand-written adjoint 6."""
+    out, launches = {}, 0
+    k = ps.parallel_kernel(JIT_FLUX_LAM.format(opt=""))
+    h = (n - 1) / 10.0
+    for dt, tag in ((np.float64, "f64"), (np.float32, "f32")):
+        T = ps.rand(n, n, n, dtype=dt, seed=2)
+        lam = ps.rand(n, n, n, dtype=dt, seed=3)
+        lam.mul_(0.5).add_(1.0)
+        Ci, T2 = ps.ones(n, n, n, dtype=dt), ps.zeros(n, n, n, dtype=dt)
+        T2b, Tb, lamb = ps.rand(n, n, n, dtype=dt, seed=4), ps.zeros(n, n, n, dtype=dt), ps.zeros(n, n, n, dtype=dt)
+        args = (T2, T, Ci, lam, 1e-4 / h ** 2, h, h, h)
+        es = np.dtype(dt).itemsize
+        row = {}
+        t = _events(torch, lambda: ps.parallel(k, *args, sync=False, grad=((T2, T2b), (T, Tb), (lam, lamb))), 10)
+        row["reverse_ms"] = round(t * 1e3, 4)
+        row["reverse_GBs_8_words"] = round(8 * es * n ** 3 / t / 1e9, 1)
+        launches += 13
+        if dt == np.float64:
+            t = _events(torch, lambda: ps.parallel(k, *args, sync=False, grad=((T, Tb), (lam, lamb)),
+                                                   ad_mode="forward"), 10)
+            row["forward_ms"] = round(t * 1e3, 4)
+            row["forward_GBs_7_words"] = round(7 * es * n ** 3 / t / 1e9, 1)
+            t = _events(torch, lambda: ps.adjoint.adjoint_step(Tb, T2b, T, Ci, lam, lamb, 1e-4 / h ** 2, h, h, h,
+                                                               sync=False), 10)
+            row["hand_written_adjoint_ms"] = round(t * 1e3, 4)
+            row["hand_written_adjoint_GBs_6_words"] = round(6 * es * n ** 3 / t / 1e9, 1)
+            launches += 26
+        out[tag] = row
+        del T, lam, Ci, T2, T2b, Tb, lamb
+    torch.cuda.empty_cache()
+    out["config"] = (f"{n}^3, flux form with a conductivity array run-time compiled, one point per thread; "
+                     "events around 10 launches after 3 warm-up launches")
     out["launches"] = launches
     return out
 

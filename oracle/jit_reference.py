@@ -29,7 +29,7 @@ import threading
 
 import numpy as np
 
-__all__ = ["parse", "run", "OracleKernel"]
+__all__ = ["parse", "run", "OracleKernel", "Dual", "jacobian", "reverse_shadows", "forward_shadows"]
 
 # ---------------------------------------------------------------- tokens
 _TOKEN = re.compile(r"""
@@ -624,6 +624,8 @@ class _Thread:
                 x = self.real(x) if not isinstance(x, int) else x
                 return x * x if n[1] == 2 else (x * x) * x
             x, p = self.real(x), self.real(E(n))
+            if isinstance(x, Dual) or isinstance(p, Dual):
+                return Dual.lift(x) ** p
             return R(float(x) ** float(p))
         if op == "cmp":
             vals = [E(v) for v in e[2]]
@@ -683,8 +685,11 @@ class _Thread:
             if f == "ifelse":
                 return E(args[1]) if E(args[0]) else E(args[2])
             if f in _FUN:
+                v = self.real(E(args[0]))
+                if isinstance(v, Dual):
+                    return v.apply(f)
                 fn = _FUN[f][0 if R is float else 1]
-                return R(fn(self.real(E(args[0]))))
+                return R(fn(v))
             raise NameError(f)
         raise ValueError(op)
 
@@ -775,7 +780,7 @@ def run(src, args, ndims=None, ranges=None, nthreads=None, nblocks=None, shmem=0
     if len(args) != len(k.argnames):
         raise TypeError("argument count")
     arrays = {n: a for n, a in zip(k.argnames, args) if isinstance(a, np.ndarray)}
-    dts = {a.dtype for a in arrays.values()}
+    dts = {a.dtype for a in arrays.values() if a.dtype != object}  # object arrays hold Duals (jacobian)
     assert len(dts) <= 1
     R = np.float32 if dts == {np.dtype(np.float32)} else float
     scalars = {}
@@ -857,3 +862,170 @@ def _walk_stmts(stmts):
             yield from _walk_stmts(s[3])
         elif s[0] == "while":
             yield from _walk_stmts(s[2])
+
+
+# ---------------------------------------------------------------- derivatives (the `@parallel ∇` checker)
+def _comb(d1, a, d2, b):
+    r = {k: a * v for k, v in d1.items()}
+    for k, v in d2.items():
+        r[k] = r.get(k, 0.0) + b * v
+    return r
+
+
+_DFUN = {"exp": lambda x, y: y, "log": lambda x, y: 1.0 / x, "sqrt": lambda x, y: 0.5 / y,
+         "sin": lambda x, y: math.cos(x), "cos": lambda x, y: -math.sin(x), "tan": lambda x, y: 1.0 + y * y,
+         "tanh": lambda x, y: 1.0 - y * y, "sinh": lambda x, y: math.cosh(x), "cosh": lambda x, y: math.sinh(x),
+         "atan": lambda x, y: 1.0 / (1.0 + x * x), "asin": lambda x, y: 1.0 / math.sqrt(1.0 - x * x),
+         "acos": lambda x, y: -1.0 / math.sqrt(1.0 - x * x), "log10": lambda x, y: 1.0 / (x * math.log(10.0)),
+         "exp2": lambda x, y: y * math.log(2.0), "cbrt": lambda x, y: 1.0 / (3.0 * y * y)}
+
+
+class Dual:
+    """A double value with its first derivatives with respect to chosen inputs (a sparse map
+    input -> derivative). The value follows IEEE double arithmetic exactly as the interpreter's
+    plain floats do; the derivatives follow the chain rule of each operation. Comparisons look at
+    the value, so branches, max / min and ifelse select like the plain run."""
+
+    __slots__ = ("v", "d")
+    __hash__ = None
+
+    def __init__(self, v, d=None):
+        self.v, self.d = float(v), d if d is not None else {}
+
+    @staticmethod
+    def lift(x):
+        return x if isinstance(x, Dual) else Dual(float(x))
+
+    def __float__(self):
+        return self.v
+
+    def __add__(self, o):
+        o = Dual.lift(o)
+        return Dual(self.v + o.v, _comb(self.d, 1.0, o.d, 1.0))
+
+    def __radd__(self, o):
+        return Dual.lift(o) + self
+
+    def __sub__(self, o):
+        o = Dual.lift(o)
+        return Dual(self.v - o.v, _comb(self.d, 1.0, o.d, -1.0))
+
+    def __rsub__(self, o):
+        return Dual.lift(o) - self
+
+    def __mul__(self, o):
+        o = Dual.lift(o)
+        return Dual(self.v * o.v, _comb(self.d, o.v, o.d, self.v))
+
+    def __rmul__(self, o):
+        return Dual.lift(o) * self
+
+    def __truediv__(self, o):
+        o = Dual.lift(o)
+        q = self.v / o.v
+        return Dual(q, _comb(self.d, 1.0 / o.v, o.d, -q / o.v))
+
+    def __rtruediv__(self, o):
+        return Dual.lift(o) / self
+
+    def __neg__(self):
+        return Dual(-self.v, {k: -v for k, v in self.d.items()})
+
+    def __abs__(self):
+        return -self if math.copysign(1.0, self.v) < 0 else self
+
+    def __pow__(self, p):
+        p = Dual.lift(p)
+        v = self.v ** p.v
+        d = {k: p.v * self.v ** (p.v - 1.0) * x for k, x in self.d.items()}
+        if p.d:
+            d = _comb(d, 1.0, p.d, v * math.log(self.v))
+        return Dual(v, d)
+
+    def apply(self, f):
+        y = float(_FUN[f][0](self.v))
+        g = _DFUN[f](self.v, y)
+        return Dual(y, {k: g * x for k, x in self.d.items()})
+
+    def _o(self, o):
+        return o.v if isinstance(o, Dual) else o
+
+    def __lt__(self, o):
+        return self.v < self._o(o)
+
+    def __le__(self, o):
+        return self.v <= self._o(o)
+
+    def __gt__(self, o):
+        return self.v > self._o(o)
+
+    def __ge__(self, o):
+        return self.v >= self._o(o)
+
+    def __eq__(self, o):
+        return self.v == self._o(o)
+
+    def __ne__(self, o):
+        return self.v != self._o(o)
+
+
+def jacobian(src, args, dup, **kw):
+    """The Jacobian of kernel `src`'s state map over the arrays at argument positions `dup` (FP64):
+    each of their elements starts as a Dual seeded with itself, the kernel runs in the interpreter
+    (other arrays and scalars as given, so values stored into them lose their derivatives, like
+    constants), and every element of a duplicated array afterwards is its output -- an element the
+    kernel did not write keeps its own seed (identity row). Returns {position: (values, rows)} with
+    rows an object array of derivative maps {(position, flat index): value}, flat indices in
+    column-major order. `kw` goes to run() (ndims, ranges, ...)."""
+    seeded = list(args)
+    for p in dup:
+        a = np.asarray(args[p], dtype=np.float64)
+        o = np.empty(a.shape, dtype=object, order="F")
+        for idx in np.ndindex(a.shape):
+            o[idx] = Dual(a[idx], {(p, int(np.ravel_multi_index(idx, a.shape, order="F"))): 1.0})
+        seeded[p] = o
+    run(src, seeded, **kw)
+    out = {}
+    for p in dup:
+        o = seeded[p]
+        vals = np.empty(o.shape, order="F")
+        rows = np.empty(o.shape, dtype=object, order="F")
+        for idx in np.ndindex(o.shape):
+            x = o[idx]
+            vals[idx] = float(x)
+            rows[idx] = x.d if isinstance(x, Dual) else {}
+        out[p] = (vals, rows)
+    return out
+
+
+def reverse_shadows(jac, shadows):
+    """Reverse mode: shadows after = J^T shadows before (`shadows`: {position: array}); the shadow of
+    an element the kernel overwrote starts from zero, and every input element gathers the adjoints
+    of the outputs it reached."""
+    new = {p: np.zeros(np.shape(s), order="F") for p, s in shadows.items()}
+    flat = {p: np.asarray(s, dtype=np.float64).ravel(order="F") for p, s in shadows.items()}
+    acc = {p: np.zeros(f.size) for p, f in flat.items()}
+    for p, (_, rows) in jac.items():
+        rf = rows.ravel(order="F")
+        for e in range(rf.size):
+            w = flat[p][e]
+            if w == 0.0:
+                continue
+            for (q, j), c in rf[e].items():
+                acc[q][j] += c * w
+    for p in new:
+        new[p] = acc[p].reshape(np.shape(shadows[p]), order="F")
+    return new
+
+
+def forward_shadows(jac, shadows):
+    """Forward mode: shadows after = J shadows before."""
+    flat = {p: np.asarray(s, dtype=np.float64).ravel(order="F") for p, s in shadows.items()}
+    new = {}
+    for p, (_, rows) in jac.items():
+        rf = rows.ravel(order="F")
+        out = np.zeros(rf.size)
+        for e in range(rf.size):
+            out[e] = sum(c * flat[q][j] for (q, j), c in rf[e].items())
+        new[p] = out.reshape(rows.shape, order="F")
+    return new

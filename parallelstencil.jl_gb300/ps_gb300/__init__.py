@@ -10,7 +10,7 @@ Mirrors the user-facing interface of ParallelStencil.jl for its finite-differenc
 Every kernel runs in libps_b200.so (hand-written sm_103a CUDA); there is no CPU or library
 fallback, and a missing library raises at import of the kernels.
 """
-from . import _lib, adjoint, core, fd, jit, kernels, nn, stokes, stokes3d
+from . import _lib, ad, adjoint, core, fd, jit, kernels, nn, stokes, stokes3d
 from ._lib import PSError
 from .core import (GB300, ArgumentError, Data, NotInitializedError, descriptor, empty, fill, fill_, from_host,
                    init_parallel_stencil, is_initialized, ones, rand, reset_parallel_stencil, synchronize, to_host,
@@ -23,5 +23,5 @@ __all__ = [
     "GB300", "ArgumentError", "Data", "NotInitializedError", "PSError", "descriptor", "empty", "fill", "fill_",
     "from_host", "init_parallel_stencil", "is_initialized", "ones", "rand", "reset_parallel_stencil", "synchronize",
     "to_host", "zeros", "fd_kernel", "from_source", "hide_communication", "parallel", "parallel_async", "kernels",
-    "fd", "core", "stokes", "stokes3d", "jit", "parallel_kernel",
+    "fd", "core", "stokes", "stokes3d", "jit", "parallel_kernel", "ad",
 ]

@@ -996,6 +996,17 @@ class _Gen:
                                     f"is not read-only within the scope of the kernel (any of: {sorted(writes)}).")
             self.temps[name] = (self.sels[sel], s.value)
 
+    def body_lines(self):
+        """The kernel body's statements as CUDA C lines (one thread's work)."""
+        out = []
+        for s in self.kd.body:
+            out += self.stmt(s, 1)
+        return out
+
+    def extra_decl(self):
+        """Further declarations at the top of the kernel (none here; the derivative kernels add theirs)."""
+        return []
+
     def types(self, real):
         if self.split:
             if real != "double":
@@ -1007,9 +1018,7 @@ class _Gen:
         kd = self.kd
         self.collect_temps()
         self.infer_locals(kd.body)
-        body = []
-        for s in kd.body:
-            body += self.stmt(s, 1)
+        body = self.body_lines()
         decl = ["    bool big_ = false;"] if self.split else []
         for name, k in self.aidx.items():
             decl.append(f"    E* const a{k} = (E*)g.a[{k}];")
@@ -1026,6 +1035,7 @@ class _Gen:
                             f"sm{j}_n2 = 1, sm{j}_cap = 0;")
             else:
                 decl.append(f"    {'long long' if t == 'int' else 'R'} v_{name} = 0;")
+        decl += self.extra_decl()
         bi = "bi" if self.ordered else "blockIdx"
         if self.uses_collectives:
             # barriers, shuffles and votes need every thread of a block: a block that reaches past the

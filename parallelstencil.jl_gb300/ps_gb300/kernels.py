@@ -170,9 +170,21 @@ def from_source(body: str, ndims: int = 3):
 
 
 def parallel(kernel, *args, memopt=None, loopsize=0, ranges=None, stream=None, sync=True, fp64="ieee",
-             nblocks=None, nthreads=None, shmem=None):
-    """`@parallel [ranges] [nblocks nthreads] [memopt=...] [shmem=...] kernel!(args...)`."""
+             nblocks=None, nthreads=None, shmem=None, grad=None, ad_mode="reverse"):
+    """`@parallel [ranges] [nblocks nthreads] [memopt=...] [shmem=...] kernel!(args...)`.
+
+    grad=((A, Ā), (B, B̄), ...) is `@parallel ∇=(A->Ā, B->B̄) [ad_mode=...] kernel!(args...)`
+    (src/ParallelKernel/parallel.jl:265-301): the derivative kernel of a run-time compiled kernel
+    (ps_gb300.ad), reverse (Enzyme.Reverse) or forward (Enzyme.Forward) mode."""
     require_initialized()
+    if grad is not None:
+        from .ad import parallel_grad
+
+        if memopt or loopsize or shmem or fp64 != "ieee":
+            raise ArgumentError("∇: memopt, loopsize, shmem and fp64 do not apply to derivative kernels")
+        parallel_grad(kernel, args, grad, ad_mode=ad_mode, ranges=ranges, stream=stream, sync=sync, nblocks=nblocks,
+                      nthreads=nthreads)
+        return
     if hasattr(kernel, "jit_launch"):  # run-time compiled kernel (ps_gb300.jit); memopt does not change results
         kernel.jit_launch(args, ranges, stream, sync, nblocks=nblocks, nthreads=nthreads, shmem=shmem, memopt=memopt,
                           loopsize=loopsize, fp64=fp64)
