@@ -315,23 +315,6 @@ def run_ours(a, world, rank, local):
         split_err = float((T2 - ref).abs().max() / ref.abs().max())
         del ref
         launches += 2
-        if not a.quick:
-            ieee_steps = max(3, a.steps // 10)
-            bench_kernel("diffusion3d_flux_lam_f64_ieee_memopt", ps.kernels.diffusion3D_step_flux_lam, arrs64,
-                         (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
-            bench_kernel("diffusion3d_flux_lam_f64_ieee_plain", ps.kernels.diffusion3D_step_flux_lam, arrs64,
-                         (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
-            bench_kernel("diffusion3d_readme_f64_split_memopt", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx),
-                         True, WORDS_README, n, np.float64, a.steps, fp64="split")
-            bench_kernel("diffusion3d_readme_f64_ieee_memopt", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx),
-                         True, WORDS_README, n, np.float64, ieee_steps)
-            bench_kernel("memcopy3d_f64", ps.kernels.copy3D, arrs64, (), False, WORDS_MEMCOPY, n, np.float64, a.steps)
-            for opt, tag in (("", "jit"), ("inbounds=true ", "jit_inbounds")):  # run-time compiled, IEEE FP64
-                bench_kernel(f"diffusion3d_flux_lam_f64_{tag}", ps.parallel_kernel(JIT_FLUX_LAM.format(opt=opt)),
-                             arrs64, (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
-            # the same run-time compiled body with its arithmetic on FP32 pairs (z sweep, default)
-            bench_kernel("diffusion3d_flux_lam_f64_jit_split", ps.parallel_kernel(JIT_FLUX_LAM.format(opt="")),
-                         arrs64, (dt, _dx, _dx, _dx), None, WORDS_FLUX_LAM, n, np.float64, a.steps, fp64="split")
         # e2e: diffusion jobs (NT_JOB steps each) through the C ABI from pinned host buffers: every
         # job copies its inputs T, Ci, lam host -> device, runs NT_JOB steps (T2 <- T on the device:
         # the run reads only T's boundary values from it) and copies T device -> host, all inside
@@ -424,6 +407,26 @@ def run_ours(a, world, rank, local):
         e2e_batches_s = [round(b[0], 5) for b in batches]
         launches += (3 * jobs + 4) * NT_JOB
         del hostbufs, hT, hCi, hlam, hout, sets
+        # the other 512^3 FP64 variants run after the e2e jobs: with the jobs measured after them, single
+        # host-to-device copies stalled for 100-250 ms (about 19 GB/s instead of 210) in most batches on
+        # several boxes; measured right after the headline (as --quick does) they ran at 210 GB/s
+        if not a.quick:
+            ieee_steps = max(3, a.steps // 10)
+            bench_kernel("diffusion3d_flux_lam_f64_ieee_memopt", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                         (dt, _dx, _dx, _dx), True, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
+            bench_kernel("diffusion3d_flux_lam_f64_ieee_plain", ps.kernels.diffusion3D_step_flux_lam, arrs64,
+                         (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
+            bench_kernel("diffusion3d_readme_f64_split_memopt", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx),
+                         True, WORDS_README, n, np.float64, a.steps, fp64="split")
+            bench_kernel("diffusion3d_readme_f64_ieee_memopt", ps.kernels.diffusion3D_step, arrs64, (dt, dx, dx, dx),
+                         True, WORDS_README, n, np.float64, ieee_steps)
+            bench_kernel("memcopy3d_f64", ps.kernels.copy3D, arrs64, (), False, WORDS_MEMCOPY, n, np.float64, a.steps)
+            for opt, tag in (("", "jit"), ("inbounds=true ", "jit_inbounds")):  # run-time compiled, IEEE FP64
+                bench_kernel(f"diffusion3d_flux_lam_f64_{tag}", ps.parallel_kernel(JIT_FLUX_LAM.format(opt=opt)),
+                             arrs64, (dt, _dx, _dx, _dx), False, WORDS_FLUX_LAM, n, np.float64, ieee_steps)
+            # the same run-time compiled body with its arithmetic on FP32 pairs (z sweep, default)
+            bench_kernel("diffusion3d_flux_lam_f64_jit_split", ps.parallel_kernel(JIT_FLUX_LAM.format(opt="")),
+                         arrs64, (dt, _dx, _dx, _dx), None, WORDS_FLUX_LAM, n, np.float64, a.steps, fp64="split")
         if not a.quick:
             del arrs64, T, T2, lam, Ci
             torch.cuda.empty_cache()

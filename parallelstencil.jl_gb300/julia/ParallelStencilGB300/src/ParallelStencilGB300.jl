@@ -56,6 +56,7 @@ const NDIMS = Dict{Module,Int}()
 
 export @init_parallel_stencil, @parallel, @parallel_async, @parallel_indices, @hide_communication, GB300
 export @zeros, @ones, @rand, @fill, @synchronize, ParallelStencil
+export diffusion3d_step, diffusion3d_misfit
 
 macro zeros(args...) esc(:(ParallelStencil.@zeros($(args...)))) end
 macro ones(args...) esc(:(ParallelStencil.@ones($(args...)))) end
@@ -251,5 +252,32 @@ diffusion3d_run!(k::GB300Kernel, T, T2, Ci, lam, dt, dx, dy, dz, nt; fp64_mode =
                  stream = CUDA.stream()) =
     LibPS.diffusion3d_run!(k.form, T, T2, Ci, lam, dt, dx, dy, dz, nt,
                            LibPS.launch_cfg(; memopt = true, fp64_mode = fp64_mode); stream)
+
+"""
+    diffusion3d_step(T, Ci, lam, dt, _dx, _dy, _dz) -> T2
+
+One step of the flux form with a conductivity array (PS_DIFF_FLUX_LAM) into a new array: inner
+cells updated, boundary cells copied from T (Dirichlet data). Differentiable in the inner cells of
+T and in lam: the ChainRules extension gives its `rrule` (pullback: the hand-written adjoint step;
+boundary cells get a zero cotangent).
+"""
+function diffusion3d_step(T, Ci, lam, dt, _dx, _dy, _dz; memopt = true)
+    T2 = copy(T)
+    LibPS.diffusion3d_step!(3, T2, T, Ci, lam, dt, _dx, _dy, _dz, LibPS.launch_cfg(; memopt = Bool(memopt)))
+    return T2
+end
+
+"""
+    diffusion3d_misfit(T0, T_obs, Ci, lam, dt, _dx, _dy, _dz, nt; checkpoint_every = 20) -> L
+
+L = 0.5 ||T_nt - T_obs||^2 after nt flux-lam steps from T0. Differentiable in lam: the ChainRules
+extension's `rrule` returns dL/dlam from the checkpointed adjoint (ps_diffusion3d_misfit_gradient).
+"""
+function diffusion3d_misfit(T0, T_obs, Ci, lam, dt, _dx, _dy, _dz, nt; checkpoint_every = 20,
+                            fp64_mode = LibPS.PS_FP64_IEEE)
+    g = similar(lam)
+    cfg = LibPS.launch_cfg(; memopt = true, fp64_mode = fp64_mode)
+    return LibPS.misfit_gradient!(g, T0, T_obs, Ci, lam, dt, _dx, _dy, _dz, nt, checkpoint_every, cfg).loss
+end
 
 end # module ParallelStencilGB300

@@ -108,3 +108,59 @@ def test_derivative_refusals_launch_nothing(ps):
     with pytest.raises(ArgumentError, match="run-time compiled"):
         ps.parallel(ps.kernels.copy3D, A, B, A, grad=((A, Ab),))
     assert np.array_equal(ps.to_host(A), before) and np.all(ps.to_host(Ab) == 0)
+
+
+def test_misfit_gradient_32_through_generated_reverse_kernels(ps):
+    """Config 4's gradient check at 32^3 with Enzyme's semantics: dL/dlam of L = 0.5||T_nt - T_obs||^2
+    over 200 flux-lam steps, built by chaining the generated reverse kernel of the step (`@parallel
+    ∇=(T2->λ, T->T̄, lam->lam̄)`) backwards through the stored states, against the hand-written
+    checkpointed adjoint (ps_diffusion3d_misfit_gradient). lam = exp(0.3 g), g a Gaussian random
+    field (sigma 8 cells); T_obs from lam (1 + 0.05 h)."""
+    import torch
+
+    n, nt = 32, 200
+    src = K.KERNELS["diffusion_flux_lam"][0]
+    k = ps.parallel_kernel(src, 3)
+
+    def grf(seed):
+        gen = torch.Generator(device="cuda").manual_seed(seed)
+        w = torch.randn((n, n, n), generator=gen, device="cuda", dtype=torch.float64)
+        f = torch.fft.fftfreq(n, device="cuda", dtype=torch.float64)
+        kx, ky, kz = torch.meshgrid(f, f, f, indexing="ij")
+        g = torch.fft.ifftn(torch.fft.fftn(w) * torch.exp(-2 * (torch.pi * 8.0) ** 2 * (kx ** 2 + ky ** 2 + kz ** 2))).real
+        return (g - g.mean()) / g.std()
+
+    def dev(t):
+        A = ps.empty(n, n, n)
+        A.copy_(t)
+        return A
+
+    x = torch.linspace(0, 10, n, device="cuda", dtype=torch.float64)
+    X, Y, Z = torch.meshgrid(x, x, x, indexing="ij")
+    T0 = dev(1.7 * torch.exp(-((X - 5) ** 2 + (Y - 5) ** 2 + (Z - 5) ** 2)))
+    lam = dev(torch.exp(0.3 * grf(4)))
+    lam_obs = dev(torch.exp(0.3 * grf(4)) * (1 + 0.05 * grf(5)))
+    Ci = ps.ones(n, n, n)
+    h = ((n - 1) / 10.0,) * 3
+    dt = (10.0 / (n - 1)) ** 2 / float(lam_obs.max()) / 8.1
+    _, _, T_obs, _ = ps.adjoint.misfit_gradient(T0, T0, Ci, lam_obs, dt, h, nt, return_final=True)
+    loss_h, g_h, _ = ps.adjoint.misfit_gradient(T0, T_obs, Ci, lam, dt, h, nt, checkpoint_every=20)
+    # forward: every state kept (the time loop of the examples, T2 starting as a copy of T)
+    states = [T0.clone()]
+    T2 = T0.clone()
+    for _ in range(nt):
+        T2.copy_(states[-1])
+        ps.parallel(k, T2, states[-1], Ci, lam, dt, *h)
+        states.append(T2.clone())
+    assert abs(0.5 * float(((states[-1] - T_obs) ** 2).sum()) - loss_h) <= 1e-12 * loss_h
+    # reverse: λ_nt = T_nt - T_obs; per step T̄ = J^T λ on all cells, the boundary (copied through the
+    # loop) keeps its λ in T2's shadow
+    lamb = states[-1].clone()
+    lamb.sub_(T_obs)
+    glam, Tb, scratch = ps.zeros(n, n, n), ps.zeros(n, n, n), ps.empty(n, n, n)
+    for s in range(nt - 1, -1, -1):
+        Tb.zero_()
+        scratch.copy_(states[s])
+        ps.parallel(k, scratch, states[s], Ci, lam, dt, *h, grad=((scratch, lamb), (states[s], Tb), (lam, glam)))
+        lamb.add_(Tb)
+    assert _rel(ps.to_host(glam), ps.to_host(g_h)) <= 1e-10

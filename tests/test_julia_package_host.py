@@ -204,3 +204,22 @@ def test_sources_say_they_were_not_run_here_or_are_bindings(fn):
     assert "module" in text or "function" in text
     if fn == "ParallelStencilGB300.jl":
         assert "no Julia toolchain" in text
+
+
+def test_chainrules_extension_matches_the_package():
+    """The ChainRules extension (ext/) is declared in Project.toml, defines an rrule for each
+    differentiable entry point of the package, and calls only LibPS functions that exist."""
+    pkg = os.path.dirname(JLDIR)
+    with open(os.path.join(pkg, "Project.toml"), encoding="utf-8") as fh:
+        proj = fh.read()
+    assert re.search(r"\[weakdeps\]\s*\nChainRulesCore\s*=", proj)
+    assert 'ParallelStencilGB300ChainRulesCoreExt = "ChainRulesCore"' in proj
+    with open(os.path.join(pkg, "ext", "ParallelStencilGB300ChainRulesCoreExt.jl"), encoding="utf-8") as fh:
+        ext = fh.read()
+    src = _sources()
+    main, lib = src["ParallelStencilGB300.jl"], src["LibPS.jl"]
+    for f in ("diffusion3d_step", "diffusion3d_misfit"):
+        assert f"rrule(::typeof(ParallelStencilGB300.{f})" in ext
+        assert re.search(rf"^function {f}\(", main, re.M) and f in main.split("export", 3)[-1]
+    for f in set(re.findall(r"LibPS\.(\w+!?)", ext)):
+        assert re.search(rf"^(function )?{re.escape(f)}\(|^const .*\b{re.escape(f)}\b", lib, re.M), f
