@@ -1253,6 +1253,19 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
         return
+    if a.only_run in ("ad", "ad32"):  # the generated reverse kernel of the flux-lam body, n^3, --steps launches
+        dt_np = np.float32 if a.only_run == "ad32" else np.float64
+        k = ps.parallel_kernel(JIT_FLUX_LAM.format(opt=""))
+        T, lam = ps.rand(n, n, n, dtype=dt_np, seed=2), ps.rand(n, n, n, dtype=dt_np, seed=3)
+        lam.mul_(0.5).add_(1.0)
+        Ci, T2 = ps.ones(n, n, n, dtype=dt_np), ps.zeros(n, n, n, dtype=dt_np)
+        T2b, Tb, lamb = ps.rand(n, n, n, dtype=dt_np, seed=4), ps.zeros(n, n, n, dtype=dt_np), ps.zeros(n, n, n, dtype=dt_np)
+        h = (n - 1) / 10.0
+        for _ in range(a.steps):
+            ps.parallel(k, T2, T, Ci, lam, 1e-4 / h ** 2, h, h, h, sync=False, grad=((T2, T2b), (T, Tb), (lam, lamb)))
+        torch.cuda.synchronize()
+        print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
+        return
     if a.only_run == "hide":  # the @hide_communication measurement alone, at --n
         print(json.dumps(bench_hide_communication(ps, torch, n=n)))
         return
@@ -1322,7 +1335,8 @@ def main():
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
                                                  "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd", "fd32",
                                                  "stokes2d_apt", "stokes2d_apt32", "adjoint_grid", "acoustic3d_fused",
-                                                 "acoustic3d_fused32", "acoustic3d_fused_split", "hide", "miniapps", "stokes3d_fused32"],
+                                                 "acoustic3d_fused32", "acoustic3d_fused_split", "hide", "miniapps", "stokes3d_fused32",
+                                                 "ad", "ad32"],
                     default=None,
                     help="profiling aid: run --steps steps of the headline workload in this fp64 mode (or as a "
                          "run-time compiled kernel: jit; or --steps calls of the tcgen05 GEMM on an --n cubed bf16 "
