@@ -510,6 +510,20 @@ int ps_jit_launch(void* kernel, const ps_array* arrays, int32_t narrays, const d
 int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
                      const int64_t lo[3], const int64_t count[3], const int32_t threads[3], int64_t shmem,
                      const int32_t loop[3], void* stream, int sync);
+/* The memopt z-sweep of a run-time compiled 3-D `@parallel` kernel with its read-only stencil
+ * arrays staged plane by plane in shared memory by TMA (src/memopt.jl:190-573 caches the same
+ * arrays in registers and shared memory; launched by src/parallel.jl:451-596). The kernel must be
+ * the TMA variant ps_gb300/jit.py generates for the definition; its argument block is
+ *   struct alignas(64) { CUtensorMap tm[8]; <the ps_jit_compile block> }
+ * with tm[i] a 3-D tiled map of arrays[maps[3i]] with box (maps[3i+1], maps[3i+2], 1), zero fill,
+ * built here for each launch. The threads start at index 0 (no ranges); loop_z z indices per
+ * thread (threads[2] == 1); shmem = the kernel's stage ring. Every staged array must meet TMA's
+ * 16-byte rules (base address, x extent x element size and x-y plane size multiples of 16 bytes:
+ * PS_ERR_ALIGN otherwise). A bounded wait for a staged plane that gives up stops the kernel and is
+ * reported as PS_ERR_TIMEOUT, otherwise as ps_jit_launch_ex. */
+int ps_jit_launch_tma(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                      const int64_t count[3], const int32_t threads[3], int64_t shmem, int32_t loop_z,
+                      const int32_t* maps, int32_t nmaps, void* stream, int sync);
 /* `@hide_communication bw begin @parallel kernel!(...); comm() end` for a run-time compiled
  * `@parallel` kernel over its full grid (count threads from index 0; threads and loop as for
  * ps_jit_launch_ex, at most 256 threads per block; no dynamic shared memory, no barriers, shuffles

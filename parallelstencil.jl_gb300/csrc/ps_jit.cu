@@ -218,14 +218,24 @@ static int jit_flags(JitKernel* k, const char* what) {
         if (flag & 4)
             return fail(PS_ERR_UNSUPPORTED, "%s: a value outside the split FP64 arithmetic's range "
                                             "(|x| >= 2^128); run the kernel with fp64 = ieee", what);
+        if (flag & 8)
+            return fail(PS_ERR_TIMEOUT, "%s: a bounded wait for a staged plane gave up (the kernel stopped)", what);
         return fail(PS_ERR_ARG, "%s: a kernel with @sync_threads, shuffles or votes needs ranges that are "
                                 "a multiple of the thread block; a partial block did not run", what);
     }
     return PS_OK;
 }
 
+// Argument block of a TMA-staged sweep kernel (ps_jit_launch_tma): the tensor maps of its staged
+// arrays beside the ordinary block (identical layout in the generated source).
+constexpr int kJitMaxMaps = 8;
+struct alignas(64) ps_jit_targs {
+    CUtensorMap tm[kJitMaxMaps];
+    ps_jit_args g;
+};
+
 static int jit_cu_launch(JitKernel* k, unsigned gx, unsigned gy, unsigned gz, const int32_t threads[3], int64_t shmem,
-                         ps_jit_args* g, void* stream) {
+                         void* g, void* stream) {
     void* params[] = {g};
     const CUresult r = g_launch(k->fn, gx, gy, gz, (unsigned)threads[0], (unsigned)threads[1], (unsigned)threads[2],
                                 (unsigned)shmem, static_cast<CUstream>(stream), params, nullptr);
@@ -251,6 +261,34 @@ int ps_jit_launch_ex(void* kernel, const ps_array* arrays, int32_t narrays, cons
     PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), sync, "ps_jit_launch"));
     if (!sync) return PS_OK;
     return jit_flags(k, "ps_jit_launch");  // flags of earlier asynchronous launches are reported too
+}
+
+int ps_jit_launch_tma(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars, int32_t nscalars,
+                      const int64_t count[3], const int32_t threads[3], int64_t shmem, int32_t loop_z,
+                      const int32_t* maps, int32_t nmaps, void* stream, int sync) {
+    const int64_t lo[3] = {0, 0, 0};
+    const int32_t loop[3] = {1, 1, loop_z};
+    JitKernel* k = nullptr;
+    ps_jit_targs t;
+    int64_t gd[3];
+    int32_t lp[3];
+    PS_TRY(jit_prepare(kernel, arrays, narrays, scalars, nscalars, lo, count, threads, shmem, loop, &k, &t.g, gd, lp));
+    if (nmaps < 0 || nmaps > kJitMaxMaps || (nmaps && !maps))
+        return fail(PS_ERR_ARG, "ps_jit_launch_tma: at most %d staged arrays", kJitMaxMaps);
+    memset(t.tm, 0, sizeof(t.tm));
+    for (int i = 0; i < nmaps; i++) {
+        const int32_t a = maps[3 * i], bx = maps[3 * i + 1], by = maps[3 * i + 2];
+        if (a < 0 || a >= narrays || bx < 1 || by < 1)
+            return fail(PS_ERR_ARG, "ps_jit_launch_tma: staged array %d: index %d, box (%d, %d)", i, a, bx, by);
+        PS_TRY(encode_plane_map(&t.tm[i], arrays[a], (uint32_t)bx, (uint32_t)by));
+    }
+    if (gd[0] == 0) return PS_OK;
+    if (gd[0] > 2147483647LL || gd[1] > 65535 || gd[2] > 65535)
+        return fail(PS_ERR_SHAPE, "ps_jit_launch_tma: grid too large");
+    PS_TRY(jit_cu_launch(k, (unsigned)gd[0], (unsigned)gd[1], (unsigned)gd[2], threads, shmem, &t, stream));
+    PS_TRY(finish_launch(static_cast<cudaStream_t>(stream), sync, "ps_jit_launch_tma"));
+    if (!sync) return PS_OK;
+    return jit_flags(k, "ps_jit_launch_tma");
 }
 
 int ps_jit_hide_communication(void* kernel, const ps_array* arrays, int32_t narrays, const double* scalars,

@@ -65,10 +65,15 @@ _lib.register("ps_jit_hide_communication", [ctypes.c_void_p, ctypes.POINTER(PSAr
                                             ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32),
                                             ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
                                             _lib.COMM_FN, ctypes.c_void_p, ctypes.c_void_p])
+_lib.register("ps_jit_launch_tma", [ctypes.c_void_p, ctypes.POINTER(PSArray), ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                    ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p, ctypes.c_int])
 _lib.register("ps_jit_check", [ctypes.c_void_p, ctypes.c_void_p])
 _lib.register("ps_jit_destroy", [ctypes.c_void_p])
 
 MAX_ARRAYS = MAX_SCALARS = 32
+TMA_RING_BYTES = 64 * 1024  # shared memory for the plane ring of a TMA sweep (sets the planes in flight)
 RESIDENT_THREADS = 152 * 2048  # threads a GB300 holds at once (152 SMs x 2048)
 # kernel-language macros (src/ParallelKernel/kernel_language.jl): a kernel that uses any of them
 # keeps one point per thread (a sweep would change what @threadIdx, @sharedMem and barriers see)
@@ -437,7 +442,8 @@ def _lit(v):
 
 
 class _Gen:
-    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False, split: bool = False, ordered: bool = False):
+    def __init__(self, kd: KernelDef, ndims: int, zloop: bool = False, split: bool = False, ordered: bool = False,
+                 tma: bool = False):
         self.kd, self.nd = kd, ndims
         # the boundary-first variant (ps_jit_hide_communication): its block index comes from the
         # launch's tile order, and every warp counts itself in host-mapped memory at the end
@@ -463,6 +469,11 @@ class _Gen:
         self.kernel_language = False
         self.uses_collectives = False  # @sync_threads, shuffles, votes
         self.table = None  # per-statement loads of an FD statement: (array, offsets) -> register
+        # the TMA variant of a 3-D sweep: read-only stencil arrays staged plane by plane in shared
+        # memory (ps_jit_launch_tma); staged: array -> offsets read; layout: set by source()
+        self.tma = bool(tma) and self.zloop and ndims == 3 and not self.ordered
+        self.staged = {}
+        self.layout = None
         written = set()
         for n in ast.walk(ast.Module(body=kd.body, type_ignores=[])):
             if isinstance(n, ast.Assign):
@@ -542,6 +553,10 @@ class _Gen:
             ro = name in self.read_only
             ld = self.wrap(f"__ldg(&{ref})" if ro else ref)
             nxt = (name, along(o, 1))
+            if ro and self.tma:  # from the staged plane (placeholder resolved once the layout is known)
+                self.staged.setdefault(name, set()).add(tuple(o))
+                loads.append(f"{p}    const R {var} = " + self.wrap(f"__TMA[{k},{o[0]},{o[1]},{o[2]}]__") + ";")
+                continue
             if ro and nxt in keys:
                 loads.append(f"{p}    const R {var} = pr{j} ? P{j}_{keys[nxt][1:]} : {ld};")
             else:
@@ -996,6 +1011,123 @@ class _Gen:
                                     f"is not read-only within the scope of the kernel (any of: {sorted(writes)}).")
             self.temps[name] = (self.sels[sel], s.value)
 
+    # ---- the TMA variant of a 3-D sweep (ps_jit_launch_tma)
+    TMA_TY = 8  # thread rows per block (blocks of 32 x 8 threads)
+
+    def tma_layout(self, real):
+        """Stage layout: per staged array (in argument order) its box (x from the tile origin rounded
+        down to 16 bytes, y from the lowest offset) and its bytes in a stage; all arrays share the z
+        planes ZL..ZH relative to the thread's index. Raises _NoTma where the variant cannot apply."""
+        es = 4 if real == "float" else 8
+        al = 16 // es
+        xc = 4 if es == 4 else 2  # x cells per thread: a block covers 32 * xc columns
+        names = [n for n in self.kd.arrays if n in self.staged]
+        if not names or len(names) > 8:
+            raise _NoTma()
+        zl = min(o[2] for n in names for o in self.staged[n])
+        zh = max(o[2] for n in names for o in self.staged[n])
+        arrays, off = [], 0
+        for n in names:
+            offs = self.staged[n]
+            xl, xh = min(o[0] for o in offs), max(o[0] for o in offs)
+            yl, yh = min(o[1] for o in offs), max(o[1] for o in offs)
+            xs = (xl // al) * al
+            bx = -(-(32 * xc + xh - xs) // al) * al
+            by = self.TMA_TY + yh - yl
+            if bx > 256 or by > 256:
+                raise _NoTma()
+            nbytes = bx * by * es
+            arrays.append({"name": n, "k": self.aidx[n], "xs": xs, "ys": yl, "bx": bx, "by": by, "off": off})
+            off += -(-nbytes // 128) * 128
+        span = zh - zl + 1
+        # planes in flight ahead of the step: as many as fit a ring of TMA_RING_BYTES (2 to 8)
+        ahead = max(2, min(8, TMA_RING_BYTES // off - span))
+        stages = span + ahead
+        smem = stages * off + 8 * stages
+        if smem > 200 * 1024:
+            raise _NoTma()
+        return {"arrays": arrays, "zl": zl, "span": span, "stages": stages, "stage": off, "smem": smem, "xc": xc,
+                "tx_bytes": sum(a["bx"] * a["by"] * es for a in arrays)}
+
+    def tma_resolve(self, body):
+        """Staged loads from the ring: the plane of index tz + oz sits in the stage of sweep step it_
+        + (oz - ZL)."""
+        L = self.layout
+        by_k = {a["k"]: a for a in L["arrays"]}
+
+        def sub(m):
+            k, ox, oy, oz = (int(x) for x in m.groups())
+            a = by_k[k]
+            return (f"((const E*)(jt_p{oz - L['zl']} + {a['off']}))[(threadIdx.y + {oy - a['ys']}) * {a['bx']} + "
+                    f"(jt_lx + {ox - a['xs']})]")
+        pat = re.compile(r"__TMA\[(\d+),(-?\d+),(-?\d+),(-?\d+)\]__")
+        head = ["    if (!jt_to) {", "    #pragma unroll",
+                f"    for (int jt_xc = 0; jt_xc < {L['xc']}; ++jt_xc) {{",
+                "    const int jt_lx = (int)threadIdx.x + 32 * jt_xc;  // this cell's column in the block's tile",
+                "    const long long tx = (long long)jt_x0 + jt_lx;"]
+        return head + [pat.sub(sub, line) for line in body] + ["    }", "    }"]
+
+    def tma_loop(self):
+        """Guard, loop head and loop tail of the TMA sweep: thread 0 keeps a ring of `stages` planes
+        in flight (one mbarrier per stage, bounded waits), every thread waits for the planes of its
+        step, and after a block barrier the stage of the plane no longer needed is refilled. The
+        ring's bookkeeping is 32-bit: stage of the step's first plane, one phase bit per stage."""
+        L = self.layout
+        S, SP = L["stages"], L["span"]
+        issue = [f"        jt_expect(jt_bar + s_, {L['tx_bytes']}u);"]
+        for i, a in enumerate(L["arrays"]):
+            issue.append(f"        jt_tma3(ps_smem + s_ * {L['stage']} + {a['off']}, &t_.tm[{i}], jt_bar + s_, "
+                         f"jt_x0 + ({a['xs']}), jt_y0 + ({a['ys']}), jt_z0 + ({L['zl']}) + q_);")
+        guard = ""  # no ranges: the statements' masks already exclude threads past the arrays
+
+        def stage(c):  # stage of plane it_ + c (c < S)
+            return f"(jt_s + {c} >= {S} ? jt_s + {c - S} : jt_s + {c})" if c else "jt_s"
+        planes = "\n".join(f"    unsigned char* const jt_p{c} = ps_smem + {stage(c)} * {L['stage']};" for c in range(SP))
+        zpre = "\n" + "\n".join(self.persist) + f"""
+    unsigned long long* const jt_bar = reinterpret_cast<unsigned long long*>(ps_smem + {S} * {L['stage']});
+    const int jt_tid = threadIdx.y * 32 + threadIdx.x;
+    const int jt_x0 = (int)blockIdx.x * {32 * L['xc']}, jt_y0 = (int)blockIdx.y * {self.TMA_TY};
+    const int jt_z0 = (int)(blockIdx.z * g.loop);
+    const int jt_nk = (int)min(g.loop, g.cnt[2] - (long long)jt_z0), jt_nq = jt_nk + {SP - 1};
+    int jt_issued = 0;
+    auto jt_issue = [&](int q_, int s_) {{
+{chr(10).join(issue)}
+    }};
+    if (jt_tid == 0) {{
+        for (int s_ = 0; s_ < {S}; ++s_) jt_bar_init(jt_bar + s_);
+        jt_fence_init();
+{chr(10).join(f"        jt_prefetch(&t_.tm[{i}]);" for i in range(len(L["arrays"])))}
+    }}
+    __syncthreads();
+    if (jt_tid == 0)
+        for (; jt_issued < jt_nq && jt_issued < {S}; ++jt_issued) jt_issue(jt_issued, jt_issued);
+    bool jt_to = false;  // a wait for a staged plane gave up
+    unsigned jt_ph = 0;  // bit s: parity of the next wait on stage s
+    for (int c_ = 0; c_ < {SP - 1}; ++c_) {{  // the first step's planes but its last
+        if (!jt_to) jt_to = !jt_wait(jt_bar + c_, 0u);
+        jt_ph ^= 1u << c_;
+    }}
+    int jt_s = 0;  // stage of plane it_
+    int jt_w = {SP - 1};  // stage of the plane this step waits for: it_ + {SP - 1}
+    for (int it_ = 0; it_ < jt_nk; ++it_) {{
+    const long long uz = (long long)jt_z0 + it_;
+    const long long tz = uz;
+    if (!jt_to) jt_to = !jt_wait(jt_bar + jt_w, (jt_ph >> jt_w) & 1u);
+    jt_ph ^= 1u << jt_w;
+{planes}"""
+        zpost = f"""    if (__syncthreads_or(jt_to)) {{
+        if (jt_tid == 0) {{
+            atomicOr(g.err, 8);
+            for (int q_ = it_; q_ < jt_issued; ++q_) jt_wait(jt_bar + q_ % {S}, (unsigned)((q_ / {S}) & 1));
+        }}
+        break;
+    }}
+    if (jt_tid == 0 && jt_issued < jt_nq) {{ jt_issue(jt_issued, jt_s); ++jt_issued; }}
+    jt_s = jt_s + 1 == {S} ? 0 : jt_s + 1;
+    jt_w = jt_w + 1 == {S} ? 0 : jt_w + 1;
+    }}"""
+        return guard, zpre, zpost
+
     def body_lines(self):
         """The kernel body's statements as CUDA C lines (one thread's work)."""
         out = []
@@ -1019,6 +1151,9 @@ class _Gen:
         self.collect_temps()
         self.infer_locals(kd.body)
         body = self.body_lines()
+        if self.tma:
+            self.layout = self.tma_layout(real)
+            body = self.tma_resolve(body)
         decl = ["    bool big_ = false;"] if self.split else []
         for name, k in self.aidx.items():
             decl.append(f"    E* const a{k} = (E*)g.a[{k}];")
@@ -1060,6 +1195,8 @@ class _Gen:
     if ({u[sd]} >= g.cnt[{sd}]) break;
     const long long {t[sd]} = g.lo[{sd}] + {u[sd]};"""
             zpost = "    }"
+        if self.tma:
+            guard, zpre, zpost = self.tma_loop()
         pos = "const long long " + ", ".join(f"{t[d]} = g.lo[{d}] + {u[d]}" for d in grid)
         # the boundary-first variant: the body in a block that a finished thread jumps past, then the count
         head = "    const uint3 bi = jl_block(g);\n    {\n" if self.ordered else ""
@@ -1071,7 +1208,7 @@ class _Gen:
         return f"""// {kd.kind} {kd.name} ({self.nd}-D, {real}{sweep}) -- generated by ps_gb300.jit
 {self.types(real)}
 struct ps_jit_args {{ void* a[{MAX_ARRAYS}]; long long n[{MAX_ARRAYS}][3]; double s[{MAX_SCALARS}]; long long lo[3]; long long cnt[3]; int* err; long long smem; long long loop; unsigned* ocnt; int ord[10]; }};
-{_BLOCK_ORDER if self.ordered else ""}
+{_TMA_HELPERS if self.tma else ""}{_BLOCK_ORDER if self.ordered else ""}
 __device__ __forceinline__ bool jl_in(long long n0, long long n1, long long n2, long long i, long long j, long long k) {{
     return (unsigned long long)i < (unsigned long long)n0 && (unsigned long long)j < (unsigned long long)n1 && (unsigned long long)k < (unsigned long long)n2; }}
 __device__ __forceinline__ E jl_ld(const E* a, long long n0, long long n1, long long n2, long long i, long long j, long long k, int* err) {{
@@ -1093,9 +1230,9 @@ __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov
 __device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
-extern "C" __global__ void {bounds}ps_jit_entry(const ps_jit_args g) {{
-    extern __shared__ __align__(16) unsigned char ps_smem[];
-{head}    const long long {udecl};
+extern "C" __global__ void {bounds}ps_jit_entry({'const __grid_constant__ ps_jit_targs t_' if self.tma else 'const ps_jit_args g'}) {{
+    extern __shared__ __align__({128 if self.tma else 16}) unsigned char ps_smem[];
+{'    const ps_jit_args& g = t_.g;' + chr(10) if self.tma else ''}{head}    const long long {udecl};
 {guard}
     {pos};
     (void)ps_smem;
@@ -1103,6 +1240,40 @@ extern "C" __global__ void {bounds}ps_jit_entry(const ps_jit_args g) {{
 {chr(10).join(body)}
 {zpost}
 {tail}}}
+"""
+
+
+class _NoTma(Exception):
+    """The TMA variant does not apply to this kernel (no staged stencil arrays, more than eight, or
+    boxes or a ring too large); the plain sweep is generated instead."""
+
+
+# TMA staging of the 3-D sweep variant: the argument block with the tensor maps in front (the
+# layout ps_jit_launch_tma fills), mbarrier set-up, a bounded wait (a wait that gives up makes the
+# block stop and report flag 8) and the 3-D tile load into shared memory.
+_TMA_HELPERS = r"""
+struct alignas(64) ps_jit_targs { alignas(64) unsigned long long tm[8][16]; ps_jit_args g; };
+__device__ __forceinline__ unsigned jt_s32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void jt_bar_init(unsigned long long* b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(jt_s32(b)) : "memory"); }
+__device__ __forceinline__ void jt_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void jt_prefetch(const void* m) {
+    asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<unsigned long long>(m)) : "memory"); }
+__device__ __forceinline__ void jt_expect(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(jt_s32(b)), "r"(bytes) : "memory"); }
+__device__ __forceinline__ bool jt_wait(unsigned long long* b, unsigned parity) {
+    for (int i = 0; i < (1 << 22); ++i) {
+        unsigned ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(jt_s32(b)), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void jt_tma3(void* dst, const void* map, unsigned long long* b, int x, int y, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
+                 :: "r"(jt_s32(dst)), "l"(reinterpret_cast<unsigned long long>(map)), "r"(jt_s32(b)), "r"(x), "r"(y), "r"(z)
+                 : "memory"); }
 """
 
 
@@ -1224,10 +1395,20 @@ def generate(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False) -> str:
 
 
 def _generate_info(kd: KernelDef, ndims: int, dtype: str, zloop: bool = False, split: bool = False,
-                   ordered: bool = False):
+                   ordered: bool = False, tma: bool = False):
+    """(source, uses collectives, TMA layout or None); tma asks for the TMA variant of a 3-D sweep,
+    which falls back to the plain sweep where it does not apply."""
+    if tma:
+        g = _Gen(kd, ndims, zloop, split, ordered, tma=True)
+        if g.tma:
+            try:
+                src = g.source(dtype)
+                return src, g.uses_collectives, g.layout
+            except _NoTma:
+                pass
     g = _Gen(kd, ndims, zloop, split, ordered)
     src = g.source(dtype)
-    return src, g.uses_collectives
+    return src, g.uses_collectives, None
 
 
 # ---- kernels -----------------------------------------------------------------------------------
@@ -1243,19 +1424,25 @@ class JitKernel:
 
     def __init__(self, src: str, ndims=None):
         self.ndims = ndims
+        # 3-D sweeps of FP32 arrays stage their stencil arrays by TMA where the launch allows it
+        # ("always": FP64 too -- slower there: the FP64 kernels are bound by arithmetic, not loads)
+        self.tma = True
+        self.tma_launches = 0  # launches that took the TMA variant
         self.kd = parse(src)
         self._kernel_language = uses_kernel_language(self.kd)
         self.name, self.nargs = self.kd.name, len(self.kd.args)
         self._handles = {}
         self._collective = {}
+        self._layouts = {}  # TMA stage layout of each TMA-variant handle (None: the plain sweep was generated)
 
     def source(self, ndims, dtype="double"):
         return generate(self.kd, ndims, dtype)
 
-    def _handle(self, ndims, dtype, zloop=False, split=False, ordered=False):
-        key = (ndims, dtype, bool(zloop), bool(split)) + (("ordered",) if ordered else ())
+    def _handle(self, ndims, dtype, zloop=False, split=False, ordered=False, tma=False):
+        key = (ndims, dtype, bool(zloop), bool(split)) + (("ordered",) if ordered else ()) + (("tma",) if tma else ())
         if key not in self._handles:
-            src, self._collective[key] = _generate_info(self.kd, ndims, dtype, zloop, split, ordered)
+            src, self._collective[key], self._layouts[key] = _generate_info(self.kd, ndims, dtype, zloop, split,
+                                                                            ordered, tma)
             h = ctypes.c_void_p()
             _lib.call("ps_jit_compile", src.encode(), b"ps_jit_entry", ctypes.byref(h))
             self._handles[key] = h
@@ -1277,8 +1464,17 @@ class JitKernel:
         launch would have fewer threads than the GPU holds at once -- with the same results.
         fp64="split" evaluates the arithmetic of FP64 kernels on FP32 pairs (each operation within
         ~2^-46 of its operands' magnitude; GB300 issues FP32 at 64x the FP64 rate)."""
-        h, A, nA, S, nS, lo, cnt, threads, shmem, loop = self._config(args, ranges, nblocks, nthreads, shmem, memopt,
-                                                                     loopsize, fp64)
+        h, A, nA, S, nS, lo, cnt, threads, shmem, loop, layout = self._config(args, ranges, nblocks, nthreads, shmem,
+                                                                             memopt, loopsize, fp64, allow_tma=True)
+        if layout is not None:  # the 3-D sweep with its stencil arrays staged by TMA
+            maps = [x for a in layout["arrays"] for x in (a["k"], a["bx"], a["by"])]
+            cnt_t = [-(-cnt[0] // layout["xc"]), cnt[1], cnt[2]]  # threads in x: each covers xc columns
+            _lib.call("ps_jit_launch_tma", h, A, nA, S, nS, (ctypes.c_int64 * 3)(*cnt_t),
+                      (ctypes.c_int32 * 3)(32, _Gen.TMA_TY, 1), int(layout["smem"]), int(loop[2]),
+                      (ctypes.c_int32 * len(maps))(*maps), len(layout["arrays"]), stream_handle(stream),
+                      int(bool(sync)))
+            self.tma_launches += 1
+            return
         _lib.call("ps_jit_launch_ex", h, A, nA, S, nS, (ctypes.c_int64 * 3)(*lo), (ctypes.c_int64 * 3)(*cnt),
                   (ctypes.c_int32 * 3)(*threads), int(shmem or 0), (ctypes.c_int32 * 3)(*loop), stream_handle(stream),
                   int(bool(sync)))
@@ -1292,14 +1488,15 @@ class JitKernel:
     def hide_communication(self, args, bw, comm_fn, stream=None, memopt=None, loopsize=0, fp64="ieee"):
         """One boundary-first launch over the kernel's full grid (ps_jit_hide_communication); comm_fn
         (a ps_comm_fn) runs once the boundary tiles are done."""
-        h, A, nA, S, nS, lo, cnt, threads, shmem, loop = self._config(args, None, None, None, None, memopt, loopsize,
-                                                                     fp64, ordered=True)
+        h, A, nA, S, nS, lo, cnt, threads, shmem, loop, _ = self._config(args, None, None, None, None, memopt,
+                                                                        loopsize, fp64, ordered=True)
         _lib.call("ps_jit_hide_communication", h, A, nA, S, nS, (ctypes.c_int64 * 3)(*cnt),
                   (ctypes.c_int32 * 3)(*threads), (ctypes.c_int32 * 3)(*loop), (ctypes.c_int64 * 3)(*bw), comm_fn,
                   None, stream_handle(stream))
 
-    def _config(self, args, ranges, nblocks, nthreads, shmem, memopt, loopsize, fp64, ordered=False):
-        """Handle, argument arrays and launch geometry of one launch (see jit_launch)."""
+    def _config(self, args, ranges, nblocks, nthreads, shmem, memopt, loopsize, fp64, ordered=False, allow_tma=False):
+        """Handle, argument arrays, launch geometry and TMA stage layout (None: no staging) of one
+        launch (see jit_launch); allow_tma picks the TMA variant of a 3-D sweep where it applies."""
         require_initialized()
         if len(args) != self.nargs:
             raise ArgumentError(f"{self.name} takes {self.nargs} arguments (obtained {len(args)})")
@@ -1357,14 +1554,24 @@ class JitKernel:
         if fp64 not in ("ieee", "split", "split_state", "split_grid"):
             raise ArgumentError("fp64 must be 'ieee' or 'split'")
         sp = fp64 != "ieee" and dt == "double"
+        A = (PSArray * max(1, len(descs)))(*descs)
+        S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
+        if allow_tma and self.tma and (dt == "float" or self.tma == "always") and zl and ndims == 3 and \
+                not ordered and ranges is None and nblocks is None and nthreads is None and not shmem:
+            # the 3-D sweep with its stencil arrays staged by TMA, where every staged array meets TMA's
+            # 16-byte rules (base address, x extent and x-y plane in bytes); else the plain sweep
+            es = 8 if dt == "double" else 4
+            ht = self._handle(ndims, dt, zl, sp, False, tma=True)
+            layout = self._layouts[(ndims, dt, zl, sp, "tma")]
+            if layout is not None and all(not ((d.ptr or 0) % 16 or (d.n[0] * es) % 16 or (d.n[0] * d.n[1] * es) % 16)
+                                          for d in (descs[a["k"]] for a in layout["arrays"])):
+                return ht, A, len(descs), S, len(scal), lo, cnt, threads, shmem, loop, layout
         h = self._handle(ndims, dt, zl, sp, ordered)
         if self._collective[(ndims, dt, zl, sp) + (("ordered",) if ordered else ())] and \
                 any(cnt[d] % threads[d] for d in range(3)):
             raise ArgumentError("a kernel with @sync_threads, shuffles or votes needs ranges that are a multiple of "
                                 f"the thread block (ranges {cnt}, nthreads {threads})")
-        A = (PSArray * max(1, len(descs)))(*descs)
-        S = (ctypes.c_double * max(1, len(scal)))(*[float(x) for x in scal])
-        return h, A, len(descs), S, len(scal), lo, cnt, threads, shmem, loop
+        return h, A, len(descs), S, len(scal), lo, cnt, threads, shmem, loop, None
 
     @staticmethod
     def _extent(descs, ndims):

@@ -395,3 +395,69 @@ def test_interpreter_and_c_oracle_agree(jr, oracle, dtn):
                 p = np.asfortranarray(np.full(shape, -7.0, dtype=dt))
                 jr.run(f"@parallel function f!(R, A)\n    @{lhs}(R) = @{op}(A)\n    return\nend", [p, A], ndims=nd)
                 assert np.array_equal(c, p, equal_nan=True), (nd, op, lhs)
+
+
+# ---------------------------------------------------------------- the TMA variant of 3-D sweeps
+_TMA_KERNELS = ["HEAT_FLUX", "HEAT_LAP", "HEAT_DIV", "BLEND3D", "FACES3D", "TWO3D", "COMPACTION"]
+
+
+def _tma_info(jit, name, real, split=False):
+    src, _, layout = jit._generate_info(jit.parse(getattr(K, name)), 3, real, True, split, False, True)
+    return src, layout
+
+
+@pytest.mark.parametrize("real", ["double", "float"])
+@pytest.mark.parametrize("name", _TMA_KERNELS)
+def test_tma_layout_covers_every_staged_read(jit, name, real):
+    """Checked on the CPU before any launch: each staged array's TMA box starts on a 16-byte
+    boundary in x (the tile origin is a multiple of 32 elements), every (thread, offset) read of the
+    generated kernel falls inside its array's box, planes lie inside the ring's span, and the
+    stages and mbarriers fit the shared memory the launch gives."""
+    src, L = _tma_info(jit, name, real)
+    assert L is not None, name
+    es = 8 if real == "double" else 4
+    g = jit._Gen(jit.parse(getattr(K, name)), 3, True, False, False, tma=True)
+    g.source(real)
+    ty = jit._Gen.TMA_TY
+    ends = sorted(a["off"] for a in L["arrays"]) + [L["stage"]]
+    for a in L["arrays"]:
+        assert (a["xs"] * es) % 16 == 0 and (32 * L["xc"] * es) % 16 == 0 and (a["bx"] * es) % 16 == 0
+        assert a["bx"] <= 256 and a["by"] <= 256 and a["off"] % 128 == 0
+        nxt = min(e for e in ends if e > a["off"])
+        assert a["off"] + a["bx"] * a["by"] * es <= nxt
+        for o in g.staged[a["name"]]:
+            assert 0 <= o[2] - L["zl"] < L["span"]
+            for lx in (0, 32 * L["xc"] - 1):
+                for ly in (0, ty - 1):
+                    assert 0 <= lx + o[0] - a["xs"] < a["bx"], (a, o)
+                    assert 0 <= ly + o[1] - a["ys"] < a["by"], (a, o)
+    assert L["stages"] >= L["span"] + 2 and L["stage"] % 128 == 0
+    assert L["smem"] == L["stages"] * L["stage"] + 8 * L["stages"] and L["smem"] <= 227 * 1024
+    assert L["tx_bytes"] == sum(a["bx"] * a["by"] * es for a in L["arrays"]) < 2 ** 20
+    assert "__TMA[" not in src and "ps_jit_targs" in src and "cp.async.bulk.tensor.3d" in src
+
+
+@pytest.mark.skipif(_nvcc() is None, reason="nvcc not available")
+def test_tma_sources_compile_for_sm103a(jit, tmp_path):
+    procs = []
+    for name in _TMA_KERNELS:
+        for real, split in (("double", False), ("float", False), ("double", True)):
+            src, L = _tma_info(jit, name, real, split)
+            f = tmp_path / f"{name}_{real}_{split}.cu"
+            f.write_text(src)
+            procs.append((f, subprocess.Popen([_nvcc(), "-arch=sm_103a", "-std=c++17", "--fmad=false", "-c", str(f),
+                                               "-o", str(f) + ".o"], stdout=subprocess.PIPE,
+                                              stderr=subprocess.STDOUT, text=True)))
+            if len(procs) % 8 == 0:
+                for _, p in procs[-8:]:
+                    p.wait()
+    for f, p in procs:
+        out = p.communicate()[0]
+        assert p.returncode == 0, (f.name, out[-2000:])
+
+
+def test_tma_variant_falls_back_where_it_cannot_apply(jit):
+    """A kernel without read-only stencil arrays has nothing to stage: the plain sweep is generated."""
+    src = "@parallel function cp!(A, B)\n    @all(A) = @all(A) * 2.0\n    return\nend"
+    s, _, layout = jit._generate_info(jit.parse(src), 3, "double", True, False, False, True)
+    assert layout is None and "cp.async.bulk.tensor" not in s
