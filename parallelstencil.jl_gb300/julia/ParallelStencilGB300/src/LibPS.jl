@@ -327,6 +327,16 @@ function jit_launch!(h::Ptr{Cvoid}, arrays::Vector{PSArray}, scalars::Vector{Flo
                 h, arrays, Int32(length(arrays)), scalars, Int32(length(scalars)), lo, count, threads, Int64(shmem),
                 loop, stream_ptr(stream), Cint(sync)))
 end
+# the TMA variant of an FP32 3-D sweep: maps = (array index, box x, box y) per staged array
+function jit_launch_tma!(h::Ptr{Cvoid}, arrays::Vector{PSArray}, scalars::Vector{Float64},
+                         count::NTuple{3,Int64}, threads::NTuple{3,Int32}, shmem::Integer, loop_z::Integer,
+                         maps::Vector{Int32}; stream = CUDA.stream(), sync = true)
+    check(ccall((:ps_jit_launch_tma, lib), Cint,
+                (Ptr{Cvoid}, Ptr{PSArray}, Int32, Ptr{Cdouble}, Int32, Ref{NTuple{3,Int64}}, Ref{NTuple{3,Int32}},
+                 Int64, Int32, Ptr{Int32}, Int32, Ptr{Cvoid}, Cint),
+                h, arrays, Int32(length(arrays)), scalars, Int32(length(scalars)), count, threads, Int64(shmem),
+                Int32(loop_z), maps, Int32(length(maps) ÷ 3), stream_ptr(stream), Cint(sync)))
+end
 jit_check(h::Ptr{Cvoid}; stream = CUDA.stream()) =
     check(ccall((:ps_jit_check, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), h, stream_ptr(stream)))
 jit_destroy(h::Ptr{Cvoid}) = check(ccall((:ps_jit_destroy, lib), Cint, (Ptr{Cvoid},), h))
