@@ -111,7 +111,8 @@ JL_TO_C = {
     "Ptr{Cvoid}": {"void*", "const void*", "ps_comm_fn"}, "Cstring": {"const char*"},
     "PSArray": {"ps_array"}, "PSFdOp": {"ps_fd_op"},
     "Ref{PSLaunch}": {"const ps_launch*"}, "Ptr{Cdouble}": {"double*", "const double*", "double[3]"},
-    "Ptr{Int64}": {"const int64_t[3]"}, "Ref{Ptr{Cvoid}}": {"void**"}, "Ptr{PSArray}": {"const ps_array*"},
+    "Ptr{Int64}": {"const int64_t[3]"}, "Ptr{Int32}": {"const int32_t*"}, "Ref{Ptr{Cvoid}}": {"void**"},
+    "Ptr{PSArray}": {"const ps_array*"},
     "Ref{NTuple{3,Int64}}": {"const int64_t[3]"}, "Ref{NTuple{3,Int32}}": {"const int32_t[3]"},
     "Ref{Stokes2DFields}": {"const ps_stokes2d_fields*"}, "Ref{Stokes2DParams}": {"const ps_stokes2d_params*"},
     "Ref{Stokes2DAPTFields}": {"const ps_stokes2d_apt_fields*"},
