@@ -407,9 +407,8 @@ def run_ours(a, world, rank, local):
         e2e_batches_s = [round(b[0], 5) for b in batches]
         launches += (3 * jobs + 4) * NT_JOB
         del hostbufs, hT, hCi, hlam, hout, sets
-        # the other 512^3 FP64 variants run after the e2e jobs: with the jobs measured after them, single
-        # host-to-device copies stalled for 100-250 ms (about 19 GB/s instead of 210) in most batches on
-        # several boxes; measured right after the headline (as --quick does) they ran at 210 GB/s
+        # the other 512^3 FP64 variants run after the e2e jobs, so that --quick measures the jobs in the
+        # same state of the process as the full run
         if not a.quick:
             ieee_steps = max(3, a.steps // 10)
             bench_kernel("diffusion3d_flux_lam_f64_ieee_memopt", ps.kernels.diffusion3D_step_flux_lam, arrs64,
