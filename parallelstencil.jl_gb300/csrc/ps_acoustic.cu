@@ -59,6 +59,8 @@ template <typename T>
 struct AcuIeee {
     using S = T;
     using V = T;
+    // CTAs per SM the kernel is compiled for: FP32 fits five (47 registers, no spills), FP64 four
+    static constexpr int kMinBlocks = sizeof(T) == 4 ? 5 : 4;
     struct C {
         T dtr, dtk;
         DivC<T> h[3];
@@ -82,6 +84,7 @@ struct AcuIeee {
 struct AcuSplit {
     using S = double;
     using V = dd;
+    static constexpr int kMinBlocks = 4;
     struct C {
         dd cv[3];  // (dt/ρ)/h_d as h + l, and its remainder r (h + l + r exact to ~2^-72)
         dd ck[3];  // (dt·k)/h_d
@@ -121,7 +124,7 @@ struct AcuSplit {
 // slower, their registers cost occupancy). I: the index type of element offsets (int when every
 // array has fewer than 2^31 elements). Offsets advance by the plane strides along the sweep.
 template <class AR, typename I>
-__global__ void __launch_bounds__(32 * ACU_W, 4) acoustic_step_kernel(AcuArrays<typename AR::S> a,
+__global__ void __launch_bounds__(32 * ACU_W, AR::kMinBlocks) acoustic_step_kernel(AcuArrays<typename AR::S> a,
                                                                     typename AR::C c, int Lz, int* err) {
     using S = typename AR::S;
     using V = typename AR::V;
@@ -163,25 +166,33 @@ __global__ void __launch_bounds__(32 * ACU_W, 4) acoustic_step_kernel(AcuArrays<
         if (xv && z0 == 0) a.Vz2[oP] = vo;  // face 0 is outside @inn(Vz)
     }
 
-    // the own-cell loads run one plane ahead: P(z+1), the Vz face z+1, the Vx and Vy faces of z
+    // every load runs one plane ahead: P(z+1), the Vz face z+1, the Vx and Vy faces of z, the Vy face
+    // y+1, the P rows y-1 and y+1 and the edge lanes' P and Vx values of the plane
+    const I xe = lane == 0 ? -1 : 1;  // the edge lanes' neighbour column
     S f_pn = (xv && z0 + 1 < nz) ? a.P[oP + sP] : S(0);
     S f_vzo = xv ? a.Vz[oP + sP] : S(0);
     S f_vxo = xv ? a.Vx[oX] : S(0);
     S f_vy0 = xv ? a.Vy[oY] : S(0);
+    S f_vy1 = xv ? a.Vy[oY + nx] : S(0);  // face y + 1 <= ny
+    S f_plo = ld_lo ? a.P[oP - nx] : S(0);
+    S f_phi = ld_hi ? a.P[oP + nx] : S(0);
+    S f_xep = (e_lo || e_p31) ? a.P[oP + xe] : S(0);
+    S f_xev = e_hi ? a.Vx[oX + 1] : S(0);
     for (I z = z0; z < z1; ++z, oP += sP, oX += sX, oY += sY) {
         const bool zin = z >= 1 && z <= nz - 2;  // the z range of @inn(Vx), @inn(Vy)
         const S pn = f_pn, vzo = f_vzo, vxo = f_vxo, vy0 = f_vy0;
+        const S vy1 = f_vy1, plo = f_plo, phi = f_phi, xep = f_xep, xev = f_xev;
         if (z + 1 < z1) {
             f_pn = (xv && z + 2 < nz) ? a.P[oP + 2 * sP] : S(0);
             f_vzo = xv ? a.Vz[oP + 2 * sP] : S(0);  // face z + 2 <= nz
             f_vxo = xv ? a.Vx[oX + sX] : S(0);
             f_vy0 = xv ? a.Vy[oY + sY] : S(0);
+            f_vy1 = xv ? a.Vy[oY + sY + nx] : S(0);
+            f_plo = ld_lo ? a.P[oP + sP - nx] : S(0);
+            f_phi = ld_hi ? a.P[oP + sP + nx] : S(0);
+            f_xep = (e_lo || e_p31) ? a.P[oP + sP + xe] : S(0);
+            f_xev = e_hi ? a.Vx[oX + sX + 1] : S(0);
         }
-        const S vy1 = xv ? a.Vy[oY + nx] : S(0);   // face y + 1 <= ny
-        const S plo = ld_lo ? a.P[oP - nx] : S(0);
-        const S phi = ld_hi ? a.P[oP + nx] : S(0);
-        const S xep = (e_lo || e_p31) ? a.P[lane == 0 ? oP - 1 : oP + 1] : S(0);
-        const S xev = e_hi ? a.Vx[oX + 1] : S(0);
 
         // Vy on faces y and y + 1
         V vyn0 = AR::in(vy0, big), vyn1 = AR::in(vy1, big);
