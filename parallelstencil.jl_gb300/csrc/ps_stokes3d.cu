@@ -60,6 +60,8 @@ struct S3A {
 enum { S3_PLAIN = 0, S3_DEFECT = 1, S3_RESIDUAL = 2 };
 
 #define I3(a, b, c, n0, n1) ((int64_t)(a) + (int64_t)(n0) * ((int64_t)(b) + (int64_t)(n1) * (int64_t)(c)))
+// the same in the index type I of the iteration kernels (32-bit where every array has < 2^31 elements)
+#define I3T(a, b, c, n0, n1) ((I)(a) + (I)(n0) * ((I)(b) + (I)(n1) * (I)(c)))
 
 // ---- statement arithmetic ------------------------------------------------------------------
 template <typename T>
@@ -72,12 +74,12 @@ __device__ __forceinline__ T s3_dtPt(T Ptsc, T m, T mn) {
     return ((Ptsc * T(6.1)) * m) / mn;
 }
 // @d_xa(Vx)/dx + @d_ya(Vy)/dy + @d_za(Vz)/dz at cell (x, y, z)
-template <typename T>
-__device__ __forceinline__ T s3_divV(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
-    const int64_t nx = a.nx, ny = a.ny;
-    return (div_c(a.Vx[I3(x + 1, y, z, nx + 1, ny)] - a.Vx[I3(x, y, z, nx + 1, ny)], p.dx) +
-            div_c(a.Vy[I3(x, y + 1, z, nx, ny + 1)] - a.Vy[I3(x, y, z, nx, ny + 1)], p.dy)) +
-           div_c(a.Vz[I3(x, y, z + 1, nx, ny)] - a.Vz[I3(x, y, z, nx, ny)], p.dz);
+template <typename T, typename I = int64_t>
+__device__ __forceinline__ T s3_divV(const S3A<T>& a, const S3P<T>& p, I x, I y, I z) {
+    const I nx = (I)a.nx, ny = (I)a.ny;
+    return (div_c(a.Vx[I3T(x + 1, y, z, nx + 1, ny)] - a.Vx[I3T(x, y, z, nx + 1, ny)], p.dx) +
+            div_c(a.Vy[I3T(x, y + 1, z, nx, ny + 1)] - a.Vy[I3T(x, y, z, nx, ny + 1)], p.dy)) +
+           div_c(a.Vz[I3T(x, y, z + 1, nx, ny)] - a.Vz[I3T(x, y, z, nx, ny)], p.dz);
 }
 // 2.0*μ*(dV/h - 1.0/3.0*∇V)
 template <typename T>
@@ -91,50 +93,49 @@ __device__ __forceinline__ T s3_tsh(T m0, T m1, T m2, T m3, T a, const DivC<T>& 
     return (T(2.0) * av) * (T(0.5) * (div_c(a, ha) + div_c(b, hb)));
 }
 
-template <typename T>
-__device__ __forceinline__ void s3_txy(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
-    const int64_t nx = a.nx, ny = a.ny;
+template <typename T, typename I = int64_t>
+__device__ __forceinline__ void s3_txy(const S3A<T>& a, const S3P<T>& p, I x, I y, I z) {
+    const I nx = (I)a.nx, ny = (I)a.ny;
     const T* M = a.Mus;
-    a.txy[I3(x, y, z, nx - 1, ny - 1)] =
-        s3_tsh(M[I3(x, y, z + 1, nx, ny)], M[I3(x + 1, y, z + 1, nx, ny)], M[I3(x, y + 1, z + 1, nx, ny)],
-               M[I3(x + 1, y + 1, z + 1, nx, ny)],
-               a.Vx[I3(x + 1, y + 1, z + 1, nx + 1, ny)] - a.Vx[I3(x + 1, y, z + 1, nx + 1, ny)], p.dy,
-               a.Vy[I3(x + 1, y + 1, z + 1, nx, ny + 1)] - a.Vy[I3(x, y + 1, z + 1, nx, ny + 1)], p.dx);
+    a.txy[I3T(x, y, z, nx - 1, ny - 1)] =
+        s3_tsh(M[I3T(x, y, z + 1, nx, ny)], M[I3T(x + 1, y, z + 1, nx, ny)], M[I3T(x, y + 1, z + 1, nx, ny)],
+               M[I3T(x + 1, y + 1, z + 1, nx, ny)],
+               a.Vx[I3T(x + 1, y + 1, z + 1, nx + 1, ny)] - a.Vx[I3T(x + 1, y, z + 1, nx + 1, ny)], p.dy,
+               a.Vy[I3T(x + 1, y + 1, z + 1, nx, ny + 1)] - a.Vy[I3T(x, y + 1, z + 1, nx, ny + 1)], p.dx);
 }
-template <typename T>
-__device__ __forceinline__ void s3_txz(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
-    const int64_t nx = a.nx, ny = a.ny;
+template <typename T, typename I = int64_t>
+__device__ __forceinline__ void s3_txz(const S3A<T>& a, const S3P<T>& p, I x, I y, I z) {
+    const I nx = (I)a.nx, ny = (I)a.ny;
     const T* M = a.Mus;
-    a.txz[I3(x, y, z, nx - 1, ny - 2)] =
-        s3_tsh(M[I3(x, y + 1, z, nx, ny)], M[I3(x + 1, y + 1, z, nx, ny)], M[I3(x, y + 1, z + 1, nx, ny)],
-               M[I3(x + 1, y + 1, z + 1, nx, ny)],
-               a.Vx[I3(x + 1, y + 1, z + 1, nx + 1, ny)] - a.Vx[I3(x + 1, y + 1, z, nx + 1, ny)], p.dz,
-               a.Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - a.Vz[I3(x, y + 1, z + 1, nx, ny)], p.dx);
+    a.txz[I3T(x, y, z, nx - 1, ny - 2)] =
+        s3_tsh(M[I3T(x, y + 1, z, nx, ny)], M[I3T(x + 1, y + 1, z, nx, ny)], M[I3T(x, y + 1, z + 1, nx, ny)],
+               M[I3T(x + 1, y + 1, z + 1, nx, ny)],
+               a.Vx[I3T(x + 1, y + 1, z + 1, nx + 1, ny)] - a.Vx[I3T(x + 1, y + 1, z, nx + 1, ny)], p.dz,
+               a.Vz[I3T(x + 1, y + 1, z + 1, nx, ny)] - a.Vz[I3T(x, y + 1, z + 1, nx, ny)], p.dx);
 }
-template <typename T>
-__device__ __forceinline__ void s3_tyz(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z) {
-    const int64_t nx = a.nx, ny = a.ny;
+template <typename T, typename I = int64_t>
+__device__ __forceinline__ void s3_tyz(const S3A<T>& a, const S3P<T>& p, I x, I y, I z) {
+    const I nx = (I)a.nx, ny = (I)a.ny;
     const T* M = a.Mus;
-    a.tyz[I3(x, y, z, nx - 2, ny - 1)] =
-        s3_tsh(M[I3(x + 1, y, z, nx, ny)], M[I3(x + 1, y + 1, z, nx, ny)], M[I3(x + 1, y, z + 1, nx, ny)],
-               M[I3(x + 1, y + 1, z + 1, nx, ny)],
-               a.Vy[I3(x + 1, y + 1, z + 1, nx, ny + 1)] - a.Vy[I3(x + 1, y + 1, z, nx, ny + 1)], p.dz,
-               a.Vz[I3(x + 1, y + 1, z + 1, nx, ny)] - a.Vz[I3(x + 1, y, z + 1, nx, ny)], p.dy);
+    a.tyz[I3T(x, y, z, nx - 2, ny - 1)] =
+        s3_tsh(M[I3T(x + 1, y, z, nx, ny)], M[I3T(x + 1, y + 1, z, nx, ny)], M[I3T(x + 1, y, z + 1, nx, ny)],
+               M[I3T(x + 1, y + 1, z + 1, nx, ny)],
+               a.Vy[I3T(x + 1, y + 1, z + 1, nx, ny + 1)] - a.Vy[I3T(x + 1, y + 1, z, nx, ny + 1)], p.dz,
+               a.Vz[I3T(x + 1, y + 1, z + 1, nx, ny)] - a.Vz[I3T(x + 1, y, z + 1, nx, ny)], p.dy);
 }
 
 // compute_dV! statements at residual index (x, y, z) and, with update_V, compute_V! at the same
 // index (it reads only the pseudo-velocity just written)
-template <typename T, int MODE = S3_PLAIN>
-__device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t x, int64_t y, int64_t z,
-                                      bool update_V) {
-    const int64_t nx = a.nx, ny = a.ny, nz = a.nz;
+template <typename T, int MODE = S3_PLAIN, typename I = int64_t>
+__device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, I x, I y, I z, bool update_V) {
+    const I nx = (I)a.nx, ny = (I)a.ny, nz = (I)a.nz;
     const T* Pt = a.Pt;
     if (x < nx - 1 && y < ny - 2 && z < nz - 2) {
-        const int64_t r = I3(x, y, z, nx - 1, ny - 2);
-        const T A = a.txx[I3(x + 1, y, z, nx, ny - 2)] - a.txx[I3(x, y, z, nx, ny - 2)];
-        const T B = a.txy[I3(x, y + 1, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
-        const T C = a.txz[I3(x, y, z + 1, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
-        const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x, y + 1, z + 1, nx, ny)];
+        const I r = I3T(x, y, z, nx - 1, ny - 2);
+        const T A = a.txx[I3T(x + 1, y, z, nx, ny - 2)] - a.txx[I3T(x, y, z, nx, ny - 2)];
+        const T B = a.txy[I3T(x, y + 1, z, nx - 1, ny - 1)] - a.txy[I3T(x, y, z, nx - 1, ny - 1)];
+        const T C = a.txz[I3T(x, y, z + 1, nx - 1, ny - 2)] - a.txz[I3T(x, y, z, nx - 1, ny - 2)];
+        const T P = Pt[I3T(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3T(x, y + 1, z + 1, nx, ny)];
         T R = ((div_c(A, p.dx) + div_c(B, p.dy)) + div_c(C, p.dz)) - div_c(P, p.dx);
         if constexpr (MODE == S3_DEFECT) R = R + a.fx[r];
         a.Rx[r] = R;
@@ -142,17 +143,17 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
             const T dv = p.dampX * a.dVx[r] + R;
             a.dVx[r] = dv;
             if (update_V) {
-                const int64_t v = I3(x + 1, y + 1, z + 1, nx + 1, ny);
+                const I v = I3T(x + 1, y + 1, z + 1, nx + 1, ny);
                 a.Vx[v] = a.Vx[v] + a.dtVx[r] * dv;
             }
         }
     }
     if (x < nx - 2 && y < ny - 1 && z < nz - 2) {
-        const int64_t r = I3(x, y, z, nx - 2, ny - 1);
-        const T A = a.tyy[I3(x, y + 1, z, nx - 2, ny)] - a.tyy[I3(x, y, z, nx - 2, ny)];
-        const T B = a.txy[I3(x + 1, y, z, nx - 1, ny - 1)] - a.txy[I3(x, y, z, nx - 1, ny - 1)];
-        const T C = a.tyz[I3(x, y, z + 1, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
-        const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y, z + 1, nx, ny)];
+        const I r = I3T(x, y, z, nx - 2, ny - 1);
+        const T A = a.tyy[I3T(x, y + 1, z, nx - 2, ny)] - a.tyy[I3T(x, y, z, nx - 2, ny)];
+        const T B = a.txy[I3T(x + 1, y, z, nx - 1, ny - 1)] - a.txy[I3T(x, y, z, nx - 1, ny - 1)];
+        const T C = a.tyz[I3T(x, y, z + 1, nx - 2, ny - 1)] - a.tyz[I3T(x, y, z, nx - 2, ny - 1)];
+        const T P = Pt[I3T(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3T(x + 1, y, z + 1, nx, ny)];
         T R = ((div_c(A, p.dy) + div_c(B, p.dx)) + div_c(C, p.dz)) - div_c(P, p.dy);
         if constexpr (MODE == S3_DEFECT) R = R + a.fy[r];
         a.Ry[r] = R;
@@ -160,22 +161,22 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
             const T dv = p.dampY * a.dVy[r] + R;
             a.dVy[r] = dv;
             if (update_V) {
-                const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny + 1);
+                const I v = I3T(x + 1, y + 1, z + 1, nx, ny + 1);
                 a.Vy[v] = a.Vy[v] + a.dtVy[r] * dv;
             }
         }
     }
     if (x < nx - 2 && y < ny - 2 && z < nz - 1) {
-        const int64_t r = I3(x, y, z, nx - 2, ny - 2);
-        const T A = a.tzz[I3(x, y, z + 1, nx - 2, ny - 2)] - a.tzz[I3(x, y, z, nx - 2, ny - 2)];
-        const T B = a.txz[I3(x + 1, y, z, nx - 1, ny - 2)] - a.txz[I3(x, y, z, nx - 1, ny - 2)];
-        const T C = a.tyz[I3(x, y + 1, z, nx - 2, ny - 1)] - a.tyz[I3(x, y, z, nx - 2, ny - 1)];
-        const T P = Pt[I3(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3(x + 1, y + 1, z, nx, ny)];
+        const I r = I3T(x, y, z, nx - 2, ny - 2);
+        const T A = a.tzz[I3T(x, y, z + 1, nx - 2, ny - 2)] - a.tzz[I3T(x, y, z, nx - 2, ny - 2)];
+        const T B = a.txz[I3T(x + 1, y, z, nx - 1, ny - 2)] - a.txz[I3T(x, y, z, nx - 1, ny - 2)];
+        const T C = a.tyz[I3T(x, y + 1, z, nx - 2, ny - 1)] - a.tyz[I3T(x, y, z, nx - 2, ny - 1)];
+        const T P = Pt[I3T(x + 1, y + 1, z + 1, nx, ny)] - Pt[I3T(x + 1, y + 1, z, nx, ny)];
         T R;
         if constexpr (MODE == S3_DEFECT) {  // the buoyancy is part of the outer residual fz
             R = (((div_c(A, p.dz) + div_c(B, p.dx)) + div_c(C, p.dy)) - div_c(P, p.dz)) + a.fz[r];
         } else {
-            const T G = (a.Rog[I3(x + 1, y + 1, z, nx, ny)] + a.Rog[I3(x + 1, y + 1, z + 1, nx, ny)]) * T(0.5);
+            const T G = (a.Rog[I3T(x + 1, y + 1, z, nx, ny)] + a.Rog[I3T(x + 1, y + 1, z + 1, nx, ny)]) * T(0.5);
             R = (((div_c(A, p.dz) + div_c(B, p.dx)) + div_c(C, p.dy)) - div_c(P, p.dz)) + G;
         }
         a.Rz[r] = R;
@@ -183,7 +184,7 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
             const T dv = p.dampZ * a.dVz[r] + R;
             a.dVz[r] = dv;
             if (update_V) {
-                const int64_t v = I3(x + 1, y + 1, z + 1, nx, ny);
+                const I v = I3T(x + 1, y + 1, z + 1, nx, ny);
                 a.Vz[v] = a.Vz[v] + a.dtVz[r] * dv;
             }
         }
@@ -195,6 +196,12 @@ __device__ __forceinline__ void s3_dV(const S3A<T>& a, const S3P<T>& p, int64_t 
     const int64_t y = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;                        \
     const int64_t z = blockIdx.z;                                                            \
     const int64_t nx = a.nx, ny = a.ny, nz = a.nz;                                           \
+    if (x >= nx || y >= ny || z >= nz) return
+#define S3_IDXT                                                                              \
+    const I x = (I)(blockIdx.x * blockDim.x + threadIdx.x);                                  \
+    const I y = (I)(blockIdx.y * blockDim.y + threadIdx.y);                                  \
+    const I z = (I)blockIdx.z;                                                               \
+    const I nx = (I)a.nx, ny = (I)a.ny, nz = (I)a.nz;                                        \
     if (x >= nx || y >= ny || z >= nz) return
 
 // ---- one-to-one kernels (grid: max extents of the kernel's array arguments) ---------------
@@ -296,11 +303,11 @@ __global__ void s3_bc_axis_k(T* A, int64_t n0, int64_t n1, int64_t n2, int ax) {
 // ---- iteration kernels ---------------------------------------------------------------------
 // compute_P! and compute_τ! of cell (x, y, z): τxx, τyy, τzz are written at the index whose ∇V
 // is this cell's, τxy, τxz, τyz at the cell's own index.
-template <typename T, int MODE = S3_PLAIN>
+template <typename T, int MODE = S3_PLAIN, typename I = int64_t>
 __global__ void s3_Ptau_k(S3A<T> a, S3P<T> p) {
-    S3_IDX;
-    const int64_t c = I3(x, y, z, nx, ny);
-    const T d = s3_divV(a, p, x, y, z);
+    S3_IDXT;
+    const I c = I3T(x, y, z, nx, ny);
+    const T d = s3_divV<T, I>(a, p, x, y, z);
     if constexpr (MODE == S3_DEFECT) {  // the correction's continuity residual includes the outer one
         const T dp = d + a.fp[c];
         a.divV[c] = dp;
@@ -312,23 +319,23 @@ __global__ void s3_Ptau_k(S3A<T> a, S3P<T> p) {
     const T m = a.Mus[c];
     const bool iy = y >= 1 && y <= ny - 2, iz = z >= 1 && z <= nz - 2, ix = x >= 1 && x <= nx - 2;
     if (iy && iz)
-        a.txx[I3(x, y - 1, z - 1, nx, ny - 2)] =
-            s3_tnn(m, a.Vx[I3(x + 1, y, z, nx + 1, ny)], a.Vx[I3(x, y, z, nx + 1, ny)], p.dx, d);
+        a.txx[I3T(x, y - 1, z - 1, nx, ny - 2)] =
+            s3_tnn(m, a.Vx[I3T(x + 1, y, z, nx + 1, ny)], a.Vx[I3T(x, y, z, nx + 1, ny)], p.dx, d);
     if (ix && iz)
-        a.tyy[I3(x - 1, y, z - 1, nx - 2, ny)] =
-            s3_tnn(m, a.Vy[I3(x, y + 1, z, nx, ny + 1)], a.Vy[I3(x, y, z, nx, ny + 1)], p.dy, d);
+        a.tyy[I3T(x - 1, y, z - 1, nx - 2, ny)] =
+            s3_tnn(m, a.Vy[I3T(x, y + 1, z, nx, ny + 1)], a.Vy[I3T(x, y, z, nx, ny + 1)], p.dy, d);
     if (ix && iy)
-        a.tzz[I3(x - 1, y - 1, z, nx - 2, ny - 2)] =
-            s3_tnn(m, a.Vz[I3(x, y, z + 1, nx, ny)], a.Vz[I3(x, y, z, nx, ny)], p.dz, d);
-    if (x < nx - 1 && y < ny - 1 && z < nz - 2) s3_txy(a, p, x, y, z);
-    if (x < nx - 1 && y < ny - 2 && z < nz - 1) s3_txz(a, p, x, y, z);
-    if (x < nx - 2 && y < ny - 1 && z < nz - 1) s3_tyz(a, p, x, y, z);
+        a.tzz[I3T(x - 1, y - 1, z, nx - 2, ny - 2)] =
+            s3_tnn(m, a.Vz[I3T(x, y, z + 1, nx, ny)], a.Vz[I3T(x, y, z, nx, ny)], p.dz, d);
+    if (x < nx - 1 && y < ny - 1 && z < nz - 2) s3_txy<T, I>(a, p, x, y, z);
+    if (x < nx - 1 && y < ny - 2 && z < nz - 1) s3_txz<T, I>(a, p, x, y, z);
+    if (x < nx - 2 && y < ny - 1 && z < nz - 1) s3_tyz<T, I>(a, p, x, y, z);
 }
 
-template <typename T, int MODE = S3_PLAIN>
+template <typename T, int MODE = S3_PLAIN, typename I = int64_t>
 __global__ void s3_dVV_k(S3A<T> a, S3P<T> p) {
-    S3_IDX;
-    s3_dV<T, MODE>(a, p, x, y, z, true);
+    S3_IDXT;
+    s3_dV<T, MODE, I>(a, p, x, y, z, true);
 }
 
 // The loop body's six copies (bc_x!(Vy), bc_x!(Vz), bc_y!(Vx), bc_y!(Vz), bc_z!(Vx), bc_z!(Vy)):
@@ -670,6 +677,23 @@ static dim3 g3(int64_t wx, int64_t wy, int64_t wz) {
 
 enum S3Kernel { S3_TIMESTEPS, S3_P, S3_TAU, S3_DV, S3_V, S3_PTAU, S3_DVV, S3_BC };
 
+// The iteration kernels in 32-bit index arithmetic where every array index fits (the largest array,
+// a staggered velocity, has fewer than (nx+1)(ny+1)(nz+1) < 2^31 elements), else 64-bit.
+template <typename T>
+static bool s3_idx32(const S3A<T>& a) {
+    return (a.nx + 1) * (a.ny + 1) * (a.nz + 1) < (int64_t(1) << 31);
+}
+template <typename T, int MODE>
+static void s3_iteration_kernels(const S3A<T>& a, const S3P<T>& p, dim3 gc, dim3 b, cudaStream_t s) {
+    if (s3_idx32(a)) {
+        s3_Ptau_k<T, MODE, int><<<gc, b, 0, s>>>(a, p);
+        s3_dVV_k<T, MODE, int><<<gc, b, 0, s>>>(a, p);
+    } else {
+        s3_Ptau_k<T, MODE, int64_t><<<gc, b, 0, s>>>(a, p);
+        s3_dVV_k<T, MODE, int64_t><<<gc, b, 0, s>>>(a, p);
+    }
+}
+
 template <typename T>
 static void s3_launch(S3Kernel k, const S3A<T>& a, const S3P<T>& p, cudaStream_t s) {
     const dim3 b(32, 8, 1);
@@ -683,8 +707,14 @@ static void s3_launch(S3Kernel k, const S3A<T>& a, const S3P<T>& p, cudaStream_t
     case S3_TAU: s3_tau_k<T><<<gc, b, 0, s>>>(a, p); break;
     case S3_DV: s3_dV_k<T><<<gc, b, 0, s>>>(a, p); break;
     case S3_V: s3_V_k<T><<<gc, b, 0, s>>>(a); break;
-    case S3_PTAU: s3_Ptau_k<T><<<gc, b, 0, s>>>(a, p); break;
-    case S3_DVV: s3_dVV_k<T><<<gc, b, 0, s>>>(a, p); break;
+    case S3_PTAU:
+        if (s3_idx32(a)) s3_Ptau_k<T, S3_PLAIN, int><<<gc, b, 0, s>>>(a, p);
+        else s3_Ptau_k<T, S3_PLAIN, int64_t><<<gc, b, 0, s>>>(a, p);
+        break;
+    case S3_DVV:
+        if (s3_idx32(a)) s3_dVV_k<T, S3_PLAIN, int><<<gc, b, 0, s>>>(a, p);
+        else s3_dVV_k<T, S3_PLAIN, int64_t><<<gc, b, 0, s>>>(a, p);
+        break;
     case S3_BC: {
         const int64_t face = std::max(std::max((a.nx + 1) * (a.ny + 1), (a.nx + 1) * (a.nz + 1)), (a.ny + 1) * (a.nz + 1));
         s3_bc_k<T><<<dim3((unsigned)std::min<int64_t>((face + 255) / 256, 1024), 12), 256, 0, s>>>(a);
@@ -715,8 +745,7 @@ static void s3_iterations(const S3A<T>& a, const S3Out<T>& B, const S3P<T>& p, i
     }
     const dim3 b3(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
     for (int64_t i = 2 * pairs; i < n; ++i) {
-        s3_Ptau_k<T, MODE><<<gc, b3, 0, s>>>(a, p);
-        s3_dVV_k<T, MODE><<<gc, b3, 0, s>>>(a, p);
+        s3_iteration_kernels<T, MODE>(a, p, gc, b3, s);
         s3_launch(S3_BC, a, p, s);
     }
 }
@@ -724,8 +753,7 @@ static void s3_iterations(const S3A<T>& a, const S3Out<T>& B, const S3P<T>& p, i
 // divV, the stresses and Rx, Ry, Rz of the FP64 state (the reference's statements, no update)
 static void s3_residual(const S3A<double>& a, const S3P<double>& p, cudaStream_t s) {
     const dim3 b(32, 8, 1), gc = g3(a.nx, a.ny, a.nz);
-    s3_Ptau_k<double, S3_RESIDUAL><<<gc, b, 0, s>>>(a, p);
-    s3_dVV_k<double, S3_RESIDUAL><<<gc, b, 0, s>>>(a, p);
+    s3_iteration_kernels<double, S3_RESIDUAL>(a, p, gc, b, s);
 }
 
 // Library scratch of the iterate entry point: grow-only, one per device and stream.
