@@ -45,6 +45,18 @@ def test_checker_reproduces_the_reference_ad_testset(jr):
     assert np.array_equal(jac[0][0], A + a * B * 100.65)  # the primal update happened
 
 
+def test_checker_forward_mode_on_the_reference_kernel(jr):
+    """Forward mode (Enzyme.Forward) of the same kernel: with both tangents at one, the written
+    element's tangent becomes 1 + a*100.65 and B's stays 1."""
+    N, a = 16, 6.5
+    rng = np.random.default_rng(4)
+    A, B = rng.random(N), rng.random(N)
+    jac = jr.jacobian(K.REF_F, [A, B, a], [0, 1])
+    sh = jr.forward_shadows(jac, {0: np.ones(N), 1: np.ones(N)})
+    assert np.array_equal(sh[0], np.full(N, 1.0 + a * 100.65))
+    assert np.array_equal(sh[1], np.ones(N))
+
+
 @pytest.mark.parametrize("name", sorted(K.KERNELS))
 def test_checker_primal_equals_plain_run_and_transpose_identity(jr, name):
     """On Duals the interpreter gives the plain run's values bit for bit, and its reverse and

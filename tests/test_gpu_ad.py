@@ -31,6 +31,21 @@ def test_reference_ad_testset(ps):
     assert np.array_equal(ps.to_host(B), B0)
 
 
+def test_reference_kernel_forward_mode(ps):
+    """The reference's AD kernel in forward mode (ad_mode=Enzyme.Forward): tangents of A and B at
+    one give the new A's tangent 1 + a*100.65; B's stays 1."""
+    N, a = 16, 6.5
+    rng = np.random.default_rng(2)
+    A0, B0 = rng.random(N), rng.random(N)
+    k = ps.parallel_kernel(K.REF_F, 1)
+    A, B = ps.from_host(A0), ps.from_host(B0)
+    Ad, Bd = ps.ones(N), ps.ones(N)
+    ps.parallel(k, A, B, a, grad=((A, Ad), (B, Bd)), ad_mode="forward")
+    assert np.array_equal(ps.to_host(Ad), np.full(N, 1.0 + a * 100.65))
+    assert np.array_equal(ps.to_host(Bd), np.ones(N))
+    assert np.array_equal(ps.to_host(A), A0 + a * B0 * 100.65)
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
 @pytest.mark.parametrize("mode", ["reverse", "forward"])
 @pytest.mark.parametrize("name", sorted(K.KERNELS))
