@@ -299,6 +299,25 @@ __device__ __forceinline__ T jl_min(T x, T y) {
     T r = signbit(diff) ? x : y;
     return (isnan(x) || isnan(y)) ? diff : r;
 }
+// The same for doubles without FP64 instructions (GB300 issues FP64 at 2 per clock per SM): the
+// bits of a double with the magnitude bits flipped for negative values order as the values do,
+// with -0.0 below 0.0, so for non-NaN operands the larger key is the result above, bit for bit
+// (equal keys are equal values); a NaN operand is returned itself, as Julia's max and min do (a
+// NaN either way: its payload is the operand's instead of the difference's).
+__device__ __forceinline__ long long jl_key(long long b) { return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL); }
+__device__ __forceinline__ bool jl_nan_bits(long long b) { return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL; }
+template <>
+__device__ __forceinline__ double jl_max<double>(double x, double y) {
+    const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+    const double r = jl_key(bx) >= jl_key(by) ? x : y;
+    return jl_nan_bits(bx) ? x : jl_nan_bits(by) ? y : r;
+}
+template <>
+__device__ __forceinline__ double jl_min<double>(double x, double y) {
+    const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+    const double r = jl_key(bx) < jl_key(by) ? x : y;
+    return jl_nan_bits(bx) ? x : jl_nan_bits(by) ? y : r;
+}
 
 // --- mbarrier / TMA inline PTX (sm_90+; used on sm_103a) ---------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {

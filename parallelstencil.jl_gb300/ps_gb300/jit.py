@@ -1227,8 +1227,26 @@ __device__ __forceinline__ void jl_sts(E* a, long long n0, long long n1, long lo
     const long long l = i + n0 * (j + n1 * k);
     if (a && jl_in(n0, n1, n2, i, j, k) && l < cap) a[l] = v; else atomicOr(err, 1); }}
 __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov.u32 %0, %%laneid;" : "=r"(l)); return l; }}
-__device__ __forceinline__ R jl_max(R x, R y) {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
-__device__ __forceinline__ R jl_min(R x, R y) {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
+template <typename T> struct jl_f64 {{ static constexpr bool v = false; }};
+template <> struct jl_f64<double> {{ static constexpr bool v = true; }};
+__device__ __forceinline__ long long jl_key(long long b) {{ return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL); }}
+__device__ __forceinline__ bool jl_nanb(long long b) {{ return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL; }}
+// Julia's max / min (NaN-propagating, -0.0 < 0.0); doubles compare as integer keys (the FP64 pipe is slow)
+// and a NaN operand is returned itself
+__device__ __forceinline__ R jl_max(R x, R y) {{
+    if constexpr (jl_f64<R>::v) {{
+        const long long bx = __double_as_longlong((double)x), by = __double_as_longlong((double)y);
+        const R r = jl_key(bx) >= jl_key(by) ? x : y;
+        return jl_nanb(bx) ? x : jl_nanb(by) ? y : r;
+    }} else {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
+}}
+__device__ __forceinline__ R jl_min(R x, R y) {{
+    if constexpr (jl_f64<R>::v) {{
+        const long long bx = __double_as_longlong((double)x), by = __double_as_longlong((double)y);
+        const R r = jl_key(bx) < jl_key(by) ? x : y;
+        return jl_nanb(bx) ? x : jl_nanb(by) ? y : r;
+    }} else {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
+}}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
 extern "C" __global__ void {bounds}ps_jit_entry({'const __grid_constant__ ps_jit_targs t_' if self.tma else 'const ps_jit_args g'}) {{
     extern __shared__ __align__({128 if self.tma else 16}) unsigned char ps_smem[];
