@@ -13,7 +13,18 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SIZES = [(32, 8, 8), (33, 7, 8), (31, 7, 9)]
+SIZES = [(32, 8, 8), (33, 7, 8), (31, 7, 9), (36, 7, 8)]  # (36, 7, 8): ragged, with 16-byte FP64 rows
+
+# FP64 kernels run the register sweep by default; "always" runs them staged by TMA where the rows
+# allow it ((32, 8, 8) and (36, 7, 8)), so the reference's memopt kernels check both schedules
+STAGED = {"tma": True}
+
+
+@pytest.fixture(autouse=True, params=[True, "always"], ids=["sweep", "tma"])
+def _schedule(request):
+    STAGED["tma"] = request.param
+    yield
+    STAGED["tma"] = True
 
 
 def cube(shape, scale=1.0):
@@ -23,7 +34,10 @@ def cube(shape, scale=1.0):
 
 def _run(ps, src, arrays, scalars=()):
     dev = [ps.from_host(np.asfortranarray(a)) for a in arrays]
-    ps.parallel(ps.parallel_kernel(src), *dev, *scalars, memopt=True)
+    k = ps.parallel_kernel(src)
+    k.tma = STAGED["tma"]
+    ps.parallel(k, *dev, *scalars, memopt=True)
+    k.tma = True
     return [ps.to_host(d) for d in dev]
 
 
