@@ -201,8 +201,8 @@ struct S2Fused {
     int64_t nx, ny;
 };
 
-template <typename T>
-__device__ __forceinline__ T ldg_or0(const T* a, int64_t i, int64_t j, int64_t n0, int64_t n1) {
+template <typename T, typename I>
+__device__ __forceinline__ T ldg_or0(const T* a, I i, I j, I n0, I n1) {
     return (i >= 0 && i < n0 && j >= 0 && j < n1) ? __ldg(a + i + n0 * j) : T(0);
 }
 
@@ -212,7 +212,8 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT>
+// I: index type (int where every array has fewer than 2^31 elements: fewer instructions per cell)
+template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT, typename I>
 __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p) {
     constexpr int TX = S2_TX, TY = S2_TY;
     constexpr int VW = TX + 2, VH = TY + 2;  // staged V / Mus window: [x0-1, x0+TX] x [y0-1, y0+TY]
@@ -221,33 +222,69 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
     __shared__ T sP[CH][CW], sTxx[CH][CW], sTyy[CH][CW], sTxy[CH][CW];
     __shared__ double sred[3][TX * TY / 32];
 
-    const int64_t nx = a.nx, ny = a.ny;
+    const I nx = (I)a.nx, ny = (I)a.ny;
     const int tid = threadIdx.y * TX + threadIdx.x;
-    const int64_t x0 = (int64_t)blockIdx.x * TX, y0 = (int64_t)blockIdx.y * TY;
+    const I x0 = (I)blockIdx.x * TX, y0 = (I)blockIdx.y * TY;
+    constexpr int NC = (CW * CH + TX * TY - 1) / (TX * TY);  // halo-window cells per thread
 
+    // Every global load of the thread is issued before the first barrier (the staged window, the
+    // cells' P / dtPt / defect source, the faces' dVdt / dt / sources), so one memory round trip
+    // covers the iteration instead of three dependent ones.
     for (int k = tid; k < VW * VH; k += TX * TY) {
         int u = k % VW, v = k / VW;
-        int64_t gi = x0 - 1 + u, gj = y0 - 1 + v;
+        I gi = x0 - 1 + u, gj = y0 - 1 + v;
         sVx[v][u] = ldg_or0(a.Vx_in, gi, gj, nx + 1, ny);
         sVy[v][u] = ldg_or0(a.Vy_in, gi, gj, nx, ny + 1);
         sMus[v][u] = ldg_or0(a.Mus, gi, gj, nx, ny);
+    }
+    T c_p[NC], c_dt[NC], c_f[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        const int k = tid + q * TX * TY;
+        const I gi = x0 - 1 + k % CW, gj = y0 - 1 + k / CW;
+        const bool in = k < CW * CH && gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+        c_p[q] = in ? __ldg(a.P_in + gi + nx * gj) : T(0);
+        c_dt[q] = (READ_DT && in) ? __ldg(a.dtPt + gi + nx * gj) : T(0);
+        c_f[q] = (DEFECT && in) ? __ldg(a.fp + gi + nx * gj) : T(0);
+    }
+    const int lx = threadIdx.x, ly = threadIdx.y;
+    const I fi = x0 + lx, fj = y0 + ly;
+    const bool xin = fi <= nx && fj < ny, xinner = fi >= 1 && fi <= nx - 1 && fj >= 1 && fj <= ny - 2;
+    const bool yin = fi < nx && fj <= ny, yinner = fi >= 1 && fi <= nx - 2 && fj >= 1 && fj <= ny - 1;
+    const I rxi = (fi - 1) + (nx - 1) * (fj - 1), ryi = (fi - 1) + (nx - 2) * (fj - 1);
+    T x_dv = T(0), x_dt = T(0), x_f = T(0), y_dv = T(0), y_dt = T(0), y_f = T(0);
+    if (xin && xinner) {
+        x_dv = a.dVxdt[rxi];
+        if constexpr (READ_DT) x_dt = __ldg(a.dtVx + rxi);
+        if constexpr (DEFECT) x_f = __ldg(a.fx + rxi);
+    }
+    if (yin && yinner) {
+        y_dv = a.dVydt[ryi];
+        if constexpr (READ_DT) y_dt = __ldg(a.dtVy + ryi);
+        if constexpr (DEFECT)
+            y_f = __ldg(a.fy + ryi);
+        else
+            y_f = (__ldg(a.Rog + fi + nx * (fj - 1)) + __ldg(a.Rog + fi + nx * fj)) * T(0.5);
     }
     __syncthreads();
 
     double acc_div = 0.0;
     // cells and corners of the halo window
-    for (int k = tid; k < CW * CH; k += TX * TY) {
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        const int k = tid + q * TX * TY;
+        if (k >= CW * CH) break;
         int u = k % CW, v = k / CW;  // window cell (u, v) = global cell (x0-1+u, y0-1+v)
-        int64_t gi = x0 - 1 + u, gj = y0 - 1 + v;
+        I gi = x0 - 1 + u, gj = y0 - 1 + v;
         if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) {
             T vx0 = sVx[v][u], vx1 = sVx[v][u + 1];  // Vx faces gi, gi+1 of row gj
             T vy0 = sVy[v][u], vy1 = sVy[v + 1][u];  // Vy faces gj, gj+1 of column gi
             T mus = sMus[v][u];
             T d = s2_divV(vx0, vx1, vy0, vy1, p.dx, p.dy);
-            T dtp = READ_DT ? __ldg(a.dtPt + gi + nx * gj) : s2_dtPt(p.Ptsc, mus, p.max_nxy);
+            T dtp = READ_DT ? c_dt[q] : s2_dtPt(p.Ptsc, mus, p.max_nxy);
             T dp = d;
-            if constexpr (DEFECT) dp = d + __ldg(a.fp + gi + nx * gj);
-            T pn = __ldg(a.P_in + gi + nx * gj) - dtp * dp;
+            if constexpr (DEFECT) dp = d + c_f[q];
+            T pn = c_p[q] - dtp * dp;
             T txx = s2_tau_nn(mus, vx0, vx1, d, p.dx);
             T tyy = s2_tau_nn(mus, vy0, vy1, d, p.dy);
             sP[v][u] = pn;
@@ -276,23 +313,19 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
     __syncthreads();
 
     // faces of this tile
-    const int lx = threadIdx.x, ly = threadIdx.y;
-    const int64_t fi = x0 + lx, fj = y0 + ly;
     const int u = lx + 1, v = ly + 1;  // window coordinates of cell (fi, fj)
     double acc_rx = 0.0, acc_ry = 0.0;
     // ---- Vx face (fi, fj), Vx is (nx+1, ny) ----
-    if (fi <= nx && fj < ny) {
-        bool inner = fi >= 1 && fi <= nx - 1 && fj >= 1 && fj <= ny - 2;
+    if (xin) {
         T vnew = sVx[v][u];
-        if (inner) {
+        if (xinner) {
             T r = s2_Rx(sTxx[v][u - 1], sTxx[v][u], sTxy[v - 1][u - 1], sTxy[v][u - 1], sP[v][u - 1], sP[v][u], p.dx, p.dy);
-            if constexpr (DEFECT) r = r + __ldg(a.fx + (fi - 1) + (nx - 1) * (fj - 1));
-            int64_t ri = (fi - 1) + (nx - 1) * (fj - 1);
-            T dv = p.dampX * a.dVxdt[ri] + r;
-            a.dVxdt[ri] = dv;
-            if constexpr (STORE_TMP) a.Rx[ri] = r;
+            if constexpr (DEFECT) r = r + x_f;
+            T dv = p.dampX * x_dv + r;
+            a.dVxdt[rxi] = dv;
+            if constexpr (STORE_TMP) a.Rx[rxi] = r;
             if (a.red) acc_rx += fabs((double)r);
-            T dt = READ_DT ? __ldg(a.dtVx + ri) : s2_dtV(p.Vsc, p.min_dxy2, sMus[v][u - 1], sMus[v][u]);
+            T dt = READ_DT ? x_dt : s2_dtV(p.Vsc, p.min_dxy2, sMus[v][u - 1], sMus[v][u]);
             vnew = vnew + dt * dv;
         }
         // bc_y!(Vx): rows 0 and ny-1 copy rows 1 and ny-2 (written by the owner of the inner row)
@@ -302,22 +335,17 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
         if (ny <= 2 && (fj == 0 || fj == ny - 1)) a.Vx_out[fi + (nx + 1) * fj] = vnew;  // degenerate grid
     }
     // ---- Vy face (fi, fj), Vy is (nx, ny+1) ----
-    if (fi < nx && fj <= ny) {
-        bool inner = fi >= 1 && fi <= nx - 2 && fj >= 1 && fj <= ny - 1;
+    if (yin) {
         T vnew = sVy[v][u];
-        if (inner) {
+        if (yinner) {
             T r = s2_Ry_core(sTyy[v - 1][u], sTyy[v][u], sTxy[v - 1][u - 1], sTxy[v - 1][u], sP[v - 1][u], sP[v][u], p.dx,
                              p.dy);
-            if constexpr (DEFECT)
-                r = r + __ldg(a.fy + (fi - 1) + (nx - 2) * (fj - 1));
-            else
-                r = r + (__ldg(a.Rog + fi + nx * (fj - 1)) + __ldg(a.Rog + fi + nx * fj)) * T(0.5);
-            int64_t ri = (fi - 1) + (nx - 2) * (fj - 1);
-            T dv = p.dampY * a.dVydt[ri] + r;
-            a.dVydt[ri] = dv;
-            if constexpr (STORE_TMP) a.Ry[ri] = r;
+            r = r + y_f;  // the defect source, or the buoyancy average of the two cells
+            T dv = p.dampY * y_dv + r;
+            a.dVydt[ryi] = dv;
+            if constexpr (STORE_TMP) a.Ry[ryi] = r;
             if (a.red) acc_ry += fabs((double)r);
-            T dt = READ_DT ? __ldg(a.dtVy + ri) : s2_dtV(p.Vsc, p.min_dxy2, sMus[v - 1][u], sMus[v][u]);
+            T dt = READ_DT ? y_dt : s2_dtV(p.Vsc, p.min_dxy2, sMus[v - 1][u], sMus[v][u]);
             vnew = vnew + dt * dv;
         }
         // bc_x!(Vy): columns 0 and nx-1 copy columns 1 and nx-2
@@ -488,7 +516,11 @@ template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT>
 static void launch_fused(const S2Fused<T>& a, const S2P<T>& p, cudaStream_t s) {
     dim3 blk(S2_TX, S2_TY);
     dim3 grd((unsigned)((a.nx + 1 + S2_TX - 1) / S2_TX), (unsigned)((a.ny + 1 + S2_TY - 1) / S2_TY));
-    s2_fused<T, DEFECT, STORE_TMP, READ_DT><<<grd, blk, 0, s>>>(a, p);
+    // 32-bit indices while the largest array and the tile origins stay below 2^31
+    if ((a.nx + 1 + S2_TX) * (a.ny + 1 + S2_TY) < ((int64_t)1 << 31))
+        s2_fused<T, DEFECT, STORE_TMP, READ_DT, int><<<grd, blk, 0, s>>>(a, p);
+    else
+        s2_fused<T, DEFECT, STORE_TMP, READ_DT, int64_t><<<grd, blk, 0, s>>>(a, p);
 }
 
 template <typename T>
