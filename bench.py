@@ -1210,13 +1210,14 @@ def only_run(a):
         torch.cuda.synchronize()
         print(json.dumps({"only_run": a.only_run, "n": n, "steps": a.steps}))
         return
-    if a.only_run in ("stokes2d", "stokes3d", "stokes3d_fused32", "acoustic3d", "memcopy", "adjoint", "acoustic3d_fused",
-                      "acoustic3d_fused32", "acoustic3d_fused_split"):  # --steps calls, size --n
+    if a.only_run in ("stokes2d", "stokes2d32", "stokes3d", "stokes3d_fused32", "acoustic3d", "memcopy", "adjoint",
+                      "acoustic3d_fused", "acoustic3d_fused32", "acoustic3d_fused_split"):  # --steps calls, size --n
         from ps_gb300 import adjoint, stokes, stokes3d
 
-        if a.only_run == "stokes2d":  # fused PT iteration, FP64, n^2
-            Mus, Rog = stokes.inclusion_setup(n, n, 1.0, 1.0, musi=0.1, radius=0.1)
-            g = stokes.Stokes2D(stokes.Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog)
+        if a.only_run in ("stokes2d", "stokes2d32"):  # fused PT iterations, FP64 / FP32, n^2
+            dtp = np.float32 if a.only_run.endswith("32") else np.float64
+            Mus, Rog = stokes.inclusion_setup(n, n, 1.0, 1.0, musi=0.1, radius=0.1, dtype=dtp)
+            g = stokes.Stokes2D(stokes.Stokes2DParams(n, n, 1.0, 1.0), Mus, Rog, dtype=dtp)
             g.compute_timesteps()
             g.iterate(a.steps)
         elif a.only_run in ("stokes3d", "stokes3d_fused32"):  # PT iterations, FP64 three launches / FP32 one
@@ -1332,7 +1333,8 @@ def main():
     ap.add_argument("--loopsize", type=int, default=0, help="z indices per thread of memopt run-time compiled kernels")
     ap.add_argument("--warm-seeds", type=int, default=2, help="unseen setups of the warm-start comparison")
     ap.add_argument("--only-run", choices=["ieee", "split", "split_state", "split_grid", "gemm", "jit", "jit32",
-                                                 "stokes2d", "stokes3d", "acoustic3d", "memcopy", "adjoint", "fd", "fd32",
+                                                 "stokes2d", "stokes2d32", "stokes3d", "acoustic3d", "memcopy", "adjoint",
+                                                 "fd", "fd32",
                                                  "stokes2d_apt", "stokes2d_apt32", "adjoint_grid", "acoustic3d_fused",
                                                  "acoustic3d_fused32", "acoustic3d_fused_split", "hide", "miniapps", "stokes3d_fused32",
                                                  "ad", "ad32"],
