@@ -1229,24 +1229,35 @@ __device__ __forceinline__ void jl_sts(E* a, long long n0, long long n1, long lo
 __device__ __forceinline__ unsigned jl_laneid() {{ unsigned l; asm volatile("mov.u32 %0, %%laneid;" : "=r"(l)); return l; }}
 template <typename T> struct jl_f64 {{ static constexpr bool v = false; }};
 template <> struct jl_f64<double> {{ static constexpr bool v = true; }};
+template <typename T> struct jl_f32 {{ static constexpr bool v = false; }};
+template <> struct jl_f32<float> {{ static constexpr bool v = true; }};
 __device__ __forceinline__ long long jl_key(long long b) {{ return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL); }}
 __device__ __forceinline__ bool jl_nanb(long long b) {{ return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL; }}
 // Julia's max / min (NaN-propagating, -0.0 < 0.0); doubles compare as integer keys (the FP64 pipe is slow)
-// and a NaN operand is returned itself
-__device__ __forceinline__ R jl_max(R x, R y) {{
-    if constexpr (jl_f64<R>::v) {{
-        const long long bx = __double_as_longlong((double)x), by = __double_as_longlong((double)y);
-        const R r = jl_key(bx) >= jl_key(by) ? x : y;
+// and a NaN operand is returned itself; floats use max.NaN / min.NaN (the same bits as the subtraction
+// form, whose NaN is the canonical one)
+template <typename T>
+__device__ __forceinline__ T jl_maxt(T x, T y) {{
+    if constexpr (jl_f64<T>::v) {{
+        const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+        const T r = jl_key(bx) >= jl_key(by) ? x : y;
         return jl_nanb(bx) ? x : jl_nanb(by) ? y : r;
-    }} else {{ R d = x - y; R r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
+    }} else if constexpr (jl_f32<T>::v) {{
+        float d; asm("max.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(x), "f"(y)); return d;
+    }} else {{ T d = x - y; T r = signbit(d) ? y : x; return (isnan(x) || isnan(y)) ? d : r; }}
 }}
-__device__ __forceinline__ R jl_min(R x, R y) {{
-    if constexpr (jl_f64<R>::v) {{
-        const long long bx = __double_as_longlong((double)x), by = __double_as_longlong((double)y);
-        const R r = jl_key(bx) < jl_key(by) ? x : y;
+template <typename T>
+__device__ __forceinline__ T jl_mint(T x, T y) {{
+    if constexpr (jl_f64<T>::v) {{
+        const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+        const T r = jl_key(bx) < jl_key(by) ? x : y;
         return jl_nanb(bx) ? x : jl_nanb(by) ? y : r;
-    }} else {{ R d = x - y; R r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
+    }} else if constexpr (jl_f32<T>::v) {{
+        float d; asm("min.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(x), "f"(y)); return d;
+    }} else {{ T d = x - y; T r = signbit(d) ? x : y; return (isnan(x) || isnan(y)) ? d : r; }}
 }}
+__device__ __forceinline__ R jl_max(R x, R y) {{ return jl_maxt<R>(x, y); }}
+__device__ __forceinline__ R jl_min(R x, R y) {{ return jl_mint<R>(x, y); }}
 __device__ __forceinline__ R jl_bmul(bool b, R x) {{ return b ? x : copysign((R)0, x); }}
 extern "C" __global__ void {bounds}ps_jit_entry({'const __grid_constant__ ps_jit_targs t_' if self.tma else 'const ps_jit_args g'}) {{
     extern __shared__ __align__({128 if self.tma else 16}) unsigned char ps_smem[];
