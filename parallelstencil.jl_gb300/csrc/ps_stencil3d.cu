@@ -57,7 +57,8 @@ __host__ __device__ constexpr int fd_popc(int opd) { return (opd & 1) + ((opd >>
 
 // The macro's value from an accessor at(ox, oy, oz) of A relative to the point (offsets are
 // compile-time constants once the loops unroll).
-template <typename T, int KIND, int OPD, class F>
+// RCP_DONE: at() already gives the reciprocals of a harmonic mean's corners.
+template <typename T, int KIND, int OPD, bool RCP_DONE = false, class F>
 __device__ __forceinline__ T fd_eval_f(F at) {
     if constexpr (KIND == PS_FD_SEL) {
         return at(0, 0, 0);
@@ -77,7 +78,7 @@ __device__ __forceinline__ T fd_eval_f(F at) {
 #pragma unroll
             for (int j = 0; j < ND; j++) o[fd_dim(OPD, j)] = (cc >> j) & 1;
             T v = at(o[0], o[1], o[2]);
-            if constexpr (KIND == PS_FD_HARM) v = T(1.0) / v;
+            if constexpr (KIND == PS_FD_HARM && !RCP_DONE) v = T(1.0) / v;
             s = cc == 0 ? v : s + v;
         }
         if constexpr (KIND == PS_FD_AV) return s * T(1.0 / NC);  // 0.5, 0.25, 0.125: exact literals
@@ -151,14 +152,34 @@ __global__ void fd_apply_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
 // Selections and differences (a few loads, little arithmetic) unroll the sweep 4 times to keep
 // more loads in flight; averages and extrema keep the compiler's own unrolling (each measured
 // fastest at 512^3 that way, against forced unrolling by 1, 2 and 4).
+// Harmonic means keep reciprocals in the window: each plane's corners are inverted once when
+// loaded and reused by the next z step. In FP64 (division bound), with x among the operated
+// dimensions, a warp outputs FD_HX = 31 columns, lane 31 only loading, and takes the x + 1
+// corners' reciprocals from the next lane (9 divisions per point -> 3 for @harm, 5 -> 3 for
+// @harm_xya; same operations, same order: FP64 @harm_xya 315 -> 442 GB/s at 512^3). FP32 keeps
+// 32 columns per warp: its rows would straddle cache lines for no gain (2886 -> 2205 GB/s).
+constexpr int FD_HX = 31;
+template <typename T, int KIND, int OPD>
+__host__ __device__ constexpr bool fd_xshare() {
+    return KIND == PS_FD_HARM && (OPD & 1) && sizeof(T) == 8;
+}
+
 template <typename T, int KIND, int OPD>
 __global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDesc d, int64_t zl) {
     constexpr int ZLO = fd_zlo<KIND, OPD>(), ZN = fd_zhi<KIND, OPD>() - ZLO + 1;
     constexpr bool UNR4 = KIND == PS_FD_SEL || KIND == PS_FD_DIFF || KIND == PS_FD_DIFF2;
-    const int64_t tx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    constexpr bool HARM = KIND == PS_FD_HARM, XSH = fd_xshare<T, KIND, OPD>();
+    const int lane = (int)(threadIdx.x & 31);
+    const int64_t tx = XSH ? ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * FD_HX + lane
+                           : blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t ty = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
     const int64_t z0 = (int64_t)blockIdx.z * zl;
-    if (tx >= d.tmax[0] || ty >= d.tmax[1] || z0 >= d.tmax[2]) return;
+    // XSH: warps leave whole (ty is the warp's own, blockDim.x being a multiple of 32); a lane past
+    // the last column stays for the shuffles, loading column tmax[0] (the last point's x + 1 corner)
+    // at most, and writes nothing
+    if ((XSH ? tx - lane : tx) >= d.tmax[0] || ty >= d.tmax[1] || z0 >= d.tmax[2]) return;
+    const bool out = !XSH || (lane < FD_HX && tx < d.tmax[0]);
+    const bool ld = !XSH || tx <= d.tmax[0];
     const int64_t z1 = min(z0 + zl, d.tmax[2]);
     const int64_t s1 = d.nA[0], s2 = d.nA[0] * d.nA[1];
     const int64_t dz = (d.inn >> 2) & 1;
@@ -172,7 +193,18 @@ __global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
         for (int oy = -1; oy <= 1; oy++)
 #pragma unroll
             for (int ox = -1; ox <= 1; ox++)
-                if (fd_reads_xy<KIND, OPD>(ox, oy)) w[(oy + 1) * 3 + ox + 1] = __ldg(q + ox + s1 * oy);
+                if (fd_reads_xy<KIND, OPD>(ox, oy) && !(XSH && ox == 1))
+                    w[(oy + 1) * 3 + ox + 1] = ld ? __ldg(q + ox + s1 * oy) : T(1);
+        if constexpr (HARM) {  // after all the plane's loads, so that they are in flight together
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                if (fd_reads_xy<KIND, OPD>(k % 3 - 1, k / 3 - 1) && !(XSH && k % 3 == 2)) w[k] = T(1.0) / w[k];
+        }
+        if constexpr (XSH) {
+#pragma unroll
+            for (int oy = 0; oy <= 1; oy++)
+                if (fd_reads_xy<KIND, OPD>(1, oy)) w[(oy + 1) * 3 + 2] = __shfl_down_sync(0xffffffffu, w[(oy + 1) * 3 + 1], 1);
+        }
     };
 #pragma unroll
     for (int k = 1; k < ZN; k++) load_plane(W[k], z0 + ZLO + k - 1);
@@ -181,8 +213,9 @@ __global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
         _Pragma("unroll") for (int k = 0; k + 1 < ZN; k++)                                               \
             _Pragma("unroll") for (int q = 0; q < 9; q++) W[k][q] = W[k + 1][q];                         \
         load_plane(W[ZN - 1], z + ZLO + ZN - 1);                                                         \
-        r[rs * (z + rz0)] =                                                                              \
-            fd_eval_f<T, KIND, OPD>([&](int ox, int oy, int oz) { return W[oz - ZLO][(oy + 1) * 3 + ox + 1]; }); \
+        const T v_ = fd_eval_f<T, KIND, OPD, HARM>(                                                      \
+            [&](int ox, int oy, int oz) { return W[oz - ZLO][(oy + 1) * 3 + ox + 1]; });                 \
+        if (out) r[rs * (z + rz0)] = v_;                                                                 \
     }
     if constexpr (UNR4) {
 #pragma unroll 4
@@ -200,8 +233,13 @@ template <typename T, int K, int O>
 static void fd_launch_one(const FdDesc& d, T* R, const T* A, cudaStream_t s) {
     // a 2-D macro arrives here as a 3-D one over (nx, 1, ny): rows of 128 threads sweep "z" (= y)
     const dim3 blk = d.tmax[1] == 1 ? dim3(128, 1, 1) : dim3(32, 8, 1);
-    const unsigned gx = (unsigned)((d.tmax[0] + blk.x - 1) / blk.x), gy = (unsigned)((d.tmax[1] + blk.y - 1) / blk.y);
+    const unsigned gy = (unsigned)((d.tmax[1] + blk.y - 1) / blk.y);
+    unsigned gx = (unsigned)((d.tmax[0] + blk.x - 1) / blk.x);
     if (d.ndims == 3) {  // every 3-D macro sweeps z; 1-D and 2-D ones keep fd_apply_kernel
+        if (fd_xshare<T, K, O>()) {  // FD_HX output columns per warp
+            const int64_t cols = (int64_t)FD_HX * (blk.x / 32);
+            gx = (unsigned)((d.tmax[0] + cols - 1) / cols);
+        }
         int64_t zl = 64;
         while (zl > 2 && d.tmax[0] * d.tmax[1] * ((d.tmax[2] + zl - 1) / zl) < kResidentThreads) zl /= 2;
         zl = std::max<int64_t>(zl, (d.tmax[2] + 65534) / 65535);
