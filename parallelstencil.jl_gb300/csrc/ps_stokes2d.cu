@@ -212,8 +212,10 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// I: index type (int where every array has fewer than 2^31 elements: fewer instructions per cell)
-template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT, typename I>
+// I: index type (int where every array has fewer than 2^31 elements: fewer instructions per cell).
+// RED: a.red is set (the FP64 sums are compiled in only then: the conversions to double run on the
+// FP64 pipe even when predicated off).
+template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT, typename I, bool RED>
 __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p) {
     constexpr int TX = S2_TX, TY = S2_TY;
     constexpr int VW = TX + 2, VH = TY + 2;  // staged V / Mus window: [x0-1, x0+TX] x [y0-1, y0+TY]
@@ -298,7 +300,7 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
                     a.txx[gi + nx * gj] = txx;
                     a.tyy[gi + nx * gj] = tyy;
                 }
-                if (a.red) acc_div += fabs((double)dp);
+                if constexpr (RED) acc_div += fabs((double)dp);
             }
         }
         // corner (gi, gj): between cells gi..gi+1, gj..gj+1
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
             T dv = p.dampX * x_dv + r;
             a.dVxdt[rxi] = dv;
             if constexpr (STORE_TMP) a.Rx[rxi] = r;
-            if (a.red) acc_rx += fabs((double)r);
+            if constexpr (RED) acc_rx += fabs((double)r);
             T dt = READ_DT ? x_dt : s2_dtV(p.Vsc, p.min_dxy2, sMus[v][u - 1], sMus[v][u]);
             vnew = vnew + dt * dv;
         }
@@ -344,7 +346,7 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
             T dv = p.dampY * y_dv + r;
             a.dVydt[ryi] = dv;
             if constexpr (STORE_TMP) a.Ry[ryi] = r;
-            if (a.red) acc_ry += fabs((double)r);
+            if constexpr (RED) acc_ry += fabs((double)r);
             T dt = READ_DT ? y_dt : s2_dtV(p.Vsc, p.min_dxy2, sMus[v - 1][u], sMus[v][u]);
             vnew = vnew + dt * dv;
         }
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p)
         if (fi == nx - 2) a.Vy_out[(nx - 1) + nx * fj] = vnew;
         if (nx <= 2 && (fi == 0 || fi == nx - 1)) a.Vy_out[fi + nx * fj] = vnew;
     }
-    if (a.red) {
+    if constexpr (RED) {
         double s0 = warp_sum(acc_rx), s1 = warp_sum(acc_ry), s2 = warp_sum(acc_div);
         int w = tid >> 5;
         if ((tid & 31) == 0) {
@@ -517,10 +519,14 @@ static void launch_fused(const S2Fused<T>& a, const S2P<T>& p, cudaStream_t s) {
     dim3 blk(S2_TX, S2_TY);
     dim3 grd((unsigned)((a.nx + 1 + S2_TX - 1) / S2_TX), (unsigned)((a.ny + 1 + S2_TY - 1) / S2_TY));
     // 32-bit indices while the largest array and the tile origins stay below 2^31
-    if ((a.nx + 1 + S2_TX) * (a.ny + 1 + S2_TY) < ((int64_t)1 << 31))
-        s2_fused<T, DEFECT, STORE_TMP, READ_DT, int><<<grd, blk, 0, s>>>(a, p);
-    else
-        s2_fused<T, DEFECT, STORE_TMP, READ_DT, int64_t><<<grd, blk, 0, s>>>(a, p);
+    const bool i32 = (a.nx + 1 + S2_TX) * (a.ny + 1 + S2_TY) < ((int64_t)1 << 31);
+    if (a.red) {
+        if (i32) s2_fused<T, DEFECT, STORE_TMP, READ_DT, int, true><<<grd, blk, 0, s>>>(a, p);
+        else s2_fused<T, DEFECT, STORE_TMP, READ_DT, int64_t, true><<<grd, blk, 0, s>>>(a, p);
+    } else {
+        if (i32) s2_fused<T, DEFECT, STORE_TMP, READ_DT, int, false><<<grd, blk, 0, s>>>(a, p);
+        else s2_fused<T, DEFECT, STORE_TMP, READ_DT, int64_t, false><<<grd, blk, 0, s>>>(a, p);
+    }
 }
 
 template <typename T>
