@@ -166,20 +166,23 @@ __device__ __forceinline__ void apt_block_add(double v0, double* out0, double v1
     }
 }
 
+#define A2I(a, i, j, n0) (a)[(i) + (n0) * (j)]  // index arithmetic in the index type I
+
 // compute_P_τ!: cells (∇V, Pt, τxx, τyy) and corners (τxy). DEFECT: the correction's sweep
 // (pressure driven by ∇δV + ∇V of the outer state). STORE: write ∇V (and add Σ|∇V| to red).
-template <typename T, bool DEFECT, bool STORE>
+// I: index type (int where every array has fewer than 2^31 elements).
+template <typename T, bool DEFECT, bool STORE, typename I>
 __global__ void __launch_bounds__(256) apt_cells_k(AptArrays<T> a) {
     grid_dependency_wait();  // V of the previous iteration's faces kernel
     grid_dependents_may_launch();
-    const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
-    const int64_t nx = a.nx, ny = a.ny;
+    const I ix = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x, iy = (I)blockIdx.y * (I)blockDim.y + (I)threadIdx.y;
+    const I nx = (I)a.nx, ny = (I)a.ny;
     const T third = (T)(1.0 / 3.0), h = (T)0.5;
     double sabs = 0.0;
     if (ix < nx && iy < ny) {
-        const int64_t c = ix + nx * iy;
-        const T dvx = A2(a.Vx, ix + 1, iy, nx + 1) - A2(a.Vx, ix, iy, nx + 1);
-        const T dvy = A2(a.Vy, ix, iy + 1, nx) - A2(a.Vy, ix, iy, nx);
+        const I c = ix + nx * iy;
+        const T dvx = A2I(a.Vx, ix + 1, iy, nx + 1) - A2I(a.Vx, ix, iy, nx + 1);
+        const T dvy = A2I(a.Vy, ix, iy + 1, nx) - A2I(a.Vy, ix, iy, nx);
         const T d = dvx * a._dx + dvy * a._dy;
         const T td = d * third;
         T dp = d;
@@ -192,9 +195,9 @@ __global__ void __launch_bounds__(256) apt_cells_k(AptArrays<T> a) {
             sabs = fabs((double)dp);
         }
         if (ix < nx - 1 && iy < ny - 1) {
-            const int64_t k = ix + (nx - 1) * iy;
-            const T e = h * ((A2(a.Vx, ix + 1, iy + 1, nx + 1) - A2(a.Vx, ix + 1, iy, nx + 1)) * a._dy +
-                             (A2(a.Vy, ix + 1, iy + 1, nx) - A2(a.Vy, ix, iy + 1, nx)) * a._dx);
+            const I k = ix + (nx - 1) * iy;
+            const T e = h * ((A2I(a.Vx, ix + 1, iy + 1, nx + 1) - A2I(a.Vx, ix + 1, iy, nx + 1)) * a._dy +
+                             (A2I(a.Vy, ix + 1, iy + 1, nx) - A2I(a.Vy, ix, iy + 1, nx)) * a._dx);
             a.txy[k] = a.aTc[k] * a.txy[k] + a.bTc[k] * e;
         }
     }
@@ -206,61 +209,61 @@ __global__ void __launch_bounds__(256) apt_cells_k(AptArrays<T> a) {
 // compute_R_V! and the free-slip copies: face residuals, V += dτV R (UPDATE) and bc_y!(Vx),
 // bc_x!(Vy). DEFECT adds the outer state's FP64 residual as source. STORE: write Rx, Ry (and add
 // Σ|Rx|, Σ|Ry| to red).
-template <typename T, bool DEFECT, bool STORE, bool UPDATE>
+template <typename T, bool DEFECT, bool STORE, bool UPDATE, typename I>
 __global__ void __launch_bounds__(256) apt_faces_k(AptArrays<T> a) {
     grid_dependency_wait();  // τ and Pt of the cells kernel
     grid_dependents_may_launch();
-    const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
-    const int64_t nx = a.nx, ny = a.ny;
+    const I ix = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x, iy = (I)blockIdx.y * (I)blockDim.y + (I)threadIdx.y;
+    const I nx = (I)a.nx, ny = (I)a.ny;
     const T h = (T)0.5;
     double sx = 0.0, sy = 0.0;
     if (ix < nx - 1 && iy < ny - 2) {
-        const int64_t k = ix + (nx - 1) * iy;
-        T R = ((A2(a.txx, ix + 1, iy + 1, nx) - A2(a.txx, ix, iy + 1, nx)) * a._dx +
-               (A2(a.txy, ix, iy + 1, nx - 1) - A2(a.txy, ix, iy, nx - 1)) * a._dy) -
-              (A2(a.Pt, ix + 1, iy + 1, nx) - A2(a.Pt, ix, iy + 1, nx)) * a._dx;
+        const I k = ix + (nx - 1) * iy;
+        T R = ((A2I(a.txx, ix + 1, iy + 1, nx) - A2I(a.txx, ix, iy + 1, nx)) * a._dx +
+               (A2I(a.txy, ix, iy + 1, nx - 1) - A2I(a.txy, ix, iy, nx - 1)) * a._dy) -
+              (A2I(a.Pt, ix + 1, iy + 1, nx) - A2I(a.Pt, ix, iy + 1, nx)) * a._dx;
         if constexpr (DEFECT) R = R + a.rx0[k];
         if constexpr (STORE) {
             a.Rx[k] = R;
             sx = fabs((double)R);
         }
         if constexpr (UPDATE) {
-            const T v = A2(a.Vx, ix + 1, iy + 1, nx + 1) + a.dtVx[k] * R;
-            A2(a.Vx, ix + 1, iy + 1, nx + 1) = v;
-            if (iy == 0) A2(a.Vx, ix + 1, 0, nx + 1) = v;
-            if (iy == ny - 3) A2(a.Vx, ix + 1, ny - 1, nx + 1) = v;
+            const T v = A2I(a.Vx, ix + 1, iy + 1, nx + 1) + a.dtVx[k] * R;
+            A2I(a.Vx, ix + 1, iy + 1, nx + 1) = v;
+            if (iy == 0) A2I(a.Vx, ix + 1, 0, nx + 1) = v;
+            if (iy == ny - 3) A2I(a.Vx, ix + 1, ny - 1, nx + 1) = v;
         }
     }
     if (ix < nx - 2 && iy < ny - 1) {
-        const int64_t k = ix + (nx - 2) * iy;
-        T R = (((A2(a.tyy, ix + 1, iy + 1, nx) - A2(a.tyy, ix + 1, iy, nx)) * a._dy +
-                (A2(a.txy, ix + 1, iy, nx - 1) - A2(a.txy, ix, iy, nx - 1)) * a._dx) -
-               (A2(a.Pt, ix + 1, iy + 1, nx) - A2(a.Pt, ix + 1, iy, nx)) * a._dy);
+        const I k = ix + (nx - 2) * iy;
+        T R = (((A2I(a.tyy, ix + 1, iy + 1, nx) - A2I(a.tyy, ix + 1, iy, nx)) * a._dy +
+                (A2I(a.txy, ix + 1, iy, nx - 1) - A2I(a.txy, ix, iy, nx - 1)) * a._dx) -
+               (A2I(a.Pt, ix + 1, iy + 1, nx) - A2I(a.Pt, ix + 1, iy, nx)) * a._dy);
         if constexpr (DEFECT)
             R = R + a.ry0[k];
         else
-            R = R + (A2(a.Rog, ix + 1, iy, nx) + A2(a.Rog, ix + 1, iy + 1, nx)) * h;
+            R = R + (A2I(a.Rog, ix + 1, iy, nx) + A2I(a.Rog, ix + 1, iy + 1, nx)) * h;
         if constexpr (STORE) {
             a.Ry[k] = R;
             sy = fabs((double)R);
         }
         if constexpr (UPDATE) {
-            const T v = A2(a.Vy, ix + 1, iy + 1, nx) + a.dtVy[k] * R;
-            A2(a.Vy, ix + 1, iy + 1, nx) = v;
-            if (ix == 0) A2(a.Vy, 0, iy + 1, nx) = v;
-            if (ix == nx - 3) A2(a.Vy, nx - 1, iy + 1, nx) = v;
+            const T v = A2I(a.Vy, ix + 1, iy + 1, nx) + a.dtVy[k] * R;
+            A2I(a.Vy, ix + 1, iy + 1, nx) = v;
+            if (ix == 0) A2I(a.Vy, 0, iy + 1, nx) = v;
+            if (ix == nx - 3) A2I(a.Vy, nx - 1, iy + 1, nx) = v;
         }
     }
     if constexpr (UPDATE) {
         if (ix == 0 && iy == 0) {  // the copies of the lines that are never updated
-            A2(a.Vx, 0, 0, nx + 1) = A2(a.Vx, 0, 1, nx + 1);
-            A2(a.Vx, 0, ny - 1, nx + 1) = A2(a.Vx, 0, ny - 2, nx + 1);
-            A2(a.Vx, nx, 0, nx + 1) = A2(a.Vx, nx, 1, nx + 1);
-            A2(a.Vx, nx, ny - 1, nx + 1) = A2(a.Vx, nx, ny - 2, nx + 1);
-            A2(a.Vy, 0, 0, nx) = A2(a.Vy, 1, 0, nx);
-            A2(a.Vy, nx - 1, 0, nx) = A2(a.Vy, nx - 2, 0, nx);
-            A2(a.Vy, 0, ny, nx) = A2(a.Vy, 1, ny, nx);
-            A2(a.Vy, nx - 1, ny, nx) = A2(a.Vy, nx - 2, ny, nx);
+            A2I(a.Vx, 0, 0, nx + 1) = A2I(a.Vx, 0, 1, nx + 1);
+            A2I(a.Vx, 0, ny - 1, nx + 1) = A2I(a.Vx, 0, ny - 2, nx + 1);
+            A2I(a.Vx, nx, 0, nx + 1) = A2I(a.Vx, nx, 1, nx + 1);
+            A2I(a.Vx, nx, ny - 1, nx + 1) = A2I(a.Vx, nx, ny - 2, nx + 1);
+            A2I(a.Vy, 0, 0, nx) = A2I(a.Vy, 1, 0, nx);
+            A2I(a.Vy, nx - 1, 0, nx) = A2I(a.Vy, nx - 2, 0, nx);
+            A2I(a.Vy, 0, ny, nx) = A2I(a.Vy, 1, ny, nx);
+            A2I(a.Vy, nx - 1, ny, nx) = A2I(a.Vy, nx - 2, ny, nx);
         }
     }
     if constexpr (STORE) {
@@ -269,7 +272,7 @@ __global__ void __launch_bounds__(256) apt_faces_k(AptArrays<T> a) {
 }
 
 // FP64 residual of the state: τ at its steady state 2μ(ε̇ - ∇V/3) into txx/tyy/txy (the given
-// arrays), ∇V into divV; then apt_faces_k<double, false, true, false> gives Rx, Ry.
+// arrays), ∇V into divV; then apt_faces_k<double, false, true, false, I> gives Rx, Ry.
 __global__ void __launch_bounds__(256) apt_res_cells_k(AptArrays<double> a, const double* __restrict__ Mus) {
     const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, iy = blockIdx.y * (int64_t)blockDim.y + threadIdx.y;
     const int64_t nx = a.nx, ny = a.ny;
@@ -382,23 +385,35 @@ static AptArrays<T> apt_arrays(const ps_stokes2d_apt_fields* f, const ps_stokes2
     return a;
 }
 
-template <typename T, bool DEFECT, bool STORE>
-static void apt_launch_iteration(const AptArrays<T>& a, cudaStream_t s, bool after_kernel = true) {
+static bool apt_i32(int64_t nx, int64_t ny) {  // 32-bit indices: every array and offset below 2^31
+    return (nx + 1 + 32) * (ny + 1 + 8) < ((int64_t)1 << 31);
+}
+
+template <typename T, bool DEFECT, bool STORE, typename I>
+static void apt_launch_iteration_i(const AptArrays<T>& a, cudaStream_t s, bool after_kernel) {
     const dim3 blk(32, 8);
     const dim3 grd = apt_grid(a.nx, a.ny, blk);
     // each kernel may start while the kernel before it ends (programmatic dependent launch; it waits
     // for that kernel's stores before reading); after_kernel = false: the stream's last operation
     // is not one of these kernels (a memset, a copy, the start of a captured graph)
     if (!after_kernel) {
-        apt_cells_k<T, DEFECT, STORE><<<grd, blk, 0, s>>>(a);
-    } else if (launch_dependent(apt_cells_k<T, DEFECT, STORE>, grd, blk, 0, s, a) != cudaSuccess) {
+        apt_cells_k<T, DEFECT, STORE, I><<<grd, blk, 0, s>>>(a);
+    } else if (launch_dependent(apt_cells_k<T, DEFECT, STORE, I>, grd, blk, 0, s, a) != cudaSuccess) {
         cudaGetLastError();
-        apt_cells_k<T, DEFECT, STORE><<<grd, blk, 0, s>>>(a);
+        apt_cells_k<T, DEFECT, STORE, I><<<grd, blk, 0, s>>>(a);
     }
-    if (launch_dependent(apt_faces_k<T, DEFECT, STORE, true>, grd, blk, 0, s, a) != cudaSuccess) {
+    if (launch_dependent(apt_faces_k<T, DEFECT, STORE, true, I>, grd, blk, 0, s, a) != cudaSuccess) {
         cudaGetLastError();
-        apt_faces_k<T, DEFECT, STORE, true><<<grd, blk, 0, s>>>(a);
+        apt_faces_k<T, DEFECT, STORE, true, I><<<grd, blk, 0, s>>>(a);
     }
+}
+
+template <typename T, bool DEFECT, bool STORE>
+static void apt_launch_iteration(const AptArrays<T>& a, cudaStream_t s, bool after_kernel = true) {
+    if (apt_i32(a.nx, a.ny))
+        apt_launch_iteration_i<T, DEFECT, STORE, int>(a, s, after_kernel);
+    else
+        apt_launch_iteration_i<T, DEFECT, STORE, int64_t>(a, s, after_kernel);
 }
 
 template <typename T>
@@ -423,7 +438,10 @@ static void apt_residual64(AptArrays<double> a, const double* Mus, double* const
     const dim3 grd = apt_grid(a.nx, a.ny, blk);
     cudaMemsetAsync(red, 0, 3 * sizeof(double), s);
     apt_res_cells_k<<<grd, blk, 0, s>>>(a, Mus);
-    apt_faces_k<double, false, true, false><<<grd, blk, 0, s>>>(a);
+    if (apt_i32(a.nx, a.ny))
+        apt_faces_k<double, false, true, false, int><<<grd, blk, 0, s>>>(a);
+    else
+        apt_faces_k<double, false, true, false, int64_t><<<grd, blk, 0, s>>>(a);
 }
 
 static double apt_err(const double h[3], int64_t nx, int64_t ny) {
