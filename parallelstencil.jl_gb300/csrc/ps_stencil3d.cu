@@ -169,6 +169,9 @@ __global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
     constexpr int ZLO = fd_zlo<KIND, OPD>(), ZN = fd_zhi<KIND, OPD>() - ZLO + 1;
     constexpr bool UNR4 = KIND == PS_FD_SEL || KIND == PS_FD_DIFF || KIND == PS_FD_DIFF2;
     constexpr bool HARM = KIND == PS_FD_HARM, XSH = fd_xshare<T, KIND, OPD>();
+    // @d2_zi: (A[z+1] - A[z]) - (A[z] - A[z-1]); the step's first difference is the next step's second
+    // one (same operands, same operation), so the sweep carries it: 2 subtractions per point, not 3
+    constexpr bool D2Z = KIND == PS_FD_DIFF2 && OPD == 4;
     const int lane = (int)(threadIdx.x & 31);
     const int64_t tx = XSH ? ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * FD_HX + lane
                            : blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -208,13 +211,22 @@ __global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
     };
 #pragma unroll
     for (int k = 1; k < ZN; k++) load_plane(W[k], z0 + ZLO + k - 1);
+    T d2_prev = T(0);  // D2Z: A[z] - A[z-1] of the coming step (planes z0 - 1 and z0 here)
+    if constexpr (D2Z) d2_prev = W[2][4] - W[1][4];
 #define PS_FD_SWEEP_STEP                                                                                 \
     {                                                                                                    \
         _Pragma("unroll") for (int k = 0; k + 1 < ZN; k++)                                               \
             _Pragma("unroll") for (int q = 0; q < 9; q++) W[k][q] = W[k + 1][q];                         \
         load_plane(W[ZN - 1], z + ZLO + ZN - 1);                                                         \
-        const T v_ = fd_eval_f<T, KIND, OPD, HARM>(                                                      \
-            [&](int ox, int oy, int oz) { return W[oz - ZLO][(oy + 1) * 3 + ox + 1]; });                 \
+        T v_;                                                                                            \
+        if constexpr (D2Z) {                                                                             \
+            const T f_ = W[2][4] - W[1][4];                                                              \
+            v_ = f_ - d2_prev;                                                                           \
+            d2_prev = f_;                                                                                \
+        } else {                                                                                         \
+            v_ = fd_eval_f<T, KIND, OPD, HARM>(                                                          \
+                [&](int ox, int oy, int oz) { return W[oz - ZLO][(oy + 1) * 3 + ox + 1]; });             \
+        }                                                                                                \
         if (out) r[rs * (z + rz0)] = v_;                                                                 \
     }
     if constexpr (UNR4) {
