@@ -407,6 +407,39 @@ __device__ __forceinline__ T diff_cell(const DiffParams<T>& p, T Tc, T Txm, T Tx
     }
 }
 
+// The flux forms with face fluxes carried: a cell's x-face flux qxm is its left neighbour's qxp and
+// its z-face flux qzm the qzp of the cell below -- the same operations on the same operands, so a
+// sweep passes them on instead of recomputing them (bit-identical; about a fifth fewer operations
+// per cell, which the FP64 pipe bounds). qx: in, qxm when xin; out, qxp. qz: in, qzm; out, qzp.
+template <typename T, int FORM>
+__device__ __forceinline__ T diff_cell_carry(const DiffParams<T>& p, T Tc, T Txm, T Txp, T Tym, T Typ, T Tzp, T ci,
+                                             T lc, T lxm, T lxp, T lym, T lyp, T lzp, bool xin, T& qx, T& qz) {
+    static_assert(FORM == PS_DIFF_FLUX || FORM == PS_DIFF_FLUX_LAM, "flux forms only");
+    const bool L = FORM == PS_DIFF_FLUX_LAM;
+    const T kxp = L ? (lc + lxp) * T(0.5) : p.lam, kyp = L ? (lc + lyp) * T(0.5) : p.lam;
+    const T kym = L ? (lym + lc) * T(0.5) : p.lam, kzp = L ? (lc + lzp) * T(0.5) : p.lam;
+    T qxm;
+    if (xin) {
+        qxm = qx;
+    } else {
+        const T kxm = L ? (lxm + lc) * T(0.5) : p.lam;
+        qxm = ((-kxm) * (Tc - Txm)) * p.hx;
+    }
+    const T qxp = ((-kxp) * (Txp - Tc)) * p.hx;
+    const T qyp = ((-kyp) * (Typ - Tc)) * p.hy, qym = ((-kym) * (Tc - Tym)) * p.hy;
+    const T qzp = ((-kzp) * (Tzp - Tc)) * p.hz, qzm = qz;
+    const T dTdt = ci * (((-(qxp - qxm)) * p.hx - (qyp - qym) * p.hy) - (qzp - qzm) * p.hz);
+    qx = qxp;
+    qz = qzp;
+    return Tc + p.dt * dTdt;
+}
+// qzm of the first cell of a sweep (the carried value's start)
+template <typename T, int FORM>
+__device__ __forceinline__ T diff_qzm(const DiffParams<T>& p, T Tc, T Tzm, T lc, T lzm) {
+    const T kzm = FORM == PS_DIFF_FLUX_LAM ? (lzm + lc) * T(0.5) : p.lam;
+    return ((-kzm) * (Tc - Tzm)) * p.hz;
+}
+
 // --- plain: one thread per cell, (32, 8, 1) threads like the reference's default --------
 template <typename T, int FORM>
 __global__ void __launch_bounds__(256) diff3d_plain(T* __restrict__ T2, const T* __restrict__ Tin,
@@ -506,6 +539,8 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
     bool full_vec = row_in && gx >= cb.lo[0] && gx + VEC <= cb.hi[0];
 
     T Tzm[VEC], Tc[VEC], Tzp[VEC], lzm[VEC], lc[VEC], lzp[VEC];
+    constexpr bool CARRY = FORM == PS_DIFF_FLUX || FORM == PS_DIFF_FLUX_LAM;
+    T qzc[VEC];  // CARRY: each cell's qzm, the qzp of the cell below
     bool timed_out = false;
     timed_out |= !mbar_wait_bounded(&bar[0], 0);
     timed_out |= !mbar_wait_bounded(&bar[1 % S], (1 / S) & 1);
@@ -529,6 +564,11 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
                 lzm[j] = lav[j];
                 lc[j] = lbv[j];
             }
+        }
+        if constexpr (CARRY) {
+#pragma unroll
+            for (int j = 0; j < VEC; j++) qzc[j] = diff_qzm<T, FORM>(p, Tc[j], Tzm[j], Z::HAS_LAM ? lc[j] : T(0),
+                                                                   Z::HAS_LAM ? lzm[j] : T(0));
         }
     }
 
@@ -573,14 +613,19 @@ __global__ void __launch_bounds__(32 * TY) diff3d_zsweep_tma(const __grid_consta
                 for (int j = 0; j < VEC; j++) lym_[j] = lyp_[j] = lzp[j] = lc[j] = lzm[j] = T(0);
             }
             T out[VEC];
+            T qxc = T(0);  // CARRY: the previous cell's qxp
 #pragma unroll
             for (int j = 0; j < VEC; j++) {
                 T txm = j == 0 ? xm : Tc[j - 1];
                 T txp = j == VEC - 1 ? xp : Tc[j + 1];
                 T lxm_j = j == 0 ? lxm : lc[j - 1];
                 T lxp_j = j == VEC - 1 ? lxp : lc[j + 1];
-                out[j] = diff_cell<T, FORM>(p, Tc[j], txm, txp, ymv[j], ypv[j], Tzm[j], Tzp[j], civ[j], lc[j], lxm_j,
-                                            lxp_j, lym_[j], lyp_[j], lzm[j], lzp[j]);
+                if constexpr (CARRY)
+                    out[j] = diff_cell_carry<T, FORM>(p, Tc[j], txm, txp, ymv[j], ypv[j], Tzp[j], civ[j], lc[j], lxm_j,
+                                                      lxp_j, lym_[j], lyp_[j], lzp[j], j > 0, qxc, qzc[j]);
+                else
+                    out[j] = diff_cell<T, FORM>(p, Tc[j], txm, txp, ymv[j], ypv[j], Tzm[j], Tzp[j], civ[j], lc[j],
+                                                lxm_j, lxp_j, lym_[j], lyp_[j], lzm[j], lzp[j]);
             }
             const int64_t gz = Z0 + k;
             T* dst = T2 + gx + nx * (gy + ny * gz);
