@@ -169,8 +169,9 @@ __global__ void fd_sweep_kernel(T* __restrict__ R, const T* __restrict__ A, FdDe
     constexpr int ZLO = fd_zlo<KIND, OPD>(), ZN = fd_zhi<KIND, OPD>() - ZLO + 1;
     constexpr bool UNR4 = KIND == PS_FD_SEL || KIND == PS_FD_DIFF || KIND == PS_FD_DIFF2;
     constexpr bool HARM = KIND == PS_FD_HARM, XSH = fd_xshare<T, KIND, OPD>();
-    // @d2_zi: (A[z+1] - A[z]) - (A[z] - A[z-1]); the step's first difference is the next step's second
-    // one (same operands, same operation), so the sweep carries it: 2 subtractions per point, not 3
+    // @d2_zi (and the 2-D @d2_yi, swept as z): (A[z+1] - A[z]) - (A[z] - A[z-1]); the step's first
+    // difference is the next step's second one (same operands, same operation), so the sweep carries
+    // it: 2 subtractions per point, not 3
     constexpr bool D2Z = KIND == PS_FD_DIFF2 && OPD == 4;
     const int lane = (int)(threadIdx.x & 31);
     const int64_t tx = XSH ? ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * FD_HX + lane
