@@ -167,7 +167,13 @@ __global__ void s2_bc_y_k(T* A, int64_t n0, int64_t n1) {
 // =======================================================================================
 // Fused PT iteration
 // =======================================================================================
-constexpr int S2_TX = 32, S2_TY = 8;
+constexpr int S2_TX = 32;
+// tile rows: FP64 16 (the halo it recomputes is FP64-pipe work: 0.366 -> 0.354 ms per 1023^2
+// iteration), FP32 8 (16 measured slower there)
+template <typename T>
+__host__ __device__ constexpr int s2_ty() {
+    return sizeof(T) == 8 ? 16 : 8;
+}
 
 template <typename T>
 struct S2Fused {
@@ -216,8 +222,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // RED: a.red is set (the FP64 sums are compiled in only then: the conversions to double run on the
 // FP64 pipe even when predicated off).
 template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT, typename I, bool RED>
-__global__ void __launch_bounds__(S2_TX* S2_TY) s2_fused(S2Fused<T> a, S2P<T> p) {
-    constexpr int TX = S2_TX, TY = S2_TY;
+__global__ void __launch_bounds__(S2_TX* s2_ty<T>()) s2_fused(S2Fused<T> a, S2P<T> p) {
+    constexpr int TX = S2_TX, TY = s2_ty<T>();
     constexpr int VW = TX + 2, VH = TY + 2;  // staged V / Mus window: [x0-1, x0+TX] x [y0-1, y0+TY]
     constexpr int CW = TX + 1, CH = TY + 1;  // computed cells / corners: [x0-1, x0+TX) x [y0-1, y0+TY)
     __shared__ T sVx[VH][VW], sVy[VH][VW], sMus[VH][VW];
@@ -516,10 +522,11 @@ static void scratch_free(void* p) {
 
 template <typename T, bool DEFECT, bool STORE_TMP, bool READ_DT>
 static void launch_fused(const S2Fused<T>& a, const S2P<T>& p, cudaStream_t s) {
-    dim3 blk(S2_TX, S2_TY);
-    dim3 grd((unsigned)((a.nx + 1 + S2_TX - 1) / S2_TX), (unsigned)((a.ny + 1 + S2_TY - 1) / S2_TY));
+    constexpr int TY = s2_ty<T>();
+    dim3 blk(S2_TX, TY);
+    dim3 grd((unsigned)((a.nx + 1 + S2_TX - 1) / S2_TX), (unsigned)((a.ny + 1 + TY - 1) / TY));
     // 32-bit indices while the largest array and the tile origins stay below 2^31
-    const bool i32 = (a.nx + 1 + S2_TX) * (a.ny + 1 + S2_TY) < ((int64_t)1 << 31);
+    const bool i32 = (a.nx + 1 + S2_TX) * (a.ny + 1 + TY) < ((int64_t)1 << 31);
     if (a.red) {
         if (i32) s2_fused<T, DEFECT, STORE_TMP, READ_DT, int, true><<<grd, blk, 0, s>>>(a, p);
         else s2_fused<T, DEFECT, STORE_TMP, READ_DT, int64_t, true><<<grd, blk, 0, s>>>(a, p);
